@@ -1,0 +1,195 @@
+/*
+ * parmoon_cd.h -- C-ABI of the GB300 convection-diffusion hot path
+ * (libparmoon_cd.so).  Plain C types only: pointers, sizes, int status codes.
+ *
+ * The library replaces, for scalar convection-diffusion, the following parts
+ * of ParMooN2022 (paths inside the ParMooN2022 source tree):
+ *   - Assemble2D / Assemble3D with a ConvDiff LocalAssembling object
+ *       include/AssembleRoutines/Assemble2D.h:22-34, Assemble3D.h:26-32
+ *       src/AssembleRoutines/LocalAssembling.C:211-249 (ConvDiff terms)
+ *   - BlockFEMatrix::apply / apply_scaled_add (identity on non-active rows)
+ *       src/Matrix/BlockFEMatrix.C:969-1095
+ *   - Solver<BlockFEMatrix,BlockVector>::update_matrix + solve with
+ *     iterative_solver_type fgmres and preconditioner jacobi | multigrid
+ *       src/Solver/Solver.C:423-501,601-696, Iteration_gmres.C:430-620,
+ *       src/Multigrid/Multigrid.C:106-410
+ *   - ConvectionDiffusion<d>::assemble / solve / output (errors)
+ *       include/System/ConvectionDiffusion.h:183-285
+ *
+ * Error convention: every entry point returns CDG_OK (0) or a negative
+ * status; cdg_last_error() gives the message of the calling thread's last
+ * failure (the reference throws std::runtime_error via ErrThrow,
+ * include/General/MooNMD_Io.h:226-232; a host shim maps status -> ErrThrow).
+ *
+ * Threading: handles are not thread-safe; one handle is driven by one host
+ * thread.  All device work of a context is ordered on the context's stream.
+ */
+#ifndef PARMOON_CD_H
+#define PARMOON_CD_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CDG_OK 0
+#define CDG_ERR_ARG (-1)          /* invalid argument                        */
+#define CDG_ERR_CUDA (-2)         /* CUDA runtime error                      */
+#define CDG_ERR_OOM (-3)          /* device allocation failed                */
+#define CDG_ERR_DIVERGED (-4)     /* IterativeMethod::converged divergence   */
+#define CDG_ERR_BREAKDOWN (-5)    /* FGMRES unhappy breakdown                */
+#define CDG_ERR_ZERO_DIAG (-6)    /* zero diagonal entry (Jacobi)            */
+#define CDG_ERR_PATTERN (-7)      /* local coupling missing in the pattern   */
+#define CDG_ERR_SINGULAR (-8)     /* singular coarse matrix                  */
+#define CDG_ERR_NO_DEVICE (-9)    /* no CUDA device                          */
+#define CDG_ERR_LIMIT (-10)       /* size beyond a documented maximum        */
+
+/* example ids: coefficient function + exact solution + boundary data of the
+ * problem (the reference's Example_CD2D/Example_CD3D callbacks) */
+#define CDG_EX_SINE_LAPLACE 0     /* include/Examples/CD_2D/SineLaplace.h    */
+#define CDG_EX_SINE 1             /* u = prod sin(freq pi x_i)               */
+#define CDG_EX_POLYEXP 2          /* u = xyz(1-x)(1-y)(1-z)exp(x)            */
+#define CDG_EX_CONST_F 3          /* f = 1, u = 0 on the boundary            */
+#define CDG_EX_POLY1 4            /* u = 1 + x + 2y (+3z)                    */
+
+/* local assembling + example: LocalAssembling<d>(db, ConvDiff, {}, coeffs,
+ * disctype) with the TDatabase globals the CD routines read */
+typedef struct {
+  int example;          /* CDG_EX_*                                           */
+  double eps;           /* diffusion coefficient                              */
+  double b[3];          /* convection field (constant)                        */
+  double c;             /* reaction                                           */
+  double freq;          /* CDG_EX_SINE frequency                              */
+  int supg;             /* space_discretization_type: 0 galerkin, 1 supg      */
+  int sdfem_type;       /* SDFEM_TYPE                                         */
+  double delta0, delta1;/* DELTA0, DELTA1                                     */
+  int cell_measure;     /* CELL_MEASURE                                       */
+  int problem_linear;   /* INTERNAL_PROBLEM_LINEAR (quadrature degree 2p)     */
+  int neumann_mask;     /* bit k: boundary component k is Neumann             */
+  int poly_degree;      /* INTERNAL_POLYNOMIAL_DEGREE (0: element order)      */
+} cdg_assembly_params;
+
+/* Solver ParameterDatabase keys (src/Solver/Solver.C:26-209,
+ * src/Multigrid/Multigrid.C:417-509) */
+typedef struct {
+  int preconditioner;          /* 0 no_preconditioner, 1 jacobi, 2 multigrid */
+  int max_n_iterations;
+  int min_n_iterations;
+  int gmres_restart;
+  double residual_tolerance;   /* absolute                                   */
+  double residual_reduction;
+  double divergence_factor;
+  int multigrid_n_levels;
+  int multigrid_cycle_type;    /* 0 V, 1 W, 2 F                              */
+  int multigrid_n_pre_smooth;
+  int multigrid_n_post_smooth;
+  double jacobi_damp;
+  double multigrid_correction_damp_factor;
+  int multigrid_smoother_coarse; /* 0 direct_solve, 1 jacobi                 */
+  double multigrid_coarse_residual;
+  int multigrid_coarse_max_n_iterations;
+  int precision;               /* 0: all FP64, 1: FP32 multigrid in FP64 FGMRES */
+} cdg_solver_params;
+
+typedef struct {
+  int iterations;
+  double residual;             /* final Givens residual estimate             */
+  double initial_residual;
+  double seconds;              /* wall time of the call                      */
+} cdg_solve_stats;
+
+typedef struct cdg_context cdg_context;     /* device + stream + scratch       */
+typedef struct cdg_hierarchy cdg_hierarchy; /* host mesh/space/pattern levels  */
+typedef struct cdg_problem cdg_problem;     /* ConvectionDiffusion<d>          */
+
+const char *cdg_last_error(void);
+int cdg_version(void);
+
+/* ---- context ------------------------------------------------------------ */
+int cdg_context_create(int device, cdg_context **out);
+int cdg_context_destroy(cdg_context *ctx);
+int cdg_context_synchronize(cdg_context *ctx);
+/* number of kernel launches the context issued since creation */
+long long cdg_context_launch_count(const cdg_context *ctx);
+
+/* ---- host setup layer (no GPU) ------------------------------------------ */
+/* TDomain(unit square/cube split into roots^dim cells) refined nref times,
+ * TFESpace of Q_order, TStructure per level and the grid transfers; level 0
+ * is the finest, level k has nref-k refinements (refine_and_get_hierarchy_
+ * of_collections, src/Geometry/Domain.C:2796-2906; FESpace2D.C:83-312;
+ * Structure.C:226-618; GridTransfer.C:29-410) */
+int cdg_hierarchy_create(int dim, int order, int roots, int nref, int n_levels,
+                         int neumann_mask, cdg_hierarchy **out);
+int cdg_hierarchy_destroy(cdg_hierarchy *h);
+/* info[0..5] = n_cells, n_local_dofs, n_dofs, n_active, nnz, verts_per_cell */
+int cdg_hierarchy_level_info(const cdg_hierarchy *h, int level, int *info);
+int cdg_hierarchy_get_mesh(const cdg_hierarchy *h, int level, double *verts);
+int cdg_hierarchy_get_dofs(const cdg_hierarchy *h, int level, int *global_numbers);
+int cdg_hierarchy_get_pattern(const cdg_hierarchy *h, int level, int *row_ptr,
+                              int *col);
+
+/* ---- problem: ConvectionDiffusion<d> (src/System/ConvectionDiffusion.C) -- */
+/* upload one hierarchy (all its levels) to the device */
+int cdg_problem_create(cdg_context *ctx, const cdg_hierarchy *h,
+                       cdg_problem **out);
+/* drop-in form: the caller's own mesh, DOF map and pattern for n_levels
+ * levels (finest first): cell_vertices[l] has n_cells[l]*2^dim*dim doubles in
+ * the cell's vertex order, global_numbers[l] n_cells[l]*(order+1)^dim ints,
+ * row_ptr[l]/col[l] the TStructure, parent[l] (l>=1) the coarse cell of each
+ * cell of level l-1 (NULL: cell/2^dim, regular refinement) */
+int cdg_problem_create_from_arrays(cdg_context *ctx, int dim, int order,
+                                   int n_levels, const int *n_cells,
+                                   const double *const *cell_vertices,
+                                   const int *const *global_numbers,
+                                   const int *n_dofs, const int *n_active,
+                                   const int *const *row_ptr,
+                                   const int *const *col,
+                                   const int *const *parent,
+                                   cdg_problem **out);
+int cdg_problem_destroy(cdg_problem *p);
+/* ConvectionDiffusion<d>::assemble: every level (Assemble2D/3D cell loop,
+ * LocalAssembling ConvDiff, CSR scatter, Dirichlet rows and data) */
+int cdg_problem_assemble(cdg_problem *p, const cdg_assembly_params *a);
+/* Solver::solve(A, rhs, sol) on the finest level from the current solution */
+int cdg_problem_solve(cdg_problem *p, const cdg_solver_params *s,
+                      cdg_solve_stats *stats);
+/* assemble + solve with host buffers in and out (the e2e call, the
+ * reference's cd.assemble(); cd.solve() with the solution vector as start
+ * iterate): solution_in is the start iterate, rhs_out and solution_out
+ * receive the finest rhs and solution; all host, n_dofs of level 0, each may
+ * be NULL */
+int cdg_problem_assemble_solve(cdg_problem *p, const cdg_assembly_params *a,
+                               const cdg_solver_params *s,
+                               const double *solution_in, double *rhs_out,
+                               double *solution_out, cdg_solve_stats *stats);
+/* ConvectionDiffusion<d>::output error norms against the example's exact
+ * solution: errors[0..4] = L2, H1-semi, SD, DG(volume), L_inf */
+int cdg_problem_errors(cdg_problem *p, const cdg_assembly_params *a,
+                       double *errors);
+
+/* ---- data access (host buffers) ----------------------------------------- */
+int cdg_problem_level_info(const cdg_problem *p, int level, int *info);
+int cdg_problem_get_matrix(cdg_problem *p, int level, double *values);
+int cdg_problem_get_rhs(cdg_problem *p, int level, double *rhs);
+int cdg_problem_get_solution(cdg_problem *p, double *sol);
+int cdg_problem_set_solution(cdg_problem *p, const double *sol);
+/* CSR slot of every local coupling: slots[cell*nloc*nloc + i*nloc + j] */
+int cdg_problem_get_slots(cdg_problem *p, int level, int *slots);
+
+/* ---- operator pieces (host buffers) ------------------------------------- */
+/* y = A x (BlockFEMatrix::apply) */
+int cdg_problem_apply(cdg_problem *p, int level, const double *x, double *y);
+/* GridTransfer::Prolongate (coarse level fine_level+1 -> fine_level) */
+int cdg_problem_prolongate(cdg_problem *p, int fine_level, const double *xc,
+                           double *xf);
+/* GridTransfer::DefectRestriction (fine_level -> fine_level+1) */
+int cdg_problem_restrict(cdg_problem *p, int fine_level, const double *df,
+                         double *rc);
+/* one preconditioner application z = M^-1 v (Iteration_multigrid::apply or
+ * Iteration_jacobi::apply) */
+int cdg_problem_precondition(cdg_problem *p, const cdg_solver_params *s,
+                             const double *v, double *z);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

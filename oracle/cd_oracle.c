@@ -1,0 +1,1703 @@
+/*
+ * cd_oracle.c -- CPU restatement of ParMooN's scalar convection-diffusion
+ * path.  TEST INFRASTRUCTURE ONLY (the checker for the CUDA path); see
+ * cd_oracle.h.  Plain C99, single thread, FP64 everywhere, per quadrature
+ * point exactly like the reference cell loop.
+ *
+ * Reference files restated (paths inside the ParMooN2022 tree):
+ *   mesh refinement   src/Refinement/RefQuadRegDesc.C:21-29,
+ *                     src/Refinement/RefHexaRegDesc.C:17-21,211-275,
+ *                     src/Geometry/It_Finest.C (depth-first cell order),
+ *                     src/Geometry/Tests.C:473-517 (UnitSquare root cell)
+ *   DOF numbering     src/FE/FESpace2D.C:58-312, src/FE/FESpace3D.C:186-,
+ *                     src/FE/FEMapper.C:385-610, src/FE/FESpace.C:1863-2099
+ *   sparsity pattern  src/Matrix/Structure.C:226-618 (full rows, sorted cols)
+ *   quadrature        src/QuadFormulas/QuadratureFormulaDatabase.C:22-151,
+ *                     src/FE/FEDatabase.C:1553-1556 (degree = N_terms*p)
+ *   basis             include/FE2D/BF_C_Q_Q1_2D.h, BF_C_Q_Q2_2D.h,
+ *                     include/FE3D/BF_C_H_Q1_3D.h, BF_C_H_Q2_3D.h
+ *   reference maps    src/FE/QuadAffin.C:175-, src/FE/HexaAffin.C:221-252
+ *   local forms       src/AssembleRoutines/ConvDiff.C:1776-1999 (Galerkin,
+ *                     SUPG), :269-495 (Compute_SDFEM_delta),
+ *                     src/AssembleRoutines/LocalAssembling.C:734-970
+ *   scatter           src/AssembleRoutines/Assemble3D.C:236-292,
+ *                     src/AssembleRoutines/Assemble2D.C:3024-3046,
+ *                     Dirichlet/Neumann data Assemble2D.C:3140-3260
+ *   cell measure      src/Geometry/BaseCell.C:102-131, Rectangle.C:12-33,
+ *                     Hexahedron.C:70-121
+ *   solver            src/Solver/Iteration_gmres.C:430-620,
+ *                     src/Solver/Utilities_gmres.C:60-108,
+ *                     include/Solver/IterativeMethod.h:83-163,
+ *                     src/Solver/Iteration_jacobi.C:14-39,168-182
+ *   multigrid         src/Multigrid/Multigrid.C:157-410, CycleControl.C:15-111,
+ *                     MultigridLevel.C:118-151, JacobiSmoother.C:21-29,
+ *                     GridTransfer.C:29-410
+ *   BlockFEMatrix     src/Matrix/BlockFEMatrix.C:969-1095 (identity on
+ *                     non-active rows)
+ *   error norms       src/FE/FEFunction2D.C:291-470,
+ *                     src/AssembleRoutines/ConvDiff.C:2124-2183
+ */
+#include "cd_oracle.h"
+
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define MAXLOC 27
+#define MAXQP 125
+#define MAXV 8
+
+static char g_err[256];
+const char *orc_last_error(void) { return g_err; }
+#define FAIL(...)                                                              \
+  do {                                                                         \
+    snprintf(g_err, sizeof g_err, __VA_ARGS__);                                \
+    return -1;                                                                 \
+  } while (0)
+
+/* ------------------------------------------------------------------------ */
+/* quadrature: Gauss-Legendre rules, tensorised                              */
+/* ------------------------------------------------------------------------ */
+static void gauss_legendre(int n, double *x, double *w) {
+  /* Newton iteration on P_n in long double, nodes in ascending order */
+  for (int i = 0; i < n; ++i) {
+    long double z = cosl(3.14159265358979323846264338327950288L *
+                         (i + 0.75L) / (n + 0.5L));
+    long double pp = 0;
+    for (int it = 0; it < 100; ++it) {
+      long double p1 = 1, p2 = 0;
+      for (int j = 1; j <= n; ++j) {
+        long double p3 = p2;
+        p2 = p1;
+        p1 = ((2 * j - 1) * z * p2 - (j - 1) * p3) / j;
+      }
+      pp = n * (z * p1 - p2) / (z * z - 1);
+      long double z1 = z;
+      z = z1 - p1 / pp;
+      if (fabsl(z - z1) < 1e-30L) break;
+    }
+    x[n - 1 - i] = (double)z;
+    w[n - 1 - i] = (double)(2 / ((1 - z * z) * pp * pp));
+  }
+}
+
+/* number of 1D Gauss points for a quad/hexa rule of the given accuracy
+ * (QuadratureFormulaDatabase.C:41-81: 0-2 -> Gauss2, 3-5 -> Gauss3,
+ * 6-7 -> Gauss4, 8-9 -> Gauss5, ...) */
+static int gauss_points_for_degree(int deg) {
+  if (deg > 17) deg = 17;
+  if (deg <= 2) return 2;
+  if (deg <= 5) return 3;
+  return deg / 2 + 1;
+}
+/* line rules (QuadratureFormulaDatabase.C:108-133) */
+static int line_points_for_degree(int deg) { return deg / 2 + 1; }
+
+typedef struct {
+  int nqp;
+  double xi[MAXQP][3];
+  double w[MAXQP];
+} quad_rule;
+
+static void make_rule(int dim, int n1, quad_rule *q) {
+  double x[10], w[10];
+  gauss_legendre(n1, x, w);
+  q->nqp = 0;
+  if (dim == 2) {
+    for (int j = 0; j < n1; ++j)
+      for (int i = 0; i < n1; ++i) {
+        q->xi[q->nqp][0] = x[i];
+        q->xi[q->nqp][1] = x[j];
+        q->xi[q->nqp][2] = 0;
+        q->w[q->nqp++] = w[i] * w[j];
+      }
+  } else {
+    for (int k = 0; k < n1; ++k)
+      for (int j = 0; j < n1; ++j)
+        for (int i = 0; i < n1; ++i) {
+          q->xi[q->nqp][0] = x[i];
+          q->xi[q->nqp][1] = x[j];
+          q->xi[q->nqp][2] = x[k];
+          q->w[q->nqp++] = w[i] * w[j] * w[k];
+        }
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Lagrange tensor basis Q1/Q2, derivatives up to order 2                    */
+/* ------------------------------------------------------------------------ */
+static void lag1d(int p, double t, double *v, double *d, double *dd) {
+  if (p == 1) {
+    v[0] = 0.5 * (1 - t); v[1] = 0.5 * (1 + t);
+    d[0] = -0.5; d[1] = 0.5;
+    dd[0] = 0; dd[1] = 0;
+  } else {
+    v[0] = 0.5 * t * (t - 1); v[1] = 1 - t * t; v[2] = 0.5 * t * (t + 1);
+    d[0] = t - 0.5; d[1] = -2 * t; d[2] = t + 0.5;
+    dd[0] = 1; dd[1] = -2; dd[2] = 1;
+  }
+}
+
+/* values: [0]=phi, [1..d]=grad, then hessian entries (xx,xy,yy) in 2D,
+ * (xx,xy,xz,yy,yz,zz) in 3D.  Local DOF k = k0 + (p+1)(k1 + (p+1)k2). */
+#define NDER 10
+static void ref_basis(int dim, int p, const double *xi, double out[][NDER]) {
+  double v[3][3], d[3][3], dd[3][3];
+  for (int a = 0; a < dim; ++a) lag1d(p, xi[a], v[a], d[a], dd[a]);
+  int n1 = p + 1;
+  if (dim == 2) {
+    for (int k1 = 0; k1 < n1; ++k1)
+      for (int k0 = 0; k0 < n1; ++k0) {
+        int k = k0 + n1 * k1;
+        out[k][0] = v[0][k0] * v[1][k1];
+        out[k][1] = d[0][k0] * v[1][k1];
+        out[k][2] = v[0][k0] * d[1][k1];
+        out[k][3] = dd[0][k0] * v[1][k1];
+        out[k][4] = d[0][k0] * d[1][k1];
+        out[k][5] = v[0][k0] * dd[1][k1];
+      }
+  } else {
+    for (int k2 = 0; k2 < n1; ++k2)
+      for (int k1 = 0; k1 < n1; ++k1)
+        for (int k0 = 0; k0 < n1; ++k0) {
+          int k = k0 + n1 * (k1 + n1 * k2);
+          double a = v[0][k0], b = v[1][k1], c = v[2][k2];
+          out[k][0] = a * b * c;
+          out[k][1] = d[0][k0] * b * c;
+          out[k][2] = a * d[1][k1] * c;
+          out[k][3] = a * b * d[2][k2];
+          out[k][4] = dd[0][k0] * b * c;
+          out[k][5] = d[0][k0] * d[1][k1] * c;
+          out[k][6] = d[0][k0] * b * d[2][k2];
+          out[k][7] = a * dd[1][k1] * c;
+          out[k][8] = a * d[1][k1] * d[2][k2];
+          out[k][9] = a * b * dd[2][k2];
+        }
+  }
+}
+
+static void local_dof_ref(int dim, int p, int k, double *r) {
+  int n1 = p + 1;
+  int i0 = k % n1, i1 = (k / n1) % n1, i2 = k / (n1 * n1);
+  double step = 2.0 / p;
+  r[0] = -1 + step * i0;
+  r[1] = -1 + step * i1;
+  r[2] = dim == 3 ? -1 + step * i2 : 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* mesh: unit square / cube root cell, regular refinement, depth-first order */
+/* ------------------------------------------------------------------------ */
+/* new-vertex definitions: each new vertex is the mean of a set of old ones */
+static const int QUAD_NEWV[9][4] = {{0}, {1}, {2}, {3}, {0, 1}, {1, 2},
+                                    {2, 3}, {3, 0}, {0, 1, 2, 3}};
+static const int QUAD_NEWV_N[9] = {1, 1, 1, 1, 2, 2, 2, 2, 4};
+static const int QUAD_CHILD[4][4] = {
+    {0, 4, 8, 7}, {1, 5, 8, 4}, {2, 6, 8, 5}, {3, 7, 8, 6}};
+
+static const int HEX_NEWV[27][8] = {
+    {0}, {1}, {2}, {3}, {4}, {5}, {6}, {7},
+    {0, 1},              /* 8  */
+    {1, 2},              /* 9  */
+    {2, 3},              /* 10 */
+    {3, 0},              /* 11 */
+    {0, 1, 2, 3},        /* 12 */
+    {1, 5},              /* 13 */
+    {4, 5},              /* 14 */
+    {0, 4},              /* 15 */
+    {0, 4, 5, 1},        /* 16 */
+    {2, 6},              /* 17 */
+    {5, 6},              /* 18 */
+    {1, 5, 6, 2},        /* 19 */
+    {3, 7},              /* 20 */
+    {6, 7},              /* 21 */
+    {2, 6, 7, 3},        /* 22 */
+    {7, 4},              /* 23 */
+    {0, 3, 7, 4},        /* 24 */
+    {4, 7, 6, 5},        /* 25 */
+    {0, 1, 2, 3, 4, 5, 6, 7}};
+static const int HEX_NEWV_N[27] = {1, 1, 1, 1, 1, 1, 1, 1, 2, 2, 2, 2, 4, 2,
+                                   2, 2, 4, 2, 2, 4, 2, 2, 4, 2, 4, 4, 8};
+static const int HEX_CHILD[8][8] = {
+    {0, 8, 12, 11, 15, 16, 26, 24}, {1, 9, 12, 8, 13, 19, 26, 16},
+    {2, 10, 12, 9, 17, 22, 26, 19}, {3, 11, 12, 10, 20, 24, 26, 22},
+    {4, 23, 25, 14, 15, 24, 26, 16}, {5, 14, 25, 18, 13, 16, 26, 19},
+    {6, 18, 25, 21, 17, 19, 26, 22}, {7, 21, 25, 23, 20, 22, 26, 24}};
+
+/* joints: 2D edges (j, j+1), 3D faces (Hexahedron shape descriptor) */
+static const int HEX_FACE[6][4] = {{0, 1, 2, 3}, {0, 4, 5, 1}, {1, 5, 6, 2},
+                                   {2, 6, 7, 3}, {0, 3, 7, 4}, {4, 7, 6, 5}};
+
+typedef struct {
+  int ncells, nloc, ndof, nactive, nnz, nv;
+  double *verts;    /* ncells*nv*dim */
+  int *gdof;        /* ncells*nloc */
+  int *row_ptr, *col;
+  double *val, *rhs, *sol, *diag;
+  /* multigrid work vectors */
+  double *mg_rhs, *mg_sol, *mg_def;
+  double *lu;       /* dense LU of the coarse matrix (coarsest level only) */
+  int *piv;
+} level_t;
+
+struct orc_problem {
+  orc_config cfg;
+  int nlev;
+  level_t *lev;
+  quad_rule qr;
+  int nqp1;
+};
+
+static int nverts(int dim) { return dim == 2 ? 4 : 8; }
+
+static double *refine_mesh(int dim, int nref, int *ncells_out) {
+  int nv = nverts(dim);
+  int nc = 1;
+  double *v = (double *)malloc(sizeof(double) * nv * dim);
+  if (dim == 2) {
+    const double sq[4][2] = {{0, 0}, {1, 0}, {1, 1}, {0, 1}};
+    memcpy(v, sq, sizeof sq);
+  } else {
+    const double cu[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
+                             {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+    memcpy(v, cu, sizeof cu);
+  }
+  for (int r = 0; r < nref; ++r) {
+    int nch = dim == 2 ? 4 : 8;
+    double *nvv = (double *)malloc(sizeof(double) * nc * nch * nv * dim);
+    for (int c = 0; c < nc; ++c) {
+      const double *pv = v + (size_t)c * nv * dim;
+      double newv[27][3];
+      int nnew = dim == 2 ? 9 : 27;
+      for (int k = 0; k < nnew; ++k) {
+        int n = dim == 2 ? QUAD_NEWV_N[k] : HEX_NEWV_N[k];
+        for (int a = 0; a < dim; ++a) {
+          double s = 0;
+          for (int m = 0; m < n; ++m)
+            s += pv[(dim == 2 ? QUAD_NEWV[k][m] : HEX_NEWV[k][m]) * dim + a];
+          newv[k][a] = s / n;
+        }
+      }
+      for (int ch = 0; ch < nch; ++ch) {
+        double *cv = nvv + ((size_t)c * nch + ch) * nv * dim;
+        for (int m = 0; m < nv; ++m) {
+          int id = dim == 2 ? QUAD_CHILD[ch][m] : HEX_CHILD[ch][m];
+          for (int a = 0; a < dim; ++a) cv[m * dim + a] = newv[id][a];
+        }
+      }
+    }
+    free(v);
+    v = nvv;
+    nc *= nch;
+  }
+  *ncells_out = nc;
+  return v;
+}
+
+/* affine reference map of a cell: x = x0 + J xi (QuadAffin / HexaAffin) */
+typedef struct {
+  double x0[3], J[3][3], Jinv[3][3], det;
+} affine_t;
+
+static void cell_affine(int dim, const double *cv, affine_t *A) {
+  /* xi along v0->v1, eta along v0->v3, zeta along v0->v4 */
+  const int e[3] = {1, 3, 4};
+  for (int r = 0; r < dim; ++r) {
+    for (int a = 0; a < dim; ++a)
+      A->J[r][a] = (cv[e[a] * dim + r] - cv[0 * dim + r]) * 0.5;
+  }
+  for (int r = 0; r < dim; ++r) {
+    double s = cv[r];
+    for (int a = 0; a < dim; ++a) s += A->J[r][a];
+    A->x0[r] = s;
+  }
+  if (dim == 2) {
+    double a = A->J[0][0], b = A->J[0][1], c = A->J[1][0], d = A->J[1][1];
+    A->det = a * d - b * c;
+    A->Jinv[0][0] = d / A->det; A->Jinv[0][1] = -b / A->det;
+    A->Jinv[1][0] = -c / A->det; A->Jinv[1][1] = a / A->det;
+  } else {
+    double(*J)[3] = A->J;
+    double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+                 J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                 J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+    A->det = det;
+    A->Jinv[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) / det;
+    A->Jinv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
+    A->Jinv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
+    A->Jinv[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) / det;
+    A->Jinv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
+    A->Jinv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
+    A->Jinv[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) / det;
+    A->Jinv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
+    A->Jinv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+  }
+}
+
+static void affine_map(int dim, const affine_t *A, const double *xi,
+                       double *x) {
+  for (int r = 0; r < dim; ++r) {
+    double s = A->x0[r];
+    for (int a = 0; a < dim; ++a) s += A->J[r][a] * xi[a];
+    x[r] = s;
+  }
+}
+
+/* cell measure hK (BaseCell.C:102-131) */
+static double cell_hK(int dim, const double *cv, int measure) {
+  if (dim == 2) {
+    if (measure == 2) {
+      double dx1 = cv[0] - cv[2], dy1 = cv[1] - cv[3];
+      double dx2 = cv[2] - cv[4], dy2 = cv[3] - cv[5];
+      double l1 = dx1 * dx1 + dy1 * dy1, l2 = dx2 * dx2 + dy2 * dy2;
+      return l1 < l2 ? sqrt(l1) : sqrt(l2);
+    }
+    if (measure == 1 || measure == 3) {
+      affine_t A;
+      cell_affine(2, cv, &A);
+      return sqrt(fabs(4 * A.det));
+    }
+    double dx = cv[0] - cv[4], dy = cv[1] - cv[5];
+    return sqrt(dx * dx + dy * dy);
+  }
+  if (measure == 2) {
+    const int pr[3][2] = {{0, 4}, {0, 1}, {0, 3}};
+    double m = 1e10;
+    for (int k = 0; k < 3; ++k) {
+      double s = 0;
+      for (int a = 0; a < 3; ++a) {
+        double dd = cv[pr[k][0] * 3 + a] - cv[pr[k][1] * 3 + a];
+        s += dd * dd;
+      }
+      if (s < m) m = s;
+    }
+    return sqrt(m);
+  }
+  if (measure == 1 || measure == 3) {
+    affine_t A;
+    cell_affine(3, cv, &A);
+    return sqrt(fabs(8 * A.det));
+  }
+  const int pr[4][2] = {{0, 6}, {1, 7}, {2, 4}, {3, 5}};
+  double m = 0;
+  for (int k = 0; k < 4; ++k) {
+    double s = 0;
+    for (int a = 0; a < 3; ++a) {
+      double dd = cv[pr[k][0] * 3 + a] - cv[pr[k][1] * 3 + a];
+      s += dd * dd;
+    }
+    if (s > m) m = s;
+  }
+  return sqrt(m);
+}
+
+/* ------------------------------------------------------------------------ */
+/* examples: coefficients, exact solution, boundary data                      */
+/* ------------------------------------------------------------------------ */
+/* exact solution: u[0]=value, u[1..dim]=gradient, u[dim+1]=laplacian */
+static void exact_sol(const orc_config *c, const double *x, double *u) {
+  int d = c->dim;
+  for (int k = 0; k < 5; ++k) u[k] = 0;
+  switch (c->example) {
+  case ORC_EX_SINE_LAPLACE:
+  case ORC_EX_SINE: {
+    double k = c->example == ORC_EX_SINE_LAPLACE ? M_PI : c->freq * M_PI;
+    double s[3], co[3];
+    for (int a = 0; a < d; ++a) {
+      s[a] = sin(k * x[a]);
+      co[a] = cos(k * x[a]);
+    }
+    if (d == 2) {
+      u[0] = s[0] * s[1];
+      u[1] = k * co[0] * s[1];
+      u[2] = k * s[0] * co[1];
+      u[3] = -2 * k * k * s[0] * s[1];
+    } else {
+      u[0] = s[0] * s[1] * s[2];
+      u[1] = k * co[0] * s[1] * s[2];
+      u[2] = k * s[0] * co[1] * s[2];
+      u[3] = k * s[0] * s[1] * co[2];
+      u[4] = -3 * k * k * s[0] * s[1] * s[2];
+    }
+    break;
+  }
+  case ORC_EX_POLYEXP: {
+    /* u = p(x) q(y) q(z), p = x(1-x)e^x, q = y(1-y) */
+    double ex = exp(x[0]);
+    double p = x[0] * (1 - x[0]) * ex;
+    double p1 = ex * (1 - x[0] - x[0] * x[0]);
+    double p2 = -ex * x[0] * (3 + x[0]);
+    double qy = x[1] * (1 - x[1]), qz = x[2] * (1 - x[2]);
+    double qy1 = 1 - 2 * x[1], qz1 = 1 - 2 * x[2];
+    u[0] = p * qy * qz;
+    u[1] = p1 * qy * qz;
+    u[2] = p * qy1 * qz;
+    u[3] = p * qy * qz1;
+    u[4] = p2 * qy * qz - 2 * p * qz - 2 * p * qy;
+    break;
+  }
+  case ORC_EX_POLY1:
+    u[0] = 1 + x[0] + 2 * x[1] + (d == 3 ? 3 * x[2] : 0);
+    u[1] = 1;
+    u[2] = 2;
+    if (d == 3) u[3] = 3;
+    break;
+  default:
+    break;
+  }
+}
+
+/* coefficients at a point: co[0]=eps, co[1..d]=b, co[d+1]=c, co[d+2]=f,
+ * co[d+3] = |b|_inf (ConvDiff.C:1858-1863, 1970-1976 coefficient layout) */
+static void coeffs_at(const orc_config *c, const double *x, double *co) {
+  int d = c->dim;
+  co[0] = c->eps;
+  double binf = 0;
+  for (int a = 0; a < d; ++a) {
+    co[1 + a] = c->b[a];
+    if (fabs(c->b[a]) > binf) binf = fabs(c->b[a]);
+  }
+  co[d + 1] = c->c;
+  if (c->example == ORC_EX_CONST_F) {
+    co[d + 2] = 1.0;
+  } else {
+    double u[5];
+    exact_sol(c, x, u);
+    /* f = -eps lap u + b.grad u + c u, with the reference's summation order
+     * (SineLaplace.h BilinearCoeffs) */
+    double f = -c->eps * u[d + 1];
+    for (int a = 0; a < d; ++a) f += c->b[a] * u[1 + a];
+    f += c->c * u[0];
+    co[d + 2] = f;
+  }
+  co[d + 3] = binf;
+}
+
+/* boundary component of a boundary joint centre (2D: SineLaplace transform,
+ * comps 0:y=0, 1:x=1, 2:y=1, 3:x=0; 3D: 0:z=0 1:y=0 2:x=1 3:y=1 4:x=0 5:z=1) */
+static int boundary_comp(int dim, const double *x) {
+  const double t = 1e-12;
+  if (dim == 2) {
+    if (fabs(x[1]) < t) return 0;
+    if (fabs(x[0] - 1) < t) return 1;
+    if (fabs(x[1] - 1) < t) return 2;
+    if (fabs(x[0]) < t) return 3;
+    return -1;
+  }
+  if (fabs(x[2]) < t) return 0;
+  if (fabs(x[1]) < t) return 1;
+  if (fabs(x[0] - 1) < t) return 2;
+  if (fabs(x[1] - 1) < t) return 3;
+  if (fabs(x[0]) < t) return 4;
+  if (fabs(x[2] - 1) < t) return 5;
+  return -1;
+}
+static int bc_type(const orc_config *c, int comp) {
+  return (c->neumann_mask >> comp) & 1; /* 0 DIRICHLET, 1 NEUMANN */
+}
+
+/* ------------------------------------------------------------------------ */
+/* FE space: DOF numbering by the reference's marker algorithm               */
+/* ------------------------------------------------------------------------ */
+#define FIRSTMARK (-10)
+#define N_BC_TYPES 7
+
+static int find_root(const int *gn, int w) {
+  int v;
+  while ((v = gn[w]) > -1) w = v;
+  return w;
+}
+
+/* FEMapper::map_single_dof (FEMapper.C:456-545) */
+static int map_single_dof(int *gn, int dof0, int dof1, int *counter) {
+  int w0 = find_root(gn, dof0), w1 = find_root(gn, dof1);
+  if (gn[dof0] == -1 && gn[dof1] == -1) {
+    (*counter)--;
+    if (dof0 < dof1) {
+      gn[dof0] = *counter;
+      gn[dof1] = dof0;
+    } else {
+      gn[dof1] = *counter;
+      gn[dof0] = dof1;
+    }
+  } else if (gn[dof0] == -1) {
+    if (w1 > dof0) {
+      gn[dof0] = gn[w1];
+      gn[dof1] = dof0;
+      gn[w1] = dof0;
+    } else {
+      gn[dof0] = w1;
+    }
+  } else if (gn[dof1] == -1) {
+    if (w0 > dof1) {
+      gn[dof1] = gn[w0];
+      gn[dof0] = dof1;
+      gn[w0] = dof1;
+    } else {
+      gn[dof1] = w0;
+    }
+  } else if (gn[w0] != gn[w1]) {
+    int e = gn[w0] > gn[w1] ? gn[w0] : gn[w1];
+    int w = w0 < w1 ? w0 : w1;
+    gn[w0] = w;
+    gn[w1] = w;
+    gn[w] = e;
+  } else if (w0 != w1) {
+    FAIL("map_single_dof: inconsistent identification");
+  }
+  if (gn[dof0] >= dof0 || gn[w0] >= w0 || gn[dof1] >= dof1 || gn[w1] >= w1)
+    FAIL("map_single_dof: link to a later entry");
+  return 0;
+}
+
+/* FEMapper::map_single_boundary_dof (FEMapper.C:555-600), no hanging nodes */
+static void map_single_boundary_dof(int *gn, int dof, int *bcounter) {
+  int w = find_root(gn, dof);
+  if (gn[w] == -1) {
+    (*bcounter)--;
+    gn[dof] = *bcounter;
+  } else if (gn[w] < *bcounter) {
+    (*bcounter)--;
+    gn[w] = *bcounter;
+    if (dof != w) gn[dof] = w;
+  }
+}
+
+/* local DOFs of a cell lying on joint j, in joint order */
+static int joint_dofs(int dim, int p, int j, int *idx) {
+  int nloc = dim == 2 ? (p + 1) * (p + 1) : (p + 1) * (p + 1) * (p + 1);
+  /* fixed ref coordinate of joint j */
+  int axis, side;
+  if (dim == 2) {
+    static const int ax[4] = {1, 0, 1, 0}, sd[4] = {-1, 1, 1, -1};
+    axis = ax[j];
+    side = sd[j];
+  } else {
+    static const int ax[6] = {2, 1, 0, 1, 0, 2}, sd[6] = {-1, -1, 1, 1, -1, 1};
+    axis = ax[j];
+    side = sd[j];
+  }
+  int n = 0;
+  for (int k = 0; k < nloc; ++k) {
+    double r[3];
+    local_dof_ref(dim, p, k, r);
+    if (r[axis] == side) idx[n++] = k;
+  }
+  return n;
+}
+
+static long lattice_key(int dim, const double *x, double scale, long n1) {
+  long k = 0;
+  for (int a = dim - 1; a >= 0; --a) k = k * n1 + lround(x[a] * scale);
+  return k;
+}
+
+static void dof_position(int dim, int p, const double *cv, int k, double *x) {
+  affine_t A;
+  cell_affine(dim, cv, &A);
+  double r[3];
+  local_dof_ref(dim, p, k, r);
+  affine_map(dim, &A, r, x);
+}
+
+static int build_space(const orc_config *cfg, level_t *L, int nref) {
+  int dim = cfg->dim, p = cfg->order, nv = L->nv;
+  int nj = dim == 2 ? 4 : 6;
+  int nc = L->ncells, nloc = L->nloc;
+  long N = 1L << nref;
+  /* joint centre lattice (resolution 2N) -> (cell, joint) of first owner */
+  long jn1 = 2 * N + 1;
+  long jsize = dim == 2 ? jn1 * jn1 : jn1 * jn1 * jn1;
+  int *jowner = (int *)malloc(sizeof(int) * jsize);
+  for (long i = 0; i < jsize; ++i) jowner[i] = -1;
+  int *neigh = (int *)malloc(sizeof(int) * nc * nj);   /* neighbour cell */
+  int *bcomp = (int *)malloc(sizeof(int) * nc * nj);   /* boundary comp */
+  for (int c = 0; c < nc; ++c) {
+    const double *cv = L->verts + (size_t)c * nv * dim;
+    for (int j = 0; j < nj; ++j) {
+      double ctr[3] = {0, 0, 0};
+      int nvj = dim == 2 ? 2 : 4;
+      for (int m = 0; m < nvj; ++m) {
+        int vid = dim == 2 ? (m == 0 ? j : (j + 1) % 4) : HEX_FACE[j][m];
+        for (int a = 0; a < dim; ++a) ctr[a] += cv[vid * dim + a] / nvj;
+      }
+      bcomp[c * nj + j] = boundary_comp(dim, ctr);
+      long key = lattice_key(dim, ctr, 2.0 * N, jn1);
+      neigh[c * nj + j] = -1;
+      if (bcomp[c * nj + j] < 0) {
+        if (jowner[key] < 0) {
+          jowner[key] = c * nj + j;
+        } else {
+          int o = jowner[key];
+          neigh[c * nj + j] = o / nj;
+          neigh[o] = c;
+        }
+      }
+    }
+  }
+  free(jowner);
+
+  /* find_boundary_upper_bounds (FESpace2D.C:58-81) */
+  int jd[MAXLOC];
+  int njd = joint_dofs(dim, p, 0, jd);
+  int bub[N_BC_TYPES] = {0};
+  for (int c = 0; c < nc; ++c)
+    for (int j = 0; j < nj; ++j)
+      if (bcomp[c * nj + j] >= 0) bub[bc_type(cfg, bcomp[c * nj + j])] += njd;
+
+  int counters[N_BC_TYPES + 1];
+  counters[0] = FIRSTMARK + 1;
+  for (int i = 0; i < N_BC_TYPES; ++i) counters[i + 1] = counters[i] - bub[i];
+  int *counter = &counters[N_BC_TYPES];
+
+  int *gn = (int *)malloc(sizeof(int) * nc * nloc);
+  for (int i = 0; i < nc * nloc; ++i) gn[i] = -1;
+
+  /* ConstructSpace cell loop (FESpace2D.C:118-309) */
+  for (int c = 0; c < nc; ++c) {
+    const double *cv = L->verts + (size_t)c * nv * dim;
+    int I0 = c * nloc;
+    for (int j = 0; j < nj; ++j) {
+      int idx0[MAXLOC];
+      int n0 = joint_dofs(dim, p, j, idx0);
+      if (bcomp[c * nj + j] >= 0) {
+        int t = bc_type(cfg, bcomp[c * nj + j]);
+        for (int m = 0; m < n0; ++m)
+          map_single_boundary_dof(gn, I0 + idx0[m], &counters[t]);
+      } else {
+        int n = neigh[c * nj + j];
+        if (n > c) {
+          const double *nvv = L->verts + (size_t)n * nv * dim;
+          int I1 = n * nloc;
+          /* joint of the neighbour: the one whose DOFs coincide */
+          for (int m = 0; m < n0; ++m) {
+            double x0[3], x1[3];
+            dof_position(dim, p, cv, idx0[m], x0);
+            int found = -1;
+            for (int k = 0; k < nloc && found < 0; ++k) {
+              dof_position(dim, p, nvv, k, x1);
+              double dd = 0;
+              for (int a = 0; a < dim; ++a) dd += fabs(x0[a] - x1[a]);
+              if (dd < 1e-12) found = k;
+            }
+            if (found < 0) FAIL("neighbour DOF not found");
+            if (map_single_dof(gn, I0 + idx0[m], I1 + found, counter))
+              return -1;
+          }
+        }
+      }
+    }
+    /* cell-inner DOFs (all ref coords strictly inside) */
+    for (int k = 0; k < nloc; ++k) {
+      double r[3];
+      local_dof_ref(dim, p, k, r);
+      int inner = 1;
+      for (int a = 0; a < dim; ++a)
+        if (r[a] == -1 || r[a] == 1) inner = 0;
+      if (inner) {
+        (*counter)--;
+        gn[I0 + k] = *counter;
+      }
+    }
+  }
+  free(neigh);
+  free(bcomp);
+
+  /* compute_various_numbers (FESpace.C:1863-2099), no hanging nodes */
+  int total_bub = 0;
+  for (int i = 0; i < N_BC_TYPES; ++i) total_bub += bub[i];
+  int boundmark[N_BC_TYPES];
+  int l = FIRSTMARK;
+  for (int i = 0; i < N_BC_TYPES; ++i) {
+    l -= bub[i];
+    boundmark[i] = l;
+  }
+  int innermark = l;
+  int sumlocdof = nc * nloc;
+  int slavemark = l - sumlocdof;
+  int dirichlet_counter = 0;
+  int boundcounter[N_BC_TYPES];
+  l = 0;
+  for (int i = 0; i < N_BC_TYPES; ++i) {
+    l += bub[i];
+    boundcounter[i] = l;
+  }
+  int count = l;
+  int n_dirichlet = 0, n_inner = 0, n_bound[N_BC_TYPES] = {0};
+  for (int i = 0; i < sumlocdof; ++i) {
+    int v = gn[i];
+    if (v < -1) {
+      if (v <= slavemark) FAIL("hanging node in a conforming mesh");
+      if (v <= innermark) {
+        gn[i] = count++;
+        n_inner++;
+        continue;
+      }
+      int m = N_BC_TYPES - 1;
+      for (; m >= 0; m--) {
+        if (v <= boundmark[m]) {
+          gn[i] = boundcounter[m]++;
+          n_bound[m]++;
+          m = -2;
+          break;
+        }
+      }
+      if (m != -2 && v <= FIRSTMARK) {
+        gn[i] = dirichlet_counter++;
+        n_dirichlet++;
+      }
+    } else if (v >= 0) {
+      gn[i] = gn[v];
+    } else {
+      FAIL("unhandled local dof");
+    }
+  }
+  int nb = 0;
+  for (int i = 0; i < N_BC_TYPES; ++i) nb += n_bound[i];
+  int dirichlet_offset = n_inner + nb;
+  int inner_offset = -total_bub;
+  int boundoffset[N_BC_TYPES];
+  l = n_inner;
+  for (int i = 0, m = 0; i < N_BC_TYPES; ++i) {
+    m += bub[i];
+    boundoffset[i] = l - m;
+    l += n_bound[i];
+  }
+  int dirichletmark = bub[0];
+  l = bub[0];
+  for (int i = 0; i < N_BC_TYPES - 1; ++i) {
+    l += bub[i + 1];
+    boundmark[i] = l;
+  }
+  boundmark[N_BC_TYPES - 1] = l;
+  for (int i = 0; i < sumlocdof; ++i) {
+    int v = gn[i];
+    if (v < dirichletmark) {
+      gn[i] += dirichlet_offset;
+    } else if (v < boundmark[N_BC_TYPES - 1]) {
+      for (int m = 0; m < N_BC_TYPES; ++m)
+        if (v < boundmark[m]) {
+          gn[i] += boundoffset[m];
+          break;
+        }
+    } else {
+      gn[i] += inner_offset;
+    }
+  }
+  L->gdof = gn;
+  L->nactive = n_inner + nb;
+  L->ndof = n_inner + nb + n_dirichlet;
+  return 0;
+}
+
+/* TStructure: union of cell couplings, full rows, sorted columns */
+static int cmp_int(const void *a, const void *b) {
+  int x = *(const int *)a, y = *(const int *)b;
+  return (x > y) - (x < y);
+}
+static int build_structure(level_t *L) {
+  int n = L->ndof, nloc = L->nloc;
+  int *ub = (int *)calloc(n + 1, sizeof(int));
+  for (int c = 0; c < L->ncells; ++c)
+    for (int m = 0; m < nloc; ++m) ub[L->gdof[c * nloc + m] + 1] += nloc;
+  for (int i = 0; i < n; ++i) ub[i + 1] += ub[i];
+  int *tmp = (int *)malloc(sizeof(int) * ub[n]);
+  int *fill = (int *)calloc(n, sizeof(int));
+  for (int c = 0; c < L->ncells; ++c)
+    for (int m = 0; m < nloc; ++m) {
+      int r = L->gdof[c * nloc + m];
+      for (int k = 0; k < nloc; ++k)
+        tmp[ub[r] + fill[r]++] = L->gdof[c * nloc + k];
+    }
+  L->row_ptr = (int *)malloc(sizeof(int) * (n + 1));
+  L->row_ptr[0] = 0;
+  int nnz = 0;
+  for (int r = 0; r < n; ++r) {
+    int *seg = tmp + ub[r];
+    qsort(seg, fill[r], sizeof(int), cmp_int);
+    int u = 0;
+    for (int k = 0; k < fill[r]; ++k)
+      if (k == 0 || seg[k] != seg[k - 1]) seg[u++] = seg[k];
+    fill[r] = u;
+    nnz += u;
+    L->row_ptr[r + 1] = nnz;
+  }
+  L->col = (int *)malloc(sizeof(int) * nnz);
+  for (int r = 0; r < n; ++r)
+    memcpy(L->col + L->row_ptr[r], tmp + ub[r], sizeof(int) * fill[r]);
+  L->nnz = nnz;
+  free(tmp);
+  free(fill);
+  free(ub);
+  return 0;
+}
+
+orc_problem *orc_create(const orc_config *cfg, int n_levels) {
+  if (cfg->dim != 2 && cfg->dim != 3) {
+    snprintf(g_err, sizeof g_err, "dim must be 2 or 3");
+    return NULL;
+  }
+  if (cfg->order != 1 && cfg->order != 2) {
+    snprintf(g_err, sizeof g_err, "order must be 1 or 2");
+    return NULL;
+  }
+  if (n_levels < 1 || n_levels > cfg->nref + 1) {
+    snprintf(g_err, sizeof g_err, "bad number of levels");
+    return NULL;
+  }
+  orc_problem *p = (orc_problem *)calloc(1, sizeof(orc_problem));
+  p->cfg = *cfg;
+  if (p->cfg.poly_degree <= 0) p->cfg.poly_degree = cfg->order;
+  p->nlev = n_levels;
+  p->lev = (level_t *)calloc(n_levels, sizeof(level_t));
+  int dim = cfg->dim;
+  for (int k = 0; k < n_levels; ++k) {
+    level_t *L = &p->lev[k];
+    L->nv = nverts(dim);
+    L->nloc = dim == 2 ? (cfg->order + 1) * (cfg->order + 1)
+                       : (cfg->order + 1) * (cfg->order + 1) * (cfg->order + 1);
+    L->verts = refine_mesh(dim, cfg->nref - k, &L->ncells);
+    if (build_space(&p->cfg, L, cfg->nref - k)) {
+      orc_destroy(p);
+      return NULL;
+    }
+    build_structure(L);
+    L->val = (double *)calloc(L->nnz, sizeof(double));
+    L->rhs = (double *)calloc(L->ndof, sizeof(double));
+    L->sol = (double *)calloc(L->ndof, sizeof(double));
+    L->diag = (double *)calloc(L->ndof, sizeof(double));
+    L->mg_rhs = (double *)calloc(L->ndof, sizeof(double));
+    L->mg_sol = (double *)calloc(L->ndof, sizeof(double));
+    L->mg_def = (double *)calloc(L->ndof, sizeof(double));
+  }
+  /* quadrature rule: degree N_terms * p (FEDatabase.C:1553-1556) */
+  int nterms = cfg->problem_linear ? 2 : 3;
+  p->nqp1 = gauss_points_for_degree(nterms * cfg->order);
+  make_rule(dim, p->nqp1, &p->qr);
+  return p;
+}
+
+void orc_destroy(orc_problem *p) {
+  if (!p) return;
+  for (int k = 0; k < p->nlev; ++k) {
+    level_t *L = &p->lev[k];
+    free(L->verts); free(L->gdof); free(L->row_ptr); free(L->col);
+    free(L->val); free(L->rhs); free(L->sol); free(L->diag);
+    free(L->mg_rhs); free(L->mg_sol); free(L->mg_def);
+    free(L->lu); free(L->piv);
+  }
+  free(p->lev);
+  free(p);
+}
+
+int orc_level_info(const orc_problem *p, int level, int *info) {
+  if (level < 0 || level >= p->nlev) FAIL("bad level");
+  const level_t *L = &p->lev[level];
+  info[0] = L->ncells; info[1] = L->nloc; info[2] = L->ndof;
+  info[3] = L->nactive; info[4] = L->nnz; info[5] = L->nv;
+  return 0;
+}
+int orc_get_mesh(const orc_problem *p, int level, double *v) {
+  const level_t *L = &p->lev[level];
+  memcpy(v, L->verts, sizeof(double) * L->ncells * L->nv * p->cfg.dim);
+  return 0;
+}
+int orc_get_gdof(const orc_problem *p, int level, int *g) {
+  const level_t *L = &p->lev[level];
+  memcpy(g, L->gdof, sizeof(int) * L->ncells * L->nloc);
+  return 0;
+}
+int orc_get_structure(const orc_problem *p, int level, int *rp, int *col) {
+  const level_t *L = &p->lev[level];
+  memcpy(rp, L->row_ptr, sizeof(int) * (L->ndof + 1));
+  memcpy(col, L->col, sizeof(int) * L->nnz);
+  return 0;
+}
+int orc_get_matrix(const orc_problem *p, int level, double *v) {
+  const level_t *L = &p->lev[level];
+  memcpy(v, L->val, sizeof(double) * L->nnz);
+  return 0;
+}
+int orc_get_rhs(const orc_problem *p, int level, double *v) {
+  const level_t *L = &p->lev[level];
+  memcpy(v, L->rhs, sizeof(double) * L->ndof);
+  return 0;
+}
+int orc_get_solution(const orc_problem *p, double *v) {
+  memcpy(v, p->lev[0].sol, sizeof(double) * p->lev[0].ndof);
+  return 0;
+}
+int orc_set_solution(orc_problem *p, const double *v) {
+  memcpy(p->lev[0].sol, v, sizeof(double) * p->lev[0].ndof);
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* local assembly                                                            */
+/* ------------------------------------------------------------------------ */
+/* Compute_SDFEM_delta (ConvDiff.C:269-495) for the steady types */
+static double sdfem_delta(const orc_config *c, double hK, double eps,
+                          const double *b, double react, double linfb) {
+  int d = c->dim;
+  double delta0 = c->delta0, delta1 = c->delta1, delta = 0, alpha;
+  if (fabs(eps) < 1e-20) eps = 1e-20;
+  double h = hK;
+  double nb = b[0] * b[0] + b[1] * b[1];
+  if (d == 3) nb += b[2] * b[2];
+  nb = sqrt(nb);
+  double reaction = fabs(react);
+  switch (c->sdfem_type) {
+  case 0:
+    if (eps < h * nb)
+      delta = delta0 * h / nb;
+    else
+      delta = delta1 * h * h / eps;
+    break;
+  case 1:
+  case 2: {
+    double nu = 1.0 / c->poly_degree;
+    if (nb > 0) {
+      alpha = nu * nb * h / (2 * eps);
+      delta = nu * h * (1 / tanh(alpha) - 1 / alpha) / (2 * nb);
+    } else
+      delta = 0;
+    delta *= delta0;
+    break;
+  }
+  case 4:
+  case 5:
+  case 8:
+    delta = -1;
+    if (c->sdfem_type == 4) {
+      if (linfb > 0) delta = h / linfb;
+    } else if (nb > 0)
+      delta = h / (2 * nb);
+    if (reaction > 0) {
+      alpha = 1.0 / reaction;
+      if (delta < 0 || alpha < delta) delta = alpha;
+    }
+    if (eps > 0) {
+      alpha = h * h / eps;
+      if (delta < 0 || alpha < delta) delta = alpha;
+    }
+    delta *= delta0;
+    if (delta < 0) delta = 0;
+    break;
+  case 7:
+    delta = delta0 * h * h / (4 * eps + 2 * h * nb + h * h * reaction);
+    break;
+  default:
+    delta = 0;
+  }
+  return delta;
+}
+
+int orc_local_system(orc_problem *p, int level, int cell, double *Aloc,
+                     double *floc) {
+  const orc_config *c = &p->cfg;
+  level_t *L = &p->lev[level];
+  int dim = c->dim, nl = L->nloc;
+  const double *cv = L->verts + (size_t)cell * L->nv * dim;
+  affine_t A;
+  cell_affine(dim, cv, &A);
+  double adet = fabs(A.det);
+  double hK = cell_hK(dim, cv, c->cell_measure);
+  for (int i = 0; i < nl * nl; ++i) Aloc[i] = 0;
+  for (int i = 0; i < nl; ++i) floc[i] = 0;
+  double ref[MAXLOC][NDER];
+  int nh = dim == 2 ? 3 : 6;
+  for (int q = 0; q < p->qr.nqp; ++q) {
+    ref_basis(dim, c->order, p->qr.xi[q], ref);
+    /* GetOrigValues: physical derivatives */
+    double u[MAXLOC], g[MAXLOC][3], lap[MAXLOC];
+    for (int k = 0; k < nl; ++k) {
+      u[k] = ref[k][0];
+      for (int r = 0; r < dim; ++r) {
+        double s = 0;
+        for (int a = 0; a < dim; ++a) s += A.Jinv[a][r] * ref[k][1 + a];
+        g[k][r] = s;
+      }
+      /* Laplacian of the affine-transformed Hessian J^-T H J^-1 */
+      double H[3][3];
+      if (dim == 2) {
+        H[0][0] = ref[k][3]; H[0][1] = H[1][0] = ref[k][4]; H[1][1] = ref[k][5];
+      } else {
+        H[0][0] = ref[k][4]; H[0][1] = H[1][0] = ref[k][5];
+        H[0][2] = H[2][0] = ref[k][6]; H[1][1] = ref[k][7];
+        H[1][2] = H[2][1] = ref[k][8]; H[2][2] = ref[k][9];
+      }
+      (void)nh;
+      double l = 0;
+      for (int r = 0; r < dim; ++r)
+        for (int a = 0; a < dim; ++a)
+          for (int b2 = 0; b2 < dim; ++b2)
+            l += A.Jinv[a][r] * A.Jinv[b2][r] * H[a][b2];
+      lap[k] = l;
+    }
+    double x[3];
+    affine_map(dim, &A, p->qr.xi[q], x);
+    double co[8];
+    coeffs_at(c, x, co);
+    double Mult = p->qr.w[q] * adet;
+    double eps = co[0], b[3] = {co[1], co[2], dim == 3 ? co[3] : 0};
+    double react = co[dim + 1], f = co[dim + 2];
+    /* BilinearAssembleGalerkin<d> (ConvDiff.C:1776-1883) */
+    for (int i = 0; i < nl; ++i) {
+      floc[i] += Mult * u[i] * f;
+      for (int j = 0; j < nl; ++j) {
+        double val = 0;
+        for (int r = 0; r < dim; ++r) val += g[i][r] * g[j][r];
+        val *= eps;
+        double bg = 0;
+        for (int r = 0; r < dim; ++r) bg += b[r] * g[j][r];
+        val += bg * u[i];
+        val += react * u[j] * u[i];
+        Aloc[i * nl + j] += val * Mult;
+      }
+    }
+    if (c->supg) {
+      /* BilinearAssemble_SD<d> (ConvDiff.C:1886-1999) */
+      double delta = sdfem_delta(c, hK, eps, b, react, co[dim + 3]);
+      for (int i = 0; i < nl; ++i) {
+        double bgradv = 0;
+        for (int r = 0; r < dim; ++r) bgradv += b[r] * g[i][r];
+        floc[i] += Mult * (delta * bgradv) * f;
+        for (int j = 0; j < nl; ++j) {
+          double val = -eps * lap[j];
+          for (int r = 0; r < dim; ++r) val += b[r] * g[j][r];
+          val += react * u[j];
+          Aloc[i * nl + j] += val * delta * bgradv * Mult;
+        }
+      }
+    }
+  }
+  return 0;
+}
+
+/* Neumann boundary integral on a 2D boundary edge (Assemble2D.C:3210-3248):
+ * g = eps * n.grad(u), line rule of degree 2p */
+static void neumann_edge(orc_problem *p, level_t *L, int cell, int j,
+                         double *rhs) {
+  const orc_config *c = &p->cfg;
+  const double *cv = L->verts + (size_t)cell * L->nv * 2;
+  int nl = L->nloc;
+  int np = line_points_for_degree(2 * c->order);
+  double lx[10], lw[10];
+  gauss_legendre(np, lx, lw);
+  const double *a = cv + 2 * j, *bb = cv + 2 * ((j + 1) % 4);
+  double hE = sqrt((bb[0] - a[0]) * (bb[0] - a[0]) +
+                   (bb[1] - a[1]) * (bb[1] - a[1])) / 2;
+  affine_t A;
+  cell_affine(2, cv, &A);
+  double ctr[2] = {0.5 * (a[0] + bb[0]), 0.5 * (a[1] + bb[1])};
+  int comp = boundary_comp(2, ctr);
+  const double nrm[4][2] = {{0, -1}, {1, 0}, {0, 1}, {-1, 0}};
+  for (int l = 0; l < np; ++l) {
+    double s = 0.5 * (lx[l] + 1);
+    double x[2] = {a[0] + s * (bb[0] - a[0]), a[1] + s * (bb[1] - a[1])};
+    double u[5];
+    exact_sol(c, x, u);
+    double g = c->eps * (nrm[comp][0] * u[1] + nrm[comp][1] * u[2]);
+    /* reference coordinates of x */
+    double xi[3] = {0, 0, 0};
+    for (int aa = 0; aa < 2; ++aa) {
+      double t = 0;
+      for (int r = 0; r < 2; ++r) t += A.Jinv[aa][r] * (x[r] - A.x0[r]);
+      xi[aa] = t;
+    }
+    double ref[MAXLOC][NDER];
+    ref_basis(2, c->order, xi, ref);
+    double sc = g * hE * lw[l];
+    for (int k = 0; k < nl; ++k) {
+      int d = L->gdof[cell * nl + k];
+      if (d < L->nactive) rhs[d] += sc * ref[k][0];
+    }
+  }
+}
+
+static int assemble_level(orc_problem *p, int level) {
+  const orc_config *c = &p->cfg;
+  level_t *L = &p->lev[level];
+  int dim = c->dim, nl = L->nloc;
+  memset(L->val, 0, sizeof(double) * L->nnz);
+  memset(L->rhs, 0, sizeof(double) * L->ndof);
+  double Aloc[MAXLOC * MAXLOC], floc[MAXLOC];
+  for (int cell = 0; cell < L->ncells; ++cell) {
+    orc_local_system(p, level, cell, Aloc, floc);
+    const int *dof = L->gdof + cell * nl;
+    /* scatter by linear row search (Assemble3D.C:257-292) */
+    for (int m = 0; m < nl; ++m) {
+      int l = dof[m];
+      if (l < L->nactive) {
+        for (int k = 0; k < nl; ++k) {
+          int found = 0;
+          for (int n = L->row_ptr[l]; n < L->row_ptr[l + 1]; ++n)
+            if (L->col[n] == dof[k]) {
+              L->val[n] += Aloc[m * nl + k];
+              found = 1;
+              break;
+            }
+          if (!found) FAIL("entry not in pattern");
+        }
+        L->rhs[l] += floc[m];
+      } else {
+        /* Dirichlet row: set(l, l, 1) (Matrix.C:225-233) */
+        for (int n = L->row_ptr[l]; n < L->row_ptr[l + 1]; ++n)
+          if (L->col[n] == l) L->val[n] = 1.0;
+      }
+    }
+  }
+  /* boundary data: Dirichlet values by point evaluation at the nodes (nodal
+   * functionals of Q1/Q2), Neumann integrals (2D) */
+  int nj = dim == 2 ? 4 : 6;
+  for (int cell = 0; cell < L->ncells; ++cell) {
+    const double *cv = L->verts + (size_t)cell * L->nv * dim;
+    for (int j = 0; j < nj; ++j) {
+      double ctr[3] = {0, 0, 0};
+      int nvj = dim == 2 ? 2 : 4;
+      for (int m = 0; m < nvj; ++m) {
+        int vid = dim == 2 ? (m == 0 ? j : (j + 1) % 4) : HEX_FACE[j][m];
+        for (int a = 0; a < dim; ++a) ctr[a] += cv[vid * dim + a] / nvj;
+      }
+      int comp = boundary_comp(dim, ctr);
+      if (comp < 0) continue;
+      if (bc_type(c, comp) == 0) {
+        int idx[MAXLOC];
+        int n = joint_dofs(dim, c->order, j, idx);
+        for (int m = 0; m < n; ++m) {
+          double x[3], u[5];
+          dof_position(dim, c->order, cv, idx[m], x);
+          exact_sol(c, x, u);
+          L->rhs[L->gdof[cell * nl + idx[m]]] = u[0];
+        }
+      } else if (dim == 2) {
+        neumann_edge(p, L, cell, j, L->rhs);
+      }
+    }
+  }
+  /* solution.copy_nonactive(rhs) (ConvectionDiffusion.C:445) */
+  for (int i = L->nactive; i < L->ndof; ++i) L->sol[i] = L->rhs[i];
+  /* diagonal for Jacobi (Iteration_jacobi.C:14-28) */
+  for (int r = 0; r < L->ndof; ++r)
+    for (int n = L->row_ptr[r]; n < L->row_ptr[r + 1]; ++n)
+      if (L->col[n] == r) L->diag[r] = L->val[n];
+  return 0;
+}
+
+int orc_assemble(orc_problem *p) {
+  for (int k = 0; k < p->nlev; ++k)
+    if (assemble_level(p, k)) return -1;
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* linear algebra                                                            */
+/* ------------------------------------------------------------------------ */
+/* y = a*A x + y on active rows; y += a*x on non-active rows */
+static void apply_scaled_add(const level_t *L, const double *x, double *y,
+                             double a) {
+  for (int r = 0; r < L->nactive; ++r) {
+    double s = 0;
+    for (int n = L->row_ptr[r]; n < L->row_ptr[r + 1]; ++n)
+      s += L->val[n] * x[L->col[n]];
+    y[r] += a * s;
+  }
+  for (int r = L->nactive; r < L->ndof; ++r) y[r] += a * x[r];
+}
+
+int orc_apply(const orc_problem *p, int level, const double *x, double *y) {
+  const level_t *L = &p->lev[level];
+  memset(y, 0, sizeof(double) * L->ndof);
+  apply_scaled_add(L, x, y, 1.0);
+  return 0;
+}
+
+static double dot(int n, const double *a, const double *b) {
+  double s = 0;
+  for (int i = 0; i < n; ++i) s += a[i] * b[i];
+  return s;
+}
+
+/* prolongation matrix of one child: QQ[k][l] = coarse basis l at fine local
+ * dof k (nodal functionals of Lagrange elements are point values) */
+static void child_prolongation(const orc_problem *p, const level_t *Lf,
+                               const level_t *Lc, int fcell, double *QQ) {
+  int dim = p->cfg.dim, nl = Lf->nloc;
+  int nch = dim == 2 ? 4 : 8;
+  int ccell = fcell / nch;
+  const double *cvc = Lc->verts + (size_t)ccell * Lc->nv * dim;
+  const double *cvf = Lf->verts + (size_t)fcell * Lf->nv * dim;
+  affine_t Ac;
+  cell_affine(dim, cvc, &Ac);
+  for (int k = 0; k < nl; ++k) {
+    double x[3], xi[3] = {0, 0, 0};
+    dof_position(dim, p->cfg.order, cvf, k, x);
+    for (int a = 0; a < dim; ++a) {
+      double t = 0;
+      for (int r = 0; r < dim; ++r) t += Ac.Jinv[a][r] * (x[r] - Ac.x0[r]);
+      xi[a] = t;
+    }
+    double ref[MAXLOC][NDER];
+    ref_basis(dim, p->cfg.order, xi, ref);
+    for (int l = 0; l < nl; ++l) QQ[k * nl + l] = ref[l][0];
+  }
+}
+
+/* GridTransfer::Prolongate (GridTransfer.C:29-218) */
+int orc_prolongate(const orc_problem *p, int fine, const double *xc,
+                   double *xf) {
+  const level_t *Lf = &p->lev[fine], *Lc = &p->lev[fine + 1];
+  int nl = Lf->nloc, nch = p->cfg.dim == 2 ? 4 : 8;
+  double *aux = (double *)calloc(Lf->ndof, sizeof(double));
+  memset(xf, 0, sizeof(double) * Lf->ndof);
+  double QQ[MAXLOC * MAXLOC];
+  for (int f = 0; f < Lf->ncells; ++f) {
+    int cc = f / nch;
+    child_prolongation(p, Lf, Lc, f, QQ);
+    for (int k = 0; k < nl; ++k) {
+      double s = 0;
+      for (int l = 0; l < nl; ++l) s += QQ[k * nl + l] * xc[Lc->gdof[cc * nl + l]];
+      int idx = Lf->gdof[f * nl + k];
+      xf[idx] += s;
+      aux[idx] += 1;
+    }
+  }
+  for (int i = 0; i < Lf->ndof; ++i) xf[i] /= aux[i];
+  free(aux);
+  return 0;
+}
+
+/* GridTransfer::DefectRestriction (GridTransfer.C:222-410) */
+int orc_restrict(const orc_problem *p, int fine, const double *df,
+                 double *rc) {
+  const level_t *Lf = &p->lev[fine], *Lc = &p->lev[fine + 1];
+  int nl = Lf->nloc, nch = p->cfg.dim == 2 ? 4 : 8;
+  double *aux = (double *)calloc(Lf->ndof, sizeof(double));
+  double *cp = (double *)malloc(sizeof(double) * Lf->ndof);
+  memset(rc, 0, sizeof(double) * Lc->ndof);
+  for (int f = 0; f < Lf->ncells; ++f)
+    for (int k = 0; k < nl; ++k) aux[Lf->gdof[f * nl + k]] += 1;
+  for (int i = 0; i < Lf->ndof; ++i) cp[i] = df[i] / aux[i];
+  double QQ[MAXLOC * MAXLOC];
+  for (int f = 0; f < Lf->ncells; ++f) {
+    int cc = f / nch;
+    child_prolongation(p, Lf, Lc, f, QQ);
+    for (int l = 0; l < nl; ++l) {
+      double s = 0;
+      for (int k = 0; k < nl; ++k) s += QQ[k * nl + l] * cp[Lf->gdof[f * nl + k]];
+      rc[Lc->gdof[cc * nl + l]] += s;
+    }
+  }
+  free(aux);
+  free(cp);
+  return 0;
+}
+
+/* dense LU with partial pivoting of the full coarse matrix */
+static int coarse_factor(level_t *L) {
+  int n = L->ndof;
+  free(L->lu);
+  free(L->piv);
+  L->lu = (double *)calloc((size_t)n * n, sizeof(double));
+  L->piv = (int *)malloc(sizeof(int) * n);
+  for (int r = 0; r < L->nactive; ++r)
+    for (int k = L->row_ptr[r]; k < L->row_ptr[r + 1]; ++k)
+      L->lu[(size_t)r * n + L->col[k]] = L->val[k];
+  for (int r = L->nactive; r < n; ++r) L->lu[(size_t)r * n + r] = 1.0;
+  double *a = L->lu;
+  for (int k = 0; k < n; ++k) {
+    int pr = k;
+    double mx = fabs(a[(size_t)k * n + k]);
+    for (int i = k + 1; i < n; ++i)
+      if (fabs(a[(size_t)i * n + k]) > mx) {
+        mx = fabs(a[(size_t)i * n + k]);
+        pr = i;
+      }
+    if (mx == 0) FAIL("singular coarse matrix");
+    L->piv[k] = pr;
+    if (pr != k)
+      for (int j = 0; j < n; ++j) {
+        double t = a[(size_t)k * n + j];
+        a[(size_t)k * n + j] = a[(size_t)pr * n + j];
+        a[(size_t)pr * n + j] = t;
+      }
+    double d = a[(size_t)k * n + k];
+    for (int i = k + 1; i < n; ++i) {
+      double m = a[(size_t)i * n + k] / d;
+      a[(size_t)i * n + k] = m;
+      if (m != 0)
+        for (int j = k + 1; j < n; ++j) a[(size_t)i * n + j] -= m * a[(size_t)k * n + j];
+    }
+  }
+  return 0;
+}
+
+static void coarse_solve(const level_t *L, const double *b, double *x) {
+  int n = L->ndof;
+  for (int i = 0; i < n; ++i) x[i] = b[i];
+  for (int k = 0; k < n; ++k) {
+    int pr = L->piv[k];
+    if (pr != k) {
+      double t = x[k];
+      x[k] = x[pr];
+      x[pr] = t;
+    }
+  }
+  for (int i = 0; i < n; ++i) {
+    double s = x[i];
+    for (int j = 0; j < i; ++j) s -= L->lu[(size_t)i * n + j] * x[j];
+    x[i] = s;
+  }
+  for (int i = n - 1; i >= 0; --i) {
+    double s = x[i];
+    for (int j = i + 1; j < n; ++j) s -= L->lu[(size_t)i * n + j] * x[j];
+    x[i] = s / L->lu[(size_t)i * n + i];
+  }
+}
+
+/* JacobiSmoother::smooth (JacobiSmoother.C:21-29) */
+static void jacobi_smooth(level_t *L, double damp) {
+  int n = L->ndof;
+  double *d = L->mg_def;
+  memcpy(d, L->mg_rhs, sizeof(double) * n);
+  apply_scaled_add(L, L->mg_sol, d, -1.0);
+  for (int i = 0; i < n; ++i) d[i] /= L->diag[i];
+  for (int i = 0; i < n; ++i) L->mg_sol[i] += damp * d[i];
+}
+
+static double calc_defect(level_t *L) {
+  int n = L->ndof;
+  memcpy(L->mg_def, L->mg_rhs, sizeof(double) * n);
+  apply_scaled_add(L, L->mg_sol, L->mg_def, -1.0);
+  return sqrt(dot(n, L->mg_def, L->mg_def));
+}
+
+/* CycleControl (CycleControl.C:15-111): direction sequence */
+enum { DIR_DUMMY, DIR_DOWN, DIR_UP, DIR_END };
+static void fill_cycle(int *seq, int *n, int *rec, int level, int nlev,
+                       int cyc) {
+  if (level == 0) {
+    seq[(*n)++] = DIR_UP;
+    return;
+  }
+  for (int j = 0; j < rec[level]; ++j) {
+    seq[(*n)++] = DIR_DOWN;
+    fill_cycle(seq, n, rec, level - 1, nlev, cyc);
+  }
+  if (cyc == 2) rec[level] = 1;
+  seq[(*n)++] = level == nlev - 1 ? DIR_END : DIR_UP;
+}
+
+/* Multigrid::cycle (Multigrid.C:157-308); MG levels are indexed coarsest
+ * first there, here lev[0] is the finest: mg level m <-> lev[nlev-1-m] */
+int orc_mg_apply(orc_problem *p, const orc_solver_config *s, const double *v,
+                 double *z) {
+  int nl = s->mg_levels;
+  if (nl < 1 || nl > p->nlev) FAIL("bad multigrid level count");
+  level_t *fine = &p->lev[0];
+  memcpy(fine->mg_rhs, v, sizeof(double) * fine->ndof);
+  /* finest start: 0, non-actives copied from rhs */
+  memset(fine->mg_sol, 0, sizeof(double) * fine->ndof);
+  for (int i = fine->nactive; i < fine->ndof; ++i) fine->mg_sol[i] = v[i];
+  int rec[8];
+  for (int i = 0; i < nl; ++i) rec[i] = s->mg_cycle == 0 ? 1 : 2;
+  rec[nl - 1] = 1;
+  static int seq[4096];
+  int ns = 0;
+  seq[ns++] = DIR_DUMMY;
+  fill_cycle(seq, &ns, rec, nl - 1, nl, s->mg_cycle);
+  int level = nl - 1; /* mg index */
+  for (int step = 1; step < ns && level >= 0; ++step) {
+    level_t *L = &p->lev[nl - 1 - level];
+    if (level == 0) {
+      double res = 1e10;
+      calc_defect(L);
+      for (int i = 0; i < s->coarse_maxit && res > s->coarse_eps; ++i) {
+        if (s->coarse_direct)
+          coarse_solve(L, L->mg_rhs, L->mg_sol);
+        else
+          jacobi_smooth(L, s->jacobi_damp);
+        res = calc_defect(L);
+      }
+      /* update_solution_in_finer_grid */
+      level_t *F = &p->lev[nl - 1 - (level + 1)];
+      double *pr = (double *)malloc(sizeof(double) * F->ndof);
+      orc_prolongate(p, nl - 1 - (level + 1), L->mg_sol, pr);
+      for (int i = 0; i < F->nactive; ++i) F->mg_sol[i] += s->correction_damp * pr[i];
+      free(pr);
+      level = level + 1;
+      continue;
+    }
+    int coming_from_below = seq[step - 1] == DIR_UP;
+    int dir = seq[step];
+    if (coming_from_below)
+      for (int i = 0; i < s->n_post; ++i) jacobi_smooth(L, s->jacobi_damp);
+    if (dir == DIR_DOWN) {
+      for (int i = 0; i < s->n_pre; ++i) jacobi_smooth(L, s->jacobi_damp);
+      calc_defect(L);
+      level_t *C = &p->lev[nl - 1 - (level - 1)];
+      memset(C->mg_sol, 0, sizeof(double) * C->ndof);
+      orc_restrict(p, nl - 1 - level, L->mg_def, C->mg_rhs);
+      for (int i = C->nactive; i < C->ndof; ++i) C->mg_rhs[i] = 0;
+      level = level - 1;
+    } else if (dir == DIR_UP) {
+      level_t *F = &p->lev[nl - 1 - (level + 1)];
+      double *pr = (double *)malloc(sizeof(double) * F->ndof);
+      orc_prolongate(p, nl - 1 - (level + 1), L->mg_sol, pr);
+      for (int i = 0; i < F->nactive; ++i) F->mg_sol[i] += s->correction_damp * pr[i];
+      free(pr);
+      level = level + 1;
+    } else {
+      break; /* END */
+    }
+  }
+  memcpy(z, fine->mg_sol, sizeof(double) * fine->ndof);
+  return 0;
+}
+
+/* GenerateGivensRotation / ApplyGivensRotation (Utilities_gmres.C:60-88) */
+static void gen_givens(double dx, double dy, double *cs, double *sn) {
+  if (dy == 0.0) {
+    *cs = 1.0;
+    *sn = 0.0;
+  } else if (fabs(dy) > fabs(dx)) {
+    double t = dx / dy;
+    *sn = 1.0 / sqrt(1.0 + t * t);
+    *cs = t * *sn;
+  } else {
+    double t = dy / dx;
+    *cs = 1.0 / sqrt(1.0 + t * t);
+    *sn = t * *cs;
+  }
+}
+static void app_givens(double *dx, double *dy, double cs, double sn) {
+  double t = cs * *dx + sn * *dy;
+  *dy = -sn * *dx + cs * *dy;
+  *dx = t;
+}
+
+typedef struct {
+  double initial, previous;
+} loop_info;
+
+/* IterativeMethod::converged (IterativeMethod.h:83-163); returns 1 to stop,
+ * 2 on divergence */
+static int converged(const orc_solver_config *s, loop_info *li, double res,
+                     int it) {
+  if (it == 0) {
+    li->initial = res;
+    li->previous = res;
+  }
+  int small = res < s->tol_abs;
+  int red = res < s->reduction * li->initial;
+  int enough = it >= s->min_it;
+  int stag = res > 1e10 * li->previous;
+  int div = res > s->divergence * li->initial;
+  int conv = (small || red || stag || div) && enough;
+  if (it == s->max_it) conv = 1;
+  li->previous = res;
+  if (div) return 2;
+  return conv;
+}
+
+static void precond(orc_problem *p, const orc_solver_config *s,
+                    const double *v, double *z) {
+  level_t *L = &p->lev[0];
+  if (s->precond == 1) {
+    for (int i = 0; i < L->ndof; ++i) z[i] = v[i] / L->diag[i];
+  } else if (s->precond == 2) {
+    orc_mg_apply(p, s, v, z);
+  } else {
+    memcpy(z, v, sizeof(double) * L->ndof);
+  }
+}
+
+/* Iteration_gmres::flexible_gmres (Iteration_gmres.C:430-620) */
+int orc_solve(orc_problem *p, const orc_solver_config *s, int *iters,
+              double *residual, double *initial) {
+  level_t *L = &p->lev[0];
+  int n = L->ndof, m = s->restart;
+  if (s->precond == 2) {
+    if (s->mg_levels > p->nlev) FAIL("not enough levels for multigrid");
+    for (int k = 0; k < s->mg_levels; ++k)
+      for (int r = 0; r < p->lev[k].ndof; ++r)
+        if (p->lev[k].diag[r] == 0) FAIL("zero diagonal entry");
+    if (s->coarse_direct && coarse_factor(&p->lev[s->mg_levels - 1])) return -1;
+  } else if (s->precond == 1) {
+    for (int r = 0; r < n; ++r)
+      if (L->diag[r] == 0) FAIL("zero entry on the diagonal using Jacobi");
+  }
+  double *x = L->sol, *b = L->rhs;
+  double *r = (double *)malloc(sizeof(double) * n);
+  double **v = (double **)malloc(sizeof(double *) * (m + 1));
+  double **z = (double **)malloc(sizeof(double *) * (m + 1));
+  for (int i = 0; i <= m; ++i) {
+    v[i] = (double *)malloc(sizeof(double) * n);
+    z[i] = (double *)malloc(sizeof(double) * n);
+  }
+  double *H = (double *)calloc((size_t)(m + 1) * (m + 1), sizeof(double));
+  double *sv = (double *)calloc(m + 1, sizeof(double));
+  double *cs = (double *)calloc(m + 1, sizeof(double));
+  double *sn = (double *)calloc(m + 1, sizeof(double));
+  loop_info li = {0, 0};
+#define HH(i, j) H[(size_t)(i) * (m + 1) + (j)]
+  memcpy(r, b, sizeof(double) * n);
+  apply_scaled_add(L, x, r, -1.0);
+  double resid = sqrt(dot(n, r, r));
+  double beta = resid;
+  int rc = 0, done = 0, jj = 1;
+  *initial = resid;
+  if (converged(s, &li, resid, 0)) {
+    *iters = 0;
+    *residual = resid;
+    done = 1;
+  }
+  while (!done && jj <= s->max_it) {
+    for (int i = 0; i < n; ++i) v[0][i] = r[i] * (1.0 / beta);
+    memset(sv, 0, sizeof(double) * (m + 1));
+    sv[0] = beta;
+    int i;
+    for (i = 0; i < m && jj <= s->max_it; ++i, ++jj) {
+      precond(p, s, v[i], z[i]);
+      orc_apply(p, 0, z[i], r);
+      for (int k = 0; k <= i; ++k) {
+        HH(k, i) = dot(n, r, v[k]);
+        double h = -HH(k, i);
+        for (int t = 0; t < n; ++t) r[t] += h * v[k][t];
+      }
+      HH(i + 1, i) = sqrt(dot(n, r, r));
+      if (HH(i + 1, i) != 0.0) {
+        double sc = 1.0 / HH(i + 1, i);
+        for (int t = 0; t < n; ++t) v[i + 1][t] = r[t] * sc;
+      } else {
+        snprintf(g_err, sizeof g_err, "Unhappy breakdown in flexible gmres");
+        rc = -1;
+        done = 1;
+        break;
+      }
+      for (int k = 0; k < i; ++k) app_givens(&HH(k, i), &HH(k + 1, i), cs[k], sn[k]);
+      gen_givens(HH(i, i), HH(i + 1, i), &cs[i], &sn[i]);
+      app_givens(&HH(i, i), &HH(i + 1, i), cs[i], sn[i]);
+      app_givens(&sv[i], &sv[i + 1], cs[i], sn[i]);
+      resid = fabs(sv[i + 1]);
+      int cv = converged(s, &li, resid, jj);
+      if (cv) {
+        /* Update (Utilities_gmres.C:90-108) */
+        double y[128];
+        for (int k = 0; k <= i; ++k) y[k] = sv[k];
+        for (int k = i; k >= 0; --k) {
+          y[k] /= HH(k, k);
+          for (int t = k - 1; t >= 0; --t) y[t] -= HH(t, k) * y[k];
+        }
+        for (int k = 0; k <= i; ++k)
+          for (int t = 0; t < n; ++t) x[t] += y[k] * z[k][t];
+        *iters = jj;
+        *residual = resid;
+        if (cv == 2) {
+          snprintf(g_err, sizeof g_err, "solver divergence");
+          rc = -2;
+        }
+        done = 1;
+        break;
+      }
+    }
+    if (done) break;
+    {
+      double y[128];
+      int k0 = m - 1;
+      for (int k = 0; k <= k0; ++k) y[k] = sv[k];
+      for (int k = k0; k >= 0; --k) {
+        y[k] /= HH(k, k);
+        for (int t = k - 1; t >= 0; --t) y[t] -= HH(t, k) * y[k];
+      }
+      for (int k = 0; k <= k0; ++k)
+        for (int t = 0; t < n; ++t) x[t] += y[k] * z[k][t];
+    }
+    memcpy(r, b, sizeof(double) * n);
+    apply_scaled_add(L, x, r, -1.0);
+    beta = sqrt(dot(n, r, r));
+    int cv = converged(s, &li, resid, jj);
+    if (cv) {
+      *iters = jj;
+      *residual = resid;
+      if (cv == 2) rc = -2;
+      done = 1;
+    }
+  }
+  if (!done) {
+    *iters = s->max_it;
+    *residual = resid;
+  }
+#undef HH
+  for (int i = 0; i <= m; ++i) {
+    free(v[i]);
+    free(z[i]);
+  }
+  free(v); free(z); free(r); free(H); free(sv); free(cs); free(sn);
+  return rc;
+}
+
+/* errors: TFEFunction2D::GetErrors + conv_diff_l2_h1_linf_error */
+int orc_errors(const orc_problem *p, double *errors) {
+  const orc_config *c = &p->cfg;
+  const level_t *L = &p->lev[0];
+  int dim = c->dim, nl = L->nloc;
+  double e[5] = {0, 0, 0, 0, 0};
+  double maxe = 0;
+  for (int cell = 0; cell < L->ncells; ++cell) {
+    const double *cv = L->verts + (size_t)cell * L->nv * dim;
+    affine_t A;
+    cell_affine(dim, cv, &A);
+    double hK = cell_hK(dim, cv, c->cell_measure);
+    double fv[MAXLOC];
+    for (int k = 0; k < nl; ++k) fv[k] = L->sol[L->gdof[cell * nl + k]];
+    for (int q = 0; q < p->qr.nqp; ++q) {
+      double ref[MAXLOC][NDER];
+      ref_basis(dim, c->order, p->qr.xi[q], ref);
+      double der[4] = {0, 0, 0, 0};
+      for (int k = 0; k < nl; ++k) {
+        der[0] += fv[k] * ref[k][0];
+      }
+      for (int r = 0; r < dim; ++r) {
+        double s = 0;
+        for (int k = 0; k < nl; ++k) {
+          double g = 0;
+          for (int a = 0; a < dim; ++a) g += A.Jinv[a][r] * ref[k][1 + a];
+          s += fv[k] * g;
+        }
+        der[1 + r] = s;
+      }
+      double x[3], u[5], co[8];
+      affine_map(dim, &A, p->qr.xi[q], x);
+      exact_sol(c, x, u);
+      coeffs_at(c, x, co);
+      double le = fabs(u[0] - der[0]);
+      if (le > maxe) maxe = le;
+      double nu = co[0], bb[3] = {co[1], co[2], dim == 3 ? co[3] : 0};
+      double react = co[dim + 1];
+      double bn = fmax(fabs(bb[0]), fabs(bb[1]));
+      if (dim == 3) bn = fmax(bn, fabs(bb[2]));
+      double delta = sdfem_delta(c, hK, nu, bb, react, bn);
+      double w = p->qr.w[q] * fabs(A.det);
+      double e0 = der[0] - u[0];
+      e[0] += w * e0 * e0;
+      double e1 = der[1] - u[1], e2 = der[2] - u[2];
+      double e3 = dim == 2 ? 0. : der[3] - u[3];
+      e[1] += w * e1 * e1;
+      e[1] += w * e2 * e2;
+      e[1] += w * e3 * e3;
+      double e4 = bb[0] * e1 + bb[1] * e2;
+      if (dim == 3) e4 += bb[2] * e3;
+      e[2] += w * (nu * (e1 * e1 + e2 * e2 + e3 * e3) + react * e0 * e0 +
+                   delta * e4 * e4);
+      e[3] += w * (nu * (e1 * e1 + e2 * e2 + e3 * e3) + (e4 + react * e0) * e0);
+    }
+  }
+  errors[0] = sqrt(e[0]);
+  errors[1] = sqrt(e[1]);
+  errors[2] = sqrt(e[2]);
+  errors[3] = sqrt(fabs(e[3]));
+  errors[4] = maxe;
+  return 0;
+}

@@ -1,0 +1,106 @@
+/*
+ * cd_oracle.h -- CPU restatement of ParMooN's scalar convection-diffusion
+ * hot path (assembly + FGMRES/Jacobi/multigrid solve + error norms).
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker for the CUDA path:
+ * only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may
+ * load it.  Nothing in parmoon2022_gb300/ links or calls it.
+ *
+ * Every routine names the reference file:line it restates (paths relative to
+ * the ParMooN2022 source tree).  Parity of this restatement is pinned against
+ * the reference's own golden values (test/cd2d_test.c++ error norms,
+ * test/structure_test.c++ pattern counts) by tests/test_oracle_golden.py.
+ */
+#ifndef CD_ORACLE_H
+#define CD_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* example ids: problem data (coefficients, exact solution, boundary data) */
+enum {
+  ORC_EX_SINE_LAPLACE = 0, /* include/Examples/CD_2D/SineLaplace.h (ex. 0)   */
+  ORC_EX_SINE = 1,         /* u = prod sin(k pi x_i), homogeneous Dirichlet    */
+  ORC_EX_POLYEXP = 2,      /* u = x y z (1-x)(1-y)(1-z) exp(x) (3D)            */
+  ORC_EX_CONST_F = 3,      /* f = 1, homogeneous Dirichlet, no exact solution  */
+  ORC_EX_POLY1 = 4         /* u = 1 + x + 2y (+3z): inside Q1, Dirichlet       */
+};
+
+typedef struct {
+  int dim;             /* 2 or 3                                              */
+  int order;           /* 1 (Q1) or 2 (Q2)                                    */
+  int nref;            /* refinement steps of the unit square / cube         */
+  int example;         /* ORC_EX_*                                            */
+  double eps;          /* diffusion coefficient                               */
+  double b[3];         /* convection                                          */
+  double c;            /* reaction                                            */
+  double freq;         /* k in sin(k pi x) for ORC_EX_SINE                    */
+  int supg;            /* 0: galerkin, 1: supg                                */
+  int sdfem_type;      /* TDatabase SDFEM_TYPE                                */
+  double delta0, delta1;
+  int cell_measure;    /* TDatabase CELL_MEASURE                              */
+  int problem_linear;  /* TDatabase INTERNAL_PROBLEM_LINEAR (quad. degree)    */
+  int neumann_mask;    /* bit k: boundary component k is Neumann              */
+  int poly_degree;     /* TDatabase INTERNAL_POLYNOMIAL_DEGREE (SDFEM 1/2)    */
+} orc_config;
+
+typedef struct {
+  int precond;         /* 0 none, 1 jacobi, 2 multigrid                        */
+  int max_it, min_it, restart;
+  double tol_abs;      /* residual_tolerance (absolute)                       */
+  double reduction;    /* residual_reduction                                  */
+  double divergence;   /* divergence_factor                                   */
+  int mg_levels;       /* multigrid_n_levels                                  */
+  int mg_cycle;        /* 0 V, 1 W, 2 F                                       */
+  int n_pre, n_post;
+  double jacobi_damp;
+  double correction_damp;
+  int coarse_direct;   /* 1: direct_solve (dense LU), 0: jacobi iterations    */
+  double coarse_eps;
+  int coarse_maxit;
+} orc_solver_config;
+
+typedef struct orc_problem orc_problem;
+
+/* n_levels grids: level 0 is the finest (nref refinements), level k has
+ * nref-k refinements. */
+orc_problem *orc_create(const orc_config *cfg, int n_levels);
+void orc_destroy(orc_problem *p);
+
+/* info[0..5] = ncells, nloc, ndof, nactive, nnz, nverts_per_cell */
+int orc_level_info(const orc_problem *p, int level, int *info);
+int orc_get_mesh(const orc_problem *p, int level, double *verts);
+int orc_get_gdof(const orc_problem *p, int level, int *gdof);
+int orc_get_structure(const orc_problem *p, int level, int *row_ptr, int *col);
+int orc_get_matrix(const orc_problem *p, int level, double *val);
+int orc_get_rhs(const orc_problem *p, int level, double *rhs);
+int orc_get_solution(const orc_problem *p, double *sol);
+int orc_set_solution(orc_problem *p, const double *sol);
+
+/* ConvectionDiffusion<d>::assemble over all levels */
+int orc_assemble(orc_problem *p);
+/* local matrix and rhs of one cell of one level (before scatter) */
+int orc_local_system(orc_problem *p, int level, int cell, double *A, double *f);
+/* y = A x on active rows, identity on non-active rows (BlockFEMatrix::apply) */
+int orc_apply(const orc_problem *p, int level, const double *x, double *y);
+/* GridTransfer::Prolongate / DefectRestriction between level+1 (coarse) and
+ * level (fine) */
+int orc_prolongate(const orc_problem *p, int fine_level, const double *xc,
+                   double *xf);
+int orc_restrict(const orc_problem *p, int fine_level, const double *df,
+                 double *rc);
+/* one multigrid cycle as the FGMRES preconditioner: z = MG(v) */
+int orc_mg_apply(orc_problem *p, const orc_solver_config *s, const double *v,
+                 double *z);
+/* Solver::solve on the finest level, starting from the current solution */
+int orc_solve(orc_problem *p, const orc_solver_config *s, int *iterations,
+              double *residual, double *initial_residual);
+/* errors[0..4] = L2, H1-semi, SD, DG(volume), L_inf */
+int orc_errors(const orc_problem *p, double *errors);
+const char *orc_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,372 @@
+"""GB300-native convection-diffusion hot path of ParMooN2022.
+
+Python face of ``libparmoon_cd.so`` (C-ABI in ``include/parmoon_cd.h``): the
+host setup hierarchy (TDomain / TFESpace / TStructure of refined unit
+squares and cubes), and the CD problem (``ConvectionDiffusion<d>``
+assemble / solve / errors) running on the GPU.  Every compute call goes to
+the CUDA library; there is no CPU fallback: without the built library or a
+CUDA device the calls raise.
+
+Parameter names follow the reference's ParameterDatabase keys
+(src/Solver/Solver.C:26-209, src/Multigrid/Multigrid.C:417-509,
+src/AssembleRoutines/LocalAssembling.C:564-581).
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libparmoon_cd.so")
+
+CDG_OK = 0
+ERRORS = {
+    -1: "CDG_ERR_ARG", -2: "CDG_ERR_CUDA", -3: "CDG_ERR_OOM", -4: "CDG_ERR_DIVERGED",
+    -5: "CDG_ERR_BREAKDOWN", -6: "CDG_ERR_ZERO_DIAG", -7: "CDG_ERR_PATTERN",
+    -8: "CDG_ERR_SINGULAR", -9: "CDG_ERR_NO_DEVICE", -10: "CDG_ERR_LIMIT",
+}
+EX_SINE_LAPLACE, EX_SINE, EX_POLYEXP, EX_CONST_F, EX_POLY1 = range(5)
+
+# every symbol include/parmoon_cd.h declares
+EXPORTED = [
+    "cdg_last_error", "cdg_version", "cdg_context_create", "cdg_context_destroy",
+    "cdg_context_synchronize", "cdg_context_launch_count", "cdg_hierarchy_create",
+    "cdg_hierarchy_destroy", "cdg_hierarchy_level_info", "cdg_hierarchy_get_mesh",
+    "cdg_hierarchy_get_dofs", "cdg_hierarchy_get_pattern", "cdg_problem_create",
+    "cdg_problem_create_from_arrays", "cdg_problem_destroy", "cdg_problem_assemble",
+    "cdg_problem_solve", "cdg_problem_assemble_solve", "cdg_problem_errors",
+    "cdg_problem_level_info", "cdg_problem_get_matrix", "cdg_problem_get_rhs",
+    "cdg_problem_get_solution", "cdg_problem_set_solution", "cdg_problem_get_slots",
+    "cdg_problem_apply", "cdg_problem_prolongate", "cdg_problem_restrict",
+    "cdg_problem_precondition",
+]
+
+
+class CdgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (%d): %s" % (ERRORS.get(code, "CDG_ERR"), code, msg))
+        self.code = code
+
+
+class AssemblyParams(ctypes.Structure):
+    _fields_ = [
+        ("example", ctypes.c_int), ("eps", ctypes.c_double), ("b", ctypes.c_double * 3),
+        ("c", ctypes.c_double), ("freq", ctypes.c_double), ("supg", ctypes.c_int),
+        ("sdfem_type", ctypes.c_int), ("delta0", ctypes.c_double), ("delta1", ctypes.c_double),
+        ("cell_measure", ctypes.c_int), ("problem_linear", ctypes.c_int),
+        ("neumann_mask", ctypes.c_int), ("poly_degree", ctypes.c_int),
+    ]
+
+
+class SolverParams(ctypes.Structure):
+    _fields_ = [
+        ("preconditioner", ctypes.c_int), ("max_n_iterations", ctypes.c_int),
+        ("min_n_iterations", ctypes.c_int), ("gmres_restart", ctypes.c_int),
+        ("residual_tolerance", ctypes.c_double), ("residual_reduction", ctypes.c_double),
+        ("divergence_factor", ctypes.c_double), ("multigrid_n_levels", ctypes.c_int),
+        ("multigrid_cycle_type", ctypes.c_int), ("multigrid_n_pre_smooth", ctypes.c_int),
+        ("multigrid_n_post_smooth", ctypes.c_int), ("jacobi_damp", ctypes.c_double),
+        ("multigrid_correction_damp_factor", ctypes.c_double),
+        ("multigrid_smoother_coarse", ctypes.c_int), ("multigrid_coarse_residual", ctypes.c_double),
+        ("multigrid_coarse_max_n_iterations", ctypes.c_int), ("precision", ctypes.c_int),
+    ]
+
+
+class SolveStats(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int), ("residual", ctypes.c_double),
+                ("initial_residual", ctypes.c_double), ("seconds", ctypes.c_double)]
+
+
+_lib = None
+
+
+def lib():
+    """Load libparmoon_cd.so; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libparmoon_cd.so is not built (run parmoon2022_gb300/build.py)")
+        L = ctypes.CDLL(LIB_PATH)
+        P, dp, ip = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)
+        PP = ctypes.POINTER(ctypes.c_void_p)
+        L.cdg_last_error.restype = ctypes.c_char_p
+        L.cdg_context_launch_count.restype = ctypes.c_longlong
+        L.cdg_context_launch_count.argtypes = [P]
+        sig = {
+            "cdg_version": [], "cdg_context_create": [ctypes.c_int, PP],
+            "cdg_context_destroy": [P], "cdg_context_synchronize": [P],
+            "cdg_hierarchy_create": [ctypes.c_int] * 6 + [PP], "cdg_hierarchy_destroy": [P],
+            "cdg_hierarchy_level_info": [P, ctypes.c_int, ip],
+            "cdg_hierarchy_get_mesh": [P, ctypes.c_int, dp],
+            "cdg_hierarchy_get_dofs": [P, ctypes.c_int, ip],
+            "cdg_hierarchy_get_pattern": [P, ctypes.c_int, ip, ip],
+            "cdg_problem_create": [P, P, PP],
+            "cdg_problem_create_from_arrays": [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ip,
+                                               PP, PP, ip, ip, PP, PP, PP, PP],
+            "cdg_problem_destroy": [P],
+            "cdg_problem_assemble": [P, ctypes.POINTER(AssemblyParams)],
+            "cdg_problem_solve": [P, ctypes.POINTER(SolverParams), ctypes.POINTER(SolveStats)],
+            "cdg_problem_assemble_solve": [P, ctypes.POINTER(AssemblyParams),
+                                           ctypes.POINTER(SolverParams), dp, dp, dp,
+                                           ctypes.POINTER(SolveStats)],
+            "cdg_problem_errors": [P, ctypes.POINTER(AssemblyParams), dp],
+            "cdg_problem_level_info": [P, ctypes.c_int, ip],
+            "cdg_problem_get_matrix": [P, ctypes.c_int, dp],
+            "cdg_problem_get_rhs": [P, ctypes.c_int, dp],
+            "cdg_problem_get_solution": [P, dp], "cdg_problem_set_solution": [P, dp],
+            "cdg_problem_get_slots": [P, ctypes.c_int, ip],
+            "cdg_problem_apply": [P, ctypes.c_int, dp, dp],
+            "cdg_problem_prolongate": [P, ctypes.c_int, dp, dp],
+            "cdg_problem_restrict": [P, ctypes.c_int, dp, dp],
+            "cdg_problem_precondition": [P, ctypes.POINTER(SolverParams), dp, dp],
+        }
+        for name, args in sig.items():
+            f = getattr(L, name)
+            f.restype = ctypes.c_int
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _chk(rc):
+    if rc != CDG_OK:
+        raise CdgError(rc, lib().cdg_last_error().decode())
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+
+
+def assembly_params(example=EX_SINE, eps=1.0, b=(0.0, 0.0, 0.0), c=0.0, freq=1.0,
+                    space_discretization_type="galerkin", sdfem_type=2, delta0=1.0, delta1=1.0,
+                    cell_measure=0, problem_linear=0, neumann_mask=0, poly_degree=0):
+    a = AssemblyParams()
+    a.example, a.eps = example, eps
+    for i in range(3):
+        a.b[i] = b[i] if i < len(b) else 0.0
+    a.c, a.freq = c, freq
+    a.supg = 1 if space_discretization_type == "supg" else 0
+    a.sdfem_type, a.delta0, a.delta1 = sdfem_type, delta0, delta1
+    a.cell_measure, a.problem_linear = cell_measure, problem_linear
+    a.neumann_mask, a.poly_degree = neumann_mask, poly_degree
+    return a
+
+
+def solver_params(preconditioner="jacobi", max_n_iterations=100, min_n_iterations=0,
+                  gmres_restart=20, residual_tolerance=1e-8, residual_reduction=0.0,
+                  divergence_factor=1e10, multigrid_n_levels=2, multigrid_cycle_type="V",
+                  multigrid_n_pre_smooth=1, multigrid_n_post_smooth=1, jacobi_damp=1.0,
+                  multigrid_correction_damp_factor=1.0, multigrid_smoother_coarse="direct_solve",
+                  multigrid_coarse_residual=0.1, multigrid_coarse_max_n_iterations=10,
+                  precision="fp64"):
+    """Defaults are the reference's database defaults."""
+    s = SolverParams()
+    s.preconditioner = {"no_preconditioner": 0, "jacobi": 1, "multigrid": 2}[preconditioner]
+    s.max_n_iterations, s.min_n_iterations = max_n_iterations, min_n_iterations
+    s.gmres_restart = gmres_restart
+    s.residual_tolerance, s.residual_reduction = residual_tolerance, residual_reduction
+    s.divergence_factor = divergence_factor
+    s.multigrid_n_levels = multigrid_n_levels
+    s.multigrid_cycle_type = {"V": 0, "W": 1, "F": 2}[multigrid_cycle_type]
+    s.multigrid_n_pre_smooth, s.multigrid_n_post_smooth = multigrid_n_pre_smooth, multigrid_n_post_smooth
+    s.jacobi_damp = jacobi_damp
+    s.multigrid_correction_damp_factor = multigrid_correction_damp_factor
+    s.multigrid_smoother_coarse = {"direct_solve": 0, "jacobi": 1}[multigrid_smoother_coarse]
+    s.multigrid_coarse_residual = multigrid_coarse_residual
+    s.multigrid_coarse_max_n_iterations = multigrid_coarse_max_n_iterations
+    s.precision = {"fp64": 0, "mixed": 1}[precision]
+    return s
+
+
+class Hierarchy:
+    """Host setup: unit square/cube (roots^dim cells) refined nref times, the
+    Q_order space and CSR pattern of each of n_levels levels (0 = finest)."""
+
+    def __init__(self, dim, order, nref, n_levels=1, roots=1, neumann_mask=0):
+        self.dim, self.order, self.nref, self.n_levels = dim, order, nref, n_levels
+        h = ctypes.c_void_p()
+        _chk(lib().cdg_hierarchy_create(dim, order, roots, nref, n_levels, neumann_mask,
+                                        ctypes.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().cdg_hierarchy_destroy(self.h)
+            self.h = None
+
+    def info(self, level=0):
+        a = np.zeros(6, dtype=np.int32)
+        _chk(lib().cdg_hierarchy_level_info(self.h, level, _ip(a)))
+        return dict(ncells=int(a[0]), nloc=int(a[1]), ndof=int(a[2]), nactive=int(a[3]),
+                    nnz=int(a[4]), nv=int(a[5]))
+
+    def mesh(self, level=0):
+        i = self.info(level)
+        v = np.zeros((i["ncells"], i["nv"], self.dim))
+        _chk(lib().cdg_hierarchy_get_mesh(self.h, level, _dp(v)))
+        return v
+
+    def dofs(self, level=0):
+        i = self.info(level)
+        g = np.zeros((i["ncells"], i["nloc"]), dtype=np.int32)
+        _chk(lib().cdg_hierarchy_get_dofs(self.h, level, _ip(g)))
+        return g
+
+    def pattern(self, level=0):
+        i = self.info(level)
+        rp = np.zeros(i["ndof"] + 1, dtype=np.int32)
+        col = np.zeros(i["nnz"], dtype=np.int32)
+        _chk(lib().cdg_hierarchy_get_pattern(self.h, level, _ip(rp), _ip(col)))
+        return rp, col
+
+
+class Context:
+    """One CUDA device and stream."""
+
+    def __init__(self, device=0):
+        c = ctypes.c_void_p()
+        _chk(lib().cdg_context_create(device, ctypes.byref(c)))
+        self.c = c
+
+    def synchronize(self):
+        _chk(lib().cdg_context_synchronize(self.c))
+
+    def launches(self):
+        return int(lib().cdg_context_launch_count(self.c))
+
+    def close(self):
+        if getattr(self, "c", None):
+            lib().cdg_context_destroy(self.c)
+            self.c = None
+
+    def __del__(self):
+        self.close()
+
+
+class ConvectionDiffusion:
+    """ConvectionDiffusion<d> on the GPU: one hierarchy's levels resident in HBM."""
+
+    def __init__(self, ctx, hierarchy):
+        self.ctx, self.hier = ctx, hierarchy
+        p = ctypes.c_void_p()
+        _chk(lib().cdg_problem_create(ctx.c, hierarchy.h, ctypes.byref(p)))
+        self.p = p
+        self.n_levels = hierarchy.n_levels
+
+    @classmethod
+    def from_arrays(cls, ctx, dim, order, levels):
+        """levels: list (finest first) of dicts with verts (ncells,nv,dim),
+        dofs (ncells,nloc), ndof, nactive, row_ptr, col, optional parent."""
+        self = cls.__new__(cls)
+        self.ctx, self.hier, self.n_levels = ctx, None, len(levels)
+        n = len(levels)
+        keep = []
+
+        def arr(dtype, key):
+            out = (ctypes.c_void_p * n)()
+            for i, l in enumerate(levels):
+                if key in l and l[key] is not None:
+                    a = np.ascontiguousarray(l[key], dtype=dtype)
+                    keep.append(a)
+                    out[i] = a.ctypes.data
+            return out
+        ncells = np.array([len(l["dofs"]) for l in levels], dtype=np.int32)
+        ndof = np.array([l["ndof"] for l in levels], dtype=np.int32)
+        nact = np.array([l["nactive"] for l in levels], dtype=np.int32)
+        p = ctypes.c_void_p()
+        _chk(lib().cdg_problem_create_from_arrays(
+            ctx.c, dim, order, n, _ip(ncells), arr(np.float64, "verts"), arr(np.int32, "dofs"),
+            _ip(ndof), _ip(nact), arr(np.int32, "row_ptr"), arr(np.int32, "col"),
+            arr(np.int32, "parent"), ctypes.byref(p)))
+        self.p = p
+        return self
+
+    def close(self):
+        if getattr(self, "p", None):
+            lib().cdg_problem_destroy(self.p)
+            self.p = None
+
+    def __del__(self):
+        self.close()
+
+    def info(self, level=0):
+        a = np.zeros(6, dtype=np.int32)
+        _chk(lib().cdg_problem_level_info(self.p, level, _ip(a)))
+        return dict(ncells=int(a[0]), nloc=int(a[1]), ndof=int(a[2]), nactive=int(a[3]),
+                    nnz=int(a[4]), nv=int(a[5]))
+
+    def assemble(self, a):
+        _chk(lib().cdg_problem_assemble(self.p, ctypes.byref(a)))
+
+    def solve(self, s):
+        st = SolveStats()
+        _chk(lib().cdg_problem_solve(self.p, ctypes.byref(s), ctypes.byref(st)))
+        return st
+
+    def assemble_solve(self, a, s, solution_in=None, rhs_out=None, solution_out=None):
+        st = SolveStats()
+        nul = ctypes.POINTER(ctypes.c_double)()
+        _chk(lib().cdg_problem_assemble_solve(
+            self.p, ctypes.byref(a), ctypes.byref(s),
+            _dp(solution_in) if solution_in is not None else nul,
+            _dp(rhs_out) if rhs_out is not None else nul,
+            _dp(solution_out) if solution_out is not None else nul, ctypes.byref(st)))
+        return st
+
+    def errors(self, a):
+        e = np.zeros(5)
+        _chk(lib().cdg_problem_errors(self.p, ctypes.byref(a), _dp(e)))
+        return e
+
+    def matrix(self, level=0):
+        v = np.zeros(self.info(level)["nnz"])
+        _chk(lib().cdg_problem_get_matrix(self.p, level, _dp(v)))
+        return v
+
+    def rhs(self, level=0):
+        v = np.zeros(self.info(level)["ndof"])
+        _chk(lib().cdg_problem_get_rhs(self.p, level, _dp(v)))
+        return v
+
+    def solution(self):
+        v = np.zeros(self.info(0)["ndof"])
+        _chk(lib().cdg_problem_get_solution(self.p, _dp(v)))
+        return v
+
+    def set_solution(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        _chk(lib().cdg_problem_set_solution(self.p, _dp(x)))
+
+    def slots(self, level=0):
+        i = self.info(level)
+        s = np.zeros((i["ncells"], i["nloc"] * i["nloc"]), dtype=np.int32)
+        _chk(lib().cdg_problem_get_slots(self.p, level, _ip(s)))
+        return s
+
+    def apply(self, x, level=0):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.zeros_like(x)
+        _chk(lib().cdg_problem_apply(self.p, level, _dp(x), _dp(y)))
+        return y
+
+    def prolongate(self, xc, fine_level=0):
+        xc = np.ascontiguousarray(xc, dtype=np.float64)
+        xf = np.zeros(self.info(fine_level)["ndof"])
+        _chk(lib().cdg_problem_prolongate(self.p, fine_level, _dp(xc), _dp(xf)))
+        return xf
+
+    def restrict(self, df, fine_level=0):
+        df = np.ascontiguousarray(df, dtype=np.float64)
+        rc = np.zeros(self.info(fine_level + 1)["ndof"])
+        _chk(lib().cdg_problem_restrict(self.p, fine_level, _dp(df), _dp(rc)))
+        return rc
+
+    def precondition(self, s, v):
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        z = np.zeros_like(v)
+        _chk(lib().cdg_problem_precondition(self.p, ctypes.byref(s), _dp(v), _dp(z)))
+        return z

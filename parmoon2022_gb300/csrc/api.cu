@@ -1,0 +1,530 @@
+// api.cu -- the extern "C" entry points of libparmoon_cd.so (declared in
+// include/parmoon_cd.h): context, host setup hierarchy, the CD problem
+// (ConvectionDiffusion<d> assemble / solve / output) and operator pieces.
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "common.cuh"
+
+namespace cdg {
+static thread_local char g_msg[512] = "";
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_msg, sizeof g_msg, fmt, ap);
+  va_end(ap);
+}
+}  // namespace cdg
+
+using namespace cdg;
+
+#define API_GUARD(expr)                                                        \
+  try {                                                                        \
+    return (expr);                                                             \
+  } catch (const std::bad_alloc&) {                                            \
+    set_error("host allocation failed");                                       \
+    return CDG_ERR_OOM;                                                        \
+  } catch (const std::exception& e) {                                          \
+    set_error("%s", e.what());                                                 \
+    return CDG_ERR_ARG;                                                        \
+  }
+
+extern "C" {
+
+const char* cdg_last_error(void) { return g_msg; }
+int cdg_version(void) { return 1; }
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+int cdg_context_create(int device, cdg_context** out) {
+  if (!out) { set_error("null output"); return CDG_ERR_ARG; }
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    set_error("no CUDA device");
+    return CDG_ERR_NO_DEVICE;
+  }
+  if (device < 0 || device >= ndev) { set_error("bad device %d", device); return CDG_ERR_ARG; }
+  CDG_CUDA(cudaSetDevice(device));
+  cdg_context* c = new cdg_context();
+  c->device = device;
+  CDG_CUDA(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device));
+  CDG_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  CDG_CUDA(cudaMalloc(&c->d_err, sizeof(int)));
+  CDG_CUDA(cudaMemset(c->d_err, 0, sizeof(int)));
+  CDG_CUDA(cudaMalloc(&c->d_red, (size_t)kRedSlots * kRedMaxBlocks * sizeof(double)));
+  CDG_CUDA(cudaMalloc(&c->d_cnt, kRedSlots * sizeof(unsigned)));
+  CDG_CUDA(cudaMemset(c->d_cnt, 0, kRedSlots * sizeof(unsigned)));
+  CDG_CUDA(cudaMallocHost(&c->h_pinned, 64 * sizeof(double)));
+  *out = c;
+  return CDG_OK;
+}
+
+int cdg_context_destroy(cdg_context* c) {
+  if (!c) return CDG_OK;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  cudaFree(c->d_err);
+  cudaFree(c->d_red);
+  cudaFree(c->d_cnt);
+  cudaFreeHost(c->h_pinned);
+  cudaStreamDestroy(c->stream);
+  delete c;
+  return CDG_OK;
+}
+
+int cdg_context_synchronize(cdg_context* c) {
+  if (!c) { set_error("null context"); return CDG_ERR_ARG; }
+  CDG_CUDA(cudaStreamSynchronize(c->stream));
+  return CDG_OK;
+}
+
+long long cdg_context_launch_count(const cdg_context* c) { return c ? c->launches : -1; }
+
+// ---------------------------------------------------------------------------
+// host setup hierarchy
+// ---------------------------------------------------------------------------
+static int hierarchy_create(int dim, int order, int roots, int nref, int n_levels, int nmask,
+                            cdg_hierarchy** out) {
+  if (!out || (dim != 2 && dim != 3) || (order != 1 && order != 2) || roots < 1 || nref < 0 ||
+      n_levels < 1 || n_levels > nref + 1) {
+    set_error("bad hierarchy arguments");
+    return CDG_ERR_ARG;
+  }
+  cdg_hierarchy* h = new cdg_hierarchy();
+  h->dim = dim;
+  h->order = order;
+  for (int l = 0; l < n_levels; ++l) {
+    h->mesh.push_back(make_refined_box(dim, roots, nref - l));
+    h->space.push_back(make_space(h->mesh.back(), order, nmask));
+    h->pattern.push_back(make_pattern(h->space.back()));
+  }
+  *out = h;
+  return CDG_OK;
+}
+
+int cdg_hierarchy_create(int dim, int order, int roots, int nref, int n_levels, int neumann_mask,
+                         cdg_hierarchy** out) {
+  API_GUARD(hierarchy_create(dim, order, roots, nref, n_levels, neumann_mask, out));
+}
+
+int cdg_hierarchy_destroy(cdg_hierarchy* h) {
+  delete h;
+  return CDG_OK;
+}
+
+int cdg_hierarchy_level_info(const cdg_hierarchy* h, int level, int* info) {
+  if (!h || level < 0 || level >= (int)h->mesh.size() || !info) { set_error("bad level"); return CDG_ERR_ARG; }
+  info[0] = h->mesh[level].ncells;
+  info[1] = h->space[level].nloc;
+  info[2] = h->space[level].ndof;
+  info[3] = h->space[level].nactive;
+  info[4] = (int)h->pattern[level].col.size();
+  info[5] = h->mesh[level].nv;
+  return CDG_OK;
+}
+
+int cdg_hierarchy_get_mesh(const cdg_hierarchy* h, int level, double* v) {
+  if (!h || level < 0 || level >= (int)h->mesh.size() || !v) { set_error("bad level"); return CDG_ERR_ARG; }
+  std::memcpy(v, h->mesh[level].verts.data(), h->mesh[level].verts.size() * sizeof(double));
+  return CDG_OK;
+}
+
+int cdg_hierarchy_get_dofs(const cdg_hierarchy* h, int level, int* g) {
+  if (!h || level < 0 || level >= (int)h->mesh.size() || !g) { set_error("bad level"); return CDG_ERR_ARG; }
+  std::memcpy(g, h->space[level].gdof.data(), h->space[level].gdof.size() * sizeof(int));
+  return CDG_OK;
+}
+
+int cdg_hierarchy_get_pattern(const cdg_hierarchy* h, int level, int* rp, int* col) {
+  if (!h || level < 0 || level >= (int)h->mesh.size() || !rp || !col) { set_error("bad level"); return CDG_ERR_ARG; }
+  const Pattern& P = h->pattern[level];
+  std::memcpy(rp, P.row_ptr.data(), P.row_ptr.size() * sizeof(int));
+  std::memcpy(col, P.col.data(), P.col.size() * sizeof(int));
+  return CDG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// problem
+// ---------------------------------------------------------------------------
+}  // extern "C"
+template <typename T>
+static int up(T** d, const std::vector<T>& h, cudaStream_t st) {
+  CDG_CUDA(cudaMalloc((void**)d, std::max<size_t>(h.size(), 1) * sizeof(T)));
+  if (!h.empty())
+    CDG_CUDA(cudaMemcpyAsync(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, st));
+  return CDG_OK;
+}
+extern "C" {
+
+static int finish_problem(cdg_context* ctx, cdg_problem* p, const std::vector<std::vector<int>>& parents) {
+  CDG_CUDA(cudaMalloc(&p->d_zero_diag, sizeof(int)));
+  CDG_CUDA(cudaMemsetAsync(p->d_zero_diag, 0, sizeof(int), ctx->stream));
+  for (auto& L : p->lev) CDG_TRY(upload_level(ctx, L));
+  for (size_t l = 0; l + 1 < p->lev.size(); ++l) {
+    DevLevel& F = p->lev[l];
+    DevLevel& C = p->lev[l + 1];
+    HostCsr P, R;
+    make_transfer(F.mesh, F.space, C.mesh, C.space, parents[l].data(), &P, &R);
+    std::vector<float> pv(P.val.begin(), P.val.end()), rv(R.val.begin(), R.val.end());
+    CDG_TRY(up(&F.P_rp, P.row_ptr, ctx->stream));
+    CDG_TRY(up(&F.P_col, P.col, ctx->stream));
+    CDG_TRY(up(&F.P_val, P.val, ctx->stream));
+    CDG_TRY(up(&F.P_val32, pv, ctx->stream));
+    CDG_TRY(up(&F.R_rp, R.row_ptr, ctx->stream));
+    CDG_TRY(up(&F.R_col, R.col, ctx->stream));
+    CDG_TRY(up(&F.R_val, R.val, ctx->stream));
+    CDG_TRY(up(&F.R_val32, rv, ctx->stream));
+    F.P_nnz = (int)P.col.size();
+    F.R_nnz = (int)R.col.size();
+  }
+  CDG_CUDA(cudaStreamSynchronize(ctx->stream));
+  return CDG_OK;
+}
+
+static void fill_level(DevLevel& L, int dim, int order) {
+  L.dim = dim;
+  L.order = order;
+  L.nv = dim == 2 ? 4 : 8;
+  L.nloc = dim == 2 ? (order + 1) * (order + 1) : (order + 1) * (order + 1) * (order + 1);
+  L.ncells = L.mesh.ncells;
+  L.ndof = L.space.ndof;
+  L.nactive = L.space.nactive;
+  L.nnz = (int)L.pattern.col.size();
+}
+
+static int problem_create(cdg_context* ctx, const cdg_hierarchy* h, cdg_problem** out) {
+  if (!ctx || !h || !out) { set_error("null argument"); return CDG_ERR_ARG; }
+  CDG_CUDA(cudaSetDevice(ctx->device));
+  cdg_problem* p = new cdg_problem();
+  p->ctx = ctx;
+  p->dim = h->dim;
+  p->order = h->order;
+  p->lev.resize(h->mesh.size());
+  std::vector<std::vector<int>> parents;
+  for (size_t l = 0; l < h->mesh.size(); ++l) {
+    DevLevel& L = p->lev[l];
+    L.mesh = h->mesh[l];
+    L.space = h->space[l];
+    L.pattern = h->pattern[l];
+    fill_level(L, h->dim, h->order);
+    if (l + 1 < h->mesh.size()) {
+      std::vector<int> par(L.ncells);
+      int nch = h->dim == 2 ? 4 : 8;
+      for (int f = 0; f < L.ncells; ++f) par[f] = f / nch;
+      parents.push_back(par);
+    }
+  }
+  int rc = finish_problem(ctx, p, parents);
+  if (rc != CDG_OK) {
+    cdg_problem_destroy(p);
+    return rc;
+  }
+  *out = p;
+  return CDG_OK;
+}
+
+int cdg_problem_create(cdg_context* ctx, const cdg_hierarchy* h, cdg_problem** out) {
+  API_GUARD(problem_create(ctx, h, out));
+}
+
+static int problem_from_arrays(cdg_context* ctx, int dim, int order, int nl, const int* n_cells,
+                               const double* const* verts, const int* const* gn,
+                               const int* n_dofs, const int* n_active, const int* const* rp,
+                               const int* const* col, const int* const* parent,
+                               cdg_problem** out) {
+  if (!ctx || !out || (dim != 2 && dim != 3) || (order != 1 && order != 2) || nl < 1 ||
+      !n_cells || !verts || !gn || !n_dofs || !n_active || !rp || !col) {
+    set_error("bad arguments");
+    return CDG_ERR_ARG;
+  }
+  CDG_CUDA(cudaSetDevice(ctx->device));
+  cdg_problem* p = new cdg_problem();
+  p->ctx = ctx;
+  p->dim = dim;
+  p->order = order;
+  p->lev.resize(nl);
+  int nv = dim == 2 ? 4 : 8;
+  int nloc = dim == 2 ? (order + 1) * (order + 1) : (order + 1) * (order + 1) * (order + 1);
+  std::vector<std::vector<int>> parents;
+  for (int l = 0; l < nl; ++l) {
+    DevLevel& L = p->lev[l];
+    if (n_cells[l] < 1 || n_dofs[l] < 1 || n_active[l] < 0 || n_active[l] > n_dofs[l]) {
+      delete p;
+      set_error("bad sizes on level %d", l);
+      return CDG_ERR_ARG;
+    }
+    L.mesh.dim = dim;
+    L.mesh.nv = nv;
+    L.mesh.ncells = n_cells[l];
+    L.mesh.verts.assign(verts[l], verts[l] + (size_t)n_cells[l] * nv * dim);
+    L.space.dim = dim;
+    L.space.order = order;
+    L.space.nloc = nloc;
+    L.space.ndof = n_dofs[l];
+    L.space.nactive = n_active[l];
+    L.space.gdof.assign(gn[l], gn[l] + (size_t)n_cells[l] * nloc);
+    for (int v : L.space.gdof)
+      if (v < 0 || v >= n_dofs[l]) {
+        delete p;
+        set_error("global number out of range on level %d", l);
+        return CDG_ERR_ARG;
+      }
+    L.pattern.nrows = n_dofs[l];
+    L.pattern.row_ptr.assign(rp[l], rp[l] + n_dofs[l] + 1);
+    int nnz = rp[l][n_dofs[l]];
+    L.pattern.col.assign(col[l], col[l] + nnz);
+    for (int v : L.pattern.col)
+      if (v < 0 || v >= n_dofs[l]) {
+        delete p;
+        set_error("column index out of range on level %d", l);
+        return CDG_ERR_ARG;
+      }
+    fill_level(L, dim, order);
+    if (l >= 1) {
+      std::vector<int> par(n_cells[l - 1]);
+      int nch = dim == 2 ? 4 : 8;
+      for (int f = 0; f < n_cells[l - 1]; ++f) {
+        par[f] = (parent && parent[l]) ? parent[l][f] : f / nch;
+        if (par[f] < 0 || par[f] >= n_cells[l]) {
+          delete p;
+          set_error("parent index out of range on level %d", l);
+          return CDG_ERR_ARG;
+        }
+      }
+      parents.push_back(par);
+    }
+  }
+  int rc = finish_problem(ctx, p, parents);
+  if (rc != CDG_OK) {
+    cdg_problem_destroy(p);
+    return rc;
+  }
+  *out = p;
+  return CDG_OK;
+}
+
+int cdg_problem_create_from_arrays(cdg_context* ctx, int dim, int order, int n_levels,
+                                   const int* n_cells, const double* const* cell_vertices,
+                                   const int* const* global_numbers, const int* n_dofs,
+                                   const int* n_active, const int* const* row_ptr,
+                                   const int* const* col, const int* const* parent,
+                                   cdg_problem** out) {
+  API_GUARD(problem_from_arrays(ctx, dim, order, n_levels, n_cells, cell_vertices,
+                                global_numbers, n_dofs, n_active, row_ptr, col, parent, out));
+}
+
+int cdg_problem_destroy(cdg_problem* p) {
+  if (!p) return CDG_OK;
+  cudaSetDevice(p->ctx->device);
+  cudaStreamSynchronize(p->ctx->stream);
+  for (auto& L : p->lev) free_level(L);
+  GmresState& g = p->gm;
+  double* ptrs[] = {g.V, g.Z, g.w, g.H, g.cs, g.sn, g.s, g.y, g.scal};
+  for (double* q : ptrs)
+    if (q) cudaFree(q);
+  if (p->d_tables) cudaFree(p->d_tables);
+  if (p->d_zero_diag) cudaFree(p->d_zero_diag);
+  delete p;
+  return CDG_OK;
+}
+
+static int check_assembly_params(const cdg_problem* p, const cdg_assembly_params* a) {
+  if (!p || !a) { set_error("null argument"); return CDG_ERR_ARG; }
+  if (a->example < 0 || a->example > CDG_EX_POLY1) { set_error("unknown example %d", a->example); return CDG_ERR_ARG; }
+  if (a->example == CDG_EX_POLYEXP && p->dim != 3) { set_error("example needs 3D"); return CDG_ERR_ARG; }
+  return CDG_OK;
+}
+
+static int assemble_all(cdg_problem* p, const cdg_assembly_params* a) {
+  CDG_CUDA(cudaMemsetAsync(p->d_zero_diag, 0, sizeof(int), p->ctx->stream));
+  for (auto& L : p->lev) CDG_TRY(assemble_level(p->ctx, p, L, *a));
+  return CDG_OK;
+}
+
+int cdg_problem_assemble(cdg_problem* p, const cdg_assembly_params* a) {
+  CDG_TRY(check_assembly_params(p, a));
+  CDG_CUDA(cudaSetDevice(p->ctx->device));
+  CDG_TRY(assemble_all(p, a));
+  return check_device_error(p->ctx);
+}
+
+static int check_solver_params(const cdg_problem* p, const cdg_solver_params* s) {
+  if (!p || !s) { set_error("null argument"); return CDG_ERR_ARG; }
+  if (s->preconditioner < 0 || s->preconditioner > 2) { set_error("unknown preconditioner"); return CDG_ERR_ARG; }
+  if (s->gmres_restart < 1 || s->gmres_restart > 120) { set_error("gmres_restart out of range [1,120]"); return CDG_ERR_ARG; }
+  if (s->precision != 0 && s->precision != 1) { set_error("precision must be 0 or 1"); return CDG_ERR_ARG; }
+  return CDG_OK;
+}
+
+int cdg_problem_solve(cdg_problem* p, const cdg_solver_params* s, cdg_solve_stats* st) {
+  CDG_TRY(check_solver_params(p, s));
+  CDG_CUDA(cudaSetDevice(p->ctx->device));
+  auto t0 = std::chrono::steady_clock::now();
+  cdg_solve_stats local{};
+  CDG_TRY(prepare_solver(p->ctx, p, *s));
+  int rc = fgmres(p->ctx, p, *s, &local);
+  CDG_CUDA(cudaStreamSynchronize(p->ctx->stream));
+  local.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (st) *st = local;
+  return rc;
+}
+
+int cdg_problem_assemble_solve(cdg_problem* p, const cdg_assembly_params* a,
+                               const cdg_solver_params* s, const double* solution_in,
+                               double* rhs_out, double* solution_out, cdg_solve_stats* st) {
+  CDG_TRY(check_assembly_params(p, a));
+  CDG_TRY(check_solver_params(p, s));
+  CDG_CUDA(cudaSetDevice(p->ctx->device));
+  auto t0 = std::chrono::steady_clock::now();
+  DevLevel& F = p->lev[0];
+  cudaStream_t stm = p->ctx->stream;
+  if (solution_in)
+    CDG_CUDA(cudaMemcpyAsync(F.sol, solution_in, (size_t)F.ndof * sizeof(double),
+                             cudaMemcpyHostToDevice, stm));
+  CDG_TRY(assemble_all(p, a));
+  cdg_solve_stats local{};
+  CDG_TRY(prepare_solver(p->ctx, p, *s));
+  int rc = fgmres(p->ctx, p, *s, &local);
+  if (rhs_out)
+    CDG_CUDA(cudaMemcpyAsync(rhs_out, F.rhs, (size_t)F.ndof * sizeof(double),
+                             cudaMemcpyDeviceToHost, stm));
+  if (solution_out)
+    CDG_CUDA(cudaMemcpyAsync(solution_out, F.sol, (size_t)F.ndof * sizeof(double),
+                             cudaMemcpyDeviceToHost, stm));
+  CDG_CUDA(cudaStreamSynchronize(stm));
+  local.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (st) *st = local;
+  return rc;
+}
+
+int cdg_problem_errors(cdg_problem* p, const cdg_assembly_params* a, double* errors) {
+  CDG_TRY(check_assembly_params(p, a));
+  if (!errors) { set_error("null output"); return CDG_ERR_ARG; }
+  CDG_CUDA(cudaSetDevice(p->ctx->device));
+  return level_errors(p->ctx, p, p->lev[0], *a, errors);
+}
+
+// ---------------------------------------------------------------------------
+// data access
+// ---------------------------------------------------------------------------
+static DevLevel* get_level(cdg_problem* p, int level) {
+  if (!p || level < 0 || level >= (int)p->lev.size()) {
+    set_error("bad level %d", level);
+    return nullptr;
+  }
+  cudaSetDevice(p->ctx->device);
+  return &p->lev[level];
+}
+
+int cdg_problem_level_info(const cdg_problem* p, int level, int* info) {
+  if (!p || level < 0 || level >= (int)p->lev.size() || !info) { set_error("bad level"); return CDG_ERR_ARG; }
+  const DevLevel& L = p->lev[level];
+  info[0] = L.ncells; info[1] = L.nloc; info[2] = L.ndof;
+  info[3] = L.nactive; info[4] = L.nnz; info[5] = L.nv;
+  return CDG_OK;
+}
+
+static int d2h(cdg_context* ctx, void* h, const void* d, size_t bytes) {
+  CDG_CUDA(cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  CDG_CUDA(cudaStreamSynchronize(ctx->stream));
+  return CDG_OK;
+}
+
+int cdg_problem_get_matrix(cdg_problem* p, int level, double* v) {
+  DevLevel* L = get_level(p, level);
+  if (!L || !v) return CDG_ERR_ARG;
+  return d2h(p->ctx, v, L->val64, (size_t)L->nnz * sizeof(double));
+}
+int cdg_problem_get_rhs(cdg_problem* p, int level, double* v) {
+  DevLevel* L = get_level(p, level);
+  if (!L || !v) return CDG_ERR_ARG;
+  return d2h(p->ctx, v, L->rhs, (size_t)L->ndof * sizeof(double));
+}
+int cdg_problem_get_solution(cdg_problem* p, double* v) {
+  DevLevel* L = get_level(p, 0);
+  if (!L || !v) return CDG_ERR_ARG;
+  return d2h(p->ctx, v, L->sol, (size_t)L->ndof * sizeof(double));
+}
+int cdg_problem_set_solution(cdg_problem* p, const double* v) {
+  DevLevel* L = get_level(p, 0);
+  if (!L || !v) return CDG_ERR_ARG;
+  CDG_CUDA(cudaMemcpyAsync(L->sol, v, (size_t)L->ndof * sizeof(double), cudaMemcpyHostToDevice,
+                           p->ctx->stream));
+  CDG_CUDA(cudaStreamSynchronize(p->ctx->stream));
+  return CDG_OK;
+}
+int cdg_problem_get_slots(cdg_problem* p, int level, int* slots) {
+  DevLevel* L = get_level(p, level);
+  if (!L || !slots) return CDG_ERR_ARG;
+  return d2h(p->ctx, slots, L->slot, (size_t)L->ncells * L->nloc * L->nloc * sizeof(int));
+}
+
+// ---------------------------------------------------------------------------
+// operator pieces with host buffers
+// ---------------------------------------------------------------------------
+struct DevBuf {
+  double* d = nullptr;
+  ~DevBuf() { if (d) cudaFree(d); }
+};
+
+static int h2d_tmp(DevBuf& b, const double* h, size_t n, cudaStream_t st) {
+  CDG_CUDA(cudaMalloc(&b.d, std::max<size_t>(n, 1) * sizeof(double)));
+  if (h) CDG_CUDA(cudaMemcpyAsync(b.d, h, n * sizeof(double), cudaMemcpyHostToDevice, st));
+  return CDG_OK;
+}
+
+int cdg_problem_apply(cdg_problem* p, int level, const double* x, double* y) {
+  DevLevel* L = get_level(p, level);
+  if (!L || !x || !y) return CDG_ERR_ARG;
+  DevBuf dx, dy;
+  CDG_TRY(h2d_tmp(dx, x, L->ndof, p->ctx->stream));
+  CDG_TRY(h2d_tmp(dy, nullptr, L->ndof, p->ctx->stream));
+  CDG_TRY(spmv_apply64(p->ctx, *L, dx.d, dy.d));
+  return d2h(p->ctx, y, dy.d, (size_t)L->ndof * sizeof(double));
+}
+
+int cdg_problem_prolongate(cdg_problem* p, int fine, const double* xc, double* xf) {
+  DevLevel* F = get_level(p, fine);
+  DevLevel* C = get_level(p, fine + 1);
+  if (!F || !C || !xc || !xf) return CDG_ERR_ARG;
+  DevBuf dc, df;
+  CDG_TRY(h2d_tmp(dc, xc, C->ndof, p->ctx->stream));
+  CDG_TRY(h2d_tmp(df, nullptr, F->ndof, p->ctx->stream));
+  CDG_TRY(prolongate64(p->ctx, *F, dc.d, df.d, 0, 0.0));
+  return d2h(p->ctx, xf, df.d, (size_t)F->ndof * sizeof(double));
+}
+
+int cdg_problem_restrict(cdg_problem* p, int fine, const double* dfine, double* rc) {
+  DevLevel* F = get_level(p, fine);
+  DevLevel* C = get_level(p, fine + 1);
+  if (!F || !C || !dfine || !rc) return CDG_ERR_ARG;
+  DevBuf df, dc;
+  CDG_TRY(h2d_tmp(df, dfine, F->ndof, p->ctx->stream));
+  CDG_TRY(h2d_tmp(dc, nullptr, C->ndof, p->ctx->stream));
+  CDG_TRY(restrict64(p->ctx, *F, *C, df.d, dc.d));
+  return d2h(p->ctx, rc, dc.d, (size_t)C->ndof * sizeof(double));
+}
+
+int cdg_problem_precondition(cdg_problem* p, const cdg_solver_params* s, const double* v,
+                             double* z) {
+  CDG_TRY(check_solver_params(p, s));
+  if (!v || !z) { set_error("null buffer"); return CDG_ERR_ARG; }
+  CDG_CUDA(cudaSetDevice(p->ctx->device));
+  CDG_TRY(prepare_solver(p->ctx, p, *s));
+  DevLevel& F = p->lev[0];
+  DevBuf dv, dz;
+  CDG_TRY(h2d_tmp(dv, v, F.ndof, p->ctx->stream));
+  CDG_TRY(h2d_tmp(dz, nullptr, F.ndof, p->ctx->stream));
+  CDG_TRY(precondition(p->ctx, p, *s, dv.d, dz.d));
+  CDG_TRY(d2h(p->ctx, z, dz.d, (size_t)F.ndof * sizeof(double)));
+  return check_device_error(p->ctx);
+}
+
+}  // extern "C"

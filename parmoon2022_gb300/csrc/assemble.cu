@@ -1,0 +1,840 @@
+// assemble.cu -- GB300 kernels of the CD assembly: cell geometry, element
+// matrices by contraction with reference tensors, CSR scatter through a
+// precomputed coupling->slot map, right-hand side with the example's source
+// term, Dirichlet rows and data, error norms.
+//
+// Reference path (ParMooN2022): ConvectionDiffusion<d>::call_assembling_
+// routine (src/System/ConvectionDiffusion.C:410-452) -> Assemble2D/3D cell
+// loop (src/AssembleRoutines/Assemble2D.C:2798-3481, Assemble3D.C:39-917) ->
+// FEDatabase::GetOrig (src/FE/FEDatabase.C:1498-1719) -> LocalAssembling::
+// GetLocalForms (src/AssembleRoutines/LocalAssembling.C:734-970) ->
+// BilinearAssembleGalerkin<d> / BilinearAssemble_SD<d>
+// (src/AssembleRoutines/ConvDiff.C:1776-1999) -> scatter by row search
+// (Assemble3D.C:257-292, Matrix.C:180-255).
+//
+// On affine cells (QuadAffin / HexaAffin, the maps of every cell these
+// meshes produce) with cell-constant eps, b, c, the per-quadrature-point
+// local forms are bilinear in reference-element integrals.  The local matrix
+// is therefore A_ij = sum_t g_t(cell) R_t[i][j] with R_t exact reference
+// integrals (the reference's Gauss rules integrate these polynomials
+// exactly) and g_t a few FP64 geometric/coefficient factors per cell; the
+// quadrature sum of the reference becomes one FP64 contraction per entry.
+// The right-hand side keeps the reference's quadrature rule because f is
+// not polynomial.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+
+#include "common.cuh"
+
+namespace cdg {
+
+// ---------------------------------------------------------------------------
+// device-side problem data
+// ---------------------------------------------------------------------------
+struct AsmCoefs {
+  int dim, order, nloc, example, supg, sdfem_type, cell_measure, poly_degree,
+      neumann_mask, nqp, nqp1, n_sym;
+  double eps, b[3], c, freq, delta0, delta1;
+};
+
+static AsmCoefs make_coefs(const cdg_assembly_params& a, int dim, int order, int nloc) {
+  AsmCoefs k;
+  k.dim = dim;
+  k.order = order;
+  k.nloc = nloc;
+  k.example = a.example;
+  k.supg = a.supg;
+  k.sdfem_type = a.sdfem_type;
+  k.cell_measure = a.cell_measure;
+  k.poly_degree = a.poly_degree > 0 ? a.poly_degree : order;
+  k.neumann_mask = a.neumann_mask;
+  k.eps = a.eps;
+  for (int i = 0; i < 3; ++i) k.b[i] = (i < dim) ? a.b[i] : 0.0;
+  k.c = a.c;
+  k.freq = a.freq;
+  k.delta0 = a.delta0;
+  k.delta1 = a.delta1;
+  int nterms = a.problem_linear ? 2 : 3;
+  k.nqp1 = gauss_points_for_degree(nterms * order);
+  k.nqp = dim == 2 ? k.nqp1 * k.nqp1 : k.nqp1 * k.nqp1 * k.nqp1;
+  k.n_sym = dim == 2 ? 3 : 6;
+  return k;
+}
+
+// exact solution of the example: u[0] value, u[1..dim] gradient, u[dim+1]
+// Laplacian (examples with a known solution; CONST_F returns zeros)
+__device__ void ex_exact(const AsmCoefs& k, const double* x, double* u) {
+  int d = k.dim;
+  for (int i = 0; i < 5; ++i) u[i] = 0.0;
+  if (k.example == CDG_EX_SINE_LAPLACE || k.example == CDG_EX_SINE) {
+    double w = (k.example == CDG_EX_SINE_LAPLACE ? 1.0 : k.freq) * M_PI;
+    double s0 = sin(w * x[0]), c0 = cos(w * x[0]);
+    double s1 = sin(w * x[1]), c1 = cos(w * x[1]);
+    if (d == 2) {
+      u[0] = s0 * s1;
+      u[1] = w * c0 * s1;
+      u[2] = w * s0 * c1;
+      u[3] = -2.0 * w * w * s0 * s1;
+    } else {
+      double s2 = sin(w * x[2]), c2 = cos(w * x[2]);
+      u[0] = s0 * s1 * s2;
+      u[1] = w * c0 * s1 * s2;
+      u[2] = w * s0 * c1 * s2;
+      u[3] = w * s0 * s1 * c2;
+      u[4] = -3.0 * w * w * s0 * s1 * s2;
+    }
+  } else if (k.example == CDG_EX_POLYEXP) {
+    double e = exp(x[0]);
+    double px = x[0] * (1 - x[0]) * e;
+    double px1 = e * (1 - x[0] - x[0] * x[0]);
+    double px2 = -e * x[0] * (3 + x[0]);
+    double qy = x[1] * (1 - x[1]), qz = x[2] * (1 - x[2]);
+    u[0] = px * qy * qz;
+    u[1] = px1 * qy * qz;
+    u[2] = px * (1 - 2 * x[1]) * qz;
+    u[3] = px * qy * (1 - 2 * x[2]);
+    u[4] = px2 * qy * qz - 2 * px * qz - 2 * px * qy;
+  } else if (k.example == CDG_EX_POLY1) {
+    u[0] = 1 + x[0] + 2 * x[1] + (d == 3 ? 3 * x[2] : 0.0);
+    u[1] = 1;
+    u[2] = 2;
+    if (d == 3) u[3] = 3;
+  }
+}
+
+// source term f = -eps lap u + b.grad u + c u (the examples' coefficient
+// callbacks, e.g. include/Examples/CD_2D/SineLaplace.h BilinearCoeffs)
+__device__ double ex_source(const AsmCoefs& k, const double* x) {
+  if (k.example == CDG_EX_CONST_F) return 1.0;
+  double u[5];
+  ex_exact(k, x, u);
+  int d = k.dim;
+  double f = -k.eps * u[d + 1];
+  for (int a = 0; a < d; ++a) f += k.b[a] * u[1 + a];
+  f += k.c * u[0];
+  return f;
+}
+
+// affine reference map from the cell vertices (QuadAffin.C:175-, HexaAffin.C:
+// 221-252): xi along v0->v1, eta along v0->v3, zeta along v0->v4
+struct Affine {
+  double x0[3], J[3][3], Ji[3][3], det;
+};
+
+__device__ void cell_affine(int dim, const double* __restrict__ cv, Affine& A) {
+  const int e[3] = {1, 3, 4};
+  for (int r = 0; r < dim; ++r)
+    for (int a = 0; a < dim; ++a) A.J[r][a] = (cv[e[a] * dim + r] - cv[r]) * 0.5;
+  for (int r = 0; r < dim; ++r) {
+    double s = cv[r];
+    for (int a = 0; a < dim; ++a) s += A.J[r][a];
+    A.x0[r] = s;
+  }
+  if (dim == 2) {
+    double det = A.J[0][0] * A.J[1][1] - A.J[0][1] * A.J[1][0];
+    A.det = det;
+    A.Ji[0][0] = A.J[1][1] / det;
+    A.Ji[0][1] = -A.J[0][1] / det;
+    A.Ji[1][0] = -A.J[1][0] / det;
+    A.Ji[1][1] = A.J[0][0] / det;
+  } else {
+    double det = A.J[0][0] * (A.J[1][1] * A.J[2][2] - A.J[1][2] * A.J[2][1]) -
+                 A.J[0][1] * (A.J[1][0] * A.J[2][2] - A.J[1][2] * A.J[2][0]) +
+                 A.J[0][2] * (A.J[1][0] * A.J[2][1] - A.J[1][1] * A.J[2][0]);
+    A.det = det;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        int j1 = (j + 1) % 3, j2 = (j + 2) % 3, i1 = (i + 1) % 3, i2 = (i + 2) % 3;
+        A.Ji[i][j] = (A.J[j1][i1] * A.J[j2][i2] - A.J[j1][i2] * A.J[j2][i1]) / det;
+      }
+  }
+}
+
+// cell measure hK (BaseCell.C:102-131; Rectangle.C:12-33; Hexahedron.C:70-121)
+__device__ double cell_hK(int dim, const double* __restrict__ cv, int measure, double det) {
+  auto d2 = [&](int i, int j) {
+    double s = 0;
+    for (int a = 0; a < dim; ++a) {
+      double t = cv[i * dim + a] - cv[j * dim + a];
+      s += t * t;
+    }
+    return s;
+  };
+  if (measure == 1 || measure == 3) return sqrt(fabs(det) * (dim == 2 ? 4.0 : 8.0));
+  if (dim == 2) {
+    if (measure == 2) {
+      double l1 = d2(0, 1), l2 = d2(1, 2);
+      return l1 < l2 ? sqrt(l1) : sqrt(l2);
+    }
+    return sqrt(d2(0, 2));
+  }
+  if (measure == 2) {
+    double m = d2(0, 4);
+    m = fmin(m, d2(0, 1));
+    m = fmin(m, d2(0, 3));
+    return sqrt(m);
+  }
+  double m = d2(0, 6);
+  m = fmax(m, d2(1, 7));
+  m = fmax(m, d2(2, 4));
+  m = fmax(m, d2(3, 5));
+  return sqrt(m);
+}
+
+// Compute_SDFEM_delta (ConvDiff.C:269-495), steady types
+__device__ double sdfem_delta(const AsmCoefs& k, double h, double eps, const double* b,
+                              double react, double linfb) {
+  double delta = 0, alpha;
+  if (fabs(eps) < 1e-20) eps = 1e-20;
+  double nb = b[0] * b[0] + b[1] * b[1];
+  if (k.dim == 3) nb += b[2] * b[2];
+  nb = sqrt(nb);
+  double reaction = fabs(react);
+  switch (k.sdfem_type) {
+    case 0:
+      delta = (eps < h * nb) ? k.delta0 * h / nb : k.delta1 * h * h / eps;
+      break;
+    case 1:
+    case 2: {
+      double nu = 1.0 / k.poly_degree;
+      if (nb > 0) {
+        alpha = nu * nb * h / (2 * eps);
+        delta = nu * h * (1 / tanh(alpha) - 1 / alpha) / (2 * nb);
+      } else {
+        delta = 0;
+      }
+      delta *= k.delta0;
+      break;
+    }
+    case 4:
+    case 5:
+    case 8:
+      delta = -1;
+      if (k.sdfem_type == 4) {
+        if (linfb > 0) delta = h / linfb;
+      } else if (nb > 0) {
+        delta = h / (2 * nb);
+      }
+      if (reaction > 0) {
+        alpha = 1.0 / reaction;
+        if (delta < 0 || alpha < delta) delta = alpha;
+      }
+      if (eps > 0) {
+        alpha = h * h / eps;
+        if (delta < 0 || alpha < delta) delta = alpha;
+      }
+      delta *= k.delta0;
+      if (delta < 0) delta = 0;
+      break;
+    case 7:
+      delta = k.delta0 * h * h / (4 * eps + 2 * h * nb + h * h * reaction);
+      break;
+    default:
+      delta = 0;
+  }
+  return delta;
+}
+
+__device__ double cell_delta(const AsmCoefs& k, const double* cv, const Affine& A) {
+  if (!k.supg) return 0.0;
+  double h = cell_hK(k.dim, cv, k.cell_measure, A.det);
+  double linfb = fmax(fabs(k.b[0]), fabs(k.b[1]));
+  if (k.dim == 3) linfb = fmax(linfb, fabs(k.b[2]));
+  return sdfem_delta(k, h, k.eps, k.b, k.c, linfb);
+}
+
+// per-cell factors g_t of the contraction (term layout of RefTensors)
+template <int DIM>
+__device__ void cell_factors(const AsmCoefs& k, const double* __restrict__ cv, double* g) {
+  constexpr int NS = DIM == 2 ? 3 : 6;
+  Affine A;
+  cell_affine(DIM, cv, A);
+  double adet = fabs(A.det);
+  double delta = cell_delta(k, cv, A);
+  double bp[3];  // beta' = J^-1 b
+  for (int a = 0; a < DIM; ++a) {
+    double s = 0;
+    for (int r = 0; r < DIM; ++r) s += A.Ji[a][r] * k.b[r];
+    bp[a] = s;
+  }
+  int s = 0;
+  double H[6];
+  for (int a = 0; a < DIM; ++a)
+    for (int bb = a; bb < DIM; ++bb) {
+      double h = 0;
+      for (int r = 0; r < DIM; ++r) h += A.Ji[a][r] * A.Ji[bb][r];
+      H[s] = h;
+      g[s] = adet * (k.eps * h + delta * bp[a] * bp[bb]);
+      ++s;
+    }
+  const int offC = NS, offM = NS + DIM, offD = NS + DIM + 1, offT = NS + 2 * DIM + 1;
+  for (int a = 0; a < DIM; ++a) g[offC + a] = adet * bp[a];
+  g[offM] = adet * k.c;
+  for (int a = 0; a < DIM; ++a) g[offD + a] = adet * delta * k.c * bp[a];
+  s = 0;
+  for (int a = 0; a < DIM; ++a)
+    for (int bb = a; bb < DIM; ++bb) {
+      double m = (a == bb) ? 1.0 : 2.0;
+      for (int c = 0; c < DIM; ++c)
+        g[offT + s * DIM + c] = -adet * delta * k.eps * m * H[s] * bp[c];
+      ++s;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// coupling -> CSR slot map (replaces the reference's linear row search)
+// ---------------------------------------------------------------------------
+__global__ void k_build_slots(int ncells, int nloc, const int* __restrict__ gdof,
+                              const int* __restrict__ row_ptr, const int* __restrict__ col,
+                              int* __restrict__ slot, int* err) {
+  long n = (long)ncells * nloc * nloc;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n;
+       t += (long)gridDim.x * blockDim.x) {
+    int cell = (int)(t / (nloc * nloc));
+    int ij = (int)(t % (nloc * nloc));
+    int row = gdof[cell * nloc + ij / nloc];
+    int c = gdof[cell * nloc + ij % nloc];
+    int lo = row_ptr[row], hi = row_ptr[row + 1] - 1, found = -1;
+    while (lo <= hi) {
+      int mid = (lo + hi) >> 1;
+      int v = col[mid];
+      if (v == c) { found = mid; break; }
+      if (v < c) lo = mid + 1; else hi = mid - 1;
+    }
+    slot[t] = found;
+    if (found < 0) atomicOr(err, kErrPattern);
+  }
+}
+
+__global__ void k_diag_slots(int n, const int* __restrict__ row_ptr, const int* __restrict__ col,
+                             int* __restrict__ dslot, int* err) {
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  int lo = row_ptr[r], hi = row_ptr[r + 1] - 1, found = -1;
+  while (lo <= hi) {
+    int mid = (lo + hi) >> 1;
+    int v = col[mid];
+    if (v == r) { found = mid; break; }
+    if (v < r) lo = mid + 1; else hi = mid - 1;
+  }
+  dslot[r] = found;
+  if (found < 0) atomicOr(err, kErrPattern);
+}
+
+// ---------------------------------------------------------------------------
+// element matrices: A_ij = sum_t g_t R_t[ij], scattered with FP64 atomics
+// ---------------------------------------------------------------------------
+// entries per block (EPB) and cell lanes per block: a block of EPB*LANES
+// threads holds EPB entries' reference-tensor columns in registers and
+// sweeps a tile of cells with LANES cells in flight
+template <int NLOC> struct ContractShape;
+template <> struct ContractShape<4> {   // Q1 quadrilateral
+  static constexpr int NE = 16, EPB = 16, LANES = 16;
+};
+template <> struct ContractShape<9> {   // Q2 quadrilateral
+  static constexpr int NE = 81, EPB = 81, LANES = 3;
+};
+template <> struct ContractShape<8> {   // Q1 hexahedron
+  static constexpr int NE = 64, EPB = 64, LANES = 4;
+};
+template <> struct ContractShape<27> {  // Q2 hexahedron
+  static constexpr int NE = 729, EPB = 243, LANES = 1;
+};
+template <int NLOC> struct ShapeInfo {
+  using S = ContractShape<NLOC>;
+  static constexpr int NEB = (S::NE + S::EPB - 1) / S::EPB;   // entry blocks
+  static constexpr int THREADS = S::EPB * S::LANES;
+};
+
+constexpr int kCellTile = 32;
+
+template <int DIM, int NLOC, int NT, bool SUPG>
+__global__ void __launch_bounds__(256)
+k_element_contract(AsmCoefs k, int ncells, int nactive, const double* __restrict__ verts,
+                   const int* __restrict__ gdof, const int* __restrict__ slot,
+                   const double* __restrict__ R, double* __restrict__ val) {
+  using S = ContractShape<NLOC>;
+  constexpr int NV = DIM == 2 ? 4 : 8;
+  constexpr int NS = DIM == 2 ? 3 : 6;
+  constexpr int NTG = NS + DIM + 1;           // Galerkin terms
+  constexpr int NTU = SUPG ? NT : NTG;        // terms used
+  __shared__ double g[kCellTile][NT];
+  const int tile0 = blockIdx.x * kCellTile;
+  // phase 1: per-cell factors
+  for (int c = threadIdx.x; c < kCellTile; c += blockDim.x) {
+    int cell = tile0 + c;
+    if (cell < ncells) cell_factors<DIM>(k, verts + (size_t)cell * NV * DIM, g[c]);
+  }
+  __syncthreads();
+  const int e_local = threadIdx.x % S::EPB;
+  const int lane = threadIdx.x / S::EPB;
+  const int e = blockIdx.y * S::EPB + e_local;
+  if (lane >= S::LANES || e >= S::NE) return;
+  double r[NTU];
+#pragma unroll
+  for (int t = 0; t < NTU; ++t) r[t] = __ldg(R + (size_t)t * S::NE + e);
+  const int i = e / NLOC;
+  for (int c = lane; c < kCellTile; c += S::LANES) {
+    int cell = tile0 + c;
+    if (cell >= ncells) break;
+    double acc = 0.0;
+#pragma unroll
+    for (int t = 0; t < NTU; ++t) acc = fma(g[c][t], r[t], acc);
+    int row = __ldg(gdof + (size_t)cell * NLOC + i);
+    if (row < nactive) atomicAdd(val + __ldg(slot + (size_t)cell * S::NE + e), acc);
+  }
+}
+
+// Dirichlet rows: diagonal 1 (Matrix.C:225-233); other entries stay zero
+__global__ void k_dirichlet_rows(int n, int nactive, const int* __restrict__ dslot,
+                                 double* __restrict__ val) {
+  int r = nactive + blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < n) val[dslot[r]] = 1.0;
+}
+
+// FP32 copy of the values and inverse diagonals (Iteration_jacobi.C:14-28)
+__global__ void k_finish_matrix(int n, int nnz, const int* __restrict__ dslot,
+                                const double* __restrict__ val, float* __restrict__ val32,
+                                double* __restrict__ invd, float* __restrict__ invd32,
+                                int* err) {
+  long stride = (long)gridDim.x * blockDim.x;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < nnz; t += stride)
+    val32[t] = (float)val[t];
+  for (long r = blockIdx.x * (long)blockDim.x + threadIdx.x; r < n; r += stride) {
+    double d = val[dslot[r]];
+    if (d == 0.0) {
+      atomicOr(err, kErrZeroDiag);
+      invd[r] = 0.0;
+      invd32[r] = 0.0f;
+    } else {
+      invd[r] = 1.0 / d;
+      invd32[r] = (float)(1.0 / d);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// right-hand side: one warp per cell
+// ---------------------------------------------------------------------------
+struct RhsTables {
+  const double* xi;    // nqp*3
+  const double* w;     // nqp
+  const double* val;   // nqp*nloc
+  const double* grad;  // nqp*dim*nloc
+};
+
+__device__ void ref_node(int dim, int p, int k, double* r) {
+  int n1 = p + 1;
+  int i[3] = {k % n1, (k / n1) % n1, k / (n1 * n1)};
+  for (int a = 0; a < 3; ++a) r[a] = (a < dim) ? -1.0 + (2.0 / p) * i[a] : 0.0;
+}
+
+__device__ void line_basis_d(int p, double t, double* v) {
+  if (p == 1) {
+    v[0] = 0.5 * (1 - t);
+    v[1] = 0.5 * (1 + t);
+  } else {
+    v[0] = 0.5 * t * (t - 1);
+    v[1] = (1 - t) * (1 + t);
+    v[2] = 0.5 * t * (t + 1);
+  }
+}
+
+__device__ int boundary_comp_d(int dim, const double* x) {
+  const double t = 1e-12;
+  if (dim == 2) {
+    if (fabs(x[1]) < t) return 0;
+    if (fabs(x[0] - 1) < t) return 1;
+    if (fabs(x[1] - 1) < t) return 2;
+    if (fabs(x[0]) < t) return 3;
+    return -1;
+  }
+  if (fabs(x[2]) < t) return 0;
+  if (fabs(x[1]) < t) return 1;
+  if (fabs(x[0] - 1) < t) return 2;
+  if (fabs(x[1] - 1) < t) return 3;
+  if (fabs(x[0]) < t) return 4;
+  if (fabs(x[2] - 1) < t) return 5;
+  return -1;
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(256)
+k_rhs(AsmCoefs k, int ncells, int nactive, const double* __restrict__ verts,
+      const int* __restrict__ gdof, RhsTables tb, double* __restrict__ rhs) {
+  constexpr int NV = DIM == 2 ? 4 : 8;
+  __shared__ double fw[8][128];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int cell = blockIdx.x * 8 + warp;
+  if (cell >= ncells) return;
+  const double* cv = verts + (size_t)cell * NV * DIM;
+  Affine A;
+  cell_affine(DIM, cv, A);
+  const double adet = fabs(A.det);
+  const double delta = cell_delta(k, cv, A);
+  double bp[3] = {0, 0, 0};
+  for (int a = 0; a < DIM; ++a)
+    for (int r = 0; r < DIM; ++r) bp[a] += A.Ji[a][r] * k.b[r];
+  for (int q = lane; q < k.nqp; q += 32) {
+    double x[3];
+    for (int r = 0; r < DIM; ++r) {
+      double s = A.x0[r];
+      for (int a = 0; a < DIM; ++a) s += A.J[r][a] * tb.xi[q * 3 + a];
+      x[r] = s;
+    }
+    fw[warp][q] = tb.w[q] * adet * ex_source(k, x);
+  }
+  __syncwarp();
+  const int nl = k.nloc;
+  if (lane < nl) {
+    double F = 0.0;
+    for (int q = 0; q < k.nqp; ++q) {
+      double v = tb.val[q * nl + lane];
+      // Galerkin: w f phi_i ; SUPG: w delta f (b.grad phi_i)
+      F += fw[warp][q] * v;
+    }
+    if (delta != 0.0) {
+      double Fs = 0.0;
+      for (int q = 0; q < k.nqp; ++q) {
+        double bg = 0.0;
+        for (int a = 0; a < DIM; ++a) bg += bp[a] * tb.grad[(q * DIM + a) * nl + lane];
+        Fs += fw[warp][q] * (delta * bg);
+      }
+      F += Fs;
+    }
+    int row = gdof[(size_t)cell * nl + lane];
+    if (row < nactive) {
+      atomicAdd(rhs + row, F);
+    } else {
+      // Dirichlet value: nodal functional of Q1/Q2 = value at the node
+      double r[3], x[3], u[5];
+      ref_node(DIM, k.order, lane, r);
+      for (int rr = 0; rr < DIM; ++rr) {
+        double s = A.x0[rr];
+        for (int a = 0; a < DIM; ++a) s += A.J[rr][a] * r[a];
+        x[rr] = s;
+      }
+      ex_exact(k, x, u);
+      rhs[row] = u[0];
+    }
+    // Neumann data on boundary edges (Assemble2D.C:3210-3248), 2D only
+    if (DIM == 2 && k.neumann_mask) {
+      const double nrm[4][2] = {{0, -1}, {1, 0}, {0, 1}, {-1, 0}};
+      for (int j = 0; j < 4; ++j) {
+        const double* a0 = cv + 2 * j;
+        const double* a1 = cv + 2 * ((j + 1) & 3);
+        double ctr[2] = {0.5 * (a0[0] + a1[0]), 0.5 * (a0[1] + a1[1])};
+        int comp = boundary_comp_d(2, ctr);
+        if (comp < 0 || !((k.neumann_mask >> comp) & 1)) continue;
+        if (row >= nactive) continue;
+        int np = k.order + 1;   // line rule of degree 2p
+        double lx[3], lw[3];
+        if (np == 2) {
+          lx[0] = -0.57735026918962576451; lx[1] = 0.57735026918962576451;
+          lw[0] = lw[1] = 1.0;
+        } else {
+          lx[0] = -0.77459666924148337704; lx[1] = 0.0; lx[2] = 0.77459666924148337704;
+          lw[0] = lw[2] = 5.0 / 9.0; lw[1] = 8.0 / 9.0;
+        }
+        double hE = 0.5 * sqrt((a1[0] - a0[0]) * (a1[0] - a0[0]) + (a1[1] - a0[1]) * (a1[1] - a0[1]));
+        double G = 0.0;
+        for (int l = 0; l < np; ++l) {
+          double s = 0.5 * (lx[l] + 1);
+          double x[2] = {a0[0] + s * (a1[0] - a0[0]), a0[1] + s * (a1[1] - a0[1])};
+          double u[5];
+          ex_exact(k, x, u);
+          double gval = k.eps * (nrm[comp][0] * u[1] + nrm[comp][1] * u[2]);
+          double xi[2];
+          for (int a = 0; a < 2; ++a)
+            xi[a] = A.Ji[a][0] * (x[0] - A.x0[0]) + A.Ji[a][1] * (x[1] - A.x0[1]);
+          double v0[3], v1[3];
+          line_basis_d(k.order, xi[0], v0);
+          line_basis_d(k.order, xi[1], v1);
+          int n1 = k.order + 1;
+          G += gval * hE * lw[l] * (v0[lane % n1] * v1[lane / n1]);
+        }
+        atomicAdd(rhs + row, G);
+      }
+    }
+  }
+}
+
+// solution.copy_nonactive(rhs)
+__global__ void k_copy_nonactive(int n, int nactive, const double* __restrict__ rhs,
+                                 double* __restrict__ sol) {
+  int i = nactive + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) sol[i] = rhs[i];
+}
+
+// ---------------------------------------------------------------------------
+// error norms (TFEFunction2D/3D::GetErrors + conv_diff_l2_h1_linf_error,
+// src/FE/FEFunction2D.C:291-470, src/AssembleRoutines/ConvDiff.C:2124-2183)
+// ---------------------------------------------------------------------------
+template <int DIM>
+__global__ void __launch_bounds__(256)
+k_errors(AsmCoefs k, int ncells, const double* __restrict__ verts, const int* __restrict__ gdof,
+         const double* __restrict__ sol, RhsTables tb, double* __restrict__ acc,
+         unsigned long long* __restrict__ linf) {
+  constexpr int NV = DIM == 2 ? 4 : 8;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int cell = blockIdx.x * 8 + warp;
+  if (cell >= ncells) return;
+  const double* cv = verts + (size_t)cell * NV * DIM;
+  Affine A;
+  cell_affine(DIM, cv, A);
+  const double adet = fabs(A.det);
+  const double hK = cell_hK(DIM, cv, k.cell_measure, A.det);
+  const int nl = k.nloc;
+  double fv = lane < nl ? sol[gdof[(size_t)cell * nl + lane]] : 0.0;
+  double e[4] = {0, 0, 0, 0}, emax = 0.0;
+  double linfb = fmax(fabs(k.b[0]), fabs(k.b[1]));
+  if (DIM == 3) linfb = fmax(linfb, fabs(k.b[2]));
+  double delta = sdfem_delta(k, hK, k.eps, k.b, k.c, linfb);
+  for (int q = 0; q < k.nqp; ++q) {
+    // u_h and its gradient at q: warp reduction over local dofs
+    double uh = lane < nl ? fv * tb.val[q * nl + lane] : 0.0;
+    double gr[3] = {0, 0, 0};
+    if (lane < nl)
+      for (int a = 0; a < DIM; ++a) gr[a] = fv * tb.grad[(q * DIM + a) * nl + lane];
+    for (int o = 16; o > 0; o >>= 1) {
+      uh += __shfl_xor_sync(0xffffffffu, uh, o);
+      for (int a = 0; a < DIM; ++a) gr[a] += __shfl_xor_sync(0xffffffffu, gr[a], o);
+    }
+    if (lane == 0) {
+      double g[3] = {0, 0, 0};
+      for (int r = 0; r < DIM; ++r)
+        for (int a = 0; a < DIM; ++a) g[r] += A.Ji[a][r] * gr[a];
+      double x[3], u[5];
+      for (int r = 0; r < DIM; ++r) {
+        double s = A.x0[r];
+        for (int a = 0; a < DIM; ++a) s += A.J[r][a] * tb.xi[q * 3 + a];
+        x[r] = s;
+      }
+      ex_exact(k, x, u);
+      double w = tb.w[q] * adet;
+      double e0 = uh - u[0];
+      emax = fmax(emax, fabs(e0));
+      double e1 = g[0] - u[1], e2 = g[1] - u[2], e3 = DIM == 2 ? 0.0 : g[2] - u[3];
+      e[0] += w * e0 * e0;
+      e[1] += w * (e1 * e1 + e2 * e2 + e3 * e3);
+      double e4 = k.b[0] * e1 + k.b[1] * e2 + (DIM == 3 ? k.b[2] * e3 : 0.0);
+      e[2] += w * (k.eps * (e1 * e1 + e2 * e2 + e3 * e3) + k.c * e0 * e0 + delta * e4 * e4);
+      e[3] += w * (k.eps * (e1 * e1 + e2 * e2 + e3 * e3) + (e4 + k.c * e0) * e0);
+    }
+  }
+  if (lane == 0) {
+    for (int i = 0; i < 4; ++i) atomicAdd(acc + i, e[i]);
+    atomicMax(linf, (unsigned long long)__double_as_longlong(emax));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+template <typename T>
+static int dalloc(T** p, size_t n) {
+  if (n == 0) n = 1;
+  CDG_CUDA(cudaMalloc((void**)p, n * sizeof(T)));
+  return CDG_OK;
+}
+
+int upload_level(cdg_context* ctx, DevLevel& L) {
+  cudaStream_t st = ctx->stream;
+  size_t nvd = (size_t)L.ncells * L.nv * L.dim;
+  size_t nsl = (size_t)L.ncells * L.nloc * L.nloc;
+  CDG_TRY(dalloc(&L.verts, nvd));
+  CDG_TRY(dalloc(&L.gdof, (size_t)L.ncells * L.nloc));
+  CDG_TRY(dalloc(&L.row_ptr, (size_t)L.ndof + 1));
+  CDG_TRY(dalloc(&L.col, (size_t)L.nnz));
+  CDG_TRY(dalloc(&L.slot, nsl));
+  CDG_TRY(dalloc(&L.diag_slot, (size_t)L.ndof));
+  CDG_TRY(dalloc(&L.val64, (size_t)L.nnz));
+  CDG_TRY(dalloc(&L.val32, (size_t)L.nnz));
+  CDG_TRY(dalloc(&L.rhs, (size_t)L.ndof));
+  CDG_TRY(dalloc(&L.sol, (size_t)L.ndof));
+  CDG_TRY(dalloc(&L.invdiag64, (size_t)L.ndof));
+  CDG_TRY(dalloc(&L.invdiag32, (size_t)L.ndof));
+  CDG_CUDA(cudaMemcpyAsync(L.verts, L.mesh.verts.data(), nvd * sizeof(double),
+                           cudaMemcpyHostToDevice, st));
+  CDG_CUDA(cudaMemcpyAsync(L.gdof, L.space.gdof.data(), L.space.gdof.size() * sizeof(int),
+                           cudaMemcpyHostToDevice, st));
+  CDG_CUDA(cudaMemcpyAsync(L.row_ptr, L.pattern.row_ptr.data(), (L.ndof + 1) * sizeof(int),
+                           cudaMemcpyHostToDevice, st));
+  CDG_CUDA(cudaMemcpyAsync(L.col, L.pattern.col.data(), (size_t)L.nnz * sizeof(int),
+                           cudaMemcpyHostToDevice, st));
+  CDG_CUDA(cudaMemsetAsync(L.sol, 0, (size_t)L.ndof * sizeof(double), st));
+  CDG_CUDA(cudaMemsetAsync(L.rhs, 0, (size_t)L.ndof * sizeof(double), st));
+  double avg = L.ndof ? (double)L.nnz / L.ndof : 1.0;
+  L.rows_per_warp_hint = avg > 48 ? 32 : avg > 20 ? 16 : avg > 10 ? 8 : 4;
+  return build_slots(ctx, L);
+}
+
+int free_level(DevLevel& L) {
+  void* ptrs[] = {L.verts, L.gdof, L.row_ptr, L.col, L.slot, L.diag_slot, L.val64, L.val32,
+                  L.rhs, L.sol, L.invdiag64, L.invdiag32, L.mg_rhs, L.mg_sol, L.mg_tmp,
+                  L.mg_def, L.P_rp, L.P_col, L.P_val, L.P_val32, L.R_rp, L.R_col, L.R_val,
+                  L.R_val32, L.coarse_inv, L.coarse_work};
+  for (void* q : ptrs)
+    if (q) cudaFree(q);
+  return CDG_OK;
+}
+
+int check_device_error(cdg_context* ctx) {
+  int h = 0;
+  CDG_CUDA(cudaMemcpyAsync(&h, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CDG_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (h) {
+    CDG_CUDA(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
+    if (h & kErrPattern) { set_error("local coupling not in the sparsity pattern"); return CDG_ERR_PATTERN; }
+    if (h & kErrZeroDiag) { set_error("zero entry on the diagonal (Jacobi)"); return CDG_ERR_ZERO_DIAG; }
+    if (h & kErrSingular) { set_error("singular coarse matrix"); return CDG_ERR_SINGULAR; }
+    if (h & kErrBreakdown) { set_error("Unhappy breakdown in flexible gmres"); return CDG_ERR_BREAKDOWN; }
+    set_error("device error word %d", h);
+    return CDG_ERR_CUDA;
+  }
+  return CDG_OK;
+}
+
+int build_slots(cdg_context* ctx, DevLevel& L) {
+  long n = (long)L.ncells * L.nloc * L.nloc;
+  int grid = (int)std::min<long>((n + 255) / 256, (long)ctx->num_sms * 32);
+  CDG_LAUNCH(ctx, k_build_slots, grid, 256, 0, L.ncells, L.nloc, L.gdof, L.row_ptr, L.col,
+             L.slot, ctx->d_err);
+  CDG_LAUNCH(ctx, k_diag_slots, grid_for<int>(L.ndof, 256), 256, 0, L.ndof, L.row_ptr, L.col,
+             L.diag_slot, ctx->d_err);
+  return check_device_error(ctx);
+}
+
+static int ensure_tables(cdg_context* ctx, cdg_problem* p) {
+  if (p->d_tables && p->rt_order == p->order) return CDG_OK;
+  RefTensors T = make_ref_tensors(p->dim, p->order);
+  if (p->d_tables) cudaFree(p->d_tables);
+  CDG_TRY(dalloc(&p->d_tables, T.R.size()));
+  CDG_CUDA(cudaMemcpyAsync(p->d_tables, T.R.data(), T.R.size() * sizeof(double),
+                           cudaMemcpyHostToDevice, ctx->stream));
+  CDG_CUDA(cudaStreamSynchronize(ctx->stream));
+  p->nterms = T.nterms;
+  p->rt_order = p->order;
+  return CDG_OK;
+}
+
+template <int DIM, int NLOC, int NT>
+static int launch_contract(cdg_context* ctx, const AsmCoefs& k, DevLevel& L, const double* R) {
+  using S = ShapeInfo<NLOC>;
+  dim3 grid((L.ncells + kCellTile - 1) / kCellTile, S::NEB);
+  if (k.supg)
+    CDG_LAUNCH(ctx, (k_element_contract<DIM, NLOC, NT, true>), grid, S::THREADS, 0, k, L.ncells,
+               L.nactive, L.verts, L.gdof, L.slot, R, L.val64);
+  else
+    CDG_LAUNCH(ctx, (k_element_contract<DIM, NLOC, NT, false>), grid, S::THREADS, 0, k,
+               L.ncells, L.nactive, L.verts, L.gdof, L.slot, R, L.val64);
+  return CDG_OK;
+}
+
+// reference tables for the rhs / error rules, cached per (dim, order, nqp1)
+struct DevRefTables {
+  int dim = 0, order = 0, nqp1 = 0;
+  double* buf = nullptr;
+  RhsTables t{};
+};
+static DevRefTables g_rt[8];
+
+static int get_rhs_tables(cdg_context* ctx, int dim, int order, int nqp1, RhsTables* out) {
+  int dev = ctx->device;
+  (void)dev;
+  for (auto& e : g_rt)
+    if (e.buf && e.dim == dim && e.order == order && e.nqp1 == nqp1) {
+      *out = e.t;
+      return CDG_OK;
+    }
+  RefTables T = make_ref_tables(dim, order, nqp1);
+  size_t n = T.xi.size() + T.w.size() + T.val.size() + T.grad.size();
+  DevRefTables* slot = nullptr;
+  for (auto& e : g_rt)
+    if (!e.buf) { slot = &e; break; }
+  if (!slot) slot = &g_rt[0];
+  if (slot->buf) cudaFree(slot->buf);
+  CDG_TRY(dalloc(&slot->buf, n));
+  std::vector<double> h;
+  h.reserve(n);
+  h.insert(h.end(), T.xi.begin(), T.xi.end());
+  h.insert(h.end(), T.w.begin(), T.w.end());
+  h.insert(h.end(), T.val.begin(), T.val.end());
+  h.insert(h.end(), T.grad.begin(), T.grad.end());
+  CDG_CUDA(cudaMemcpy(slot->buf, h.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+  slot->dim = dim;
+  slot->order = order;
+  slot->nqp1 = nqp1;
+  slot->t.xi = slot->buf;
+  slot->t.w = slot->t.xi + T.xi.size();
+  slot->t.val = slot->t.w + T.w.size();
+  slot->t.grad = slot->t.val + T.val.size();
+  *out = slot->t;
+  return CDG_OK;
+}
+
+int assemble_level(cdg_context* ctx, cdg_problem* p, DevLevel& L, const cdg_assembly_params& a) {
+  CDG_TRY(ensure_tables(ctx, p));
+  AsmCoefs k = make_coefs(a, L.dim, L.order, L.nloc);
+  if (k.nqp > 128) { set_error("quadrature rule too large"); return CDG_ERR_ARG; }
+  cudaStream_t st = ctx->stream;
+  // block->reset(), rhs.reset()
+  CDG_CUDA(cudaMemsetAsync(L.val64, 0, (size_t)L.nnz * sizeof(double), st));
+  CDG_CUDA(cudaMemsetAsync(L.rhs, 0, (size_t)L.ndof * sizeof(double), st));
+  const double* R = p->d_tables;
+  if (L.dim == 2 && L.nloc == 4) CDG_TRY((launch_contract<2, 4, 14>(ctx, k, L, R)));
+  else if (L.dim == 2 && L.nloc == 9) CDG_TRY((launch_contract<2, 9, 14>(ctx, k, L, R)));
+  else if (L.dim == 3 && L.nloc == 8) CDG_TRY((launch_contract<3, 8, 31>(ctx, k, L, R)));
+  else if (L.dim == 3 && L.nloc == 27) CDG_TRY((launch_contract<3, 27, 31>(ctx, k, L, R)));
+  else { set_error("unsupported element"); return CDG_ERR_ARG; }
+  int nd = L.ndof - L.nactive;
+  if (nd > 0)
+    CDG_LAUNCH(ctx, k_dirichlet_rows, grid_for<int>(nd, 256), 256, 0, L.ndof, L.nactive,
+               L.diag_slot, L.val64);
+  RhsTables tb;
+  CDG_TRY(get_rhs_tables(ctx, L.dim, L.order, k.nqp1, &tb));
+  if (L.dim == 2)
+    CDG_LAUNCH(ctx, k_rhs<2>, grid_for<int>(L.ncells, 8), 256, 0, k, L.ncells, L.nactive,
+               L.verts, L.gdof, tb, L.rhs);
+  else
+    CDG_LAUNCH(ctx, k_rhs<3>, grid_for<int>(L.ncells, 8), 256, 0, k, L.ncells, L.nactive,
+               L.verts, L.gdof, tb, L.rhs);
+  if (nd > 0)
+    CDG_LAUNCH(ctx, k_copy_nonactive, grid_for<int>(nd, 256), 256, 0, L.ndof, L.nactive, L.rhs,
+               L.sol);
+  int g = (int)std::min<long>(((long)std::max(L.nnz, L.ndof) + 255) / 256, (long)ctx->num_sms * 16);
+  CDG_LAUNCH(ctx, k_finish_matrix, g, 256, 0, L.ndof, L.nnz, L.diag_slot, L.val64, L.val32,
+             L.invdiag64, L.invdiag32, p->d_zero_diag);
+  return CDG_OK;
+}
+
+int level_errors(cdg_context* ctx, cdg_problem* p, DevLevel& L, const cdg_assembly_params& a,
+                 double* errors) {
+  AsmCoefs k = make_coefs(a, L.dim, L.order, L.nloc);
+  RhsTables tb;
+  CDG_TRY(get_rhs_tables(ctx, L.dim, L.order, k.nqp1, &tb));
+  double* acc = nullptr;
+  CDG_TRY(dalloc(&acc, 5));
+  CDG_CUDA(cudaMemsetAsync(acc, 0, 5 * sizeof(double), ctx->stream));
+  unsigned long long* lm = (unsigned long long*)(acc + 4);
+  if (L.dim == 2)
+    CDG_LAUNCH(ctx, k_errors<2>, grid_for<int>(L.ncells, 8), 256, 0, k, L.ncells, L.verts,
+               L.gdof, L.sol, tb, acc, lm);
+  else
+    CDG_LAUNCH(ctx, k_errors<3>, grid_for<int>(L.ncells, 8), 256, 0, k, L.ncells, L.verts,
+               L.gdof, L.sol, tb, acc, lm);
+  double h[5];
+  CDG_CUDA(cudaMemcpyAsync(h, acc, 5 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CDG_CUDA(cudaStreamSynchronize(ctx->stream));
+  cudaFree(acc);
+  errors[0] = sqrt(h[0]);
+  errors[1] = sqrt(h[1]);
+  errors[2] = sqrt(h[2]);
+  errors[3] = sqrt(fabs(h[3]));
+  errors[4] = h[4];
+  (void)p;
+  return CDG_OK;
+}
+
+}  // namespace cdg

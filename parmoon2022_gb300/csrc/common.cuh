@@ -1,0 +1,178 @@
+// common.cuh -- device-side helpers and the context / problem structures
+// shared by the assembly, linear-algebra and solver translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "cdg_internal.h"
+#include "parmoon_cd.h"
+
+namespace cdg {
+
+void set_error(const char* fmt, ...);
+
+#define CDG_CUDA(expr)                                                        \
+  do {                                                                         \
+    cudaError_t e_ = (expr);                                                   \
+    if (e_ != cudaSuccess) {                                                   \
+      cdg::set_error("%s:%d: %s: %s", __FILE__, __LINE__, #expr,               \
+                     cudaGetErrorString(e_));                                  \
+      return e_ == cudaErrorMemoryAllocation ? CDG_ERR_OOM : CDG_ERR_CUDA;     \
+    }                                                                          \
+  } while (0)
+
+#define CDG_TRY(expr)                                                          \
+  do {                                                                         \
+    int rc_ = (expr);                                                          \
+    if (rc_ != CDG_OK) return rc_;                                             \
+  } while (0)
+
+// device-side error word bits (set by kernels, read by the host at syncs)
+enum : int {
+  kErrPattern = 1,     // a local coupling is not in the CSR pattern
+  kErrZeroDiag = 2,    // zero diagonal entry
+  kErrSingular = 4,    // zero pivot in the coarse Gauss-Jordan
+  kErrBreakdown = 8,   // FGMRES H(i+1,i) == 0
+};
+
+constexpr int kRedSlots = 8;          // concurrent reductions
+constexpr int kRedMaxBlocks = 1024;   // partial sums per reduction
+
+}  // namespace cdg
+
+struct cdg_context {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  int* d_err = nullptr;           // device error word
+  double* d_red = nullptr;        // kRedSlots * kRedMaxBlocks partial sums
+  unsigned* d_cnt = nullptr;      // kRedSlots last-block counters
+  double* h_pinned = nullptr;     // 64 doubles of pinned readback space
+  long long launches = 0;
+};
+
+namespace cdg {
+
+// one discretisation level on the device
+struct DevLevel {
+  int dim = 2, order = 1, nloc = 4, nv = 4;
+  int ncells = 0, ndof = 0, nactive = 0, nnz = 0;
+  // host copies of the inputs (info queries, transfers)
+  Mesh mesh;
+  Space space;
+  Pattern pattern;
+  // device arrays
+  double* verts = nullptr;       // ncells*nv*dim
+  int* gdof = nullptr;           // ncells*nloc
+  int* row_ptr = nullptr;        // ndof+1
+  int* col = nullptr;            // nnz
+  int* slot = nullptr;           // ncells*nloc*nloc CSR slot of each coupling
+  int* diag_slot = nullptr;      // ndof
+  double* val64 = nullptr;       // nnz
+  float* val32 = nullptr;        // nnz (FP32 copy for the multigrid)
+  double* rhs = nullptr;         // ndof
+  double* sol = nullptr;         // ndof
+  double* invdiag64 = nullptr;   // ndof
+  float* invdiag32 = nullptr;    // ndof
+  int rows_per_warp_hint = 1;    // SpMV shape (avg row length)
+  // multigrid work vectors (double or float, per precision)
+  void* mg_rhs = nullptr;
+  void* mg_sol = nullptr;
+  void* mg_tmp = nullptr;
+  void* mg_def = nullptr;
+  int mg_elem = 0;               // sizeof element of mg vectors
+  // transfer to the next coarser level (this = fine)
+  int* P_rp = nullptr; int* P_col = nullptr; double* P_val = nullptr; float* P_val32 = nullptr;
+  int* R_rp = nullptr; int* R_col = nullptr; double* R_val = nullptr; float* R_val32 = nullptr;
+  int P_nnz = 0, R_nnz = 0;
+  // dense inverse of the active block (coarsest multigrid level)
+  double* coarse_inv = nullptr;  // na*na
+  double* coarse_work = nullptr; // 2 * na * 2na (Gauss-Jordan ping-pong)
+  int coarse_na = 0;
+};
+
+// FGMRES device state
+struct GmresState {
+  int n = 0, m = 0;
+  double* V = nullptr;       // (m+1)*n
+  double* Z = nullptr;       // m*n
+  double* w = nullptr;       // n
+  double* H = nullptr;       // (m+1)*(m+1), column-major by Arnoldi column
+  double* cs = nullptr;      // m+1
+  double* sn = nullptr;      // m+1
+  double* s = nullptr;       // m+1
+  double* y = nullptr;       // m+1
+  double* scal = nullptr;    // 8 scalars: [0] resid, [1] beta, ...
+};
+
+}  // namespace cdg
+
+struct cdg_problem {
+  cdg_context* ctx = nullptr;
+  int dim = 2, order = 1;
+  std::vector<cdg::DevLevel> lev;
+  cdg::GmresState gm;
+  double* d_tables = nullptr;     // reference tensors (device)
+  int* d_zero_diag = nullptr;     // set by the assembly when a diagonal is 0
+  int nterms = 0;
+  int rt_order = -1;
+};
+
+struct cdg_hierarchy {
+  int dim = 2, order = 1;
+  std::vector<cdg::Mesh> mesh;
+  std::vector<cdg::Space> space;
+  std::vector<cdg::Pattern> pattern;
+};
+
+namespace cdg {
+
+template <typename K>
+inline int grid_for(long n, int block) {
+  long g = (n + block - 1) / block;
+  return (int)(g < 1 ? 1 : g);
+}
+
+// launch accounting: every kernel launch of the library goes through this
+#define CDG_LAUNCH(ctx, kernel, grid, block, smem, ...)                        \
+  do {                                                                         \
+    kernel<<<(grid), (block), (smem), (ctx)->stream>>>(__VA_ARGS__);           \
+    (ctx)->launches++;                                                         \
+    cudaError_t le_ = cudaGetLastError();                                      \
+    if (le_ != cudaSuccess) {                                                  \
+      cdg::set_error("launch %s: %s", #kernel, cudaGetErrorString(le_));       \
+      return CDG_ERR_CUDA;                                                     \
+    }                                                                          \
+  } while (0)
+
+// host launchers implemented in the .cu files
+int upload_level(cdg_context* ctx, DevLevel& L);
+int free_level(DevLevel& L);
+int build_slots(cdg_context* ctx, DevLevel& L);
+int assemble_level(cdg_context* ctx, cdg_problem* p, DevLevel& L,
+                   const cdg_assembly_params& a);
+int check_device_error(cdg_context* ctx);
+int level_errors(cdg_context* ctx, cdg_problem* p, DevLevel& L,
+                 const cdg_assembly_params& a, double* errors);
+
+// linear algebra (linalg.cu)
+int spmv_apply64(cdg_context* ctx, const DevLevel& L, const double* x, double* y);
+int residual64(cdg_context* ctx, const DevLevel& L, const double* b, const double* x,
+               double* r);
+int dot64(cdg_context* ctx, int n, const double* a, const double* b, double* out,
+          int slot);
+int prolongate64(cdg_context* ctx, const DevLevel& F, const double* xc, double* xf,
+                 int add_actives_only, double damp);
+int restrict64(cdg_context* ctx, const DevLevel& F, const DevLevel& C, const double* df,
+               double* rc);
+int precondition(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s,
+                 const double* v, double* z);
+int prepare_solver(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s);
+int fgmres(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s,
+           cdg_solve_stats* st);
+
+}  // namespace cdg

@@ -1,0 +1,748 @@
+// linalg.cu -- GB300 kernels and host drivers of the CD solve: CSR SpMV with
+// identity on non-active rows, damped-Jacobi smoothing, grid transfers,
+// multigrid cycle, dense coarse inverse, Arnoldi reductions and the FGMRES
+// loop with all Krylov scalars resident on the device.
+//
+// Reference path (ParMooN2022): Solver::solve (src/Solver/Solver.C:601-696)
+// -> Iteration_gmres::flexible_gmres (src/Solver/Iteration_gmres.C:430-620,
+// Utilities_gmres.C:60-108, IterativeMethod.h:83-163) with preconditioner
+// Iteration_jacobi (src/Solver/Iteration_jacobi.C:168-182) or
+// Iteration_multigrid -> Multigrid::cycle (src/Multigrid/Multigrid.C:157-410,
+// CycleControl.C:15-111, MultigridLevel.C:118-151, JacobiSmoother.C:21-29,
+// GridTransfer.C:29-410, DirectSmoother.C:25-42);
+// BlockFEMatrix::apply_scaled_add (src/Matrix/BlockFEMatrix.C:969-1095).
+#include <chrono>
+#include <cmath>
+#include <cstring>
+
+#include "common.cuh"
+
+namespace cdg {
+
+// ---------------------------------------------------------------------------
+// SpMV family: TPR threads per row; non-active rows act as identity rows
+//   MODE 0: y = A x
+//   MODE 1: y = b - A x                         (calculate_defect)
+//   MODE 2: y = x + w D^-1 (b - A x)            (JacobiSmoother::smooth)
+// ---------------------------------------------------------------------------
+template <typename T, int TPR, int MODE>
+__global__ void __launch_bounds__(256)
+k_spmv(int n, int nactive, const int* __restrict__ rp, const int* __restrict__ col,
+       const T* __restrict__ val, const T* __restrict__ x, const T* __restrict__ b,
+       const T* __restrict__ invd, T w, T* __restrict__ y) {
+  const long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const int row = (int)(gt / TPR);
+  const int sub = threadIdx.x % TPR;
+  T s = 0;
+  const bool valid = row < n;
+  if (valid && row < nactive) {
+    const int e = __ldg(rp + row + 1);
+    for (int k = __ldg(rp + row) + sub; k < e; k += TPR) s += __ldg(val + k) * __ldg(x + __ldg(col + k));
+  }
+#pragma unroll
+  for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, TPR);
+  if (!valid || sub != 0) return;
+  const T xr = x[row];
+  if (row >= nactive) s = xr;
+  if (MODE == 0) y[row] = s;
+  else if (MODE == 1) y[row] = b[row] - s;
+  else y[row] = xr + w * (invd[row] * (b[row] - s));
+}
+
+template <typename T, int MODE>
+static int spmv_t(cdg_context* ctx, const DevLevel& L, const T* val, const T* x, const T* b,
+                  const T* invd, T w, T* y) {
+  const int tpr = L.rows_per_warp_hint;
+  long threads = (long)L.ndof * tpr;
+  int grid = (int)((threads + 255) / 256);
+  switch (tpr) {
+    case 4: CDG_LAUNCH(ctx, (k_spmv<T, 4, MODE>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y); break;
+    case 8: CDG_LAUNCH(ctx, (k_spmv<T, 8, MODE>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y); break;
+    case 16: CDG_LAUNCH(ctx, (k_spmv<T, 16, MODE>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y); break;
+    default: CDG_LAUNCH(ctx, (k_spmv<T, 32, MODE>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y); break;
+  }
+  return CDG_OK;
+}
+
+int spmv_apply64(cdg_context* ctx, const DevLevel& L, const double* x, double* y) {
+  return spmv_t<double, 0>(ctx, L, L.val64, x, nullptr, nullptr, 0.0, y);
+}
+int residual64(cdg_context* ctx, const DevLevel& L, const double* b, const double* x,
+               double* r) {
+  return spmv_t<double, 1>(ctx, L, L.val64, x, b, nullptr, 0.0, r);
+}
+
+// ---------------------------------------------------------------------------
+// deterministic reductions: per-block partial sums, the last block to finish
+// sums the partials in block order and writes the result to device memory
+// ---------------------------------------------------------------------------
+template <int NT>
+__device__ double block_sum(double v) {
+  __shared__ double sh[NT / 32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x < 32) {
+    r = (l < NT / 32) ? sh[l] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+  }
+  return r;  // valid in thread 0
+}
+
+template <int NT>
+__device__ void finalize_sum(double blocksum, double* partials, unsigned* cnt, double* out,
+                             bool take_sqrt) {
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = blocksum;
+    __threadfence();
+    unsigned t = atomicAdd(cnt, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double v = 0.0;
+  for (int i = threadIdx.x; i < (int)gridDim.x; i += NT) v += ((volatile double*)partials)[i];
+  v = block_sum<NT>(v);
+  if (threadIdx.x == 0) {
+    *out = take_sqrt ? sqrt(v) : v;
+    *cnt = 0u;
+  }
+}
+
+// out = dot(a, b) (MODE 0) or ||a|| (MODE 1)
+template <int MODE>
+__global__ void __launch_bounds__(256)
+k_dot(int n, const double* __restrict__ a, const double* __restrict__ b, double* partials,
+      unsigned* cnt, double* out) {
+  double s = 0.0;
+  for (long i = blockIdx.x * 256L + threadIdx.x; i < n; i += (long)gridDim.x * 256)
+    s += MODE == 0 ? a[i] * b[i] : a[i] * a[i];
+  s = block_sum<256>(s);
+  finalize_sum<256>(s, partials, cnt, out, MODE == 1);
+}
+
+// modified Gram-Schmidt step k of the Arnoldi process, fused with the next
+// inner product: w -= H(k,i) v_k; out = (w, v_{k+1}) or ||w|| (last step)
+__global__ void __launch_bounds__(256)
+k_mgs(int n, double* __restrict__ w, const double* __restrict__ vk, const double* hk,
+      const double* __restrict__ vnext, double* partials, unsigned* cnt, double* out) {
+  const double h = -(*hk);
+  double s = 0.0;
+  for (long i = blockIdx.x * 256L + threadIdx.x; i < n; i += (long)gridDim.x * 256) {
+    double wi = w[i] + h * vk[i];
+    w[i] = wi;
+    s += vnext ? wi * vnext[i] : wi * wi;
+  }
+  s = block_sum<256>(s);
+  finalize_sum<256>(s, partials, cnt, out, vnext == nullptr);
+}
+
+static int red_grid(cdg_context* ctx, int n) {
+  int g = (n + 255) / 256;
+  int cap = ctx->num_sms * 4;
+  if (g > cap) g = cap;
+  if (g > kRedMaxBlocks) g = kRedMaxBlocks;
+  return g < 1 ? 1 : g;
+}
+
+int dot64(cdg_context* ctx, int n, const double* a, const double* b, double* out, int slot) {
+  double* part = ctx->d_red + (size_t)slot * kRedMaxBlocks;
+  unsigned* cnt = ctx->d_cnt + slot;
+  if (b)
+    CDG_LAUNCH(ctx, k_dot<0>, red_grid(ctx, n), 256, 0, n, a, b, part, cnt, out);
+  else
+    CDG_LAUNCH(ctx, k_dot<1>, red_grid(ctx, n), 256, 0, n, a, a, part, cnt, out);
+  return CDG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// small vector kernels
+// ---------------------------------------------------------------------------
+// dst = src * (1 / *s); flags a zero scalar (FGMRES breakdown)
+__global__ void k_scale_inv(int n, const double* __restrict__ src, const double* s,
+                            double* __restrict__ dst, int* err) {
+  const double d = *s;
+  if (d == 0.0) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(err, kErrBreakdown);
+    return;
+  }
+  const double f = 1.0 / d;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    dst[i] = src[i] * f;
+}
+
+__global__ void k_mul(int n, const double* __restrict__ a, const double* __restrict__ b,
+                      double* __restrict__ c) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    c[i] = a[i] * b[i];
+}
+
+template <typename T>
+__global__ void k_mg_init(int n, int nactive, const double* __restrict__ v, T* __restrict__ rhs,
+                          T* __restrict__ sol) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    T r = (T)v[i];
+    rhs[i] = r;
+    sol[i] = i >= nactive ? r : (T)0;
+  }
+}
+
+template <typename T>
+__global__ void k_to_double(int n, const T* __restrict__ a, double* __restrict__ b) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    b[i] = (double)a[i];
+}
+
+// x_f[i] += damp * (P x_c)[i] for fine actives (update_solution_in_finer_grid)
+// or x_f = P x_c for all rows (GridTransfer::Prolongate) when damp == 0
+template <typename T>
+__global__ void k_prolong(int nf, int nactive_f, const int* __restrict__ rp,
+                          const int* __restrict__ col, const T* __restrict__ val,
+                          const T* __restrict__ xc, T* __restrict__ xf, T damp, int add) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < nf; i += (long)gridDim.x * blockDim.x) {
+    T s = 0;
+    for (int k = rp[i]; k < rp[i + 1]; ++k) s += val[k] * xc[col[k]];
+    if (!add) xf[i] = s;
+    else if (i < nactive_f) xf[i] += damp * s;
+  }
+}
+
+// r_c = R d_f; coarse non-actives zeroed when mask (ResetNonActive)
+template <typename T>
+__global__ void k_restrict(int nc, int nactive_c, const int* __restrict__ rp,
+                           const int* __restrict__ col, const T* __restrict__ val,
+                           const T* __restrict__ df, T* __restrict__ rc, int mask) {
+  for (long j = blockIdx.x * (long)blockDim.x + threadIdx.x; j < nc; j += (long)gridDim.x * blockDim.x) {
+    T s = 0;
+    if (!mask || j < nactive_c)
+      for (int k = rp[j]; k < rp[j + 1]; ++k) s += val[k] * df[col[k]];
+    rc[j] = s;
+  }
+}
+
+template <typename T>
+__global__ void k_coarse_init(int n, int na, const T* __restrict__ b, T* __restrict__ x) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    x[i] = i < na ? (T)0 : b[i];
+}
+
+// x_a += Inv d_a  (FP64 dense inverse of the coarsest active block), warp/row
+template <typename T>
+__global__ void k_coarse_apply(int na, const double* __restrict__ inv, const T* __restrict__ d,
+                               T* __restrict__ x) {
+  const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, l = threadIdx.x & 31;
+  if (row >= na) return;
+  double s = 0.0;
+  for (int j = l; j < na; j += 32) s += inv[(size_t)row * na + j] * (double)d[j];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (l == 0) x[row] = (T)((double)x[row] + s);
+}
+
+// ---------------------------------------------------------------------------
+// coarsest level: Gauss-Jordan inversion with partial pivoting of the active
+// block, one kernel per pivot step on an n x 2n augmented matrix
+// ---------------------------------------------------------------------------
+__global__ void k_extract_dense(int na, const int* __restrict__ rp, const int* __restrict__ col,
+                                const double* __restrict__ val, double* __restrict__ M) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= na) return;
+  const long W = 2L * na;
+  for (int k = rp[i]; k < rp[i + 1]; ++k)
+    if (col[k] < na) M[i * W + col[k]] = val[k];
+  M[i * W + na + i] = 1.0;
+}
+
+__global__ void __launch_bounds__(256)
+k_gj_step(int na, int k, const double* __restrict__ Min, double* __restrict__ Mout, int* err) {
+  const long W = 2L * na;
+  __shared__ double sv[256];
+  __shared__ int si[256];
+  // pivot: first row of maximal |Min[i][k]|, i >= k (every block agrees)
+  double best = -1.0;
+  int bi = k;
+  for (int i = k + threadIdx.x; i < na; i += 256) {
+    double a = fabs(Min[i * W + k]);
+    if (a > best) { best = a; bi = i; }
+  }
+  sv[threadIdx.x] = best;
+  si[threadIdx.x] = bi;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      double a = sv[threadIdx.x + o];
+      int ai = si[threadIdx.x + o];
+      if (a > sv[threadIdx.x] || (a == sv[threadIdx.x] && ai < si[threadIdx.x])) {
+        sv[threadIdx.x] = a;
+        si[threadIdx.x] = ai;
+      }
+    }
+    __syncthreads();
+  }
+  const int p = si[0];
+  const double piv = Min[p * W + k];
+  if (piv == 0.0) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(err, kErrSingular);
+    return;
+  }
+  const long ncol = (na - k) + na;  // live columns: left [k, na), right [na, 2na)
+  const long total = (long)na * ncol;
+  for (long t = blockIdx.x * 256L + threadIdx.x; t < total; t += (long)gridDim.x * 256) {
+    const int i = (int)(t / ncol);
+    const long jj = t % ncol;
+    const long j = jj < (na - k) ? k + jj : na + (jj - (na - k));
+    const double prow = Min[p * W + j] / piv;
+    if (i == k) {
+      Mout[i * W + j] = prow;
+    } else {
+      const int r = (i == p) ? k : i;
+      Mout[i * W + j] = Min[r * W + j] - Min[r * W + k] * prow;
+    }
+  }
+}
+
+__global__ void k_right_half(int na, const double* __restrict__ M, double* __restrict__ inv) {
+  const long total = (long)na * na;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
+    const long i = t / na, j = t % na;
+    inv[t] = M[i * 2L * na + na + j];
+  }
+}
+
+static int coarse_inverse(cdg_context* ctx, DevLevel& C) {
+  const int na = C.nactive;
+  C.coarse_na = na;
+  if (na == 0) return CDG_OK;
+  if (na > 8192) { set_error("coarse level too large for the dense inverse (%d)", na); return CDG_ERR_LIMIT; }
+  size_t sz = (size_t)na * 2 * na;
+  if (!C.coarse_work) {
+    CDG_CUDA(cudaMalloc(&C.coarse_work, 2 * sz * sizeof(double)));
+    CDG_CUDA(cudaMalloc(&C.coarse_inv, (size_t)na * na * sizeof(double)));
+  }
+  double* A = C.coarse_work;
+  double* B = C.coarse_work + sz;
+  CDG_CUDA(cudaMemsetAsync(A, 0, sz * sizeof(double), ctx->stream));
+  CDG_LAUNCH(ctx, k_extract_dense, grid_for<int>(na, 128), 128, 0, na, C.row_ptr, C.col, C.val64, A);
+  for (int k = 0; k < na; ++k) {
+    long total = (long)na * ((na - k) + na);
+    int g = (int)std::min<long>((total + 255) / 256, (long)ctx->num_sms * 8);
+    CDG_LAUNCH(ctx, k_gj_step, g, 256, 0, na, k, A, B, ctx->d_err);
+    std::swap(A, B);
+  }
+  CDG_LAUNCH(ctx, k_right_half, grid_for<int>(na * na, 256), 256, 0, na, A, C.coarse_inv);
+  return CDG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// multigrid (Multigrid::cycle); levels: p->lev[0] finest ... lev[nl-1]
+// ---------------------------------------------------------------------------
+template <typename T> struct Prec;
+template <> struct Prec<double> {
+  static const double* val(const DevLevel& L) { return L.val64; }
+  static const double* invd(const DevLevel& L) { return L.invdiag64; }
+  static const double* P(const DevLevel& L) { return L.P_val; }
+  static const double* R(const DevLevel& L) { return L.R_val; }
+};
+template <> struct Prec<float> {
+  static const float* val(const DevLevel& L) { return L.val32; }
+  static const float* invd(const DevLevel& L) { return L.invdiag32; }
+  static const float* P(const DevLevel& L) { return L.P_val32; }
+  static const float* R(const DevLevel& L) { return L.R_val32; }
+};
+
+static int vec_grid(cdg_context* ctx, long n) {
+  long g = (n + 255) / 256;
+  long cap = (long)ctx->num_sms * 8;
+  return (int)(g > cap ? cap : (g < 1 ? 1 : g));
+}
+
+template <typename T>
+static int smooth(cdg_context* ctx, DevLevel& L, T damp) {
+  CDG_TRY((spmv_t<T, 2>(ctx, L, Prec<T>::val(L), (const T*)L.mg_sol, (const T*)L.mg_rhs,
+                         Prec<T>::invd(L), damp, (T*)L.mg_tmp)));
+  std::swap(L.mg_sol, L.mg_tmp);
+  return CDG_OK;
+}
+
+template <typename T>
+static int defect(cdg_context* ctx, DevLevel& L) {
+  return spmv_t<T, 1>(ctx, L, Prec<T>::val(L), (const T*)L.mg_sol, (const T*)L.mg_rhs, nullptr,
+                      (T)0, (T*)L.mg_def);
+}
+
+// update_solution_in_finer_grid: fine.sol += damp * P coarse.sol on actives
+template <typename T>
+static int prolong_correct(cdg_context* ctx, DevLevel& F, DevLevel& C, T damp) {
+  CDG_LAUNCH(ctx, k_prolong<T>, vec_grid(ctx, F.ndof), 256, 0, F.ndof, F.nactive, F.P_rp,
+             F.P_col, Prec<T>::P(F), (const T*)C.mg_sol, (T*)F.mg_sol, damp, 1);
+  return CDG_OK;
+}
+
+template <typename T>
+static int coarse_solve(cdg_context* ctx, DevLevel& C, const cdg_solver_params& s) {
+  if (s.multigrid_smoother_coarse == 0) {
+    // direct_solve: x = A^-1 rhs (idempotent, one application suffices)
+    CDG_LAUNCH(ctx, k_coarse_init<T>, vec_grid(ctx, C.ndof), 256, 0, C.ndof, C.nactive,
+               (const T*)C.mg_rhs, (T*)C.mg_sol);
+    CDG_TRY(defect<T>(ctx, C));
+    CDG_LAUNCH(ctx, k_coarse_apply<T>, grid_for<int>((long)C.nactive * 32, 256), 256, 0,
+               C.nactive, C.coarse_inv, (const T*)C.mg_def, (T*)C.mg_sol);
+    return CDG_OK;
+  }
+  // jacobi iterations until the coarse residual is small enough
+  double res = 1e10;
+  double* d_norm = ctx->d_red + (size_t)(kRedSlots - 1) * kRedMaxBlocks - 8;  // spare scalars
+  (void)d_norm;
+  for (int i = 0; i < s.multigrid_coarse_max_n_iterations && res > s.multigrid_coarse_residual; ++i) {
+    CDG_TRY(smooth<T>(ctx, C, (T)s.jacobi_damp));
+    CDG_TRY(defect<T>(ctx, C));
+    // residual norm on the host (rarely used path)
+    std::vector<T> h(C.ndof);
+    CDG_CUDA(cudaMemcpyAsync(h.data(), C.mg_def, C.ndof * sizeof(T), cudaMemcpyDeviceToHost,
+                             ctx->stream));
+    CDG_CUDA(cudaStreamSynchronize(ctx->stream));
+    double ss = 0;
+    for (T v : h) ss += (double)v * (double)v;
+    res = sqrt(ss);
+  }
+  return CDG_OK;
+}
+
+enum { kDummy, kDown, kUp, kEnd };
+static void fill_cycle(std::vector<int>& seq, std::vector<int>& rec, int level, int nlev, int cyc) {
+  if (level == 0) {
+    seq.push_back(kUp);
+    return;
+  }
+  for (int j = 0; j < rec[level]; ++j) {
+    seq.push_back(kDown);
+    fill_cycle(seq, rec, level - 1, nlev, cyc);
+  }
+  if (cyc == 2) rec[level] = 1;
+  seq.push_back(level == nlev - 1 ? kEnd : kUp);
+}
+
+template <typename T>
+static int mg_cycle(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s,
+                    const double* v, double* z) {
+  const int nl = s.multigrid_n_levels;
+  auto lv = [&](int m) -> DevLevel& { return p->lev[nl - 1 - m]; };
+  DevLevel& F = p->lev[0];
+  CDG_LAUNCH(ctx, k_mg_init<T>, vec_grid(ctx, F.ndof), 256, 0, F.ndof, F.nactive, v,
+             (T*)F.mg_rhs, (T*)F.mg_sol);
+  std::vector<int> rec(nl, s.multigrid_cycle_type == 0 ? 1 : 2), seq;
+  rec[nl - 1] = 1;
+  seq.push_back(kDummy);
+  fill_cycle(seq, rec, nl - 1, nl, s.multigrid_cycle_type);
+  const T damp = (T)s.jacobi_damp;
+  const T cdamp = (T)s.multigrid_correction_damp_factor;
+  int level = nl - 1;
+  if (nl == 1) {
+    CDG_TRY(coarse_solve<T>(ctx, F, s));
+  } else {
+    for (size_t step = 1; step < seq.size() && level >= 0; ++step) {
+      DevLevel& L = lv(level);
+      if (level == 0) {
+        CDG_TRY(coarse_solve<T>(ctx, L, s));
+        CDG_TRY(prolong_correct<T>(ctx, lv(level + 1), L, cdamp));
+        level += 1;
+        continue;
+      }
+      const bool from_below = seq[step - 1] == kUp;
+      const int dir = seq[step];
+      if (from_below)
+        for (int i = 0; i < s.multigrid_n_post_smooth; ++i) CDG_TRY(smooth<T>(ctx, L, damp));
+      if (dir == kDown) {
+        for (int i = 0; i < s.multigrid_n_pre_smooth; ++i) CDG_TRY(smooth<T>(ctx, L, damp));
+        CDG_TRY(defect<T>(ctx, L));
+        DevLevel& C = lv(level - 1);
+        // coarse start iterate is set by the restriction target's consumer:
+        // the coarse solution starts from zero
+        CDG_CUDA(cudaMemsetAsync(C.mg_sol, 0, (size_t)C.ndof * sizeof(T), ctx->stream));
+        CDG_LAUNCH(ctx, k_restrict<T>, vec_grid(ctx, C.ndof), 256, 0, C.ndof, C.nactive, L.R_rp,
+                   L.R_col, Prec<T>::R(L), (const T*)L.mg_def, (T*)C.mg_rhs, 1);
+        level -= 1;
+      } else if (dir == kUp) {
+        CDG_TRY(prolong_correct<T>(ctx, lv(level + 1), L, cdamp));
+        level += 1;
+      } else {
+        break;
+      }
+    }
+  }
+  CDG_LAUNCH(ctx, k_to_double<T>, vec_grid(ctx, F.ndof), 256, 0, F.ndof, (const T*)F.mg_sol, z);
+  return CDG_OK;
+}
+
+int prepare_solver(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s) {
+  CDG_TRY(check_device_error(ctx));
+  if (s.preconditioner != 0) {
+    // extract_diagonal_entries (Iteration_jacobi.C:14-28) rejects zero
+    // diagonals; the assembly recorded them per problem
+    int zd = 0;
+    CDG_CUDA(cudaMemcpyAsync(&zd, p->d_zero_diag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CDG_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (zd) {
+      set_error("zero entry on the diagonal using Jacobi solver/preconditioner");
+      return CDG_ERR_ZERO_DIAG;
+    }
+  }
+  if (s.preconditioner != 2) return CDG_OK;
+  const int nl = s.multigrid_n_levels;
+  if (nl < 1 || nl > (int)p->lev.size()) {
+    set_error("multigrid_n_levels=%d but the problem has %d levels", nl, (int)p->lev.size());
+    return CDG_ERR_ARG;
+  }
+  const int elem = s.precision == 1 ? (int)sizeof(float) : (int)sizeof(double);
+  for (int k = 0; k < nl; ++k) {
+    DevLevel& L = p->lev[k];
+    if (L.mg_elem != elem) {
+      void** bufs[4] = {&L.mg_rhs, &L.mg_sol, &L.mg_tmp, &L.mg_def};
+      for (void** b : bufs) {
+        if (*b) cudaFree(*b);
+        CDG_CUDA(cudaMalloc(b, (size_t)std::max(L.ndof, 1) * elem));
+        CDG_CUDA(cudaMemsetAsync(*b, 0, (size_t)std::max(L.ndof, 1) * elem, ctx->stream));
+      }
+      L.mg_elem = elem;
+    }
+  }
+  if (s.multigrid_smoother_coarse == 0) {
+    CDG_TRY(coarse_inverse(ctx, p->lev[nl - 1]));
+    CDG_TRY(check_device_error(ctx));
+  }
+  return CDG_OK;
+}
+
+int precondition(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s, const double* v,
+                 double* z) {
+  DevLevel& F = p->lev[0];
+  if (s.preconditioner == 1) {
+    CDG_LAUNCH(ctx, k_mul, vec_grid(ctx, F.ndof), 256, 0, F.ndof, v, F.invdiag64, z);
+    return CDG_OK;
+  }
+  if (s.preconditioner == 2) {
+    if (s.precision == 1) return mg_cycle<float>(ctx, p, s, v, z);
+    return mg_cycle<double>(ctx, p, s, v, z);
+  }
+  CDG_CUDA(cudaMemcpyAsync(z, v, (size_t)F.ndof * sizeof(double), cudaMemcpyDeviceToDevice,
+                           ctx->stream));
+  return CDG_OK;
+}
+
+int prolongate64(cdg_context* ctx, const DevLevel& F, const double* xc, double* xf,
+                 int add_actives_only, double damp) {
+  CDG_LAUNCH(ctx, k_prolong<double>, vec_grid(ctx, F.ndof), 256, 0, F.ndof, F.nactive, F.P_rp,
+             F.P_col, F.P_val, xc, xf, damp, add_actives_only);
+  return CDG_OK;
+}
+
+int restrict64(cdg_context* ctx, const DevLevel& F, const DevLevel& C, const double* df,
+               double* rc) {
+  CDG_LAUNCH(ctx, k_restrict<double>, vec_grid(ctx, C.ndof), 256, 0, C.ndof, C.nactive, F.R_rp,
+             F.R_col, F.R_val, df, rc, 0);
+  return CDG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// FGMRES(m): Hessenberg column i stored at H[i*(m+1) + k] = H(k, i)
+// ---------------------------------------------------------------------------
+__global__ void k_givens(int i, int m, double* H, double* cs, double* sn, double* s,
+                         double* resid) {
+  double* col = H + (size_t)i * (m + 1);
+  for (int k = 0; k < i; ++k) {
+    double dx = col[k], dy = col[k + 1];
+    col[k] = cs[k] * dx + sn[k] * dy;
+    col[k + 1] = -sn[k] * dx + cs[k] * dy;
+  }
+  double dx = col[i], dy = col[i + 1], c, sg;
+  if (dy == 0.0) {
+    c = 1.0;
+    sg = 0.0;
+  } else if (fabs(dy) > fabs(dx)) {
+    double t = dx / dy;
+    sg = 1.0 / sqrt(1.0 + t * t);
+    c = t * sg;
+  } else {
+    double t = dy / dx;
+    c = 1.0 / sqrt(1.0 + t * t);
+    sg = t * c;
+  }
+  cs[i] = c;
+  sn[i] = sg;
+  col[i] = c * dx + sg * dy;
+  col[i + 1] = -sg * dx + c * dy;
+  double a = s[i], b = s[i + 1];
+  s[i] = c * a + sg * b;
+  s[i + 1] = -sg * a + c * b;
+  *resid = fabs(s[i + 1]);
+}
+
+// s = (beta, 0, ..., 0)
+__global__ void k_init_s(int m, const double* beta, double* s) {
+  for (int i = threadIdx.x; i <= m; i += blockDim.x) s[i] = i == 0 ? *beta : 0.0;
+}
+
+// Hessenberg back substitution (Utilities_gmres.C:90-108)
+__global__ void k_backsolve(int k, int m, const double* H, const double* s, double* y) {
+  for (int i = 0; i <= k; ++i) y[i] = s[i];
+  for (int i = k; i >= 0; --i) {
+    y[i] /= H[(size_t)i * (m + 1) + i];
+    for (int j = i - 1; j >= 0; --j) y[j] -= H[(size_t)i * (m + 1) + j] * y[i];
+  }
+}
+
+// x += sum_j y_j z_j (accumulated from zero in order j = 0..k, then added)
+__global__ void k_update(int n, int k, const double* __restrict__ Z, const double* __restrict__ y,
+                         double* __restrict__ x) {
+  __shared__ double ys[128];
+  for (int j = threadIdx.x; j <= k; j += blockDim.x) ys[j] = y[j];
+  __syncthreads();
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int j = 0; j <= k; ++j) acc += ys[j] * Z[(size_t)j * n + t];
+    x[t] += acc;
+  }
+}
+
+static int ensure_gmres(cdg_problem* p, int n, int m) {
+  GmresState& g = p->gm;
+  if (g.n == n && g.m == m && g.V) return CDG_OK;
+  double* ptrs[] = {g.V, g.Z, g.w, g.H, g.cs, g.sn, g.s, g.y, g.scal};
+  for (double* q : ptrs)
+    if (q) cudaFree(q);
+  g = GmresState();
+  g.n = n;
+  g.m = m;
+  CDG_CUDA(cudaMalloc(&g.V, (size_t)(m + 1) * n * sizeof(double)));
+  CDG_CUDA(cudaMalloc(&g.Z, (size_t)m * n * sizeof(double)));
+  CDG_CUDA(cudaMalloc(&g.w, (size_t)n * sizeof(double)));
+  CDG_CUDA(cudaMalloc(&g.H, (size_t)(m + 1) * (m + 1) * sizeof(double)));
+  CDG_CUDA(cudaMalloc(&g.cs, (size_t)(m + 1) * sizeof(double)));
+  CDG_CUDA(cudaMalloc(&g.sn, (size_t)(m + 1) * sizeof(double)));
+  CDG_CUDA(cudaMalloc(&g.s, (size_t)(m + 1) * sizeof(double)));
+  CDG_CUDA(cudaMalloc(&g.y, (size_t)(m + 1) * sizeof(double)));
+  CDG_CUDA(cudaMalloc(&g.scal, 8 * sizeof(double)));
+  CDG_CUDA(cudaMemset(g.H, 0, (size_t)(m + 1) * (m + 1) * sizeof(double)));
+  return CDG_OK;
+}
+
+struct LoopInfo {
+  double initial = 0, previous = 0;
+};
+
+// IterativeMethod::converged: 0 continue, 1 stop, 2 diverged
+static int converged(const cdg_solver_params& s, LoopInfo& li, double res, int it) {
+  if (it == 0) {
+    li.initial = res;
+    li.previous = res;
+  }
+  bool small = res < s.residual_tolerance;
+  bool red = res < s.residual_reduction * li.initial;
+  bool enough = it >= s.min_n_iterations;
+  bool stag = res > 1e10 * li.previous;
+  bool div = res > s.divergence_factor * li.initial;
+  bool conv = (small || red || stag || div) && enough;
+  if (it == s.max_n_iterations) conv = true;
+  li.previous = res;
+  if (div) return 2;
+  return conv ? 1 : 0;
+}
+
+static int read_scalar(cdg_context* ctx, const double* d, double* h) {
+  CDG_CUDA(cudaMemcpyAsync(ctx->h_pinned, d, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CDG_CUDA(cudaStreamSynchronize(ctx->stream));
+  *h = ctx->h_pinned[0];
+  return CDG_OK;
+}
+
+// Iteration_gmres::flexible_gmres on the finest level: x = lev[0].sol,
+// b = lev[0].rhs
+int fgmres(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s, cdg_solve_stats* st) {
+  DevLevel& L = p->lev[0];
+  const int n = L.ndof, m = s.gmres_restart;
+  if (m < 1 || m > 120) { set_error("gmres_restart must be in [1, 120]"); return CDG_ERR_ARG; }
+  CDG_TRY(ensure_gmres(p, n, m));
+  GmresState& g = p->gm;
+  double* x = L.sol;
+  const double* b = L.rhs;
+  double* beta_d = g.scal + 1;
+  double* resid_d = g.scal + 0;
+  LoopInfo li;
+  // r = b - A x; beta = ||r||
+  CDG_TRY(residual64(ctx, L, b, x, g.w));
+  CDG_TRY(dot64(ctx, n, g.w, nullptr, beta_d, 0));
+  double beta = 0;
+  CDG_TRY(read_scalar(ctx, beta_d, &beta));
+  double resid = beta;
+  st->initial_residual = beta;
+  st->iterations = 0;
+  st->residual = beta;
+  if (converged(s, li, resid, 0)) return CDG_OK;
+  int j = 1;
+  const int vg = vec_grid(ctx, n);
+  while (j <= s.max_n_iterations) {
+    CDG_LAUNCH(ctx, k_scale_inv, vg, 256, 0, n, g.w, beta_d, g.V, ctx->d_err);
+    CDG_LAUNCH(ctx, k_init_s, 1, 128, 0, m, beta_d, g.s);
+    int i;
+    for (i = 0; i < m && j <= s.max_n_iterations; ++i, ++j) {
+      double* vi = g.V + (size_t)i * n;
+      double* zi = g.Z + (size_t)i * n;
+      double* col = g.H + (size_t)i * (m + 1);
+      CDG_TRY(precondition(ctx, p, s, vi, zi));
+      CDG_TRY(spmv_apply64(ctx, L, zi, g.w));
+      CDG_TRY(dot64(ctx, n, g.w, g.V, col + 0, 0));
+      for (int k = 0; k <= i; ++k) {
+        const double* vk = g.V + (size_t)k * n;
+        const double* vn = (k < i) ? g.V + (size_t)(k + 1) * n : nullptr;
+        CDG_LAUNCH(ctx, k_mgs, red_grid(ctx, n), 256, 0, n, g.w, vk, col + k, vn,
+                   ctx->d_red, ctx->d_cnt, col + k + 1);
+      }
+      CDG_LAUNCH(ctx, k_scale_inv, vg, 256, 0, n, g.w, col + i + 1, g.V + (size_t)(i + 1) * n,
+                 ctx->d_err);
+      CDG_LAUNCH(ctx, k_givens, 1, 1, 0, i, m, g.H, g.cs, g.sn, g.s, resid_d);
+      CDG_TRY(read_scalar(ctx, resid_d, &resid));
+      CDG_TRY(check_device_error(ctx));
+      int cv = converged(s, li, resid, j);
+      if (cv == 2) {
+        set_error("Execution of the code stopped because of solver divergence.");
+        st->iterations = j;
+        st->residual = resid;
+        return CDG_ERR_DIVERGED;
+      }
+      if (cv) {
+        CDG_LAUNCH(ctx, k_backsolve, 1, 1, 0, i, m, g.H, g.s, g.y);
+        CDG_LAUNCH(ctx, k_update, vg, 256, 0, n, i, g.Z, g.y, x);
+        st->iterations = j;
+        st->residual = resid;
+        return CDG_OK;
+      }
+    }
+    CDG_LAUNCH(ctx, k_backsolve, 1, 1, 0, m - 1, m, g.H, g.s, g.y);
+    CDG_LAUNCH(ctx, k_update, vg, 256, 0, n, m - 1, g.Z, g.y, x);
+    CDG_TRY(residual64(ctx, L, b, x, g.w));
+    CDG_TRY(dot64(ctx, n, g.w, nullptr, beta_d, 0));
+    CDG_TRY(read_scalar(ctx, beta_d, &beta));
+    int cv = converged(s, li, resid, j);
+    if (cv == 2) {
+      set_error("Execution of the code stopped because of solver divergence.");
+      return CDG_ERR_DIVERGED;
+    }
+    if (cv) {
+      st->iterations = j;
+      st->residual = resid;
+      return CDG_OK;
+    }
+  }
+  st->iterations = s.max_n_iterations;
+  st->residual = resid;
+  return CDG_OK;
+}
+
+}  // namespace cdg

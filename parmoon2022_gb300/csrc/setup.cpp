@@ -1,0 +1,487 @@
+// setup.cpp -- host-side setup layer: structured mesh hierarchies, DOF
+// numbering, CSR sparsity pattern, grid-transfer matrices and the reference
+// tensors of the element contraction.  This is the part of ParMooN's setup
+// (TDomain refinement, TFESpace::ConstructSpace, TStructure, FEDatabase
+// prolongation matrices) that the hot path consumes as input; it runs once
+// per mesh hierarchy and needs no GPU.
+//
+// Reference behaviour restated here:
+//  * cell order after regular refinement: depth-first over the refinement
+//    tree (src/Geometry/It_Finest.C), children and their local vertex order
+//    from src/Refinement/RefQuadRegDesc.C:21-22 and RefHexaRegDesc.C:17-21;
+//  * DOF numbering (src/FE/FESpace2D.C:83-312, FESpace.C:1863-2099,
+//    FEMapper.C:456-600): the FE mapper keeps the smallest (cell, local dof)
+//    position of every global DOF as its representative and the final pass
+//    numbers representatives in traversal order, inner DOFs first, then
+//    non-Dirichlet boundary DOFs, then Dirichlet DOFs.  make_space applies
+//    that rule directly;
+//  * TStructure (src/Matrix/Structure.C:226-618): full rows also for
+//    Dirichlet DOFs, columns sorted ascending;
+//  * GridTransfer::Prolongate / DefectRestriction (src/Multigrid/
+//    GridTransfer.C:29-410): averaged child-local interpolation and its
+//    transpose; written as two CSR matrices.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <stdexcept>
+#include <unordered_map>
+
+#include "cdg_internal.h"
+
+namespace cdg {
+
+// ---------------------------------------------------------------------------
+// quadrature
+// ---------------------------------------------------------------------------
+void gauss_legendre(int n, double* x, double* w) {
+  // roots of P_n by Newton's method from Tricomi's initial guesses, in
+  // extended precision; nodes ascending
+  for (int i = 0; i < n; ++i) {
+    long double th = 3.14159265358979323846264338327950288L * (4 * i + 3) / (4 * n + 2);
+    long double z = cosl(th);
+    long double dp = 1;
+    for (int it = 0; it < 64; ++it) {
+      long double p0 = 1, p1 = z;
+      for (int k = 2; k <= n; ++k) {
+        long double pk = ((2 * k - 1) * z * p1 - (k - 1) * p0) / k;
+        p0 = p1;
+        p1 = pk;
+      }
+      if (n == 1) { p1 = z; p0 = 1; }
+      dp = n * (z * p1 - p0) / (z * z - 1);
+      long double dz = p1 / dp;
+      z -= dz;
+      if (fabsl(dz) < 1e-32L) break;
+    }
+    x[n - 1 - i] = (double)z;
+    w[n - 1 - i] = (double)(2.0L / ((1 - z * z) * dp * dp));
+  }
+}
+
+int gauss_points_for_degree(int deg) {
+  // QuadratureFormulaDatabase.C:41-81 (quad / hexa rules by accuracy)
+  if (deg > 17) deg = 17;
+  if (deg <= 2) return 2;
+  if (deg <= 5) return 3;
+  return deg / 2 + 1;
+}
+
+// ---------------------------------------------------------------------------
+// reference element: tensor-product Lagrange Q1/Q2, local DOF k = k0 +
+// (p+1)(k1 + (p+1)k2) at nodes {-1,1} (Q1) or {-1,0,1} (Q2), xi fastest
+// (include/FE2D/BF_C_Q_Q{1,2}_2D.h, include/FE3D/BF_C_H_Q{1,2}_3D.h)
+// ---------------------------------------------------------------------------
+static void line_basis(int p, double t, double* v, double* d, double* dd) {
+  if (p == 1) {
+    v[0] = 0.5 * (1 - t); v[1] = 0.5 * (1 + t);
+    d[0] = -0.5; d[1] = 0.5;
+    dd[0] = 0; dd[1] = 0;
+  } else {
+    v[0] = 0.5 * t * (t - 1); v[1] = (1 - t) * (1 + t); v[2] = 0.5 * t * (t + 1);
+    d[0] = t - 0.5; d[1] = -2 * t; d[2] = t + 0.5;
+    dd[0] = 1; dd[1] = -2; dd[2] = 1;
+  }
+}
+
+void local_dof_ref(int dim, int p, int k, double* r) {
+  int n1 = p + 1;
+  int i[3] = {k % n1, (k / n1) % n1, k / (n1 * n1)};
+  for (int a = 0; a < 3; ++a) r[a] = (a < dim) ? -1.0 + (2.0 / p) * i[a] : 0.0;
+}
+
+// hess: symmetric pairs (a<=b) in order (00,01,11) / (00,01,02,11,12,22)
+void ref_basis_point(int dim, int p, const double* xi, double* val, double* grad,
+                     double* hess) {
+  double v[3][3], d[3][3], dd[3][3];
+  for (int a = 0; a < dim; ++a) line_basis(p, xi[a], v[a], d[a], dd[a]);
+  int n1 = p + 1;
+  int nloc = dim == 2 ? n1 * n1 : n1 * n1 * n1;
+  for (int k = 0; k < nloc; ++k) {
+    int i[3] = {k % n1, (k / n1) % n1, k / (n1 * n1)};
+    // per direction: value, first, second derivative
+    auto f = [&](int a, int order) {
+      return order == 0 ? v[a][i[a]] : order == 1 ? d[a][i[a]] : dd[a][i[a]];
+    };
+    auto prod = [&](int o0, int o1, int o2) {
+      double r = f(0, o0) * f(1, o1);
+      if (dim == 3) r *= f(2, o2);
+      return r;
+    };
+    if (val) val[k] = prod(0, 0, 0);
+    if (grad) {
+      grad[0 * nloc + k] = prod(1, 0, 0);
+      grad[1 * nloc + k] = prod(0, 1, 0);
+      if (dim == 3) grad[2 * nloc + k] = prod(0, 0, 1);
+    }
+    if (hess) {
+      int np = dim == 2 ? 3 : 6;
+      int pr = 0;
+      for (int a = 0; a < dim; ++a)
+        for (int b = a; b < dim; ++b) {
+          int o[3] = {0, 0, 0};
+          o[a] += 1;
+          o[b] += 1;
+          hess[pr * nloc + k] = prod(o[0], o[1], o[2]);
+          ++pr;
+        }
+      (void)np;
+    }
+  }
+}
+
+RefTensors make_ref_tensors(int dim, int p) {
+  RefTensors T;
+  T.dim = dim;
+  T.order = p;
+  int n1 = p + 1;
+  T.nloc = dim == 2 ? n1 * n1 : n1 * n1 * n1;
+  T.n_sym = dim == 2 ? 3 : 6;
+  int nl = T.nloc, ns = T.n_sym;
+  T.nterms = ns + dim + 1 + dim + ns * dim;
+  T.R.assign((size_t)T.nterms * nl * nl, 0.0);
+  // Gauss with 4 points per direction integrates every product exactly
+  // (degree <= 4 per direction for Q2), like the reference's rules do.
+  const int nq1 = 4;
+  double x[kMaxQp1], w[kMaxQp1];
+  gauss_legendre(nq1, x, w);
+  int pa[6], pb[6];
+  {
+    int k = 0;
+    for (int a = 0; a < dim; ++a)
+      for (int b = a; b < dim; ++b) { pa[k] = a; pb[k] = b; ++k; }
+  }
+  const int offC = ns, offM = ns + dim, offD = ns + dim + 1, offT = ns + 2 * dim + 1;
+  std::vector<double> val(nl), grad(3 * nl), hess(6 * nl);
+  int nq = dim == 2 ? nq1 * nq1 : nq1 * nq1 * nq1;
+  for (int q = 0; q < nq; ++q) {
+    int qi[3] = {q % nq1, (q / nq1) % nq1, q / (nq1 * nq1)};
+    double xi[3] = {x[qi[0]], x[qi[1]], dim == 3 ? x[qi[2]] : 0.0};
+    double wq = w[qi[0]] * w[qi[1]] * (dim == 3 ? w[qi[2]] : 1.0);
+    ref_basis_point(dim, p, xi, val.data(), grad.data(), hess.data());
+    for (int i = 0; i < nl; ++i)
+      for (int j = 0; j < nl; ++j) {
+        size_t ij = (size_t)i * nl + j;
+        for (int s = 0; s < ns; ++s) {
+          int a = pa[s], b = pb[s];
+          double v = grad[a * nl + i] * grad[b * nl + j];
+          if (a != b) v += grad[b * nl + i] * grad[a * nl + j];
+          T.R[(size_t)s * nl * nl + ij] += wq * v;
+        }
+        for (int a = 0; a < dim; ++a) {
+          T.R[(size_t)(offC + a) * nl * nl + ij] += wq * val[i] * grad[a * nl + j];
+          T.R[(size_t)(offD + a) * nl * nl + ij] += wq * grad[a * nl + i] * val[j];
+        }
+        T.R[(size_t)offM * nl * nl + ij] += wq * val[i] * val[j];
+        for (int s = 0; s < ns; ++s)
+          for (int c = 0; c < dim; ++c)
+            T.R[(size_t)(offT + s * dim + c) * nl * nl + ij] +=
+                wq * grad[c * nl + i] * hess[s * nl + j];
+      }
+  }
+  return T;
+}
+
+RefTables make_ref_tables(int dim, int p, int nqp1) {
+  RefTables t;
+  t.dim = dim;
+  t.order = p;
+  int n1 = p + 1;
+  t.nloc = dim == 2 ? n1 * n1 : n1 * n1 * n1;
+  t.nqp1 = nqp1;
+  t.nqp = dim == 2 ? nqp1 * nqp1 : nqp1 * nqp1 * nqp1;
+  double x[kMaxQp1], w[kMaxQp1];
+  gauss_legendre(nqp1, x, w);
+  t.xi.resize((size_t)t.nqp * 3);
+  t.w.resize(t.nqp);
+  t.val.resize((size_t)t.nqp * t.nloc);
+  t.grad.resize((size_t)t.nqp * dim * t.nloc);
+  for (int q = 0; q < t.nqp; ++q) {
+    int qi[3] = {q % nqp1, (q / nqp1) % nqp1, q / (nqp1 * nqp1)};
+    double xi[3] = {x[qi[0]], x[qi[1]], dim == 3 ? x[qi[2]] : 0.0};
+    t.w[q] = w[qi[0]] * w[qi[1]] * (dim == 3 ? w[qi[2]] : 1.0);
+    for (int a = 0; a < 3; ++a) t.xi[q * 3 + a] = xi[a];
+    ref_basis_point(dim, p, xi, &t.val[(size_t)q * t.nloc],
+                    &t.grad[(size_t)q * dim * t.nloc], nullptr);
+  }
+  return t;
+}
+
+// ---------------------------------------------------------------------------
+// mesh: root grid of M^d unit-cube cells (lexicographic) refined nref times
+// ---------------------------------------------------------------------------
+namespace {
+// refined-cell vertices as means of parent vertices (regular refinement of a
+// quadrangle / hexahedron), and the child cells' vertex lists
+const int kQuadNew[9][4] = {{0}, {1}, {2}, {3}, {0, 1}, {1, 2}, {2, 3}, {3, 0}, {0, 1, 2, 3}};
+const int kQuadNewN[9] = {1, 1, 1, 1, 2, 2, 2, 2, 4};
+const int kQuadChild[4][4] = {{0, 4, 8, 7}, {1, 5, 8, 4}, {2, 6, 8, 5}, {3, 7, 8, 6}};
+const int kHexNew[27][8] = {
+    {0}, {1}, {2}, {3}, {4}, {5}, {6}, {7}, {0, 1}, {1, 2}, {2, 3}, {3, 0},
+    {0, 1, 2, 3}, {1, 5}, {4, 5}, {0, 4}, {0, 4, 5, 1}, {2, 6}, {5, 6},
+    {1, 5, 6, 2}, {3, 7}, {6, 7}, {2, 6, 7, 3}, {7, 4}, {0, 3, 7, 4},
+    {4, 7, 6, 5}, {0, 1, 2, 3, 4, 5, 6, 7}};
+const int kHexNewN[27] = {1, 1, 1, 1, 1, 1, 1, 1, 2, 2, 2, 2, 4, 2,
+                          2, 2, 4, 2, 2, 4, 2, 2, 4, 2, 4, 4, 8};
+const int kHexChild[8][8] = {
+    {0, 8, 12, 11, 15, 16, 26, 24}, {1, 9, 12, 8, 13, 19, 26, 16},
+    {2, 10, 12, 9, 17, 22, 26, 19}, {3, 11, 12, 10, 20, 24, 26, 22},
+    {4, 23, 25, 14, 15, 24, 26, 16}, {5, 14, 25, 18, 13, 16, 26, 19},
+    {6, 18, 25, 21, 17, 19, 26, 22}, {7, 21, 25, 23, 20, 22, 26, 24}};
+}  // namespace
+
+Mesh make_refined_box(int dim, int roots, int nref) {
+  // root cells: roots^dim unit-cube cells in lexicographic order (x fastest),
+  // each with the standard vertex order; It_Finest visits root cells in order
+  // and the refinement tree of each depth-first
+  Mesh m;
+  m.dim = dim;
+  m.nv = dim == 2 ? 4 : 8;
+  m.ncells = dim == 2 ? roots * roots : roots * roots * roots;
+  static const double sq[4][2] = {{0, 0}, {1, 0}, {1, 1}, {0, 1}};
+  static const double cu[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
+                                  {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+  m.verts.resize((size_t)m.ncells * m.nv * dim);
+  for (int c = 0; c < m.ncells; ++c) {
+    int ijk[3] = {c % roots, (c / roots) % roots, c / (roots * roots)};
+    for (int v = 0; v < m.nv; ++v)
+      for (int a = 0; a < dim; ++a) {
+        double corner = dim == 2 ? sq[v][a] : cu[v][a];
+        m.verts[((size_t)c * m.nv + v) * dim + a] = (ijk[a] + corner) / roots;
+      }
+  }
+  for (int r = 0; r < nref; ++r) {
+    int nch = dim == 2 ? 4 : 8, nnew = dim == 2 ? 9 : 27;
+    std::vector<double> out((size_t)m.ncells * nch * m.nv * dim);
+    for (int c = 0; c < m.ncells; ++c) {
+      const double* pv = &m.verts[(size_t)c * m.nv * dim];
+      double nv[27][3];
+      for (int k = 0; k < nnew; ++k) {
+        int n = dim == 2 ? kQuadNewN[k] : kHexNewN[k];
+        for (int a = 0; a < dim; ++a) {
+          double s = 0;
+          for (int q = 0; q < n; ++q) s += pv[(dim == 2 ? kQuadNew[k][q] : kHexNew[k][q]) * dim + a];
+          nv[k][a] = s / n;
+        }
+      }
+      for (int ch = 0; ch < nch; ++ch)
+        for (int v = 0; v < m.nv; ++v) {
+          int id = dim == 2 ? kQuadChild[ch][v] : kHexChild[ch][v];
+          for (int a = 0; a < dim; ++a)
+            out[(((size_t)c * nch + ch) * m.nv + v) * dim + a] = nv[id][a];
+        }
+    }
+    m.verts.swap(out);
+    m.ncells *= nch;
+  }
+  return m;
+}
+
+// ---------------------------------------------------------------------------
+// DOF numbering
+// ---------------------------------------------------------------------------
+int boundary_component(int dim, const double* x) {
+  const double t = 1e-12;
+  if (dim == 2) {
+    if (std::fabs(x[1]) < t) return 0;
+    if (std::fabs(x[0] - 1) < t) return 1;
+    if (std::fabs(x[1] - 1) < t) return 2;
+    if (std::fabs(x[0]) < t) return 3;
+    return -1;
+  }
+  if (std::fabs(x[2]) < t) return 0;
+  if (std::fabs(x[1]) < t) return 1;
+  if (std::fabs(x[0] - 1) < t) return 2;
+  if (std::fabs(x[1] - 1) < t) return 3;
+  if (std::fabs(x[0]) < t) return 4;
+  if (std::fabs(x[2] - 1) < t) return 5;
+  return -1;
+}
+
+static void affine_point(int dim, const double* cv, const double* r, double* x) {
+  // x = v0 + sum_a (r_a + 1)/2 (v_{e_a} - v0), e = (1, 3, 4) (QuadAffin/HexaAffin)
+  const int e[3] = {1, 3, 4};
+  for (int c = 0; c < dim; ++c) {
+    double s = cv[c];
+    for (int a = 0; a < dim; ++a) s += 0.5 * (r[a] + 1.0) * (cv[e[a] * dim + c] - cv[c]);
+    x[c] = s;
+  }
+}
+
+Space make_space(const Mesh& m, int p, int neumann_mask) {
+  Space s;
+  s.dim = m.dim;
+  s.order = p;
+  int n1 = p + 1;
+  s.nloc = m.dim == 2 ? n1 * n1 : n1 * n1 * n1;
+  int dim = m.dim, nl = s.nloc;
+  // lattice resolution from the first cell's edge length (uniform meshes)
+  double h = std::fabs(m.verts[dim] - m.verts[0]) + std::fabs(m.verts[dim + 1] - m.verts[1]);
+  if (dim == 3) h += std::fabs(m.verts[dim + 2] - m.verts[2]);
+  long nres = std::lround(p / h);
+  long n1l = nres + 1;
+  size_t nkeys = dim == 2 ? (size_t)n1l * n1l : (size_t)n1l * n1l * n1l;
+  // class per lattice point: 0 inner, 1 non-Dirichlet boundary, 2 Dirichlet
+  std::vector<int> first(nkeys, -1);
+  std::vector<long> keys((size_t)m.ncells * nl);
+  std::vector<signed char> cls((size_t)m.ncells * nl);
+  for (int c = 0; c < m.ncells; ++c) {
+    const double* cv = &m.verts[(size_t)c * m.nv * dim];
+    for (int k = 0; k < nl; ++k) {
+      double r[3], x[3];
+      local_dof_ref(dim, p, k, r);
+      affine_point(dim, cv, r, x);
+      long key = 0;
+      for (int a = dim - 1; a >= 0; --a) key = key * n1l + std::lround(x[a] * nres);
+      keys[(size_t)c * nl + k] = key;
+      // boundary components this point lies on
+      int cl = 0;
+      const double t = 1e-12;
+      for (int a = 0; a < dim; ++a)
+        for (int side = 0; side < 2; ++side) {
+          if (std::fabs(x[a] - side) >= t) continue;
+          double probe[3] = {0.5, 0.5, 0.5};
+          probe[a] = side;
+          int comp = boundary_component(dim, probe);
+          int t_ = ((neumann_mask >> comp) & 1) ? 1 : 2;
+          cl = std::max(cl, t_);
+        }
+      cls[(size_t)c * nl + k] = (signed char)cl;
+    }
+  }
+  // number representatives by class, in order of first appearance
+  std::vector<int> id(nkeys, -1);
+  int count[3] = {0, 0, 0};
+  std::vector<int> cls_of_key(nkeys, 0);
+  for (size_t i = 0; i < keys.size(); ++i) {
+    long key = keys[i];
+    if (id[key] < 0) {
+      id[key] = count[cls[i]]++;
+      cls_of_key[key] = cls[i];
+    }
+  }
+  int off[3] = {0, count[0], count[0] + count[1]};
+  s.gdof.resize(keys.size());
+  for (size_t i = 0; i < keys.size(); ++i) s.gdof[i] = off[cls_of_key[keys[i]]] + id[keys[i]];
+  s.nactive = count[0] + count[1];
+  s.ndof = s.nactive + count[2];
+  return s;
+}
+
+Pattern make_pattern(const Space& s) {
+  Pattern P;
+  int n = s.ndof, nl = s.nloc;
+  int ncells = (int)(s.gdof.size() / nl);
+  std::vector<int> cnt(n + 1, 0);
+  for (int c = 0; c < ncells; ++c)
+    for (int m = 0; m < nl; ++m) cnt[s.gdof[(size_t)c * nl + m] + 1] += nl;
+  for (int i = 0; i < n; ++i) cnt[i + 1] += cnt[i];
+  std::vector<int> tmp(cnt[n]), fill(n, 0);
+  for (int c = 0; c < ncells; ++c)
+    for (int m = 0; m < nl; ++m) {
+      int r = s.gdof[(size_t)c * nl + m];
+      for (int k = 0; k < nl; ++k) tmp[cnt[r] + fill[r]++] = s.gdof[(size_t)c * nl + k];
+    }
+  P.nrows = n;
+  P.row_ptr.assign(n + 1, 0);
+  P.col.reserve(cnt[n] / 2);
+  for (int r = 0; r < n; ++r) {
+    int* b = tmp.data() + cnt[r];
+    std::sort(b, b + fill[r]);
+    int* e = std::unique(b, b + fill[r]);
+    P.col.insert(P.col.end(), b, e);
+    P.row_ptr[r + 1] = (int)P.col.size();
+  }
+  return P;
+}
+
+// ---------------------------------------------------------------------------
+// grid transfer (fine <- coarse), parent[f] = coarse cell of fine cell f
+// ---------------------------------------------------------------------------
+void make_transfer(const Mesh& fm, const Space& fs, const Mesh& cm, const Space& cs,
+                   const int* parent, HostCsr* P, HostCsr* R) {
+  int dim = fm.dim, nl = fs.nloc, p = fs.order;
+  // child-local interpolation: fine dof k of cell f gets coarse basis l of
+  // parent evaluated at the fine node (nodal functionals are point values)
+  std::vector<std::unordered_map<int, double>> rows(fs.ndof);
+  std::vector<int> mult(fs.ndof, 0);
+  std::vector<double> val(nl);
+  for (int f = 0; f < fm.ncells; ++f) {
+    int c = parent[f];
+    const double* cvf = &fm.verts[(size_t)f * fm.nv * dim];
+    const double* cvc = &cm.verts[(size_t)c * cm.nv * dim];
+    // inverse of the coarse affine map
+    const int e[3] = {1, 3, 4};
+    double J[3][3], Ji[3][3], x0[3];
+    for (int r = 0; r < dim; ++r)
+      for (int a = 0; a < dim; ++a) J[r][a] = 0.5 * (cvc[e[a] * dim + r] - cvc[r]);
+    for (int r = 0; r < dim; ++r) {
+      double s = cvc[r];
+      for (int a = 0; a < dim; ++a) s += J[r][a];
+      x0[r] = s;
+    }
+    if (dim == 2) {
+      double det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+      Ji[0][0] = J[1][1] / det; Ji[0][1] = -J[0][1] / det;
+      Ji[1][0] = -J[1][0] / det; Ji[1][1] = J[0][0] / det;
+    } else {
+      double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+                   J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                   J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          int i1 = (j + 1) % 3, i2 = (j + 2) % 3, j1 = (i + 1) % 3, j2 = (i + 2) % 3;
+          Ji[i][j] = (J[i1][j1] * J[i2][j2] - J[i1][j2] * J[i2][j1]) / det;
+        }
+    }
+    for (int k = 0; k < nl; ++k) {
+      double r[3], x[3], xi[3] = {0, 0, 0};
+      local_dof_ref(dim, p, k, r);
+      affine_point(dim, cvf, r, x);
+      for (int a = 0; a < dim; ++a) {
+        double t = 0;
+        for (int rr = 0; rr < dim; ++rr) t += Ji[a][rr] * (x[rr] - x0[rr]);
+        xi[a] = t;
+      }
+      ref_basis_point(dim, p, xi, val.data(), nullptr, nullptr);
+      int fi = fs.gdof[(size_t)f * nl + k];
+      mult[fi] += 1;
+      for (int l = 0; l < nl; ++l) {
+        if (val[l] == 0.0) continue;
+        rows[fi][cs.gdof[(size_t)c * nl + l]] += val[l];
+      }
+    }
+  }
+  // averaged prolongation (all fine rows) and its transpose (all coarse
+  // rows); the multigrid masks non-active rows in the transfer kernels
+  P->nrows = fs.ndof;
+  P->ncols = cs.ndof;
+  P->row_ptr.assign(fs.ndof + 1, 0);
+  P->col.clear();
+  P->val.clear();
+  std::vector<std::vector<std::pair<int, double>>> Rrows(cs.ndof);
+  for (int i = 0; i < fs.ndof; ++i) {
+    std::vector<std::pair<int, double>> e(rows[i].begin(), rows[i].end());
+    std::sort(e.begin(), e.end());
+    for (auto& kv : e) {
+      double v = kv.second / mult[i];
+      P->col.push_back(kv.first);
+      P->val.push_back(v);
+      Rrows[kv.first].push_back({i, v});
+    }
+    P->row_ptr[i + 1] = (int)P->col.size();
+  }
+  R->nrows = cs.ndof;
+  R->ncols = fs.ndof;
+  R->row_ptr.assign(cs.ndof + 1, 0);
+  R->col.clear();
+  R->val.clear();
+  for (int j = 0; j < cs.ndof; ++j) {
+    for (auto& kv : Rrows[j]) {
+      R->col.push_back(kv.first);
+      R->val.push_back(kv.second);
+    }
+    R->row_ptr[j + 1] = (int)R->col.size();
+  }
+}
+
+}  // namespace cdg

@@ -1,0 +1,77 @@
+"""Host setup layer of the library (no GPU): meshes, DOF numbering and CSR
+patterns must equal the oracle's restatement of the reference's
+ConstructSpace marker algorithm (src/FE/FESpace2D.C:83-312,
+FEMapper.C:456-600, FESpace.C:1863-2099) and TStructure
+(src/Matrix/Structure.C:226-618) bit for bit; the C-ABI library must load
+without a GPU and export every symbol include/parmoon_cd.h declares."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import parmoon2022_gb300 as pg
+import pyoracle as po
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.mark.parametrize("dim,order,nref,nmask", [
+    (2, 1, 3, 0), (2, 2, 3, 0), (2, 1, 2, 2), (2, 2, 3, 2), (2, 2, 4, 0b1010),
+    (3, 1, 2, 0), (3, 2, 2, 0), (3, 2, 3, 0), (3, 1, 2, 4), (3, 2, 2, 0b100001),
+])
+def test_mesh_dofs_pattern_bit_exact(built, dim, order, nref, nmask):
+    h = pg.Hierarchy(dim, order, nref, n_levels=2, neumann_mask=nmask)
+    o = po.Problem(po.make_config(dim, order, nref, po.EX_SINE, neumann_mask=nmask), 2)
+    for lvl in range(2):
+        assert h.info(lvl)["ndof"] == o.info(lvl)["ndof"]
+        assert h.info(lvl)["nactive"] == o.info(lvl)["nactive"]
+        assert np.array_equal(h.mesh(lvl), o.mesh(lvl))
+        assert np.array_equal(h.dofs(lvl), o.dofs(lvl) if hasattr(o, "dofs") else o.gdof(lvl))
+        rp1, c1 = h.pattern(lvl)
+        rp2, c2 = o.structure(lvl)
+        assert np.array_equal(rp1, rp2) and np.array_equal(c1, c2)
+
+
+def test_config_sizes(built):
+    # 64x64 Q1: 4225 DOFs, 3969 active, nnz (3N+1)^2 (configs' CD2D case)
+    h = pg.Hierarchy(2, 1, 6)
+    i = h.info()
+    assert (i["ndof"], i["nactive"], i["nnz"]) == (4225, 3969, 193 ** 2)
+    # 32^3 Q2: 274625 DOFs, nnz (8N+1)^3
+    h = pg.Hierarchy(3, 2, 5)
+    i = h.info()
+    assert (i["ndof"], i["nnz"]) == (274625, 257 ** 3)
+
+
+def test_root_grid_hierarchy(built):
+    # 3 roots per direction refined twice: 12^3 cells, parent(f) = f // 8
+    h = pg.Hierarchy(3, 1, 2, n_levels=3, roots=3)
+    assert h.info(0)["ncells"] == 12 ** 3 and h.info(2)["ncells"] == 27
+    fine, coarse = h.mesh(0), h.mesh(1)
+    ctr_f = fine.mean(axis=1)
+    lo, hi = coarse.min(axis=1), coarse.max(axis=1)
+    par = np.arange(len(fine)) // 8
+    assert np.all((ctr_f >= lo[par]) & (ctr_f <= hi[par]))
+
+
+def test_abi_exports_every_declared_symbol(built):
+    L = ctypes.CDLL(pg.LIB_PATH)
+    hdr = open(os.path.join(ROOT, "include", "parmoon_cd.h")).read()
+    declared = set(re.findall(r"^\s*(?:const char \*|int|long long)\s*(cdg_\w+)\(", hdr, re.M))
+    assert declared == set(pg.EXPORTED)
+    for name in declared:
+        assert hasattr(L, name), name
+
+
+def test_no_device_is_reported_not_faked(built):
+    # without a GPU the library reports CDG_ERR_NO_DEVICE instead of running
+    # anything on the CPU
+    import subprocess
+    code = ("import parmoon2022_gb300 as pg\n"
+            "try:\n pg.Context(0)\nexcept pg.CdgError as e:\n print('ERR', e.code)\n"
+            "else:\n print('OK')\n")
+    out = subprocess.run(["python", "-c", code], capture_output=True, text=True, cwd=ROOT,
+                         env=dict(os.environ, CUDA_VISIBLE_DEVICES=""))
+    assert "ERR -9" in out.stdout, out.stdout + out.stderr
