@@ -110,6 +110,9 @@ int cdg_context_destroy(cdg_context *ctx);
 int cdg_context_synchronize(cdg_context *ctx);
 /* number of kernel launches the context issued since creation */
 long long cdg_context_launch_count(const cdg_context *ctx);
+/* the context's CUDA stream (a cudaStream_t), for callers that order their
+ * own work or record timing events against the library's launches */
+int cdg_context_stream(cdg_context *ctx, void **stream);
 
 /* ---- host setup layer (no GPU) ------------------------------------------ */
 /* TDomain(unit square/cube split into roots^dim cells) refined nref times,
@@ -188,6 +191,17 @@ int cdg_problem_restrict(cdg_problem *p, int fine_level, const double *df,
  * Iteration_jacobi::apply) */
 int cdg_problem_precondition(cdg_problem *p, const cdg_solver_params *s,
                              const double *v, double *z);
+
+/* ---- measurement -------------------------------------------------------- */
+/* average device time (ms) of one launch of a hot kernel on `level`, from
+ * CUDA events around `reps` back-to-back launches on the context stream.
+ * kernel: 0 multigrid Jacobi smoothing step in FP32 (x' = x + w D^-1 (b-Ax)),
+ *         1 FP64 operator SpMV (y = A x),
+ *         2 element contraction + CSR scatter of the matrix (FP64),
+ *         3 FP32 defect (d = b - A x).
+ * Kernel 2 re-assembles the level afterwards (a is required for it). */
+int cdg_problem_time_kernel(cdg_problem *p, const cdg_assembly_params *a,
+                            int kernel, int level, int reps, double *ms);
 
 #ifdef __cplusplus
 }

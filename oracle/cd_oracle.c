@@ -239,6 +239,7 @@ typedef struct {
   double *mg_rhs, *mg_sol, *mg_def;
   double *lu;       /* dense LU of the coarse matrix (coarsest level only) */
   int *piv;
+  int lu_gen;       /* assembly generation the LU belongs to */
 } level_t;
 
 struct orc_problem {
@@ -247,6 +248,7 @@ struct orc_problem {
   level_t *lev;
   quad_rule qr;
   int nqp1;
+  int asm_gen;      /* incremented by every orc_assemble */
 };
 
 static int nverts(int dim) { return dim == 2 ? 4 : 8; }
@@ -1186,6 +1188,7 @@ static int assemble_level(orc_problem *p, int level) {
 }
 
 int orc_assemble(orc_problem *p) {
+  p->asm_gen++;
   for (int k = 0; k < p->nlev; ++k)
     if (assemble_level(p, k)) return -1;
   return 0;
@@ -1396,6 +1399,11 @@ int orc_mg_apply(orc_problem *p, const orc_solver_config *s, const double *v,
   int nl = s->mg_levels;
   if (nl < 1 || nl > p->nlev) FAIL("bad multigrid level count");
   level_t *fine = &p->lev[0];
+  level_t *crs = &p->lev[nl - 1];
+  if (s->coarse_direct && (crs->lu == NULL || crs->lu_gen != p->asm_gen)) {
+    if (coarse_factor(crs)) return -1;
+    crs->lu_gen = p->asm_gen;
+  }
   memcpy(fine->mg_rhs, v, sizeof(double) * fine->ndof);
   /* finest start: 0, non-actives copied from rhs */
   memset(fine->mg_sol, 0, sizeof(double) * fine->ndof);
@@ -1523,7 +1531,11 @@ int orc_solve(orc_problem *p, const orc_solver_config *s, int *iters,
     for (int k = 0; k < s->mg_levels; ++k)
       for (int r = 0; r < p->lev[k].ndof; ++r)
         if (p->lev[k].diag[r] == 0) FAIL("zero diagonal entry");
-    if (s->coarse_direct && coarse_factor(&p->lev[s->mg_levels - 1])) return -1;
+    level_t *crs = &p->lev[s->mg_levels - 1];
+    if (s->coarse_direct) {
+      if (coarse_factor(crs)) return -1;
+      crs->lu_gen = p->asm_gen;
+    }
   } else if (s->precond == 1) {
     for (int r = 0; r < n; ++r)
       if (L->diag[r] == 0) FAIL("zero entry on the diagonal using Jacobi");

@@ -38,7 +38,7 @@ EXPORTED = [
     "cdg_problem_level_info", "cdg_problem_get_matrix", "cdg_problem_get_rhs",
     "cdg_problem_get_solution", "cdg_problem_set_solution", "cdg_problem_get_slots",
     "cdg_problem_apply", "cdg_problem_prolongate", "cdg_problem_restrict",
-    "cdg_problem_precondition",
+    "cdg_problem_precondition", "cdg_context_stream", "cdg_problem_time_kernel",
 ]
 
 
@@ -119,6 +119,9 @@ def lib():
             "cdg_problem_prolongate": [P, ctypes.c_int, dp, dp],
             "cdg_problem_restrict": [P, ctypes.c_int, dp, dp],
             "cdg_problem_precondition": [P, ctypes.POINTER(SolverParams), dp, dp],
+            "cdg_context_stream": [P, PP],
+            "cdg_problem_time_kernel": [P, ctypes.POINTER(AssemblyParams), ctypes.c_int,
+                                        ctypes.c_int, ctypes.c_int, dp],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -237,6 +240,12 @@ class Context:
 
     def launches(self):
         return int(lib().cdg_context_launch_count(self.c))
+
+    def stream(self):
+        """The library's cudaStream_t as an integer handle."""
+        s = ctypes.c_void_p()
+        _chk(lib().cdg_context_stream(self.c, ctypes.byref(s)))
+        return int(s.value or 0)
 
     def close(self):
         if getattr(self, "c", None):
@@ -364,6 +373,14 @@ class ConvectionDiffusion:
         rc = np.zeros(self.info(fine_level + 1)["ndof"])
         _chk(lib().cdg_problem_restrict(self.p, fine_level, _dp(df), _dp(rc)))
         return rc
+
+    def time_kernel(self, kernel, a=None, level=0, reps=20):
+        """Average ms per launch of a hot kernel (0 FP32 Jacobi smoothing step,
+        1 FP64 SpMV, 2 element contraction + scatter, 3 FP32 defect)."""
+        ms = np.zeros(1)
+        _chk(lib().cdg_problem_time_kernel(self.p, ctypes.byref(a) if a is not None else None,
+                                           kernel, level, reps, _dp(ms)))
+        return float(ms[0])
 
     def precondition(self, s, v):
         v = np.ascontiguousarray(v, dtype=np.float64)

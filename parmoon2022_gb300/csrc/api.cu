@@ -87,6 +87,12 @@ int cdg_context_synchronize(cdg_context* c) {
 
 long long cdg_context_launch_count(const cdg_context* c) { return c ? c->launches : -1; }
 
+int cdg_context_stream(cdg_context* c, void** stream) {
+  if (!c || !stream) { set_error("null argument"); return CDG_ERR_ARG; }
+  *stream = (void*)c->stream;
+  return CDG_OK;
+}
+
 // ---------------------------------------------------------------------------
 // host setup hierarchy
 // ---------------------------------------------------------------------------
@@ -525,6 +531,51 @@ int cdg_problem_precondition(cdg_problem* p, const cdg_solver_params* s, const d
   CDG_TRY(precondition(p->ctx, p, *s, dv.d, dz.d));
   CDG_TRY(d2h(p->ctx, z, dz.d, (size_t)F.ndof * sizeof(double)));
   return check_device_error(p->ctx);
+}
+
+// ---------------------------------------------------------------------------
+// measurement
+// ---------------------------------------------------------------------------
+int cdg_problem_time_kernel(cdg_problem* p, const cdg_assembly_params* a, int kernel, int level,
+                            int reps, double* ms) {
+  DevLevel* L = get_level(p, level);
+  if (!L || !ms || reps < 1 || kernel < 0 || kernel > 3 || (kernel == 2 && !a)) {
+    set_error("bad arguments");
+    return CDG_ERR_ARG;
+  }
+  cdg_context* ctx = p->ctx;
+  cudaEvent_t e0, e1;
+  CDG_CUDA(cudaEventCreate(&e0));
+  CDG_CUDA(cudaEventCreate(&e1));
+  auto once = [&]() -> int {
+    switch (kernel) {
+      case 0: return smooth32_once(ctx, *L, 0.8f);
+      case 1: return spmv_apply64(ctx, *L, L->sol, L->invdiag64);
+      case 2: return contract_only(ctx, p, *L, *a);
+      default: return defect32_once(ctx, *L);
+    }
+  };
+  // scratch target of the FP64 SpMV: invdiag64 is restored below
+  int rc = once();  // warm-up (allocates multigrid vectors if needed)
+  if (rc == CDG_OK) {
+    CDG_CUDA(cudaEventRecord(e0, ctx->stream));
+    for (int r = 0; r < reps && rc == CDG_OK; ++r) rc = once();
+    CDG_CUDA(cudaEventRecord(e1, ctx->stream));
+    CDG_CUDA(cudaEventSynchronize(e1));
+    float t = 0;
+    CDG_CUDA(cudaEventElapsedTime(&t, e0, e1));
+    *ms = (double)t / reps;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc != CDG_OK) return rc;
+  if (kernel == 1 || kernel == 2) {
+    // restore the level's matrix data (the timing loop overwrote them)
+    if (!a) { set_error("assembly parameters needed to restore the level"); return CDG_ERR_ARG; }
+    CDG_TRY(assemble_level(ctx, p, *L, *a));
+    CDG_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
+  return CDG_OK;
 }
 
 }  // extern "C"

@@ -774,6 +774,18 @@ static int get_rhs_tables(cdg_context* ctx, int dim, int order, int nqp1, RhsTab
   return CDG_OK;
 }
 
+int contract_only(cdg_context* ctx, cdg_problem* p, DevLevel& L, const cdg_assembly_params& a) {
+  CDG_TRY(ensure_tables(ctx, p));
+  AsmCoefs k = make_coefs(a, L.dim, L.order, L.nloc);
+  const double* R = p->d_tables;
+  if (L.dim == 2 && L.nloc == 4) return launch_contract<2, 4, 14>(ctx, k, L, R);
+  if (L.dim == 2 && L.nloc == 9) return launch_contract<2, 9, 14>(ctx, k, L, R);
+  if (L.dim == 3 && L.nloc == 8) return launch_contract<3, 8, 31>(ctx, k, L, R);
+  if (L.dim == 3 && L.nloc == 27) return launch_contract<3, 27, 31>(ctx, k, L, R);
+  set_error("unsupported element");
+  return CDG_ERR_ARG;
+}
+
 int assemble_level(cdg_context* ctx, cdg_problem* p, DevLevel& L, const cdg_assembly_params& a) {
   CDG_TRY(ensure_tables(ctx, p));
   AsmCoefs k = make_coefs(a, L.dim, L.order, L.nloc);

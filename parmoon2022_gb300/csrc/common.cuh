@@ -174,5 +174,10 @@ int precondition(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s,
 int prepare_solver(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s);
 int fgmres(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s,
            cdg_solve_stats* st);
+// single hot-kernel launches for measurement
+int smooth32_once(cdg_context* ctx, DevLevel& L, float damp);
+int defect32_once(cdg_context* ctx, DevLevel& L);
+int ensure_mg_vectors(cdg_context* ctx, DevLevel& L, int elem);
+int contract_only(cdg_context* ctx, cdg_problem* p, DevLevel& L, const cdg_assembly_params& a);
 
 }  // namespace cdg

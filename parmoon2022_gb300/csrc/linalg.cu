@@ -481,6 +481,29 @@ static int mg_cycle(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s
   return CDG_OK;
 }
 
+int ensure_mg_vectors(cdg_context* ctx, DevLevel& L, int elem) {
+  if (L.mg_elem == elem) return CDG_OK;
+  void** bufs[4] = {&L.mg_rhs, &L.mg_sol, &L.mg_tmp, &L.mg_def};
+  for (void** b : bufs) {
+    if (*b) cudaFree(*b);
+    *b = nullptr;
+    CDG_CUDA(cudaMalloc(b, (size_t)std::max(L.ndof, 1) * elem));
+    CDG_CUDA(cudaMemsetAsync(*b, 0, (size_t)std::max(L.ndof, 1) * elem, ctx->stream));
+  }
+  L.mg_elem = elem;
+  return CDG_OK;
+}
+
+int smooth32_once(cdg_context* ctx, DevLevel& L, float damp) {
+  CDG_TRY(ensure_mg_vectors(ctx, L, (int)sizeof(float)));
+  return smooth<float>(ctx, L, damp);
+}
+
+int defect32_once(cdg_context* ctx, DevLevel& L) {
+  CDG_TRY(ensure_mg_vectors(ctx, L, (int)sizeof(float)));
+  return defect<float>(ctx, L);
+}
+
 int prepare_solver(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s) {
   CDG_TRY(check_device_error(ctx));
   if (s.preconditioner != 0) {
@@ -501,18 +524,7 @@ int prepare_solver(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s)
     return CDG_ERR_ARG;
   }
   const int elem = s.precision == 1 ? (int)sizeof(float) : (int)sizeof(double);
-  for (int k = 0; k < nl; ++k) {
-    DevLevel& L = p->lev[k];
-    if (L.mg_elem != elem) {
-      void** bufs[4] = {&L.mg_rhs, &L.mg_sol, &L.mg_tmp, &L.mg_def};
-      for (void** b : bufs) {
-        if (*b) cudaFree(*b);
-        CDG_CUDA(cudaMalloc(b, (size_t)std::max(L.ndof, 1) * elem));
-        CDG_CUDA(cudaMemsetAsync(*b, 0, (size_t)std::max(L.ndof, 1) * elem, ctx->stream));
-      }
-      L.mg_elem = elem;
-    }
-  }
+  for (int k = 0; k < nl; ++k) CDG_TRY(ensure_mg_vectors(ctx, p->lev[k], elem));
   if (s.multigrid_smoother_coarse == 0) {
     CDG_TRY(coarse_inverse(ctx, p->lev[nl - 1]));
     CDG_TRY(check_device_error(ctx));
