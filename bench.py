@@ -1,0 +1,416 @@
+"""Benchmark of the GB300 CD hot path (one JSON line on rank 0).
+
+Workload (the precision configuration of the reference's CD3D path): CD3D on
+the unit cube, 32^3 hexahedra, Q2 (274,625 DOFs), eps=1e-3,
+b=(1,1,1)/sqrt(3), c=0, SUPG with delta = h/(2|b|) (SDFEM_TYPE 5, h = edge
+length), manufactured u = x y z (1-x)(1-y)(1-z) exp(x), 3x3x3 Gauss
+quadrature.  One step = ConvectionDiffusion::assemble (all 4 multigrid
+levels) + Solver::solve: FGMRES(30) in FP64 preconditioned by a 4-level
+geometric multigrid V(2,2) with damped Jacobi (omega=0.8) in FP32 and an FP64
+dense coarse solve, to a relative residual of 1e-10.  The all-FP64 run of the
+same solve is measured beside it.  Synthetic data only (generated mesh and
+manufactured solution; no dataset).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the CPU restatement of the reference's algorithm
+(oracle/, per-quadrature-point assembly with row-search scatter, FP64
+multigrid) on all host cores, one solve per core per step.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_CELLS_1D = 32            # 32^3 hexahedra = unit cube refined 5 times
+NREF, LEVELS, ORDER, DIM = 5, 4, 2, 3
+EPS, B, C = 1e-3, (1 / np.sqrt(3.0),) * 3, 0.0
+WORKLOAD = "CD3D 32^3 Q2 SUPG eps=1e-3 b=(1,1,1)/sqrt3 c=0, FGMRES(30)+MG V(2,2) 4 levels to 1e-10"
+METRIC = "CD solves/s, p50/p99 latency, mixed vs FP64 GPU at 1e-10 res; assembly GDOF/s"
+
+
+def assembly_kw():
+    return dict(eps=EPS, b=B, c=C, supg=True, sdfem_type=5, delta0=1.0, cell_measure=2,
+                problem_linear=1)
+
+
+def solver_kw():
+    return dict(max_n_iterations=1000, gmres_restart=30, residual_tolerance=0.0,
+                residual_reduction=1e-10, multigrid_n_levels=LEVELS, multigrid_cycle_type="V",
+                multigrid_n_pre_smooth=2, multigrid_n_post_smooth=2, jacobi_damp=0.8,
+                multigrid_correction_damp_factor=1.0, multigrid_smoother_coarse="direct_solve")
+
+
+# ---------------------------------------------------------------------------
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def init_dist(world):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    dist.init_process_group("gloo")
+    return dist
+
+
+def max_over_ranks(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu, self.proc, self.lines = gpu, None, []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.gpu)], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm():
+    try:
+        d = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profile_traffic(kernel_tag):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu
+    summary (profiles/*.md line 'traffic_bytes_per_launch <tag> <bytes>')."""
+    pdir = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(pdir):
+        return None
+    for fn in sorted(os.listdir(pdir)):
+        if not fn.endswith((".md", ".txt")):
+            continue
+        for ln in open(os.path.join(pdir, fn)):
+            f = ln.split()
+            if len(f) >= 3 and f[0] == "traffic_bytes_per_launch" and f[1] == kernel_tag:
+                try:
+                    return float(f[2])
+                except ValueError:
+                    pass
+    return None
+
+
+# ---------------------------------------------------------------------------
+def run_gpu(args):
+    import torch
+    import parmoon2022_gb300 as pg
+    rank, world, local = dist_env()
+    dist = init_dist(world)
+    torch.cuda.set_device(local)
+    ctx = pg.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=local)
+    hier = pg.Hierarchy(DIM, ORDER, NREF, n_levels=LEVELS)
+    cd = pg.ConvectionDiffusion(ctx, hier)
+    a = pg.assembly_params(example=pg.EX_POLYEXP, space_discretization_type="supg",
+                           **{k: v for k, v in assembly_kw().items() if k != "supg"})
+    s_mixed = pg.solver_params("multigrid", precision="mixed", **solver_kw())
+    s_fp64 = pg.solver_params("multigrid", precision="fp64", **solver_kw())
+    info = [cd.info(l) for l in range(LEVELS)]
+    n = info[0]["ndof"]
+
+    def step(s):
+        cd.set_solution(None)   # start iterate 0 on the device (assemble sets Dirichlet values)
+        cd.assemble(a)
+        return cd.solve(s)
+
+    def timed(s, k, w):
+        for _ in range(w):
+            step(s)
+        barrier(dist)
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(k)]
+        l0 = ctx.launches()
+        t0 = time.perf_counter()
+        stats = []
+        for i in range(k):
+            ev[i][0].record(stream)
+            stats.append(step(s))
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        barrier(dist)
+        per = [e0.elapsed_time(e1) for e0, e1 in ev]
+        return per, stats, ctx.launches() - l0, wall
+
+    zero = np.zeros(n)
+    cd.set_solution(zero)
+    if args.profile:
+        # one mixed step between cudaProfilerStart/Stop (ncu --profile-from-start off)
+        for _ in range(2):
+            step(s_mixed)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        l0 = ctx.launches()
+        st = step(s_mixed)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
+        print(json.dumps({"profile_step": True, "launches": ctx.launches() - l0,
+                          "iterations": st.iterations}))
+        return
+    # headline: mixed precision, inputs resident in HBM
+    clocks = ClockSampler(local)
+    clocks.start()
+    per_m, st_m, launches, wall_m = timed(s_mixed, args.steps, args.warmup)
+    clk = clocks.stop()
+    err_m = cd.errors(a)
+    x_m = cd.solution()
+    # side by side: all-FP64 GPU solve of the same problem
+    per_d, st_d, _, _ = timed(s_fp64, max(2, min(args.steps, 5)), 1)
+    err_d = cd.errors(a)
+    x_d = cd.solution()
+    # assembly only (all levels, FP64)
+    for _ in range(2):
+        cd.assemble(a)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ka = max(3, args.steps)
+    e0.record(stream)
+    for _ in range(ka):
+        cd.assemble(a)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_asm = e0.elapsed_time(e1) / ka / 1e3
+    dofs_all = sum(i["ndof"] for i in info)
+    # e2e: the reference-facing call with host buffers (pinned), copies inside
+    sol_in = torch.zeros(n, dtype=torch.float64).pin_memory()
+    sol_out = torch.empty(n, dtype=torch.float64).pin_memory()
+    import ctypes
+    dp = ctypes.POINTER(ctypes.c_double)
+    nul = dp()
+
+    def e2e_step():
+        st = pg.SolveStats()
+        pg._chk(pg.lib().cdg_problem_assemble_solve(
+            cd.p, ctypes.byref(a), ctypes.byref(s_mixed),
+            ctypes.cast(sol_in.data_ptr(), dp), nul, ctypes.cast(sol_out.data_ptr(), dp),
+            ctypes.byref(st)))
+        return st
+    for _ in range(args.warmup):
+        e2e_step()
+    barrier(dist)
+    torch.cuda.synchronize()
+    te = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    t_e2e = max_over_ranks(dist, (time.perf_counter() - te) / args.steps)
+    # dominant kernel: the FP32 Jacobi smoothing SpMV of the finest level
+    ms_smooth = cd.time_kernel(0, a, level=0, reps=50)
+    ms_spmv64 = cd.time_kernel(1, a, level=0, reps=50)
+    ms_contract = cd.time_kernel(2, a, level=0, reps=5)
+    nnz0 = info[0]["nnz"]
+    bytes_smooth = 8 * nnz0 + 4 * (n + 1) + 4 * 4 * n          # val+col, row_ptr, x,b,invd,y
+    bytes_spmv64 = 12 * nnz0 + 4 * (n + 1) + 8 * 2 * n
+    peak, peak_kind = measured_peak_hbm()
+    achieved = bytes_smooth / (ms_smooth * 1e-3) / 1e9
+    traffic = profile_traffic("k_spmv_f32_jacobi_q2_32")
+
+    t_step_m = max_over_ranks(dist, sum(per_m) / len(per_m) / 1e3)
+    t_step_d = max_over_ranks(dist, sum(per_d) / len(per_d) / 1e3)
+    value = world / t_step_m
+    if rank != 0:
+        return
+    cpu = cpu_baseline_sample() if not args.skip_cpu else None
+    rel = float(np.max(np.abs(x_m - x_d)) / np.max(np.abs(x_d)))
+    line = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step_m * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 FGMRES + f32 multigrid (mixed)", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "dofs": n, "nnz": nnz0,
+                   "levels_dofs": [i["ndof"] for i in info], "quadrature": "3x3x3 Gauss",
+                   "sdfem": "type 5, delta=h/(2|b|), h=edge length",
+                   "l2": "working set > L2 (finest CSR alone %.0f MB); no flush" % (nnz0 * 16 / 1e6),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "p50_ms": statistics.median(per_m), "p99_ms": float(np.percentile(per_m, 99)),
+        "iterations": st_m[-1].iterations,
+        "rel_residual": st_m[-1].residual / st_m[-1].initial_residual,
+        "errors": {"L2": err_m[0], "H1_semi": err_m[1], "L2_fp64": err_d[0],
+                   "H1_semi_fp64": err_d[1], "solution_rel_diff_vs_fp64": rel},
+        "fp64": {"value": world / t_step_d, "ms_per_step": t_step_d * 1e3,
+                 "iterations": st_d[-1].iterations},
+        "mixed_over_fp64": t_step_d / t_step_m,
+        "assembly_gdofs": dofs_all / t_asm / 1e9,
+        "assembly_ms": t_asm * 1e3,
+        "kernels_ms": {"jacobi_smooth_f32_L0": ms_smooth, "spmv_f64_L0": ms_spmv64,
+                       "element_contract_f64_L0": ms_contract},
+        "roofline": {"bound": "hbm", "kernel": "k_spmv<float,32,2> (Jacobi smoothing, finest)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     "algorithmic_bytes": bytes_smooth,
+                     "traffic": traffic},
+        "cpu_baseline": cpu,
+        "e2e": {"value": world / t_e2e, "unit": "solves/s",
+                "h2d_bytes_per_step": 8 * n + 2 * 136,
+                "d2h_bytes_per_step": 8 * n + 8 * 4},
+        "clocks": clk,
+        "gpu_launches": launches,
+    }
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------------------
+def oracle_solve_once():
+    """One C2 assemble + solve by the CPU oracle (reference algorithm)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    kw = assembly_kw()
+    cfg = po.make_config(DIM, ORDER, NREF, po.EX_POLYEXP, eps=kw["eps"], b=kw["b"], c=kw["c"],
+                         supg=True, sdfem_type=kw["sdfem_type"], delta0=kw["delta0"],
+                         cell_measure=kw["cell_measure"], problem_linear=kw["problem_linear"])
+    p = po.Problem(cfg, LEVELS)
+    t0 = time.perf_counter()
+    p.assemble()
+    t1 = time.perf_counter()
+    it, res, ini = p.solve(po.make_solver("multigrid", max_it=1000, restart=30, tol_abs=0.0,
+                                          reduction=1e-10, mg_levels=LEVELS, mg_cycle="V",
+                                          n_pre=2, n_post=2, jacobi_damp=0.8,
+                                          correction_damp=1.0, coarse_direct=True))
+    t2 = time.perf_counter()
+    return t2 - t0, t1 - t0, it
+
+
+def cpu_baseline_sample():
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    po.build()
+    t, t_asm, it = oracle_solve_once()
+    return {"value": 1.0 / t, "unit": "solves/s", "cores": 1, "kind": "port",
+            "sample": "one full solve (assemble 4 levels %.1f s + FGMRES/MG %d its) of the same "
+                      "workload by the C restatement of the reference, 1 thread" % (t_asm, it)}
+
+
+def _worker(q):
+    q.put(oracle_solve_once()[0])
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import multiprocessing as mp
+    import pyoracle as po
+    po.build()
+    cores = os.cpu_count() or 1
+    ctxm = mp.get_context("spawn")
+    # each step: every core solves one instance; bounded to keep the run short
+    steps = max(1, min(args.steps, 3))
+    warm = 1 if args.warmup > 0 else 0
+    times = []
+    for i in range(warm + steps):
+        q = ctxm.Queue()
+        procs = [ctxm.Process(target=_worker, args=(q,)) for _ in range(cores)]
+        t0 = time.perf_counter()
+        for pr in procs:
+            pr.start()
+        for pr in procs:
+            pr.join()
+        dt = time.perf_counter() - t0
+        if i >= warm:
+            times.append(dt)
+    t = sum(times) / len(times)
+    value = cores / t
+    print(json.dumps({
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+        "steps": steps, "warmup": warm, "ms_per_step": t * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "impl": "reference",
+        "config": {"workload": WORKLOAD, "dofs": 274625},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
+                         "sample": "each step: %d concurrent full solves (one per host core) by "
+                                   "the C restatement of the reference; steps capped at 3" % cores},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU-baseline sample")
+    ap.add_argument("--profile", action="store_true",
+                    help="run one bracketed step for an ncu capture and exit")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl != "reference":
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

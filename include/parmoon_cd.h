@@ -174,6 +174,7 @@ int cdg_problem_level_info(const cdg_problem *p, int level, int *info);
 int cdg_problem_get_matrix(cdg_problem *p, int level, double *values);
 int cdg_problem_get_rhs(cdg_problem *p, int level, double *rhs);
 int cdg_problem_get_solution(cdg_problem *p, double *sol);
+/* sol == NULL sets the solution to zero on the device */
 int cdg_problem_set_solution(cdg_problem *p, const double *sol);
 /* CSR slot of every local coupling: slots[cell*nloc*nloc + i*nloc + j] */
 int cdg_problem_get_slots(cdg_problem *p, int level, int *slots);

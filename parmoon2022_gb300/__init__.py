@@ -347,6 +347,10 @@ class ConvectionDiffusion:
         return v
 
     def set_solution(self, x):
+        """Host vector, or None to zero the solution on the device."""
+        if x is None:
+            _chk(lib().cdg_problem_set_solution(self.p, ctypes.POINTER(ctypes.c_double)()))
+            return
         x = np.ascontiguousarray(x, dtype=np.float64)
         _chk(lib().cdg_problem_set_solution(self.p, _dp(x)))
 

@@ -460,9 +460,12 @@ int cdg_problem_get_solution(cdg_problem* p, double* v) {
 }
 int cdg_problem_set_solution(cdg_problem* p, const double* v) {
   DevLevel* L = get_level(p, 0);
-  if (!L || !v) return CDG_ERR_ARG;
-  CDG_CUDA(cudaMemcpyAsync(L->sol, v, (size_t)L->ndof * sizeof(double), cudaMemcpyHostToDevice,
-                           p->ctx->stream));
+  if (!L) return CDG_ERR_ARG;
+  if (!v)
+    CDG_CUDA(cudaMemsetAsync(L->sol, 0, (size_t)L->ndof * sizeof(double), p->ctx->stream));
+  else
+    CDG_CUDA(cudaMemcpyAsync(L->sol, v, (size_t)L->ndof * sizeof(double), cudaMemcpyHostToDevice,
+                             p->ctx->stream));
   CDG_CUDA(cudaStreamSynchronize(p->ctx->stream));
   return CDG_OK;
 }
