@@ -303,7 +303,7 @@ def run_gpu(args):
         "assembly_ms": t_asm * 1e3,
         "kernels_ms": {"jacobi_smooth_f32_L0": ms_smooth, "spmv_f64_L0": ms_spmv64,
                        "element_contract_f64_L0": ms_contract},
-        "roofline": {"bound": "hbm", "kernel": "k_spmv<float,32,2> (Jacobi smoothing, finest)",
+        "roofline": {"bound": "hbm", "kernel": "k_spmv<float,8,8,2> (Jacobi smoothing, finest level)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
                      "algorithmic_bytes": bytes_smooth,

@@ -88,6 +88,9 @@ typedef struct {
   double multigrid_coarse_residual;
   int multigrid_coarse_max_n_iterations;
   int precision;               /* 0: all FP64, 1: FP32 multigrid in FP64 FGMRES */
+  int gram_schmidt;            /* Arnoldi orthogonalisation: 0 classical, all
+                                  inner products first (Iteration_gmres.C:
+                                  515-527), 1 modified (:528-534)            */
 } cdg_solver_params;
 
 typedef struct {
@@ -106,6 +109,7 @@ int cdg_version(void);
 
 /* ---- context ------------------------------------------------------------ */
 int cdg_context_create(int device, cdg_context **out);
+/* destroy every problem of the context before the context itself */
 int cdg_context_destroy(cdg_context *ctx);
 int cdg_context_synchronize(cdg_context *ctx);
 /* number of kernel launches the context issued since creation */

@@ -1573,10 +1573,18 @@ int orc_solve(orc_problem *p, const orc_solver_config *s, int *iters,
     for (i = 0; i < m && jj <= s->max_it; ++i, ++jj) {
       precond(p, s, v[i], z[i]);
       orc_apply(p, 0, z[i], r);
-      for (int k = 0; k <= i; ++k) {
-        HH(k, i) = dot(n, r, v[k]);
-        double h = -HH(k, i);
-        for (int t = 0; t < n; ++t) r[t] += h * v[k][t];
+      if (s->classical_gs) {
+        for (int k = 0; k <= i; ++k) HH(k, i) = dot(n, r, v[k]);
+        for (int k = 0; k <= i; ++k) {
+          double h = -HH(k, i);
+          for (int t = 0; t < n; ++t) r[t] += h * v[k][t];
+        }
+      } else {
+        for (int k = 0; k <= i; ++k) {
+          HH(k, i) = dot(n, r, v[k]);
+          double h = -HH(k, i);
+          for (int t = 0; t < n; ++t) r[t] += h * v[k][t];
+        }
       }
       HH(i + 1, i) = sqrt(dot(n, r, r));
       if (HH(i + 1, i) != 0.0) {

@@ -59,6 +59,8 @@ typedef struct {
   int coarse_direct;   /* 1: direct_solve (dense LU), 0: jacobi iterations    */
   double coarse_eps;
   int coarse_maxit;
+  int classical_gs;    /* 1: all inner products first (Iteration_gmres.C:515-527)
+                          0: modified Gram-Schmidt (:528-534)                */
 } orc_solver_config;
 
 typedef struct orc_problem orc_problem;

@@ -38,6 +38,7 @@ class SolverConfig(ctypes.Structure):
         ("n_post", ctypes.c_int), ("jacobi_damp", ctypes.c_double),
         ("correction_damp", ctypes.c_double), ("coarse_direct", ctypes.c_int),
         ("coarse_eps", ctypes.c_double), ("coarse_maxit", ctypes.c_int),
+        ("classical_gs", ctypes.c_int),
     ]
 
 
@@ -113,7 +114,7 @@ def make_config(dim, order, nref, example, eps=1.0, b=(0, 0, 0), c=0.0, freq=1.0
 def make_solver(precond="jacobi", max_it=1000, min_it=0, restart=50, tol_abs=0.0,
                 reduction=1e-10, divergence=1e10, mg_levels=2, mg_cycle="V",
                 n_pre=2, n_post=2, jacobi_damp=1.0, correction_damp=1.0,
-                coarse_direct=True, coarse_eps=0.1, coarse_maxit=10):
+                coarse_direct=True, coarse_eps=0.1, coarse_maxit=10, gram_schmidt="classical"):
     s = SolverConfig()
     s.precond = {"none": 0, "jacobi": 1, "multigrid": 2}[precond]
     s.max_it, s.min_it, s.restart = max_it, min_it, restart
@@ -123,6 +124,7 @@ def make_solver(precond="jacobi", max_it=1000, min_it=0, restart=50, tol_abs=0.0
     s.n_pre, s.n_post = n_pre, n_post
     s.jacobi_damp, s.correction_damp = jacobi_damp, correction_damp
     s.coarse_direct, s.coarse_eps, s.coarse_maxit = int(coarse_direct), coarse_eps, coarse_maxit
+    s.classical_gs = 1 if gram_schmidt == "classical" else 0
     return s
 
 

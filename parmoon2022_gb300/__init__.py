@@ -13,6 +13,7 @@ src/AssembleRoutines/LocalAssembling.C:564-581).
 """
 import ctypes
 import os
+import weakref
 
 import numpy as np
 
@@ -69,6 +70,7 @@ class SolverParams(ctypes.Structure):
         ("multigrid_correction_damp_factor", ctypes.c_double),
         ("multigrid_smoother_coarse", ctypes.c_int), ("multigrid_coarse_residual", ctypes.c_double),
         ("multigrid_coarse_max_n_iterations", ctypes.c_int), ("precision", ctypes.c_int),
+        ("gram_schmidt", ctypes.c_int),
     ]
 
 
@@ -165,7 +167,7 @@ def solver_params(preconditioner="jacobi", max_n_iterations=100, min_n_iteration
                   multigrid_n_pre_smooth=1, multigrid_n_post_smooth=1, jacobi_damp=1.0,
                   multigrid_correction_damp_factor=1.0, multigrid_smoother_coarse="direct_solve",
                   multigrid_coarse_residual=0.1, multigrid_coarse_max_n_iterations=10,
-                  precision="fp64"):
+                  precision="fp64", gram_schmidt="classical"):
     """Defaults are the reference's database defaults."""
     s = SolverParams()
     s.preconditioner = {"no_preconditioner": 0, "jacobi": 1, "multigrid": 2}[preconditioner]
@@ -182,6 +184,7 @@ def solver_params(preconditioner="jacobi", max_n_iterations=100, min_n_iteration
     s.multigrid_coarse_residual = multigrid_coarse_residual
     s.multigrid_coarse_max_n_iterations = multigrid_coarse_max_n_iterations
     s.precision = {"fp64": 0, "mixed": 1}[precision]
+    s.gram_schmidt = {"classical": 0, "modified": 1}[gram_schmidt]
     return s
 
 
@@ -234,6 +237,7 @@ class Context:
         c = ctypes.c_void_p()
         _chk(lib().cdg_context_create(device, ctypes.byref(c)))
         self.c = c
+        self._problems = weakref.WeakSet()   # destroyed before the context
 
     def synchronize(self):
         _chk(lib().cdg_context_synchronize(self.c))
@@ -249,6 +253,8 @@ class Context:
 
     def close(self):
         if getattr(self, "c", None):
+            for p in list(getattr(self, "_problems", ())):
+                p.close()
             lib().cdg_context_destroy(self.c)
             self.c = None
 
@@ -265,6 +271,7 @@ class ConvectionDiffusion:
         _chk(lib().cdg_problem_create(ctx.c, hierarchy.h, ctypes.byref(p)))
         self.p = p
         self.n_levels = hierarchy.n_levels
+        ctx._problems.add(self)
 
     @classmethod
     def from_arrays(cls, ctx, dim, order, levels):
@@ -292,11 +299,13 @@ class ConvectionDiffusion:
             _ip(ndof), _ip(nact), arr(np.int32, "row_ptr"), arr(np.int32, "col"),
             arr(np.int32, "parent"), ctypes.byref(p)))
         self.p = p
+        ctx._problems.add(self)
         return self
 
     def close(self):
         if getattr(self, "p", None):
-            lib().cdg_problem_destroy(self.p)
+            if getattr(self.ctx, "c", None):
+                lib().cdg_problem_destroy(self.p)
             self.p = None
 
     def __del__(self):

@@ -665,8 +665,31 @@ int upload_level(cdg_context* ctx, DevLevel& L) {
                            cudaMemcpyHostToDevice, st));
   CDG_CUDA(cudaMemsetAsync(L.sol, 0, (size_t)L.ndof * sizeof(double), st));
   CDG_CUDA(cudaMemsetAsync(L.rhs, 0, (size_t)L.ndof * sizeof(double), st));
+  {
+    std::vector<int> rp(L.nactive + 1, 0), dcol, dpos;
+    for (int r = 0; r < L.nactive; ++r) {
+      for (int k = L.pattern.row_ptr[r]; k < L.pattern.row_ptr[r + 1]; ++k)
+        if (L.pattern.col[k] >= L.nactive) {
+          dcol.push_back(L.pattern.col[k]);
+          dpos.push_back(k);
+        }
+      rp[r + 1] = (int)dcol.size();
+    }
+    CDG_TRY(dalloc(&L.dc_rp, rp.size()));
+    CDG_TRY(dalloc(&L.dc_col, dcol.size()));
+    CDG_TRY(dalloc(&L.dc_pos, dpos.size()));
+    CDG_CUDA(cudaMemcpyAsync(L.dc_rp, rp.data(), rp.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    if (!dcol.empty()) {
+      CDG_CUDA(cudaMemcpyAsync(L.dc_col, dcol.data(), dcol.size() * sizeof(int),
+                               cudaMemcpyHostToDevice, st));
+      CDG_CUDA(cudaMemcpyAsync(L.dc_pos, dpos.data(), dpos.size() * sizeof(int),
+                               cudaMemcpyHostToDevice, st));
+    }
+    CDG_CUDA(cudaStreamSynchronize(st));   // host vectors go out of scope
+  }
   double avg = L.ndof ? (double)L.nnz / L.ndof : 1.0;
-  L.rows_per_warp_hint = avg > 48 ? 32 : avg > 20 ? 16 : avg > 10 ? 8 : 4;
+  // lanes per CSR row for 8-deep unrolled row sums: 8 * lanes >= avg row length
+  L.rows_per_warp_hint = avg > 64 ? 16 : avg > 32 ? 8 : avg > 16 ? 4 : 2;
   return build_slots(ctx, L);
 }
 
@@ -674,7 +697,7 @@ int free_level(DevLevel& L) {
   void* ptrs[] = {L.verts, L.gdof, L.row_ptr, L.col, L.slot, L.diag_slot, L.val64, L.val32,
                   L.rhs, L.sol, L.invdiag64, L.invdiag32, L.mg_rhs, L.mg_sol, L.mg_tmp,
                   L.mg_def, L.P_rp, L.P_col, L.P_val, L.P_val32, L.R_rp, L.R_col, L.R_val,
-                  L.R_val32, L.coarse_inv, L.coarse_work};
+                  L.R_val32, L.coarse_inv, L.coarse_work, L.dc_rp, L.dc_col, L.dc_pos};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   return CDG_OK;

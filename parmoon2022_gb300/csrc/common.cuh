@@ -39,7 +39,7 @@ enum : int {
   kErrBreakdown = 8,   // FGMRES H(i+1,i) == 0
 };
 
-constexpr int kRedSlots = 8;          // concurrent reductions
+constexpr int kRedSlots = 32;         // partial-sum rows (one per inner product)
 constexpr int kRedMaxBlocks = 1024;   // partial sums per reduction
 
 }  // namespace cdg
@@ -79,12 +79,18 @@ struct DevLevel {
   double* invdiag64 = nullptr;   // ndof
   float* invdiag32 = nullptr;    // ndof
   int rows_per_warp_hint = 1;    // SpMV shape (avg row length)
+  // couplings of active rows to non-active columns: CSR over active rows,
+  // column and CSR slot of each (first smoothing step from a zero start)
+  int* dc_rp = nullptr;
+  int* dc_col = nullptr;
+  int* dc_pos = nullptr;
   // multigrid work vectors (double or float, per precision)
   void* mg_rhs = nullptr;
   void* mg_sol = nullptr;
   void* mg_tmp = nullptr;
   void* mg_def = nullptr;
   int mg_elem = 0;               // sizeof element of mg vectors
+  bool mg_visited = false;       // level already descended through this cycle
   // transfer to the next coarser level (this = fine)
   int* P_rp = nullptr; int* P_col = nullptr; double* P_val = nullptr; float* P_val32 = nullptr;
   int* R_rp = nullptr; int* R_col = nullptr; double* R_val = nullptr; float* R_val32 = nullptr;

@@ -11,21 +11,59 @@
 // CycleControl.C:15-111, MultigridLevel.C:118-151, JacobiSmoother.C:21-29,
 // GridTransfer.C:29-410, DirectSmoother.C:25-42);
 // BlockFEMatrix::apply_scaled_add (src/Matrix/BlockFEMatrix.C:969-1095).
+#include <cooperative_groups.h>
+
 #include <chrono>
 #include <cmath>
 #include <cstring>
 
 #include "common.cuh"
 
+namespace cgrp = cooperative_groups;
+
 namespace cdg {
 
 // ---------------------------------------------------------------------------
-// SpMV family: TPR threads per row; non-active rows act as identity rows
+// CSR row reductions: TPR threads per row, each lane issues UNR independent
+// (col, val) loads before the dependent x gathers, so a warp keeps
+// TPR*UNR*(4+sizeof(T)) bytes of matrix data in flight per pass
+// ---------------------------------------------------------------------------
+template <typename T, int TPR, int UNR>
+__device__ __forceinline__ T csr_row_partial(const int* __restrict__ rp, const int* __restrict__ col,
+                                             const T* __restrict__ val, const T* __restrict__ x,
+                                             int row, int sub) {
+  T s = 0;
+  const int b = __ldg(rp + row), e = __ldg(rp + row + 1);
+  for (int k0 = b + sub; k0 < e; k0 += TPR * UNR) {
+    int c[UNR];
+    T v[UNR];
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) {
+      const int k = k0 + u * TPR;
+      c[u] = k < e ? __ldcs(col + k) : -1;
+      v[u] = k < e ? __ldcs(val + k) : (T)0;
+    }
+    // padding slots issue neither a gather nor a multiply-add
+#pragma unroll
+    for (int u = 0; u < UNR; ++u)
+      if (c[u] >= 0) s = fma(v[u], __ldg(x + c[u]), s);
+  }
+  return s;
+}
+
+// sum over the TPR lanes of a row group; every lane of the warp must call it
+template <typename T, int TPR>
+__device__ __forceinline__ T group_sum(T s) {
+#pragma unroll
+  for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, TPR);
+  return s;
+}
+
+// SpMV family; non-active rows act as identity rows
 //   MODE 0: y = A x
 //   MODE 1: y = b - A x                         (calculate_defect)
 //   MODE 2: y = x + w D^-1 (b - A x)            (JacobiSmoother::smooth)
-// ---------------------------------------------------------------------------
-template <typename T, int TPR, int MODE>
+template <typename T, int TPR, int UNR, int MODE>
 __global__ void __launch_bounds__(256)
 k_spmv(int n, int nactive, const int* __restrict__ rp, const int* __restrict__ col,
        const T* __restrict__ val, const T* __restrict__ x, const T* __restrict__ b,
@@ -34,14 +72,9 @@ k_spmv(int n, int nactive, const int* __restrict__ rp, const int* __restrict__ c
   const int row = (int)(gt / TPR);
   const int sub = threadIdx.x % TPR;
   T s = 0;
-  const bool valid = row < n;
-  if (valid && row < nactive) {
-    const int e = __ldg(rp + row + 1);
-    for (int k = __ldg(rp + row) + sub; k < e; k += TPR) s += __ldg(val + k) * __ldg(x + __ldg(col + k));
-  }
-#pragma unroll
-  for (int o = TPR / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, TPR);
-  if (!valid || sub != 0) return;
+  if (row < nactive) s = csr_row_partial<T, TPR, UNR>(rp, col, val, x, row, sub);
+  s = group_sum<T, TPR>(s);
+  if (row >= n || sub != 0) return;
   const T xr = x[row];
   if (row >= nactive) s = xr;
   if (MODE == 0) y[row] = s;
@@ -49,6 +82,8 @@ k_spmv(int n, int nactive, const int* __restrict__ rp, const int* __restrict__ c
   else y[row] = xr + w * (invd[row] * (b[row] - s));
 }
 
+// lanes per row chosen from the average row length so that 8 * TPR covers a
+// typical row in one pass (Q2 hexahedra: 62 entries -> 8 lanes, 4 rows/warp)
 template <typename T, int MODE>
 static int spmv_t(cdg_context* ctx, const DevLevel& L, const T* val, const T* x, const T* b,
                   const T* invd, T w, T* y) {
@@ -56,15 +91,23 @@ static int spmv_t(cdg_context* ctx, const DevLevel& L, const T* val, const T* x,
   long threads = (long)L.ndof * tpr;
   int grid = (int)((threads + 255) / 256);
   switch (tpr) {
-    case 4: CDG_LAUNCH(ctx, (k_spmv<T, 4, MODE>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y); break;
-    case 8: CDG_LAUNCH(ctx, (k_spmv<T, 8, MODE>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y); break;
-    case 16: CDG_LAUNCH(ctx, (k_spmv<T, 16, MODE>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y); break;
-    default: CDG_LAUNCH(ctx, (k_spmv<T, 32, MODE>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y); break;
+    case 2: CDG_LAUNCH(ctx, (k_spmv<T, 2, 8, MODE>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y); break;
+    case 4: CDG_LAUNCH(ctx, (k_spmv<T, 4, 8, MODE>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y); break;
+    case 8: CDG_LAUNCH(ctx, (k_spmv<T, 8, 8, MODE>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y); break;
+    default: CDG_LAUNCH(ctx, (k_spmv<T, 16, 8, MODE>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y); break;
   }
   return CDG_OK;
 }
 
+// the FP64 operator: FP64 issue rate bounds it on GB300, so rows use 4 lanes
+// x 16-deep unrolling (2 reduction levels instead of 3)
 int spmv_apply64(cdg_context* ctx, const DevLevel& L, const double* x, double* y) {
+  if (L.rows_per_warp_hint == 8) {
+    int grid = (int)(((long)L.ndof * 4 + 255) / 256);
+    CDG_LAUNCH(ctx, (k_spmv<double, 4, 16, 0>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr,
+               L.col, L.val64, x, (const double*)nullptr, (const double*)nullptr, 0.0, y);
+    return CDG_OK;
+  }
   return spmv_t<double, 0>(ctx, L, L.val64, x, nullptr, nullptr, 0.0, y);
 }
 int residual64(cdg_context* ctx, const DevLevel& L, const double* b, const double* x,
@@ -144,6 +187,131 @@ k_mgs(int n, double* __restrict__ w, const double* __restrict__ vk, const double
   finalize_sum<256>(s, partials, cnt, out, vnext == nullptr);
 }
 
+// classical Gram-Schmidt (Iteration_gmres.C:515-527, the branch that queues
+// all inner products before the updates): H(k0+j, i) = (w, v_{k0+j}) for
+// j < cnt <= 32 in one pass over w and the basis
+template <int NT>
+__global__ void __launch_bounds__(NT)
+k_multidot(int n, const double* __restrict__ w, const double* __restrict__ V, int k0, int cnt,
+           double* partials, unsigned* counter, double* out) {
+  __shared__ double sh[NT / 32][32];
+  __shared__ bool last;
+  const int wp = threadIdx.x >> 5, l = threadIdx.x & 31;
+  // one inner product at a time: the block's slice of w stays in L1 across j
+  for (int j = 0; j < cnt; ++j) {
+    const double* __restrict__ vj = V + (size_t)(k0 + j) * n;
+    double a = 0.0;
+    for (long t = blockIdx.x * (long)NT + threadIdx.x; t < n; t += (long)gridDim.x * NT)
+      a = fma(__ldg(w + t), __ldcs(vj + t), a);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if (l == 0) sh[wp][j] = a;
+  }
+  __syncthreads();
+  if (threadIdx.x < cnt) {
+    double v = 0.0;
+    for (int q = 0; q < NT / 32; ++q) v += sh[q][threadIdx.x];
+    partials[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = v;
+    __threadfence();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  // one warp per inner product, lanes stride over the block partials
+  for (int j = wp; j < cnt; j += NT / 32) {
+    double v = 0.0;
+    for (int q = l; q < (int)gridDim.x; q += 32)
+      v += ((volatile double*)partials)[(size_t)j * gridDim.x + q];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (l == 0) out[j] = v;
+  }
+  if (threadIdx.x == 0) *counter = 0u;
+}
+
+// Givens rotations of Hessenberg column i (Utilities_gmres.C:60-88): apply
+// the previous rotations, generate and apply rotation i, rotate s, write
+// |s_{i+1}| to *resid
+__device__ void givens_column(int i, double* col, double* cs, double* sn, double* s,
+                              double* resid) {
+  for (int k = 0; k < i; ++k) {
+    double dx = col[k], dy = col[k + 1];
+    col[k] = cs[k] * dx + sn[k] * dy;
+    col[k + 1] = -sn[k] * dx + cs[k] * dy;
+  }
+  double dx = col[i], dy = col[i + 1], c, sg;
+  if (dy == 0.0) {
+    c = 1.0;
+    sg = 0.0;
+  } else if (fabs(dy) > fabs(dx)) {
+    double t = dx / dy;
+    sg = 1.0 / sqrt(1.0 + t * t);
+    c = t * sg;
+  } else {
+    double t = dy / dx;
+    c = 1.0 / sqrt(1.0 + t * t);
+    sg = t * c;
+  }
+  cs[i] = c;
+  sn[i] = sg;
+  col[i] = c * dx + sg * dy;
+  col[i + 1] = -sg * dx + c * dy;
+  double a = s[i], b = s[i + 1];
+  s[i] = c * a + sg * b;
+  s[i + 1] = -sg * a + c * b;
+  *resid = fabs(s[i + 1]);
+}
+
+// w -= sum_k H(k,i) v_k (k in order), H(i+1,i) = ||w||, then the Givens
+// step of column i in the block that finishes last
+__global__ void __launch_bounds__(256)
+k_cgs_update(int n, double* __restrict__ w, const double* __restrict__ V, int i,
+             double* __restrict__ hcol, double* partials, unsigned* counter, double* cs,
+             double* sn, double* gs, double* resid, double* norm_out) {
+  __shared__ double h[128];
+  __shared__ bool last;
+  for (int j = threadIdx.x; j <= i; j += 256) h[j] = -hcol[j];
+  __syncthreads();
+  double s = 0.0;
+  for (long t = blockIdx.x * 256L + threadIdx.x; t < n; t += (long)gridDim.x * 256) {
+    double wt = w[t];
+    int j = 0;
+    // four independent basis loads in flight, additions kept in k order
+    for (; j + 3 <= i; j += 4) {
+      const double a0 = __ldcs(V + (size_t)j * n + t), a1 = __ldcs(V + (size_t)(j + 1) * n + t);
+      const double a2 = __ldcs(V + (size_t)(j + 2) * n + t), a3 = __ldcs(V + (size_t)(j + 3) * n + t);
+      wt = fma(h[j], a0, wt);
+      wt = fma(h[j + 1], a1, wt);
+      wt = fma(h[j + 2], a2, wt);
+      wt = fma(h[j + 3], a3, wt);
+    }
+    for (; j <= i; ++j) wt = fma(h[j], __ldcs(V + (size_t)j * n + t), wt);
+    w[t] = wt;
+    s += wt * wt;
+  }
+  s = block_sum<256>(s);
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = s;
+    __threadfence();
+    last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double v = 0.0;
+  for (int q = threadIdx.x; q < (int)gridDim.x; q += 256) v += ((volatile double*)partials)[q];
+  v = block_sum<256>(v);
+  if (threadIdx.x == 0) {
+    const double nrm = sqrt(v);
+    hcol[i + 1] = nrm;
+    *norm_out = nrm;   // v_{i+1} = w / H(i+1,i) uses the value before rotation
+    *counter = 0u;
+    givens_column(i, hcol, cs, sn, gs, resid);
+  }
+}
+
 static int red_grid(cdg_context* ctx, int n) {
   int g = (n + 255) / 256;
   int cap = ctx->num_sms * 4;
@@ -201,30 +369,34 @@ __global__ void k_to_double(int n, const T* __restrict__ a, double* __restrict__
 }
 
 // x_f[i] += damp * (P x_c)[i] for fine actives (update_solution_in_finer_grid)
-// or x_f = P x_c for all rows (GridTransfer::Prolongate) when damp == 0
-template <typename T>
-__global__ void k_prolong(int nf, int nactive_f, const int* __restrict__ rp,
-                          const int* __restrict__ col, const T* __restrict__ val,
-                          const T* __restrict__ xc, T* __restrict__ xf, T damp, int add) {
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < nf; i += (long)gridDim.x * blockDim.x) {
-    T s = 0;
-    for (int k = rp[i]; k < rp[i + 1]; ++k) s += val[k] * xc[col[k]];
-    if (!add) xf[i] = s;
-    else if (i < nactive_f) xf[i] += damp * s;
-  }
+// or x_f = P x_c for all rows (GridTransfer::Prolongate) when add == 0
+template <typename T, int TPR>
+__global__ void __launch_bounds__(256)
+k_prolong(int nf, int nactive_f, const int* __restrict__ rp, const int* __restrict__ col,
+          const T* __restrict__ val, const T* __restrict__ xc, T* __restrict__ xf, T damp,
+          int add) {
+  const long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const int i = (int)(gt / TPR), sub = threadIdx.x % TPR;
+  T s = 0;
+  if (i < nf) s = csr_row_partial<T, TPR, 4>(rp, col, val, xc, i, sub);
+  s = group_sum<T, TPR>(s);
+  if (i >= nf || sub != 0) return;
+  if (!add) xf[i] = s;
+  else if (i < nactive_f) xf[i] += damp * s;
 }
 
 // r_c = R d_f; coarse non-actives zeroed when mask (ResetNonActive)
-template <typename T>
-__global__ void k_restrict(int nc, int nactive_c, const int* __restrict__ rp,
-                           const int* __restrict__ col, const T* __restrict__ val,
-                           const T* __restrict__ df, T* __restrict__ rc, int mask) {
-  for (long j = blockIdx.x * (long)blockDim.x + threadIdx.x; j < nc; j += (long)gridDim.x * blockDim.x) {
-    T s = 0;
-    if (!mask || j < nactive_c)
-      for (int k = rp[j]; k < rp[j + 1]; ++k) s += val[k] * df[col[k]];
-    rc[j] = s;
-  }
+template <typename T, int TPR>
+__global__ void __launch_bounds__(256)
+k_restrict(int nc, int nactive_c, const int* __restrict__ rp, const int* __restrict__ col,
+           const T* __restrict__ val, const T* __restrict__ df, T* __restrict__ rc, int mask) {
+  const long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const int j = (int)(gt / TPR), sub = threadIdx.x % TPR;
+  T s = 0;
+  if (j < nc && (!mask || j < nactive_c)) s = csr_row_partial<T, TPR, 8>(rp, col, val, df, j, sub);
+  s = group_sum<T, TPR>(s);
+  if (j >= nc || sub != 0) return;
+  rc[j] = s;
 }
 
 template <typename T>
@@ -260,12 +432,12 @@ __global__ void k_extract_dense(int na, const int* __restrict__ rp, const int* _
   M[i * W + na + i] = 1.0;
 }
 
-__global__ void __launch_bounds__(256)
-k_gj_step(int na, int k, const double* __restrict__ Min, double* __restrict__ Mout, int* err) {
+// one pivot step k: pivot = first row of maximal |M[i][k]|, i >= k (every
+// block finds the same one); rows k and p swap; Mout = eliminated Min
+__device__ __forceinline__ bool gj_step(int na, int k, const double* __restrict__ Min,
+                                        double* __restrict__ Mout, int* err, double* sv,
+                                        int* si) {
   const long W = 2L * na;
-  __shared__ double sv[256];
-  __shared__ int si[256];
-  // pivot: first row of maximal |Min[i][k]|, i >= k (every block agrees)
   double best = -1.0;
   int bi = k;
   for (int i = k + threadIdx.x; i < na; i += 256) {
@@ -288,9 +460,10 @@ k_gj_step(int na, int k, const double* __restrict__ Min, double* __restrict__ Mo
   }
   const int p = si[0];
   const double piv = Min[p * W + k];
+  __syncthreads();   // sv/si are reused by the next step
   if (piv == 0.0) {
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(err, kErrSingular);
-    return;
+    return false;
   }
   const long ncol = (na - k) + na;  // live columns: left [k, na), right [na, 2na)
   const long total = (long)na * ncol;
@@ -305,6 +478,32 @@ k_gj_step(int na, int k, const double* __restrict__ Min, double* __restrict__ Mo
       const int r = (i == p) ? k : i;
       Mout[i * W + j] = Min[r * W + j] - Min[r * W + k] * prow;
     }
+  }
+  return true;
+}
+
+__global__ void __launch_bounds__(256)
+k_gj_step(int na, int k, const double* __restrict__ Min, double* __restrict__ Mout, int* err) {
+  __shared__ double sv[256];
+  __shared__ int si[256];
+  gj_step(na, k, Min, Mout, err, sv, si);
+}
+
+// all na pivot steps in one cooperative launch, grid-wide sync between steps;
+// every block sees the same pivot, so all blocks leave together on a zero pivot
+__global__ void __launch_bounds__(256)
+k_gj_coop(int na, double* A, double* B, int* err) {
+  __shared__ double sv[256];
+  __shared__ int si[256];
+  cgrp::grid_group grid = cgrp::this_grid();
+  double* Min = A;
+  double* Mout = B;
+  for (int k = 0; k < na; ++k) {
+    if (!gj_step(na, k, Min, Mout, err, sv, si)) return;
+    grid.sync();
+    double* t = Min;
+    Min = Mout;
+    Mout = t;
   }
 }
 
@@ -330,11 +529,24 @@ static int coarse_inverse(cdg_context* ctx, DevLevel& C) {
   double* B = C.coarse_work + sz;
   CDG_CUDA(cudaMemsetAsync(A, 0, sz * sizeof(double), ctx->stream));
   CDG_LAUNCH(ctx, k_extract_dense, grid_for<int>(na, 128), 128, 0, na, C.row_ptr, C.col, C.val64, A);
-  for (int k = 0; k < na; ++k) {
-    long total = (long)na * ((na - k) + na);
-    int g = (int)std::min<long>((total + 255) / 256, (long)ctx->num_sms * 8);
-    CDG_LAUNCH(ctx, k_gj_step, g, 256, 0, na, k, A, B, ctx->d_err);
-    std::swap(A, B);
+  int coop = 0, per_sm = 0;
+  CDG_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device));
+  CDG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gj_coop, 256, 0));
+  long want = ((long)na * 2 * na + 255) / 256;
+  int g = (int)std::min<long>(want, (long)ctx->num_sms * std::min(per_sm, 2));
+  if (coop && per_sm > 0 && g >= 1) {
+    void* args[] = {(void*)&na, (void*)&A, (void*)&B, (void*)&ctx->d_err};
+    CDG_CUDA(cudaLaunchCooperativeKernel((const void*)k_gj_coop, dim3(g), dim3(256), args, 0,
+                                         ctx->stream));
+    ctx->launches++;
+    if (na % 2 == 1) std::swap(A, B);   // result of step na-1 is in B when na is odd
+  } else {
+    for (int k = 0; k < na; ++k) {
+      long total = (long)na * ((na - k) + na);
+      int gg = (int)std::min<long>((total + 255) / 256, (long)ctx->num_sms * 8);
+      CDG_LAUNCH(ctx, k_gj_step, gg, 256, 0, na, k, A, B, ctx->d_err);
+      std::swap(A, B);
+    }
   }
   CDG_LAUNCH(ctx, k_right_half, grid_for<int>(na * na, 256), 256, 0, na, A, C.coarse_inv);
   return CDG_OK;
@@ -371,6 +583,37 @@ static int smooth(cdg_context* ctx, DevLevel& L, T damp) {
   return CDG_OK;
 }
 
+// first smoothing step from x0 = 0 on active rows and x0 = b on non-active
+// rows (zero there on coarse levels): A x0 on an active row only involves its
+// non-active columns, so the step needs no full SpMV
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_first_smooth(int n, int nactive, int with_dirichlet, const int* __restrict__ dc_rp,
+               const int* __restrict__ dc_col, const int* __restrict__ dc_pos,
+               const T* __restrict__ val, const T* __restrict__ b, const T* __restrict__ invd,
+               T w, T* __restrict__ x1) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    if (i < nactive) {
+      T s = 0;
+      if (with_dirichlet)
+        for (int k = dc_rp[i]; k < dc_rp[i + 1]; ++k) s += val[dc_pos[k]] * b[dc_col[k]];
+      x1[i] = w * (invd[i] * (b[i] - s));
+    } else {
+      const T x0 = with_dirichlet ? b[i] : (T)0;
+      x1[i] = x0 + w * (invd[i] * (b[i] - x0));
+    }
+  }
+}
+
+template <typename T>
+static int first_smooth(cdg_context* ctx, DevLevel& L, T damp, bool finest) {
+  CDG_LAUNCH(ctx, k_first_smooth<T>, vec_grid(ctx, L.ndof), 256, 0, L.ndof, L.nactive,
+             finest ? 1 : 0, L.dc_rp, L.dc_col, L.dc_pos, Prec<T>::val(L), (const T*)L.mg_rhs,
+             Prec<T>::invd(L), damp, (T*)L.mg_tmp);
+  std::swap(L.mg_sol, L.mg_tmp);
+  return CDG_OK;
+}
+
 template <typename T>
 static int defect(cdg_context* ctx, DevLevel& L) {
   return spmv_t<T, 1>(ctx, L, Prec<T>::val(L), (const T*)L.mg_sol, (const T*)L.mg_rhs, nullptr,
@@ -380,8 +623,8 @@ static int defect(cdg_context* ctx, DevLevel& L) {
 // update_solution_in_finer_grid: fine.sol += damp * P coarse.sol on actives
 template <typename T>
 static int prolong_correct(cdg_context* ctx, DevLevel& F, DevLevel& C, T damp) {
-  CDG_LAUNCH(ctx, k_prolong<T>, vec_grid(ctx, F.ndof), 256, 0, F.ndof, F.nactive, F.P_rp,
-             F.P_col, Prec<T>::P(F), (const T*)C.mg_sol, (T*)F.mg_sol, damp, 1);
+  CDG_LAUNCH(ctx, (k_prolong<T, 2>), grid_for<int>((long)F.ndof * 2, 256), 256, 0, F.ndof,
+             F.nactive, F.P_rp, F.P_col, Prec<T>::P(F), (const T*)C.mg_sol, (T*)F.mg_sol, damp, 1);
   return CDG_OK;
 }
 
@@ -443,6 +686,7 @@ static int mg_cycle(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s
   fill_cycle(seq, rec, nl - 1, nl, s.multigrid_cycle_type);
   const T damp = (T)s.jacobi_damp;
   const T cdamp = (T)s.multigrid_correction_damp_factor;
+  for (int m = 0; m < nl; ++m) lv(m).mg_visited = false;
   int level = nl - 1;
   if (nl == 1) {
     CDG_TRY(coarse_solve<T>(ctx, F, s));
@@ -460,14 +704,24 @@ static int mg_cycle(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s
       if (from_below)
         for (int i = 0; i < s.multigrid_n_post_smooth; ++i) CDG_TRY(smooth<T>(ctx, L, damp));
       if (dir == kDown) {
-        for (int i = 0; i < s.multigrid_n_pre_smooth; ++i) CDG_TRY(smooth<T>(ctx, L, damp));
+        for (int i = 0; i < s.multigrid_n_pre_smooth; ++i) {
+          // the start iterate is zero (finest: Dirichlet values) unless the
+          // level was smoothed since its solution was last reset (W, F cycles)
+          if (i == 0 && !L.mg_visited)
+            CDG_TRY(first_smooth<T>(ctx, L, damp, level == nl - 1));
+          else
+            CDG_TRY(smooth<T>(ctx, L, damp));
+        }
+        L.mg_visited = true;
         CDG_TRY(defect<T>(ctx, L));
         DevLevel& C = lv(level - 1);
         // coarse start iterate is set by the restriction target's consumer:
         // the coarse solution starts from zero
         CDG_CUDA(cudaMemsetAsync(C.mg_sol, 0, (size_t)C.ndof * sizeof(T), ctx->stream));
-        CDG_LAUNCH(ctx, k_restrict<T>, vec_grid(ctx, C.ndof), 256, 0, C.ndof, C.nactive, L.R_rp,
-                   L.R_col, Prec<T>::R(L), (const T*)L.mg_def, (T*)C.mg_rhs, 1);
+        C.mg_visited = false;   // zero start iterate again: shortcut valid
+        CDG_LAUNCH(ctx, (k_restrict<T, 8>), grid_for<int>((long)C.ndof * 8, 256), 256, 0,
+                   C.ndof, C.nactive, L.R_rp, L.R_col, Prec<T>::R(L), (const T*)L.mg_def,
+                   (T*)C.mg_rhs, 1);
         level -= 1;
       } else if (dir == kUp) {
         CDG_TRY(prolong_correct<T>(ctx, lv(level + 1), L, cdamp));
@@ -550,15 +804,15 @@ int precondition(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s, c
 
 int prolongate64(cdg_context* ctx, const DevLevel& F, const double* xc, double* xf,
                  int add_actives_only, double damp) {
-  CDG_LAUNCH(ctx, k_prolong<double>, vec_grid(ctx, F.ndof), 256, 0, F.ndof, F.nactive, F.P_rp,
-             F.P_col, F.P_val, xc, xf, damp, add_actives_only);
+  CDG_LAUNCH(ctx, (k_prolong<double, 2>), grid_for<int>((long)F.ndof * 2, 256), 256, 0, F.ndof,
+             F.nactive, F.P_rp, F.P_col, F.P_val, xc, xf, damp, add_actives_only);
   return CDG_OK;
 }
 
 int restrict64(cdg_context* ctx, const DevLevel& F, const DevLevel& C, const double* df,
                double* rc) {
-  CDG_LAUNCH(ctx, k_restrict<double>, vec_grid(ctx, C.ndof), 256, 0, C.ndof, C.nactive, F.R_rp,
-             F.R_col, F.R_val, df, rc, 0);
+  CDG_LAUNCH(ctx, (k_restrict<double, 8>), grid_for<int>((long)C.ndof * 8, 256), 256, 0,
+             C.ndof, C.nactive, F.R_rp, F.R_col, F.R_val, df, rc, 0);
   return CDG_OK;
 }
 
@@ -567,33 +821,7 @@ int restrict64(cdg_context* ctx, const DevLevel& F, const DevLevel& C, const dou
 // ---------------------------------------------------------------------------
 __global__ void k_givens(int i, int m, double* H, double* cs, double* sn, double* s,
                          double* resid) {
-  double* col = H + (size_t)i * (m + 1);
-  for (int k = 0; k < i; ++k) {
-    double dx = col[k], dy = col[k + 1];
-    col[k] = cs[k] * dx + sn[k] * dy;
-    col[k + 1] = -sn[k] * dx + cs[k] * dy;
-  }
-  double dx = col[i], dy = col[i + 1], c, sg;
-  if (dy == 0.0) {
-    c = 1.0;
-    sg = 0.0;
-  } else if (fabs(dy) > fabs(dx)) {
-    double t = dx / dy;
-    sg = 1.0 / sqrt(1.0 + t * t);
-    c = t * sg;
-  } else {
-    double t = dy / dx;
-    c = 1.0 / sqrt(1.0 + t * t);
-    sg = t * c;
-  }
-  cs[i] = c;
-  sn[i] = sg;
-  col[i] = c * dx + sg * dy;
-  col[i + 1] = -sg * dx + c * dy;
-  double a = s[i], b = s[i + 1];
-  s[i] = c * a + sg * b;
-  s[i + 1] = -sg * a + c * b;
-  *resid = fabs(s[i + 1]);
+  givens_column(i, H + (size_t)i * (m + 1), cs, sn, s, resid);
 }
 
 // s = (beta, 0, ..., 0)
@@ -709,16 +937,32 @@ int fgmres(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s, cdg_sol
       double* col = g.H + (size_t)i * (m + 1);
       CDG_TRY(precondition(ctx, p, s, vi, zi));
       CDG_TRY(spmv_apply64(ctx, L, zi, g.w));
-      CDG_TRY(dot64(ctx, n, g.w, g.V, col + 0, 0));
-      for (int k = 0; k <= i; ++k) {
-        const double* vk = g.V + (size_t)k * n;
-        const double* vn = (k < i) ? g.V + (size_t)(k + 1) * n : nullptr;
-        CDG_LAUNCH(ctx, k_mgs, red_grid(ctx, n), 256, 0, n, g.w, vk, col + k, vn,
-                   ctx->d_red, ctx->d_cnt, col + k + 1);
+      if (s.gram_schmidt == 0) {
+        // classical: all inner products, then all updates and the norm
+        for (int k0 = 0; k0 <= i; k0 += 32) {
+          int cnt = std::min(32, i + 1 - k0);
+          CDG_LAUNCH(ctx, k_multidot<256>, red_grid(ctx, n), 256, 0, n, g.w, g.V, k0, cnt,
+                     ctx->d_red, ctx->d_cnt + 1, col + k0);
+        }
+        CDG_LAUNCH(ctx, k_cgs_update, red_grid(ctx, n), 256, 0, n, g.w, g.V, i, col,
+                   ctx->d_red, ctx->d_cnt, g.cs, g.sn, g.s, resid_d, g.scal + 2);
+        CDG_LAUNCH(ctx, k_scale_inv, vg, 256, 0, n, g.w, g.scal + 2,
+                   g.V + (size_t)(i + 1) * n, ctx->d_err);
+      } else {
+        // modified: dot and update interleaved (sequential build)
+        CDG_TRY(dot64(ctx, n, g.w, g.V, col + 0, 0));
+        for (int k = 0; k <= i; ++k) {
+          const double* vk = g.V + (size_t)k * n;
+          const double* vn = (k < i) ? g.V + (size_t)(k + 1) * n : nullptr;
+          CDG_LAUNCH(ctx, k_mgs, red_grid(ctx, n), 256, 0, n, g.w, vk, col + k, vn,
+                     ctx->d_red, ctx->d_cnt, col + k + 1);
+        }
       }
-      CDG_LAUNCH(ctx, k_scale_inv, vg, 256, 0, n, g.w, col + i + 1, g.V + (size_t)(i + 1) * n,
-                 ctx->d_err);
-      CDG_LAUNCH(ctx, k_givens, 1, 1, 0, i, m, g.H, g.cs, g.sn, g.s, resid_d);
+      if (s.gram_schmidt != 0) {
+        CDG_LAUNCH(ctx, k_scale_inv, vg, 256, 0, n, g.w, col + i + 1,
+                   g.V + (size_t)(i + 1) * n, ctx->d_err);
+        CDG_LAUNCH(ctx, k_givens, 1, 1, 0, i, m, g.H, g.cs, g.sn, g.s, resid_d);
+      }
       CDG_TRY(read_scalar(ctx, resid_d, &resid));
       CDG_TRY(check_device_error(ctx));
       int cv = converged(s, li, resid, j);

@@ -170,6 +170,22 @@ def test_solve_parity(ctx, name, prec_name, levels, restart):
         gpu.close()
 
 
+@pytest.mark.parametrize("gs", ["classical", "modified"])
+def test_gram_schmidt_variants(ctx, gs):
+    # both Arnoldi branches of Iteration_gmres::flexible_gmres (:515-534)
+    o, h, a = make_pair("q1_2d_cd", n_levels=1)
+    o.assemble()
+    it_o, res_o, ini_o = o.solve(po.make_solver("jacobi", max_it=2000, restart=50,
+                                                reduction=1e-10, gram_schmidt=gs))
+    gpu = pg.ConvectionDiffusion(ctx, h)
+    gpu.assemble(a)
+    st = gpu.solve(pg.solver_params("jacobi", max_n_iterations=2000, gmres_restart=50,
+                                    residual_tolerance=0.0, residual_reduction=1e-10,
+                                    gram_schmidt=gs))
+    assert abs(st.iterations - it_o) <= 1
+    assert rel(gpu.solution(), o.solution()) < 1e-8
+
+
 def test_from_arrays_equals_hierarchy(ctx):
     o, h, a = make_pair("q2_2d_supg", n_levels=2)
     levels = []
