@@ -197,15 +197,25 @@ k_multidot(int n, const double* __restrict__ w, const double* __restrict__ V, in
   __shared__ double sh[NT / 32][32];
   __shared__ bool last;
   const int wp = threadIdx.x >> 5, l = threadIdx.x & 31;
-  // one inner product at a time: the block's slice of w stays in L1 across j
-  for (int j = 0; j < cnt; ++j) {
-    const double* __restrict__ vj = V + (size_t)(k0 + j) * n;
-    double a = 0.0;
-    for (long t = blockIdx.x * (long)NT + threadIdx.x; t < n; t += (long)gridDim.x * NT)
-      a = fma(__ldg(w + t), __ldcs(vj + t), a);
+  // eight inner products per pass (eight independent basis loads in flight);
+  // the block's slice of w stays in L1 across passes
+  for (int j0 = 0; j0 < cnt; j0 += 8) {
+    double a[8];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
-    if (l == 0) sh[wp][j] = a;
+    for (int jj = 0; jj < 8; ++jj) a[jj] = 0.0;
+    for (long t = blockIdx.x * (long)NT + threadIdx.x; t < n; t += (long)gridDim.x * NT) {
+      const double wt = __ldg(w + t);
+#pragma unroll
+      for (int jj = 0; jj < 8; ++jj)
+        if (j0 + jj < cnt) a[jj] = fma(wt, __ldcs(V + (size_t)(k0 + j0 + jj) * n + t), a[jj]);
+    }
+#pragma unroll
+    for (int jj = 0; jj < 8; ++jj) {
+      double v = a[jj];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (l == 0 && j0 + jj < cnt) sh[wp][j0 + jj] = v;
+    }
   }
   __syncthreads();
   if (threadIdx.x < cnt) {
@@ -278,14 +288,13 @@ k_cgs_update(int n, double* __restrict__ w, const double* __restrict__ V, int i,
   for (long t = blockIdx.x * 256L + threadIdx.x; t < n; t += (long)gridDim.x * 256) {
     double wt = w[t];
     int j = 0;
-    // four independent basis loads in flight, additions kept in k order
-    for (; j + 3 <= i; j += 4) {
-      const double a0 = __ldcs(V + (size_t)j * n + t), a1 = __ldcs(V + (size_t)(j + 1) * n + t);
-      const double a2 = __ldcs(V + (size_t)(j + 2) * n + t), a3 = __ldcs(V + (size_t)(j + 3) * n + t);
-      wt = fma(h[j], a0, wt);
-      wt = fma(h[j + 1], a1, wt);
-      wt = fma(h[j + 2], a2, wt);
-      wt = fma(h[j + 3], a3, wt);
+    // eight independent basis loads in flight, additions kept in k order
+    for (; j + 7 <= i; j += 8) {
+      double a[8];
+#pragma unroll
+      for (int jj = 0; jj < 8; ++jj) a[jj] = __ldcs(V + (size_t)(j + jj) * n + t);
+#pragma unroll
+      for (int jj = 0; jj < 8; ++jj) wt = fma(h[j + jj], a[jj], wt);
     }
     for (; j <= i; ++j) wt = fma(h[j], __ldcs(V + (size_t)j * n + t), wt);
     w[t] = wt;
