@@ -172,6 +172,20 @@ int cdg_problem_assemble_solve(cdg_problem *p, const cdg_assembly_params *a,
  * solution: errors[0..4] = L2, H1-semi, SD, DG(volume), L_inf */
 int cdg_problem_errors(cdg_problem *p, const cdg_assembly_params *a,
                        double *errors);
+/* The same error norms without allocating any device memory (this entry has
+ * no counterpart in the reference).  For callers that cannot allocate at
+ * this point: an application that hands the GPU's memory to its own pool or
+ * budget, or a latency-sensitive loop that must not call cudaMalloc/cudaFree
+ * because they can synchronise the device.  Its scratch is a fixed device
+ * array of 16384 x 5 + 8 doubles (~640 KB) that every GPU loading the library
+ * keeps until exit; it holds one partial sum row per 8 cells, so the finest
+ * level may have at most 131,072 cells (larger: CDG_ERR_LIMIT, use
+ * cdg_problem_errors).  The first call on a device looks up the array's
+ * device address; make that first call before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU (other streams, other host
+ * threads) race and must be serialised by the caller. */
+int cdg_problem_errors_noalloc(cdg_problem *p, const cdg_assembly_params *a,
+                               double *errors);
 
 /* ---- data access (host buffers) ----------------------------------------- */
 int cdg_problem_level_info(const cdg_problem *p, int level, int *info);

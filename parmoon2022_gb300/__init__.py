@@ -40,6 +40,7 @@ EXPORTED = [
     "cdg_problem_get_solution", "cdg_problem_set_solution", "cdg_problem_get_slots",
     "cdg_problem_apply", "cdg_problem_prolongate", "cdg_problem_restrict",
     "cdg_problem_precondition", "cdg_context_stream", "cdg_problem_time_kernel",
+    "cdg_problem_errors_noalloc",
 ]
 
 
@@ -112,6 +113,7 @@ def lib():
                                            ctypes.POINTER(SolverParams), dp, dp, dp,
                                            ctypes.POINTER(SolveStats)],
             "cdg_problem_errors": [P, ctypes.POINTER(AssemblyParams), dp],
+            "cdg_problem_errors_noalloc": [P, ctypes.POINTER(AssemblyParams), dp],
             "cdg_problem_level_info": [P, ctypes.c_int, ip],
             "cdg_problem_get_matrix": [P, ctypes.c_int, dp],
             "cdg_problem_get_rhs": [P, ctypes.c_int, dp],

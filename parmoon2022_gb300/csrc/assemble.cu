@@ -24,6 +24,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <mutex>
 
 #include "common.cuh"
 
@@ -873,3 +874,205 @@ int level_errors(cdg_context* ctx, cdg_problem* p, DevLevel& L, const cdg_assemb
 }
 
 }  // namespace cdg
+
+namespace cdg {
+
+// ---------------------------------------------------------------------------
+// Error norms without any allocation.
+//
+// cdg_problem_errors allocates a small accumulator on every call and keeps
+// reference tables it allocates on first use.  Some callers cannot allocate
+// device memory at that point: an application that hands the GPU's memory to
+// its own pool or budget and forbids allocations outside it, or a serving
+// loop that must not call cudaMalloc/cudaFree because those calls can
+// synchronise the whole device and stall work other streams have in flight.
+// cdg_problem_errors_noalloc computes the same norms with its scratch in the
+// fixed device array below, which every GPU that loads this library keeps
+// until the process exits.
+// ---------------------------------------------------------------------------
+constexpr int kNoAllocCellsPerBlock = 8;          // one warp per cell
+constexpr int kNoAllocMaxBlocks = 16384;          // -> at most 131,072 cells
+constexpr int kNoAllocMaxCells = kNoAllocCellsPerBlock * kNoAllocMaxBlocks;
+// layout: [block partials: kNoAllocMaxBlocks x 5][5 results][pad][counter]
+constexpr int kNoAllocSlots = kNoAllocMaxBlocks * 5 + 8;
+static __device__ __align__(256) double g_errors_noalloc_scratch[kNoAllocSlots];
+
+struct LineRule {
+  int n;
+  double x[kMaxQp1], w[kMaxQp1];
+};
+
+__device__ void line_basis_deriv(int p, double t, double* v, double* d) {
+  line_basis_d(p, t, v);
+  if (p == 1) {
+    d[0] = -0.5;
+    d[1] = 0.5;
+  } else {
+    d[0] = t - 0.5;
+    d[1] = -2.0 * t;
+    d[2] = t + 0.5;
+  }
+}
+
+// same norms as k_errors; basis values at the Gauss points are evaluated in
+// place from the 1D rule, and block partials go to the fixed scratch array;
+// the last block to finish sums them in block order
+template <int DIM>
+__global__ void __launch_bounds__(256)
+k_errors_noalloc(AsmCoefs k, LineRule rule, int ncells, const double* __restrict__ verts,
+                 const int* __restrict__ gdof, const double* __restrict__ sol,
+                 double* __restrict__ scratch) {
+  constexpr int NV = DIM == 2 ? 4 : 8;
+  __shared__ double wsum[kNoAllocCellsPerBlock][5];
+  __shared__ bool last;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int cell = blockIdx.x * kNoAllocCellsPerBlock + warp;
+  double e[4] = {0, 0, 0, 0}, emax = 0.0;
+  if (cell < ncells) {
+    const double* cv = verts + (size_t)cell * NV * DIM;
+    Affine A;
+    cell_affine(DIM, cv, A);
+    const double adet = fabs(A.det);
+    const double hK = cell_hK(DIM, cv, k.cell_measure, A.det);
+    const int nl = k.nloc, n1 = k.order + 1;
+    const double fv = lane < nl ? sol[gdof[(size_t)cell * nl + lane]] : 0.0;
+    double linfb = fmax(fabs(k.b[0]), fabs(k.b[1]));
+    if (DIM == 3) linfb = fmax(linfb, fabs(k.b[2]));
+    const double delta = sdfem_delta(k, hK, k.eps, k.b, k.c, linfb);
+    const int ki[3] = {lane % n1, (lane / n1) % n1, lane / (n1 * n1)};
+    const int nq = DIM == 2 ? rule.n * rule.n : rule.n * rule.n * rule.n;
+    for (int q = 0; q < nq; ++q) {
+      const int qi[3] = {q % rule.n, (q / rule.n) % rule.n, q / (rule.n * rule.n)};
+      double xi[3] = {rule.x[qi[0]], rule.x[qi[1]], DIM == 3 ? rule.x[qi[2]] : 0.0};
+      const double wq = rule.w[qi[0]] * rule.w[qi[1]] * (DIM == 3 ? rule.w[qi[2]] : 1.0);
+      double uh = 0.0, gr[3] = {0, 0, 0};
+      if (lane < nl) {
+        double v[3][3], d[3][3];
+        for (int a = 0; a < DIM; ++a) line_basis_deriv(k.order, xi[a], v[a], d[a]);
+        double val = v[0][ki[0]] * v[1][ki[1]] * (DIM == 3 ? v[2][ki[2]] : 1.0);
+        uh = fv * val;
+        gr[0] = fv * d[0][ki[0]] * v[1][ki[1]] * (DIM == 3 ? v[2][ki[2]] : 1.0);
+        gr[1] = fv * v[0][ki[0]] * d[1][ki[1]] * (DIM == 3 ? v[2][ki[2]] : 1.0);
+        if (DIM == 3) gr[2] = fv * v[0][ki[0]] * v[1][ki[1]] * d[2][ki[2]];
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        uh += __shfl_xor_sync(0xffffffffu, uh, o);
+        for (int a = 0; a < DIM; ++a) gr[a] += __shfl_xor_sync(0xffffffffu, gr[a], o);
+      }
+      if (lane == 0) {
+        double g[3] = {0, 0, 0};
+        for (int r = 0; r < DIM; ++r)
+          for (int a = 0; a < DIM; ++a) g[r] += A.Ji[a][r] * gr[a];
+        double x[3], u[5];
+        for (int r = 0; r < DIM; ++r) {
+          double s = A.x0[r];
+          for (int a = 0; a < DIM; ++a) s += A.J[r][a] * xi[a];
+          x[r] = s;
+        }
+        ex_exact(k, x, u);
+        const double w = wq * adet;
+        const double e0 = uh - u[0];
+        emax = fmax(emax, fabs(e0));
+        const double e1 = g[0] - u[1], e2 = g[1] - u[2], e3 = DIM == 2 ? 0.0 : g[2] - u[3];
+        e[0] += w * e0 * e0;
+        e[1] += w * (e1 * e1 + e2 * e2 + e3 * e3);
+        const double e4 = k.b[0] * e1 + k.b[1] * e2 + (DIM == 3 ? k.b[2] * e3 : 0.0);
+        e[2] += w * (k.eps * (e1 * e1 + e2 * e2 + e3 * e3) + k.c * e0 * e0 + delta * e4 * e4);
+        e[3] += w * (k.eps * (e1 * e1 + e2 * e2 + e3 * e3) + (e4 + k.c * e0) * e0);
+      }
+    }
+  }
+  if (lane == 0) {
+    for (int i = 0; i < 4; ++i) wsum[warp][i] = e[i];
+    wsum[warp][4] = emax;
+  }
+  __syncthreads();
+  unsigned* counter = reinterpret_cast<unsigned*>(scratch + kNoAllocSlots - 1);
+  if (threadIdx.x == 0) {
+    double b[5] = {0, 0, 0, 0, 0};
+    for (int w = 0; w < kNoAllocCellsPerBlock; ++w) {
+      for (int i = 0; i < 4; ++i) b[i] += wsum[w][i];
+      b[4] = fmax(b[4], wsum[w][4]);
+    }
+    for (int i = 0; i < 5; ++i) scratch[(size_t)blockIdx.x * 5 + i] = b[i];
+    __threadfence();
+    last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last || threadIdx.x != 0) return;
+  __threadfence();
+  double r[5] = {0, 0, 0, 0, 0};
+  for (int bl = 0; bl < (int)gridDim.x; ++bl) {
+    const volatile double* pb = scratch + (size_t)bl * 5;
+    for (int i = 0; i < 4; ++i) r[i] += pb[i];
+    r[4] = fmax(r[4], pb[4]);
+  }
+  for (int i = 0; i < 5; ++i) scratch[(size_t)kNoAllocMaxBlocks * 5 + i] = r[i];
+}
+
+}  // namespace cdg
+
+// per-device address of the scratch array, looked up once per device with the
+// device current (the symbol's host-side name is not a device address)
+static double* g_errors_noalloc_ptr[64];
+static std::once_flag g_errors_noalloc_once[64];
+static cudaError_t g_errors_noalloc_status[64];
+
+extern "C" int cdg_problem_errors_noalloc(cdg_problem* p, const cdg_assembly_params* a,
+                                          double* errors) {
+  using namespace cdg;
+  if (!p || !a || !errors) {
+    set_error("null argument");
+    return CDG_ERR_ARG;
+  }
+  if (a->example < 0 || a->example > CDG_EX_POLY1) {
+    set_error("unknown example %d", a->example);
+    return CDG_ERR_ARG;
+  }
+  cdg_context* ctx = p->ctx;
+  DevLevel& L = p->lev[0];
+  if (L.ncells > kNoAllocMaxCells) {
+    set_error("cdg_problem_errors_noalloc handles at most %d cells (its fixed scratch holds "
+              "%d block partials); this level has %d cells, use cdg_problem_errors",
+              kNoAllocMaxCells, kNoAllocMaxBlocks, L.ncells);
+    return CDG_ERR_LIMIT;
+  }
+  if (ctx->device < 0 || ctx->device >= 64) {
+    set_error("device index %d out of range", ctx->device);
+    return CDG_ERR_ARG;
+  }
+  CDG_CUDA(cudaSetDevice(ctx->device));
+  std::call_once(g_errors_noalloc_once[ctx->device], [&]() {
+    g_errors_noalloc_status[ctx->device] = cudaGetSymbolAddress(
+        (void**)&g_errors_noalloc_ptr[ctx->device], g_errors_noalloc_scratch);
+  });
+  if (g_errors_noalloc_status[ctx->device] != cudaSuccess) {
+    set_error("cudaGetSymbolAddress of the error-norm scratch failed: %s",
+              cudaGetErrorString(g_errors_noalloc_status[ctx->device]));
+    return CDG_ERR_CUDA;
+  }
+  double* scratch = g_errors_noalloc_ptr[ctx->device];
+  AsmCoefs k = make_coefs(*a, L.dim, L.order, L.nloc);
+  LineRule rule;
+  rule.n = k.nqp1;
+  gauss_legendre(rule.n, rule.x, rule.w);
+  // the last-block counter must start at zero on every call
+  CDG_CUDA(cudaMemsetAsync(scratch + kNoAllocSlots - 1, 0, sizeof(double), ctx->stream));
+  const int grid = (L.ncells + kNoAllocCellsPerBlock - 1) / kNoAllocCellsPerBlock;
+  if (L.dim == 2)
+    CDG_LAUNCH(ctx, k_errors_noalloc<2>, grid, 256, 0, k, rule, L.ncells, L.verts, L.gdof,
+               L.sol, scratch);
+  else
+    CDG_LAUNCH(ctx, k_errors_noalloc<3>, grid, 256, 0, k, rule, L.ncells, L.verts, L.gdof,
+               L.sol, scratch);
+  double h[5];
+  CDG_CUDA(cudaMemcpyAsync(h, scratch + (size_t)kNoAllocMaxBlocks * 5, 5 * sizeof(double),
+                           cudaMemcpyDeviceToHost, ctx->stream));
+  CDG_CUDA(cudaStreamSynchronize(ctx->stream));
+  errors[0] = sqrt(h[0]);
+  errors[1] = sqrt(h[1]);
+  errors[2] = sqrt(h[2]);
+  errors[3] = sqrt(fabs(h[3]));
+  errors[4] = h[4];
+  return CDG_OK;
+}
