@@ -50,6 +50,9 @@ extern "C" {
 #define CDG_EX_POLYEXP 2          /* u = xyz(1-x)(1-y)(1-z)exp(x)            */
 #define CDG_EX_CONST_F 3          /* f = 1, u = 0 on the boundary            */
 #define CDG_EX_POLY1 4            /* u = 1 + x + 2y (+3z)                    */
+#define CDG_EX_BUMP 5             /* f = 0, u = 0 on the boundary, initial
+                                     condition exp(-|x-c|^2 / (2 sigma^2))    */
+#define CDG_EX_POLY1_T 6          /* u = (1+t)(1 + x + 2y (+3z)), in time     */
 
 /* local assembling + example: LocalAssembling<d>(db, ConvDiff, {}, coeffs,
  * disctype) with the TDatabase globals the CD routines read */
@@ -66,6 +69,10 @@ typedef struct {
   int problem_linear;   /* INTERNAL_PROBLEM_LINEAR (quadrature degree 2p)     */
   int neumann_mask;     /* bit k: boundary component k is Neumann             */
   int poly_degree;      /* INTERNAL_POLYNOMIAL_DEGREE (0: element order)      */
+  double b_grad[9];     /* convection linear in x: b_i(x) = b[i] + sum_j
+                           b_grad[3i+j] x_j (zero: constant field)           */
+  double t;             /* time at which f and the boundary data are taken   */
+  double ic[4];         /* CDG_EX_BUMP: centre x, y, z and sigma              */
 } cdg_assembly_params;
 
 /* Solver ParameterDatabase keys (src/Solver/Solver.C:26-209,
@@ -100,6 +107,10 @@ typedef struct {
   double seconds;              /* wall time of the call                      */
 } cdg_solve_stats;
 
+#define CDG_CELL_QUAD 2
+#define CDG_CELL_HEXA 3
+#define CDG_CELL_TETRA 4
+
 typedef struct cdg_context cdg_context;     /* device + stream + scratch       */
 typedef struct cdg_hierarchy cdg_hierarchy; /* host mesh/space/pattern levels  */
 typedef struct cdg_problem cdg_problem;     /* ConvectionDiffusion<d>          */
@@ -126,6 +137,14 @@ int cdg_context_stream(cdg_context *ctx, void **stream);
  * Structure.C:226-618; GridTransfer.C:29-410) */
 int cdg_hierarchy_create(int dim, int order, int roots, int nref, int n_levels,
                          int neumann_mask, cdg_hierarchy **out);
+/* unit cube split into roots^3 cubes of 6 Kuhn tetrahedra, P1 or P2 (order),
+ * refined nref times (regular refinement, children of cell c are the eight
+ * cells 8c..8c+7 of the next level); perturb > 0 moves every interior vertex
+ * of the finest level by perturb*h*U(-1,1) per coordinate (seeded), as the
+ * perturbed-tetrahedra configuration of TCD3D asks */
+int cdg_hierarchy_create_tetra(int order, int roots, int nref, int n_levels,
+                               double perturb, unsigned long long seed,
+                               cdg_hierarchy **out);
 int cdg_hierarchy_destroy(cdg_hierarchy *h);
 /* info[0..5] = n_cells, n_local_dofs, n_dofs, n_active, nnz, verts_per_cell */
 int cdg_hierarchy_level_info(const cdg_hierarchy *h, int level, int *info);
@@ -139,11 +158,12 @@ int cdg_hierarchy_get_pattern(const cdg_hierarchy *h, int level, int *row_ptr,
 int cdg_problem_create(cdg_context *ctx, const cdg_hierarchy *h,
                        cdg_problem **out);
 /* drop-in form: the caller's own mesh, DOF map and pattern for n_levels
- * levels (finest first): cell_vertices[l] has n_cells[l]*2^dim*dim doubles in
- * the cell's vertex order, global_numbers[l] n_cells[l]*(order+1)^dim ints,
+ * levels (finest first); cell_type CDG_CELL_QUAD (2), CDG_CELL_HEXA (3) or
+ * CDG_CELL_TETRA (4): cell_vertices[l] has n_cells[l]*verts*dim doubles in
+ * the cell's vertex order, global_numbers[l] n_cells[l]*n_local_dofs ints,
  * row_ptr[l]/col[l] the TStructure, parent[l] (l>=1) the coarse cell of each
  * cell of level l-1 (NULL: cell/2^dim, regular refinement) */
-int cdg_problem_create_from_arrays(cdg_context *ctx, int dim, int order,
+int cdg_problem_create_from_arrays(cdg_context *ctx, int cell_type, int order,
                                    int n_levels, const int *n_cells,
                                    const double *const *cell_vertices,
                                    const int *const *global_numbers,
@@ -186,6 +206,23 @@ int cdg_problem_errors(cdg_problem *p, const cdg_assembly_params *a,
  * threads) race and must be serialised by the caller. */
 int cdg_problem_errors_noalloc(cdg_problem *p, const cdg_assembly_params *a,
                                double *errors);
+
+/* ---- time-dependent CD: TimeConvectionDiffusion<d> with Crank-Nicolson -- */
+/* assemble_initial_time (src/System/TimeConvectionDiffusion.C:260-311): on
+ * every level stiffness, mass and rhs at time a->t (Dirichlet rows assembled
+ * in full); the finest solution becomes the interpolant of the example's
+ * initial condition */
+int cdg_problem_tcd_initialize(cdg_problem *p, const cdg_assembly_params *a);
+/* one Crank-Nicolson step to time a->t = t_old + tau
+ * (TimeConvectionDiffusion.C:315-450, TimeDiscretizations.C:117-283):
+ * reassemble stiffness and rhs on every level, rhs = tau/2 (f_new + f_old) +
+ * M u_old - tau/2 A u_old on active rows, system M + tau/2 A on active rows,
+ * Dirichlet data at the new time, then Solver::solve warm-started from u_old */
+int cdg_problem_tcd_step(cdg_problem *p, const cdg_assembly_params *a, double tau,
+                         const cdg_solver_params *s, cdg_solve_stats *stats);
+/* which: 0 stiffness A, 1 mass M, 2 system matrix (after a step) */
+int cdg_problem_get_tcd_matrix(cdg_problem *p, int level, int which,
+                               double *values);
 
 /* ---- data access (host buffers) ----------------------------------------- */
 int cdg_problem_level_info(const cdg_problem *p, int level, int *info);

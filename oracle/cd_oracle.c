@@ -124,6 +124,24 @@ static void make_rule(int dim, int n1, quad_rule *q) {
   }
 }
 
+/* collapsed Gauss rule on the unit tetrahedron, n points per direction:
+ * xi = u, eta = v (1-u), zeta = w (1-u)(1-v), weight (1-u)^2 (1-v) / 8 */
+static void make_tet_rule(int n, quad_rule *q) {
+  double x[10], w[10];
+  gauss_legendre(n, x, w);
+  q->nqp = 0;
+  for (int k = 0; k < n; ++k)
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) {
+        double u = 0.5 * (x[i] + 1), v = 0.5 * (x[j] + 1), t = 0.5 * (x[k] + 1);
+        q->xi[q->nqp][0] = u;
+        q->xi[q->nqp][1] = v * (1 - u);
+        q->xi[q->nqp][2] = t * (1 - u) * (1 - v);
+        q->w[q->nqp++] = 0.125 * w[i] * w[j] * w[k] * (1 - u) * (1 - u) * (1 - v);
+      }
+}
+static int tet_points_for_degree(int deg) { return (deg + 4) / 2; }
+
 /* ------------------------------------------------------------------------ */
 /* Lagrange tensor basis Q1/Q2, derivatives up to order 2                    */
 /* ------------------------------------------------------------------------ */
@@ -174,6 +192,44 @@ static void ref_basis(int dim, int p, const double *xi, double out[][NDER]) {
           out[k][8] = a * d[1][k1] * d[2][k2];
           out[k][9] = a * b * dd[2][k2];
         }
+  }
+}
+
+/* P1/P2 on the unit tetrahedron, local DOF order of
+ * include/FE3D/BF_C_T_P2_3D.h: vertices 0,2,5,9, edge midpoints 1 (v0v1),
+ * 3 (v0v2), 4 (v1v2), 6 (v0v3), 7 (v1v3), 8 (v2v3); values laid out like
+ * ref_basis: [0] phi, [1..3] grad, [4..9] Hessian (xx,xy,xz,yy,yz,zz) */
+static const double TET_P2_NODES[10][3] = {{0, 0, 0}, {.5, 0, 0}, {1, 0, 0}, {0, .5, 0},
+                                           {.5, .5, 0}, {0, 1, 0}, {0, 0, .5}, {.5, 0, .5},
+                                           {0, .5, .5}, {0, 0, 1}};
+static const double TET_P1_NODES[4][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+static void tet_basis(int p, const double *xi, double out[][NDER]) {
+  double l[4] = {1 - xi[0] - xi[1] - xi[2], xi[0], xi[1], xi[2]};
+  double dl[4][3] = {{-1, -1, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  static const int hp[6][2] = {{0, 0}, {0, 1}, {0, 2}, {1, 1}, {1, 2}, {2, 2}};
+  if (p == 1) {
+    for (int k = 0; k < 4; ++k) {
+      out[k][0] = l[k];
+      for (int a = 0; a < 3; ++a) out[k][1 + a] = dl[k][a];
+      for (int s2 = 0; s2 < 6; ++s2) out[k][4 + s2] = 0;
+    }
+    return;
+  }
+  static const int va[10] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3};
+  static const int vb[10] = {0, 1, 1, 2, 2, 2, 3, 3, 3, 3};
+  for (int k = 0; k < 10; ++k) {
+    int a0 = va[k], b0 = vb[k];
+    if (a0 == b0) {
+      out[k][0] = l[a0] * (2 * l[a0] - 1);
+      for (int a = 0; a < 3; ++a) out[k][1 + a] = (4 * l[a0] - 1) * dl[a0][a];
+      for (int s2 = 0; s2 < 6; ++s2) out[k][4 + s2] = 4 * dl[a0][hp[s2][0]] * dl[a0][hp[s2][1]];
+    } else {
+      out[k][0] = 4 * l[a0] * l[b0];
+      for (int a = 0; a < 3; ++a) out[k][1 + a] = 4 * (dl[a0][a] * l[b0] + l[a0] * dl[b0][a]);
+      for (int s2 = 0; s2 < 6; ++s2)
+        out[k][4 + s2] = 4 * (dl[a0][hp[s2][0]] * dl[b0][hp[s2][1]] +
+                              dl[a0][hp[s2][1]] * dl[b0][hp[s2][0]]);
+    }
   }
 }
 
@@ -240,10 +296,14 @@ typedef struct {
   double *lu;       /* dense LU of the coarse matrix (coarsest level only) */
   int *piv;
   int lu_gen;       /* assembly generation the LU belongs to */
+  /* time-dependent problem: stiffness, mass, rhs of this and the last step */
+  double *tA, *tM, *tf, *tfold;
 } level_t;
 
 struct orc_problem {
   orc_config cfg;
+  int shape;        /* 0 quadrilateral, 1 hexahedron, 2 tetrahedron */
+  int from_arrays;  /* levels supplied by the caller */
   int nlev;
   level_t *lev;
   quad_rule qr;
@@ -397,10 +457,11 @@ static double cell_hK(int dim, const double *cv, int measure) {
 /* ------------------------------------------------------------------------ */
 /* examples: coefficients, exact solution, boundary data                      */
 /* ------------------------------------------------------------------------ */
-/* exact solution: u[0]=value, u[1..dim]=gradient, u[dim+1]=laplacian */
+/* exact solution: u[0]=value, u[1..dim]=gradient, u[dim+1]=laplacian,
+ * u[dim+2]=time derivative */
 static void exact_sol(const orc_config *c, const double *x, double *u) {
   int d = c->dim;
-  for (int k = 0; k < 5; ++k) u[k] = 0;
+  for (int k = 0; k < 6; ++k) u[k] = 0;
   switch (c->example) {
   case ORC_EX_SINE_LAPLACE:
   case ORC_EX_SINE: {
@@ -440,13 +501,27 @@ static void exact_sol(const orc_config *c, const double *x, double *u) {
     break;
   }
   case ORC_EX_POLY1:
-    u[0] = 1 + x[0] + 2 * x[1] + (d == 3 ? 3 * x[2] : 0);
-    u[1] = 1;
-    u[2] = 2;
-    if (d == 3) u[3] = 3;
+  case ORC_EX_POLY1_T: {
+    double sc = c->example == ORC_EX_POLY1_T ? 1 + c->t : 1.0;
+    double q = 1 + x[0] + 2 * x[1] + (d == 3 ? 3 * x[2] : 0);
+    u[0] = sc * q;
+    u[1] = sc;
+    u[2] = 2 * sc;
+    if (d == 3) u[3] = 3 * sc;
+    if (c->example == ORC_EX_POLY1_T) u[d + 2] = q;
     break;
+  }
   default:
     break;
+  }
+}
+
+/* convection at x: constant part plus the gradient times x */
+static void b_at(const orc_config *c, const double *x, double *bx) {
+  for (int i = 0; i < 3; ++i) {
+    double s = i < c->dim ? c->b[i] : 0.0;
+    for (int j = 0; j < c->dim; ++j) s += c->b_grad[3 * i + j] * x[j];
+    bx[i] = i < c->dim ? s : 0.0;
   }
 }
 
@@ -454,26 +529,42 @@ static void exact_sol(const orc_config *c, const double *x, double *u) {
  * co[d+3] = |b|_inf (ConvDiff.C:1858-1863, 1970-1976 coefficient layout) */
 static void coeffs_at(const orc_config *c, const double *x, double *co) {
   int d = c->dim;
+  double bx[3];
+  b_at(c, x, bx);
   co[0] = c->eps;
   double binf = 0;
   for (int a = 0; a < d; ++a) {
-    co[1 + a] = c->b[a];
-    if (fabs(c->b[a]) > binf) binf = fabs(c->b[a]);
+    co[1 + a] = bx[a];
+    if (fabs(bx[a]) > binf) binf = fabs(bx[a]);
   }
   co[d + 1] = c->c;
   if (c->example == ORC_EX_CONST_F) {
     co[d + 2] = 1.0;
+  } else if (c->example == ORC_EX_BUMP) {
+    co[d + 2] = 0.0;
   } else {
-    double u[5];
+    double u[6];
     exact_sol(c, x, u);
-    /* f = -eps lap u + b.grad u + c u, with the reference's summation order
-     * (SineLaplace.h BilinearCoeffs) */
+    /* f = u_t - eps lap u + b.grad u + c u, with the reference's summation
+     * order (SineLaplace.h BilinearCoeffs) */
     double f = -c->eps * u[d + 1];
-    for (int a = 0; a < d; ++a) f += c->b[a] * u[1 + a];
+    for (int a = 0; a < d; ++a) f += bx[a] * u[1 + a];
     f += c->c * u[0];
+    f += u[d + 2];
     co[d + 2] = f;
   }
   co[d + 3] = binf;
+}
+
+static double initial_value(const orc_config *c, const double *x) {
+  if (c->example == ORC_EX_BUMP) {
+    double r2 = 0;
+    for (int a = 0; a < c->dim; ++a) r2 += (x[a] - c->ic[a]) * (x[a] - c->ic[a]);
+    return exp(-r2 / (2 * c->ic[3] * c->ic[3]));
+  }
+  double u[6];
+  exact_sol(c, x, u);
+  return u[0];
 }
 
 /* boundary component of a boundary joint centre (2D: SineLaplace transform,
@@ -601,6 +692,85 @@ static void dof_position(int dim, int p, const double *cv, int k, double *x) {
   double r[3];
   local_dof_ref(dim, p, k, r);
   affine_map(dim, &A, r, x);
+}
+
+/* shape-aware cell helpers (shape 2: tetrahedron; TetraAffin.C:235-265:
+ * x = v0 + (v1-v0) xi + (v2-v0) eta + (v3-v0) zeta) */
+static void cell_affine_s(int shape, int dim, const double *cv, affine_t *A) {
+  if (shape != 2) {
+    cell_affine(dim, cv, A);
+    return;
+  }
+  for (int r = 0; r < 3; ++r) {
+    A->x0[r] = cv[r];
+    for (int a = 0; a < 3; ++a) A->J[r][a] = cv[(a + 1) * 3 + r] - cv[r];
+  }
+  double(*J)[3] = A->J;
+  double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+               J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+               J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+  A->det = det;
+  A->Jinv[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) / det;
+  A->Jinv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
+  A->Jinv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
+  A->Jinv[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) / det;
+  A->Jinv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
+  A->Jinv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
+  A->Jinv[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) / det;
+  A->Jinv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
+  A->Jinv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+}
+
+/* Tetrahedron.C:64-113 (diameter = longest edge, shortest edge) */
+static double cell_hK_s(int shape, int dim, const double *cv, int measure) {
+  if (shape != 2) return cell_hK(dim, cv, measure);
+  if (measure == 1 || measure == 3) {
+    affine_t A;
+    cell_affine_s(2, 3, cv, &A);
+    return sqrt(fabs(A.det) / 6.0);
+  }
+  double m = measure == 2 ? 1e10 : 0.0;
+  for (int i = 0; i < 4; ++i)
+    for (int j = i + 1; j < 4; ++j) {
+      double s2 = 0;
+      for (int a = 0; a < 3; ++a) {
+        double dd = cv[i * 3 + a] - cv[j * 3 + a];
+        s2 += dd * dd;
+      }
+      if (measure == 2 ? s2 < m : s2 > m) m = s2;
+    }
+  return sqrt(m);
+}
+
+static void basis_s(int shape, int dim, int p, const double *xi, double out[][NDER]) {
+  if (shape == 2)
+    tet_basis(p, xi, out);
+  else
+    ref_basis(dim, p, xi, out);
+}
+
+static void local_dof_ref_s(int shape, int dim, int p, int k, double *r) {
+  if (shape == 2) {
+    const double *q = p == 1 ? TET_P1_NODES[k] : TET_P2_NODES[k];
+    r[0] = q[0];
+    r[1] = q[1];
+    r[2] = q[2];
+    return;
+  }
+  local_dof_ref(dim, p, k, r);
+}
+
+static void dof_position_s(int shape, int dim, int p, const double *cv, int k, double *x) {
+  affine_t A;
+  cell_affine_s(shape, dim, cv, &A);
+  double r[3];
+  local_dof_ref_s(shape, dim, p, k, r);
+  affine_map(dim, &A, r, x);
+}
+
+static int nloc_of(int shape, int dim, int p) {
+  if (shape == 2) return p == 1 ? 4 : 10;
+  return dim == 2 ? (p + 1) * (p + 1) : (p + 1) * (p + 1) * (p + 1);
 }
 
 static int build_space(const orc_config *cfg, level_t *L, int nref) {
@@ -848,8 +1018,13 @@ orc_problem *orc_create(const orc_config *cfg, int n_levels) {
     snprintf(g_err, sizeof g_err, "bad number of levels");
     return NULL;
   }
+  if (cfg->tetra) {
+    snprintf(g_err, sizeof g_err, "tetrahedral levels come from orc_create_from_arrays");
+    return NULL;
+  }
   orc_problem *p = (orc_problem *)calloc(1, sizeof(orc_problem));
   p->cfg = *cfg;
+  p->shape = cfg->dim == 2 ? 0 : 1;
   if (p->cfg.poly_degree <= 0) p->cfg.poly_degree = cfg->order;
   p->nlev = n_levels;
   p->lev = (level_t *)calloc(n_levels, sizeof(level_t));
@@ -888,9 +1063,71 @@ void orc_destroy(orc_problem *p) {
     free(L->val); free(L->rhs); free(L->sol); free(L->diag);
     free(L->mg_rhs); free(L->mg_sol); free(L->mg_def);
     free(L->lu); free(L->piv);
+    free(L->tA); free(L->tM); free(L->tf); free(L->tfold);
   }
   free(p->lev);
   free(p);
+}
+
+/* ConvectionDiffusion<d> on the caller's levels: the FE spaces, DOF maps and
+ * TStructure patterns are taken as given (FESpace GlobalNumbers,
+ * TStructure row_ptr/columns), the cell type from cfg->tetra / cfg->dim */
+orc_problem *orc_create_from_arrays(const orc_config *cfg, int n_levels,
+                                    const int *ncells, const double *const *verts,
+                                    const int *const *gdof, const int *ndof,
+                                    const int *nactive, const int *const *row_ptr,
+                                    const int *const *col) {
+  if (cfg->dim != 2 && cfg->dim != 3) {
+    snprintf(g_err, sizeof g_err, "dim must be 2 or 3");
+    return NULL;
+  }
+  if ((cfg->order != 1 && cfg->order != 2) || (cfg->tetra && cfg->dim != 3) ||
+      n_levels < 1) {
+    snprintf(g_err, sizeof g_err, "bad order, cell type or number of levels");
+    return NULL;
+  }
+  orc_problem *p = (orc_problem *)calloc(1, sizeof(orc_problem));
+  p->cfg = *cfg;
+  p->shape = cfg->tetra ? 2 : (cfg->dim == 2 ? 0 : 1);
+  p->from_arrays = 1;
+  if (p->cfg.poly_degree <= 0) p->cfg.poly_degree = cfg->order;
+  p->nlev = n_levels;
+  p->lev = (level_t *)calloc(n_levels, sizeof(level_t));
+  int dim = cfg->dim;
+  for (int k = 0; k < n_levels; ++k) {
+    level_t *L = &p->lev[k];
+    L->nv = p->shape == 2 ? 4 : nverts(dim);
+    L->nloc = nloc_of(p->shape, dim, cfg->order);
+    L->ncells = ncells[k];
+    L->ndof = ndof[k];
+    L->nactive = nactive[k];
+    L->nnz = row_ptr[k][ndof[k]];
+    size_t nvd = (size_t)L->ncells * L->nv * dim, ng = (size_t)L->ncells * L->nloc;
+    L->verts = (double *)malloc(sizeof(double) * nvd);
+    memcpy(L->verts, verts[k], sizeof(double) * nvd);
+    L->gdof = (int *)malloc(sizeof(int) * ng);
+    memcpy(L->gdof, gdof[k], sizeof(int) * ng);
+    L->row_ptr = (int *)malloc(sizeof(int) * (L->ndof + 1));
+    memcpy(L->row_ptr, row_ptr[k], sizeof(int) * (L->ndof + 1));
+    L->col = (int *)malloc(sizeof(int) * (L->nnz ? L->nnz : 1));
+    memcpy(L->col, col[k], sizeof(int) * L->nnz);
+    L->val = (double *)calloc(L->nnz, sizeof(double));
+    L->rhs = (double *)calloc(L->ndof, sizeof(double));
+    L->sol = (double *)calloc(L->ndof, sizeof(double));
+    L->diag = (double *)calloc(L->ndof, sizeof(double));
+    L->mg_rhs = (double *)calloc(L->ndof, sizeof(double));
+    L->mg_sol = (double *)calloc(L->ndof, sizeof(double));
+    L->mg_def = (double *)calloc(L->ndof, sizeof(double));
+  }
+  int nterms = cfg->problem_linear ? 2 : 3;
+  if (p->shape == 2) {
+    p->nqp1 = tet_points_for_degree(nterms * cfg->order);
+    make_tet_rule(p->nqp1, &p->qr);
+  } else {
+    p->nqp1 = gauss_points_for_degree(nterms * cfg->order);
+    make_rule(dim, p->nqp1, &p->qr);
+  }
+  return p;
 }
 
 int orc_level_info(const orc_problem *p, int level, int *info) {
@@ -1002,15 +1239,15 @@ int orc_local_system(orc_problem *p, int level, int cell, double *Aloc,
   int dim = c->dim, nl = L->nloc;
   const double *cv = L->verts + (size_t)cell * L->nv * dim;
   affine_t A;
-  cell_affine(dim, cv, &A);
+  cell_affine_s(p->shape, dim, cv, &A);
   double adet = fabs(A.det);
-  double hK = cell_hK(dim, cv, c->cell_measure);
+  double hK = cell_hK_s(p->shape, dim, cv, c->cell_measure);
   for (int i = 0; i < nl * nl; ++i) Aloc[i] = 0;
   for (int i = 0; i < nl; ++i) floc[i] = 0;
   double ref[MAXLOC][NDER];
   int nh = dim == 2 ? 3 : 6;
   for (int q = 0; q < p->qr.nqp; ++q) {
-    ref_basis(dim, c->order, p->qr.xi[q], ref);
+    basis_s(p->shape, dim, c->order, p->qr.xi[q], ref);
     /* GetOrigValues: physical derivatives */
     double u[MAXLOC], g[MAXLOC][3], lap[MAXLOC];
     for (int k = 0; k < nl; ++k) {
@@ -1098,7 +1335,7 @@ static void neumann_edge(orc_problem *p, level_t *L, int cell, int j,
   for (int l = 0; l < np; ++l) {
     double s = 0.5 * (lx[l] + 1);
     double x[2] = {a[0] + s * (bb[0] - a[0]), a[1] + s * (bb[1] - a[1])};
-    double u[5];
+    double u[6];
     exact_sol(c, x, u);
     double g = c->eps * (nrm[comp][0] * u[1] + nrm[comp][1] * u[2]);
     /* reference coordinates of x */
@@ -1118,37 +1355,84 @@ static void neumann_edge(orc_problem *p, level_t *L, int cell, int j,
   }
 }
 
-static int assemble_level(orc_problem *p, int level) {
+/* local mass matrix, TCDMass (CD_local_assembling_routines.C:156-167):
+ * M_ij = int phi_i phi_j */
+static void local_mass(orc_problem *p, level_t *L, int cell, double *Mloc) {
+  int dim = p->cfg.dim, nl = L->nloc;
+  const double *cv = L->verts + (size_t)cell * L->nv * dim;
+  affine_t A;
+  cell_affine_s(p->shape, dim, cv, &A);
+  double adet = fabs(A.det);
+  for (int i = 0; i < nl * nl; ++i) Mloc[i] = 0;
+  double ref[MAXLOC][NDER];
+  for (int q = 0; q < p->qr.nqp; ++q) {
+    basis_s(p->shape, dim, p->cfg.order, p->qr.xi[q], ref);
+    double Mult = p->qr.w[q] * adet;
+    for (int i = 0; i < nl; ++i)
+      for (int j = 0; j < nl; ++j) Mloc[i * nl + j] += Mult * ref[j][0] * ref[i][0];
+  }
+}
+
+/* scatter of a local matrix by linear row search (Assemble3D.C:257-292) */
+static int scatter_row(const level_t *L, int l, const int *dof, const double *row,
+                       double *val) {
+  for (int k = 0; k < L->nloc; ++k) {
+    int found = 0;
+    for (int n = L->row_ptr[l]; n < L->row_ptr[l + 1]; ++n)
+      if (L->col[n] == dof[k]) {
+        val[n] += row[k];
+        found = 1;
+        break;
+      }
+    if (!found) FAIL("entry not in pattern");
+  }
+  return 0;
+}
+
+/* Assemble2D/3D over one level into (val, rhs).  all_rows: Dirichlet rows
+ * receive the full local rows (assemble_dirichlet_rows, as the time-dependent
+ * problem does); otherwise they are identity rows (Matrix.C:225-233).
+ * mval != NULL: the mass matrix is assembled alongside. */
+static int assemble_into(orc_problem *p, int level, double *val, double *rhs,
+                         int all_rows, double *mval) {
   const orc_config *c = &p->cfg;
   level_t *L = &p->lev[level];
   int dim = c->dim, nl = L->nloc;
-  memset(L->val, 0, sizeof(double) * L->nnz);
-  memset(L->rhs, 0, sizeof(double) * L->ndof);
-  double Aloc[MAXLOC * MAXLOC], floc[MAXLOC];
+  memset(val, 0, sizeof(double) * L->nnz);
+  memset(rhs, 0, sizeof(double) * L->ndof);
+  if (mval) memset(mval, 0, sizeof(double) * L->nnz);
+  double Aloc[MAXLOC * MAXLOC], floc[MAXLOC], Mloc[MAXLOC * MAXLOC];
   for (int cell = 0; cell < L->ncells; ++cell) {
     orc_local_system(p, level, cell, Aloc, floc);
+    if (mval) local_mass(p, L, cell, Mloc);
     const int *dof = L->gdof + cell * nl;
-    /* scatter by linear row search (Assemble3D.C:257-292) */
     for (int m = 0; m < nl; ++m) {
       int l = dof[m];
-      if (l < L->nactive) {
-        for (int k = 0; k < nl; ++k) {
-          int found = 0;
-          for (int n = L->row_ptr[l]; n < L->row_ptr[l + 1]; ++n)
-            if (L->col[n] == dof[k]) {
-              L->val[n] += Aloc[m * nl + k];
-              found = 1;
-              break;
-            }
-          if (!found) FAIL("entry not in pattern");
-        }
-        L->rhs[l] += floc[m];
+      if (l < L->nactive || all_rows) {
+        if (scatter_row(L, l, dof, Aloc + m * nl, val)) return -1;
+        if (mval && scatter_row(L, l, dof, Mloc + m * nl, mval)) return -1;
+        if (l < L->nactive) rhs[l] += floc[m];
       } else {
-        /* Dirichlet row: set(l, l, 1) (Matrix.C:225-233) */
         for (int n = L->row_ptr[l]; n < L->row_ptr[l + 1]; ++n)
-          if (L->col[n] == l) L->val[n] = 1.0;
+          if (L->col[n] == l) val[n] = 1.0;
       }
     }
+  }
+  if (p->shape == 2) {
+    /* tetrahedra: every non-active DOF is a Dirichlet node; value = nodal
+     * functional of P1/P2 = point value */
+    for (int cell = 0; cell < L->ncells; ++cell) {
+      const double *cv = L->verts + (size_t)cell * L->nv * dim;
+      for (int k = 0; k < nl; ++k) {
+        int d = L->gdof[cell * nl + k];
+        if (d < L->nactive) continue;
+        double x[3], u[6];
+        dof_position_s(2, 3, c->order, cv, k, x);
+        exact_sol(c, x, u);
+        rhs[d] = u[0];
+      }
+    }
+    return 0;
   }
   /* boundary data: Dirichlet values by point evaluation at the nodes (nodal
    * functionals of Q1/Q2), Neumann integrals (2D) */
@@ -1168,16 +1452,22 @@ static int assemble_level(orc_problem *p, int level) {
         int idx[MAXLOC];
         int n = joint_dofs(dim, c->order, j, idx);
         for (int m = 0; m < n; ++m) {
-          double x[3], u[5];
+          double x[3], u[6];
           dof_position(dim, c->order, cv, idx[m], x);
           exact_sol(c, x, u);
-          L->rhs[L->gdof[cell * nl + idx[m]]] = u[0];
+          rhs[L->gdof[cell * nl + idx[m]]] = u[0];
         }
       } else if (dim == 2) {
-        neumann_edge(p, L, cell, j, L->rhs);
+        neumann_edge(p, L, cell, j, rhs);
       }
     }
   }
+  return 0;
+}
+
+static int assemble_level(orc_problem *p, int level) {
+  level_t *L = &p->lev[level];
+  if (assemble_into(p, level, L->val, L->rhs, 0, NULL)) return -1;
   /* solution.copy_nonactive(rhs) (ConvectionDiffusion.C:445) */
   for (int i = L->nactive; i < L->ndof; ++i) L->sol[i] = L->rhs[i];
   /* diagonal for Jacobi (Iteration_jacobi.C:14-28) */
@@ -1227,22 +1517,22 @@ static double dot(int n, const double *a, const double *b) {
 static void child_prolongation(const orc_problem *p, const level_t *Lf,
                                const level_t *Lc, int fcell, double *QQ) {
   int dim = p->cfg.dim, nl = Lf->nloc;
-  int nch = dim == 2 ? 4 : 8;
+  int nch = dim == 2 ? 4 : 8;   /* children per cell, also 8 for tetrahedra */
   int ccell = fcell / nch;
   const double *cvc = Lc->verts + (size_t)ccell * Lc->nv * dim;
   const double *cvf = Lf->verts + (size_t)fcell * Lf->nv * dim;
   affine_t Ac;
-  cell_affine(dim, cvc, &Ac);
+  cell_affine_s(p->shape, dim, cvc, &Ac);
   for (int k = 0; k < nl; ++k) {
     double x[3], xi[3] = {0, 0, 0};
-    dof_position(dim, p->cfg.order, cvf, k, x);
+    dof_position_s(p->shape, dim, p->cfg.order, cvf, k, x);
     for (int a = 0; a < dim; ++a) {
       double t = 0;
       for (int r = 0; r < dim; ++r) t += Ac.Jinv[a][r] * (x[r] - Ac.x0[r]);
       xi[a] = t;
     }
     double ref[MAXLOC][NDER];
-    ref_basis(dim, p->cfg.order, xi, ref);
+    basis_s(p->shape, dim, p->cfg.order, xi, ref);
     for (int l = 0; l < nl; ++l) QQ[k * nl + l] = ref[l][0];
   }
 }
@@ -1668,13 +1958,13 @@ int orc_errors(const orc_problem *p, double *errors) {
   for (int cell = 0; cell < L->ncells; ++cell) {
     const double *cv = L->verts + (size_t)cell * L->nv * dim;
     affine_t A;
-    cell_affine(dim, cv, &A);
-    double hK = cell_hK(dim, cv, c->cell_measure);
+    cell_affine_s(p->shape, dim, cv, &A);
+    double hK = cell_hK_s(p->shape, dim, cv, c->cell_measure);
     double fv[MAXLOC];
     for (int k = 0; k < nl; ++k) fv[k] = L->sol[L->gdof[cell * nl + k]];
     for (int q = 0; q < p->qr.nqp; ++q) {
       double ref[MAXLOC][NDER];
-      ref_basis(dim, c->order, p->qr.xi[q], ref);
+      basis_s(p->shape, dim, c->order, p->qr.xi[q], ref);
       double der[4] = {0, 0, 0, 0};
       for (int k = 0; k < nl; ++k) {
         der[0] += fv[k] * ref[k][0];
@@ -1688,7 +1978,7 @@ int orc_errors(const orc_problem *p, double *errors) {
         }
         der[1 + r] = s;
       }
-      double x[3], u[5], co[8];
+      double x[3], u[6], co[8];
       affine_map(dim, &A, p->qr.xi[q], x);
       exact_sol(c, x, u);
       coeffs_at(c, x, co);
@@ -1719,5 +2009,98 @@ int orc_errors(const orc_problem *p, double *errors) {
   errors[2] = sqrt(e[2]);
   errors[3] = sqrt(fabs(e[3]));
   errors[4] = maxe;
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* TimeConvectionDiffusion, Crank-Nicolson                                    */
+/* ------------------------------------------------------------------------ */
+static void ensure_tcd(level_t *L) {
+  if (L->tA) return;
+  L->tA = (double *)calloc(L->nnz ? L->nnz : 1, sizeof(double));
+  L->tM = (double *)calloc(L->nnz ? L->nnz : 1, sizeof(double));
+  L->tf = (double *)calloc(L->ndof, sizeof(double));
+  L->tfold = (double *)calloc(L->ndof, sizeof(double));
+}
+
+/* TimeConvectionDiffusion::assemble_initial_time (TimeConvectionDiffusion.C
+ * call_assembling_routine with assemble_dirichlet_rows): stiffness, mass and
+ * rhs at cfg.t on every level, old_rhs = rhs, then the initial condition
+ * interpolated into the finest solution (every DOF) */
+int orc_tcd_initialize(orc_problem *p) {
+  if (p->cfg.supg) FAIL("SUPG for the time-dependent problem is not supported");
+  for (int k = 0; k < p->nlev; ++k) {
+    level_t *L = &p->lev[k];
+    ensure_tcd(L);
+    if (assemble_into(p, k, L->tA, L->tf, 1, L->tM)) return -1;
+    memcpy(L->tfold, L->tf, sizeof(double) * L->ndof);
+  }
+  level_t *F = &p->lev[0];
+  int dim = p->cfg.dim, nl = F->nloc;
+  for (int cell = 0; cell < F->ncells; ++cell) {
+    const double *cv = F->verts + (size_t)cell * F->nv * dim;
+    for (int k = 0; k < nl; ++k) {
+      double x[3];
+      dof_position_s(p->shape, dim, p->cfg.order, cv, k, x);
+      F->sol[F->gdof[cell * nl + k]] = initial_value(&p->cfg, x);
+    }
+  }
+  return 0;
+}
+
+/* one Crank-Nicolson step (TimeDiscretizations.C:171-189 rhs, :219-251
+ * system matrix; TimeConvectionDiffusion::assemble / solve):
+ *   rhs (active)     = tau/2 (f_new + f_old) + M u_old - tau/2 A u_old
+ *   rhs (non-active) = f_new (Dirichlet data at t_new), copied into u
+ *   S (active rows)  = tau/2 A + M, Dirichlet rows keep A
+ * then FGMRES on S from u_old */
+int orc_tcd_step(orc_problem *p, double t_new, double tau, const orc_solver_config *s,
+                 int *iterations, double *residual, double *initial_residual) {
+  if (!p->lev[0].tA) FAIL("call orc_tcd_initialize first");
+  if (!(tau > 0)) FAIL("time step must be positive");
+  p->cfg.t = t_new;
+  for (int k = 0; k < p->nlev; ++k) {
+    level_t *L = &p->lev[k];
+    if (assemble_into(p, k, L->tA, L->tf, 1, NULL)) return -1;
+  }
+  level_t *F = &p->lev[0];
+  double ht = 0.5 * tau;
+  for (int r = 0; r < F->ndof; ++r) {
+    if (r < F->nactive) {
+      double sa = 0, sm = 0;
+      for (int n = F->row_ptr[r]; n < F->row_ptr[r + 1]; ++n) {
+        sa += F->tA[n] * F->sol[F->col[n]];
+        sm += F->tM[n] * F->sol[F->col[n]];
+      }
+      double v = ht * F->tf[r];
+      v += ht * F->tfold[r];
+      v += sm;
+      v += -ht * sa;
+      F->rhs[r] = v;
+    } else {
+      F->rhs[r] = F->tf[r];
+    }
+  }
+  memcpy(F->tfold, F->tf, sizeof(double) * F->ndof);
+  for (int r = F->nactive; r < F->ndof; ++r) F->sol[r] = F->rhs[r];
+  for (int k = 0; k < p->nlev; ++k) {
+    level_t *L = &p->lev[k];
+    int nae = L->row_ptr[L->nactive];
+    for (int n = 0; n < L->nnz; ++n)
+      L->val[n] = n < nae ? L->tA[n] * ht + L->tM[n] : L->tA[n];
+    for (int r = 0; r < L->ndof; ++r)
+      for (int n = L->row_ptr[r]; n < L->row_ptr[r + 1]; ++n)
+        if (L->col[n] == r) L->diag[r] = L->val[n];
+  }
+  p->asm_gen++;
+  return orc_solve(p, s, iterations, residual, initial_residual);
+}
+
+int orc_get_tcd_matrix(const orc_problem *p, int level, int which, double *val) {
+  if (level < 0 || level >= p->nlev || which < 0 || which > 2) FAIL("bad arguments");
+  const level_t *L = &p->lev[level];
+  if (!L->tA) FAIL("no time-dependent matrices");
+  const double *src = which == 0 ? L->tA : which == 1 ? L->tM : L->val;
+  memcpy(val, src, sizeof(double) * L->nnz);
   return 0;
 }

@@ -24,7 +24,9 @@ enum {
   ORC_EX_SINE = 1,         /* u = prod sin(k pi x_i), homogeneous Dirichlet    */
   ORC_EX_POLYEXP = 2,      /* u = x y z (1-x)(1-y)(1-z) exp(x) (3D)            */
   ORC_EX_CONST_F = 3,      /* f = 1, homogeneous Dirichlet, no exact solution  */
-  ORC_EX_POLY1 = 4         /* u = 1 + x + 2y (+3z): inside Q1, Dirichlet       */
+  ORC_EX_POLY1 = 4,        /* u = 1 + x + 2y (+3z): inside Q1, Dirichlet       */
+  ORC_EX_BUMP = 5,         /* f = 0, u_D = 0, u0 = exp(-|x-c|^2/(2 s^2))       */
+  ORC_EX_POLY1_T = 6       /* u = (1+t)(1 + x + 2y (+3z))                      */
 };
 
 typedef struct {
@@ -43,6 +45,10 @@ typedef struct {
   int problem_linear;  /* TDatabase INTERNAL_PROBLEM_LINEAR (quad. degree)    */
   int neumann_mask;    /* bit k: boundary component k is Neumann              */
   int poly_degree;     /* TDatabase INTERNAL_POLYNOMIAL_DEGREE (SDFEM 1/2)    */
+  int tetra;           /* cells are tetrahedra (P1/P2); arrays constructor    */
+  double b_grad[9];    /* b_i(x) = b[i] + sum_j b_grad[3i+j] x_j              */
+  double t;            /* time of f and the boundary data                     */
+  double ic[4];        /* ORC_EX_BUMP centre and sigma                        */
 } orc_config;
 
 typedef struct {
@@ -69,6 +75,22 @@ typedef struct orc_problem orc_problem;
  * nref-k refinements. */
 orc_problem *orc_create(const orc_config *cfg, int n_levels);
 void orc_destroy(orc_problem *p);
+/* levels from the caller's arrays (finest first): cell vertices, DOF map,
+ * numbers of DOFs / actives and CSR pattern per level; parents implied by
+ * regular refinement (fine cell f has coarse parent f / 2^dim) */
+orc_problem *orc_create_from_arrays(const orc_config *cfg, int n_levels,
+                                    const int *ncells, const double *const *verts,
+                                    const int *const *gdof, const int *ndof,
+                                    const int *nactive, const int *const *row_ptr,
+                                    const int *const *col);
+/* TimeConvectionDiffusion with Crank-Nicolson: initialize (assemble stiffness,
+ * mass and rhs at cfg.t on every level, interpolate the initial condition),
+ * one step to time t_new with time step tau, matrices for parity checks */
+int orc_tcd_initialize(orc_problem *p);
+int orc_tcd_step(orc_problem *p, double t_new, double tau, const orc_solver_config *s,
+                 int *iterations, double *residual, double *initial_residual);
+/* which: 0 stiffness, 1 mass, 2 system */
+int orc_get_tcd_matrix(const orc_problem *p, int level, int which, double *val);
 
 /* info[0..5] = ncells, nloc, ndof, nactive, nnz, nverts_per_cell */
 int orc_level_info(const orc_problem *p, int level, int *info);

@@ -12,7 +12,7 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "libcd_oracle.so")
 
-EX_SINE_LAPLACE, EX_SINE, EX_POLYEXP, EX_CONST_F, EX_POLY1 = range(5)
+EX_SINE_LAPLACE, EX_SINE, EX_POLYEXP, EX_CONST_F, EX_POLY1, EX_BUMP, EX_POLY1_T = range(7)
 
 
 class Config(ctypes.Structure):
@@ -24,7 +24,9 @@ class Config(ctypes.Structure):
         ("sdfem_type", ctypes.c_int), ("delta0", ctypes.c_double),
         ("delta1", ctypes.c_double), ("cell_measure", ctypes.c_int),
         ("problem_linear", ctypes.c_int), ("neumann_mask", ctypes.c_int),
-        ("poly_degree", ctypes.c_int),
+        ("poly_degree", ctypes.c_int), ("tetra", ctypes.c_int),
+        ("b_grad", ctypes.c_double * 9), ("t", ctypes.c_double),
+        ("ic", ctypes.c_double * 4),
     ]
 
 
@@ -62,6 +64,10 @@ def lib():
         L.orc_create.restype = P
         L.orc_create.argtypes = [ctypes.POINTER(Config), ctypes.c_int]
         L.orc_destroy.argtypes = [P]
+        L.orc_create_from_arrays.restype = P
+        L.orc_create_from_arrays.argtypes = [
+            ctypes.POINTER(Config), ctypes.c_int, ip, ctypes.POINTER(dp),
+            ctypes.POINTER(ip), ip, ip, ctypes.POINTER(ip), ctypes.POINTER(ip)]
         L.orc_last_error.restype = ctypes.c_char_p
         for name, args in [
             ("orc_level_info", [P, ctypes.c_int, ip]),
@@ -80,6 +86,10 @@ def lib():
             ("orc_mg_apply", [P, ctypes.POINTER(SolverConfig), dp, dp]),
             ("orc_solve", [P, ctypes.POINTER(SolverConfig), ip, dp, dp]),
             ("orc_errors", [P, dp]),
+            ("orc_tcd_initialize", [P]),
+            ("orc_tcd_step", [P, ctypes.c_double, ctypes.c_double,
+                              ctypes.POINTER(SolverConfig), ip, dp, dp]),
+            ("orc_get_tcd_matrix", [P, ctypes.c_int, ctypes.c_int, dp]),
         ]:
             f = getattr(L, name)
             f.restype = ctypes.c_int
@@ -98,7 +108,8 @@ def _ip(a):
 
 def make_config(dim, order, nref, example, eps=1.0, b=(0, 0, 0), c=0.0, freq=1.0,
                 supg=False, sdfem_type=2, delta0=1.0, delta1=1.0, cell_measure=0,
-                problem_linear=0, neumann_mask=0, poly_degree=0):
+                problem_linear=0, neumann_mask=0, poly_degree=0, tetra=False,
+                b_grad=None, t=0.0, ic=(0.5, 0.5, 0.5, 0.1)):
     cfg = Config()
     cfg.dim, cfg.order, cfg.nref, cfg.example = dim, order, nref, example
     cfg.eps = eps
@@ -108,6 +119,14 @@ def make_config(dim, order, nref, example, eps=1.0, b=(0, 0, 0), c=0.0, freq=1.0
     cfg.sdfem_type, cfg.delta0, cfg.delta1 = sdfem_type, delta0, delta1
     cfg.cell_measure, cfg.problem_linear = cell_measure, problem_linear
     cfg.neumann_mask, cfg.poly_degree = neumann_mask, poly_degree
+    cfg.tetra = int(tetra)
+    if b_grad is not None:
+        bg = np.asarray(b_grad, dtype=np.float64).reshape(-1)
+        for i in range(9):
+            cfg.b_grad[i] = float(bg[i])
+    cfg.t = t
+    for i in range(4):
+        cfg.ic[i] = ic[i]
     return cfg
 
 
@@ -131,10 +150,33 @@ def make_solver(precond="jacobi", max_it=1000, min_it=0, restart=50, tol_abs=0.0
 class Problem:
     """One CD problem on a hierarchy of uniformly refined grids (level 0 finest)."""
 
-    def __init__(self, cfg, n_levels=1):
+    def __init__(self, cfg, n_levels=1, arrays=None):
+        """arrays: list (finest first) of dicts with verts (ncells, nv, dim),
+        gdof (ncells, nloc), ndof, nactive, row_ptr, col -- the levels are
+        taken as given (orc_create_from_arrays)."""
         self.cfg = cfg
         self.n_levels = n_levels
-        self.h = lib().orc_create(ctypes.byref(cfg), n_levels)
+        if arrays is None:
+            self.h = lib().orc_create(ctypes.byref(cfg), n_levels)
+        else:
+            n = len(arrays)
+            self.n_levels = n
+            keep = []
+            ncells = np.array([a["gdof"].shape[0] for a in arrays], dtype=np.int32)
+            ndof = np.array([a["ndof"] for a in arrays], dtype=np.int32)
+            nact = np.array([a["nactive"] for a in arrays], dtype=np.int32)
+            dp = ctypes.POINTER(ctypes.c_double)
+            ipt = ctypes.POINTER(ctypes.c_int)
+            vp, gp, rp, cp = (dp * n)(), (ipt * n)(), (ipt * n)(), (ipt * n)()
+            for k, a in enumerate(arrays):
+                v = np.ascontiguousarray(a["verts"], dtype=np.float64)
+                g = np.ascontiguousarray(a["gdof"], dtype=np.int32)
+                r = np.ascontiguousarray(a["row_ptr"], dtype=np.int32)
+                c = np.ascontiguousarray(a["col"], dtype=np.int32)
+                keep += [v, g, r, c]
+                vp[k], gp[k], rp[k], cp[k] = _dp(v), _ip(g), _ip(r), _ip(c)
+            self.h = lib().orc_create_from_arrays(ctypes.byref(cfg), n, _ip(ncells), vp, gp,
+                                                  _ip(ndof), _ip(nact), rp, cp)
         if not self.h:
             raise RuntimeError(lib().orc_last_error().decode())
 
@@ -237,3 +279,20 @@ class Problem:
         e = np.zeros(5)
         self._chk(lib().orc_errors(self.h, _dp(e)))
         return e
+
+    def tcd_initialize(self):
+        self._chk(lib().orc_tcd_initialize(self.h))
+
+    def tcd_step(self, t_new, tau, scfg):
+        it = np.zeros(1, dtype=np.int32)
+        res = np.zeros(1)
+        ini = np.zeros(1)
+        self._chk(lib().orc_tcd_step(self.h, t_new, tau, ctypes.byref(scfg), _ip(it),
+                                     _dp(res), _dp(ini)))
+        return int(it[0]), float(res[0]), float(ini[0])
+
+    def tcd_matrix(self, which, level=0):
+        """which: 0 stiffness, 1 mass, 2 system"""
+        v = np.zeros(self.info(level)["nnz"])
+        self._chk(lib().orc_get_tcd_matrix(self.h, level, which, _dp(v)))
+        return v

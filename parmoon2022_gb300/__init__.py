@@ -26,7 +26,8 @@ ERRORS = {
     -5: "CDG_ERR_BREAKDOWN", -6: "CDG_ERR_ZERO_DIAG", -7: "CDG_ERR_PATTERN",
     -8: "CDG_ERR_SINGULAR", -9: "CDG_ERR_NO_DEVICE", -10: "CDG_ERR_LIMIT",
 }
-EX_SINE_LAPLACE, EX_SINE, EX_POLYEXP, EX_CONST_F, EX_POLY1 = range(5)
+EX_SINE_LAPLACE, EX_SINE, EX_POLYEXP, EX_CONST_F, EX_POLY1, EX_BUMP, EX_POLY1_T = range(7)
+CELL_QUAD, CELL_HEXA, CELL_TETRA = 2, 3, 4
 
 # every symbol include/parmoon_cd.h declares
 EXPORTED = [
@@ -40,7 +41,8 @@ EXPORTED = [
     "cdg_problem_get_solution", "cdg_problem_set_solution", "cdg_problem_get_slots",
     "cdg_problem_apply", "cdg_problem_prolongate", "cdg_problem_restrict",
     "cdg_problem_precondition", "cdg_context_stream", "cdg_problem_time_kernel",
-    "cdg_problem_errors_noalloc",
+    "cdg_problem_errors_noalloc", "cdg_hierarchy_create_tetra", "cdg_problem_tcd_initialize",
+    "cdg_problem_tcd_step", "cdg_problem_get_tcd_matrix",
 ]
 
 
@@ -57,6 +59,7 @@ class AssemblyParams(ctypes.Structure):
         ("sdfem_type", ctypes.c_int), ("delta0", ctypes.c_double), ("delta1", ctypes.c_double),
         ("cell_measure", ctypes.c_int), ("problem_linear", ctypes.c_int),
         ("neumann_mask", ctypes.c_int), ("poly_degree", ctypes.c_int),
+        ("b_grad", ctypes.c_double * 9), ("t", ctypes.c_double), ("ic", ctypes.c_double * 4),
     ]
 
 
@@ -114,6 +117,12 @@ def lib():
                                            ctypes.POINTER(SolveStats)],
             "cdg_problem_errors": [P, ctypes.POINTER(AssemblyParams), dp],
             "cdg_problem_errors_noalloc": [P, ctypes.POINTER(AssemblyParams), dp],
+            "cdg_hierarchy_create_tetra": [ctypes.c_int] * 4 + [ctypes.c_double,
+                                                                ctypes.c_ulonglong, PP],
+            "cdg_problem_tcd_initialize": [P, ctypes.POINTER(AssemblyParams)],
+            "cdg_problem_tcd_step": [P, ctypes.POINTER(AssemblyParams), ctypes.c_double,
+                                     ctypes.POINTER(SolverParams), ctypes.POINTER(SolveStats)],
+            "cdg_problem_get_tcd_matrix": [P, ctypes.c_int, ctypes.c_int, dp],
             "cdg_problem_level_info": [P, ctypes.c_int, ip],
             "cdg_problem_get_matrix": [P, ctypes.c_int, dp],
             "cdg_problem_get_rhs": [P, ctypes.c_int, dp],
@@ -150,8 +159,17 @@ def _ip(a):
 
 def assembly_params(example=EX_SINE, eps=1.0, b=(0.0, 0.0, 0.0), c=0.0, freq=1.0,
                     space_discretization_type="galerkin", sdfem_type=2, delta0=1.0, delta1=1.0,
-                    cell_measure=0, problem_linear=0, neumann_mask=0, poly_degree=0):
+                    cell_measure=0, problem_linear=0, neumann_mask=0, poly_degree=0,
+                    b_grad=None, t=0.0, ic=(0.0, 0.0, 0.0, 1.0)):
+    """b_grad: 3x3 gradient of a convection field linear in x (row-major)."""
     a = AssemblyParams()
+    if b_grad is not None:
+        g = np.asarray(b_grad, dtype=np.float64).reshape(-1)
+        for i in range(9):
+            a.b_grad[i] = g[i]
+    a.t = t
+    for i in range(4):
+        a.ic[i] = ic[i]
     a.example, a.eps = example, eps
     for i in range(3):
         a.b[i] = b[i] if i < len(b) else 0.0
@@ -192,13 +210,21 @@ def solver_params(preconditioner="jacobi", max_n_iterations=100, min_n_iteration
 
 class Hierarchy:
     """Host setup: unit square/cube (roots^dim cells) refined nref times, the
-    Q_order space and CSR pattern of each of n_levels levels (0 = finest)."""
+    Q_order space and CSR pattern of each of n_levels levels (0 = finest).
+    tetra=True: roots^3 cubes of 6 Kuhn tetrahedra, P_order, with the finest
+    interior vertices perturbed by perturb*h (seeded)."""
 
-    def __init__(self, dim, order, nref, n_levels=1, roots=1, neumann_mask=0):
+    def __init__(self, dim, order, nref, n_levels=1, roots=1, neumann_mask=0, tetra=False,
+                 perturb=0.0, seed=0):
         self.dim, self.order, self.nref, self.n_levels = dim, order, nref, n_levels
+        self.tetra = tetra
         h = ctypes.c_void_p()
-        _chk(lib().cdg_hierarchy_create(dim, order, roots, nref, n_levels, neumann_mask,
-                                        ctypes.byref(h)))
+        if tetra:
+            _chk(lib().cdg_hierarchy_create_tetra(order, roots, nref, n_levels, perturb, seed,
+                                                  ctypes.byref(h)))
+        else:
+            _chk(lib().cdg_hierarchy_create(dim, order, roots, nref, n_levels, neumann_mask,
+                                            ctypes.byref(h)))
         self.h = h
 
     def __del__(self):
@@ -276,9 +302,10 @@ class ConvectionDiffusion:
         ctx._problems.add(self)
 
     @classmethod
-    def from_arrays(cls, ctx, dim, order, levels):
-        """levels: list (finest first) of dicts with verts (ncells,nv,dim),
-        dofs (ncells,nloc), ndof, nactive, row_ptr, col, optional parent."""
+    def from_arrays(cls, ctx, cell_type, order, levels):
+        """cell_type: CELL_QUAD (2), CELL_HEXA (3), CELL_TETRA (4); levels:
+        list (finest first) of dicts with verts (ncells,nv,dim), dofs
+        (ncells,nloc), ndof, nactive, row_ptr, col, optional parent."""
         self = cls.__new__(cls)
         self.ctx, self.hier, self.n_levels = ctx, None, len(levels)
         n = len(levels)
@@ -297,7 +324,7 @@ class ConvectionDiffusion:
         nact = np.array([l["nactive"] for l in levels], dtype=np.int32)
         p = ctypes.c_void_p()
         _chk(lib().cdg_problem_create_from_arrays(
-            ctx.c, dim, order, n, _ip(ncells), arr(np.float64, "verts"), arr(np.int32, "dofs"),
+            ctx.c, cell_type, order, n, _ip(ncells), arr(np.float64, "verts"), arr(np.int32, "dofs"),
             _ip(ndof), _ip(nact), arr(np.int32, "row_ptr"), arr(np.int32, "col"),
             arr(np.int32, "parent"), ctypes.byref(p)))
         self.p = p
@@ -341,6 +368,22 @@ class ConvectionDiffusion:
         e = np.zeros(5)
         _chk(lib().cdg_problem_errors(self.p, ctypes.byref(a), _dp(e)))
         return e
+
+    # time-dependent CD (Crank-Nicolson)
+    def tcd_initialize(self, a):
+        _chk(lib().cdg_problem_tcd_initialize(self.p, ctypes.byref(a)))
+
+    def tcd_step(self, a, tau, s):
+        st = SolveStats()
+        _chk(lib().cdg_problem_tcd_step(self.p, ctypes.byref(a), tau, ctypes.byref(s),
+                                        ctypes.byref(st)))
+        return st
+
+    def tcd_matrix(self, which, level=0):
+        """which: 0 stiffness, 1 mass, 2 system."""
+        v = np.zeros(self.info(level)["nnz"])
+        _chk(lib().cdg_problem_get_tcd_matrix(self.p, level, which, _dp(v)))
+        return v
 
     def matrix(self, level=0):
         v = np.zeros(self.info(level)["nnz"])

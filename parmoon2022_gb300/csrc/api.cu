@@ -105,12 +105,36 @@ static int hierarchy_create(int dim, int order, int roots, int nref, int n_level
   }
   cdg_hierarchy* h = new cdg_hierarchy();
   h->dim = dim;
+  h->shape = dim == 2 ? kQuad : kHexa;
   h->order = order;
   for (int l = 0; l < n_levels; ++l) {
     h->mesh.push_back(make_refined_box(dim, roots, nref - l));
     h->space.push_back(make_space(h->mesh.back(), order, nmask));
     h->pattern.push_back(make_pattern(h->space.back()));
   }
+  h->mesh_nested = h->mesh;
+  *out = h;
+  return CDG_OK;
+}
+
+static int hierarchy_create_tetra(int order, int roots, int nref, int n_levels, double perturb,
+                                  unsigned long long seed, cdg_hierarchy** out) {
+  if (!out || (order != 1 && order != 2) || roots < 1 || nref < 0 || n_levels < 1 ||
+      n_levels > nref + 1 || perturb < 0 || perturb >= 0.5) {
+    set_error("bad tetrahedral hierarchy arguments");
+    return CDG_ERR_ARG;
+  }
+  cdg_hierarchy* h = new cdg_hierarchy();
+  h->dim = 3;
+  h->shape = kTetra;
+  h->order = order;
+  for (int l = 0; l < n_levels; ++l) {
+    h->mesh.push_back(make_kuhn_box(roots, nref - l));
+    h->space.push_back(make_space(h->mesh.back(), order, 0));
+    h->pattern.push_back(make_pattern(h->space.back()));
+  }
+  h->mesh_nested = h->mesh;
+  if (perturb > 0) perturb_interior(h->mesh[0], 1.0 / (roots << nref), perturb, seed);
   *out = h;
   return CDG_OK;
 }
@@ -118,6 +142,11 @@ static int hierarchy_create(int dim, int order, int roots, int nref, int n_level
 int cdg_hierarchy_create(int dim, int order, int roots, int nref, int n_levels, int neumann_mask,
                          cdg_hierarchy** out) {
   API_GUARD(hierarchy_create(dim, order, roots, nref, n_levels, neumann_mask, out));
+}
+
+int cdg_hierarchy_create_tetra(int order, int roots, int nref, int n_levels, double perturb,
+                               unsigned long long seed, cdg_hierarchy** out) {
+  API_GUARD(hierarchy_create_tetra(order, roots, nref, n_levels, perturb, seed, out));
 }
 
 int cdg_hierarchy_destroy(cdg_hierarchy* h) {
@@ -169,7 +198,8 @@ static int up(T** d, const std::vector<T>& h, cudaStream_t st) {
 }
 extern "C" {
 
-static int finish_problem(cdg_context* ctx, cdg_problem* p, const std::vector<std::vector<int>>& parents) {
+static int finish_problem(cdg_context* ctx, cdg_problem* p, const std::vector<std::vector<int>>& parents,
+                          const std::vector<Mesh>* nested) {
   CDG_CUDA(cudaMalloc(&p->d_zero_diag, sizeof(int)));
   CDG_CUDA(cudaMemsetAsync(p->d_zero_diag, 0, sizeof(int), ctx->stream));
   for (auto& L : p->lev) CDG_TRY(upload_level(ctx, L));
@@ -177,7 +207,9 @@ static int finish_problem(cdg_context* ctx, cdg_problem* p, const std::vector<st
     DevLevel& F = p->lev[l];
     DevLevel& C = p->lev[l + 1];
     HostCsr P, R;
-    make_transfer(F.mesh, F.space, C.mesh, C.space, parents[l].data(), &P, &R);
+    const Mesh& fm = nested ? (*nested)[l] : F.mesh;
+    const Mesh& cm = nested ? (*nested)[l + 1] : C.mesh;
+    make_transfer(fm, F.space, cm, C.space, parents[l].data(), &P, &R);
     std::vector<float> pv(P.val.begin(), P.val.end()), rv(R.val.begin(), R.val.end());
     CDG_TRY(up(&F.P_rp, P.row_ptr, ctx->stream));
     CDG_TRY(up(&F.P_col, P.col, ctx->stream));
@@ -194,11 +226,12 @@ static int finish_problem(cdg_context* ctx, cdg_problem* p, const std::vector<st
   return CDG_OK;
 }
 
-static void fill_level(DevLevel& L, int dim, int order) {
-  L.dim = dim;
+static void fill_level(DevLevel& L, int shape, int order) {
+  L.shape = shape;
+  L.dim = shape == kQuad ? 2 : 3;
   L.order = order;
-  L.nv = dim == 2 ? 4 : 8;
-  L.nloc = dim == 2 ? (order + 1) * (order + 1) : (order + 1) * (order + 1) * (order + 1);
+  L.nv = n_vertices(shape);
+  L.nloc = n_local_dofs(shape, order);
   L.ncells = L.mesh.ncells;
   L.ndof = L.space.ndof;
   L.nactive = L.space.nactive;
@@ -211,6 +244,7 @@ static int problem_create(cdg_context* ctx, const cdg_hierarchy* h, cdg_problem*
   cdg_problem* p = new cdg_problem();
   p->ctx = ctx;
   p->dim = h->dim;
+  p->shape = h->shape;
   p->order = h->order;
   p->lev.resize(h->mesh.size());
   std::vector<std::vector<int>> parents;
@@ -219,7 +253,7 @@ static int problem_create(cdg_context* ctx, const cdg_hierarchy* h, cdg_problem*
     L.mesh = h->mesh[l];
     L.space = h->space[l];
     L.pattern = h->pattern[l];
-    fill_level(L, h->dim, h->order);
+    fill_level(L, h->shape, h->order);
     if (l + 1 < h->mesh.size()) {
       std::vector<int> par(L.ncells);
       int nch = h->dim == 2 ? 4 : 8;
@@ -227,7 +261,7 @@ static int problem_create(cdg_context* ctx, const cdg_hierarchy* h, cdg_problem*
       parents.push_back(par);
     }
   }
-  int rc = finish_problem(ctx, p, parents);
+  int rc = finish_problem(ctx, p, parents, &h->mesh_nested);
   if (rc != CDG_OK) {
     cdg_problem_destroy(p);
     return rc;
@@ -240,24 +274,28 @@ int cdg_problem_create(cdg_context* ctx, const cdg_hierarchy* h, cdg_problem** o
   API_GUARD(problem_create(ctx, h, out));
 }
 
-static int problem_from_arrays(cdg_context* ctx, int dim, int order, int nl, const int* n_cells,
+static int problem_from_arrays(cdg_context* ctx, int cell_type, int order, int nl, const int* n_cells,
                                const double* const* verts, const int* const* gn,
                                const int* n_dofs, const int* n_active, const int* const* rp,
                                const int* const* col, const int* const* parent,
                                cdg_problem** out) {
-  if (!ctx || !out || (dim != 2 && dim != 3) || (order != 1 && order != 2) || nl < 1 ||
-      !n_cells || !verts || !gn || !n_dofs || !n_active || !rp || !col) {
+  if (!ctx || !out || cell_type < CDG_CELL_QUAD || cell_type > CDG_CELL_TETRA ||
+      (order != 1 && order != 2) || nl < 1 || !n_cells || !verts || !gn || !n_dofs ||
+      !n_active || !rp || !col) {
     set_error("bad arguments");
     return CDG_ERR_ARG;
   }
+  const int shape = cell_type == CDG_CELL_QUAD ? kQuad : cell_type == CDG_CELL_HEXA ? kHexa : kTetra;
+  const int dim = shape == kQuad ? 2 : 3;
   CDG_CUDA(cudaSetDevice(ctx->device));
   cdg_problem* p = new cdg_problem();
   p->ctx = ctx;
   p->dim = dim;
+  p->shape = shape;
   p->order = order;
   p->lev.resize(nl);
-  int nv = dim == 2 ? 4 : 8;
-  int nloc = dim == 2 ? (order + 1) * (order + 1) : (order + 1) * (order + 1) * (order + 1);
+  int nv = n_vertices(shape);
+  int nloc = n_local_dofs(shape, order);
   std::vector<std::vector<int>> parents;
   for (int l = 0; l < nl; ++l) {
     DevLevel& L = p->lev[l];
@@ -267,10 +305,12 @@ static int problem_from_arrays(cdg_context* ctx, int dim, int order, int nl, con
       return CDG_ERR_ARG;
     }
     L.mesh.dim = dim;
+    L.mesh.shape = shape;
     L.mesh.nv = nv;
     L.mesh.ncells = n_cells[l];
     L.mesh.verts.assign(verts[l], verts[l] + (size_t)n_cells[l] * nv * dim);
     L.space.dim = dim;
+    L.space.shape = shape;
     L.space.order = order;
     L.space.nloc = nloc;
     L.space.ndof = n_dofs[l];
@@ -292,7 +332,7 @@ static int problem_from_arrays(cdg_context* ctx, int dim, int order, int nl, con
         set_error("column index out of range on level %d", l);
         return CDG_ERR_ARG;
       }
-    fill_level(L, dim, order);
+    fill_level(L, shape, order);
     if (l >= 1) {
       std::vector<int> par(n_cells[l - 1]);
       int nch = dim == 2 ? 4 : 8;
@@ -307,7 +347,7 @@ static int problem_from_arrays(cdg_context* ctx, int dim, int order, int nl, con
       parents.push_back(par);
     }
   }
-  int rc = finish_problem(ctx, p, parents);
+  int rc = finish_problem(ctx, p, parents, nullptr);
   if (rc != CDG_OK) {
     cdg_problem_destroy(p);
     return rc;
@@ -316,13 +356,13 @@ static int problem_from_arrays(cdg_context* ctx, int dim, int order, int nl, con
   return CDG_OK;
 }
 
-int cdg_problem_create_from_arrays(cdg_context* ctx, int dim, int order, int n_levels,
+int cdg_problem_create_from_arrays(cdg_context* ctx, int cell_type, int order, int n_levels,
                                    const int* n_cells, const double* const* cell_vertices,
                                    const int* const* global_numbers, const int* n_dofs,
                                    const int* n_active, const int* const* row_ptr,
                                    const int* const* col, const int* const* parent,
                                    cdg_problem** out) {
-  API_GUARD(problem_from_arrays(ctx, dim, order, n_levels, n_cells, cell_vertices,
+  API_GUARD(problem_from_arrays(ctx, cell_type, order, n_levels, n_cells, cell_vertices,
                                 global_numbers, n_dofs, n_active, row_ptr, col, parent, out));
 }
 
@@ -343,7 +383,7 @@ int cdg_problem_destroy(cdg_problem* p) {
 
 static int check_assembly_params(const cdg_problem* p, const cdg_assembly_params* a) {
   if (!p || !a) { set_error("null argument"); return CDG_ERR_ARG; }
-  if (a->example < 0 || a->example > CDG_EX_POLY1) { set_error("unknown example %d", a->example); return CDG_ERR_ARG; }
+  if (a->example < 0 || a->example > CDG_EX_POLY1_T) { set_error("unknown example %d", a->example); return CDG_ERR_ARG; }
   if (a->example == CDG_EX_POLYEXP && p->dim != 3) { set_error("example needs 3D"); return CDG_ERR_ARG; }
   return CDG_OK;
 }
@@ -418,6 +458,52 @@ int cdg_problem_errors(cdg_problem* p, const cdg_assembly_params* a, double* err
 }
 
 // ---------------------------------------------------------------------------
+// time-dependent CD
+// ---------------------------------------------------------------------------
+int cdg_problem_tcd_initialize(cdg_problem* p, const cdg_assembly_params* a) {
+  CDG_TRY(check_assembly_params(p, a));
+  CDG_CUDA(cudaSetDevice(p->ctx->device));
+  CDG_CUDA(cudaMemsetAsync(p->d_zero_diag, 0, sizeof(int), p->ctx->stream));
+  for (auto& L : p->lev) {
+    CDG_TRY(tcd_assemble_level(p->ctx, p, L, *a, true));
+    // old_rhs = rhs
+    CDG_CUDA(cudaMemcpyAsync(L.tcd_fold, L.tcd_f, (size_t)L.ndof * sizeof(double),
+                             cudaMemcpyDeviceToDevice, p->ctx->stream));
+  }
+  CDG_TRY(tcd_interpolate(p->ctx, p, *a));
+  return check_device_error(p->ctx);
+}
+
+int cdg_problem_tcd_step(cdg_problem* p, const cdg_assembly_params* a, double tau,
+                         const cdg_solver_params* s, cdg_solve_stats* st) {
+  CDG_TRY(check_assembly_params(p, a));
+  CDG_TRY(check_solver_params(p, s));
+  if (!(tau > 0)) { set_error("time step must be positive"); return CDG_ERR_ARG; }
+  if (!p->lev[0].tcd_A) { set_error("call cdg_problem_tcd_initialize first"); return CDG_ERR_ARG; }
+  CDG_CUDA(cudaSetDevice(p->ctx->device));
+  auto t0 = std::chrono::steady_clock::now();
+  cudaStream_t stm = p->ctx->stream;
+  CDG_CUDA(cudaMemsetAsync(p->d_zero_diag, 0, sizeof(int), stm));
+  // reassemble stiffness and rhs on every level (mass is time independent)
+  for (auto& L : p->lev) CDG_TRY(tcd_assemble_level(p->ctx, p, L, *a, false));
+  DevLevel& F = p->lev[0];
+  CDG_TRY(tcd_cn_rhs(p->ctx, F, tau));
+  // solution.copy_nonactive(rhs): Dirichlet data at the new time
+  const int nd = F.ndof - F.nactive;
+  if (nd > 0)
+    CDG_CUDA(cudaMemcpyAsync(F.sol + F.nactive, F.rhs + F.nactive, (size_t)nd * sizeof(double),
+                             cudaMemcpyDeviceToDevice, stm));
+  for (auto& L : p->lev) CDG_TRY(tcd_system(p->ctx, p, L, tau));
+  cdg_solve_stats local{};
+  CDG_TRY(prepare_solver(p->ctx, p, *s));
+  int rc = fgmres(p->ctx, p, *s, &local);
+  CDG_CUDA(cudaStreamSynchronize(stm));
+  local.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (st) *st = local;
+  return rc;
+}
+
+// ---------------------------------------------------------------------------
 // data access
 // ---------------------------------------------------------------------------
 static DevLevel* get_level(cdg_problem* p, int level) {
@@ -448,6 +534,14 @@ int cdg_problem_get_matrix(cdg_problem* p, int level, double* v) {
   if (!L || !v) return CDG_ERR_ARG;
   return d2h(p->ctx, v, L->val64, (size_t)L->nnz * sizeof(double));
 }
+int cdg_problem_get_tcd_matrix(cdg_problem* p, int level, int which, double* v) {
+  DevLevel* L = get_level(p, level);
+  if (!L || !v || which < 0 || which > 2) { set_error("bad arguments"); return CDG_ERR_ARG; }
+  if (!L->tcd_A) { set_error("no time-dependent matrices: call cdg_problem_tcd_initialize"); return CDG_ERR_ARG; }
+  const double* src = which == 0 ? L->tcd_A : which == 1 ? L->tcd_M : L->val64;
+  return d2h(p->ctx, v, src, (size_t)L->nnz * sizeof(double));
+}
+
 int cdg_problem_get_rhs(cdg_problem* p, int level, double* v) {
   DevLevel* L = get_level(p, level);
   if (!L || !v) return CDG_ERR_ARG;

@@ -1,7 +1,8 @@
 // assemble.cu -- GB300 kernels of the CD assembly: cell geometry, element
 // matrices by contraction with reference tensors, CSR scatter through a
 // precomputed coupling->slot map, right-hand side with the example's source
-// term, Dirichlet rows and data, error norms.
+// term, Dirichlet rows and data, error norms, and the Crank-Nicolson pieces of
+// the time-dependent problem.
 //
 // Reference path (ParMooN2022): ConvectionDiffusion<d>::call_assembling_
 // routine (src/System/ConvectionDiffusion.C:410-452) -> Assemble2D/3D cell
@@ -9,18 +10,21 @@
 // FEDatabase::GetOrig (src/FE/FEDatabase.C:1498-1719) -> LocalAssembling::
 // GetLocalForms (src/AssembleRoutines/LocalAssembling.C:734-970) ->
 // BilinearAssembleGalerkin<d> / BilinearAssemble_SD<d>
-// (src/AssembleRoutines/ConvDiff.C:1776-1999) -> scatter by row search
-// (Assemble3D.C:257-292, Matrix.C:180-255).
+// (src/AssembleRoutines/ConvDiff.C:1776-1999), TCDStiff / TCDMass / TCDRhs
+// (src/AssembleRoutines/CD_local_assembling_routines.C:9-181) -> scatter by
+// row search (Assemble3D.C:257-292, Matrix.C:180-255); time discretisation
+// src/TimeDiscRoutines/TimeDiscretizations.C:117-283.
 //
-// On affine cells (QuadAffin / HexaAffin, the maps of every cell these
-// meshes produce) with cell-constant eps, b, c, the per-quadrature-point
-// local forms are bilinear in reference-element integrals.  The local matrix
-// is therefore A_ij = sum_t g_t(cell) R_t[i][j] with R_t exact reference
-// integrals (the reference's Gauss rules integrate these polynomials
-// exactly) and g_t a few FP64 geometric/coefficient factors per cell; the
-// quadrature sum of the reference becomes one FP64 contraction per entry.
-// The right-hand side keeps the reference's quadrature rule because f is
-// not polynomial.
+// On affine cells (QuadAffin / HexaAffin / TetraAffin, the maps of every cell
+// these meshes produce) with cell-constant eps, c and a convection field that
+// is constant or linear in x, the per-quadrature-point local forms are
+// bilinear in reference-element integrals.  The local matrix is therefore
+// A_ij = sum_t g_t(cell) R_t[i][j] with R_t exact reference integrals (the
+// reference's Gauss rules integrate these polynomials exactly) and g_t a few
+// FP64 geometric/coefficient factors per cell; the quadrature sum of the
+// reference becomes one FP64 contraction per entry.  The right-hand side
+// keeps a quadrature rule of the reference's degree because f is not
+// polynomial.
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -34,16 +38,17 @@ namespace cdg {
 // device-side problem data
 // ---------------------------------------------------------------------------
 struct AsmCoefs {
-  int dim, order, nloc, example, supg, sdfem_type, cell_measure, poly_degree,
-      neumann_mask, nqp, nqp1, n_sym;
-  double eps, b[3], c, freq, delta0, delta1;
+  int dim, shape, order, nloc, example, supg, sdfem_type, cell_measure, poly_degree,
+      neumann_mask, nqp, nqp1, n_sym, linear_b;
+  double eps, b[3], bg[9], c, freq, delta0, delta1, t, ic[4];
 };
 
-static AsmCoefs make_coefs(const cdg_assembly_params& a, int dim, int order, int nloc) {
+static AsmCoefs make_coefs(const cdg_assembly_params& a, int shape, int order) {
   AsmCoefs k;
-  k.dim = dim;
+  k.shape = shape;
+  k.dim = shape == kQuad ? 2 : 3;
   k.order = order;
-  k.nloc = nloc;
+  k.nloc = n_local_dofs(shape, order);
   k.example = a.example;
   k.supg = a.supg;
   k.sdfem_type = a.sdfem_type;
@@ -51,23 +56,48 @@ static AsmCoefs make_coefs(const cdg_assembly_params& a, int dim, int order, int
   k.poly_degree = a.poly_degree > 0 ? a.poly_degree : order;
   k.neumann_mask = a.neumann_mask;
   k.eps = a.eps;
-  for (int i = 0; i < 3; ++i) k.b[i] = (i < dim) ? a.b[i] : 0.0;
+  k.linear_b = 0;
+  for (int i = 0; i < 3; ++i) k.b[i] = (i < k.dim) ? a.b[i] : 0.0;
+  for (int i = 0; i < 9; ++i) {
+    const int r = i / 3, c = i % 3;
+    k.bg[i] = (r < k.dim && c < k.dim) ? a.b_grad[i] : 0.0;
+    if (k.bg[i] != 0.0) k.linear_b = 1;
+  }
   k.c = a.c;
   k.freq = a.freq;
   k.delta0 = a.delta0;
   k.delta1 = a.delta1;
-  int nterms = a.problem_linear ? 2 : 3;
-  k.nqp1 = gauss_points_for_degree(nterms * order);
-  k.nqp = dim == 2 ? k.nqp1 * k.nqp1 : k.nqp1 * k.nqp1 * k.nqp1;
-  k.n_sym = dim == 2 ? 3 : 6;
+  k.t = a.t;
+  for (int i = 0; i < 4; ++i) k.ic[i] = a.ic[i];
+  const int nterms = a.problem_linear ? 2 : 3;
+  const int deg = nterms * order;
+  if (shape == kTetra) {
+    k.nqp1 = tetra_points_for_degree(deg);
+    k.nqp = k.nqp1 * k.nqp1 * k.nqp1;
+  } else {
+    k.nqp1 = gauss_points_for_degree(deg);
+    k.nqp = k.dim == 2 ? k.nqp1 * k.nqp1 : k.nqp1 * k.nqp1 * k.nqp1;
+  }
+  k.n_sym = k.dim == 2 ? 3 : 6;
   return k;
 }
 
+// convection at x
+__device__ __forceinline__ void b_at(const AsmCoefs& k, const double* x, double* bx) {
+  for (int i = 0; i < 3; ++i) {
+    double s = k.b[i];
+    if (k.linear_b)
+      for (int j = 0; j < k.dim; ++j) s += k.bg[3 * i + j] * x[j];
+    bx[i] = s;
+  }
+}
+
 // exact solution of the example: u[0] value, u[1..dim] gradient, u[dim+1]
-// Laplacian (examples with a known solution; CONST_F returns zeros)
+// Laplacian, u[dim+2] time derivative (examples with a known solution;
+// CONST_F and BUMP return zeros)
 __device__ void ex_exact(const AsmCoefs& k, const double* x, double* u) {
   int d = k.dim;
-  for (int i = 0; i < 5; ++i) u[i] = 0.0;
+  for (int i = 0; i < 6; ++i) u[i] = 0.0;
   if (k.example == CDG_EX_SINE_LAPLACE || k.example == CDG_EX_SINE) {
     double w = (k.example == CDG_EX_SINE_LAPLACE ? 1.0 : k.freq) * M_PI;
     double s0 = sin(w * x[0]), c0 = cos(w * x[0]);
@@ -96,42 +126,54 @@ __device__ void ex_exact(const AsmCoefs& k, const double* x, double* u) {
     u[2] = px * (1 - 2 * x[1]) * qz;
     u[3] = px * qy * (1 - 2 * x[2]);
     u[4] = px2 * qy * qz - 2 * px * qz - 2 * px * qy;
-  } else if (k.example == CDG_EX_POLY1) {
-    u[0] = 1 + x[0] + 2 * x[1] + (d == 3 ? 3 * x[2] : 0.0);
-    u[1] = 1;
-    u[2] = 2;
-    if (d == 3) u[3] = 3;
+  } else if (k.example == CDG_EX_POLY1 || k.example == CDG_EX_POLY1_T) {
+    const double s = k.example == CDG_EX_POLY1_T ? 1.0 + k.t : 1.0;
+    const double q = 1 + x[0] + 2 * x[1] + (d == 3 ? 3 * x[2] : 0.0);
+    u[0] = s * q;
+    u[1] = s;
+    u[2] = 2 * s;
+    if (d == 3) u[3] = 3 * s;
+    if (k.example == CDG_EX_POLY1_T) u[d + 2] = q;
   }
 }
 
-// source term f = -eps lap u + b.grad u + c u (the examples' coefficient
+// source term f = u_t - eps lap u + b.grad u + c u (the examples' coefficient
 // callbacks, e.g. include/Examples/CD_2D/SineLaplace.h BilinearCoeffs)
 __device__ double ex_source(const AsmCoefs& k, const double* x) {
   if (k.example == CDG_EX_CONST_F) return 1.0;
-  double u[5];
+  if (k.example == CDG_EX_BUMP) return 0.0;
+  double u[6], bx[3];
   ex_exact(k, x, u);
+  b_at(k, x, bx);
   int d = k.dim;
   double f = -k.eps * u[d + 1];
-  for (int a = 0; a < d; ++a) f += k.b[a] * u[1 + a];
+  for (int a = 0; a < d; ++a) f += bx[a] * u[1 + a];
   f += k.c * u[0];
+  f += u[d + 2];
   return f;
 }
 
-// affine reference map from the cell vertices (QuadAffin.C:175-, HexaAffin.C:
-// 221-252): xi along v0->v1, eta along v0->v3, zeta along v0->v4
+// initial condition (interpolated at the nodes) and boundary data
+__device__ double ex_initial(const AsmCoefs& k, const double* x) {
+  if (k.example == CDG_EX_BUMP) {
+    double r2 = 0;
+    for (int a = 0; a < k.dim; ++a) r2 += (x[a] - k.ic[a]) * (x[a] - k.ic[a]);
+    return exp(-r2 / (2.0 * k.ic[3] * k.ic[3]));
+  }
+  double u[6];
+  ex_exact(k, x, u);
+  return u[0];
+}
+
+// affine reference map from the cell vertices: x = x0 + J xi
+// QuadAffin.C:175- / HexaAffin.C:221-252 (xi in [-1,1]^d along v0->v1,
+// v0->v3, v0->v4; x0 the centre) and TetraAffin.C:235-265 (xi in the unit
+// tetrahedron, columns v1-v0, v2-v0, v3-v0; x0 = v0)
 struct Affine {
   double x0[3], J[3][3], Ji[3][3], det;
 };
 
-__device__ void cell_affine(int dim, const double* __restrict__ cv, Affine& A) {
-  const int e[3] = {1, 3, 4};
-  for (int r = 0; r < dim; ++r)
-    for (int a = 0; a < dim; ++a) A.J[r][a] = (cv[e[a] * dim + r] - cv[r]) * 0.5;
-  for (int r = 0; r < dim; ++r) {
-    double s = cv[r];
-    for (int a = 0; a < dim; ++a) s += A.J[r][a];
-    A.x0[r] = s;
-  }
+__device__ void invert_J(int dim, Affine& A) {
   if (dim == 2) {
     double det = A.J[0][0] * A.J[1][1] - A.J[0][1] * A.J[1][0];
     A.det = det;
@@ -152,8 +194,34 @@ __device__ void cell_affine(int dim, const double* __restrict__ cv, Affine& A) {
   }
 }
 
-// cell measure hK (BaseCell.C:102-131; Rectangle.C:12-33; Hexahedron.C:70-121)
-__device__ double cell_hK(int dim, const double* __restrict__ cv, int measure, double det) {
+__device__ void cell_affine_s(int shape, int dim, const double* __restrict__ cv, Affine& A) {
+  if (shape == kTetra) {
+    for (int r = 0; r < 3; ++r) {
+      A.x0[r] = cv[r];
+      for (int a = 0; a < 3; ++a) A.J[r][a] = cv[(a + 1) * 3 + r] - cv[r];
+    }
+  } else {
+    const int e[3] = {1, 3, 4};
+    for (int r = 0; r < dim; ++r)
+      for (int a = 0; a < dim; ++a) A.J[r][a] = (cv[e[a] * dim + r] - cv[r]) * 0.5;
+    for (int r = 0; r < dim; ++r) {
+      double s = cv[r];
+      for (int a = 0; a < dim; ++a) s += A.J[r][a];
+      A.x0[r] = s;
+    }
+  }
+  invert_J(dim, A);
+}
+
+// quadrilateral / hexahedron form used by the fixed-scratch error norms
+__device__ void cell_affine(int dim, const double* __restrict__ cv, Affine& A) {
+  cell_affine_s(dim == 2 ? kQuad : kHexa, dim, cv, A);
+}
+
+// cell measure hK (BaseCell.C:102-131; Rectangle.C:12-33; Hexahedron.C:70-121;
+// Tetrahedron.C:64-113)
+__device__ double cell_hK_s(int shape, int dim, const double* __restrict__ cv, int measure,
+                            double det) {
   auto d2 = [&](int i, int j) {
     double s = 0;
     for (int a = 0; a < dim; ++a) {
@@ -162,6 +230,14 @@ __device__ double cell_hK(int dim, const double* __restrict__ cv, int measure, d
     }
     return s;
   };
+  if (shape == kTetra) {
+    if (measure == 1 || measure == 3) return sqrt(fabs(det) / 6.0);
+    double m = d2(0, 1);
+    const int pr[5][2] = {{0, 2}, {0, 3}, {1, 2}, {1, 3}, {2, 3}};
+    for (int k = 0; k < 5; ++k)
+      m = measure == 2 ? fmin(m, d2(pr[k][0], pr[k][1])) : fmax(m, d2(pr[k][0], pr[k][1]));
+    return sqrt(m);
+  }
   if (measure == 1 || measure == 3) return sqrt(fabs(det) * (dim == 2 ? 4.0 : 8.0));
   if (dim == 2) {
     if (measure == 2) {
@@ -181,6 +257,10 @@ __device__ double cell_hK(int dim, const double* __restrict__ cv, int measure, d
   m = fmax(m, d2(2, 4));
   m = fmax(m, d2(3, 5));
   return sqrt(m);
+}
+
+__device__ double cell_hK(int dim, const double* __restrict__ cv, int measure, double det) {
+  return cell_hK_s(dim == 2 ? kQuad : kHexa, dim, cv, measure, det);
 }
 
 // Compute_SDFEM_delta (ConvDiff.C:269-495), steady types
@@ -239,24 +319,44 @@ __device__ double sdfem_delta(const AsmCoefs& k, double h, double eps, const dou
 
 __device__ double cell_delta(const AsmCoefs& k, const double* cv, const Affine& A) {
   if (!k.supg) return 0.0;
-  double h = cell_hK(k.dim, cv, k.cell_measure, A.det);
+  double h = cell_hK_s(k.shape, k.dim, cv, k.cell_measure, A.det);
   double linfb = fmax(fabs(k.b[0]), fabs(k.b[1]));
   if (k.dim == 3) linfb = fmax(linfb, fabs(k.b[2]));
   return sdfem_delta(k, h, k.eps, k.b, k.c, linfb);
 }
 
-// per-cell factors g_t of the contraction (term layout of RefTensors)
+// term blocks of RefTensors: S (ns), C (d), M (1), L (d*d), D (d), T (ns*d)
 template <int DIM>
-__device__ void cell_factors(const AsmCoefs& k, const double* __restrict__ cv, double* g) {
-  constexpr int NS = DIM == 2 ? 3 : 6;
+struct Terms {
+  static constexpr int NS = DIM == 2 ? 3 : 6;
+  static constexpr int offC = NS, offM = NS + DIM, offL = NS + DIM + 1;
+  static constexpr int offD = offL + DIM * DIM, offT = offD + DIM;
+  static constexpr int NT = offT + NS * DIM;
+};
+
+// per-cell factors g_t of the contraction; mass_only: g = |det J| on M
+template <int DIM>
+__device__ void cell_factors(const AsmCoefs& k, const double* __restrict__ cv, double* g,
+                             bool mass_only) {
+  using TT = Terms<DIM>;
   Affine A;
-  cell_affine(DIM, cv, A);
-  double adet = fabs(A.det);
-  double delta = cell_delta(k, cv, A);
-  double bp[3];  // beta' = J^-1 b
+  cell_affine_s(k.shape, DIM, cv, A);
+  const double adet = fabs(A.det);
+  if (mass_only) {
+    for (int t = 0; t < TT::NT; ++t) g[t] = 0.0;
+    g[TT::offM] = adet;
+    return;
+  }
+  const double delta = cell_delta(k, cv, A);
+  // convection at the map origin and its gradient: b(x0 + J xi) =
+  // b(x0) + B J xi, in reference coordinates beta0 = J^-1 b(x0),
+  // Gamma = J^-1 B J
+  double bx0[3];
+  b_at(k, A.x0, bx0);
+  double bp[3];
   for (int a = 0; a < DIM; ++a) {
     double s = 0;
-    for (int r = 0; r < DIM; ++r) s += A.Ji[a][r] * k.b[r];
+    for (int r = 0; r < DIM; ++r) s += A.Ji[a][r] * bx0[r];
     bp[a] = s;
   }
   int s = 0;
@@ -269,16 +369,23 @@ __device__ void cell_factors(const AsmCoefs& k, const double* __restrict__ cv, d
       g[s] = adet * (k.eps * h + delta * bp[a] * bp[bb]);
       ++s;
     }
-  const int offC = NS, offM = NS + DIM, offD = NS + DIM + 1, offT = NS + 2 * DIM + 1;
-  for (int a = 0; a < DIM; ++a) g[offC + a] = adet * bp[a];
-  g[offM] = adet * k.c;
-  for (int a = 0; a < DIM; ++a) g[offD + a] = adet * delta * k.c * bp[a];
+  for (int a = 0; a < DIM; ++a) g[TT::offC + a] = adet * bp[a];
+  g[TT::offM] = adet * k.c;
+  for (int a = 0; a < DIM; ++a)
+    for (int c = 0; c < DIM; ++c) {
+      double gam = 0;
+      if (k.linear_b)
+        for (int r = 0; r < DIM; ++r)
+          for (int q = 0; q < DIM; ++q) gam += A.Ji[a][r] * k.bg[3 * r + q] * A.J[q][c];
+      g[TT::offL + a * DIM + c] = adet * gam;
+    }
+  for (int a = 0; a < DIM; ++a) g[TT::offD + a] = adet * delta * k.c * bp[a];
   s = 0;
   for (int a = 0; a < DIM; ++a)
     for (int bb = a; bb < DIM; ++bb) {
       double m = (a == bb) ? 1.0 : 2.0;
       for (int c = 0; c < DIM; ++c)
-        g[offT + s * DIM + c] = -adet * delta * k.eps * m * H[s] * bp[c];
+        g[TT::offT + s * DIM + c] = -adet * delta * k.eps * m * H[s] * bp[c];
       ++s;
     }
 }
@@ -330,7 +437,7 @@ __global__ void k_diag_slots(int n, const int* __restrict__ row_ptr, const int* 
 // threads holds EPB entries' reference-tensor columns in registers and
 // sweeps a tile of cells with LANES cells in flight
 template <int NLOC> struct ContractShape;
-template <> struct ContractShape<4> {   // Q1 quadrilateral
+template <> struct ContractShape<4> {   // Q1 quadrilateral, P1 tetrahedron
   static constexpr int NE = 16, EPB = 16, LANES = 16;
 };
 template <> struct ContractShape<9> {   // Q2 quadrilateral
@@ -338,6 +445,9 @@ template <> struct ContractShape<9> {   // Q2 quadrilateral
 };
 template <> struct ContractShape<8> {   // Q1 hexahedron
   static constexpr int NE = 64, EPB = 64, LANES = 4;
+};
+template <> struct ContractShape<10> {  // P2 tetrahedron
+  static constexpr int NE = 100, EPB = 100, LANES = 2;
 };
 template <> struct ContractShape<27> {  // Q2 hexahedron
   static constexpr int NE = 729, EPB = 243, LANES = 1;
@@ -350,22 +460,26 @@ template <int NLOC> struct ShapeInfo {
 
 constexpr int kCellTile = 32;
 
-template <int DIM, int NLOC, int NT, bool SUPG>
+// which reference tensors a launch contracts
+struct TermList {
+  int idx[kMaxTerms];
+};
+
+template <int DIM, int NLOC, int NTU>
 __global__ void __launch_bounds__(256)
-k_element_contract(AsmCoefs k, int ncells, int nactive, const double* __restrict__ verts,
-                   const int* __restrict__ gdof, const int* __restrict__ slot,
-                   const double* __restrict__ R, double* __restrict__ val) {
+k_element_contract(AsmCoefs k, TermList tl, int mass_only, int all_rows, int ncells,
+                   int nactive, const double* __restrict__ verts, const int* __restrict__ gdof,
+                   const int* __restrict__ slot, const double* __restrict__ R,
+                   double* __restrict__ val) {
   using S = ContractShape<NLOC>;
-  constexpr int NV = DIM == 2 ? 4 : 8;
-  constexpr int NS = DIM == 2 ? 3 : 6;
-  constexpr int NTG = NS + DIM + 1;           // Galerkin terms
-  constexpr int NTU = SUPG ? NT : NTG;        // terms used
+  constexpr int NV = DIM == 2 ? 4 : (NLOC == 8 || NLOC == 27 ? 8 : 4);
+  constexpr int NT = Terms<DIM>::NT;
   __shared__ double g[kCellTile][NT];
   const int tile0 = blockIdx.x * kCellTile;
   // phase 1: per-cell factors
   for (int c = threadIdx.x; c < kCellTile; c += blockDim.x) {
     int cell = tile0 + c;
-    if (cell < ncells) cell_factors<DIM>(k, verts + (size_t)cell * NV * DIM, g[c]);
+    if (cell < ncells) cell_factors<DIM>(k, verts + (size_t)cell * NV * DIM, g[c], mass_only);
   }
   __syncthreads();
   const int e_local = threadIdx.x % S::EPB;
@@ -374,16 +488,16 @@ k_element_contract(AsmCoefs k, int ncells, int nactive, const double* __restrict
   if (lane >= S::LANES || e >= S::NE) return;
   double r[NTU];
 #pragma unroll
-  for (int t = 0; t < NTU; ++t) r[t] = __ldg(R + (size_t)t * S::NE + e);
+  for (int t = 0; t < NTU; ++t) r[t] = __ldg(R + (size_t)tl.idx[t] * S::NE + e);
   const int i = e / NLOC;
   for (int c = lane; c < kCellTile; c += S::LANES) {
     int cell = tile0 + c;
     if (cell >= ncells) break;
     double acc = 0.0;
 #pragma unroll
-    for (int t = 0; t < NTU; ++t) acc = fma(g[c][t], r[t], acc);
+    for (int t = 0; t < NTU; ++t) acc = fma(g[c][tl.idx[t]], r[t], acc);
     int row = __ldg(gdof + (size_t)cell * NLOC + i);
-    if (row < nactive) atomicAdd(val + __ldg(slot + (size_t)cell * S::NE + e), acc);
+    if (all_rows || row < nactive) atomicAdd(val + __ldg(slot + (size_t)cell * S::NE + e), acc);
   }
 }
 
@@ -425,11 +539,22 @@ struct RhsTables {
   const double* grad;  // nqp*dim*nloc
 };
 
-__device__ void ref_node(int dim, int p, int k, double* r) {
+__constant__ double c_tet_p2_nodes[10][3] = {
+    {0, 0, 0}, {0.5, 0, 0}, {1, 0, 0}, {0, 0.5, 0}, {0.5, 0.5, 0},
+    {0, 1, 0}, {0, 0, 0.5}, {0.5, 0, 0.5}, {0, 0.5, 0.5}, {0, 0, 1}};
+__constant__ double c_tet_p1_nodes[4][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+
+__device__ void ref_node_s(int shape, int dim, int p, int k, double* r) {
+  if (shape == kTetra) {
+    for (int a = 0; a < 3; ++a) r[a] = p == 1 ? c_tet_p1_nodes[k][a] : c_tet_p2_nodes[k][a];
+    return;
+  }
   int n1 = p + 1;
   int i[3] = {k % n1, (k / n1) % n1, k / (n1 * n1)};
   for (int a = 0; a < 3; ++a) r[a] = (a < dim) ? -1.0 + (2.0 / p) * i[a] : 0.0;
 }
+
+__device__ void ref_node(int dim, int p, int k, double* r) { ref_node_s(dim == 2 ? kQuad : kHexa, dim, p, k, r); }
 
 __device__ void line_basis_d(int p, double t, double* v) {
   if (p == 1) {
@@ -464,14 +589,14 @@ template <int DIM>
 __global__ void __launch_bounds__(256)
 k_rhs(AsmCoefs k, int ncells, int nactive, const double* __restrict__ verts,
       const int* __restrict__ gdof, RhsTables tb, double* __restrict__ rhs) {
-  constexpr int NV = DIM == 2 ? 4 : 8;
+  const int NV = k.shape == kHexa ? 8 : 4;
   __shared__ double fw[8][128];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int cell = blockIdx.x * 8 + warp;
   if (cell >= ncells) return;
   const double* cv = verts + (size_t)cell * NV * DIM;
   Affine A;
-  cell_affine(DIM, cv, A);
+  cell_affine_s(k.shape, DIM, cv, A);
   const double adet = fabs(A.det);
   const double delta = cell_delta(k, cv, A);
   double bp[3] = {0, 0, 0};
@@ -508,9 +633,9 @@ k_rhs(AsmCoefs k, int ncells, int nactive, const double* __restrict__ verts,
     if (row < nactive) {
       atomicAdd(rhs + row, F);
     } else {
-      // Dirichlet value: nodal functional of Q1/Q2 = value at the node
-      double r[3], x[3], u[5];
-      ref_node(DIM, k.order, lane, r);
+      // Dirichlet value: nodal functional of Lagrange elements = value at the node
+      double r[3], x[3], u[6];
+      ref_node_s(k.shape, DIM, k.order, lane, r);
       for (int rr = 0; rr < DIM; ++rr) {
         double s = A.x0[rr];
         for (int a = 0; a < DIM; ++a) s += A.J[rr][a] * r[a];
@@ -543,7 +668,7 @@ k_rhs(AsmCoefs k, int ncells, int nactive, const double* __restrict__ verts,
         for (int l = 0; l < np; ++l) {
           double s = 0.5 * (lx[l] + 1);
           double x[2] = {a0[0] + s * (a1[0] - a0[0]), a0[1] + s * (a1[1] - a0[1])};
-          double u[5];
+          double u[6];
           ex_exact(k, x, u);
           double gval = k.eps * (nrm[comp][0] * u[1] + nrm[comp][1] * u[2]);
           double xi[2];
@@ -577,21 +702,18 @@ __global__ void __launch_bounds__(256)
 k_errors(AsmCoefs k, int ncells, const double* __restrict__ verts, const int* __restrict__ gdof,
          const double* __restrict__ sol, RhsTables tb, double* __restrict__ acc,
          unsigned long long* __restrict__ linf) {
-  constexpr int NV = DIM == 2 ? 4 : 8;
+  const int NV = k.shape == kHexa ? 8 : 4;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int cell = blockIdx.x * 8 + warp;
   if (cell >= ncells) return;
   const double* cv = verts + (size_t)cell * NV * DIM;
   Affine A;
-  cell_affine(DIM, cv, A);
+  cell_affine_s(k.shape, DIM, cv, A);
   const double adet = fabs(A.det);
-  const double hK = cell_hK(DIM, cv, k.cell_measure, A.det);
+  const double hK = cell_hK_s(k.shape, DIM, cv, k.cell_measure, A.det);
   const int nl = k.nloc;
   double fv = lane < nl ? sol[gdof[(size_t)cell * nl + lane]] : 0.0;
   double e[4] = {0, 0, 0, 0}, emax = 0.0;
-  double linfb = fmax(fabs(k.b[0]), fabs(k.b[1]));
-  if (DIM == 3) linfb = fmax(linfb, fabs(k.b[2]));
-  double delta = sdfem_delta(k, hK, k.eps, k.b, k.c, linfb);
   for (int q = 0; q < k.nqp; ++q) {
     // u_h and its gradient at q: warp reduction over local dofs
     double uh = lane < nl ? fv * tb.val[q * nl + lane] : 0.0;
@@ -606,20 +728,24 @@ k_errors(AsmCoefs k, int ncells, const double* __restrict__ verts, const int* __
       double g[3] = {0, 0, 0};
       for (int r = 0; r < DIM; ++r)
         for (int a = 0; a < DIM; ++a) g[r] += A.Ji[a][r] * gr[a];
-      double x[3], u[5];
+      double x[3], u[6], bx[3];
       for (int r = 0; r < DIM; ++r) {
         double s = A.x0[r];
         for (int a = 0; a < DIM; ++a) s += A.J[r][a] * tb.xi[q * 3 + a];
         x[r] = s;
       }
       ex_exact(k, x, u);
+      b_at(k, x, bx);
+      double linfb = fmax(fabs(bx[0]), fabs(bx[1]));
+      if (DIM == 3) linfb = fmax(linfb, fabs(bx[2]));
+      const double delta = sdfem_delta(k, hK, k.eps, bx, k.c, linfb);
       double w = tb.w[q] * adet;
       double e0 = uh - u[0];
       emax = fmax(emax, fabs(e0));
       double e1 = g[0] - u[1], e2 = g[1] - u[2], e3 = DIM == 2 ? 0.0 : g[2] - u[3];
       e[0] += w * e0 * e0;
       e[1] += w * (e1 * e1 + e2 * e2 + e3 * e3);
-      double e4 = k.b[0] * e1 + k.b[1] * e2 + (DIM == 3 ? k.b[2] * e3 : 0.0);
+      double e4 = bx[0] * e1 + bx[1] * e2 + (DIM == 3 ? bx[2] * e3 : 0.0);
       e[2] += w * (k.eps * (e1 * e1 + e2 * e2 + e3 * e3) + k.c * e0 * e0 + delta * e4 * e4);
       e[3] += w * (k.eps * (e1 * e1 + e2 * e2 + e3 * e3) + (e4 + k.c * e0) * e0);
     }
@@ -628,6 +754,77 @@ k_errors(AsmCoefs k, int ncells, const double* __restrict__ verts, const int* __
     for (int i = 0; i < 4; ++i) atomicAdd(acc + i, e[i]);
     atomicMax(linf, (unsigned long long)__double_as_longlong(emax));
   }
+}
+
+// ---------------------------------------------------------------------------
+// time-dependent CD pieces
+// ---------------------------------------------------------------------------
+// initial condition: nodal interpolation of the example's u0 (every DOF)
+__global__ void k_interpolate(AsmCoefs k, int ncells, const double* __restrict__ verts,
+                              const int* __restrict__ gdof, double* __restrict__ sol) {
+  const int NV = k.shape == kHexa ? 8 : 4;
+  const long n = (long)ncells * k.nloc;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < n;
+       t += (long)gridDim.x * blockDim.x) {
+    const int cell = (int)(t / k.nloc), loc = (int)(t % k.nloc);
+    const double* cv = verts + (size_t)cell * NV * k.dim;
+    Affine A;
+    cell_affine_s(k.shape, k.dim, cv, A);
+    double r[3], x[3];
+    ref_node_s(k.shape, k.dim, k.order, loc, r);
+    for (int rr = 0; rr < k.dim; ++rr) {
+      double s = A.x0[rr];
+      for (int a = 0; a < k.dim; ++a) s += A.J[rr][a] * r[a];
+      x[rr] = s;
+    }
+    sol[gdof[t]] = ex_initial(k, x);   // all cells sharing a node write one value
+  }
+}
+
+// Crank-Nicolson right-hand side (TimeDiscretizations.C:171-189):
+//   active rows:     tau/2 (f_new + f_old) + M u_old - tau/2 A u_old
+//   non-active rows: f_new (Dirichlet data, copy_nonactive)
+template <int TPR>
+__global__ void __launch_bounds__(256)
+k_cn_rhs(int n, int nactive, const int* __restrict__ rp, const int* __restrict__ col,
+         const double* __restrict__ Aval, const double* __restrict__ Mval,
+         const double* __restrict__ u, const double* __restrict__ fnew,
+         const double* __restrict__ fold, double half_tau, double* __restrict__ out) {
+  const long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  const int row = (int)(gt / TPR), sub = threadIdx.x % TPR;
+  double sa = 0.0, sm = 0.0;
+  if (row < nactive) {
+    const int e = rp[row + 1];
+    for (int k = rp[row] + sub; k < e; k += TPR) {
+      const double x = __ldg(u + __ldg(col + k));
+      sa = fma(__ldcs(Aval + k), x, sa);
+      sm = fma(__ldcs(Mval + k), x, sm);
+    }
+  }
+#pragma unroll
+  for (int o = TPR / 2; o > 0; o >>= 1) {
+    sa += __shfl_xor_sync(0xffffffffu, sa, o, TPR);
+    sm += __shfl_xor_sync(0xffffffffu, sm, o, TPR);
+  }
+  if (row >= n || sub != 0) return;
+  if (row < nactive) {
+    double r = half_tau * fnew[row];
+    r += half_tau * fold[row];
+    r += 1.0 * sm;
+    r += -half_tau * sa;
+    out[row] = r;
+  } else {
+    out[row] = fnew[row];
+  }
+}
+
+// system matrix (TimeDiscretizations.C:219-251): active rows tau/2 A + M,
+// non-active rows keep the assembled stiffness rows
+__global__ void k_cn_system(int nactive_entries, int nnz, const double* __restrict__ Aval,
+                            const double* __restrict__ Mval, double half_tau,
+                            double* __restrict__ S) {
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < nnz; t += (long)gridDim.x * blockDim.x)
+    S[t] = t < nactive_entries ? Aval[t] * half_tau + 1.0 * Mval[t] : Aval[t];
 }
 
 // ---------------------------------------------------------------------------
@@ -698,7 +895,8 @@ int free_level(DevLevel& L) {
   void* ptrs[] = {L.verts, L.gdof, L.row_ptr, L.col, L.slot, L.diag_slot, L.val64, L.val32,
                   L.rhs, L.sol, L.invdiag64, L.invdiag32, L.mg_rhs, L.mg_sol, L.mg_tmp,
                   L.mg_def, L.P_rp, L.P_col, L.P_val, L.P_val32, L.R_rp, L.R_col, L.R_val,
-                  L.R_val32, L.coarse_inv, L.coarse_work, L.dc_rp, L.dc_col, L.dc_pos};
+                  L.R_val32, L.coarse_inv, L.coarse_work, L.dc_rp, L.dc_col, L.dc_pos,
+                  L.tcd_A, L.tcd_M, L.tcd_f, L.tcd_fold};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   return CDG_OK;
@@ -732,7 +930,7 @@ int build_slots(cdg_context* ctx, DevLevel& L) {
 
 static int ensure_tables(cdg_context* ctx, cdg_problem* p) {
   if (p->d_tables && p->rt_order == p->order) return CDG_OK;
-  RefTensors T = make_ref_tensors(p->dim, p->order);
+  RefTensors T = make_ref_tensors(p->dim, p->order, p->shape);
   if (p->d_tables) cudaFree(p->d_tables);
   CDG_TRY(dalloc(&p->d_tables, T.R.size()));
   CDG_CUDA(cudaMemcpyAsync(p->d_tables, T.R.data(), T.R.size() * sizeof(double),
@@ -743,36 +941,93 @@ static int ensure_tables(cdg_context* ctx, cdg_problem* p) {
   return CDG_OK;
 }
 
-template <int DIM, int NLOC, int NT>
-static int launch_contract(cdg_context* ctx, const AsmCoefs& k, DevLevel& L, const double* R) {
+// contraction of the terms in `tl` (count NTU) into val
+template <int DIM, int NLOC, int NTU>
+static int launch_terms(cdg_context* ctx, const AsmCoefs& k, DevLevel& L, const double* R,
+                        const TermList& tl, bool mass_only, bool all_rows, double* out) {
   using S = ShapeInfo<NLOC>;
   dim3 grid((L.ncells + kCellTile - 1) / kCellTile, S::NEB);
-  if (k.supg)
-    CDG_LAUNCH(ctx, (k_element_contract<DIM, NLOC, NT, true>), grid, S::THREADS, 0, k, L.ncells,
-               L.nactive, L.verts, L.gdof, L.slot, R, L.val64);
-  else
-    CDG_LAUNCH(ctx, (k_element_contract<DIM, NLOC, NT, false>), grid, S::THREADS, 0, k,
-               L.ncells, L.nactive, L.verts, L.gdof, L.slot, R, L.val64);
+  CDG_LAUNCH(ctx, (k_element_contract<DIM, NLOC, NTU>), grid, S::THREADS, 0, k, tl,
+             mass_only ? 1 : 0, all_rows ? 1 : 0, L.ncells, L.nactive, L.verts, L.gdof,
+             L.slot, R, out);
   return CDG_OK;
 }
 
-// reference tables for the rhs / error rules, cached per (dim, order, nqp1)
+// term selection: galerkin (S, C, M [, L]), supg (S, C, M, D, T), mass (M)
+enum class TermSet { Galerkin, GalerkinLinear, Supg, Mass };
+
+template <int DIM, int NLOC>
+static int contract_set(cdg_context* ctx, const AsmCoefs& k, DevLevel& L, const double* R,
+                        TermSet set, bool all_rows, double* out) {
+  using TT = Terms<DIM>;
+  TermList tl{};
+  int n = 0;
+  if (set == TermSet::Mass) {
+    tl.idx[n++] = TT::offM;
+    return launch_terms<DIM, NLOC, 1>(ctx, k, L, R, tl, true, all_rows, out);
+  }
+  for (int t = 0; t < TT::offL; ++t) tl.idx[n++] = t;   // S, C, M
+  if (set == TermSet::GalerkinLinear) {
+    for (int t = TT::offL; t < TT::offD; ++t) tl.idx[n++] = t;
+    return launch_terms<DIM, NLOC, TT::offD>(ctx, k, L, R, tl, false, all_rows, out);
+  }
+  if (set == TermSet::Supg) {
+    for (int t = TT::offD; t < TT::NT; ++t) tl.idx[n++] = t;
+    return launch_terms<DIM, NLOC, TT::NT - DIM * DIM>(ctx, k, L, R, tl, false, all_rows, out);
+  }
+  return launch_terms<DIM, NLOC, TT::offL>(ctx, k, L, R, tl, false, all_rows, out);
+}
+
+static int contract(cdg_context* ctx, const AsmCoefs& k, DevLevel& L, const double* R,
+                    TermSet set, bool all_rows, double* out) {
+  if (L.shape == kQuad && L.nloc == 4) return contract_set<2, 4>(ctx, k, L, R, set, all_rows, out);
+  if (L.shape == kQuad && L.nloc == 9) return contract_set<2, 9>(ctx, k, L, R, set, all_rows, out);
+  if (L.shape == kHexa && L.nloc == 8) return contract_set<3, 8>(ctx, k, L, R, set, all_rows, out);
+  if (L.shape == kHexa && L.nloc == 27) return contract_set<3, 27>(ctx, k, L, R, set, all_rows, out);
+  if (L.shape == kTetra && L.nloc == 4) return contract_set<3, 4>(ctx, k, L, R, set, all_rows, out);
+  if (L.shape == kTetra && L.nloc == 10) return contract_set<3, 10>(ctx, k, L, R, set, all_rows, out);
+  set_error("unsupported element");
+  return CDG_ERR_ARG;
+}
+
+static TermSet stiffness_set(const AsmCoefs& k) {
+  if (k.supg) return TermSet::Supg;
+  return k.linear_b ? TermSet::GalerkinLinear : TermSet::Galerkin;
+}
+
+static int check_coefs(const AsmCoefs& k) {
+  if (k.nqp > 128) { set_error("quadrature rule too large"); return CDG_ERR_ARG; }
+  if (k.supg && k.linear_b) {
+    set_error("SUPG with a convection field linear in x is not supported");
+    return CDG_ERR_ARG;
+  }
+  return CDG_OK;
+}
+
+int contract_only(cdg_context* ctx, cdg_problem* p, DevLevel& L, const cdg_assembly_params& a) {
+  CDG_TRY(ensure_tables(ctx, p));
+  AsmCoefs k = make_coefs(a, L.shape, L.order);
+  CDG_TRY(check_coefs(k));
+  return contract(ctx, k, L, p->d_tables, stiffness_set(k), false, L.val64);
+}
+
+// reference tables for the rhs / error rules, cached per (shape, order, rule)
 struct DevRefTables {
-  int dim = 0, order = 0, nqp1 = 0;
+  int shape = -1, order = 0, nqp1 = 0;
   double* buf = nullptr;
   RhsTables t{};
 };
 static DevRefTables g_rt[8];
 
-static int get_rhs_tables(cdg_context* ctx, int dim, int order, int nqp1, RhsTables* out) {
-  int dev = ctx->device;
-  (void)dev;
+static int get_rhs_tables(cdg_context* ctx, int shape, int order, int nqp1, RhsTables* out) {
+  (void)ctx;
   for (auto& e : g_rt)
-    if (e.buf && e.dim == dim && e.order == order && e.nqp1 == nqp1) {
+    if (e.buf && e.shape == shape && e.order == order && e.nqp1 == nqp1) {
       *out = e.t;
       return CDG_OK;
     }
-  RefTables T = make_ref_tables(dim, order, nqp1);
+  const int dim = shape == kQuad ? 2 : 3;
+  RefTables T = make_ref_tables(dim, order, nqp1, shape);
   size_t n = T.xi.size() + T.w.size() + T.val.size() + T.grad.size();
   DevRefTables* slot = nullptr;
   for (auto& e : g_rt)
@@ -787,7 +1042,7 @@ static int get_rhs_tables(cdg_context* ctx, int dim, int order, int nqp1, RhsTab
   h.insert(h.end(), T.val.begin(), T.val.end());
   h.insert(h.end(), T.grad.begin(), T.grad.end());
   CDG_CUDA(cudaMemcpy(slot->buf, h.data(), n * sizeof(double), cudaMemcpyHostToDevice));
-  slot->dim = dim;
+  slot->shape = shape;
   slot->order = order;
   slot->nqp1 = nqp1;
   slot->t.xi = slot->buf;
@@ -798,58 +1053,51 @@ static int get_rhs_tables(cdg_context* ctx, int dim, int order, int nqp1, RhsTab
   return CDG_OK;
 }
 
-int contract_only(cdg_context* ctx, cdg_problem* p, DevLevel& L, const cdg_assembly_params& a) {
-  CDG_TRY(ensure_tables(ctx, p));
-  AsmCoefs k = make_coefs(a, L.dim, L.order, L.nloc);
-  const double* R = p->d_tables;
-  if (L.dim == 2 && L.nloc == 4) return launch_contract<2, 4, 14>(ctx, k, L, R);
-  if (L.dim == 2 && L.nloc == 9) return launch_contract<2, 9, 14>(ctx, k, L, R);
-  if (L.dim == 3 && L.nloc == 8) return launch_contract<3, 8, 31>(ctx, k, L, R);
-  if (L.dim == 3 && L.nloc == 27) return launch_contract<3, 27, 31>(ctx, k, L, R);
-  set_error("unsupported element");
-  return CDG_ERR_ARG;
-}
-
-int assemble_level(cdg_context* ctx, cdg_problem* p, DevLevel& L, const cdg_assembly_params& a) {
-  CDG_TRY(ensure_tables(ctx, p));
-  AsmCoefs k = make_coefs(a, L.dim, L.order, L.nloc);
-  if (k.nqp > 128) { set_error("quadrature rule too large"); return CDG_ERR_ARG; }
-  cudaStream_t st = ctx->stream;
-  // block->reset(), rhs.reset()
-  CDG_CUDA(cudaMemsetAsync(L.val64, 0, (size_t)L.nnz * sizeof(double), st));
-  CDG_CUDA(cudaMemsetAsync(L.rhs, 0, (size_t)L.ndof * sizeof(double), st));
-  const double* R = p->d_tables;
-  if (L.dim == 2 && L.nloc == 4) CDG_TRY((launch_contract<2, 4, 14>(ctx, k, L, R)));
-  else if (L.dim == 2 && L.nloc == 9) CDG_TRY((launch_contract<2, 9, 14>(ctx, k, L, R)));
-  else if (L.dim == 3 && L.nloc == 8) CDG_TRY((launch_contract<3, 8, 31>(ctx, k, L, R)));
-  else if (L.dim == 3 && L.nloc == 27) CDG_TRY((launch_contract<3, 27, 31>(ctx, k, L, R)));
-  else { set_error("unsupported element"); return CDG_ERR_ARG; }
-  int nd = L.ndof - L.nactive;
-  if (nd > 0)
-    CDG_LAUNCH(ctx, k_dirichlet_rows, grid_for<int>(nd, 256), 256, 0, L.ndof, L.nactive,
-               L.diag_slot, L.val64);
+static int launch_rhs(cdg_context* ctx, const AsmCoefs& k, DevLevel& L, double* out) {
   RhsTables tb;
-  CDG_TRY(get_rhs_tables(ctx, L.dim, L.order, k.nqp1, &tb));
+  CDG_TRY(get_rhs_tables(ctx, L.shape, L.order, k.nqp1, &tb));
   if (L.dim == 2)
     CDG_LAUNCH(ctx, k_rhs<2>, grid_for<int>(L.ncells, 8), 256, 0, k, L.ncells, L.nactive,
-               L.verts, L.gdof, tb, L.rhs);
+               L.verts, L.gdof, tb, out);
   else
     CDG_LAUNCH(ctx, k_rhs<3>, grid_for<int>(L.ncells, 8), 256, 0, k, L.ncells, L.nactive,
-               L.verts, L.gdof, tb, L.rhs);
-  if (nd > 0)
-    CDG_LAUNCH(ctx, k_copy_nonactive, grid_for<int>(nd, 256), 256, 0, L.ndof, L.nactive, L.rhs,
-               L.sol);
+               L.verts, L.gdof, tb, out);
+  return CDG_OK;
+}
+
+static int finish_matrix(cdg_context* ctx, cdg_problem* p, DevLevel& L) {
   int g = (int)std::min<long>(((long)std::max(L.nnz, L.ndof) + 255) / 256, (long)ctx->num_sms * 16);
   CDG_LAUNCH(ctx, k_finish_matrix, g, 256, 0, L.ndof, L.nnz, L.diag_slot, L.val64, L.val32,
              L.invdiag64, L.invdiag32, p->d_zero_diag);
   return CDG_OK;
 }
 
+int assemble_level(cdg_context* ctx, cdg_problem* p, DevLevel& L, const cdg_assembly_params& a) {
+  CDG_TRY(ensure_tables(ctx, p));
+  AsmCoefs k = make_coefs(a, L.shape, L.order);
+  CDG_TRY(check_coefs(k));
+  cudaStream_t st = ctx->stream;
+  // block->reset(), rhs.reset()
+  CDG_CUDA(cudaMemsetAsync(L.val64, 0, (size_t)L.nnz * sizeof(double), st));
+  CDG_CUDA(cudaMemsetAsync(L.rhs, 0, (size_t)L.ndof * sizeof(double), st));
+  CDG_TRY(contract(ctx, k, L, p->d_tables, stiffness_set(k), false, L.val64));
+  int nd = L.ndof - L.nactive;
+  if (nd > 0)
+    CDG_LAUNCH(ctx, k_dirichlet_rows, grid_for<int>(nd, 256), 256, 0, L.ndof, L.nactive,
+               L.diag_slot, L.val64);
+  CDG_TRY(launch_rhs(ctx, k, L, L.rhs));
+  if (nd > 0)
+    CDG_LAUNCH(ctx, k_copy_nonactive, grid_for<int>(nd, 256), 256, 0, L.ndof, L.nactive, L.rhs,
+               L.sol);
+  return finish_matrix(ctx, p, L);
+}
+
 int level_errors(cdg_context* ctx, cdg_problem* p, DevLevel& L, const cdg_assembly_params& a,
                  double* errors) {
-  AsmCoefs k = make_coefs(a, L.dim, L.order, L.nloc);
+  AsmCoefs k = make_coefs(a, L.shape, L.order);
+  if (k.nqp > 128) { set_error("quadrature rule too large"); return CDG_ERR_ARG; }
   RhsTables tb;
-  CDG_TRY(get_rhs_tables(ctx, L.dim, L.order, k.nqp1, &tb));
+  CDG_TRY(get_rhs_tables(ctx, L.shape, L.order, k.nqp1, &tb));
   double* acc = nullptr;
   CDG_TRY(dalloc(&acc, 5));
   CDG_CUDA(cudaMemsetAsync(acc, 0, 5 * sizeof(double), ctx->stream));
@@ -871,6 +1119,69 @@ int level_errors(cdg_context* ctx, cdg_problem* p, DevLevel& L, const cdg_assemb
   errors[4] = h[4];
   (void)p;
   return CDG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// time-dependent CD host pieces
+// ---------------------------------------------------------------------------
+static int ensure_tcd(DevLevel& L) {
+  if (L.tcd_A) return CDG_OK;
+  CDG_TRY(dalloc(&L.tcd_A, (size_t)L.nnz));
+  CDG_TRY(dalloc(&L.tcd_M, (size_t)L.nnz));
+  CDG_TRY(dalloc(&L.tcd_f, (size_t)L.ndof));
+  CDG_TRY(dalloc(&L.tcd_fold, (size_t)L.ndof));
+  CDG_CUDA(cudaMemset(L.tcd_fold, 0, (size_t)L.ndof * sizeof(double)));
+  return CDG_OK;
+}
+
+int tcd_interpolate(cdg_context* ctx, cdg_problem* p, const cdg_assembly_params& a) {
+  DevLevel& L = p->lev[0];
+  AsmCoefs k = make_coefs(a, L.shape, L.order);
+  long n = (long)L.ncells * L.nloc;
+  int g = (int)std::min<long>((n + 255) / 256, (long)ctx->num_sms * 16);
+  CDG_LAUNCH(ctx, k_interpolate, g, 256, 0, k, L.ncells, L.verts, L.gdof, L.sol);
+  return CDG_OK;
+}
+
+// TimeConvectionDiffusion::call_assembling_routine with assemble_dirichlet_rows
+// (TimeConvectionDiffusion.C:987-1052): stiffness (and mass) with full
+// Dirichlet rows, rhs f at time a.t
+int tcd_assemble_level(cdg_context* ctx, cdg_problem* p, DevLevel& L,
+                       const cdg_assembly_params& a, bool with_mass) {
+  CDG_TRY(ensure_tables(ctx, p));
+  CDG_TRY(ensure_tcd(L));
+  AsmCoefs k = make_coefs(a, L.shape, L.order);
+  CDG_TRY(check_coefs(k));
+  if (k.supg) { set_error("SUPG for the time-dependent problem is not supported"); return CDG_ERR_ARG; }
+  cudaStream_t st = ctx->stream;
+  CDG_CUDA(cudaMemsetAsync(L.tcd_A, 0, (size_t)L.nnz * sizeof(double), st));
+  CDG_TRY(contract(ctx, k, L, p->d_tables, stiffness_set(k), true, L.tcd_A));
+  if (with_mass) {
+    CDG_CUDA(cudaMemsetAsync(L.tcd_M, 0, (size_t)L.nnz * sizeof(double), st));
+    CDG_TRY(contract(ctx, k, L, p->d_tables, TermSet::Mass, true, L.tcd_M));
+  }
+  CDG_CUDA(cudaMemsetAsync(L.tcd_f, 0, (size_t)L.ndof * sizeof(double), st));
+  return launch_rhs(ctx, k, L, L.tcd_f);
+}
+
+// rhs of the step into L.rhs from L.sol (u_old), tcd_f (new) and tcd_fold;
+// then tcd_fold <- tcd_f
+int tcd_cn_rhs(cdg_context* ctx, DevLevel& L, double tau) {
+  const int tpr = 4;
+  int grid = (int)(((long)L.ndof * tpr + 255) / 256);
+  CDG_LAUNCH(ctx, k_cn_rhs<4>, grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, L.tcd_A,
+             L.tcd_M, L.sol, L.tcd_f, L.tcd_fold, 0.5 * tau, L.rhs);
+  CDG_CUDA(cudaMemcpyAsync(L.tcd_fold, L.tcd_f, (size_t)L.ndof * sizeof(double),
+                           cudaMemcpyDeviceToDevice, ctx->stream));
+  return CDG_OK;
+}
+
+// system matrix into val64 (+ FP32 copy and inverse diagonals)
+int tcd_system(cdg_context* ctx, cdg_problem* p, DevLevel& L, double tau) {
+  const int nae = L.pattern.row_ptr[L.nactive];
+  int g = (int)std::min<long>(((long)L.nnz + 255) / 256, (long)ctx->num_sms * 16);
+  CDG_LAUNCH(ctx, k_cn_system, g, 256, 0, nae, L.nnz, L.tcd_A, L.tcd_M, 0.5 * tau, L.val64);
+  return finish_matrix(ctx, p, L);
 }
 
 }  // namespace cdg
@@ -963,7 +1274,7 @@ k_errors_noalloc(AsmCoefs k, LineRule rule, int ncells, const double* __restrict
         double g[3] = {0, 0, 0};
         for (int r = 0; r < DIM; ++r)
           for (int a = 0; a < DIM; ++a) g[r] += A.Ji[a][r] * gr[a];
-        double x[3], u[5];
+        double x[3], u[6];
         for (int r = 0; r < DIM; ++r) {
           double s = A.x0[r];
           for (int a = 0; a < DIM; ++a) s += A.J[r][a] * xi[a];
@@ -1031,6 +1342,11 @@ extern "C" int cdg_problem_errors_noalloc(cdg_problem* p, const cdg_assembly_par
   }
   cdg_context* ctx = p->ctx;
   DevLevel& L = p->lev[0];
+  if (L.shape == kTetra) {
+    set_error("cdg_problem_errors_noalloc evaluates tensor-product bases only "
+              "(quadrilaterals, hexahedra); use cdg_problem_errors");
+    return CDG_ERR_ARG;
+  }
   if (L.ncells > kNoAllocMaxCells) {
     set_error("cdg_problem_errors_noalloc handles at most %d cells (its fixed scratch holds "
               "%d block partials); this level has %d cells, use cdg_problem_errors",
@@ -1052,7 +1368,7 @@ extern "C" int cdg_problem_errors_noalloc(cdg_problem* p, const cdg_assembly_par
     return CDG_ERR_CUDA;
   }
   double* scratch = g_errors_noalloc_ptr[ctx->device];
-  AsmCoefs k = make_coefs(*a, L.dim, L.order, L.nloc);
+  AsmCoefs k = make_coefs(*a, L.shape, L.order);
   LineRule rule;
   rule.n = k.nqp1;
   gauss_legendre(rule.n, rule.x, rule.w);

@@ -11,13 +11,24 @@ namespace cdg {
 
 constexpr int kMaxLoc = 27;    // Q2 hexahedron
 constexpr int kMaxQp1 = 10;    // 1D Gauss points
-constexpr int kMaxTerms = 32;  // reference tensors of one element type
+constexpr int kMaxTerms = 40;  // reference tensors of one element type
+
+// cell shapes
+enum Shape : int { kQuad = 0, kHexa = 1, kTetra = 2 };
+inline int shape_of(int dim, bool tetra) { return tetra ? kTetra : (dim == 2 ? kQuad : kHexa); }
+inline int n_vertices(int shape) { return shape == kHexa ? 8 : 4; }
+inline int n_local_dofs(int shape, int order) {
+  if (shape == kTetra) return order == 1 ? 4 : 10;
+  int n1 = order + 1;
+  return shape == kQuad ? n1 * n1 : n1 * n1 * n1;
+}
 
 // ---------------------------------------------------------------------------
 // mesh hierarchy (the reference's TDomain/TCollection as plain arrays)
 // ---------------------------------------------------------------------------
 struct Mesh {
   int dim = 2;
+  int shape = kQuad;
   int nv = 4;          // vertices per cell
   int ncells = 0;
   std::vector<double> verts;   // ncells * nv * dim, cell-local vertex order
@@ -25,7 +36,7 @@ struct Mesh {
 
 // FE space: the reference's TFESpace (GlobalNumbers with uniform BeginIndex)
 struct Space {
-  int dim = 2, order = 1, nloc = 4;
+  int dim = 2, shape = kQuad, order = 1, nloc = 4;
   int ndof = 0, nactive = 0;
   std::vector<int> gdof;       // ncells * nloc
 };
@@ -49,19 +60,21 @@ struct HostCsr {
 void gauss_legendre(int n, double* x, double* w);
 int gauss_points_for_degree(int degree);   // quad/hexa accuracy -> points/dir
 
-// Reference tensors of one (dim, order) element, used by the element-matrix
-// contraction A_ij = sum_t g_t(cell) R_t[i][j].  Term layout (2D sizes in
-// brackets): [0..5]  (3) S^{ab}: sym. gradient-gradient pairs
-//            [6..8]  (2) C^a:  phi_i d_a phi_j          (convection)
-//            [9]     (1) M:    phi_i phi_j              (reaction)
-//            [10..12](2) D^a:  d_a phi_i phi_j          (SUPG reaction)
-//            [13..30](6) T^{(ab),c}: d_c phi_i d_ab phi_j (SUPG diffusion)
+// Reference tensors of one element type, used by the element-matrix
+// contraction A_ij = sum_t g_t(cell) R_t[i][j].  Term blocks in order:
+//   S^{ab}  (ns = d(d+1)/2) symmetric gradient pairs d_a phi_i d_b phi_j (+ba)
+//   C^a     (d)    phi_i d_a phi_j                 (convection)
+//   M       (1)    phi_i phi_j                     (reaction, mass)
+//   L^{a,c} (d*d)  phi_i xi_c d_a phi_j            (convection linear in x)
+//   D^a     (d)    d_a phi_i phi_j                 (SUPG reaction)
+//   T^{(ab),c} (ns*d) d_c phi_i d_ab phi_j         (SUPG diffusion)
 struct RefTensors {
-  int dim = 2, order = 1, nloc = 4, nterms = 0;
+  int dim = 2, shape = kQuad, order = 1, nloc = 4, nterms = 0;
   int n_sym = 3;                  // symmetric derivative pairs
+  int offC = 0, offM = 0, offL = 0, offD = 0, offT = 0;
   std::vector<double> R;          // nterms * nloc * nloc
 };
-RefTensors make_ref_tensors(int dim, int order);
+RefTensors make_ref_tensors(int dim, int order, int shape);
 
 // values / gradients / Hessians of the reference basis at quadrature points
 struct RefTables {
@@ -71,11 +84,18 @@ struct RefTables {
   std::vector<double> val;  // nqp * nloc   phi
   std::vector<double> grad; // nqp * dim * nloc  d_a phi
 };
-RefTables make_ref_tables(int dim, int order, int nqp1);
+RefTables make_ref_tables(int dim, int order, int nqp1, int shape);
+// points per direction of the collapsed Gauss rule that integrates degree
+// `degree` exactly on the reference tetrahedron
+int tetra_points_for_degree(int degree);
 
 void ref_basis_point(int dim, int order, const double* xi, double* val,
                      double* grad /* dim*nloc */, double* hess /* sym */);
+void tetra_basis_point(int order, const double* xi, double* val, double* grad, double* hess);
 void local_dof_ref(int dim, int order, int k, double* r);
+void local_dof_ref_shape(int shape, int order, int k, double* r);
+// x = affine map of the cell (QuadAffin / HexaAffin / TetraAffin) at r
+void cell_point(int shape, int dim, const double* cv, const double* r, double* x);
 
 // ---------------------------------------------------------------------------
 // setup: structured meshes, DOF numbering, pattern, grid transfer
@@ -83,6 +103,13 @@ void local_dof_ref(int dim, int order, int k, double* r);
 // unit square / cube split into roots^dim cells, each refined nref times;
 // children in depth-first order, so parent(fine cell f) = f / 2^dim
 Mesh make_refined_box(int dim, int roots, int nref);
+// unit cube split into roots^3 cubes of 6 Kuhn tetrahedra each (permutation
+// order), refined nref times by Bey's red refinement (children stay Kuhn
+// tetrahedra, parent(fine cell f) = f / 8)
+Mesh make_kuhn_box(int roots, int nref);
+// move every vertex off the boundary by amplitude*h*U(-1,1) per coordinate,
+// the same displacement for every cell sharing the vertex (seeded)
+void perturb_interior(Mesh& m, double h, double amplitude, unsigned long long seed);
 // DOF numbering: inner, then non-Dirichlet boundary, then Dirichlet; each
 // class numbered in order of first appearance over (cell, local dof)
 Space make_space(const Mesh& m, int order, int neumann_mask);

@@ -59,7 +59,7 @@ namespace cdg {
 
 // one discretisation level on the device
 struct DevLevel {
-  int dim = 2, order = 1, nloc = 4, nv = 4;
+  int dim = 2, shape = kQuad, order = 1, nloc = 4, nv = 4;
   int ncells = 0, ndof = 0, nactive = 0, nnz = 0;
   // host copies of the inputs (info queries, transfers)
   Mesh mesh;
@@ -95,6 +95,12 @@ struct DevLevel {
   int* P_rp = nullptr; int* P_col = nullptr; double* P_val = nullptr; float* P_val32 = nullptr;
   int* R_rp = nullptr; int* R_col = nullptr; double* R_val = nullptr; float* R_val32 = nullptr;
   int P_nnz = 0, R_nnz = 0;
+  // time-dependent CD (Crank-Nicolson): stiffness and mass values (the system
+  // M + tau/2 A lives in val64), rhs of the current and the previous step
+  double* tcd_A = nullptr;
+  double* tcd_M = nullptr;
+  double* tcd_f = nullptr;
+  double* tcd_fold = nullptr;
   // dense inverse of the active block (coarsest multigrid level)
   double* coarse_inv = nullptr;  // na*na
   double* coarse_work = nullptr; // 2 * na * 2na (Gauss-Jordan ping-pong)
@@ -119,7 +125,7 @@ struct GmresState {
 
 struct cdg_problem {
   cdg_context* ctx = nullptr;
-  int dim = 2, order = 1;
+  int dim = 2, shape = cdg::kQuad, order = 1;
   std::vector<cdg::DevLevel> lev;
   cdg::GmresState gm;
   double* d_tables = nullptr;     // reference tensors (device)
@@ -129,8 +135,9 @@ struct cdg_problem {
 };
 
 struct cdg_hierarchy {
-  int dim = 2, order = 1;
-  std::vector<cdg::Mesh> mesh;
+  int dim = 2, shape = cdg::kQuad, order = 1;
+  std::vector<cdg::Mesh> mesh;           // geometry (finest level perturbed)
+  std::vector<cdg::Mesh> mesh_nested;    // unperturbed, locates fine nodes in parents
   std::vector<cdg::Space> space;
   std::vector<cdg::Pattern> pattern;
 };
@@ -164,6 +171,12 @@ int assemble_level(cdg_context* ctx, cdg_problem* p, DevLevel& L,
 int check_device_error(cdg_context* ctx);
 int level_errors(cdg_context* ctx, cdg_problem* p, DevLevel& L,
                  const cdg_assembly_params& a, double* errors);
+// time-dependent CD (TimeConvectionDiffusion with Crank-Nicolson)
+int tcd_interpolate(cdg_context* ctx, cdg_problem* p, const cdg_assembly_params& a);
+int tcd_assemble_level(cdg_context* ctx, cdg_problem* p, DevLevel& L,
+                       const cdg_assembly_params& a, bool with_mass);
+int tcd_cn_rhs(cdg_context* ctx, DevLevel& L, double tau);
+int tcd_system(cdg_context* ctx, cdg_problem* p, DevLevel& L, double tau);
 
 // linear algebra (linalg.cu)
 int spmv_apply64(cdg_context* ctx, const DevLevel& L, const double* x, double* y);

@@ -89,6 +89,84 @@ void local_dof_ref(int dim, int p, int k, double* r) {
   for (int a = 0; a < 3; ++a) r[a] = (a < dim) ? -1.0 + (2.0 / p) * i[a] : 0.0;
 }
 
+// P1/P2 tetrahedron: local DOFs in the order of include/FE3D/NF_C_T_P2_3D.h
+// (vertices 0, 2, 5, 9 and edge midpoints 1 (v0v1), 3 (v0v2), 4 (v1v2),
+// 6 (v0v3), 7 (v1v3), 8 (v2v3)); P1: the four vertices
+static const double kTetP2Nodes[10][3] = {{0, 0, 0},     {0.5, 0, 0}, {1, 0, 0},     {0, 0.5, 0},
+                                          {0.5, 0.5, 0}, {0, 1, 0},   {0, 0, 0.5},   {0.5, 0, 0.5},
+                                          {0, 0.5, 0.5}, {0, 0, 1}};
+static const double kTetP1Nodes[4][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+
+void local_dof_ref_shape(int shape, int order, int k, double* r) {
+  if (shape == kTetra) {
+    const double* q = order == 1 ? kTetP1Nodes[k] : kTetP2Nodes[k];
+    r[0] = q[0];
+    r[1] = q[1];
+    r[2] = q[2];
+    return;
+  }
+  local_dof_ref(shape == kQuad ? 2 : 3, order, k, r);
+}
+
+// barycentric Lagrange basis on the reference tetrahedron, with gradient and
+// Hessian (pairs 00,01,02,11,12,22) in reference coordinates
+void tetra_basis_point(int order, const double* xi, double* val, double* grad, double* hess) {
+  const double l[4] = {1.0 - xi[0] - xi[1] - xi[2], xi[0], xi[1], xi[2]};
+  // d lambda_v / d xi_a
+  auto dl = [](int v, int a) { return v == 0 ? -1.0 : (v - 1 == a ? 1.0 : 0.0); };
+  const int nl = order == 1 ? 4 : 10;
+  if (order == 1) {
+    for (int k = 0; k < 4; ++k) {
+      if (val) val[k] = l[k];
+      if (grad)
+        for (int a = 0; a < 3; ++a) grad[a * nl + k] = dl(k, a);
+      if (hess)
+        for (int s = 0; s < 6; ++s) hess[s * nl + k] = 0.0;
+    }
+    return;
+  }
+  // node k: vertex (va == vb) -> l(2l-1); edge -> 4 la lb
+  static const int va[10] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3};
+  static const int vb[10] = {0, 1, 1, 2, 2, 2, 3, 3, 3, 3};
+  static const int pa[6] = {0, 0, 0, 1, 1, 2}, pb[6] = {0, 1, 2, 1, 2, 2};
+  for (int k = 0; k < 10; ++k) {
+    const int a0 = va[k], b0 = vb[k];
+    if (a0 == b0) {
+      if (val) val[k] = l[a0] * (2.0 * l[a0] - 1.0);
+      if (grad)
+        for (int a = 0; a < 3; ++a) grad[a * nl + k] = (4.0 * l[a0] - 1.0) * dl(a0, a);
+      if (hess)
+        for (int s = 0; s < 6; ++s) hess[s * nl + k] = 4.0 * dl(a0, pa[s]) * dl(a0, pb[s]);
+    } else {
+      if (val) val[k] = 4.0 * l[a0] * l[b0];
+      if (grad)
+        for (int a = 0; a < 3; ++a) grad[a * nl + k] = 4.0 * (dl(a0, a) * l[b0] + l[a0] * dl(b0, a));
+      if (hess)
+        for (int s = 0; s < 6; ++s)
+          hess[s * nl + k] = 4.0 * (dl(a0, pa[s]) * dl(b0, pb[s]) + dl(a0, pb[s]) * dl(b0, pa[s]));
+    }
+  }
+}
+
+void cell_point(int shape, int dim, const double* cv, const double* r, double* x) {
+  if (shape == kTetra) {
+    // TetraAffin: x = v0 + (v1-v0) xi + (v2-v0) eta + (v3-v0) zeta
+    for (int c = 0; c < 3; ++c) {
+      double s = cv[c];
+      for (int a = 0; a < 3; ++a) s += r[a] * (cv[(a + 1) * 3 + c] - cv[c]);
+      x[c] = s;
+    }
+    return;
+  }
+  // QuadAffin / HexaAffin: x = v0 + sum_a (r_a + 1)/2 (v_{e_a} - v0), e = (1, 3, 4)
+  const int e[3] = {1, 3, 4};
+  for (int c = 0; c < dim; ++c) {
+    double s = cv[c];
+    for (int a = 0; a < dim; ++a) s += 0.5 * (r[a] + 1.0) * (cv[e[a] * dim + c] - cv[c]);
+    x[c] = s;
+  }
+}
+
 // hess: symmetric pairs (a<=b) in order (00,01,11) / (00,01,02,11,12,22)
 void ref_basis_point(int dim, int p, const double* xi, double* val, double* grad,
                      double* hess) {
@@ -129,80 +207,128 @@ void ref_basis_point(int dim, int p, const double* xi, double* val, double* grad
   }
 }
 
-RefTensors make_ref_tensors(int dim, int p) {
+// collapsed (Duffy) Gauss rule on the reference tetrahedron with n points per
+// direction: xi = u, eta = v (1-u), zeta = w (1-u)(1-v), exact for degree
+// <= 2n-3
+int tetra_points_for_degree(int degree) { return (degree + 4) / 2; }
+
+static void tetra_rule(int n, std::vector<double>& pts, std::vector<double>& wts) {
+  double x[kMaxQp1], w[kMaxQp1];
+  gauss_legendre(n, x, w);
+  pts.clear();
+  wts.clear();
+  for (int k = 0; k < n; ++k)
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) {
+        const double u = 0.5 * (x[i] + 1), v = 0.5 * (x[j] + 1), t = 0.5 * (x[k] + 1);
+        pts.push_back(u);
+        pts.push_back(v * (1 - u));
+        pts.push_back(t * (1 - u) * (1 - v));
+        wts.push_back(0.125 * w[i] * w[j] * w[k] * (1 - u) * (1 - u) * (1 - v));
+      }
+}
+
+// quadrature points/weights on the reference cell of `shape`
+static void shape_rule(int shape, int n, std::vector<double>& pts, std::vector<double>& wts) {
+  if (shape == kTetra) {
+    tetra_rule(n, pts, wts);
+    return;
+  }
+  const int dim = shape == kQuad ? 2 : 3;
+  double x[kMaxQp1], w[kMaxQp1];
+  gauss_legendre(n, x, w);
+  pts.clear();
+  wts.clear();
+  const int nq = dim == 2 ? n * n : n * n * n;
+  for (int q = 0; q < nq; ++q) {
+    const int qi[3] = {q % n, (q / n) % n, q / (n * n)};
+    pts.push_back(x[qi[0]]);
+    pts.push_back(x[qi[1]]);
+    pts.push_back(dim == 3 ? x[qi[2]] : 0.0);
+    wts.push_back(w[qi[0]] * w[qi[1]] * (dim == 3 ? w[qi[2]] : 1.0));
+  }
+}
+
+static void basis_at(int shape, int p, const double* xi, double* val, double* grad, double* hess) {
+  if (shape == kTetra)
+    tetra_basis_point(p, xi, val, grad, hess);
+  else
+    ref_basis_point(shape == kQuad ? 2 : 3, p, xi, val, grad, hess);
+}
+
+RefTensors make_ref_tensors(int dim, int p, int shape) {
   RefTensors T;
   T.dim = dim;
+  T.shape = shape;
   T.order = p;
-  int n1 = p + 1;
-  T.nloc = dim == 2 ? n1 * n1 : n1 * n1 * n1;
+  T.nloc = n_local_dofs(shape, p);
   T.n_sym = dim == 2 ? 3 : 6;
-  int nl = T.nloc, ns = T.n_sym;
-  T.nterms = ns + dim + 1 + dim + ns * dim;
+  const int nl = T.nloc, ns = T.n_sym;
+  T.offC = ns;
+  T.offM = ns + dim;
+  T.offL = ns + dim + 1;
+  T.offD = T.offL + dim * dim;
+  T.offT = T.offD + dim;
+  T.nterms = T.offT + ns * dim;
   T.R.assign((size_t)T.nterms * nl * nl, 0.0);
-  // Gauss with 4 points per direction integrates every product exactly
-  // (degree <= 4 per direction for Q2), like the reference's rules do.
-  const int nq1 = 4;
-  double x[kMaxQp1], w[kMaxQp1];
-  gauss_legendre(nq1, x, w);
+  // every integrand is a polynomial of degree <= 5 per direction (Q2: 4 + the
+  // linear factor of L); these rules integrate all of them exactly, like the
+  // reference's rules do for the terms it assembles
+  std::vector<double> pts, wts;
+  shape_rule(shape, shape == kTetra ? 5 : 4, pts, wts);
   int pa[6], pb[6];
   {
     int k = 0;
     for (int a = 0; a < dim; ++a)
       for (int b = a; b < dim; ++b) { pa[k] = a; pb[k] = b; ++k; }
   }
-  const int offC = ns, offM = ns + dim, offD = ns + dim + 1, offT = ns + 2 * dim + 1;
   std::vector<double> val(nl), grad(3 * nl), hess(6 * nl);
-  int nq = dim == 2 ? nq1 * nq1 : nq1 * nq1 * nq1;
-  for (int q = 0; q < nq; ++q) {
-    int qi[3] = {q % nq1, (q / nq1) % nq1, q / (nq1 * nq1)};
-    double xi[3] = {x[qi[0]], x[qi[1]], dim == 3 ? x[qi[2]] : 0.0};
-    double wq = w[qi[0]] * w[qi[1]] * (dim == 3 ? w[qi[2]] : 1.0);
-    ref_basis_point(dim, p, xi, val.data(), grad.data(), hess.data());
+  const size_t NE = (size_t)nl * nl;
+  for (size_t q = 0; q < wts.size(); ++q) {
+    const double* xi = &pts[3 * q];
+    const double wq = wts[q];
+    basis_at(shape, p, xi, val.data(), grad.data(), hess.data());
     for (int i = 0; i < nl; ++i)
       for (int j = 0; j < nl; ++j) {
-        size_t ij = (size_t)i * nl + j;
-        for (int s = 0; s < ns; ++s) {
-          int a = pa[s], b = pb[s];
+        const size_t ij = (size_t)i * nl + j;
+        for (int s2 = 0; s2 < ns; ++s2) {
+          const int a = pa[s2], b = pb[s2];
           double v = grad[a * nl + i] * grad[b * nl + j];
           if (a != b) v += grad[b * nl + i] * grad[a * nl + j];
-          T.R[(size_t)s * nl * nl + ij] += wq * v;
+          T.R[(size_t)s2 * NE + ij] += wq * v;
         }
         for (int a = 0; a < dim; ++a) {
-          T.R[(size_t)(offC + a) * nl * nl + ij] += wq * val[i] * grad[a * nl + j];
-          T.R[(size_t)(offD + a) * nl * nl + ij] += wq * grad[a * nl + i] * val[j];
-        }
-        T.R[(size_t)offM * nl * nl + ij] += wq * val[i] * val[j];
-        for (int s = 0; s < ns; ++s)
+          T.R[(size_t)(T.offC + a) * NE + ij] += wq * val[i] * grad[a * nl + j];
+          T.R[(size_t)(T.offD + a) * NE + ij] += wq * grad[a * nl + i] * val[j];
           for (int c = 0; c < dim; ++c)
-            T.R[(size_t)(offT + s * dim + c) * nl * nl + ij] +=
-                wq * grad[c * nl + i] * hess[s * nl + j];
+            T.R[(size_t)(T.offL + a * dim + c) * NE + ij] += wq * val[i] * xi[c] * grad[a * nl + j];
+        }
+        T.R[(size_t)T.offM * NE + ij] += wq * val[i] * val[j];
+        for (int s2 = 0; s2 < ns; ++s2)
+          for (int c = 0; c < dim; ++c)
+            T.R[(size_t)(T.offT + s2 * dim + c) * NE + ij] +=
+                wq * grad[c * nl + i] * hess[s2 * nl + j];
       }
   }
   return T;
 }
 
-RefTables make_ref_tables(int dim, int p, int nqp1) {
+RefTables make_ref_tables(int dim, int p, int nqp1, int shape) {
   RefTables t;
   t.dim = dim;
   t.order = p;
-  int n1 = p + 1;
-  t.nloc = dim == 2 ? n1 * n1 : n1 * n1 * n1;
+  t.nloc = n_local_dofs(shape, p);
   t.nqp1 = nqp1;
-  t.nqp = dim == 2 ? nqp1 * nqp1 : nqp1 * nqp1 * nqp1;
-  double x[kMaxQp1], w[kMaxQp1];
-  gauss_legendre(nqp1, x, w);
-  t.xi.resize((size_t)t.nqp * 3);
-  t.w.resize(t.nqp);
+  std::vector<double> pts, wts;
+  shape_rule(shape, nqp1, pts, wts);
+  t.nqp = (int)wts.size();
+  t.xi = pts;
+  t.w = wts;
   t.val.resize((size_t)t.nqp * t.nloc);
   t.grad.resize((size_t)t.nqp * dim * t.nloc);
-  for (int q = 0; q < t.nqp; ++q) {
-    int qi[3] = {q % nqp1, (q / nqp1) % nqp1, q / (nqp1 * nqp1)};
-    double xi[3] = {x[qi[0]], x[qi[1]], dim == 3 ? x[qi[2]] : 0.0};
-    t.w[q] = w[qi[0]] * w[qi[1]] * (dim == 3 ? w[qi[2]] : 1.0);
-    for (int a = 0; a < 3; ++a) t.xi[q * 3 + a] = xi[a];
-    ref_basis_point(dim, p, xi, &t.val[(size_t)q * t.nloc],
-                    &t.grad[(size_t)q * dim * t.nloc], nullptr);
-  }
+  for (int q = 0; q < t.nqp; ++q)
+    basis_at(shape, p, &pts[3 * q], &t.val[(size_t)q * t.nloc], &t.grad[(size_t)q * dim * t.nloc],
+             nullptr);
   return t;
 }
 
@@ -235,6 +361,7 @@ Mesh make_refined_box(int dim, int roots, int nref) {
   // and the refinement tree of each depth-first
   Mesh m;
   m.dim = dim;
+  m.shape = dim == 2 ? kQuad : kHexa;
   m.nv = dim == 2 ? 4 : 8;
   m.ncells = dim == 2 ? roots * roots : roots * roots * roots;
   static const double sq[4][2] = {{0, 0}, {1, 0}, {1, 1}, {0, 1}};
@@ -276,6 +403,82 @@ Mesh make_refined_box(int dim, int roots, int nref) {
   return m;
 }
 
+// Bey's regular refinement of a tetrahedron (x0,x1,x2,x3): the four corner
+// tetrahedra and the four of the inner octahedron split along x02-x13; with a
+// Kuhn-ordered parent every child is a Kuhn tetrahedron of the halved grid
+static const int kTetChild[8][4][2] = {
+    {{0, 0}, {0, 1}, {0, 2}, {0, 3}}, {{0, 1}, {1, 1}, {1, 2}, {1, 3}},
+    {{0, 2}, {1, 2}, {2, 2}, {2, 3}}, {{0, 3}, {1, 3}, {2, 3}, {3, 3}},
+    {{0, 1}, {0, 2}, {0, 3}, {1, 3}}, {{0, 1}, {0, 2}, {1, 2}, {1, 3}},
+    {{0, 2}, {0, 3}, {1, 3}, {2, 3}}, {{0, 2}, {1, 2}, {1, 3}, {2, 3}}};
+
+Mesh make_kuhn_box(int roots, int nref) {
+  Mesh m;
+  m.dim = 3;
+  m.shape = kTetra;
+  m.nv = 4;
+  // six tetrahedra per cube, one per permutation of the axes (lexicographic)
+  static const int perm[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+  const int ncube = roots * roots * roots;
+  m.ncells = 6 * ncube;
+  m.verts.resize((size_t)m.ncells * 12);
+  for (int c = 0; c < ncube; ++c) {
+    const int ijk[3] = {c % roots, (c / roots) % roots, c / (roots * roots)};
+    for (int t = 0; t < 6; ++t) {
+      int pt[3] = {ijk[0], ijk[1], ijk[2]};
+      double* cv = &m.verts[((size_t)c * 6 + t) * 12];
+      for (int a = 0; a < 3; ++a) cv[a] = (double)pt[a] / roots;
+      for (int s = 0; s < 3; ++s) {
+        pt[perm[t][s]] += 1;
+        for (int a = 0; a < 3; ++a) cv[(s + 1) * 3 + a] = (double)pt[a] / roots;
+      }
+    }
+  }
+  for (int r = 0; r < nref; ++r) {
+    std::vector<double> out((size_t)m.ncells * 8 * 12);
+    for (int c = 0; c < m.ncells; ++c) {
+      const double* pv = &m.verts[(size_t)c * 12];
+      for (int ch = 0; ch < 8; ++ch)
+        for (int v = 0; v < 4; ++v)
+          for (int a = 0; a < 3; ++a)
+            out[(((size_t)c * 8 + ch) * 4 + v) * 3 + a] =
+                0.5 * (pv[kTetChild[ch][v][0] * 3 + a] + pv[kTetChild[ch][v][1] * 3 + a]);
+    }
+    m.verts.swap(out);
+    m.ncells *= 8;
+  }
+  return m;
+}
+
+static inline unsigned long long mix64(unsigned long long z) {
+  z += 0x9e3779b97f4a7c15ULL;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+  return z ^ (z >> 31);
+}
+
+void perturb_interior(Mesh& m, double h, double amplitude, unsigned long long seed) {
+  const int dim = m.dim;
+  const long res = std::lround(1.0 / h);
+  const size_t nvt = (size_t)m.ncells * m.nv;
+  for (size_t v = 0; v < nvt; ++v) {
+    double* x = &m.verts[v * dim];
+    bool boundary = false;
+    long key = 0;
+    for (int a = dim - 1; a >= 0; --a) {
+      const long ia = std::lround(x[a] * res);
+      if (ia == 0 || ia == res) boundary = true;
+      key = key * (res + 1) + ia;
+    }
+    if (boundary) continue;
+    for (int a = 0; a < dim; ++a) {
+      const unsigned long long r = mix64(mix64((unsigned long long)key * 3 + a) ^ seed);
+      const double u = (double)(r >> 11) * (1.0 / 9007199254740992.0);   // [0,1)
+      x[a] += amplitude * h * (2.0 * u - 1.0);
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // DOF numbering
 // ---------------------------------------------------------------------------
@@ -297,43 +500,32 @@ int boundary_component(int dim, const double* x) {
   return -1;
 }
 
-static void affine_point(int dim, const double* cv, const double* r, double* x) {
-  // x = v0 + sum_a (r_a + 1)/2 (v_{e_a} - v0), e = (1, 3, 4) (QuadAffin/HexaAffin)
-  const int e[3] = {1, 3, 4};
-  for (int c = 0; c < dim; ++c) {
-    double s = cv[c];
-    for (int a = 0; a < dim; ++a) s += 0.5 * (r[a] + 1.0) * (cv[e[a] * dim + c] - cv[c]);
-    x[c] = s;
-  }
-}
-
 Space make_space(const Mesh& m, int p, int neumann_mask) {
   Space s;
   s.dim = m.dim;
+  s.shape = m.shape;
   s.order = p;
-  int n1 = p + 1;
-  s.nloc = m.dim == 2 ? n1 * n1 : n1 * n1 * n1;
-  int dim = m.dim, nl = s.nloc;
-  // lattice resolution from the first cell's edge length (uniform meshes)
-  double h = std::fabs(m.verts[dim] - m.verts[0]) + std::fabs(m.verts[dim + 1] - m.verts[1]);
-  if (dim == 3) h += std::fabs(m.verts[dim + 2] - m.verts[2]);
-  long nres = std::lround(p / h);
-  long n1l = nres + 1;
-  size_t nkeys = dim == 2 ? (size_t)n1l * n1l : (size_t)n1l * n1l * n1l;
+  s.nloc = n_local_dofs(m.shape, p);
+  const int dim = m.dim, nl = s.nloc;
+  // lattice resolution from the first cell's first edge (axis-aligned length h
+  // for all meshes built here); DOFs sit on multiples of h/p
+  double h = 0;
+  for (int a = 0; a < dim; ++a) h += std::fabs(m.verts[dim + a] - m.verts[a]);
+  const long nres = std::lround(p / h);
+  const long n1l = nres + 1;
+  const size_t nkeys = dim == 2 ? (size_t)n1l * n1l : (size_t)n1l * n1l * n1l;
   // class per lattice point: 0 inner, 1 non-Dirichlet boundary, 2 Dirichlet
-  std::vector<int> first(nkeys, -1);
   std::vector<long> keys((size_t)m.ncells * nl);
   std::vector<signed char> cls((size_t)m.ncells * nl);
   for (int c = 0; c < m.ncells; ++c) {
     const double* cv = &m.verts[(size_t)c * m.nv * dim];
     for (int k = 0; k < nl; ++k) {
       double r[3], x[3];
-      local_dof_ref(dim, p, k, r);
-      affine_point(dim, cv, r, x);
+      local_dof_ref_shape(m.shape, p, k, r);
+      cell_point(m.shape, dim, cv, r, x);
       long key = 0;
       for (int a = dim - 1; a >= 0; --a) key = key * n1l + std::lround(x[a] * nres);
       keys[(size_t)c * nl + k] = key;
-      // boundary components this point lies on
       int cl = 0;
       const double t = 1e-12;
       for (int a = 0; a < dim; ++a)
@@ -341,8 +533,8 @@ Space make_space(const Mesh& m, int p, int neumann_mask) {
           if (std::fabs(x[a] - side) >= t) continue;
           double probe[3] = {0.5, 0.5, 0.5};
           probe[a] = side;
-          int comp = boundary_component(dim, probe);
-          int t_ = ((neumann_mask >> comp) & 1) ? 1 : 2;
+          const int comp = boundary_component(dim, probe);
+          const int t_ = ((neumann_mask >> comp) & 1) ? 1 : 2;
           cl = std::max(cl, t_);
         }
       cls[(size_t)c * nl + k] = (signed char)cl;
@@ -350,16 +542,16 @@ Space make_space(const Mesh& m, int p, int neumann_mask) {
   }
   // number representatives by class, in order of first appearance
   std::vector<int> id(nkeys, -1);
+  std::vector<signed char> cls_of_key(nkeys, 0);
   int count[3] = {0, 0, 0};
-  std::vector<int> cls_of_key(nkeys, 0);
   for (size_t i = 0; i < keys.size(); ++i) {
-    long key = keys[i];
+    const long key = keys[i];
     if (id[key] < 0) {
       id[key] = count[cls[i]]++;
       cls_of_key[key] = cls[i];
     }
   }
-  int off[3] = {0, count[0], count[0] + count[1]};
+  const int off[3] = {0, count[0], count[0] + count[1]};
   s.gdof.resize(keys.size());
   for (size_t i = 0; i < keys.size(); ++i) s.gdof[i] = off[cls_of_key[keys[i]]] + id[keys[i]];
   s.nactive = count[0] + count[1];
@@ -399,54 +591,62 @@ Pattern make_pattern(const Space& s) {
 // ---------------------------------------------------------------------------
 void make_transfer(const Mesh& fm, const Space& fs, const Mesh& cm, const Space& cs,
                    const int* parent, HostCsr* P, HostCsr* R) {
-  int dim = fm.dim, nl = fs.nloc, p = fs.order;
+  const int dim = fm.dim, nl = fs.nloc, p = fs.order, shape = fm.shape;
   // child-local interpolation: fine dof k of cell f gets coarse basis l of
-  // parent evaluated at the fine node (nodal functionals are point values)
+  // parent evaluated at the fine node (nodal functionals are point values);
+  // the fine node is located in the parent's reference cell through the
+  // (unperturbed) geometry
   std::vector<std::unordered_map<int, double>> rows(fs.ndof);
   std::vector<int> mult(fs.ndof, 0);
   std::vector<double> val(nl);
   for (int f = 0; f < fm.ncells; ++f) {
-    int c = parent[f];
+    const int c = parent[f];
     const double* cvf = &fm.verts[(size_t)f * fm.nv * dim];
     const double* cvc = &cm.verts[(size_t)c * cm.nv * dim];
-    // inverse of the coarse affine map
-    const int e[3] = {1, 3, 4};
-    double J[3][3], Ji[3][3], x0[3];
-    for (int r = 0; r < dim; ++r)
-      for (int a = 0; a < dim; ++a) J[r][a] = 0.5 * (cvc[e[a] * dim + r] - cvc[r]);
-    for (int r = 0; r < dim; ++r) {
-      double s = cvc[r];
-      for (int a = 0; a < dim; ++a) s += J[r][a];
-      x0[r] = s;
+    // coarse affine map x = x0 + J r and its inverse
+    double J[3][3], Ji[3][3], x0[3], zero[3] = {0, 0, 0}, unit[3];
+    if (shape == kTetra) {
+      cell_point(shape, dim, cvc, zero, x0);
+    } else {
+      const double m1[3] = {-1, -1, -1};
+      cell_point(shape, dim, cvc, m1, x0);   // vertex 0 at r = (-1,-1,-1)
+    }
+    for (int a = 0; a < dim; ++a) {
+      for (int b = 0; b < 3; ++b) unit[b] = shape == kTetra ? 0.0 : -1.0;
+      unit[a] = 1.0;
+      double xa[3];
+      cell_point(shape, dim, cvc, unit, xa);
+      for (int r = 0; r < dim; ++r) J[r][a] = (xa[r] - x0[r]) / (shape == kTetra ? 1.0 : 2.0);
     }
     if (dim == 2) {
-      double det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+      const double det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
       Ji[0][0] = J[1][1] / det; Ji[0][1] = -J[0][1] / det;
       Ji[1][0] = -J[1][0] / det; Ji[1][1] = J[0][0] / det;
     } else {
-      double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
-                   J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
-                   J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+      const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+                         J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                         J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
       for (int i = 0; i < 3; ++i)
         for (int j = 0; j < 3; ++j) {
-          int i1 = (j + 1) % 3, i2 = (j + 2) % 3, j1 = (i + 1) % 3, j2 = (i + 2) % 3;
+          const int i1 = (j + 1) % 3, i2 = (j + 2) % 3, j1 = (i + 1) % 3, j2 = (i + 2) % 3;
           Ji[i][j] = (J[i1][j1] * J[i2][j2] - J[i1][j2] * J[i2][j1]) / det;
         }
     }
+    const double r0 = shape == kTetra ? 0.0 : -1.0;
     for (int k = 0; k < nl; ++k) {
       double r[3], x[3], xi[3] = {0, 0, 0};
-      local_dof_ref(dim, p, k, r);
-      affine_point(dim, cvf, r, x);
+      local_dof_ref_shape(shape, p, k, r);
+      cell_point(shape, dim, cvf, r, x);
       for (int a = 0; a < dim; ++a) {
         double t = 0;
         for (int rr = 0; rr < dim; ++rr) t += Ji[a][rr] * (x[rr] - x0[rr]);
-        xi[a] = t;
+        xi[a] = r0 + t;
       }
-      ref_basis_point(dim, p, xi, val.data(), nullptr, nullptr);
-      int fi = fs.gdof[(size_t)f * nl + k];
+      basis_at(shape, p, xi, val.data(), nullptr, nullptr);
+      const int fi = fs.gdof[(size_t)f * nl + k];
       mult[fi] += 1;
       for (int l = 0; l < nl; ++l) {
-        if (val[l] == 0.0) continue;
+        if (std::fabs(val[l]) < 1e-14) continue;
         rows[fi][cs.gdof[(size_t)c * nl + l]] += val[l];
       }
     }

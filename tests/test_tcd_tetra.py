@@ -1,0 +1,234 @@
+"""P2/P1 tetrahedra and the time-dependent problem (Crank-Nicolson).
+
+CPU tests check the oracle on its own: quadrature on tetrahedra (the mass
+matrix sums to the volume), known answers (a solution inside the FE space is
+reproduced exactly, also through Crank-Nicolson steps, which are exact for a
+solution linear in time), and the arrays constructor against the structured
+one.  GPU tests compare the CUDA path with the oracle through the C-ABI:
+matrices and rhs to 1e-12 relative, transfers to 1e-13, Crank-Nicolson
+solutions to 1e-8 relative (same iteration count +-1).
+"""
+import numpy as np
+import pytest
+
+import parmoon2022_gb300 as pg
+import pyoracle as po
+
+B_ROT = (0.5, -0.5, 0.2)                      # b(x) = (-(y-1/2), x-1/2, 0.2)
+B_ROT_GRAD = ((0.0, -1.0, 0.0), (1.0, 0.0, 0.0), (0.0, 0.0, 0.0))
+
+
+def rel(x, y):
+    return float(np.max(np.abs(x - y)) / max(np.max(np.abs(y)), 1e-300))
+
+
+def hierarchy_levels(h):
+    out = []
+    for l in range(h.n_levels):
+        rp, col = h.pattern(l)
+        i = h.info(l)
+        out.append(dict(verts=h.mesh(l), gdof=h.dofs(l), dofs=h.dofs(l), ndof=i["ndof"],
+                        nactive=i["nactive"], row_ptr=rp, col=col))
+    return out
+
+
+def tet_oracle(h, order, example, **kw):
+    cfg = po.make_config(3, order, 0, example, tetra=True, **kw)
+    return po.Problem(cfg, arrays=hierarchy_levels(h))
+
+
+def fgmres_jacobi(red=1e-12):
+    return po.make_solver("jacobi", max_it=2000, restart=50, reduction=red)
+
+
+# ---------------------------------------------------------------------------
+# oracle on its own (CPU)
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("order", [1, 2])
+def test_oracle_tet_mass_sums_to_volume(built, order):
+    h = pg.Hierarchy(3, order, 1, roots=2, tetra=True, perturb=0.2, seed=3)
+    o = tet_oracle(h, order, po.EX_POLY1)
+    o.tcd_initialize()
+    assert abs(o.tcd_matrix(1).sum() - 1.0) < 1e-12
+
+
+def test_oracle_tet_p2_reproduces_linear_solution(built):
+    # u = 1 + x + 2y + 3z lies in P2: Galerkin gives the interpolant
+    h = pg.Hierarchy(3, 2, 1, roots=2, tetra=True, perturb=0.2, seed=5)
+    o = tet_oracle(h, 2, po.EX_POLY1, eps=0.1, b=B_ROT, b_grad=B_ROT_GRAD, c=0.5)
+    o.assemble()
+    it, res, ini = o.solve(fgmres_jacobi())
+    assert res <= 1e-12 * ini
+    e = o.errors()
+    assert e[0] < 1e-10 and e[1] < 1e-9
+
+
+def test_oracle_crank_nicolson_exact_for_linear_in_time(built):
+    # u = (1+t)(1 + x + 2y + 3z): in space inside P2, linear in time, so the
+    # trapezoidal rule has no time error either
+    h = pg.Hierarchy(3, 2, 1, roots=1, tetra=True, perturb=0.15, seed=1)
+    o = tet_oracle(h, 2, po.EX_POLY1_T, eps=0.05, b=B_ROT, b_grad=B_ROT_GRAD, c=0.3)
+    o.tcd_initialize()
+    tau = 0.05
+    for k in range(1, 4):
+        it, res, ini = o.tcd_step(k * tau, tau, fgmres_jacobi())
+        assert res <= 1e-12 * max(ini, 1e-300) or res < 1e-13
+    e = o.errors()
+    assert e[0] < 1e-10 and e[1] < 1e-9
+
+
+def test_oracle_arrays_equal_structured(built):
+    cfg = po.make_config(3, 2, 2, po.EX_SINE, eps=0.1, b=(1.0, 0.3, -0.2), c=1.0)
+    o1 = po.Problem(cfg, 2)
+    levels = []
+    for l in range(2):
+        rp, col = o1.structure(l)
+        i = o1.info(l)
+        levels.append(dict(verts=o1.mesh(l), gdof=o1.gdof(l), ndof=i["ndof"],
+                           nactive=i["nactive"], row_ptr=rp, col=col))
+    o2 = po.Problem(cfg, arrays=levels)
+    o1.assemble()
+    o2.assemble()
+    for l in range(2):
+        assert np.array_equal(o1.matrix(l), o2.matrix(l))
+        assert np.array_equal(o1.rhs(l), o2.rhs(l))
+    xc = np.random.default_rng(0).standard_normal(o1.info(1)["ndof"])
+    assert np.array_equal(o1.prolongate(xc), o2.prolongate(xc))
+
+
+# ---------------------------------------------------------------------------
+# CUDA path against the oracle (GPU)
+# ---------------------------------------------------------------------------
+TET_CASES = {
+    # name: (order, nref, roots, perturb, kwargs)
+    "p2_galerkin_linear_b": (2, 1, 2, 0.2, dict(example=po.EX_SINE, eps=1e-2, b=B_ROT,
+                                                b_grad=B_ROT_GRAD, c=0.5)),
+    "p2_supg": (2, 1, 2, 0.2, dict(example=po.EX_POLYEXP, eps=1e-4, b=(0.577, 0.577, 0.577),
+                                   supg=True, sdfem_type=2, cell_measure=2)),
+    "p1_galerkin": (1, 2, 1, 0.2, dict(example=po.EX_SINE, eps=0.1, b=(1.0, 0.3, -0.2), c=1.0)),
+}
+
+
+def gpu_params(kw, t=0.0, ic=(0.5, 0.5, 0.5, 0.1)):
+    return pg.assembly_params(
+        example=kw["example"], eps=kw.get("eps", 1.0), b=kw.get("b", (0, 0, 0)),
+        c=kw.get("c", 0.0), b_grad=kw.get("b_grad"), t=t, ic=ic,
+        space_discretization_type="supg" if kw.get("supg") else "galerkin",
+        sdfem_type=kw.get("sdfem_type", 2), cell_measure=kw.get("cell_measure", 0))
+
+
+def oracle_kw(kw):
+    return {k: v for k, v in kw.items() if k != "example"}
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", list(TET_CASES))
+def test_tet_assembly_parity(ctx, name):
+    order, nref, roots, perturb, kw = TET_CASES[name]
+    h = pg.Hierarchy(3, order, nref, n_levels=2, roots=roots, tetra=True, perturb=perturb,
+                     seed=7)
+    o = tet_oracle(h, order, kw["example"], **oracle_kw(kw))
+    gpu = pg.ConvectionDiffusion(ctx, h)
+    o.assemble()
+    gpu.assemble(gpu_params(kw))
+    for l in range(2):
+        assert rel(gpu.matrix(l), o.matrix(l)) < 1e-12, l
+        assert rel(gpu.rhs(l), o.rhs(l)) < 1e-12, l
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("order", [1, 2])
+def test_tet_transfer_parity(ctx, order):
+    h = pg.Hierarchy(3, order, 2, n_levels=3, roots=1, tetra=True)
+    o = tet_oracle(h, order, po.EX_SINE)
+    gpu = pg.ConvectionDiffusion(ctx, h)
+    rng = np.random.default_rng(11)
+    for fine in range(2):
+        xc = rng.standard_normal(h.info(fine + 1)["ndof"])
+        df = rng.standard_normal(h.info(fine)["ndof"])
+        assert rel(gpu.prolongate(xc, fine), o.prolongate(xc, fine)) < 1e-13
+        assert rel(gpu.restrict(df, fine), o.restrict(df, fine)) < 1e-13
+
+
+def mg_solver(levels, precision="fp64"):
+    g = pg.solver_params("multigrid", max_n_iterations=100, gmres_restart=30,
+                         residual_tolerance=0.0, residual_reduction=1e-10,
+                         multigrid_n_levels=levels, multigrid_n_pre_smooth=2,
+                         multigrid_n_post_smooth=2, jacobi_damp=0.8, precision=precision)
+    o = po.make_solver("multigrid", max_it=100, restart=30, reduction=1e-10, mg_levels=levels,
+                       n_pre=2, n_post=2, jacobi_damp=0.8)
+    return g, o
+
+
+TCD_CASES = {
+    # name: (tetra, order, nref, levels, kwargs)
+    "p2_tet_bump": (True, 2, 2, 3, dict(example=po.EX_BUMP, eps=1e-3, b=B_ROT,
+                                        b_grad=B_ROT_GRAD)),
+    "q2_hex_sine": (False, 2, 2, 2, dict(example=po.EX_SINE, eps=1e-2, b=(1.0, 0.3, -0.2),
+                                         c=0.5)),
+}
+
+
+def tcd_pair(ctx, name):
+    tetra, order, nref, levels, kw = TCD_CASES[name]
+    ic = (0.4, 0.5, 0.6, 0.15)
+    if tetra:
+        h = pg.Hierarchy(3, order, nref, n_levels=levels, roots=1, tetra=True)
+        o = tet_oracle(h, order, kw["example"], ic=ic, **oracle_kw(kw))
+    else:
+        h = pg.Hierarchy(3, order, nref, n_levels=levels)
+        cfg = po.make_config(3, order, nref, kw["example"], ic=ic, **oracle_kw(kw))
+        o = po.Problem(cfg, levels)
+    gpu = pg.ConvectionDiffusion(ctx, h)
+    return o, gpu, levels, kw, ic
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", list(TCD_CASES))
+def test_tcd_matrices_and_steps_parity(ctx, name):
+    o, gpu, levels, kw, ic = tcd_pair(ctx, name)
+    tau = 1e-2
+    o.tcd_initialize()
+    gpu.tcd_initialize(gpu_params(kw, t=0.0, ic=ic))
+    for l in range(levels):
+        assert rel(gpu.tcd_matrix(0, l), o.tcd_matrix(0, l)) < 1e-12
+        assert rel(gpu.tcd_matrix(1, l), o.tcd_matrix(1, l)) < 1e-12
+    assert rel(gpu.solution(), o.solution()) < 1e-14
+    gs, osv = mg_solver(levels)
+    for k in range(1, 4):
+        st = gpu.tcd_step(gpu_params(kw, t=k * tau, ic=ic), tau, gs)
+        it_o, res_o, ini_o = o.tcd_step(k * tau, tau, osv)
+        assert abs(st.iterations - it_o) <= 1
+        assert rel(gpu.rhs(0), o.rhs(0)) < 1e-11
+        assert rel(gpu.solution(), o.solution()) < 1e-8
+    for l in range(levels):
+        assert rel(gpu.tcd_matrix(2, l), o.tcd_matrix(2, l)) < 1e-12
+
+
+@pytest.mark.gpu
+def test_tcd_mixed_precision_matches_fp64(ctx):
+    o, gpu, levels, kw, ic = tcd_pair(ctx, "p2_tet_bump")
+    tau = 1e-2
+    o.tcd_initialize()
+    gpu.tcd_initialize(gpu_params(kw, t=0.0, ic=ic))
+    gs, osv = mg_solver(levels, precision="mixed")
+    for k in range(1, 3):
+        st = gpu.tcd_step(gpu_params(kw, t=k * tau, ic=ic), tau, gs)
+        o.tcd_step(k * tau, tau, osv)
+        assert st.residual <= 1e-10 * st.initial_residual * 1.0001
+        assert rel(gpu.solution(), o.solution()) < 1e-7
+
+
+@pytest.mark.gpu
+def test_tcd_known_answer_on_perturbed_tets(ctx):
+    h = pg.Hierarchy(3, 2, 2, n_levels=2, roots=1, tetra=True, perturb=0.2, seed=9)
+    gpu = pg.ConvectionDiffusion(ctx, h)
+    kw = dict(example=po.EX_POLY1_T, eps=0.05, b=B_ROT, b_grad=B_ROT_GRAD, c=0.3)
+    gpu.tcd_initialize(gpu_params(kw))
+    s = pg.solver_params("jacobi", max_n_iterations=1000, gmres_restart=50,
+                         residual_tolerance=0.0, residual_reduction=1e-13)
+    tau = 0.05
+    for k in range(1, 4):
+        gpu.tcd_step(gpu_params(kw, t=k * tau), tau, s)
+    e = gpu.errors(gpu_params(kw, t=3 * tau))
+    assert e[0] < 1e-10 and e[1] < 1e-9
