@@ -12,10 +12,25 @@ same solve is measured beside it.  Synthetic data only (generated mesh and
 manufactured solution; no dataset).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+                  [--workload cd3d_q2_32|tcd3d_p2_48|cd2d_q1_64|cd3d_q2_96]
 
 --impl reference times the CPU restatement of the reference's algorithm
 (oracle/, per-quadrature-point assembly with row-search scatter, FP64
 multigrid) on all host cores, one solve per core per step.
+
+Other workloads (--workload), each printing its own JSON line:
+  tcd3d_p2_48  time-dependent CD3D on 48^3 cubes x 6 tetrahedra (Kuhn), finest
+               interior vertices perturbed by U(+-0.2h) (seed 2024), P2
+               (912,673 DOFs), eps=1e-4, b=(-(y-1/2), x-1/2, 0.2), Gaussian bump
+               sigma=0.1 at (0.3,0.5,0.5), Crank-Nicolson dt=1e-3; one step =
+               reassembly of stiffness and rhs on all 4 levels + CN rhs and
+               system + FGMRES(30) with FP32 MG V(2,2) warm-started to 1e-10.
+  cd2d_q1_64   stationary CD2D, 64x64 Q1 (4,225 DOFs), eps=1e-2, b=(1,0.5), c=1,
+               u=sin(pi x)sin(pi y), Galerkin, 3x3 Gauss, FP64 FGMRES(50)+Jacobi
+               to 1e-10.
+  cd3d_q2_96   stationary CD3D, 96^3 Q2 hexahedra (7,189,057 DOFs), eps=1e-6,
+               SUPG, b=(1,0.25,0.1), u=sin(2 pi x)sin(2 pi y)sin(2 pi z), 6-level
+               FP32 MG V(3,3) inside FP64 FGMRES(30) to 1e-10.
 """
 import argparse
 import json
@@ -319,6 +334,197 @@ def run_gpu(args):
 
 
 # ---------------------------------------------------------------------------
+# time-dependent CD3D on perturbed P2 tetrahedra (Crank-Nicolson)
+# ---------------------------------------------------------------------------
+TCD = dict(roots=6, nref=3, levels=4, perturb=0.2, seed=2024, eps=1e-4, b=(0.5, -0.5, 0.2),
+           b_grad=((0.0, -1.0, 0.0), (1.0, 0.0, 0.0), (0.0, 0.0, 0.0)),
+           ic=(0.3, 0.5, 0.5, 0.1), tau=1e-3)
+TCD_WORKLOAD = ("TCD3D 48^3x6 P2 tetrahedra perturbed 0.2h, eps=1e-4, b=(-(y-.5),x-.5,.2), "
+                "bump sigma .1 at (.3,.5,.5), CN dt=1e-3, FGMRES(30)+MG V(2,2) omega .45 4 levels "
+                "to 1e-10")
+TCD_METRIC = "TCD steps/s (reassembly + CN solve to 1e-10), mixed vs FP64; assembly GDOF/s"
+
+
+def tcd_solver_kw(levels):
+    # the Crank-Nicolson system tau/2 A + M is mass dominated; for P2
+    # tetrahedra the Jacobi-scaled spectrum reaches ~4.2, so damped Jacobi
+    # needs omega < 2/4.2: omega = 0.45 (0.8 amplifies the high modes)
+    return dict(max_n_iterations=1000, gmres_restart=30, residual_tolerance=0.0,
+                residual_reduction=1e-10, multigrid_n_levels=levels, multigrid_cycle_type="V",
+                multigrid_n_pre_smooth=2, multigrid_n_post_smooth=2, jacobi_damp=0.45,
+                multigrid_correction_damp_factor=1.0, multigrid_smoother_coarse="direct_solve")
+
+
+def tcd_params(pg, t):
+    return pg.assembly_params(example=pg.EX_BUMP, eps=TCD["eps"], b=TCD["b"],
+                              b_grad=TCD["b_grad"], t=t, ic=TCD["ic"])
+
+
+def run_gpu_tcd(args):
+    import torch
+    import parmoon2022_gb300 as pg
+    rank, world, local = dist_env()
+    dist = init_dist(world)
+    torch.cuda.set_device(local)
+    ctx = pg.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=local)
+    L = TCD["levels"]
+    hier = pg.Hierarchy(3, 2, TCD["nref"], n_levels=L, roots=TCD["roots"], tetra=True,
+                        perturb=TCD["perturb"], seed=TCD["seed"])
+    cd = pg.ConvectionDiffusion(ctx, hier)
+    info = [cd.info(l) for l in range(L)]
+    n = info[0]["ndof"]
+    tau = TCD["tau"]
+    s_mixed = pg.solver_params("multigrid", precision="mixed", **tcd_solver_kw(L))
+    s_fp64 = pg.solver_params("multigrid", precision="fp64", **tcd_solver_kw(L))
+
+    def run(s, k, w):
+        """initial condition, w untimed steps, k timed steps (event per step)"""
+        cd.tcd_initialize(tcd_params(pg, 0.0))
+        t = 0.0
+        for _ in range(w):
+            t += tau
+            cd.tcd_step(tcd_params(pg, t), tau, s)
+        barrier(dist)
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(k)]
+        l0 = ctx.launches()
+        stats = []
+        for i in range(k):
+            t += tau
+            ev[i][0].record(stream)
+            stats.append(cd.tcd_step(tcd_params(pg, t), tau, s))
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+        barrier(dist)
+        return [e0.elapsed_time(e1) for e0, e1 in ev], stats, ctx.launches() - l0, t
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    per_m, st_m, launches, t_end = run(s_mixed, args.steps, args.warmup)
+    clk = clocks.stop()
+    x_m = cd.solution()
+    per_d, st_d, _, _ = run(s_fp64, args.steps, args.warmup)
+    x_d = cd.solution()
+    # stationary assembly of the same stiffness and rhs on all levels (FP64)
+    a_end = tcd_params(pg, t_end)
+    for _ in range(2):
+        cd.assemble(a_end)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ka = 10
+    e0.record(stream)
+    for _ in range(ka):
+        cd.assemble(a_end)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    t_asm = e0.elapsed_time(e1) / ka / 1e3
+    dofs_all = sum(i["ndof"] for i in info)
+    # e2e: each step through the C-ABI with the solution read back to pinned host memory
+    import ctypes
+    sol_out = torch.empty(n, dtype=torch.float64).pin_memory()
+    dp = ctypes.POINTER(ctypes.c_double)
+    cd.tcd_initialize(tcd_params(pg, 0.0))
+    t = 0.0
+    ke = args.steps
+    for i in range(args.warmup + ke):
+        if i == args.warmup:
+            torch.cuda.synchronize()
+            te = time.perf_counter()
+        t += tau
+        a_t = tcd_params(pg, t)
+        st = pg.SolveStats()
+        pg._chk(pg.lib().cdg_problem_tcd_step(cd.p, ctypes.byref(a_t), tau, ctypes.byref(s_mixed),
+                                             ctypes.byref(st)))
+        pg._chk(pg.lib().cdg_problem_get_solution(cd.p, ctypes.cast(sol_out.data_ptr(), dp)))
+    t_e2e = max_over_ranks(dist, (time.perf_counter() - te) / ke)
+    # dominant kernels of a step
+    ms_smooth = cd.time_kernel(0, a_end, level=0, reps=50)
+    ms_spmv64 = cd.time_kernel(1, a_end, level=0, reps=50)
+    ms_contract = cd.time_kernel(2, a_end, level=0, reps=5)
+    nnz0 = info[0]["nnz"]
+    bytes_smooth = 8 * nnz0 + 4 * (n + 1) + 4 * 4 * n
+    peak, peak_kind = measured_peak_hbm()
+    achieved = bytes_smooth / (ms_smooth * 1e-3) / 1e9
+    traffic = profile_traffic("k_spmv_f32_jacobi_tcd3d_p2_48")
+    t_step_m = max_over_ranks(dist, sum(per_m) / len(per_m) / 1e3)
+    t_step_d = max_over_ranks(dist, sum(per_d) / len(per_d) / 1e3)
+    if rank != 0:
+        return
+    cpu = cpu_baseline_tcd() if not args.skip_cpu else None
+    rel = float(np.max(np.abs(x_m - x_d)) / np.max(np.abs(x_d)))
+    its = [s.iterations for s in st_m]
+    print(json.dumps({
+        "metric": TCD_METRIC, "value": world / t_step_m, "unit": "steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step_m * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 FGMRES + f32 multigrid (mixed)", "data": "synthetic",
+        "config": {"workload": TCD_WORKLOAD, "dofs": n, "nnz": nnz0,
+                   "cells": info[0]["ncells"], "levels_dofs": [i["ndof"] for i in info],
+                   "quadrature": "collapsed Gauss 5^3 (degree 6)",
+                   "l2": "working set > L2 (finest stiffness+mass+system CSR %.0f MB); no flush"
+                         % (nnz0 * 32 / 1e6),
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "p50_ms": statistics.median(per_m), "p99_ms": float(np.percentile(per_m, 99)),
+        "iterations_per_step": {"min": min(its), "max": max(its), "mean": sum(its) / len(its)},
+        "rel_residual": st_m[-1].residual / max(st_m[-1].initial_residual, 1e-300),
+        "solution_rel_diff_vs_fp64": rel,
+        "fp64": {"value": world / t_step_d, "ms_per_step": t_step_d * 1e3,
+                 "iterations_last": st_d[-1].iterations},
+        "mixed_over_fp64": t_step_d / t_step_m,
+        "assembly_gdofs": dofs_all / t_asm / 1e9, "assembly_ms": t_asm * 1e3,
+        "kernels_ms": {"jacobi_smooth_f32_L0": ms_smooth, "spmv_f64_L0": ms_spmv64,
+                       "element_contract_f64_L0": ms_contract},
+        "roofline": {"bound": "hbm", "kernel": "k_spmv<float,4,8,2> (Jacobi smoothing, finest level)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "algorithmic_bytes": bytes_smooth,
+                     "traffic": traffic},
+        "cpu_baseline": cpu,
+        "e2e": {"value": world / t_e2e, "unit": "steps/s", "h2d_bytes_per_step": 136 + 136,
+                "d2h_bytes_per_step": 8 * n + 8 * 4},
+        "clocks": clk, "gpu_launches": launches,
+    }))
+
+
+def oracle_tcd_step_time(roots, nref, levels):
+    """Seconds of one Crank-Nicolson step (reassembly + FP64 MG solve) by the
+    CPU oracle on a roots*2^nref tetrahedral mesh of the same workload."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    import parmoon2022_gb300 as pg
+    h = pg.Hierarchy(3, 2, nref, n_levels=levels, roots=roots, tetra=True,
+                     perturb=TCD["perturb"], seed=TCD["seed"])
+    arrays = []
+    for l in range(levels):
+        rp, col = h.pattern(l)
+        i = h.info(l)
+        arrays.append(dict(verts=h.mesh(l), gdof=h.dofs(l), ndof=i["ndof"],
+                           nactive=i["nactive"], row_ptr=rp, col=col))
+    cfg = po.make_config(3, 2, 0, po.EX_BUMP, eps=TCD["eps"], b=TCD["b"], b_grad=TCD["b_grad"],
+                         ic=TCD["ic"], tetra=True)
+    p = po.Problem(cfg, arrays=arrays)
+    p.tcd_initialize()
+    s = po.make_solver("multigrid", max_it=1000, restart=30, reduction=1e-10, mg_levels=levels,
+                       n_pre=2, n_post=2, jacobi_damp=0.45)
+    t0 = time.perf_counter()
+    it, _, _ = p.tcd_step(TCD["tau"], TCD["tau"], s)
+    return time.perf_counter() - t0, it, h.info(0)["ndof"]
+
+
+def cpu_baseline_tcd():
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+    po.build()
+    dt, it, nd = oracle_tcd_step_time(6, 2, 3)
+    scale = 912673 / nd
+    return {"value": 1.0 / (dt * scale), "unit": "steps/s", "cores": 1, "kind": "port",
+            "sample": "one CN step (reassembly + FP64 MG solve, %d its) of the same workload on "
+                      "24^3x6 tetrahedra (%d DOFs, %.1f s), scaled by DOFs x%.2f to 912,673 DOFs; "
+                      "C restatement of the reference, 1 thread" % (it, nd, dt, scale)}
+
+
+# ---------------------------------------------------------------------------
 def oracle_solve_once():
     """One C2 assemble + solve by the CPU oracle (reference algorithm)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -353,10 +559,16 @@ def _worker(q):
     q.put(oracle_solve_once()[0])
 
 
+def _worker_tcd(q):
+    dt, it, nd = oracle_tcd_step_time(6, 2, 3)
+    q.put(dt * 912673 / nd)
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
+    tcd = args.workload == "tcd3d_p2_48"
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import multiprocessing as mp
     import pyoracle as po
@@ -369,7 +581,8 @@ def run_reference(args):
     times = []
     for i in range(warm + steps):
         q = ctxm.Queue()
-        procs = [ctxm.Process(target=_worker, args=(q,)) for _ in range(cores)]
+        procs = [ctxm.Process(target=_worker_tcd if tcd else _worker, args=(q,))
+                 for _ in range(cores)]
         t0 = time.perf_counter()
         for pr in procs:
             pr.start()
@@ -377,9 +590,24 @@ def run_reference(args):
             pr.join()
         dt = time.perf_counter() - t0
         if i >= warm:
-            times.append(dt)
+            times.append(max(q.get() for _ in range(cores)) if tcd else dt)
     t = sum(times) / len(times)
     value = cores / t
+    if tcd:
+        print(json.dumps({
+            "metric": TCD_METRIC, "value": value, "unit": "steps/s", "n_gpus": world,
+            "steps": steps, "warmup": warm, "ms_per_step": t * 1e3 / cores,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": TCD_WORKLOAD, "dofs": 912673},
+            "cpu_baseline": {"value": value, "unit": "steps/s", "cores": cores, "kind": "port",
+                             "sample": "each step: %d concurrent CN steps (one per host core) of "
+                                       "the workload on 24^3x6 tetrahedra, each scaled by DOFs "
+                                       "to 912,673 DOFs; C restatement of the reference" % cores},
+            "e2e": {"value": value, "unit": "steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+        }))
+        return
     print(json.dumps({
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
         "steps": steps, "warmup": warm, "ms_per_step": t * 1e3, "higher_is_better": True,
@@ -401,6 +629,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU-baseline sample")
+    ap.add_argument("--workload", default="cd3d_q2_32",
+                    choices=["cd3d_q2_32", "tcd3d_p2_48", "cd2d_q1_64", "cd3d_q2_96"])
     ap.add_argument("--profile", action="store_true",
                     help="run one bracketed step for an ncu capture and exit")
     args = ap.parse_args()
@@ -408,6 +638,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "tcd3d_p2_48":
+        run_gpu_tcd(args)
     else:
         run_gpu(args)
 

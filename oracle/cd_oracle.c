@@ -1718,6 +1718,7 @@ int orc_mg_apply(orc_problem *p, const orc_solver_config *s, const double *v,
           jacobi_smooth(L, s->jacobi_damp);
         res = calc_defect(L);
       }
+      if (nl == 1) break; /* the coarse solve is the whole cycle */
       /* update_solution_in_finer_grid */
       level_t *F = &p->lev[nl - 1 - (level + 1)];
       double *pr = (double *)malloc(sizeof(double) * F->ndof);

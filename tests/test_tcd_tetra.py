@@ -77,6 +77,17 @@ def test_oracle_crank_nicolson_exact_for_linear_in_time(built):
     assert e[0] < 1e-10 and e[1] < 1e-9
 
 
+def test_oracle_crank_nicolson_multigrid_converges(built):
+    h = pg.Hierarchy(3, 2, 2, n_levels=3, roots=1, tetra=True, perturb=0.2, seed=4)
+    o = tet_oracle(h, 2, po.EX_BUMP, eps=1e-4, b=B_ROT, b_grad=B_ROT_GRAD,
+                   ic=(0.3, 0.5, 0.5, 0.1))
+    o.tcd_initialize()
+    _, s = mg_solver(3)
+    for k in range(1, 3):
+        it, res, ini = o.tcd_step(k * 1e-3, 1e-3, s)
+        assert it < 40 and res <= 1e-10 * ini
+
+
 def test_oracle_arrays_equal_structured(built):
     cfg = po.make_config(3, 2, 2, po.EX_SINE, eps=0.1, b=(1.0, 0.3, -0.2), c=1.0)
     o1 = po.Problem(cfg, 2)
@@ -150,13 +161,15 @@ def test_tet_transfer_parity(ctx, order):
         assert rel(gpu.restrict(df, fine), o.restrict(df, fine)) < 1e-13
 
 
-def mg_solver(levels, precision="fp64"):
+def mg_solver(levels, precision="fp64", damp=0.45):
+    # omega 0.45: the Jacobi-scaled Crank-Nicolson system of P2 tetrahedra has
+    # eigenvalues up to ~4.2 (mass dominated), damped Jacobi needs omega < 0.48
     g = pg.solver_params("multigrid", max_n_iterations=100, gmres_restart=30,
                          residual_tolerance=0.0, residual_reduction=1e-10,
                          multigrid_n_levels=levels, multigrid_n_pre_smooth=2,
-                         multigrid_n_post_smooth=2, jacobi_damp=0.8, precision=precision)
+                         multigrid_n_post_smooth=2, jacobi_damp=damp, precision=precision)
     o = po.make_solver("multigrid", max_it=100, restart=30, reduction=1e-10, mg_levels=levels,
-                       n_pre=2, n_post=2, jacobi_damp=0.8)
+                       n_pre=2, n_post=2, jacobi_damp=damp)
     return g, o
 
 
@@ -198,6 +211,7 @@ def test_tcd_matrices_and_steps_parity(ctx, name):
     for k in range(1, 4):
         st = gpu.tcd_step(gpu_params(kw, t=k * tau, ic=ic), tau, gs)
         it_o, res_o, ini_o = o.tcd_step(k * tau, tau, osv)
+        assert it_o < 100 and res_o <= 1e-10 * ini_o
         assert abs(st.iterations - it_o) <= 1
         assert rel(gpu.rhs(0), o.rhs(0)) < 1e-11
         assert rel(gpu.solution(), o.solution()) < 1e-8
@@ -215,6 +229,7 @@ def test_tcd_mixed_precision_matches_fp64(ctx):
     for k in range(1, 3):
         st = gpu.tcd_step(gpu_params(kw, t=k * tau, ic=ic), tau, gs)
         o.tcd_step(k * tau, tau, osv)
+        assert st.iterations < 100
         assert st.residual <= 1e-10 * st.initial_residual * 1.0001
         assert rel(gpu.solution(), o.solution()) < 1e-7
 
@@ -232,3 +247,20 @@ def test_tcd_known_answer_on_perturbed_tets(ctx):
         gpu.tcd_step(gpu_params(kw, t=k * tau), tau, s)
     e = gpu.errors(gpu_params(kw, t=3 * tau))
     assert e[0] < 1e-10 and e[1] < 1e-9
+
+
+@pytest.mark.gpu
+def test_single_level_multigrid_is_the_coarse_solve(ctx):
+    # multigrid_n_levels = 1: the cycle is the direct coarse solve on the
+    # finest level, so FGMRES converges in one iteration on both sides
+    h = pg.Hierarchy(3, 2, 1, n_levels=1, roots=1, tetra=True, perturb=0.1, seed=2)
+    kw = dict(example=po.EX_SINE, eps=0.1, b=(1.0, 0.3, -0.2), c=1.0)
+    o = tet_oracle(h, 2, kw["example"], **oracle_kw(kw))
+    gpu = pg.ConvectionDiffusion(ctx, h)
+    o.assemble()
+    gpu.assemble(gpu_params(kw))
+    gs, osv = mg_solver(1, damp=0.8)
+    st = gpu.solve(gs)
+    it_o, _, _ = o.solve(osv)
+    assert st.iterations == it_o == 1
+    assert rel(gpu.solution(), o.solution()) < 1e-10
