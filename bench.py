@@ -24,13 +24,15 @@ Other workloads (--workload), each printing its own JSON line:
                (912,673 DOFs), eps=1e-4, b=(-(y-1/2), x-1/2, 0.2), Gaussian bump
                sigma=0.1 at (0.3,0.5,0.5), Crank-Nicolson dt=1e-3; one step =
                reassembly of stiffness and rhs on all 4 levels + CN rhs and
-               system + FGMRES(30) with FP32 MG V(2,2) warm-started to 1e-10.
+               system + FGMRES(30) with FP32 MG V(2,2) (omega 0.45, 5 levels, coarse
+               3^3x6) warm-started to 1e-10.
   cd2d_q1_64   stationary CD2D, 64x64 Q1 (4,225 DOFs), eps=1e-2, b=(1,0.5), c=1,
                u=sin(pi x)sin(pi y), Galerkin, 3x3 Gauss, FP64 FGMRES(50)+Jacobi
                to 1e-10.
   cd3d_q2_96   stationary CD3D, 96^3 Q2 hexahedra (7,189,057 DOFs), eps=1e-6,
                SUPG, b=(1,0.25,0.1), u=sin(2 pi x)sin(2 pi y)sin(2 pi z), 6-level
-               FP32 MG V(3,3) inside FP64 FGMRES(30) to 1e-10.
+               FP32 MG V(3,3) (damped Jacobi omega 0.5) inside FP64 FGMRES(30)
+               to 1e-10.
 """
 import argparse
 import json
@@ -46,23 +48,55 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-N_CELLS_1D = 32            # 32^3 hexahedra = unit cube refined 5 times
-NREF, LEVELS, ORDER, DIM = 5, 4, 2, 3
-EPS, B, C = 1e-3, (1 / np.sqrt(3.0),) * 3, 0.0
-WORKLOAD = "CD3D 32^3 Q2 SUPG eps=1e-3 b=(1,1,1)/sqrt3 c=0, FGMRES(30)+MG V(2,2) 4 levels to 1e-10"
 METRIC = "CD solves/s, p50/p99 latency, mixed vs FP64 GPU at 1e-10 res; assembly GDOF/s"
 
+# stationary workloads: mesh, problem data, solver (the reference's database keys)
+STATIONARY = {
+    "cd3d_q2_32": dict(
+        workload="CD3D 32^3 Q2 SUPG eps=1e-3 b=(1,1,1)/sqrt3 c=0, FGMRES(30)+MG V(2,2) 4 levels "
+                 "to 1e-10",
+        dim=3, order=2, roots=1, nref=5, levels=4, example="POLYEXP", freq=1.0, eps=1e-3,
+        b=(1 / np.sqrt(3.0),) * 3, c=0.0, supg=True, sdfem_type=5, delta0=1.0, cell_measure=2,
+        problem_linear=1, quadrature="3x3x3 Gauss", sdfem="type 5, delta=h/(2|b|), h=edge length",
+        precond="multigrid", restart=30, n_pre=2, n_post=2, damp=0.8, precisions=("mixed", "fp64"),
+        cpu_sample=None, profile_tag="k_spmv_f32_jacobi_q2_32"),
+    "cd2d_q1_64": dict(
+        workload="CD2D 64^2 Q1 Galerkin eps=1e-2 b=(1,.5) c=1 u=sin(pi x)sin(pi y), "
+                 "FGMRES(50)+Jacobi FP64 to 1e-10",
+        dim=2, order=1, roots=1, nref=6, levels=1, example="SINE", freq=1.0, eps=1e-2,
+        b=(1.0, 0.5), c=1.0, supg=False, sdfem_type=2, delta0=1.0, cell_measure=0,
+        problem_linear=0, quadrature="Gauss rule of degree 3 (reference map)", sdfem="none",
+        precond="jacobi", restart=50, n_pre=0, n_post=0, damp=1.0, precisions=("fp64",),
+        cpu_sample=None, profile_tag="k_spmv_f64_cd2d_q1_64"),
+    "cd3d_q2_96": dict(
+        workload="CD3D 96^3 Q2 SUPG eps=1e-6 b=(1,.25,.1) c=0 u=sin(2pi x)sin(2pi y)sin(2pi z), "
+                 "FGMRES(30)+MG V(3,3) omega .5 6 levels to 1e-10",
+        dim=3, order=2, roots=3, nref=5, levels=6, example="SINE", freq=2.0, eps=1e-6,
+        b=(1.0, 0.25, 0.1), c=0.0, supg=True, sdfem_type=5, delta0=1.0, cell_measure=2,
+        problem_linear=1, quadrature="3x3x3 Gauss", sdfem="type 5, delta=h/(2|b|), h=edge length",
+        # omega 0.5: with 0.8 the Jacobi smoother amplifies high modes of this
+        # convection-dominated Q2 SUPG operator and FGMRES stagnates
+        precond="multigrid", restart=30, n_pre=3, n_post=3, damp=0.5, precisions=("mixed", "fp64"),
+        cpu_sample=dict(roots=3, nref=3, levels=4), profile_tag="k_spmv_f32_jacobi_q2_96"),
+}
 
-def assembly_kw():
-    return dict(eps=EPS, b=B, c=C, supg=True, sdfem_type=5, delta0=1.0, cell_measure=2,
-                problem_linear=1)
+
+def spec_assembly(pg, w):
+    return pg.assembly_params(
+        example=getattr(pg, "EX_" + w["example"]), eps=w["eps"], b=w["b"], c=w["c"],
+        freq=w["freq"], space_discretization_type="supg" if w["supg"] else "galerkin",
+        sdfem_type=w["sdfem_type"], delta0=w["delta0"], cell_measure=w["cell_measure"],
+        problem_linear=w["problem_linear"])
 
 
-def solver_kw():
-    return dict(max_n_iterations=1000, gmres_restart=30, residual_tolerance=0.0,
-                residual_reduction=1e-10, multigrid_n_levels=LEVELS, multigrid_cycle_type="V",
-                multigrid_n_pre_smooth=2, multigrid_n_post_smooth=2, jacobi_damp=0.8,
-                multigrid_correction_damp_factor=1.0, multigrid_smoother_coarse="direct_solve")
+def spec_solver(pg, w, precision, levels=None):
+    return pg.solver_params(
+        w["precond"], precision=precision, max_n_iterations=5000, gmres_restart=w["restart"],
+        residual_tolerance=0.0, residual_reduction=1e-10,
+        multigrid_n_levels=levels or w["levels"], multigrid_cycle_type="V",
+        multigrid_n_pre_smooth=w["n_pre"], multigrid_n_post_smooth=w["n_post"],
+        jacobi_damp=w["damp"], multigrid_correction_damp_factor=1.0,
+        multigrid_smoother_coarse="direct_solve")
 
 
 # ---------------------------------------------------------------------------
@@ -177,17 +211,19 @@ def profile_traffic(kernel_tag):
 def run_gpu(args):
     import torch
     import parmoon2022_gb300 as pg
+    w = STATIONARY[args.workload]
     rank, world, local = dist_env()
     dist = init_dist(world)
     torch.cuda.set_device(local)
     ctx = pg.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream(), device=local)
-    hier = pg.Hierarchy(DIM, ORDER, NREF, n_levels=LEVELS)
+    LEVELS = w["levels"]
+    hier = pg.Hierarchy(w["dim"], w["order"], w["nref"], n_levels=LEVELS, roots=w["roots"])
     cd = pg.ConvectionDiffusion(ctx, hier)
-    a = pg.assembly_params(example=pg.EX_POLYEXP, space_discretization_type="supg",
-                           **{k: v for k, v in assembly_kw().items() if k != "supg"})
-    s_mixed = pg.solver_params("multigrid", precision="mixed", **solver_kw())
-    s_fp64 = pg.solver_params("multigrid", precision="fp64", **solver_kw())
+    a = spec_assembly(pg, w)
+    precs = w["precisions"]
+    s_main = spec_solver(pg, w, precs[0])
+    s_fp64 = spec_solver(pg, w, "fp64")
     info = [cd.info(l) for l in range(LEVELS)]
     n = info[0]["ndof"]
 
@@ -196,52 +232,50 @@ def run_gpu(args):
         cd.assemble(a)
         return cd.solve(s)
 
-    def timed(s, k, w):
-        for _ in range(w):
+    def timed(s, k, w_):
+        for _ in range(w_):
             step(s)
         barrier(dist)
         torch.cuda.synchronize()
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
               for _ in range(k)]
         l0 = ctx.launches()
-        t0 = time.perf_counter()
         stats = []
         for i in range(k):
             ev[i][0].record(stream)
             stats.append(step(s))
             ev[i][1].record(stream)
         torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
         barrier(dist)
-        per = [e0.elapsed_time(e1) for e0, e1 in ev]
-        return per, stats, ctx.launches() - l0, wall
+        return [e0.elapsed_time(e1) for e0, e1 in ev], stats, ctx.launches() - l0
 
-    zero = np.zeros(n)
-    cd.set_solution(zero)
+    cd.set_solution(np.zeros(n))
     if args.profile:
-        # one mixed step between cudaProfilerStart/Stop (ncu --profile-from-start off)
+        # one step between cudaProfilerStart/Stop (ncu --profile-from-start off)
         for _ in range(2):
-            step(s_mixed)
+            step(s_main)
         torch.cuda.synchronize()
         torch.cuda.profiler.start()
         l0 = ctx.launches()
-        st = step(s_mixed)
+        st = step(s_main)
         torch.cuda.synchronize()
         torch.cuda.profiler.stop()
         print(json.dumps({"profile_step": True, "launches": ctx.launches() - l0,
                           "iterations": st.iterations}))
         return
-    # headline: mixed precision, inputs resident in HBM
+    # headline: inputs resident in HBM
     clocks = ClockSampler(local)
     clocks.start()
-    per_m, st_m, launches, wall_m = timed(s_mixed, args.steps, args.warmup)
+    per_m, st_m, launches = timed(s_main, args.steps, args.warmup)
     clk = clocks.stop()
     err_m = cd.errors(a)
     x_m = cd.solution()
-    # side by side: all-FP64 GPU solve of the same problem
-    per_d, st_d, _, _ = timed(s_fp64, max(2, min(args.steps, 5)), 1)
-    err_d = cd.errors(a)
-    x_d = cd.solution()
+    fp64_side = len(precs) > 1
+    if fp64_side:
+        # side by side: all-FP64 GPU solve of the same problem
+        per_d, st_d, _ = timed(s_fp64, max(2, min(args.steps, 5)), 1)
+        err_d = cd.errors(a)
+        x_d = cd.solution()
     # assembly only (all levels, FP64)
     for _ in range(2):
         cd.assemble(a)
@@ -265,7 +299,7 @@ def run_gpu(args):
     def e2e_step():
         st = pg.SolveStats()
         pg._chk(pg.lib().cdg_problem_assemble_solve(
-            cd.p, ctypes.byref(a), ctypes.byref(s_mixed),
+            cd.p, ctypes.byref(a), ctypes.byref(s_main),
             ctypes.cast(sol_in.data_ptr(), dp), nul, ctypes.cast(sol_out.data_ptr(), dp),
             ctypes.byref(st)))
         return st
@@ -278,7 +312,8 @@ def run_gpu(args):
         e2e_step()
     torch.cuda.synchronize()
     t_e2e = max_over_ranks(dist, (time.perf_counter() - te) / args.steps)
-    # dominant kernel: the FP32 Jacobi smoothing SpMV of the finest level
+    # dominant kernel: the FP32 Jacobi smoothing SpMV of the finest level (MG),
+    # the FP64 operator SpMV (Jacobi-preconditioned FGMRES)
     ms_smooth = cd.time_kernel(0, a, level=0, reps=50)
     ms_spmv64 = cd.time_kernel(1, a, level=0, reps=50)
     ms_contract = cd.time_kernel(2, a, level=0, reps=5)
@@ -286,43 +321,50 @@ def run_gpu(args):
     bytes_smooth = 8 * nnz0 + 4 * (n + 1) + 4 * 4 * n          # val+col, row_ptr, x,b,invd,y
     bytes_spmv64 = 12 * nnz0 + 4 * (n + 1) + 8 * 2 * n
     peak, peak_kind = measured_peak_hbm()
-    achieved = bytes_smooth / (ms_smooth * 1e-3) / 1e9
-    traffic = profile_traffic("k_spmv_f32_jacobi_q2_32")
+    mg = w["precond"] == "multigrid"
+    if mg:
+        rl_kernel = "k_spmv<float,%d,8,2> (Jacobi smoothing, finest level)" % (
+            8 if nnz0 / n > 32 else 4)
+        achieved = bytes_smooth / (ms_smooth * 1e-3) / 1e9
+        rl_bytes = bytes_smooth
+    else:
+        rl_kernel = "k_spmv<double,...,0> (FP64 operator, finest level)"
+        achieved = bytes_spmv64 / (ms_spmv64 * 1e-3) / 1e9
+        rl_bytes = bytes_spmv64
+    traffic = profile_traffic(w["profile_tag"])
 
     t_step_m = max_over_ranks(dist, sum(per_m) / len(per_m) / 1e3)
-    t_step_d = max_over_ranks(dist, sum(per_d) / len(per_d) / 1e3)
+    if fp64_side:
+        t_step_d = max_over_ranks(dist, sum(per_d) / len(per_d) / 1e3)
     value = world / t_step_m
     if rank != 0:
         return
-    cpu = cpu_baseline_sample() if not args.skip_cpu else None
-    rel = float(np.max(np.abs(x_m - x_d)) / np.max(np.abs(x_d)))
+    cpu = cpu_baseline_sample(args.workload) if not args.skip_cpu else None
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step_m * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64 FGMRES + f32 multigrid (mixed)", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "dofs": n, "nnz": nnz0,
-                   "levels_dofs": [i["ndof"] for i in info], "quadrature": "3x3x3 Gauss",
-                   "sdfem": "type 5, delta=h/(2|b|), h=edge length",
-                   "l2": "working set > L2 (finest CSR alone %.0f MB); no flush" % (nnz0 * 16 / 1e6),
+        "dtype": "f64 FGMRES + f32 multigrid (mixed)" if precs[0] == "mixed" else "f64",
+        "data": "synthetic",
+        "config": {"workload": w["workload"], "dofs": n, "nnz": nnz0,
+                   "levels_dofs": [i["ndof"] for i in info], "quadrature": w["quadrature"],
+                   "sdfem": w["sdfem"],
+                   "l2": ("working set > L2 (finest CSR alone %.0f MB); no flush"
+                          % (nnz0 * 16 / 1e6)) if nnz0 * 16 > 129e6 else
+                         "working set fits in L2 (%.1f MB); no flush, latency-bound"
+                         % (nnz0 * 16 / 1e6),
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "p50_ms": statistics.median(per_m), "p99_ms": float(np.percentile(per_m, 99)),
         "iterations": st_m[-1].iterations,
         "rel_residual": st_m[-1].residual / st_m[-1].initial_residual,
-        "errors": {"L2": err_m[0], "H1_semi": err_m[1], "L2_fp64": err_d[0],
-                   "H1_semi_fp64": err_d[1], "solution_rel_diff_vs_fp64": rel},
-        "fp64": {"value": world / t_step_d, "ms_per_step": t_step_d * 1e3,
-                 "iterations": st_d[-1].iterations},
-        "mixed_over_fp64": t_step_d / t_step_m,
+        "errors": {"L2": err_m[0], "H1_semi": err_m[1]},
         "assembly_gdofs": dofs_all / t_asm / 1e9,
         "assembly_ms": t_asm * 1e3,
         "kernels_ms": {"jacobi_smooth_f32_L0": ms_smooth, "spmv_f64_L0": ms_spmv64,
                        "element_contract_f64_L0": ms_contract},
-        "roofline": {"bound": "hbm", "kernel": "k_spmv<float,8,8,2> (Jacobi smoothing, finest level)",
-                     "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_kind": peak_kind,
-                     "algorithmic_bytes": bytes_smooth,
-                     "traffic": traffic},
+        "roofline": {"bound": "hbm", "kernel": rl_kernel, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                     "algorithmic_bytes": rl_bytes, "traffic": traffic},
         "cpu_baseline": cpu,
         "e2e": {"value": world / t_e2e, "unit": "solves/s",
                 "h2d_bytes_per_step": 8 * n + 2 * 136,
@@ -330,17 +372,24 @@ def run_gpu(args):
         "clocks": clk,
         "gpu_launches": launches,
     }
+    if fp64_side:
+        rel = float(np.max(np.abs(x_m - x_d)) / np.max(np.abs(x_d)))
+        line["errors"].update({"L2_fp64": err_d[0], "H1_semi_fp64": err_d[1],
+                               "solution_rel_diff_vs_fp64": rel})
+        line["fp64"] = {"value": world / t_step_d, "ms_per_step": t_step_d * 1e3,
+                        "iterations": st_d[-1].iterations}
+        line["mixed_over_fp64"] = t_step_d / t_step_m
     print(json.dumps(line))
 
 
 # ---------------------------------------------------------------------------
 # time-dependent CD3D on perturbed P2 tetrahedra (Crank-Nicolson)
 # ---------------------------------------------------------------------------
-TCD = dict(roots=6, nref=3, levels=4, perturb=0.2, seed=2024, eps=1e-4, b=(0.5, -0.5, 0.2),
+TCD = dict(roots=3, nref=4, levels=5, perturb=0.2, seed=2024, eps=1e-4, b=(0.5, -0.5, 0.2),
            b_grad=((0.0, -1.0, 0.0), (1.0, 0.0, 0.0), (0.0, 0.0, 0.0)),
            ic=(0.3, 0.5, 0.5, 0.1), tau=1e-3)
 TCD_WORKLOAD = ("TCD3D 48^3x6 P2 tetrahedra perturbed 0.2h, eps=1e-4, b=(-(y-.5),x-.5,.2), "
-                "bump sigma .1 at (.3,.5,.5), CN dt=1e-3, FGMRES(30)+MG V(2,2) omega .45 4 levels "
+                "bump sigma .1 at (.3,.5,.5), CN dt=1e-3, FGMRES(30)+MG V(2,2) omega .45 5 levels "
                 "to 1e-10")
 TCD_METRIC = "TCD steps/s (reassembly + CN solve to 1e-10), mixed vs FP64; assembly GDOF/s"
 
@@ -368,8 +417,9 @@ def run_gpu_tcd(args):
     torch.cuda.set_device(local)
     ctx = pg.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream(), device=local)
-    L = TCD["levels"]
-    hier = pg.Hierarchy(3, 2, TCD["nref"], n_levels=L, roots=TCD["roots"], tetra=True,
+    L = TCD["levels"] - (1 if args.small else 0)
+    nref = TCD["nref"] - (1 if args.small else 0)
+    hier = pg.Hierarchy(3, 2, nref, n_levels=L, roots=TCD["roots"], tetra=True,
                         perturb=TCD["perturb"], seed=TCD["seed"])
     cd = pg.ConvectionDiffusion(ctx, hier)
     info = [cd.info(l) for l in range(L)]
@@ -400,6 +450,18 @@ def run_gpu_tcd(args):
         barrier(dist)
         return [e0.elapsed_time(e1) for e0, e1 in ev], stats, ctx.launches() - l0, t
 
+    if args.profile:
+        # one mixed step between cudaProfilerStart/Stop (ncu --profile-from-start off)
+        run(s_mixed, 1, 2)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        l0 = ctx.launches()
+        st = cd.tcd_step(tcd_params(pg, 4 * tau), tau, s_mixed)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
+        print(json.dumps({"profile_step": True, "launches": ctx.launches() - l0,
+                          "iterations": st.iterations}))
+        return
     clocks = ClockSampler(local)
     clocks.start()
     per_m, st_m, launches, t_end = run(s_mixed, args.steps, args.warmup)
@@ -516,7 +578,7 @@ def cpu_baseline_tcd():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as po
     po.build()
-    dt, it, nd = oracle_tcd_step_time(6, 2, 3)
+    dt, it, nd = oracle_tcd_step_time(3, 3, 4)
     scale = 912673 / nd
     return {"value": 1.0 / (dt * scale), "unit": "steps/s", "cores": 1, "kind": "port",
             "sample": "one CN step (reassembly + FP64 MG solve, %d its) of the same workload on "
@@ -525,42 +587,77 @@ def cpu_baseline_tcd():
 
 
 # ---------------------------------------------------------------------------
-def oracle_solve_once():
-    """One C2 assemble + solve by the CPU oracle (reference algorithm)."""
+def oracle_solve_once(name, sample=None):
+    """One assemble + solve of a stationary workload by the CPU oracle
+    (reference algorithm); sample: smaller mesh (roots, nref, levels)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as po
-    kw = assembly_kw()
-    cfg = po.make_config(DIM, ORDER, NREF, po.EX_POLYEXP, eps=kw["eps"], b=kw["b"], c=kw["c"],
-                         supg=True, sdfem_type=kw["sdfem_type"], delta0=kw["delta0"],
-                         cell_measure=kw["cell_measure"], problem_linear=kw["problem_linear"])
-    p = po.Problem(cfg, LEVELS)
+    w = STATIONARY[name]
+    roots, nref, levels = (w["roots"], w["nref"], w["levels"]) if sample is None else (
+        sample["roots"], sample["nref"], sample["levels"])
+    kw = dict(eps=w["eps"], b=w["b"], c=w["c"], freq=w["freq"], supg=w["supg"],
+              sdfem_type=w["sdfem_type"], delta0=w["delta0"], cell_measure=w["cell_measure"],
+              problem_linear=w["problem_linear"])
+    ex = getattr(po, "EX_" + w["example"])
+    if roots == 1:
+        cfg = po.make_config(w["dim"], w["order"], nref, ex, **kw)
+        p = po.Problem(cfg, levels)
+    else:
+        import parmoon2022_gb300 as pg
+        h = pg.Hierarchy(w["dim"], w["order"], nref, n_levels=levels, roots=roots)
+        arrays = []
+        for l in range(levels):
+            rp, col = h.pattern(l)
+            i = h.info(l)
+            arrays.append(dict(verts=h.mesh(l), gdof=h.dofs(l), ndof=i["ndof"],
+                               nactive=i["nactive"], row_ptr=rp, col=col))
+        cfg = po.make_config(w["dim"], w["order"], 0, ex, **kw)
+        p = po.Problem(cfg, arrays=arrays)
+    ndof = p.info(0)["ndof"]
     t0 = time.perf_counter()
     p.assemble()
     t1 = time.perf_counter()
-    it, res, ini = p.solve(po.make_solver("multigrid", max_it=1000, restart=30, tol_abs=0.0,
-                                          reduction=1e-10, mg_levels=LEVELS, mg_cycle="V",
-                                          n_pre=2, n_post=2, jacobi_damp=0.8,
-                                          correction_damp=1.0, coarse_direct=True))
+    it, res, ini = p.solve(po.make_solver(w["precond"], max_it=5000, restart=w["restart"],
+                                          tol_abs=0.0, reduction=1e-10, mg_levels=levels,
+                                          mg_cycle="V", n_pre=w["n_pre"], n_post=w["n_post"],
+                                          jacobi_damp=w["damp"], correction_damp=1.0,
+                                          coarse_direct=True))
     t2 = time.perf_counter()
-    return t2 - t0, t1 - t0, it
+    return t2 - t0, t1 - t0, it, ndof
 
 
-def cpu_baseline_sample():
+def full_ndof(name):
+    w = STATIONARY[name]
+    n1 = w["roots"] * 2 ** w["nref"] * w["order"] + 1
+    return n1 ** w["dim"]
+
+
+def cpu_baseline_sample(name):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as po
     po.build()
-    t, t_asm, it = oracle_solve_once()
-    return {"value": 1.0 / t, "unit": "solves/s", "cores": 1, "kind": "port",
-            "sample": "one full solve (assemble 4 levels %.1f s + FGMRES/MG %d its) of the same "
-                      "workload by the C restatement of the reference, 1 thread" % (t_asm, it)}
+    w = STATIONARY[name]
+    t, t_asm, it, nd = oracle_solve_once(name, w["cpu_sample"])
+    scale = full_ndof(name) / nd
+    if w["cpu_sample"] is None:
+        sample = ("one full solve (assemble %d levels %.1f s + FGMRES %d its) of the same "
+                  "workload by the C restatement of the reference, 1 thread" % (w["levels"], t_asm, it))
+    else:
+        sample = ("one solve (assemble + FGMRES %d its, %.1f s) of the same problem on %d DOFs, "
+                  "scaled by DOFs x%.1f to the full size; C restatement of the reference, 1 thread"
+                  % (it, t, nd, scale))
+    return {"value": 1.0 / (t * scale), "unit": "solves/s", "cores": 1, "kind": "port",
+            "sample": sample}
 
 
-def _worker(q):
-    q.put(oracle_solve_once()[0])
+def _worker(q, name):
+    w = STATIONARY[name]
+    t, _, _, nd = oracle_solve_once(name, w["cpu_sample"])
+    q.put(t * full_ndof(name) / nd)
 
 
 def _worker_tcd(q):
-    dt, it, nd = oracle_tcd_step_time(6, 2, 3)
+    dt, it, nd = oracle_tcd_step_time(3, 3, 4)
     q.put(dt * 912673 / nd)
 
 
@@ -581,8 +678,8 @@ def run_reference(args):
     times = []
     for i in range(warm + steps):
         q = ctxm.Queue()
-        procs = [ctxm.Process(target=_worker_tcd if tcd else _worker, args=(q,))
-                 for _ in range(cores)]
+        procs = [ctxm.Process(target=_worker_tcd, args=(q,)) if tcd else
+                 ctxm.Process(target=_worker, args=(q, args.workload)) for _ in range(cores)]
         t0 = time.perf_counter()
         for pr in procs:
             pr.start()
@@ -590,7 +687,7 @@ def run_reference(args):
             pr.join()
         dt = time.perf_counter() - t0
         if i >= warm:
-            times.append(max(q.get() for _ in range(cores)) if tcd else dt)
+            times.append(max(q.get() for _ in range(cores)))
     t = sum(times) / len(times)
     value = cores / t
     if tcd:
@@ -613,10 +710,14 @@ def run_reference(args):
         "steps": steps, "warmup": warm, "ms_per_step": t * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "impl": "reference",
-        "config": {"workload": WORKLOAD, "dofs": 274625},
+        "config": {"workload": STATIONARY[args.workload]["workload"],
+                   "dofs": full_ndof(args.workload)},
         "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
-                         "sample": "each step: %d concurrent full solves (one per host core) by "
-                                   "the C restatement of the reference; steps capped at 3" % cores},
+                         "sample": "each step: %d concurrent solves (one per host core) by the C "
+                                   "restatement of the reference%s; steps capped at 3" % (
+                                       cores, "" if STATIONARY[args.workload]["cpu_sample"] is None
+                                       else " on a smaller mesh, each scaled by DOFs to the "
+                                            "full size")},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }))
@@ -633,6 +734,8 @@ def main():
                     choices=["cd3d_q2_32", "tcd3d_p2_48", "cd2d_q1_64", "cd3d_q2_96"])
     ap.add_argument("--profile", action="store_true",
                     help="run one bracketed step for an ncu capture and exit")
+    ap.add_argument("--small", action="store_true",
+                    help="with --profile: the 24^3x6 tetrahedral mesh (for detailed captures)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3

@@ -194,6 +194,31 @@ __device__ void invert_J(int dim, Affine& A) {
   }
 }
 
+// x0, J and det only (no inverse): what the Galerkin rhs needs
+__device__ void cell_geom_s(int shape, int dim, const double* __restrict__ cv, Affine& A) {
+  if (shape == kTetra) {
+    for (int r = 0; r < 3; ++r) {
+      A.x0[r] = cv[r];
+      for (int a = 0; a < 3; ++a) A.J[r][a] = cv[(a + 1) * 3 + r] - cv[r];
+    }
+  } else {
+    const int e[3] = {1, 3, 4};
+    for (int r = 0; r < dim; ++r)
+      for (int a = 0; a < dim; ++a) A.J[r][a] = (cv[e[a] * dim + r] - cv[r]) * 0.5;
+    for (int r = 0; r < dim; ++r) {
+      double s = cv[r];
+      for (int a = 0; a < dim; ++a) s += A.J[r][a];
+      A.x0[r] = s;
+    }
+  }
+  if (dim == 2)
+    A.det = A.J[0][0] * A.J[1][1] - A.J[0][1] * A.J[1][0];
+  else
+    A.det = A.J[0][0] * (A.J[1][1] * A.J[2][2] - A.J[1][2] * A.J[2][1]) -
+            A.J[0][1] * (A.J[1][0] * A.J[2][2] - A.J[1][2] * A.J[2][0]) +
+            A.J[0][2] * (A.J[1][0] * A.J[2][1] - A.J[1][1] * A.J[2][0]);
+}
+
 __device__ void cell_affine_s(int shape, int dim, const double* __restrict__ cv, Affine& A) {
   if (shape == kTetra) {
     for (int r = 0; r < 3; ++r) {
@@ -588,52 +613,73 @@ __device__ int boundary_comp_d(int dim, const double* x) {
 template <int DIM>
 __global__ void __launch_bounds__(256)
 k_rhs(AsmCoefs k, int ncells, int nactive, const double* __restrict__ verts,
-      const int* __restrict__ gdof, RhsTables tb, double* __restrict__ rhs) {
+      const int* __restrict__ gdof, RhsTables tb, double* __restrict__ rhs,
+      double* __restrict__ loc) {
   const int NV = k.shape == kHexa ? 8 : 4;
   __shared__ double fw[8][128];
+  __shared__ double part[8][32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int cell = blockIdx.x * 8 + warp;
   if (cell >= ncells) return;
   const double* cv = verts + (size_t)cell * NV * DIM;
+  // the FP64 pipe is scarce: the inverse Jacobian only where SUPG or the
+  // Neumann integrals need it
+  const bool need_inv = k.supg || (DIM == 2 && k.neumann_mask);
   Affine A;
-  cell_affine_s(k.shape, DIM, cv, A);
+  if (need_inv)
+    cell_affine_s(k.shape, DIM, cv, A);
+  else
+    cell_geom_s(k.shape, DIM, cv, A);
   const double adet = fabs(A.det);
-  const double delta = cell_delta(k, cv, A);
+  const double delta = k.supg ? cell_delta(k, cv, A) : 0.0;
   double bp[3] = {0, 0, 0};
-  for (int a = 0; a < DIM; ++a)
-    for (int r = 0; r < DIM; ++r) bp[a] += A.Ji[a][r] * k.b[r];
-  for (int q = lane; q < k.nqp; q += 32) {
-    double x[3];
-    for (int r = 0; r < DIM; ++r) {
-      double s = A.x0[r];
-      for (int a = 0; a < DIM; ++a) s += A.J[r][a] * tb.xi[q * 3 + a];
-      x[r] = s;
+  if (delta != 0.0)
+    for (int a = 0; a < DIM; ++a)
+      for (int r = 0; r < DIM; ++r) bp[a] += A.Ji[a][r] * k.b[r];
+  const int nl = k.nloc;
+  const int ng = 32 / nl;
+  // an identically zero source (CDG_EX_BUMP) has a zero volume integral: the
+  // quadrature would add exact zeros, so it is not run (same bits)
+  if (k.example != CDG_EX_BUMP) {
+    for (int q = lane; q < k.nqp; q += 32) {
+      double x[3];
+      for (int r = 0; r < DIM; ++r) {
+        double s = A.x0[r];
+        for (int a = 0; a < DIM; ++a) s += A.J[r][a] * tb.xi[q * 3 + a];
+        x[r] = s;
+      }
+      fw[warp][q] = tb.w[q] * adet * ex_source(k, x);
     }
-    fw[warp][q] = tb.w[q] * adet * ex_source(k, x);
+    __syncwarp();
+    // lanes = (basis function i, quadrature group g): 32 / nloc groups split
+    // the quadrature points, partial sums meet in shared memory
+    const int i = lane % nl, g = lane / nl;
+    double F = 0.0;
+    if (g < ng) {
+      if (delta == 0.0) {
+        // Galerkin: w f phi_i
+        for (int q = g; q < k.nqp; q += ng) F = fma(fw[warp][q], tb.val[q * nl + i], F);
+      } else {
+        // SUPG: w f (phi_i + delta b.grad phi_i)
+        for (int q = g; q < k.nqp; q += ng) {
+          double bg = 0.0;
+          for (int a = 0; a < DIM; ++a) bg += bp[a] * tb.grad[(q * DIM + a) * nl + i];
+          F = fma(fw[warp][q], fma(delta, bg, tb.val[q * nl + i]), F);
+        }
+      }
+    }
+    part[warp][lane] = F;
+  } else {
+    part[warp][lane] = 0.0;
   }
   __syncwarp();
-  const int nl = k.nloc;
   if (lane < nl) {
     double F = 0.0;
-    for (int q = 0; q < k.nqp; ++q) {
-      double v = tb.val[q * nl + lane];
-      // Galerkin: w f phi_i ; SUPG: w delta f (b.grad phi_i)
-      F += fw[warp][q] * v;
-    }
-    if (delta != 0.0) {
-      double Fs = 0.0;
-      for (int q = 0; q < k.nqp; ++q) {
-        double bg = 0.0;
-        for (int a = 0; a < DIM; ++a) bg += bp[a] * tb.grad[(q * DIM + a) * nl + lane];
-        Fs += fw[warp][q] * (delta * bg);
-      }
-      F += Fs;
-    }
+    for (int g = 0; g < ng; ++g) F += part[warp][g * nl + lane];
     int row = gdof[(size_t)cell * nl + lane];
-    if (row < nactive) {
-      atomicAdd(rhs + row, F);
-    } else {
-      // Dirichlet value: nodal functional of Lagrange elements = value at the node
+    if (row >= nactive) {
+      // Dirichlet value: nodal functional of Lagrange elements = value at the
+      // node (every cell sharing the node writes the same value)
       double r[3], x[3], u[6];
       ref_node_s(k.shape, DIM, k.order, lane, r);
       for (int rr = 0; rr < DIM; ++rr) {
@@ -643,6 +689,7 @@ k_rhs(AsmCoefs k, int ncells, int nactive, const double* __restrict__ verts,
       }
       ex_exact(k, x, u);
       rhs[row] = u[0];
+      return;
     }
     // Neumann data on boundary edges (Assemble2D.C:3210-3248), 2D only
     if (DIM == 2 && k.neumann_mask) {
@@ -653,7 +700,6 @@ k_rhs(AsmCoefs k, int ncells, int nactive, const double* __restrict__ verts,
         double ctr[2] = {0.5 * (a0[0] + a1[0]), 0.5 * (a0[1] + a1[1])};
         int comp = boundary_comp_d(2, ctr);
         if (comp < 0 || !((k.neumann_mask >> comp) & 1)) continue;
-        if (row >= nactive) continue;
         int np = k.order + 1;   // line rule of degree 2p
         double lx[3], lw[3];
         if (np == 2) {
@@ -680,9 +726,27 @@ k_rhs(AsmCoefs k, int ncells, int nactive, const double* __restrict__ verts,
           int n1 = k.order + 1;
           G += gval * hE * lw[l] * (v0[lane % n1] * v1[lane / n1]);
         }
-        atomicAdd(rhs + row, G);
+        F += G;
       }
     }
+    // local rhs entry; the rows gather them in cell order (no atomics: the
+    // cells around a vertex follow one another, same-address atomics would
+    // serialise)
+    loc[(size_t)cell * nl + lane] = F;
+  }
+}
+
+// rhs of the active rows: sum of the local entries of the row's DOF in
+// (cell, local DOF) order -- the scatter of Assemble3D.C:257-292, reordered
+// as a gather, deterministic
+__global__ void k_rhs_gather(int nactive, const int* __restrict__ dof_rp,
+                             const int* __restrict__ dof_ent, const double* __restrict__ loc,
+                             double* __restrict__ rhs) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nactive; r += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    const int e = dof_rp[r + 1];
+    for (int q = dof_rp[r]; q < e; ++q) s += loc[__ldg(dof_ent + q)];
+    rhs[r] = s;
   }
 }
 
@@ -885,6 +949,25 @@ int upload_level(cdg_context* ctx, DevLevel& L) {
     }
     CDG_CUDA(cudaStreamSynchronize(st));   // host vectors go out of scope
   }
+  {
+    // active DOF -> local entries (cell * nloc + i) in increasing order
+    std::vector<int> rp(L.nactive + 1, 0);
+    const std::vector<int>& g = L.space.gdof;
+    for (size_t e = 0; e < g.size(); ++e)
+      if (g[e] < L.nactive) rp[g[e] + 1]++;
+    for (int r = 0; r < L.nactive; ++r) rp[r + 1] += rp[r];
+    std::vector<int> ent(rp[L.nactive]), fill(rp.begin(), rp.end() - 1);
+    for (size_t e = 0; e < g.size(); ++e)
+      if (g[e] < L.nactive) ent[fill[g[e]]++] = (int)e;
+    CDG_TRY(dalloc(&L.dof_rp, rp.size()));
+    CDG_TRY(dalloc(&L.dof_ent, ent.size()));
+    CDG_TRY(dalloc(&L.rhs_loc, g.size()));
+    CDG_CUDA(cudaMemcpyAsync(L.dof_rp, rp.data(), rp.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    if (!ent.empty())
+      CDG_CUDA(cudaMemcpyAsync(L.dof_ent, ent.data(), ent.size() * sizeof(int),
+                               cudaMemcpyHostToDevice, st));
+    CDG_CUDA(cudaStreamSynchronize(st));
+  }
   double avg = L.ndof ? (double)L.nnz / L.ndof : 1.0;
   // lanes per CSR row for 8-deep unrolled row sums: 8 * lanes >= avg row length
   L.rows_per_warp_hint = avg > 64 ? 16 : avg > 32 ? 8 : avg > 16 ? 4 : 2;
@@ -896,7 +979,7 @@ int free_level(DevLevel& L) {
                   L.rhs, L.sol, L.invdiag64, L.invdiag32, L.mg_rhs, L.mg_sol, L.mg_tmp,
                   L.mg_def, L.P_rp, L.P_col, L.P_val, L.P_val32, L.R_rp, L.R_col, L.R_val,
                   L.R_val32, L.coarse_inv, L.coarse_work, L.dc_rp, L.dc_col, L.dc_pos,
-                  L.tcd_A, L.tcd_M, L.tcd_f, L.tcd_fold};
+                  L.tcd_A, L.tcd_M, L.tcd_f, L.tcd_fold, L.dof_rp, L.dof_ent, L.rhs_loc};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   return CDG_OK;
@@ -1058,10 +1141,13 @@ static int launch_rhs(cdg_context* ctx, const AsmCoefs& k, DevLevel& L, double* 
   CDG_TRY(get_rhs_tables(ctx, L.shape, L.order, k.nqp1, &tb));
   if (L.dim == 2)
     CDG_LAUNCH(ctx, k_rhs<2>, grid_for<int>(L.ncells, 8), 256, 0, k, L.ncells, L.nactive,
-               L.verts, L.gdof, tb, out);
+               L.verts, L.gdof, tb, out, L.rhs_loc);
   else
     CDG_LAUNCH(ctx, k_rhs<3>, grid_for<int>(L.ncells, 8), 256, 0, k, L.ncells, L.nactive,
-               L.verts, L.gdof, tb, out);
+               L.verts, L.gdof, tb, out, L.rhs_loc);
+  if (L.nactive > 0)
+    CDG_LAUNCH(ctx, k_rhs_gather, (int)std::min<long>((L.nactive + 255) / 256, (long)ctx->num_sms * 16),
+               256, 0, L.nactive, L.dof_rp, L.dof_ent, L.rhs_loc, out);
   return CDG_OK;
 }
 

@@ -79,6 +79,11 @@ struct DevLevel {
   double* invdiag64 = nullptr;   // ndof
   float* invdiag32 = nullptr;    // ndof
   int rows_per_warp_hint = 1;    // SpMV shape (avg row length)
+  // rhs assembly: local entries per (cell, local DOF) and, per active DOF,
+  // the list of its local entries (CSR over active rows)
+  double* rhs_loc = nullptr;     // ncells*nloc
+  int* dof_rp = nullptr;         // nactive+1
+  int* dof_ent = nullptr;        // entries: cell*nloc + i
   // couplings of active rows to non-active columns: CSR over active rows,
   // column and CSR slot of each (first smoothing step from a zero start)
   int* dc_rp = nullptr;
@@ -103,7 +108,7 @@ struct DevLevel {
   double* tcd_fold = nullptr;
   // dense inverse of the active block (coarsest multigrid level)
   double* coarse_inv = nullptr;  // na*na
-  double* coarse_work = nullptr; // 2 * na * 2na (Gauss-Jordan ping-pong)
+  double* coarse_work = nullptr; // 2 na^2 (Gauss-Jordan ping-pong) + pivots + column map
   int coarse_na = 0;
 };
 

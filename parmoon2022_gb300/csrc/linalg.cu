@@ -194,7 +194,12 @@ template <int NT>
 __global__ void __launch_bounds__(NT)
 k_multidot(int n, const double* __restrict__ w, const double* __restrict__ V, int k0, int cnt,
            double* partials, unsigned* counter, double* out) {
-  __shared__ double sh[NT / 32][32];
+  static_assert(NT == 256, "one reducing warp per inner product of a group of 8");
+  // FP64 issue is scarce on this GPU: per-thread partials are transposed
+  // through shared memory so each inner product is reduced by one warp,
+  // instead of every warp shuffling all eight
+  __shared__ double tr[8][NT + 1];
+  __shared__ double sh[32];
   __shared__ bool last;
   const int wp = threadIdx.x >> 5, l = threadIdx.x & 31;
   // eight inner products per pass (eight independent basis loads in flight);
@@ -210,18 +215,20 @@ k_multidot(int n, const double* __restrict__ w, const double* __restrict__ V, in
         if (j0 + jj < cnt) a[jj] = fma(wt, __ldcs(V + (size_t)(k0 + j0 + jj) * n + t), a[jj]);
     }
 #pragma unroll
-    for (int jj = 0; jj < 8; ++jj) {
-      double v = a[jj];
+    for (int jj = 0; jj < 8; ++jj) tr[jj][threadIdx.x] = a[jj];
+    __syncthreads();
+    if (j0 + wp < cnt) {
+      double v = 0.0;
+#pragma unroll
+      for (int q = 0; q < NT / 32; ++q) v += tr[wp][q * 32 + l];
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      if (l == 0 && j0 + jj < cnt) sh[wp][j0 + jj] = v;
+      if (l == 0) sh[j0 + wp] = v;
     }
+    __syncthreads();
   }
-  __syncthreads();
   if (threadIdx.x < cnt) {
-    double v = 0.0;
-    for (int q = 0; q < NT / 32; ++q) v += sh[q][threadIdx.x];
-    partials[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = v;
+    partials[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = sh[threadIdx.x];
     __threadfence();
   }
   __syncthreads();
@@ -428,100 +435,220 @@ __global__ void k_coarse_apply(int na, const double* __restrict__ inv, const T* 
 }
 
 // ---------------------------------------------------------------------------
-// coarsest level: Gauss-Jordan inversion with partial pivoting of the active
-// block, one kernel per pivot step on an n x 2n augmented matrix
+// coarsest level: in-place Gauss-Jordan inversion with partial pivoting of
+// the active block (n x n, double-buffered between pivot steps).  Step k:
+//   p = first row of maximal |a_ik|, i >= k; rows k and p exchange;
+//   a_kj <- a_pj / a_pk (j != k),  a_kk <- 1 / a_pk;
+//   a_ij <- a_rj - a_rk a_kj (j != k),  a_ik <- -a_rk / a_pk  (i != k, r =
+//   the row that moves to i).
+// After the last step the columns exchange in reverse pivot order, giving the
+// inverse of the active block.  One reciprocal per step, one FMA per entry.
 // ---------------------------------------------------------------------------
 __global__ void k_extract_dense(int na, const int* __restrict__ rp, const int* __restrict__ col,
                                 const double* __restrict__ val, double* __restrict__ M) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= na) return;
-  const long W = 2L * na;
   for (int k = rp[i]; k < rp[i + 1]; ++k)
-    if (col[k] < na) M[i * W + col[k]] = val[k];
-  M[i * W + na + i] = 1.0;
+    if (col[k] < na) M[(size_t)i * na + col[k]] = val[k];
 }
 
-// one pivot step k: pivot = first row of maximal |M[i][k]|, i >= k (every
-// block finds the same one); rows k and p swap; Mout = eliminated Min
-__device__ __forceinline__ bool gj_step(int na, int k, const double* __restrict__ Min,
-                                        double* __restrict__ Mout, int* err, double* sv,
-                                        int* si) {
-  const long W = 2L * na;
+// pivot of step k (every block computes the same one)
+__device__ __forceinline__ int gj_pivot(int na, int k, const double* __restrict__ Min,
+                                        double* sv, int* si) {
   double best = -1.0;
   int bi = k;
   for (int i = k + threadIdx.x; i < na; i += 256) {
-    double a = fabs(Min[i * W + k]);
+    double a = fabs(Min[(size_t)i * na + k]);
     if (a > best) { best = a; bi = i; }
   }
-  sv[threadIdx.x] = best;
-  si[threadIdx.x] = bi;
-  __syncthreads();
-  for (int o = 128; o > 0; o >>= 1) {
-    if (threadIdx.x < o) {
-      double a = sv[threadIdx.x + o];
-      int ai = si[threadIdx.x + o];
-      if (a > sv[threadIdx.x] || (a == sv[threadIdx.x] && ai < si[threadIdx.x])) {
-        sv[threadIdx.x] = a;
-        si[threadIdx.x] = ai;
-      }
-    }
-    __syncthreads();
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    double a = __shfl_xor_sync(0xffffffffu, best, o);
+    int ai = __shfl_xor_sync(0xffffffffu, bi, o);
+    if (a > best || (a == best && ai < bi)) { best = a; bi = ai; }
   }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) { sv[w] = best; si[w] = bi; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int q = 1; q < 8; ++q)
+      if (sv[q] > sv[0] || (sv[q] == sv[0] && si[q] < si[0])) { sv[0] = sv[q]; si[0] = si[q]; }
+  }
+  __syncthreads();
   const int p = si[0];
-  const double piv = Min[p * W + k];
   __syncthreads();   // sv/si are reused by the next step
+  return p;
+}
+
+// rows of step k handled by this block: i = blockIdx.x, + gridDim.x, ...
+__device__ __forceinline__ bool gj_step(int na, int k, const double* __restrict__ Min,
+                                        double* __restrict__ Mout, int* __restrict__ perm,
+                                        int* err, double* sv, int* si) {
+  const int p = gj_pivot(na, k, Min, sv, si);
+  const double piv = Min[(size_t)p * na + k];
   if (piv == 0.0) {
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(err, kErrSingular);
     return false;
   }
-  const long ncol = (na - k) + na;  // live columns: left [k, na), right [na, 2na)
-  const long total = (long)na * ncol;
-  for (long t = blockIdx.x * 256L + threadIdx.x; t < total; t += (long)gridDim.x * 256) {
-    const int i = (int)(t / ncol);
-    const long jj = t % ncol;
-    const long j = jj < (na - k) ? k + jj : na + (jj - (na - k));
-    const double prow = Min[p * W + j] / piv;
+  if (blockIdx.x == 0 && threadIdx.x == 0) perm[k] = p;
+  const double rpiv = 1.0 / piv;
+  const double* prow = Min + (size_t)p * na;
+  for (int i = blockIdx.x; i < na; i += gridDim.x) {
+    double* out = Mout + (size_t)i * na;
     if (i == k) {
-      Mout[i * W + j] = prow;
+      for (int j = threadIdx.x; j < na; j += 256) out[j] = j == k ? rpiv : prow[j] * rpiv;
     } else {
-      const int r = (i == p) ? k : i;
-      Mout[i * W + j] = Min[r * W + j] - Min[r * W + k] * prow;
+      const double* src = Min + (size_t)(i == p ? k : i) * na;
+      const double f = src[k];
+      for (int j = threadIdx.x; j < na; j += 256)
+        out[j] = j == k ? -f * rpiv : fma(-f, prow[j] * rpiv, src[j]);
     }
   }
   return true;
 }
 
 __global__ void __launch_bounds__(256)
-k_gj_step(int na, int k, const double* __restrict__ Min, double* __restrict__ Mout, int* err) {
-  __shared__ double sv[256];
-  __shared__ int si[256];
-  gj_step(na, k, Min, Mout, err, sv, si);
+k_gj_step(int na, int k, const double* __restrict__ Min, double* __restrict__ Mout,
+          int* __restrict__ perm, int* err) {
+  __shared__ double sv[8];
+  __shared__ int si[8];
+  gj_step(na, k, Min, Mout, perm, err, sv, si);
+}
+
+// column exchanges in reverse pivot order: inv[:, j] = M[:, q[j]]
+__global__ void k_gj_colmap(int na, const int* __restrict__ perm, int* __restrict__ q) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  for (int j = 0; j < na; ++j) q[j] = j;
+  for (int k = na - 1; k >= 0; --k) {
+    const int a = q[k];
+    q[k] = q[perm[k]];
+    q[perm[k]] = a;
+  }
+}
+
+__global__ void k_gj_unpermute(int na, const double* __restrict__ M, const int* __restrict__ q,
+                               double* __restrict__ inv) {
+  for (int i = blockIdx.x; i < na; i += gridDim.x)
+    for (int j = threadIdx.x; j < na; j += blockDim.x)
+      inv[(size_t)i * na + j] = M[(size_t)i * na + q[j]];
 }
 
 // all na pivot steps in one cooperative launch, grid-wide sync between steps;
 // every block sees the same pivot, so all blocks leave together on a zero pivot
 __global__ void __launch_bounds__(256)
-k_gj_coop(int na, double* A, double* B, int* err) {
-  __shared__ double sv[256];
-  __shared__ int si[256];
+k_gj_coop(int na, double* A, double* B, int* perm, int* q, double* inv, int* err) {
+  __shared__ double sv[8];
+  __shared__ int si[8];
   cgrp::grid_group grid = cgrp::this_grid();
   double* Min = A;
   double* Mout = B;
   for (int k = 0; k < na; ++k) {
-    if (!gj_step(na, k, Min, Mout, err, sv, si)) return;
+    if (!gj_step(na, k, Min, Mout, perm, err, sv, si)) return;
     grid.sync();
     double* t = Min;
     Min = Mout;
     Mout = t;
   }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    for (int j = 0; j < na; ++j) q[j] = j;
+    for (int k = na - 1; k >= 0; --k) {
+      const int a = q[k];
+      q[k] = q[perm[k]];
+      q[perm[k]] = a;
+    }
+  }
+  grid.sync();
+  for (int i = blockIdx.x; i < na; i += gridDim.x)
+    for (int j = threadIdx.x; j < na; j += 256) inv[(size_t)i * na + j] = Min[(size_t)i * na + q[j]];
 }
 
-__global__ void k_right_half(int na, const double* __restrict__ M, double* __restrict__ inv) {
-  const long total = (long)na * na;
-  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < total; t += (long)gridDim.x * blockDim.x) {
-    const long i = t / na, j = t % na;
-    inv[t] = M[i * 2L * na + na + j];
+// small active blocks (na <= 160): the whole matrix in one CTA's shared
+// memory, in place; the pivot row (scaled) and column k are buffered first,
+// then every row except k is eliminated (row p reads the old row k), then
+// row k is replaced.  Same pivots and arithmetic as the cooperative kernel.
+constexpr int kGjSmemThreads = 1024;
+
+__global__ void __launch_bounds__(kGjSmemThreads)
+k_gj_smem(int na, const double* __restrict__ Ain, double* __restrict__ inv, int* err) {
+  extern __shared__ double sm[];
+  double* a = sm;                       // na * na
+  double* prow = a + (size_t)na * na;   // na
+  double* colk = prow + na;             // na
+  int* perm = (int*)(colk + na);        // na
+  int* q = perm + na;                   // na
+  __shared__ double wv[32];
+  __shared__ int wi[32];
+  __shared__ int s_p;
+  __shared__ double s_piv;
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, w = tid >> 5;
+  for (int t = tid; t < na * na; t += nt) a[t] = Ain[t];
+  __syncthreads();
+  for (int k = 0; k < na; ++k) {
+    double best = -1.0;
+    int bi = k;
+    for (int i = k + tid; i < na; i += nt) {
+      double v = fabs(a[(size_t)i * na + k]);
+      if (v > best) { best = v; bi = i; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      double v = __shfl_xor_sync(0xffffffffu, best, o);
+      int vi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (v > best || (v == best && vi < bi)) { best = v; bi = vi; }
+    }
+    if (lane == 0) { wv[w] = best; wi[w] = bi; }
+    __syncthreads();
+    if (tid == 0) {
+      double b = wv[0];
+      int p = wi[0];
+      for (int u = 1; u < nt / 32; ++u)
+        if (wv[u] > b || (wv[u] == b && wi[u] < p)) { b = wv[u]; p = wi[u]; }
+      s_p = p;
+      s_piv = a[(size_t)p * na + k];
+      perm[k] = p;
+    }
+    __syncthreads();
+    const int p = s_p;
+    const double piv = s_piv;
+    if (piv == 0.0) {
+      if (tid == 0) atomicOr(err, kErrSingular);
+      return;   // uniform: every thread read the same pivot
+    }
+    const double rpiv = 1.0 / piv;
+    for (int j = tid; j < na; j += nt) prow[j] = j == k ? rpiv : a[(size_t)p * na + j] * rpiv;
+    for (int i = tid; i < na; i += nt) colk[i] = a[(size_t)(i == p ? k : i) * na + k];
+    __syncthreads();
+    // rows i != k; row p takes the old row k (row k is not written in this
+    // pass, row p is read by no other row)
+    for (int t = tid; t < na * na; t += nt) {
+      const int i = t / na, j = t - i * na;
+      if (i == k) continue;
+      const double f = colk[i];
+      const double old = a[(size_t)(i == p ? k : i) * na + j];
+      a[t] = j == k ? -f * rpiv : fma(-f, prow[j], old);
+    }
+    __syncthreads();
+    for (int j = tid; j < na; j += nt) a[(size_t)k * na + j] = prow[j];
+    __syncthreads();
   }
+  if (tid == 0) {
+    for (int j = 0; j < na; ++j) q[j] = j;
+    for (int k = na - 1; k >= 0; --k) {
+      const int t = q[k];
+      q[k] = q[perm[k]];
+      q[perm[k]] = t;
+    }
+  }
+  __syncthreads();
+  for (int t = tid; t < na * na; t += nt) {
+    const int i = t / na, j = t - (t / na) * na;
+    inv[t] = a[(size_t)i * na + q[j]];
+  }
+}
+
+static size_t gj_smem_bytes(int na) {
+  return (size_t)na * na * sizeof(double) + 2 * (size_t)na * sizeof(double) +
+         2 * (size_t)na * sizeof(int);
 }
 
 static int coarse_inverse(cdg_context* ctx, DevLevel& C) {
@@ -529,35 +656,45 @@ static int coarse_inverse(cdg_context* ctx, DevLevel& C) {
   C.coarse_na = na;
   if (na == 0) return CDG_OK;
   if (na > 8192) { set_error("coarse level too large for the dense inverse (%d)", na); return CDG_ERR_LIMIT; }
-  size_t sz = (size_t)na * 2 * na;
+  const size_t sz = (size_t)na * na;
   if (!C.coarse_work) {
-    CDG_CUDA(cudaMalloc(&C.coarse_work, 2 * sz * sizeof(double)));
-    CDG_CUDA(cudaMalloc(&C.coarse_inv, (size_t)na * na * sizeof(double)));
+    // two n x n buffers + pivot rows + column map
+    CDG_CUDA(cudaMalloc(&C.coarse_work, (2 * sz + na) * sizeof(double)));
+    CDG_CUDA(cudaMalloc(&C.coarse_inv, sz * sizeof(double)));
   }
   double* A = C.coarse_work;
   double* B = C.coarse_work + sz;
+  int* perm = (int*)(C.coarse_work + 2 * sz);
+  int* q = perm + na;
   CDG_CUDA(cudaMemsetAsync(A, 0, sz * sizeof(double), ctx->stream));
   CDG_LAUNCH(ctx, k_extract_dense, grid_for<int>(na, 128), 128, 0, na, C.row_ptr, C.col, C.val64, A);
+  const size_t smem = gj_smem_bytes(na);
+  if (smem <= 220 * 1024) {
+    CDG_CUDA(cudaFuncSetAttribute(k_gj_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CDG_LAUNCH(ctx, k_gj_smem, 1, kGjSmemThreads, smem, na, A, C.coarse_inv, ctx->d_err);
+    return CDG_OK;
+  }
   int coop = 0, per_sm = 0;
   CDG_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device));
   CDG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gj_coop, 256, 0));
-  long want = ((long)na * 2 * na + 255) / 256;
-  int g = (int)std::min<long>(want, (long)ctx->num_sms * std::min(per_sm, 2));
+  // one block per row up to one (or two) per SM: fewer blocks, cheaper grid syncs
+  int g = (int)std::min<long>((long)na, (long)ctx->num_sms * std::min(per_sm, na > 1024 ? 2 : 1));
   if (coop && per_sm > 0 && g >= 1) {
-    void* args[] = {(void*)&na, (void*)&A, (void*)&B, (void*)&ctx->d_err};
+    double* inv = C.coarse_inv;
+    void* args[] = {(void*)&na, (void*)&A, (void*)&B, (void*)&perm, (void*)&q, (void*)&inv,
+                    (void*)&ctx->d_err};
     CDG_CUDA(cudaLaunchCooperativeKernel((const void*)k_gj_coop, dim3(g), dim3(256), args, 0,
                                          ctx->stream));
     ctx->launches++;
-    if (na % 2 == 1) std::swap(A, B);   // result of step na-1 is in B when na is odd
-  } else {
-    for (int k = 0; k < na; ++k) {
-      long total = (long)na * ((na - k) + na);
-      int gg = (int)std::min<long>((total + 255) / 256, (long)ctx->num_sms * 8);
-      CDG_LAUNCH(ctx, k_gj_step, gg, 256, 0, na, k, A, B, ctx->d_err);
-      std::swap(A, B);
-    }
+    return CDG_OK;
   }
-  CDG_LAUNCH(ctx, k_right_half, grid_for<int>(na * na, 256), 256, 0, na, A, C.coarse_inv);
+  for (int k = 0; k < na; ++k) {
+    int gg = std::min(na, ctx->num_sms * 4);
+    CDG_LAUNCH(ctx, k_gj_step, gg, 256, 0, na, k, A, B, perm, ctx->d_err);
+    std::swap(A, B);
+  }
+  CDG_LAUNCH(ctx, k_gj_colmap, 1, 32, 0, na, perm, q);
+  CDG_LAUNCH(ctx, k_gj_unpermute, std::min(na, ctx->num_sms * 4), 256, 0, na, A, q, C.coarse_inv);
   return CDG_OK;
 }
 
@@ -950,8 +1087,9 @@ int fgmres(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s, cdg_sol
         // classical: all inner products, then all updates and the norm
         for (int k0 = 0; k0 <= i; k0 += 32) {
           int cnt = std::min(32, i + 1 - k0);
-          CDG_LAUNCH(ctx, k_multidot<256>, red_grid(ctx, n), 256, 0, n, g.w, g.V, k0, cnt,
-                     ctx->d_red, ctx->d_cnt + 1, col + k0);
+          // two blocks per SM: several elements per thread, fewer FP64 reductions
+          CDG_LAUNCH(ctx, k_multidot<256>, std::min(red_grid(ctx, n), ctx->num_sms * 2), 256, 0,
+                     n, g.w, g.V, k0, cnt, ctx->d_red, ctx->d_cnt + 1, col + k0);
         }
         CDG_LAUNCH(ctx, k_cgs_update, red_grid(ctx, n), 256, 0, n, g.w, g.V, i, col,
                    ctx->d_red, ctx->d_cnt, g.cs, g.sn, g.s, resid_d, g.scal + 2);
