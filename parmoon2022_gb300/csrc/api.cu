@@ -371,10 +371,7 @@ int cdg_problem_destroy(cdg_problem* p) {
   cudaSetDevice(p->ctx->device);
   cudaStreamSynchronize(p->ctx->stream);
   for (auto& L : p->lev) free_level(L);
-  GmresState& g = p->gm;
-  double* ptrs[] = {g.V, g.Z, g.w, g.H, g.cs, g.sn, g.s, g.y, g.scal};
-  for (double* q : ptrs)
-    if (q) cudaFree(q);
+  free_gmres(p->gm);
   if (p->d_tables) cudaFree(p->d_tables);
   if (p->d_zero_diag) cudaFree(p->d_zero_diag);
   delete p;

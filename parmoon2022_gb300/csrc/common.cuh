@@ -95,6 +95,7 @@ struct DevLevel {
   void* mg_tmp = nullptr;
   void* mg_def = nullptr;
   int mg_elem = 0;               // sizeof element of mg vectors
+  int realloc_count = 0;         // multigrid vector (re)allocations
   bool mg_visited = false;       // level already descended through this cycle
   // transfer to the next coarser level (this = fine)
   int* P_rp = nullptr; int* P_col = nullptr; double* P_val = nullptr; float* P_val32 = nullptr;
@@ -123,13 +124,23 @@ struct GmresState {
   double* sn = nullptr;      // m+1
   double* s = nullptr;       // m+1
   double* y = nullptr;       // m+1
-  double* scal = nullptr;    // 8 scalars: [0] resid, [1] beta, ...
+  double* scal = nullptr;    // 8 scalars: [0] resid, [1] beta, [2] norm, [4..5] loop info
+  // graph-captured iteration loop (a WHILE conditional node around one
+  // FGMRES iteration); rebuilt when the solver parameters or buffers change
+  int* dstate = nullptr;     // [0] i (column), [1] j (iteration), [2] flag
+  double* zcur = nullptr;    // n: z_i for the operator application
+  cudaGraphExec_t exec = nullptr;
+  cudaGraph_t graph = nullptr;
+  cdg_solver_params key{};   // parameters the graph was captured with
+  unsigned long long key_gen = 0;
+  long long body_launches = 0;   // kernels per iteration
 };
 
 }  // namespace cdg
 
 struct cdg_problem {
   cdg_context* ctx = nullptr;
+  unsigned long long alloc_gen = 1;   // bumped when device work buffers move
   int dim = 2, shape = cdg::kQuad, order = 1;
   std::vector<cdg::DevLevel> lev;
   cdg::GmresState gm;
@@ -194,8 +205,9 @@ int prolongate64(cdg_context* ctx, const DevLevel& F, const double* xc, double* 
 int restrict64(cdg_context* ctx, const DevLevel& F, const DevLevel& C, const double* df,
                double* rc);
 int precondition(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s,
-                 const double* v, double* z);
+                 const double* v, double* z, const int* di = nullptr, double* zcur = nullptr);
 int prepare_solver(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s);
+void free_gmres(GmresState& g);
 int fgmres(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s,
            cdg_solve_stats* st);
 // single hot-kernel launches for measurement

@@ -193,8 +193,16 @@ k_mgs(int n, double* __restrict__ w, const double* __restrict__ vk, const double
 template <int NT>
 __global__ void __launch_bounds__(NT)
 k_multidot(int n, const double* __restrict__ w, const double* __restrict__ V, int k0, int cnt,
-           double* partials, unsigned* counter, double* out) {
+           double* partials, unsigned* counter, double* out, const int* di = nullptr,
+           int hstride = 0) {
   static_assert(NT == 256, "one reducing warp per inner product of a group of 8");
+  if (di) {
+    // graph-captured loop: inner products k0 .. min(k0 + 32, i + 1) of column i
+    const int i = *di;
+    cnt = min(32, i + 1 - k0);
+    out += (size_t)i * hstride + k0;
+    if (cnt <= 0) return;   // uniform over the grid
+  }
   // FP64 issue is scarce on this GPU: per-thread partials are transposed
   // through shared memory so each inner product is reduced by one warp,
   // instead of every warp shuffling all eight
@@ -286,9 +294,14 @@ __device__ void givens_column(int i, double* col, double* cs, double* sn, double
 __global__ void __launch_bounds__(256)
 k_cgs_update(int n, double* __restrict__ w, const double* __restrict__ V, int i,
              double* __restrict__ hcol, double* partials, unsigned* counter, double* cs,
-             double* sn, double* gs, double* resid, double* norm_out) {
+             double* sn, double* gs, double* resid, double* norm_out, const int* di = nullptr,
+             int hstride = 0) {
   __shared__ double h[128];
   __shared__ bool last;
+  if (di) {
+    i = *di;
+    hcol += (size_t)i * hstride;
+  }
   for (int j = threadIdx.x; j <= i; j += 256) h[j] = -hcol[j];
   __syncthreads();
   double s = 0.0;
@@ -349,9 +362,11 @@ int dot64(cdg_context* ctx, int n, const double* a, const double* b, double* out
 // ---------------------------------------------------------------------------
 // small vector kernels
 // ---------------------------------------------------------------------------
-// dst = src * (1 / *s); flags a zero scalar (FGMRES breakdown)
+// dst = src * (1 / *s); flags a zero scalar (FGMRES breakdown).  di != null:
+// dst is the basis vector (*di + 1) of the block dst (graph-captured loop)
 __global__ void k_scale_inv(int n, const double* __restrict__ src, const double* s,
-                            double* __restrict__ dst, int* err) {
+                            double* __restrict__ dst, int* err, const int* di = nullptr) {
+  if (di) dst += (size_t)(*di + 1) * n;
   const double d = *s;
   if (d == 0.0) {
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(err, kErrBreakdown);
@@ -362,15 +377,37 @@ __global__ void k_scale_inv(int n, const double* __restrict__ src, const double*
     dst[i] = src[i] * f;
 }
 
+// c = a .* b; di != null: a and c are vector *di of their blocks, c2 gets a copy
 __global__ void k_mul(int n, const double* __restrict__ a, const double* __restrict__ b,
-                      double* __restrict__ c) {
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
-    c[i] = a[i] * b[i];
+                      double* __restrict__ c, const int* di = nullptr, double* c2 = nullptr) {
+  if (di) {
+    a += (size_t)(*di) * n;
+    c += (size_t)(*di) * n;
+  }
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const double v = a[i] * b[i];
+    c[i] = v;
+    if (c2) c2[i] = v;
+  }
+}
+
+// c = a (no preconditioner), same indexing as k_mul
+__global__ void k_copy_idx(int n, const double* __restrict__ a, double* __restrict__ c,
+                           const int* di, double* c2) {
+  if (di) {
+    a += (size_t)(*di) * n;
+    c += (size_t)(*di) * n;
+  }
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    c[i] = a[i];
+    if (c2) c2[i] = a[i];
+  }
 }
 
 template <typename T>
 __global__ void k_mg_init(int n, int nactive, const double* __restrict__ v, T* __restrict__ rhs,
-                          T* __restrict__ sol) {
+                          T* __restrict__ sol, const int* di = nullptr) {
+  if (di) v += (size_t)(*di) * n;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     T r = (T)v[i];
     rhs[i] = r;
@@ -379,9 +416,14 @@ __global__ void k_mg_init(int n, int nactive, const double* __restrict__ v, T* _
 }
 
 template <typename T>
-__global__ void k_to_double(int n, const T* __restrict__ a, double* __restrict__ b) {
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
-    b[i] = (double)a[i];
+__global__ void k_to_double(int n, const T* __restrict__ a, double* __restrict__ b,
+                            const int* di = nullptr, double* b2 = nullptr) {
+  if (di) b += (size_t)(*di) * n;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const double v = (double)a[i];
+    b[i] = v;
+    if (b2) b2[i] = v;
+  }
 }
 
 // x_f[i] += damp * (P x_c)[i] for fine actives (update_solution_in_finer_grid)
@@ -820,12 +862,12 @@ static void fill_cycle(std::vector<int>& seq, std::vector<int>& rec, int level, 
 
 template <typename T>
 static int mg_cycle(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s,
-                    const double* v, double* z) {
+                    const double* v, double* z, const int* di = nullptr, double* zcur = nullptr) {
   const int nl = s.multigrid_n_levels;
   auto lv = [&](int m) -> DevLevel& { return p->lev[nl - 1 - m]; };
   DevLevel& F = p->lev[0];
   CDG_LAUNCH(ctx, k_mg_init<T>, vec_grid(ctx, F.ndof), 256, 0, F.ndof, F.nactive, v,
-             (T*)F.mg_rhs, (T*)F.mg_sol);
+             (T*)F.mg_rhs, (T*)F.mg_sol, di);
   std::vector<int> rec(nl, s.multigrid_cycle_type == 0 ? 1 : 2), seq;
   rec[nl - 1] = 1;
   seq.push_back(kDummy);
@@ -877,12 +919,14 @@ static int mg_cycle(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s
       }
     }
   }
-  CDG_LAUNCH(ctx, k_to_double<T>, vec_grid(ctx, F.ndof), 256, 0, F.ndof, (const T*)F.mg_sol, z);
+  CDG_LAUNCH(ctx, k_to_double<T>, vec_grid(ctx, F.ndof), 256, 0, F.ndof, (const T*)F.mg_sol, z,
+             di, zcur);
   return CDG_OK;
 }
 
 int ensure_mg_vectors(cdg_context* ctx, DevLevel& L, int elem) {
   if (L.mg_elem == elem) return CDG_OK;
+  L.realloc_count++;
   void** bufs[4] = {&L.mg_rhs, &L.mg_sol, &L.mg_tmp, &L.mg_def};
   for (void** b : bufs) {
     if (*b) cudaFree(*b);
@@ -932,16 +976,23 @@ int prepare_solver(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s)
   return CDG_OK;
 }
 
+// z = B v (Iteration_jacobi / Iteration_multigrid apply, or a copy).  di !=
+// null: v and z are the blocks V and Z, the vector index *di is read on the
+// device (graph-captured FGMRES loop) and zcur receives a copy of z_i
 int precondition(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s, const double* v,
-                 double* z) {
+                 double* z, const int* di, double* zcur) {
   DevLevel& F = p->lev[0];
   if (s.preconditioner == 1) {
-    CDG_LAUNCH(ctx, k_mul, vec_grid(ctx, F.ndof), 256, 0, F.ndof, v, F.invdiag64, z);
+    CDG_LAUNCH(ctx, k_mul, vec_grid(ctx, F.ndof), 256, 0, F.ndof, v, F.invdiag64, z, di, zcur);
     return CDG_OK;
   }
   if (s.preconditioner == 2) {
-    if (s.precision == 1) return mg_cycle<float>(ctx, p, s, v, z);
-    return mg_cycle<double>(ctx, p, s, v, z);
+    if (s.precision == 1) return mg_cycle<float>(ctx, p, s, v, z, di, zcur);
+    return mg_cycle<double>(ctx, p, s, v, z, di, zcur);
+  }
+  if (di) {
+    CDG_LAUNCH(ctx, k_copy_idx, vec_grid(ctx, F.ndof), 256, 0, F.ndof, v, z, di, zcur);
+    return CDG_OK;
   }
   CDG_CUDA(cudaMemcpyAsync(z, v, (size_t)F.ndof * sizeof(double), cudaMemcpyDeviceToDevice,
                            ctx->stream));
@@ -997,15 +1048,25 @@ __global__ void k_update(int n, int k, const double* __restrict__ Z, const doubl
   }
 }
 
+void free_gmres(GmresState& g) {
+  double* ptrs[] = {g.V, g.Z, g.w, g.H, g.cs, g.sn, g.s, g.y, g.scal, g.zcur};
+  for (double* q : ptrs)
+    if (q) cudaFree(q);
+  if (g.dstate) cudaFree(g.dstate);
+  if (g.exec) cudaGraphExecDestroy(g.exec);
+  if (g.graph) cudaGraphDestroy(g.graph);
+  g = GmresState();
+}
+
 static int ensure_gmres(cdg_problem* p, int n, int m) {
   GmresState& g = p->gm;
   if (g.n == n && g.m == m && g.V) return CDG_OK;
-  double* ptrs[] = {g.V, g.Z, g.w, g.H, g.cs, g.sn, g.s, g.y, g.scal};
-  for (double* q : ptrs)
-    if (q) cudaFree(q);
-  g = GmresState();
+  free_gmres(g);
+  p->alloc_gen++;
   g.n = n;
   g.m = m;
+  CDG_CUDA(cudaMalloc(&g.zcur, (size_t)n * sizeof(double)));
+  CDG_CUDA(cudaMalloc(&g.dstate, 4 * sizeof(int)));
   CDG_CUDA(cudaMalloc(&g.V, (size_t)(m + 1) * n * sizeof(double)));
   CDG_CUDA(cudaMalloc(&g.Z, (size_t)m * n * sizeof(double)));
   CDG_CUDA(cudaMalloc(&g.w, (size_t)n * sizeof(double)));
@@ -1048,6 +1109,231 @@ static int read_scalar(cdg_context* ctx, const double* d, double* h) {
   return CDG_OK;
 }
 
+// ---------------------------------------------------------------------------
+// device-resident FGMRES: one iteration is captured once as the body of a
+// WHILE conditional graph node; the convergence test (IterativeMethod::
+// converged) runs on the device and ends the loop, so the host waits once
+// per restart cycle instead of once per iteration
+// ---------------------------------------------------------------------------
+struct ConvParams {
+  double tol, red, div;
+  int min_it, max_it, m;
+};
+
+// IterativeMethod::converged (IterativeMethod.h:83-163): 0 continue, 1 stop,
+// 2 diverged; li[0] initial, li[1] previous residual
+__device__ int conv_test(const ConvParams& c, double* li, double res, int it) {
+  if (it == 0) {
+    li[0] = res;
+    li[1] = res;
+  }
+  const bool small = res < c.tol;
+  const bool red = res < c.red * li[0];
+  const bool enough = it >= c.min_it;
+  const bool stag = res > 1e10 * li[1];
+  const bool div = res > c.div * li[0];
+  bool conv = (small || red || stag || div) && enough;
+  if (it == c.max_it) conv = true;
+  li[1] = res;
+  if (div) return 2;
+  return conv ? 1 : 0;
+}
+
+// st: [0] column i, [1] iteration j, [2] flag (0 run, 1 converged,
+// 2 diverged, 3 end of the restart cycle)
+__global__ void k_fgmres_start(ConvParams c, int* st, const double* beta, double* li) {
+  st[0] = 0;
+  st[1] = 1;
+  st[2] = conv_test(c, li, *beta, 0);
+}
+
+__global__ void k_fgmres_iter_check(ConvParams c, int* st, const double* resid, double* li,
+                                    cudaGraphConditionalHandle h) {
+  const int i = st[0], j = st[1];
+  const int cv = conv_test(c, li, *resid, j);
+  unsigned cont = 0;
+  if (cv == 2) {
+    st[2] = 2;
+  } else if (cv == 1) {
+    st[2] = 1;
+  } else if (i + 1 == c.m) {
+    st[2] = 3;
+    st[1] = j + 1;
+  } else {
+    st[0] = i + 1;
+    st[1] = j + 1;
+    cont = 1;
+  }
+  cudaGraphSetConditional(h, cont);
+}
+
+// after a full cycle: the test with the last estimate at iteration j
+__global__ void k_fgmres_restart_check(ConvParams c, int* st, const double* resid, double* li) {
+  st[2] = conv_test(c, li, *resid, st[1]);
+  st[0] = 0;
+}
+
+static ConvParams conv_params(const cdg_solver_params& s) {
+  return ConvParams{s.residual_tolerance, s.residual_reduction, s.divergence_factor,
+                    s.min_n_iterations, s.max_n_iterations, s.gmres_restart};
+}
+
+// one FGMRES iteration (classical Gram-Schmidt), column index on the device
+static int iteration_body(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s,
+                          cudaGraphConditionalHandle h) {
+  DevLevel& L = p->lev[0];
+  GmresState& g = p->gm;
+  const int n = L.ndof, m = s.gmres_restart;
+  int* di = g.dstate;
+  CDG_TRY(precondition(ctx, p, s, g.V, g.Z, di, g.zcur));
+  CDG_TRY(spmv_apply64(ctx, L, g.zcur, g.w));
+  const int mg = std::min(red_grid(ctx, n), ctx->num_sms * 2);
+  for (int k0 = 0; k0 < m; k0 += 32)
+    CDG_LAUNCH(ctx, k_multidot<256>, mg, 256, 0, n, g.w, g.V, k0, 0, ctx->d_red,
+               ctx->d_cnt + 1, g.H, di, m + 1);
+  CDG_LAUNCH(ctx, k_cgs_update, red_grid(ctx, n), 256, 0, n, g.w, g.V, 0, g.H, ctx->d_red,
+             ctx->d_cnt, g.cs, g.sn, g.s, g.scal + 0, g.scal + 2, di, m + 1);
+  CDG_LAUNCH(ctx, k_scale_inv, vec_grid(ctx, n), 256, 0, n, g.w, g.scal + 2, g.V, ctx->d_err, di);
+  CDG_LAUNCH(ctx, k_fgmres_iter_check, 1, 1, 0, conv_params(s), g.dstate, g.scal + 0,
+             g.scal + 4, h);
+  return CDG_OK;
+}
+
+static unsigned long long graph_generation(const cdg_problem* p) {
+  unsigned long long gen = p->alloc_gen;
+  for (const DevLevel& L : p->lev)
+    gen = gen * 1000003ull + (unsigned long long)L.realloc_count * 7919ull +
+          (unsigned long long)(uintptr_t)L.coarse_inv;
+  return gen;
+}
+
+static int ensure_iteration_graph(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s) {
+  GmresState& g = p->gm;
+  const unsigned long long gen = graph_generation(p);
+  if (g.exec && g.key_gen == gen && std::memcmp(&g.key, &s, sizeof(s)) == 0) return CDG_OK;
+  if (g.exec) cudaGraphExecDestroy(g.exec);
+  if (g.graph) cudaGraphDestroy(g.graph);
+  g.exec = nullptr;
+  g.graph = nullptr;
+  cudaGraph_t graph = nullptr;
+  CDG_CUDA(cudaGraphCreate(&graph, 0));
+  cudaGraphConditionalHandle h;
+  cudaGraphNodeParams np = {};
+  cudaGraphNode_t node;
+  cudaError_t e = cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault);
+  if (e == cudaSuccess) {
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    e = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np);
+  }
+  if (e == cudaSuccess)
+    e = cudaStreamBeginCaptureToGraph(ctx->stream, np.conditional.phGraph_out[0], nullptr,
+                                      nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    set_error("graph setup: %s", cudaGetErrorString(e));
+    return CDG_ERR_CUDA;
+  }
+  const long long l0 = ctx->launches;
+  int rc = iteration_body(ctx, p, s, h);
+  cudaGraph_t body = nullptr;
+  e = cudaStreamEndCapture(ctx->stream, &body);
+  g.body_launches = ctx->launches - l0;
+  ctx->launches = l0;   // captured, not launched
+  if (rc != CDG_OK || e != cudaSuccess) {
+    cudaGetLastError();
+    cudaGraphDestroy(graph);
+    if (rc == CDG_OK) set_error("graph capture: %s", cudaGetErrorString(e));
+    return rc != CDG_OK ? rc : CDG_ERR_CUDA;
+  }
+  e = cudaGraphInstantiate(&g.exec, graph, 0);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    g.exec = nullptr;
+    set_error("graph instantiate: %s", cudaGetErrorString(e));
+    return CDG_ERR_CUDA;
+  }
+  g.graph = graph;
+  g.key = s;
+  g.key_gen = gen;
+  return CDG_OK;
+}
+
+static int read_state(cdg_context* ctx, const GmresState& g, int* st4, double* resid) {
+  CDG_CUDA(cudaMemcpyAsync(st4, g.dstate, 4 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CDG_CUDA(cudaMemcpyAsync(ctx->h_pinned, g.scal, sizeof(double), cudaMemcpyDeviceToHost,
+                           ctx->stream));
+  CDG_CUDA(cudaStreamSynchronize(ctx->stream));
+  *resid = ctx->h_pinned[0];
+  return CDG_OK;
+}
+
+static int fgmres_graph(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s,
+                        cdg_solve_stats* st) {
+  DevLevel& L = p->lev[0];
+  const int n = L.ndof, m = s.gmres_restart;
+  GmresState& g = p->gm;
+  double* x = L.sol;
+  const double* b = L.rhs;
+  double* beta_d = g.scal + 1;
+  const int vg = vec_grid(ctx, n);
+  const ConvParams cp = conv_params(s);
+  CDG_TRY(ensure_iteration_graph(ctx, p, s));
+  // r = b - A x; beta = ||r||; the test at iteration 0
+  CDG_TRY(residual64(ctx, L, b, x, g.w));
+  CDG_TRY(dot64(ctx, n, g.w, nullptr, beta_d, 0));
+  CDG_LAUNCH(ctx, k_fgmres_start, 1, 1, 0, cp, g.dstate, beta_d, g.scal + 4);
+  int sv[4];
+  double beta = 0;
+  CDG_CUDA(cudaMemcpyAsync(sv, g.dstate, 4 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CDG_TRY(read_scalar(ctx, beta_d, &beta));
+  st->initial_residual = beta;
+  st->iterations = 0;
+  st->residual = beta;
+  if (sv[2] != 0) return CDG_OK;
+  double resid = beta;
+  for (;;) {
+    CDG_LAUNCH(ctx, k_scale_inv, vg, 256, 0, n, g.w, beta_d, g.V, ctx->d_err);
+    CDG_LAUNCH(ctx, k_init_s, 1, 128, 0, m, beta_d, g.s);
+    CDG_CUDA(cudaGraphLaunch(g.exec, ctx->stream));
+    CDG_TRY(read_state(ctx, g, sv, &resid));
+    const int i = sv[0], j = sv[1], flag = sv[2];
+    ctx->launches += g.body_launches * (long long)(flag == 3 ? m : i + 1);
+    CDG_TRY(check_device_error(ctx));
+    if (flag == 2) {
+      set_error("Execution of the code stopped because of solver divergence.");
+      st->iterations = j;
+      st->residual = resid;
+      return CDG_ERR_DIVERGED;
+    }
+    if (flag == 1) {
+      CDG_LAUNCH(ctx, k_backsolve, 1, 1, 0, i, m, g.H, g.s, g.y);
+      CDG_LAUNCH(ctx, k_update, vg, 256, 0, n, i, g.Z, g.y, x);
+      st->iterations = j;
+      st->residual = resid;
+      return CDG_OK;
+    }
+    // end of the restart cycle: update x, new residual, test
+    CDG_LAUNCH(ctx, k_backsolve, 1, 1, 0, m - 1, m, g.H, g.s, g.y);
+    CDG_LAUNCH(ctx, k_update, vg, 256, 0, n, m - 1, g.Z, g.y, x);
+    CDG_TRY(residual64(ctx, L, b, x, g.w));
+    CDG_TRY(dot64(ctx, n, g.w, nullptr, beta_d, 0));
+    CDG_LAUNCH(ctx, k_fgmres_restart_check, 1, 1, 0, cp, g.dstate, g.scal + 0, g.scal + 4);
+    CDG_TRY(read_state(ctx, g, sv, &resid));
+    if (sv[2] == 2) {
+      set_error("Execution of the code stopped because of solver divergence.");
+      return CDG_ERR_DIVERGED;
+    }
+    if (sv[2] == 1 || sv[1] > s.max_n_iterations) {
+      st->iterations = std::min(sv[1], s.max_n_iterations);
+      st->residual = resid;
+      return CDG_OK;
+    }
+  }
+}
+
 // Iteration_gmres::flexible_gmres on the finest level: x = lev[0].sol,
 // b = lev[0].rhs
 int fgmres(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s, cdg_solve_stats* st) {
@@ -1055,6 +1341,10 @@ int fgmres(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s, cdg_sol
   const int n = L.ndof, m = s.gmres_restart;
   if (m < 1 || m > 120) { set_error("gmres_restart must be in [1, 120]"); return CDG_ERR_ARG; }
   CDG_TRY(ensure_gmres(p, n, m));
+  // classical Gram-Schmidt with a preconditioner free of host reads: the
+  // graph-captured loop (same kernels, same order)
+  if (s.gram_schmidt == 0 && !(s.preconditioner == 2 && s.multigrid_smoother_coarse != 0))
+    return fgmres_graph(ctx, p, s, st);
   GmresState& g = p->gm;
   double* x = L.sol;
   const double* b = L.rhs;
