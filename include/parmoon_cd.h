@@ -259,6 +259,58 @@ int cdg_problem_precondition(cdg_problem *p, const cdg_solver_params *s,
 int cdg_problem_time_kernel(cdg_problem *p, const cdg_assembly_params *a,
                             int kernel, int level, int reps, double *ms);
 
+/* ------------------------------------------------------------------------ */
+/* Request server: stationary CD solves of differing meshes and coefficients,
+ * served concurrently on one GPU.  Replaces a driver that constructs a
+ * ConvectionDiffusion<d> per request and calls assemble() + solve()
+ * (src/System/ConvectionDiffusion.C:112-281): here the meshes, CSR matrices,
+ * multigrid hierarchies and Krylov state of each mesh class stay resident on
+ * the device between requests.
+ *
+ * n_slots workers each own a stream; a request waits in the queue until a
+ * slot is free and its problem instance fits the HBM budget (idle instances
+ * are evicted least recently used first), then assemble + solve run on the
+ * slot's stream, overlapping with the other slots' work on the device. */
+typedef struct cdg_server cdg_server;
+
+typedef struct {
+  int dim;                 /* 2 or 3                                           */
+  int order;               /* 1 (Q1) or 2 (Q2)                                 */
+  int n;                   /* cells per direction: roots * 2^k, roots 1 or 3   */
+  cdg_assembly_params a;   /* coefficients and discretisation                  */
+  cdg_solver_params s;     /* solver; multigrid_n_levels <= 0: chosen so the
+                              coarsest grid has 3 or 4 cells per direction     */
+} cdg_request;
+
+typedef struct {
+  int status;              /* CDG_OK or an error code                          */
+  cdg_solve_stats stats;
+  double queue_seconds;    /* submit -> start on a slot                        */
+  double latency_seconds;  /* submit -> solution copied out                     */
+  int slot;                /* worker that ran it                               */
+  int ndof;
+} cdg_result;
+
+/* n_slots concurrent workers (1..64); hbm_budget_bytes 0 = 80 % of free */
+int cdg_server_create(int device, int n_slots, long long hbm_budget_bytes,
+                      cdg_server **out);
+int cdg_server_destroy(cdg_server *srv);
+/* number of DOFs of a request's finest level (size of its solution) */
+int cdg_request_ndof(const cdg_request *req, int *ndof);
+/* queue a request; solution_out (ndof doubles, host) receives the solution;
+ * the buffer must stay valid until the request is complete */
+int cdg_server_submit(cdg_server *srv, const cdg_request *req, double *solution_out,
+                      long long *ticket);
+/* wait for a request (timeout_seconds < 0: no timeout); 1 = still pending
+ * after the timeout, 0 = done and *res filled */
+int cdg_server_wait(cdg_server *srv, long long ticket, double timeout_seconds,
+                    cdg_result *res);
+/* counters: [0] submitted, [1] completed, [2] failed, [3] queued now,
+ * [4] running now, [5] instances resident, [6] bytes resident, [7] evictions,
+ * [8] budget bytes, [9] peak concurrent running, [10] kernel launches of all
+ * slots, [11] mesh classes seen */
+int cdg_server_counters(cdg_server *srv, long long *c12);
+
 #ifdef __cplusplus
 }
 #endif

@@ -42,7 +42,9 @@ EXPORTED = [
     "cdg_problem_apply", "cdg_problem_prolongate", "cdg_problem_restrict",
     "cdg_problem_precondition", "cdg_context_stream", "cdg_problem_time_kernel",
     "cdg_problem_errors_noalloc", "cdg_hierarchy_create_tetra", "cdg_problem_tcd_initialize",
-    "cdg_problem_tcd_step", "cdg_problem_get_tcd_matrix",
+    "cdg_problem_tcd_step", "cdg_problem_get_tcd_matrix", "cdg_server_create",
+    "cdg_server_destroy", "cdg_request_ndof", "cdg_server_submit", "cdg_server_wait",
+    "cdg_server_counters",
 ]
 
 
@@ -81,6 +83,17 @@ class SolverParams(ctypes.Structure):
 class SolveStats(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int), ("residual", ctypes.c_double),
                 ("initial_residual", ctypes.c_double), ("seconds", ctypes.c_double)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("dim", ctypes.c_int), ("order", ctypes.c_int), ("n", ctypes.c_int),
+                ("a", AssemblyParams), ("s", SolverParams)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("stats", SolveStats),
+                ("queue_seconds", ctypes.c_double), ("latency_seconds", ctypes.c_double),
+                ("slot", ctypes.c_int), ("ndof", ctypes.c_int)]
 
 
 _lib = None
@@ -135,6 +148,12 @@ def lib():
             "cdg_context_stream": [P, PP],
             "cdg_problem_time_kernel": [P, ctypes.POINTER(AssemblyParams), ctypes.c_int,
                                         ctypes.c_int, ctypes.c_int, dp],
+            "cdg_server_create": [ctypes.c_int, ctypes.c_int, ctypes.c_longlong, PP],
+            "cdg_server_destroy": [P],
+            "cdg_request_ndof": [ctypes.POINTER(Request), ip],
+            "cdg_server_submit": [P, ctypes.POINTER(Request), dp, ctypes.POINTER(ctypes.c_longlong)],
+            "cdg_server_wait": [P, ctypes.c_longlong, ctypes.c_double, ctypes.POINTER(Result)],
+            "cdg_server_counters": [P, ctypes.POINTER(ctypes.c_longlong)],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -445,3 +464,66 @@ class ConvectionDiffusion:
         z = np.zeros_like(v)
         _chk(lib().cdg_problem_precondition(self.p, ctypes.byref(s), _dp(v), _dp(z)))
         return z
+
+
+# ---------------------------------------------------------------------------
+# request server (served form: concurrent stationary solves on one GPU)
+# ---------------------------------------------------------------------------
+def request(dim, order, n, a, s):
+    """A stationary CD solve on the unit square/cube with n cells per
+    direction (n = roots * 2^k, roots 1 or 3); s.multigrid_n_levels <= 0 picks
+    levels down to a 3- or 4-cell coarsest grid."""
+    r = Request()
+    r.dim, r.order, r.n, r.a, r.s = dim, order, n, a, s
+    return r
+
+
+def request_ndof(r):
+    nd = ctypes.c_int()
+    _chk(lib().cdg_request_ndof(ctypes.byref(r), ctypes.byref(nd)))
+    return nd.value
+
+
+class Server:
+    """n_slots workers on one GPU; requests are admitted as slots free up and
+    their problem instances fit the HBM budget (bytes; 0 = 80 % of free)."""
+
+    COUNTERS = ("submitted", "completed", "failed", "queued", "running", "instances",
+                "resident_bytes", "evictions", "budget_bytes", "peak_running", "launches",
+                "classes")
+
+    def __init__(self, device=0, n_slots=4, hbm_budget=0):
+        h = ctypes.c_void_p()
+        _chk(lib().cdg_server_create(device, n_slots, int(hbm_budget), ctypes.byref(h)))
+        self.h = h
+        self._out = {}
+
+    def submit(self, r):
+        """Queue a request; returns its ticket."""
+        out = np.empty(request_ndof(r))
+        t = ctypes.c_longlong()
+        _chk(lib().cdg_server_submit(self.h, ctypes.byref(r), _dp(out), ctypes.byref(t)))
+        self._out[t.value] = out
+        return t.value
+
+    def wait(self, ticket, timeout=-1.0):
+        """(Result, solution) of a finished request, or None after the timeout."""
+        res = Result()
+        rc = lib().cdg_server_wait(self.h, ticket, timeout, ctypes.byref(res))
+        if rc == 1:
+            return None
+        _chk(rc)
+        return res, self._out.pop(ticket)
+
+    def counters(self):
+        c = (ctypes.c_longlong * 12)()
+        _chk(lib().cdg_server_counters(self.h, c))
+        return dict(zip(self.COUNTERS, list(c)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().cdg_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()

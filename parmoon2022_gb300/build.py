@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libparmoon_cd.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["setup.cpp", "assemble.cu", "linalg.cu", "api.cu"]
+SOURCES = ["setup.cpp", "assemble.cu", "linalg.cu", "api.cu", "server.cpp"]
 
 
 def nvcc():
@@ -53,7 +53,7 @@ def build(verbose=False):
         objs = list(ex.map(lambda s: _compile(s, verbose), SOURCES))
     if os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs):
         return LIB
-    cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-cudart", "static"]
+    cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-cudart", "static", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))

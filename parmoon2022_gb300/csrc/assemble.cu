@@ -1094,18 +1094,22 @@ int contract_only(cdg_context* ctx, cdg_problem* p, DevLevel& L, const cdg_assem
   return contract(ctx, k, L, p->d_tables, stiffness_set(k), false, L.val64);
 }
 
-// reference tables for the rhs / error rules, cached per (shape, order, rule)
+// reference tables for the rhs / error rules, cached per (device, shape,
+// order, rule); shared by every problem and thread, never evicted (a few KB
+// per entry, a handful of entries)
 struct DevRefTables {
-  int shape = -1, order = 0, nqp1 = 0;
+  int device = -1, shape = -1, order = 0, nqp1 = 0;
   double* buf = nullptr;
   RhsTables t{};
 };
-static DevRefTables g_rt[8];
+static DevRefTables g_rt[64];
+static std::mutex g_rt_mutex;
 
 static int get_rhs_tables(cdg_context* ctx, int shape, int order, int nqp1, RhsTables* out) {
-  (void)ctx;
+  std::lock_guard<std::mutex> lock(g_rt_mutex);
   for (auto& e : g_rt)
-    if (e.buf && e.shape == shape && e.order == order && e.nqp1 == nqp1) {
+    if (e.buf && e.device == ctx->device && e.shape == shape && e.order == order &&
+        e.nqp1 == nqp1) {
       *out = e.t;
       return CDG_OK;
     }
@@ -1115,8 +1119,7 @@ static int get_rhs_tables(cdg_context* ctx, int shape, int order, int nqp1, RhsT
   DevRefTables* slot = nullptr;
   for (auto& e : g_rt)
     if (!e.buf) { slot = &e; break; }
-  if (!slot) slot = &g_rt[0];
-  if (slot->buf) cudaFree(slot->buf);
+  if (!slot) { set_error("reference table cache full"); return CDG_ERR_LIMIT; }
   CDG_TRY(dalloc(&slot->buf, n));
   std::vector<double> h;
   h.reserve(n);
@@ -1124,7 +1127,10 @@ static int get_rhs_tables(cdg_context* ctx, int shape, int order, int nqp1, RhsT
   h.insert(h.end(), T.w.begin(), T.w.end());
   h.insert(h.end(), T.val.begin(), T.val.end());
   h.insert(h.end(), T.grad.begin(), T.grad.end());
-  CDG_CUDA(cudaMemcpy(slot->buf, h.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+  CDG_CUDA(cudaMemcpyAsync(slot->buf, h.data(), n * sizeof(double), cudaMemcpyHostToDevice,
+                           ctx->stream));
+  CDG_CUDA(cudaStreamSynchronize(ctx->stream));
+  slot->device = ctx->device;
   slot->shape = shape;
   slot->order = order;
   slot->nqp1 = nqp1;

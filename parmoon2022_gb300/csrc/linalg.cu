@@ -1200,7 +1200,9 @@ static int iteration_body(cdg_context* ctx, cdg_problem* p, const cdg_solver_par
 }
 
 static unsigned long long graph_generation(const cdg_problem* p) {
-  unsigned long long gen = p->alloc_gen;
+  // the captured kernels use the context's stream and scratch: a problem
+  // moved to another context is recaptured
+  unsigned long long gen = p->alloc_gen * 1000003ull + (unsigned long long)(uintptr_t)p->ctx;
   for (const DevLevel& L : p->lev)
     gen = gen * 1000003ull + (unsigned long long)L.realloc_count * 7919ull +
           (unsigned long long)(uintptr_t)L.coarse_inv;
