@@ -610,89 +610,108 @@ __device__ int boundary_comp_d(int dim, const double* x) {
   return -1;
 }
 
+// Right-hand side, cell tiles of kRhsTile cells per block.  GB300's FP64 pipe
+// issues one warp instruction per 16 cycles per SM whatever the number of
+// active lanes, so warp-uniform per-cell work (geometry, delta) runs one cell
+// per thread:
+//   phase 1  thread per cell: x0, J, |det J| (inverse and delta for SUPG)
+//   phase 2  (cell, quadrature point): w |det J| f(x_q)
+//   phase 3  (cell, local DOF): F_i = sum_q fw_q (phi_i + delta b.grad phi_i),
+//            Dirichlet values at the nodes, Neumann edge integrals (2D)
+constexpr int kRhsTile = 32;
+constexpr int kRhsGeo = 18;   // x0[3], J[9], |det|, delta, b'[3]
+
 template <int DIM>
 __global__ void __launch_bounds__(256)
 k_rhs(AsmCoefs k, int ncells, int nactive, const double* __restrict__ verts,
       const int* __restrict__ gdof, RhsTables tb, double* __restrict__ rhs,
       double* __restrict__ loc) {
   const int NV = k.shape == kHexa ? 8 : 4;
-  __shared__ double fw[8][128];
-  __shared__ double part[8][32];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int cell = blockIdx.x * 8 + warp;
-  if (cell >= ncells) return;
-  const double* cv = verts + (size_t)cell * NV * DIM;
-  // the FP64 pipe is scarce: the inverse Jacobian only where SUPG or the
-  // Neumann integrals need it
+  __shared__ double geo[kRhsTile][kRhsGeo];
+  __shared__ double fw[kRhsTile][128];
+  const int tile0 = blockIdx.x * kRhsTile;
+  const int nt = min(kRhsTile, ncells - tile0);
   const bool need_inv = k.supg || (DIM == 2 && k.neumann_mask);
-  Affine A;
-  if (need_inv)
-    cell_affine_s(k.shape, DIM, cv, A);
-  else
-    cell_geom_s(k.shape, DIM, cv, A);
-  const double adet = fabs(A.det);
-  const double delta = k.supg ? cell_delta(k, cv, A) : 0.0;
-  double bp[3] = {0, 0, 0};
-  if (delta != 0.0)
-    for (int a = 0; a < DIM; ++a)
-      for (int r = 0; r < DIM; ++r) bp[a] += A.Ji[a][r] * k.b[r];
-  const int nl = k.nloc;
-  const int ng = 32 / nl;
+  if (threadIdx.x < nt) {
+    const int c = threadIdx.x;
+    const double* cv = verts + (size_t)(tile0 + c) * NV * DIM;
+    Affine A;
+    if (need_inv)
+      cell_affine_s(k.shape, DIM, cv, A);
+    else
+      cell_geom_s(k.shape, DIM, cv, A);
+    double* g = geo[c];
+    for (int r = 0; r < 3; ++r) g[r] = r < DIM ? A.x0[r] : 0.0;
+    for (int r = 0; r < 3; ++r)
+      for (int a = 0; a < 3; ++a) g[3 + 3 * r + a] = (r < DIM && a < DIM) ? A.J[r][a] : 0.0;
+    g[12] = fabs(A.det);
+    const double delta = k.supg ? cell_delta(k, cv, A) : 0.0;
+    g[13] = delta;
+    for (int a = 0; a < 3; ++a) {
+      double s = 0.0;
+      if (delta != 0.0 && a < DIM)
+        for (int r = 0; r < DIM; ++r) s += A.Ji[a][r] * k.b[r];
+      g[14 + a] = s;
+    }
+  }
+  __syncthreads();
   // an identically zero source (CDG_EX_BUMP) has a zero volume integral: the
   // quadrature would add exact zeros, so it is not run (same bits)
-  if (k.example != CDG_EX_BUMP) {
-    for (int q = lane; q < k.nqp; q += 32) {
+  const bool zero_f = k.example == CDG_EX_BUMP;
+  const int nqp = k.nqp, nl = k.nloc;
+  if (!zero_f) {
+    for (int t = threadIdx.x; t < nt * nqp; t += blockDim.x) {
+      const int c = t / nqp, q = t - c * nqp;
+      const double* g = geo[c];
       double x[3];
       for (int r = 0; r < DIM; ++r) {
-        double s = A.x0[r];
-        for (int a = 0; a < DIM; ++a) s += A.J[r][a] * tb.xi[q * 3 + a];
+        double s = g[r];
+        for (int a = 0; a < DIM; ++a) s += g[3 + 3 * r + a] * tb.xi[q * 3 + a];
         x[r] = s;
       }
-      fw[warp][q] = tb.w[q] * adet * ex_source(k, x);
+      fw[c][q] = tb.w[q] * g[12] * ex_source(k, x);
     }
-    __syncwarp();
-    // lanes = (basis function i, quadrature group g): 32 / nloc groups split
-    // the quadrature points, partial sums meet in shared memory
-    const int i = lane % nl, g = lane / nl;
-    double F = 0.0;
-    if (g < ng) {
-      if (delta == 0.0) {
-        // Galerkin: w f phi_i
-        for (int q = g; q < k.nqp; q += ng) F = fma(fw[warp][q], tb.val[q * nl + i], F);
-      } else {
-        // SUPG: w f (phi_i + delta b.grad phi_i)
-        for (int q = g; q < k.nqp; q += ng) {
-          double bg = 0.0;
-          for (int a = 0; a < DIM; ++a) bg += bp[a] * tb.grad[(q * DIM + a) * nl + i];
-          F = fma(fw[warp][q], fma(delta, bg, tb.val[q * nl + i]), F);
-        }
-      }
-    }
-    part[warp][lane] = F;
-  } else {
-    part[warp][lane] = 0.0;
   }
-  __syncwarp();
-  if (lane < nl) {
-    double F = 0.0;
-    for (int g = 0; g < ng; ++g) F += part[warp][g * nl + lane];
-    int row = gdof[(size_t)cell * nl + lane];
+  __syncthreads();
+  for (int t = threadIdx.x; t < nt * nl; t += blockDim.x) {
+    const int c = t / nl, i = t - c * nl;
+    const int cell = tile0 + c;
+    const double* g = geo[c];
+    const int row = gdof[(size_t)cell * nl + i];
     if (row >= nactive) {
       // Dirichlet value: nodal functional of Lagrange elements = value at the
       // node (every cell sharing the node writes the same value)
       double r[3], x[3], u[6];
-      ref_node_s(k.shape, DIM, k.order, lane, r);
+      ref_node_s(k.shape, DIM, k.order, i, r);
       for (int rr = 0; rr < DIM; ++rr) {
-        double s = A.x0[rr];
-        for (int a = 0; a < DIM; ++a) s += A.J[rr][a] * r[a];
+        double s = g[rr];
+        for (int a = 0; a < DIM; ++a) s += g[3 + 3 * rr + a] * r[a];
         x[rr] = s;
       }
       ex_exact(k, x, u);
       rhs[row] = u[0];
-      return;
+      continue;
+    }
+    double F = 0.0;
+    if (!zero_f) {
+      const double delta = g[13];
+      if (delta == 0.0) {
+        // Galerkin: w f phi_i
+        for (int q = 0; q < nqp; ++q) F = fma(fw[c][q], tb.val[q * nl + i], F);
+      } else {
+        // SUPG: w f (phi_i + delta b.grad phi_i)
+        for (int q = 0; q < nqp; ++q) {
+          double bg = 0.0;
+          for (int a = 0; a < DIM; ++a) bg += g[14 + a] * tb.grad[(q * DIM + a) * nl + i];
+          F = fma(fw[c][q], fma(delta, bg, tb.val[q * nl + i]), F);
+        }
+      }
     }
     // Neumann data on boundary edges (Assemble2D.C:3210-3248), 2D only
     if (DIM == 2 && k.neumann_mask) {
+      const double* cv = verts + (size_t)cell * NV * DIM;
+      Affine A;
+      cell_affine_s(k.shape, DIM, cv, A);
       const double nrm[4][2] = {{0, -1}, {1, 0}, {0, 1}, {-1, 0}};
       for (int j = 0; j < 4; ++j) {
         const double* a0 = cv + 2 * j;
@@ -712,8 +731,8 @@ k_rhs(AsmCoefs k, int ncells, int nactive, const double* __restrict__ verts,
         double hE = 0.5 * sqrt((a1[0] - a0[0]) * (a1[0] - a0[0]) + (a1[1] - a0[1]) * (a1[1] - a0[1]));
         double G = 0.0;
         for (int l = 0; l < np; ++l) {
-          double s = 0.5 * (lx[l] + 1);
-          double x[2] = {a0[0] + s * (a1[0] - a0[0]), a0[1] + s * (a1[1] - a0[1])};
+          double sp = 0.5 * (lx[l] + 1);
+          double x[2] = {a0[0] + sp * (a1[0] - a0[0]), a0[1] + sp * (a1[1] - a0[1])};
           double u[6];
           ex_exact(k, x, u);
           double gval = k.eps * (nrm[comp][0] * u[1] + nrm[comp][1] * u[2]);
@@ -724,15 +743,13 @@ k_rhs(AsmCoefs k, int ncells, int nactive, const double* __restrict__ verts,
           line_basis_d(k.order, xi[0], v0);
           line_basis_d(k.order, xi[1], v1);
           int n1 = k.order + 1;
-          G += gval * hE * lw[l] * (v0[lane % n1] * v1[lane / n1]);
+          G += gval * hE * lw[l] * (v0[i % n1] * v1[i / n1]);
         }
         F += G;
       }
     }
-    // local rhs entry; the rows gather them in cell order (no atomics: the
-    // cells around a vertex follow one another, same-address atomics would
-    // serialise)
-    loc[(size_t)cell * nl + lane] = F;
+    // local rhs entry; the rows gather them in cell order (no atomics)
+    loc[(size_t)cell * nl + i] = F;
   }
 }
 
@@ -1146,11 +1163,11 @@ static int launch_rhs(cdg_context* ctx, const AsmCoefs& k, DevLevel& L, double* 
   RhsTables tb;
   CDG_TRY(get_rhs_tables(ctx, L.shape, L.order, k.nqp1, &tb));
   if (L.dim == 2)
-    CDG_LAUNCH(ctx, k_rhs<2>, grid_for<int>(L.ncells, 8), 256, 0, k, L.ncells, L.nactive,
-               L.verts, L.gdof, tb, out, L.rhs_loc);
+    CDG_LAUNCH(ctx, k_rhs<2>, grid_for<int>(L.ncells, kRhsTile), 256, 0, k, L.ncells,
+               L.nactive, L.verts, L.gdof, tb, out, L.rhs_loc);
   else
-    CDG_LAUNCH(ctx, k_rhs<3>, grid_for<int>(L.ncells, 8), 256, 0, k, L.ncells, L.nactive,
-               L.verts, L.gdof, tb, out, L.rhs_loc);
+    CDG_LAUNCH(ctx, k_rhs<3>, grid_for<int>(L.ncells, kRhsTile), 256, 0, k, L.ncells,
+               L.nactive, L.verts, L.gdof, tb, out, L.rhs_loc);
   if (L.nactive > 0)
     CDG_LAUNCH(ctx, k_rhs_gather, (int)std::min<long>((L.nactive + 255) / 256, (long)ctx->num_sms * 16),
                256, 0, L.nactive, L.dof_rp, L.dof_ent, L.rhs_loc, out);
