@@ -617,6 +617,8 @@ def run_gpu_serve(args):
     rank, world, local = dist_env()
     dist = init_dist(world)
     torch.cuda.set_device(local)
+    if args.slots:
+        SERVE["slots"] = args.slots
     srv = pg.Server(local, n_slots=SERVE["slots"])
     # warm the pools: one request of every mesh class (hierarchies, device
     # instances, captured graphs), not timed
@@ -688,7 +690,7 @@ def run_gpu_serve(args):
         "dtype": "f64 FGMRES + f32 multigrid (mixed)", "data": "synthetic",
         "config": {"workload": SERVE_WORKLOAD, "slots": SERVE["slots"],
                    "classes": len(SERVE["classes"]), "mean_dofs": ndof_mean,
-                   "l2": "mixed sizes; no flush", "parallelism": "single GPU, 8 streams"},
+                   "l2": "mixed sizes; no flush", "parallelism": "single GPU, %d streams" % SERVE["slots"]},
         "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"], "sweep": sweep,
         "one_at_a_time": {"fp64_solves_per_s": one["fp64"], "mixed_solves_per_s": one["mixed"]},
         "served_over_one_at_a_time_fp64": sat / one["fp64"],
@@ -969,6 +971,8 @@ def main():
                     choices=["cd3d_q2_32", "tcd3d_p2_48", "cd2d_q1_64", "cd3d_q2_96", "serve"])
     ap.add_argument("--profile", action="store_true",
                     help="run one bracketed step for an ncu capture and exit")
+    ap.add_argument("--slots", type=int, default=0,
+                    help="serve: concurrent request slots (default 8)")
     ap.add_argument("--small", action="store_true",
                     help="with --profile: the 24^3x6 tetrahedral mesh (for detailed captures)")
     args = ap.parse_args()

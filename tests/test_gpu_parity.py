@@ -27,9 +27,10 @@ CASES = {
     # name: (dim, order, nref, example, eps, b, c, supg, sdfem, nmask)
     "q1_2d_cd": (2, 1, 4, po.EX_SINE, 1e-2, (1.0, 0.5), 1.0, False, 2, 0),
     "q2_2d_supg": (2, 2, 3, po.EX_SINE, 1e-3, (1.0, 0.5), 0.5, True, 2, 0),
-    # coarse level with 225 active DOFs: the grid-wide (cooperative) inverse;
-    # smaller coarse blocks take the single-CTA shared-memory inverse
     "q2_2d_supg_r4": (2, 2, 4, po.EX_SINE, 1e-3, (1.0, 0.5), 0.5, True, 2, 0),
+    # coarse block of 961 active DOFs: beyond a cluster's shared memory, the
+    # grid-wide Gauss-Jordan; smaller blocks take the cluster kernel
+    "q2_2d_supg_r5": (2, 2, 5, po.EX_SINE, 1e-3, (1.0, 0.5), 0.5, True, 2, 0),
     "q1_2d_neumann": (2, 1, 3, po.EX_SINE_LAPLACE, 1.0, (0.0, 0.0), 0.0, False, 2, 2),
     "q2_2d_neumann": (2, 2, 2, po.EX_SINE_LAPLACE, 1.0, (0.0, 0.0), 0.0, False, 2, 2),
     "q1_3d_cd": (3, 1, 3, po.EX_SINE, 0.1, (1.0, 0.3, -0.2), 1.0, False, 2, 0),
@@ -137,6 +138,7 @@ def test_cd2d_reference_golden_errors_on_gpu(ctx, solver, order):
     ("q1_3d_cd", "multigrid", 3, 30),
     ("q2_3d_supg", "multigrid", 2, 30),
     ("q2_2d_supg_r4", "multigrid", 2, 30),
+    ("q2_2d_supg_r5", "multigrid", 2, 30),
 ])
 def test_solve_parity(ctx, name, prec_name, levels, restart):
     o, h, a = make_pair(name, n_levels=levels)
