@@ -689,208 +689,6 @@ k_gj_smem(int na, const double* __restrict__ Ain, double* __restrict__ inv, int*
   }
 }
 
-// Gauss-Jordan on a thread-block cluster: rows are dealt round-robin to the
-// cluster's CTAs (row i lives in CTA i % cs at local index i / cs) and kept in
-// shared memory; the pivot search, the pivot row and the old row k travel
-// through distributed shared memory.  Per pivot step two cluster barriers:
-// after the candidates, after the broadcast rows.  All CTAs see the same
-// pivots, so every exit (the singular one included) is uniform and comes
-// after a final barrier: no CTA leaves while others may read its memory.
-constexpr int kGjClusterThreads = 256;
-
-__global__ void __launch_bounds__(kGjClusterThreads)
-k_gj_cluster(int na, const double* __restrict__ Ain, double* __restrict__ inv, int* err) {
-  extern __shared__ double sm[];
-  cgrp::cluster_group cl = cgrp::this_cluster();
-  const int cs = (int)cl.num_blocks(), rank = (int)cl.block_rank();
-  const int nloc = (na - rank + cs - 1) / cs;          // rows of this CTA
-  const int rmax = (na + cs - 1) / cs;
-  double* a = sm;                                      // rmax * na
-  double* bufP = a + (size_t)rmax * na;                // pivot row (broadcast)
-  double* bufK = bufP + na;                            // old row k (broadcast)
-  double* prow = bufK + na;                            // scaled pivot row (local)
-  double* oldk = prow + na;                            // old row k (local copy)
-  double* colk = oldk + na;                            // rmax: column k of the local rows
-  int* perm = (int*)(colk + rmax);                     // na
-  __shared__ double cand_v[1];
-  __shared__ int cand_i[1];
-  __shared__ double wv[kGjClusterThreads / 32];
-  __shared__ int wi[kGjClusterThreads / 32];
-  __shared__ int s_p;
-  __shared__ double s_piv;
-  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, w = tid >> 5;
-  for (int t = tid; t < nloc * na; t += nt) {
-    const int li = t / na, j = t - li * na;
-    a[t] = Ain[(size_t)(li * cs + rank) * na + j];
-  }
-  __syncthreads();
-  bool singular = false;
-  for (int k = 0; k < na; ++k) {
-    // 1. local candidate: first row of maximal |a_ik|, i >= k
-    double best = -1.0;
-    int bi = na;
-    for (int li = tid; li < nloc; li += nt) {
-      const int i = li * cs + rank;
-      if (i < k) continue;
-      const double v = fabs(a[(size_t)li * na + k]);
-      if (v > best || (v == best && i < bi)) { best = v; bi = i; }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      double v = __shfl_xor_sync(0xffffffffu, best, o);
-      int vi = __shfl_xor_sync(0xffffffffu, bi, o);
-      if (v > best || (v == best && vi < bi)) { best = v; bi = vi; }
-    }
-    if (lane == 0) { wv[w] = best; wi[w] = bi; }
-    __syncthreads();
-    if (tid == 0) {
-      double b = wv[0];
-      int p = wi[0];
-      for (int u = 1; u < nt / 32; ++u)
-        if (wv[u] > b || (wv[u] == b && wi[u] < p)) { b = wv[u]; p = wi[u]; }
-      cand_v[0] = b;
-      cand_i[0] = p;
-    }
-    cl.sync();
-    // 2. global pivot (same on every CTA): lane r reads CTA r's candidate
-    if (w == 0) {
-      double b = -1.0;
-      int p = na;
-      if (lane < cs) {
-        b = *cl.map_shared_rank(cand_v, lane);
-        p = *cl.map_shared_rank(cand_i, lane);
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        double v = __shfl_xor_sync(0xffffffffu, b, o);
-        int vi = __shfl_xor_sync(0xffffffffu, p, o);
-        if (v > b || (v == b && vi < p)) { b = v; p = vi; }
-      }
-      if (lane == 0) {
-        s_p = p;
-        perm[k] = p;
-      }
-    }
-    __syncthreads();
-    const int p = s_p;
-    // 3. owners publish the pivot row and the old row k
-    if (p % cs == rank)
-      for (int j = tid; j < na; j += nt) bufP[j] = a[(size_t)(p / cs) * na + j];
-    if (k % cs == rank)
-      for (int j = tid; j < na; j += nt) bufK[j] = a[(size_t)(k / cs) * na + j];
-    cl.sync();
-    const double* rP = cl.map_shared_rank(bufP, p % cs);
-    const double* rK = cl.map_shared_rank(bufK, k % cs);
-    if (tid == 0) s_piv = rP[k];
-    __syncthreads();
-    const double piv = s_piv;
-    if (piv == 0.0) {
-      singular = true;
-      break;   // uniform: every CTA read the same pivot value
-    }
-    const double rpiv = 1.0 / piv;
-    for (int j = tid; j < na; j += nt) prow[j] = j == k ? rpiv : rP[j] * rpiv;
-    const bool own_p = (p % cs == rank) && p != k;
-    if (own_p)
-      for (int j = tid; j < na; j += nt) oldk[j] = rK[j];
-    // multipliers first: the pass below overwrites column k
-    for (int li = tid; li < nloc; li += nt) {
-      const int i = li * cs + rank;
-      colk[li] = (i == p && p != k) ? rK[k] : a[(size_t)li * na + k];
-    }
-    __syncthreads();
-    // 4. eliminate the local rows i != k (row p takes the old row k)
-    for (int t = tid; t < nloc * na; t += nt) {
-      const int li = t / na, j = t - li * na;
-      const int i = li * cs + rank;
-      if (i == k) continue;
-      const double* src = (i == p) ? oldk : a + (size_t)li * na;
-      const double f = colk[li];
-      const double old = src[j];
-      a[t] = j == k ? -f * rpiv : fma(-f, prow[j], old);
-    }
-    __syncthreads();
-    if (k % cs == rank)
-      for (int j = tid; j < na; j += nt) a[(size_t)(k / cs) * na + j] = prow[j];
-    __syncthreads();
-  }
-  if (singular) {
-    if (rank == 0 && tid == 0) atomicOr(err, kErrSingular);
-    cl.sync();
-    return;
-  }
-  // column exchanges in reverse pivot order, then the local rows out
-  int* q = (int*)prow;   // prow is free now (na ints fit in na doubles)
-  if (tid == 0) {
-    for (int j = 0; j < na; ++j) q[j] = j;
-    for (int k = na - 1; k >= 0; --k) {
-      const int t = q[k];
-      q[k] = q[perm[k]];
-      q[perm[k]] = t;
-    }
-  }
-  __syncthreads();
-  for (int t = tid; t < nloc * na; t += nt) {
-    const int li = t / na, j = t - li * na;
-    inv[(size_t)(li * cs + rank) * na + j] = a[(size_t)li * na + q[j]];
-  }
-  cl.sync();   // no CTA leaves while another may still read its buffers
-}
-
-static size_t gj_cluster_bytes(int na, int cs) {
-  const size_t rmax = (na + cs - 1) / cs;
-  return rmax * na * sizeof(double) + 4 * (size_t)na * sizeof(double) + rmax * sizeof(double) +
-         (size_t)na * sizeof(int);
-}
-
-// launch on a cluster of 16 (or 8) CTAs when the rows fit; false if not
-static bool gj_cluster_launch(cdg_context* ctx, int na, const double* A, double* inv, int* rc) {
-  *rc = CDG_OK;
-  static const int allow16 = [] {
-    const int ok = cudaFuncSetAttribute(k_gj_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed,
-                                        1) == cudaSuccess ? 1 : 0;
-    cudaGetLastError();
-    return ok;
-  }();
-  for (int cs : {16, 8}) {
-    if (cs == 16 && !allow16) continue;
-    const size_t smem = gj_cluster_bytes(na, cs);
-    if (smem > 200 * 1024) continue;
-    if (cudaFuncSetAttribute(k_gj_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)smem) != cudaSuccess) {
-      cudaGetLastError();
-      continue;
-    }
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(cs);
-    cfg.blockDim = dim3(kGjClusterThreads);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = ctx->stream;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = cs;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    int nclusters = 0;
-    if (cudaOccupancyMaxActiveClusters(&nclusters, k_gj_cluster, &cfg) != cudaSuccess ||
-        nclusters < 1) {
-      cudaGetLastError();
-      continue;
-    }
-    cudaError_t e = cudaLaunchKernelEx(&cfg, k_gj_cluster, na, A, inv, ctx->d_err);
-    if (e != cudaSuccess) {
-      set_error("cluster Gauss-Jordan launch: %s", cudaGetErrorString(e));
-      *rc = CDG_ERR_CUDA;
-      return true;
-    }
-    ctx->launches++;
-    return true;
-  }
-  return false;
-}
-
 static size_t gj_smem_bytes(int na) {
   return (size_t)na * na * sizeof(double) + 2 * (size_t)na * sizeof(double) +
          2 * (size_t)na * sizeof(int);
@@ -913,24 +711,24 @@ static int coarse_inverse(cdg_context* ctx, DevLevel& C) {
   int* q = perm + na;
   CDG_CUDA(cudaMemsetAsync(A, 0, sz * sizeof(double), ctx->stream));
   CDG_LAUNCH(ctx, k_extract_dense, grid_for<int>(na, 128), 128, 0, na, C.row_ptr, C.col, C.val64, A);
-  // a cluster of CTAs when the active block fits their shared memory (16x
-  // the FP64 issue of one SM); otherwise one CTA (small blocks on devices
-  // without clusters) or the grid-wide kernel
-  {
-    int rc = CDG_OK;
-    if (gj_cluster_launch(ctx, na, A, C.coarse_inv, &rc)) return rc;
-  }
+  // the grid-wide kernel (a pivot step costs one grid sync); one CTA holding
+  // the block in shared memory where cooperative launches are unavailable.
+  // Measured on GB300: grid-wide 0.54 ms (125 rows) / 2.25 ms (343 rows), one
+  // CTA 2.2 ms (125, one SM's FP64 pipe), a 16-CTA cluster with the rows in
+  // distributed shared memory 0.71 / 3.56 ms (barriers per pivot step)
+  int coop = 0, per_sm = 0;
+  CDG_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device));
+  CDG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gj_coop, 256, 0));
+  // one block per row up to one (or two) per SM: the elimination (na^2 FMA
+  // per step) is bound by FP64 issue, so it wants every SM's pipe (32 blocks
+  // measured 1.9x slower at 343 rows)
+  int g = (int)std::min<long>((long)na, (long)ctx->num_sms * std::min(per_sm, na > 1024 ? 2 : 1));
   const size_t smem = gj_smem_bytes(na);
-  if (smem <= 220 * 1024) {
+  if (!(coop && per_sm > 0) && smem <= 220 * 1024) {
     CDG_CUDA(cudaFuncSetAttribute(k_gj_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     CDG_LAUNCH(ctx, k_gj_smem, 1, kGjSmemThreads, smem, na, A, C.coarse_inv, ctx->d_err);
     return CDG_OK;
   }
-  int coop = 0, per_sm = 0;
-  CDG_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device));
-  CDG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gj_coop, 256, 0));
-  // one block per row up to one (or two) per SM: fewer blocks, cheaper grid syncs
-  int g = (int)std::min<long>((long)na, (long)ctx->num_sms * std::min(per_sm, na > 1024 ? 2 : 1));
   if (coop && per_sm > 0 && g >= 1) {
     double* inv = C.coarse_inv;
     void* args[] = {(void*)&na, (void*)&A, (void*)&B, (void*)&perm, (void*)&q, (void*)&inv,
