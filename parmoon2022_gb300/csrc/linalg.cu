@@ -1280,6 +1280,8 @@ static int read_state(cdg_context* ctx, const GmresState& g, int* st4, double* r
   return CDG_OK;
 }
 
+constexpr int kGraphUnavailable = 1;   // internal: use the host loop
+
 static int fgmres_graph(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s,
                         cdg_solve_stats* st) {
   DevLevel& L = p->lev[0];
@@ -1290,7 +1292,11 @@ static int fgmres_graph(cdg_context* ctx, cdg_problem* p, const cdg_solver_param
   double* beta_d = g.scal + 1;
   const int vg = vec_grid(ctx, n);
   const ConvParams cp = conv_params(s);
-  CDG_TRY(ensure_iteration_graph(ctx, p, s));
+  // a graph that cannot be built (capture rejected) falls back to the host loop
+  if (ensure_iteration_graph(ctx, p, s) != CDG_OK) {
+    cudaGetLastError();
+    return kGraphUnavailable;
+  }
   // r = b - A x; beta = ||r||; the test at iteration 0
   CDG_TRY(residual64(ctx, L, b, x, g.w));
   CDG_TRY(dot64(ctx, n, g.w, nullptr, beta_d, 0));
@@ -1360,8 +1366,10 @@ int fgmres(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s, cdg_sol
     return e && e[0] == '0';
   }();
   if (!graph_off && s.gram_schmidt == 0 &&
-      !(s.preconditioner == 2 && s.multigrid_smoother_coarse != 0))
-    return fgmres_graph(ctx, p, s, st);
+      !(s.preconditioner == 2 && s.multigrid_smoother_coarse != 0)) {
+    const int rc = fgmres_graph(ctx, p, s, st);
+    if (rc != kGraphUnavailable) return rc;
+  }
   GmresState& g = p->gm;
   double* x = L.sol;
   const double* b = L.rhs;
