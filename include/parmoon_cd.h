@@ -73,6 +73,10 @@ typedef struct {
                            b_grad[3i+j] x_j (zero: constant field)           */
   double t;             /* time at which f and the boundary data are taken   */
   double ic[4];         /* CDG_EX_BUMP: centre x, y, z and sigma              */
+  double time_step;     /* TIMESTEPLENGTH: the time step the SUPG parameter of
+                           the time-dependent routines takes at
+                           cdg_problem_tcd_initialize (each step uses its own
+                           tau); ignored by the stationary problem          */
 } cdg_assembly_params;
 
 /* Solver ParameterDatabase keys (src/Solver/Solver.C:26-209,
@@ -211,11 +215,14 @@ int cdg_problem_errors_noalloc(cdg_problem *p, const cdg_assembly_params *a,
 /* assemble_initial_time (src/System/TimeConvectionDiffusion.C:260-311): on
  * every level stiffness, mass and rhs at time a->t (Dirichlet rows assembled
  * in full); the finest solution becomes the interpolant of the example's
- * initial condition */
+ * initial condition.  With SUPG (TCDStiffSUPG, TCDMassSUPG, TCDRhsSUPG,
+ * src/General/CD_local_assembling_routines.C:184-387) the stabilisation
+ * parameter uses theta1 * a->time_step, which must then be positive */
 int cdg_problem_tcd_initialize(cdg_problem *p, const cdg_assembly_params *a);
 /* one Crank-Nicolson step to time a->t = t_old + tau
  * (TimeConvectionDiffusion.C:315-450, TimeDiscretizations.C:117-283):
- * reassemble stiffness and rhs on every level, rhs = tau/2 (f_new + f_old) +
+ * reassemble stiffness and rhs on every level (with SUPG the mass matrix too,
+ * with the parameter of this tau), rhs = tau/2 (f_new + f_old) +
  * M u_old - tau/2 A u_old on active rows, system M + tau/2 A on active rows,
  * Dirichlet data at the new time, then Solver::solve warm-started from u_old */
 int cdg_problem_tcd_step(cdg_problem *p, const cdg_assembly_params *a, double tau,

@@ -309,6 +309,8 @@ struct orc_problem {
   quad_rule qr;
   int nqp1;
   int asm_gen;      /* incremented by every orc_assemble */
+  int tcd;          /* assembling for the time-dependent problem */
+  double ttau;      /* THETA1 * CURRENTTIMESTEPLENGTH (Crank-Nicolson: tau/2) */
 };
 
 static int nverts(int dim) { return dim == 2 ? 4 : 8; }
@@ -1232,6 +1234,32 @@ static double sdfem_delta(const orc_config *c, double hK, double eps,
   return delta;
 }
 
+/* the stabilisation parameter of TCDStiffSUPG, TCDMassSUPG and TCDRhsSUPG
+ * (CD_local_assembling_routines.C:184-387): in 2D, except for SDFEM_TYPE 2
+ * and 12, Compute_SDFEM_delta takes the coefficients scaled by theta1 * tau
+ * (reaction 1 + theta1 tau c, type 8: theta1 tau c); the L_inf norm of b is
+ * always the scaled one in 2D.  Then delta *= theta1 * tau except for the
+ * types 2, 9, 10, 11, 12. */
+static double tcd_delta(const orc_problem *p, double hK, double eps, const double *b,
+                        double react, double linfb) {
+  const orc_config *c = &p->cfg;
+  const double tt = p->ttau;
+  const int ty = c->sdfem_type;
+  double delta;
+  if (c->dim == 2) {
+    double bs[3] = {tt * b[0], tt * b[1], 0};
+    double bb = fabs(bs[0]) > fabs(bs[1]) ? fabs(bs[0]) : fabs(bs[1]);
+    if (ty != 2 && ty != 12)
+      delta = sdfem_delta(c, hK, tt * eps, bs, ty == 8 ? tt * react : 1.0 + tt * react, bb);
+    else
+      delta = sdfem_delta(c, hK, eps, b, react, bb);
+  } else {
+    delta = sdfem_delta(c, hK, eps, b, react, linfb);
+  }
+  if (ty != 2 && ty != 9 && ty != 10 && ty != 11 && ty != 12) delta *= tt;
+  return delta;
+}
+
 int orc_local_system(orc_problem *p, int level, int cell, double *Aloc,
                      double *floc) {
   const orc_config *c = &p->cfg;
@@ -1296,8 +1324,10 @@ int orc_local_system(orc_problem *p, int level, int cell, double *Aloc,
       }
     }
     if (c->supg) {
-      /* BilinearAssemble_SD<d> (ConvDiff.C:1886-1999) */
-      double delta = sdfem_delta(c, hK, eps, b, react, co[dim + 3]);
+      /* BilinearAssemble_SD<d> (ConvDiff.C:1886-1999); the time-dependent
+       * TCDStiffSUPG / TCDRhsSUPG have the same form with their own delta */
+      double delta = p->tcd ? tcd_delta(p, hK, eps, b, react, co[dim + 3])
+                            : sdfem_delta(c, hK, eps, b, react, co[dim + 3]);
       for (int i = 0; i < nl; ++i) {
         double bgradv = 0;
         for (int r = 0; r < dim; ++r) bgradv += b[r] * g[i][r];
@@ -1356,20 +1386,39 @@ static void neumann_edge(orc_problem *p, level_t *L, int cell, int j,
 }
 
 /* local mass matrix, TCDMass (CD_local_assembling_routines.C:156-167):
- * M_ij = int phi_i phi_j */
+ * M_ij = int phi_i phi_j; with SUPG plus TCDMassSUPG (:261-321):
+ * int delta (b . grad phi_i) phi_j */
 static void local_mass(orc_problem *p, level_t *L, int cell, double *Mloc) {
-  int dim = p->cfg.dim, nl = L->nloc;
+  const orc_config *c = &p->cfg;
+  int dim = c->dim, nl = L->nloc;
   const double *cv = L->verts + (size_t)cell * L->nv * dim;
   affine_t A;
   cell_affine_s(p->shape, dim, cv, &A);
   double adet = fabs(A.det);
+  double hK = cell_hK_s(p->shape, dim, cv, c->cell_measure);
   for (int i = 0; i < nl * nl; ++i) Mloc[i] = 0;
   double ref[MAXLOC][NDER];
   for (int q = 0; q < p->qr.nqp; ++q) {
-    basis_s(p->shape, dim, p->cfg.order, p->qr.xi[q], ref);
+    basis_s(p->shape, dim, c->order, p->qr.xi[q], ref);
     double Mult = p->qr.w[q] * adet;
     for (int i = 0; i < nl; ++i)
       for (int j = 0; j < nl; ++j) Mloc[i * nl + j] += Mult * ref[j][0] * ref[i][0];
+    if (!c->supg) continue;
+    double x[3], co[8];
+    affine_map(dim, &A, p->qr.xi[q], x);
+    coeffs_at(c, x, co);
+    double b[3] = {co[1], co[2], dim == 3 ? co[3] : 0};
+    double delta = tcd_delta(p, hK, co[0], b, co[dim + 1], co[dim + 3]);
+    for (int i = 0; i < nl; ++i) {
+      double bgradv = 0;
+      for (int r = 0; r < dim; ++r) {
+        double gr = 0;
+        for (int a = 0; a < dim; ++a) gr += A.Jinv[a][r] * ref[i][1 + a];
+        bgradv += b[r] * gr;
+      }
+      bgradv *= delta;
+      for (int j = 0; j < nl; ++j) Mloc[i * nl + j] += Mult * ref[j][0] * bgradv;
+    }
   }
 }
 
@@ -1479,6 +1528,7 @@ static int assemble_level(orc_problem *p, int level) {
 
 int orc_assemble(orc_problem *p) {
   p->asm_gen++;
+  p->tcd = 0;
   for (int k = 0; k < p->nlev; ++k)
     if (assemble_level(p, k)) return -1;
   return 0;
@@ -2029,7 +2079,12 @@ static void ensure_tcd(level_t *L) {
  * rhs at cfg.t on every level, old_rhs = rhs, then the initial condition
  * interpolated into the finest solution (every DOF) */
 int orc_tcd_initialize(orc_problem *p) {
-  if (p->cfg.supg) FAIL("SUPG for the time-dependent problem is not supported");
+  if (p->cfg.supg) {
+    if (!(p->cfg.time_step > 0)) FAIL("SUPG for the time-dependent problem needs the time step");
+    if (p->cfg.sdfem_type >= 9 && p->cfg.sdfem_type <= 12) FAIL("SDFEM_TYPE not supported");
+  }
+  p->tcd = 1;
+  p->ttau = 0.5 * p->cfg.time_step;
   for (int k = 0; k < p->nlev; ++k) {
     level_t *L = &p->lev[k];
     ensure_tcd(L);
@@ -2060,9 +2115,13 @@ int orc_tcd_step(orc_problem *p, double t_new, double tau, const orc_solver_conf
   if (!p->lev[0].tA) FAIL("call orc_tcd_initialize first");
   if (!(tau > 0)) FAIL("time step must be positive");
   p->cfg.t = t_new;
+  p->tcd = 1;
+  p->ttau = 0.5 * tau;
+  /* with SUPG the mass matrix is reassembled too (TimeConvectionDiffusion.C
+   * assemble: TCDStiffMassRhs, assemble_both) */
   for (int k = 0; k < p->nlev; ++k) {
     level_t *L = &p->lev[k];
-    if (assemble_into(p, k, L->tA, L->tf, 1, NULL)) return -1;
+    if (assemble_into(p, k, L->tA, L->tf, 1, p->cfg.supg ? L->tM : NULL)) return -1;
   }
   level_t *F = &p->lev[0];
   double ht = 0.5 * tau;

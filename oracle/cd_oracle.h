@@ -49,6 +49,7 @@ typedef struct {
   double b_grad[9];    /* b_i(x) = b[i] + sum_j b_grad[3i+j] x_j              */
   double t;            /* time of f and the boundary data                     */
   double ic[4];        /* ORC_EX_BUMP centre and sigma                        */
+  double time_step;    /* TIMESTEPLENGTH at orc_tcd_initialize (SUPG only)    */
 } orc_config;
 
 typedef struct {

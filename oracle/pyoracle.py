@@ -26,7 +26,7 @@ class Config(ctypes.Structure):
         ("problem_linear", ctypes.c_int), ("neumann_mask", ctypes.c_int),
         ("poly_degree", ctypes.c_int), ("tetra", ctypes.c_int),
         ("b_grad", ctypes.c_double * 9), ("t", ctypes.c_double),
-        ("ic", ctypes.c_double * 4),
+        ("ic", ctypes.c_double * 4), ("time_step", ctypes.c_double),
     ]
 
 
@@ -109,7 +109,7 @@ def _ip(a):
 def make_config(dim, order, nref, example, eps=1.0, b=(0, 0, 0), c=0.0, freq=1.0,
                 supg=False, sdfem_type=2, delta0=1.0, delta1=1.0, cell_measure=0,
                 problem_linear=0, neumann_mask=0, poly_degree=0, tetra=False,
-                b_grad=None, t=0.0, ic=(0.5, 0.5, 0.5, 0.1)):
+                b_grad=None, t=0.0, ic=(0.5, 0.5, 0.5, 0.1), time_step=0.0):
     cfg = Config()
     cfg.dim, cfg.order, cfg.nref, cfg.example = dim, order, nref, example
     cfg.eps = eps
@@ -125,6 +125,7 @@ def make_config(dim, order, nref, example, eps=1.0, b=(0, 0, 0), c=0.0, freq=1.0
         for i in range(9):
             cfg.b_grad[i] = float(bg[i])
     cfg.t = t
+    cfg.time_step = time_step
     for i in range(4):
         cfg.ic[i] = ic[i]
     return cfg

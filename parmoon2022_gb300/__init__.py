@@ -62,6 +62,7 @@ class AssemblyParams(ctypes.Structure):
         ("cell_measure", ctypes.c_int), ("problem_linear", ctypes.c_int),
         ("neumann_mask", ctypes.c_int), ("poly_degree", ctypes.c_int),
         ("b_grad", ctypes.c_double * 9), ("t", ctypes.c_double), ("ic", ctypes.c_double * 4),
+        ("time_step", ctypes.c_double),
     ]
 
 
@@ -179,7 +180,7 @@ def _ip(a):
 def assembly_params(example=EX_SINE, eps=1.0, b=(0.0, 0.0, 0.0), c=0.0, freq=1.0,
                     space_discretization_type="galerkin", sdfem_type=2, delta0=1.0, delta1=1.0,
                     cell_measure=0, problem_linear=0, neumann_mask=0, poly_degree=0,
-                    b_grad=None, t=0.0, ic=(0.0, 0.0, 0.0, 1.0)):
+                    b_grad=None, t=0.0, ic=(0.0, 0.0, 0.0, 1.0), time_step=0.0):
     """b_grad: 3x3 gradient of a convection field linear in x (row-major)."""
     a = AssemblyParams()
     if b_grad is not None:
@@ -187,6 +188,7 @@ def assembly_params(example=EX_SINE, eps=1.0, b=(0.0, 0.0, 0.0), c=0.0, freq=1.0
         for i in range(9):
             a.b_grad[i] = g[i]
     a.t = t
+    a.time_step = time_step
     for i in range(4):
         a.ic[i] = ic[i]
     a.example, a.eps = example, eps

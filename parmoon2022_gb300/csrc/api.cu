@@ -462,7 +462,7 @@ int cdg_problem_tcd_initialize(cdg_problem* p, const cdg_assembly_params* a) {
   CDG_CUDA(cudaSetDevice(p->ctx->device));
   CDG_CUDA(cudaMemsetAsync(p->d_zero_diag, 0, sizeof(int), p->ctx->stream));
   for (auto& L : p->lev) {
-    CDG_TRY(tcd_assemble_level(p->ctx, p, L, *a, true));
+    CDG_TRY(tcd_assemble_level(p->ctx, p, L, *a, true, a->time_step));
     // old_rhs = rhs
     CDG_CUDA(cudaMemcpyAsync(L.tcd_fold, L.tcd_f, (size_t)L.ndof * sizeof(double),
                              cudaMemcpyDeviceToDevice, p->ctx->stream));
@@ -481,8 +481,9 @@ int cdg_problem_tcd_step(cdg_problem* p, const cdg_assembly_params* a, double ta
   auto t0 = std::chrono::steady_clock::now();
   cudaStream_t stm = p->ctx->stream;
   CDG_CUDA(cudaMemsetAsync(p->d_zero_diag, 0, sizeof(int), stm));
-  // reassemble stiffness and rhs on every level (mass is time independent)
-  for (auto& L : p->lev) CDG_TRY(tcd_assemble_level(p->ctx, p, L, *a, false));
+  // reassemble stiffness and rhs on every level (the Galerkin mass is time
+  // independent; the SUPG mass is reassembled with this tau)
+  for (auto& L : p->lev) CDG_TRY(tcd_assemble_level(p->ctx, p, L, *a, false, tau));
   DevLevel& F = p->lev[0];
   CDG_TRY(tcd_cn_rhs(p->ctx, F, tau));
   // solution.copy_nonactive(rhs): Dirichlet data at the new time

@@ -41,6 +41,8 @@ struct AsmCoefs {
   int dim, shape, order, nloc, example, supg, sdfem_type, cell_measure, poly_degree,
       neumann_mask, nqp, nqp1, n_sym, linear_b;
   double eps, b[3], bg[9], c, freq, delta0, delta1, t, ic[4];
+  int tcd;        // time-dependent assembly (SUPG parameter of the TCD routines)
+  double ttau;    // theta1 * time step (Crank-Nicolson: theta1 = 1/2)
 };
 
 static AsmCoefs make_coefs(const cdg_assembly_params& a, int shape, int order) {
@@ -51,6 +53,8 @@ static AsmCoefs make_coefs(const cdg_assembly_params& a, int shape, int order) {
   k.nloc = n_local_dofs(shape, order);
   k.example = a.example;
   k.supg = a.supg;
+  k.tcd = 0;
+  k.ttau = 0.0;
   k.sdfem_type = a.sdfem_type;
   k.cell_measure = a.cell_measure;
   k.poly_degree = a.poly_degree > 0 ? a.poly_degree : order;
@@ -347,7 +351,26 @@ __device__ double cell_delta(const AsmCoefs& k, const double* cv, const Affine& 
   double h = cell_hK_s(k.shape, k.dim, cv, k.cell_measure, A.det);
   double linfb = fmax(fabs(k.b[0]), fabs(k.b[1]));
   if (k.dim == 3) linfb = fmax(linfb, fabs(k.b[2]));
-  return sdfem_delta(k, h, k.eps, k.b, k.c, linfb);
+  if (!k.tcd) return sdfem_delta(k, h, k.eps, k.b, k.c, linfb);
+  // TCDStiffSUPG / TCDMassSUPG / TCDRhsSUPG (CD_local_assembling_routines.C:
+  // 184-387): in 2D the coefficients are scaled by theta1*tau first (except
+  // SDFEM_TYPE 2 and 12, which keep them but take the scaled L_inf norm);
+  // then delta *= theta1*tau except for the types 2, 9, 10, 11, 12
+  const int ty = k.sdfem_type;
+  double delta;
+  if (k.dim == 2) {
+    const double bs[3] = {k.ttau * k.b[0], k.ttau * k.b[1], 0.0};
+    const double bb = fmax(fabs(bs[0]), fabs(bs[1]));
+    if (ty != 2 && ty != 12)
+      delta = sdfem_delta(k, h, k.ttau * k.eps, bs,
+                          ty == 8 ? k.ttau * k.c : 1.0 + k.ttau * k.c, bb);
+    else
+      delta = sdfem_delta(k, h, k.eps, k.b, k.c, bb);
+  } else {
+    delta = sdfem_delta(k, h, k.eps, k.b, k.c, linfb);
+  }
+  if (ty != 2 && ty != 9 && ty != 10 && ty != 11 && ty != 12) delta *= k.ttau;
+  return delta;
 }
 
 // term blocks of RefTensors: S (ns), C (d), M (1), L (d*d), D (d), T (ns*d)
@@ -359,17 +382,28 @@ struct Terms {
   static constexpr int NT = offT + NS * DIM;
 };
 
-// per-cell factors g_t of the contraction; mass_only: g = |det J| on M
+// per-cell factors g_t of the contraction.  mode 0: the stiffness terms;
+// mode 1: mass, g = |det J| on M; mode 2: mass with the SUPG mass term of the
+// time-dependent problem (TCDMassSUPG): delta (b.grad phi_i) phi_j, the D
+// block with factor 1 in place of the reaction
 template <int DIM>
 __device__ void cell_factors(const AsmCoefs& k, const double* __restrict__ cv, double* g,
-                             bool mass_only) {
+                             int mode) {
   using TT = Terms<DIM>;
   Affine A;
   cell_affine_s(k.shape, DIM, cv, A);
   const double adet = fabs(A.det);
-  if (mass_only) {
+  if (mode != 0) {
     for (int t = 0; t < TT::NT; ++t) g[t] = 0.0;
     g[TT::offM] = adet;
+    if (mode == 2) {
+      const double delta = cell_delta(k, cv, A);
+      for (int a = 0; a < DIM; ++a) {
+        double s = 0;
+        for (int r = 0; r < DIM; ++r) s += A.Ji[a][r] * k.b[r];
+        g[TT::offD + a] = adet * delta * s;
+      }
+    }
     return;
   }
   const double delta = cell_delta(k, cv, A);
@@ -492,7 +526,7 @@ struct TermList {
 
 template <int DIM, int NLOC, int NTU>
 __global__ void __launch_bounds__(256)
-k_element_contract(AsmCoefs k, TermList tl, int mass_only, int all_rows, int ncells,
+k_element_contract(AsmCoefs k, TermList tl, int mode, int all_rows, int ncells,
                    int nactive, const double* __restrict__ verts, const int* __restrict__ gdof,
                    const int* __restrict__ slot, const double* __restrict__ R,
                    double* __restrict__ val) {
@@ -504,7 +538,7 @@ k_element_contract(AsmCoefs k, TermList tl, int mass_only, int all_rows, int nce
   // phase 1: per-cell factors
   for (int c = threadIdx.x; c < kCellTile; c += blockDim.x) {
     int cell = tile0 + c;
-    if (cell < ncells) cell_factors<DIM>(k, verts + (size_t)cell * NV * DIM, g[c], mass_only);
+    if (cell < ncells) cell_factors<DIM>(k, verts + (size_t)cell * NV * DIM, g[c], mode);
   }
   __syncthreads();
   const int e_local = threadIdx.x % S::EPB;
@@ -1044,17 +1078,18 @@ static int ensure_tables(cdg_context* ctx, cdg_problem* p) {
 // contraction of the terms in `tl` (count NTU) into val
 template <int DIM, int NLOC, int NTU>
 static int launch_terms(cdg_context* ctx, const AsmCoefs& k, DevLevel& L, const double* R,
-                        const TermList& tl, bool mass_only, bool all_rows, double* out) {
+                        const TermList& tl, int mode, bool all_rows, double* out) {
   using S = ShapeInfo<NLOC>;
   dim3 grid((L.ncells + kCellTile - 1) / kCellTile, S::NEB);
   CDG_LAUNCH(ctx, (k_element_contract<DIM, NLOC, NTU>), grid, S::THREADS, 0, k, tl,
-             mass_only ? 1 : 0, all_rows ? 1 : 0, L.ncells, L.nactive, L.verts, L.gdof,
+             mode, all_rows ? 1 : 0, L.ncells, L.nactive, L.verts, L.gdof,
              L.slot, R, out);
   return CDG_OK;
 }
 
-// term selection: galerkin (S, C, M [, L]), supg (S, C, M, D, T), mass (M)
-enum class TermSet { Galerkin, GalerkinLinear, Supg, Mass };
+// term selection: galerkin (S, C, M [, L]), supg (S, C, M, D, T), mass (M),
+// mass with the SUPG mass term (M, D)
+enum class TermSet { Galerkin, GalerkinLinear, Supg, Mass, MassSupg };
 
 template <int DIM, int NLOC>
 static int contract_set(cdg_context* ctx, const AsmCoefs& k, DevLevel& L, const double* R,
@@ -1064,18 +1099,23 @@ static int contract_set(cdg_context* ctx, const AsmCoefs& k, DevLevel& L, const 
   int n = 0;
   if (set == TermSet::Mass) {
     tl.idx[n++] = TT::offM;
-    return launch_terms<DIM, NLOC, 1>(ctx, k, L, R, tl, true, all_rows, out);
+    return launch_terms<DIM, NLOC, 1>(ctx, k, L, R, tl, 1, all_rows, out);
+  }
+  if (set == TermSet::MassSupg) {
+    tl.idx[n++] = TT::offM;
+    for (int a = 0; a < DIM; ++a) tl.idx[n++] = TT::offD + a;
+    return launch_terms<DIM, NLOC, 1 + DIM>(ctx, k, L, R, tl, 2, all_rows, out);
   }
   for (int t = 0; t < TT::offL; ++t) tl.idx[n++] = t;   // S, C, M
   if (set == TermSet::GalerkinLinear) {
     for (int t = TT::offL; t < TT::offD; ++t) tl.idx[n++] = t;
-    return launch_terms<DIM, NLOC, TT::offD>(ctx, k, L, R, tl, false, all_rows, out);
+    return launch_terms<DIM, NLOC, TT::offD>(ctx, k, L, R, tl, 0, all_rows, out);
   }
   if (set == TermSet::Supg) {
     for (int t = TT::offD; t < TT::NT; ++t) tl.idx[n++] = t;
-    return launch_terms<DIM, NLOC, TT::NT - DIM * DIM>(ctx, k, L, R, tl, false, all_rows, out);
+    return launch_terms<DIM, NLOC, TT::NT - DIM * DIM>(ctx, k, L, R, tl, 0, all_rows, out);
   }
-  return launch_terms<DIM, NLOC, TT::offL>(ctx, k, L, R, tl, false, all_rows, out);
+  return launch_terms<DIM, NLOC, TT::offL>(ctx, k, L, R, tl, 0, all_rows, out);
 }
 
 static int contract(cdg_context* ctx, const AsmCoefs& k, DevLevel& L, const double* R,
@@ -1255,19 +1295,31 @@ int tcd_interpolate(cdg_context* ctx, cdg_problem* p, const cdg_assembly_params&
 // TimeConvectionDiffusion::call_assembling_routine with assemble_dirichlet_rows
 // (TimeConvectionDiffusion.C:987-1052): stiffness (and mass) with full
 // Dirichlet rows, rhs f at time a.t
+// With SUPG (TCDStiffSUPG, TCDMassSUPG, TCDRhsSUPG) the stabilisation
+// parameter depends on theta1 * tau, and the mass matrix carries a SUPG term,
+// so it is reassembled with every step (TimeConvectionDiffusion.C:315-346).
 int tcd_assemble_level(cdg_context* ctx, cdg_problem* p, DevLevel& L,
-                       const cdg_assembly_params& a, bool with_mass) {
+                       const cdg_assembly_params& a, bool with_mass, double tau) {
   CDG_TRY(ensure_tables(ctx, p));
   CDG_TRY(ensure_tcd(L));
   AsmCoefs k = make_coefs(a, L.shape, L.order);
   CDG_TRY(check_coefs(k));
-  if (k.supg) { set_error("SUPG for the time-dependent problem is not supported"); return CDG_ERR_ARG; }
+  k.tcd = 1;
+  k.ttau = 0.5 * tau;
+  if (k.supg) {
+    if (!(tau > 0)) { set_error("SUPG for the time-dependent problem needs the time step"); return CDG_ERR_ARG; }
+    if (k.sdfem_type >= 9 && k.sdfem_type <= 12) {
+      set_error("SDFEM_TYPE %d (time-step dependent) is not supported", k.sdfem_type);
+      return CDG_ERR_ARG;
+    }
+  }
   cudaStream_t st = ctx->stream;
   CDG_CUDA(cudaMemsetAsync(L.tcd_A, 0, (size_t)L.nnz * sizeof(double), st));
   CDG_TRY(contract(ctx, k, L, p->d_tables, stiffness_set(k), true, L.tcd_A));
-  if (with_mass) {
+  if (with_mass || k.supg) {
     CDG_CUDA(cudaMemsetAsync(L.tcd_M, 0, (size_t)L.nnz * sizeof(double), st));
-    CDG_TRY(contract(ctx, k, L, p->d_tables, TermSet::Mass, true, L.tcd_M));
+    CDG_TRY(contract(ctx, k, L, p->d_tables, k.supg ? TermSet::MassSupg : TermSet::Mass, true,
+                     L.tcd_M));
   }
   CDG_CUDA(cudaMemsetAsync(L.tcd_f, 0, (size_t)L.ndof * sizeof(double), st));
   return launch_rhs(ctx, k, L, L.tcd_f);

@@ -190,7 +190,7 @@ int level_errors(cdg_context* ctx, cdg_problem* p, DevLevel& L,
 // time-dependent CD (TimeConvectionDiffusion with Crank-Nicolson)
 int tcd_interpolate(cdg_context* ctx, cdg_problem* p, const cdg_assembly_params& a);
 int tcd_assemble_level(cdg_context* ctx, cdg_problem* p, DevLevel& L,
-                       const cdg_assembly_params& a, bool with_mass);
+                       const cdg_assembly_params& a, bool with_mass, double tau);
 int tcd_cn_rhs(cdg_context* ctx, DevLevel& L, double tau);
 int tcd_system(cdg_context* ctx, cdg_problem* p, DevLevel& L, double tau);
 

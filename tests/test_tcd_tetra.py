@@ -77,6 +77,49 @@ def test_oracle_crank_nicolson_exact_for_linear_in_time(built):
     assert e[0] < 1e-10 and e[1] < 1e-9
 
 
+@pytest.mark.parametrize("dim,order,sdfem_type", [(3, 2, 2), (3, 1, 5), (2, 2, 5), (2, 1, 0)])
+def test_oracle_crank_nicolson_supg_exact_for_linear_in_time(built, dim, order, sdfem_type):
+    # SUPG in time is consistent: with the same delta in the stiffness, mass
+    # and rhs terms, a solution linear in space and time is reproduced
+    tau = 0.05
+    kw = dict(eps=1e-3, b=(1.0, -0.5, 0.3)[:dim], c=0.4, supg=True, sdfem_type=sdfem_type,
+              time_step=tau)
+    if dim == 3:
+        h = pg.Hierarchy(3, order, 3 - order, roots=1, tetra=True, perturb=0.15, seed=2)
+        o = tet_oracle(h, order, po.EX_POLY1_T, **kw)
+    else:
+        o = po.Problem(po.make_config(2, order, 3, po.EX_POLY1_T, **kw), 1)
+    o.tcd_initialize()
+    for k in range(1, 4):
+        it, res, ini = o.tcd_step(k * tau, tau, fgmres_jacobi())
+        assert res <= 1e-12 * max(ini, 1e-300) or res < 1e-13
+    e = o.errors()
+    assert e[0] < 1e-10 and e[1] < 1e-9
+
+
+def test_oracle_tcd_supg_terms(built):
+    # the SUPG mass term integrates delta (b . grad phi_i) phi_j: summed over
+    # j (sum phi_j = 1) every row holds delta * int b . grad phi_i, and those
+    # sum to zero over all i; SDFEM_TYPE 5 delta scales with theta1*tau
+    cfg = dict(eps=1e-3, b=(1.0, 0.5), supg=True, sdfem_type=5)
+    mats = []
+    for tau in (0.01, 0.02):
+        o = po.Problem(po.make_config(2, 1, 3, po.EX_SINE, time_step=tau, **cfg), 1)
+        o.tcd_initialize()
+        mats.append(o.tcd_matrix(1))
+    g = po.Problem(po.make_config(2, 1, 3, po.EX_SINE, **dict(cfg, supg=False)), 1)
+    g.tcd_initialize()
+    m0 = g.tcd_matrix(1)
+    s1, s2 = mats[0] - m0, mats[1] - m0
+    assert np.max(np.abs(s1)) > 1e-8
+    assert abs(s1.sum()) < 1e-14
+    # h/(2|b|) >> the scaled eps: delta ~ (theta1 tau)^2 h/(2 theta1 tau |b|)
+    # = theta1 tau h/(2|b|) up to the reaction term 1 in the scaled
+    # reaction, so doubling tau doubles it up to that correction
+    r = np.max(np.abs(s2)) / np.max(np.abs(s1))
+    assert 1.5 < r < 2.05
+
+
 def test_oracle_crank_nicolson_multigrid_converges(built):
     h = pg.Hierarchy(3, 2, 2, n_levels=3, roots=1, tetra=True, perturb=0.2, seed=4)
     o = tet_oracle(h, 2, po.EX_BUMP, eps=1e-4, b=B_ROT, b_grad=B_ROT_GRAD,
@@ -125,7 +168,8 @@ def gpu_params(kw, t=0.0, ic=(0.5, 0.5, 0.5, 0.1)):
         example=kw["example"], eps=kw.get("eps", 1.0), b=kw.get("b", (0, 0, 0)),
         c=kw.get("c", 0.0), b_grad=kw.get("b_grad"), t=t, ic=ic,
         space_discretization_type="supg" if kw.get("supg") else "galerkin",
-        sdfem_type=kw.get("sdfem_type", 2), cell_measure=kw.get("cell_measure", 0))
+        sdfem_type=kw.get("sdfem_type", 2), cell_measure=kw.get("cell_measure", 0),
+        time_step=kw.get("time_step", 0.0))
 
 
 def oracle_kw(kw):
@@ -173,24 +217,38 @@ def mg_solver(levels, precision="fp64", damp=0.45):
     return g, o
 
 
+TAU = 1e-2
 TCD_CASES = {
-    # name: (tetra, order, nref, levels, kwargs)
-    "p2_tet_bump": (True, 2, 2, 3, dict(example=po.EX_BUMP, eps=1e-3, b=B_ROT,
-                                        b_grad=B_ROT_GRAD)),
-    "q2_hex_sine": (False, 2, 2, 2, dict(example=po.EX_SINE, eps=1e-2, b=(1.0, 0.3, -0.2),
-                                         c=0.5)),
+    # name: (dim, tetra, order, nref, levels, kwargs)
+    "p2_tet_bump": (3, True, 2, 2, 3, dict(example=po.EX_BUMP, eps=1e-3, b=B_ROT,
+                                           b_grad=B_ROT_GRAD)),
+    "q2_hex_sine": (3, False, 2, 2, 2, dict(example=po.EX_SINE, eps=1e-2, b=(1.0, 0.3, -0.2),
+                                            c=0.5)),
+    # SUPG (TCDStiffSUPG, TCDMassSUPG, TCDRhsSUPG): SDFEM_TYPE 2 keeps the
+    # unscaled delta, 5 and 0 take the theta1*tau-scaled coefficients in 2D
+    # and delta *= theta1*tau
+    "p2_tet_supg_t2": (3, True, 2, 2, 3, dict(example=po.EX_BUMP, eps=1e-4, b=(0.8, 0.3, 0.2),
+                                              supg=True, sdfem_type=2, time_step=TAU)),
+    "q2_hex_supg_t5": (3, False, 2, 2, 2, dict(example=po.EX_SINE, eps=1e-3, b=(1.0, 0.3, -0.2),
+                                               c=0.5, supg=True, sdfem_type=5,
+                                               time_step=TAU)),
+    "q2_quad_supg_t5": (2, False, 2, 4, 3, dict(example=po.EX_POLY1_T, eps=1e-3, b=(1.0, 0.5),
+                                                c=0.5, supg=True, sdfem_type=5,
+                                                time_step=TAU)),
+    "q1_quad_supg_t0": (2, False, 1, 5, 3, dict(example=po.EX_SINE, eps=1e-4, b=(-0.6, 0.8),
+                                                supg=True, sdfem_type=0, time_step=TAU)),
 }
 
 
 def tcd_pair(ctx, name):
-    tetra, order, nref, levels, kw = TCD_CASES[name]
+    dim, tetra, order, nref, levels, kw = TCD_CASES[name]
     ic = (0.4, 0.5, 0.6, 0.15)
     if tetra:
         h = pg.Hierarchy(3, order, nref, n_levels=levels, roots=1, tetra=True)
         o = tet_oracle(h, order, kw["example"], ic=ic, **oracle_kw(kw))
     else:
-        h = pg.Hierarchy(3, order, nref, n_levels=levels)
-        cfg = po.make_config(3, order, nref, kw["example"], ic=ic, **oracle_kw(kw))
+        h = pg.Hierarchy(dim, order, nref, n_levels=levels)
+        cfg = po.make_config(dim, order, nref, kw["example"], ic=ic, **oracle_kw(kw))
         o = po.Problem(cfg, levels)
     gpu = pg.ConvectionDiffusion(ctx, h)
     return o, gpu, levels, kw, ic
@@ -200,7 +258,7 @@ def tcd_pair(ctx, name):
 @pytest.mark.parametrize("name", list(TCD_CASES))
 def test_tcd_matrices_and_steps_parity(ctx, name):
     o, gpu, levels, kw, ic = tcd_pair(ctx, name)
-    tau = 1e-2
+    tau = TAU
     o.tcd_initialize()
     gpu.tcd_initialize(gpu_params(kw, t=0.0, ic=ic))
     for l in range(levels):
@@ -216,7 +274,16 @@ def test_tcd_matrices_and_steps_parity(ctx, name):
         assert rel(gpu.rhs(0), o.rhs(0)) < 1e-11
         assert rel(gpu.solution(), o.solution()) < 1e-8
     for l in range(levels):
+        assert rel(gpu.tcd_matrix(1, l), o.tcd_matrix(1, l)) < 1e-12
         assert rel(gpu.tcd_matrix(2, l), o.tcd_matrix(2, l)) < 1e-12
+
+
+@pytest.mark.gpu
+def test_tcd_supg_needs_time_step(ctx):
+    o, gpu, levels, kw, ic = tcd_pair(ctx, "q1_quad_supg_t0")
+    with pytest.raises(pg.CdgError) as e:
+        gpu.tcd_initialize(gpu_params(dict(kw, time_step=0.0), ic=ic))
+    assert e.value.code == -1
 
 
 @pytest.mark.gpu
