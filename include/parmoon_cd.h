@@ -233,6 +233,12 @@ int cdg_problem_get_tcd_matrix(cdg_problem *p, int level, int which,
 
 /* ---- data access (host buffers) ----------------------------------------- */
 int cdg_problem_level_info(const cdg_problem *p, int level, int *info);
+/* storage of the level's FP64 operator on the device (no reference
+ * counterpart: ParMooN keeps CSR only): *lanes = 0 for CSR, otherwise the
+ * sliced ELLPACK copy with *lanes lanes per row and *slots stored entries
+ * (padding included) */
+int cdg_problem_operator_layout(const cdg_problem *p, int level, int *lanes,
+                                long long *slots);
 int cdg_problem_get_matrix(cdg_problem *p, int level, double *values);
 int cdg_problem_get_rhs(cdg_problem *p, int level, double *rhs);
 int cdg_problem_get_solution(cdg_problem *p, double *sol);

@@ -37,7 +37,7 @@ EXPORTED = [
     "cdg_hierarchy_get_dofs", "cdg_hierarchy_get_pattern", "cdg_problem_create",
     "cdg_problem_create_from_arrays", "cdg_problem_destroy", "cdg_problem_assemble",
     "cdg_problem_solve", "cdg_problem_assemble_solve", "cdg_problem_errors",
-    "cdg_problem_level_info", "cdg_problem_get_matrix", "cdg_problem_get_rhs",
+    "cdg_problem_level_info", "cdg_problem_operator_layout", "cdg_problem_get_matrix", "cdg_problem_get_rhs",
     "cdg_problem_get_solution", "cdg_problem_set_solution", "cdg_problem_get_slots",
     "cdg_problem_apply", "cdg_problem_prolongate", "cdg_problem_restrict",
     "cdg_problem_precondition", "cdg_context_stream", "cdg_problem_time_kernel",
@@ -138,6 +138,8 @@ def lib():
                                      ctypes.POINTER(SolverParams), ctypes.POINTER(SolveStats)],
             "cdg_problem_get_tcd_matrix": [P, ctypes.c_int, ctypes.c_int, dp],
             "cdg_problem_level_info": [P, ctypes.c_int, ip],
+            "cdg_problem_operator_layout": [P, ctypes.c_int, ip,
+                                            ctypes.POINTER(ctypes.c_longlong)],
             "cdg_problem_get_matrix": [P, ctypes.c_int, dp],
             "cdg_problem_get_rhs": [P, ctypes.c_int, dp],
             "cdg_problem_get_solution": [P, dp], "cdg_problem_set_solution": [P, dp],
@@ -366,6 +368,13 @@ class ConvectionDiffusion:
         _chk(lib().cdg_problem_level_info(self.p, level, _ip(a)))
         return dict(ncells=int(a[0]), nloc=int(a[1]), ndof=int(a[2]), nactive=int(a[3]),
                     nnz=int(a[4]), nv=int(a[5]))
+
+    def operator_layout(self, level=0):
+        """lanes 0: CSR; else sliced ELLPACK with `lanes` lanes per row."""
+        g = ctypes.c_int(0)
+        t = ctypes.c_longlong(0)
+        _chk(lib().cdg_problem_operator_layout(self.p, level, ctypes.byref(g), ctypes.byref(t)))
+        return dict(lanes=g.value, slots=t.value)
 
     def assemble(self, a):
         _chk(lib().cdg_problem_assemble(self.p, ctypes.byref(a)))

@@ -202,7 +202,10 @@ static int finish_problem(cdg_context* ctx, cdg_problem* p, const std::vector<st
                           const std::vector<Mesh>* nested) {
   CDG_CUDA(cudaMalloc(&p->d_zero_diag, sizeof(int)));
   CDG_CUDA(cudaMemsetAsync(p->d_zero_diag, 0, sizeof(int), ctx->stream));
-  for (auto& L : p->lev) CDG_TRY(upload_level(ctx, L));
+  for (auto& L : p->lev) {
+    CDG_TRY(upload_level(ctx, L));
+    CDG_TRY(build_sell(ctx, L));
+  }
   for (size_t l = 0; l + 1 < p->lev.size(); ++l) {
     DevLevel& F = p->lev[l];
     DevLevel& C = p->lev[l + 1];
@@ -511,6 +514,17 @@ static DevLevel* get_level(cdg_problem* p, int level) {
   }
   cudaSetDevice(p->ctx->device);
   return &p->lev[level];
+}
+
+int cdg_problem_operator_layout(const cdg_problem* p, int level, int* lanes, long long* slots) {
+  if (!p || level < 0 || level >= (int)p->lev.size() || !lanes || !slots) {
+    set_error("bad arguments");
+    return CDG_ERR_ARG;
+  }
+  const DevLevel& L = p->lev[level];
+  *lanes = L.sell_nslices ? L.sell_lanes : 0;
+  *slots = L.sell_nslices ? L.sell_total : 0;
+  return CDG_OK;
 }
 
 int cdg_problem_level_info(const cdg_problem* p, int level, int* info) {

@@ -25,9 +25,11 @@
 // reference becomes one FP64 contraction per entry.  The right-hand side
 // keeps a quadrature rule of the reference's degree because f is not
 // polynomial.
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <mutex>
 
 #include "common.cuh"
@@ -567,14 +569,22 @@ __global__ void k_dirichlet_rows(int n, int nactive, const int* __restrict__ dsl
   if (r < n) val[dslot[r]] = 1.0;
 }
 
-// FP32 copy of the values and inverse diagonals (Iteration_jacobi.C:14-28)
+// FP32 copy of the values and inverse diagonals (Iteration_jacobi.C:14-28);
+// sell_val != null: the values of the active rows into the sliced ELLPACK copy
 __global__ void k_finish_matrix(int n, int nnz, const int* __restrict__ dslot,
                                 const double* __restrict__ val, float* __restrict__ val32,
                                 double* __restrict__ invd, float* __restrict__ invd32,
+                                const int* __restrict__ sell_pos, double* __restrict__ sell_val,
                                 int* err) {
   long stride = (long)gridDim.x * blockDim.x;
-  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < nnz; t += stride)
-    val32[t] = (float)val[t];
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < nnz; t += stride) {
+    const double v = val[t];
+    val32[t] = (float)v;
+    if (sell_val) {
+      const int q = sell_pos[t];
+      if (q >= 0) sell_val[q] = v;
+    }
+  }
   for (long r = blockIdx.x * (long)blockDim.x + threadIdx.x; r < n; r += stride) {
     double d = val[dslot[r]];
     if (d == 0.0) {
@@ -1025,8 +1035,114 @@ int upload_level(cdg_context* ctx, DevLevel& L) {
   return build_slots(ctx, L);
 }
 
+__global__ void k_sell_identity(int nd, const long long* __restrict__ q, double* __restrict__ v) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nd) v[q[i]] = 1.0;
+}
+
+// Sliced ELLPACK layout of the level's pattern (see DevLevel::sell_*).  A
+// warp takes one slice of 32/G rows whose lengths agree, so every FP64
+// multiply-add has a full warp of useful lanes: CSR rows of 27..125 entries
+// (Q2) split over a fixed number of lanes leave half of the FP64 issue slots
+// to padding, and the FP64 pipe is what bounds these kernels on GB300.  The G
+// lanes of a row take its consecutive entries, whose columns are close, so a
+// gather touches few cache lines.  Sorting by length inside 256-row windows
+// keeps the padding small and the rows of a slice close together.  (For the
+// FP32 multigrid, bound by memory latency rather than the FP32 pipe, the CSR
+// kernels measured faster, and it keeps them.)
+int build_sell(cdg_context* ctx, DevLevel& L) {
+  const int n = L.ndof, na = L.nactive;
+  if (n < kSellMinRows) return CDG_OK;
+  const std::vector<int>& rp = L.pattern.row_ptr;
+  const std::vector<int>& cl = L.pattern.col;
+  auto len = [&](int r) { return r < na ? rp[r + 1] - rp[r] : 1; };
+  // lanes per row (measured on GB300, FP64 operator: 2 lanes beat 1, 4 and
+  // 8 for Q2 hexahedra, 62 entries per row, and P2 tetrahedra, 28), doubled
+  // on smaller levels until the launch has enough warps to cover the GPU
+  const double avg = (double)L.nnz / n;
+  int G = avg > 160 ? 4 : avg > 16 ? 2 : 1;
+  while (G < 16 && (long)n * G / 32 < kSellMinWarps) G *= 2;
+  if (const char* e = getenv("CDG_SELL_LANES")) {
+    const int g = atoi(e);
+    if (g == 0) return CDG_OK;                  // CSR kernels
+    if (g == 1 || g == 2 || g == 4 || g == 8 || g == 16) G = g;
+  }
+  const int R = 32 / G;                         // rows per slice
+  const int nslices = (n + R - 1) / R;
+  std::vector<int> order(n);
+  for (int w0 = 0; w0 < n; w0 += kSellWindow) {
+    const int w1 = std::min(n, w0 + kSellWindow);
+    for (int r = w0; r < w1; ++r) order[r] = r;
+    std::stable_sort(order.begin() + w0, order.begin() + w1,
+                     [&](int a, int b) { return len(a) > len(b); });
+  }
+  std::vector<long long> off(nslices + 1, 0);
+  std::vector<int> srow((size_t)nslices * R, -1);
+  for (int s = 0; s < nslices; ++s) {
+    int steps = 0;
+    for (int i = 0; i < R && (long)s * R + i < n; ++i) {
+      const int r = order[(size_t)s * R + i];
+      srow[(size_t)s * R + i] = r;
+      steps = std::max(steps, (len(r) + G - 1) / G);
+    }
+    off[s + 1] = off[s] + 32LL * steps;
+  }
+  const long long total = off[nslices];
+  if (total >= (1LL << 31)) return CDG_OK;   // positions are int: keep the CSR operator
+  std::vector<int> scol((size_t)total, 0), pos((size_t)L.nnz, -1);
+  std::vector<long long> ident;
+  for (int s = 0; s < nslices; ++s) {
+    const int slots = (int)((off[s + 1] - off[s]) / 32) * G;   // per row
+    for (int i = 0; i < R; ++i) {
+      const int r = srow[(size_t)s * R + i];
+      if (r < 0) continue;                      // padding row: column 0, value 0
+      const int m = r < na ? rp[r + 1] - rp[r] : 0;
+      for (int k = 0; k < slots; ++k) {
+        const long long q = off[s] + 32LL * (k / G) + G * i + k % G;
+        if (k < m) {
+          scol[q] = cl[rp[r] + k];
+          pos[rp[r] + k] = (int)q;
+        } else {
+          scol[q] = r;                          // padding: own row, value 0
+        }
+      }
+      if (r >= na) ident.push_back(off[s] + G * i);   // identity row: 1 at its first slot
+    }
+  }
+  cudaStream_t st = ctx->stream;
+  CDG_TRY(dalloc(&L.sell_off, off.size()));
+  CDG_TRY(dalloc(&L.sell_row, srow.size()));
+  CDG_TRY(dalloc(&L.sell_col, (size_t)total));
+  CDG_TRY(dalloc(&L.sell_val, (size_t)total));
+  CDG_TRY(dalloc(&L.sell_pos, (size_t)L.nnz));
+  CDG_CUDA(cudaMemcpyAsync(L.sell_off, off.data(), off.size() * sizeof(long long),
+                           cudaMemcpyHostToDevice, st));
+  CDG_CUDA(cudaMemcpyAsync(L.sell_row, srow.data(), srow.size() * sizeof(int),
+                           cudaMemcpyHostToDevice, st));
+  CDG_CUDA(cudaMemcpyAsync(L.sell_col, scol.data(), (size_t)total * sizeof(int),
+                           cudaMemcpyHostToDevice, st));
+  CDG_CUDA(cudaMemcpyAsync(L.sell_pos, pos.data(), (size_t)L.nnz * sizeof(int),
+                           cudaMemcpyHostToDevice, st));
+  CDG_CUDA(cudaMemsetAsync(L.sell_val, 0, (size_t)total * sizeof(double), st));
+  if (!ident.empty()) {
+    long long* dq = nullptr;
+    CDG_TRY(dalloc(&dq, ident.size()));
+    CDG_CUDA(cudaMemcpyAsync(dq, ident.data(), ident.size() * sizeof(long long),
+                             cudaMemcpyHostToDevice, st));
+    CDG_LAUNCH(ctx, k_sell_identity, grid_for<int>((long)ident.size(), 256), 256, 0,
+               (int)ident.size(), dq, L.sell_val);
+    CDG_CUDA(cudaStreamSynchronize(st));
+    CDG_CUDA(cudaFree(dq));
+  }
+  CDG_CUDA(cudaStreamSynchronize(st));      // host vectors go out of scope
+  L.sell_nslices = nslices;
+  L.sell_lanes = G;
+  L.sell_total = total;
+  return CDG_OK;
+}
+
 int free_level(DevLevel& L) {
-  void* ptrs[] = {L.verts, L.gdof, L.row_ptr, L.col, L.slot, L.diag_slot, L.val64, L.val32,
+  void* ptrs[] = {L.sell_off, L.sell_row, L.sell_col, L.sell_val, L.sell_pos,L.verts, L.gdof, L.row_ptr, L.col, L.slot, L.diag_slot, L.val64, L.val32,
                   L.rhs, L.sol, L.invdiag64, L.invdiag32, L.mg_rhs, L.mg_sol, L.mg_tmp,
                   L.mg_def, L.P_rp, L.P_col, L.P_val, L.P_val32, L.R_rp, L.R_col, L.R_val,
                   L.R_val32, L.coarse_inv, L.coarse_work, L.dc_rp, L.dc_col, L.dc_pos,
@@ -1217,7 +1333,7 @@ static int launch_rhs(cdg_context* ctx, const AsmCoefs& k, DevLevel& L, double* 
 static int finish_matrix(cdg_context* ctx, cdg_problem* p, DevLevel& L) {
   int g = (int)std::min<long>(((long)std::max(L.nnz, L.ndof) + 255) / 256, (long)ctx->num_sms * 16);
   CDG_LAUNCH(ctx, k_finish_matrix, g, 256, 0, L.ndof, L.nnz, L.diag_slot, L.val64, L.val32,
-             L.invdiag64, L.invdiag32, p->d_zero_diag);
+             L.invdiag64, L.invdiag32, L.sell_pos, L.sell_val, p->d_zero_diag);
   return CDG_OK;
 }
 

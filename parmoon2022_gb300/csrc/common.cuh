@@ -79,6 +79,20 @@ struct DevLevel {
   double* invdiag64 = nullptr;   // ndof
   float* invdiag32 = nullptr;    // ndof
   int rows_per_warp_hint = 1;    // SpMV shape (avg row length)
+  // sliced ELLPACK copy of the FP64 matrix (the FGMRES operator, the FP64
+  // multigrid smoother and defect) on levels of at least kSellMinRows rows:
+  // G = sell_lanes lanes per row, slices of 32/G rows (one warp),
+  // rows sorted by length inside windows of 256 consecutive rows; entry k of
+  // the slice's row i at sell_off[s] + 32 (k / G) + G i + k % G.  Non-active
+  // rows are stored as identity rows; the padding is zero.
+  int sell_nslices = 0;
+  int sell_lanes = 0;
+  long long sell_total = 0;      // stored entries (padding included)
+  long long* sell_off = nullptr; // nslices+1
+  int* sell_row = nullptr;       // nslices*32/G: row of each slice row (-1: none)
+  int* sell_col = nullptr;       // sell_off[nslices]
+  double* sell_val = nullptr;    // sell_off[nslices]
+  int* sell_pos = nullptr;       // nnz: SELL position of each CSR entry (-1: non-active row)
   // rhs assembly: local entries per (cell, local DOF) and, per active DOF,
   // the list of its local entries (CSR over active rows)
   double* rhs_loc = nullptr;     // ncells*nloc
@@ -180,6 +194,10 @@ inline int grid_for(long n, int block) {
 
 // host launchers implemented in the .cu files
 int upload_level(cdg_context* ctx, DevLevel& L);
+constexpr int kSellWindow = 256;    // rows sorted by length inside windows of this many rows
+constexpr int kSellMinRows = 32768; // smaller levels keep the CSR kernels (latency bound)
+constexpr int kSellMinWarps = 4096; // lanes per row doubled until a launch has this many warps
+int build_sell(cdg_context* ctx, DevLevel& L);
 int free_level(DevLevel& L);
 int build_slots(cdg_context* ctx, DevLevel& L);
 int assemble_level(cdg_context* ctx, cdg_problem* p, DevLevel& L,

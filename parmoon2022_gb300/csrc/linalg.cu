@@ -100,9 +100,72 @@ static int spmv_t(cdg_context* ctx, const DevLevel& L, const T* val, const T* x,
   return CDG_OK;
 }
 
-// the FP64 operator: FP64 issue rate bounds it on GB300, so rows use 4 lanes
-// x 16-deep unrolling (2 reduction levels instead of 3)
+// Sliced ELLPACK SpMV (same MODEs as k_spmv): one warp per slice of 32/G
+// rows, G lanes per row; the slice's step count is warp-uniform, so every
+// multiply-add issues for 32 useful lanes (padding: zero values) and every
+// load of a step is one coalesced 32-wide access.  UNR steps are loaded
+// before their gathers.  Non-active rows are identity rows of the layout.
+template <typename T, int G, int UNR, int MODE>
+__global__ void __launch_bounds__(256)
+k_sell(int nslices, const long long* __restrict__ off, const int* __restrict__ srow,
+       const int* __restrict__ scol, const T* __restrict__ sval, const T* __restrict__ x,
+       const T* __restrict__ b, const T* __restrict__ invd, T w, T* __restrict__ y) {
+  const int slice = (int)((blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (slice >= nslices) return;              // warp-uniform
+  const long long o = __ldg(off + slice);
+  const int width = (int)((__ldg(off + slice + 1) - o) >> 5);
+  const int* __restrict__ cp = scol + o + lane;
+  const T* __restrict__ vp = sval + o + lane;
+  T s = 0;
+  for (int k0 = 0; k0 < width; k0 += UNR) {
+    int c[UNR];
+    T v[UNR];
+#pragma unroll
+    for (int u = 0; u < UNR; ++u) {
+      const bool in = k0 + u < width;       // warp-uniform
+      c[u] = in ? __ldcs(cp + (long)(k0 + u) * 32) : 0;
+      v[u] = in ? __ldcs(vp + (long)(k0 + u) * 32) : (T)0;
+    }
+#pragma unroll
+    for (int u = 0; u < UNR; ++u)
+      if (k0 + u < width) s = fma(v[u], __ldg(x + c[u]), s);
+  }
+  s = group_sum<T, G>(s);
+  if (lane % G) return;
+  const int row = __ldg(srow + (long)slice * (32 / G) + lane / G);
+  if (row < 0) return;
+  if (MODE == 0) y[row] = s;
+  else if (MODE == 1) y[row] = b[row] - s;
+  else y[row] = x[row] + w * (invd[row] * (b[row] - s));
+}
+
+template <int G, int MODE>
+static int sell64_g(cdg_context* ctx, const DevLevel& L, const double* x, const double* b,
+                    double* y) {
+  const int grid = (int)(((long)L.sell_nslices * 32 + 255) / 256);
+  CDG_LAUNCH(ctx, (k_sell<double, G, 8, MODE>), grid, 256, 0, L.sell_nslices, L.sell_off,
+             L.sell_row, L.sell_col, L.sell_val, x, b, (const double*)nullptr, 0.0, y);
+  return CDG_OK;
+}
+
+template <int MODE>
+static int sell64(cdg_context* ctx, const DevLevel& L, const double* x, const double* b,
+                  double* y) {
+  switch (L.sell_lanes) {
+    case 1: return sell64_g<1, MODE>(ctx, L, x, b, y);
+    case 2: return sell64_g<2, MODE>(ctx, L, x, b, y);
+    case 4: return sell64_g<4, MODE>(ctx, L, x, b, y);
+    case 8: return sell64_g<8, MODE>(ctx, L, x, b, y);
+    default: return sell64_g<16, MODE>(ctx, L, x, b, y);
+  }
+}
+
+// the FP64 operator: FP64 issue rate bounds it on GB300.  With the sliced
+// ELLPACK copy every FP64 multiply-add is useful; otherwise CSR rows use 4
+// lanes x 16-deep unrolling (2 reduction levels instead of 3)
 int spmv_apply64(cdg_context* ctx, const DevLevel& L, const double* x, double* y) {
+  if (L.sell_nslices) return sell64<0>(ctx, L, x, nullptr, y);
   if (L.rows_per_warp_hint == 8) {
     int grid = (int)(((long)L.ndof * 4 + 255) / 256);
     CDG_LAUNCH(ctx, (k_spmv<double, 4, 16, 0>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr,
@@ -113,6 +176,7 @@ int spmv_apply64(cdg_context* ctx, const DevLevel& L, const double* x, double* y
 }
 int residual64(cdg_context* ctx, const DevLevel& L, const double* b, const double* x,
                double* r) {
+  if (L.sell_nslices) return sell64<1>(ctx, L, x, b, r);
   return spmv_t<double, 1>(ctx, L, L.val64, x, b, nullptr, 0.0, r);
 }
 
@@ -754,12 +818,16 @@ static int coarse_inverse(cdg_context* ctx, DevLevel& C) {
 template <typename T> struct Prec;
 template <> struct Prec<double> {
   static const double* val(const DevLevel& L) { return L.val64; }
+  static const double* sell(const DevLevel& L) { return L.sell_val; }
+  static bool has_sell(const DevLevel& L) { return L.sell_nslices > 0; }
   static const double* invd(const DevLevel& L) { return L.invdiag64; }
   static const double* P(const DevLevel& L) { return L.P_val; }
   static const double* R(const DevLevel& L) { return L.R_val; }
 };
 template <> struct Prec<float> {
   static const float* val(const DevLevel& L) { return L.val32; }
+  static const float* sell(const DevLevel&) { return nullptr; }
+  static bool has_sell(const DevLevel&) { return false; }   // CSR measured faster in FP32
   static const float* invd(const DevLevel& L) { return L.invdiag32; }
   static const float* P(const DevLevel& L) { return L.P_val32; }
   static const float* R(const DevLevel& L) { return L.R_val32; }
@@ -771,10 +839,29 @@ static int vec_grid(cdg_context* ctx, long n) {
   return (int)(g > cap ? cap : (g < 1 ? 1 : g));
 }
 
+// sliced ELLPACK smoothing / defect on a multigrid level
+template <typename T, int MODE>
+static int sell_mg(cdg_context* ctx, const DevLevel& L, const T* val, const T* x, const T* b,
+                   const T* invd, T w, T* y) {
+  const int grid = (int)(((long)L.sell_nslices * 32 + 255) / 256);
+  switch (L.sell_lanes) {
+    case 1: CDG_LAUNCH(ctx, (k_sell<T, 1, 8, MODE>), grid, 256, 0, L.sell_nslices, L.sell_off, L.sell_row, L.sell_col, val, x, b, invd, w, y); break;
+    case 2: CDG_LAUNCH(ctx, (k_sell<T, 2, 8, MODE>), grid, 256, 0, L.sell_nslices, L.sell_off, L.sell_row, L.sell_col, val, x, b, invd, w, y); break;
+    case 4: CDG_LAUNCH(ctx, (k_sell<T, 4, 8, MODE>), grid, 256, 0, L.sell_nslices, L.sell_off, L.sell_row, L.sell_col, val, x, b, invd, w, y); break;
+    case 8: CDG_LAUNCH(ctx, (k_sell<T, 8, 8, MODE>), grid, 256, 0, L.sell_nslices, L.sell_off, L.sell_row, L.sell_col, val, x, b, invd, w, y); break;
+    default: CDG_LAUNCH(ctx, (k_sell<T, 16, 8, MODE>), grid, 256, 0, L.sell_nslices, L.sell_off, L.sell_row, L.sell_col, val, x, b, invd, w, y); break;
+  }
+  return CDG_OK;
+}
+
 template <typename T>
 static int smooth(cdg_context* ctx, DevLevel& L, T damp) {
-  CDG_TRY((spmv_t<T, 2>(ctx, L, Prec<T>::val(L), (const T*)L.mg_sol, (const T*)L.mg_rhs,
-                         Prec<T>::invd(L), damp, (T*)L.mg_tmp)));
+  if (Prec<T>::has_sell(L))
+    CDG_TRY((sell_mg<T, 2>(ctx, L, Prec<T>::sell(L), (const T*)L.mg_sol, (const T*)L.mg_rhs,
+                           Prec<T>::invd(L), damp, (T*)L.mg_tmp)));
+  else
+    CDG_TRY((spmv_t<T, 2>(ctx, L, Prec<T>::val(L), (const T*)L.mg_sol, (const T*)L.mg_rhs,
+                           Prec<T>::invd(L), damp, (T*)L.mg_tmp)));
   std::swap(L.mg_sol, L.mg_tmp);
   return CDG_OK;
 }
@@ -812,6 +899,9 @@ static int first_smooth(cdg_context* ctx, DevLevel& L, T damp, bool finest) {
 
 template <typename T>
 static int defect(cdg_context* ctx, DevLevel& L) {
+  if (Prec<T>::has_sell(L))
+    return sell_mg<T, 1>(ctx, L, Prec<T>::sell(L), (const T*)L.mg_sol, (const T*)L.mg_rhs,
+                         nullptr, (T)0, (T*)L.mg_def);
   return spmv_t<T, 1>(ctx, L, Prec<T>::val(L), (const T*)L.mg_sol, (const T*)L.mg_rhs, nullptr,
                       (T)0, (T*)L.mg_def);
 }

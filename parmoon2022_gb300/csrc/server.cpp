@@ -103,6 +103,7 @@ long long estimate_bytes(const cdg_hierarchy* h, int n_levels, int restart) {
                     nv = info[5];
     b += nnz * 16 + ncells * nloc * nloc * 4 + ncells * nloc * 16 + ndof * 112 +
          ncells * nv * 3 * 8;
+    b += ndof >= 32768 ? nnz * 17 + ndof * 8 : 0;   // sliced ELLPACK copy
     b += (l + 1 < n_levels) ? ndof * 24 * 16 : 0;   // transfer matrices
   }
   cdg_hierarchy_level_info(h, 0, info);
@@ -123,6 +124,7 @@ long long estimate_bytes_unbuilt(const ClassKey& k, int restart) {
     const long long ncells = k.dim == 2 ? (long long)n * n : (long long)n * n * n;
     b += ndof * band * 16 + ncells * nloc * nloc * 4 + ncells * nloc * 16 + ndof * 112 +
          ncells * 8 * 3 * 8 + ndof * 24 * 16;
+    b += ndof >= 32768 ? ndof * band * 17 + ndof * 8 : 0;   // sliced ELLPACK copy
   }
   const long long m = (long long)k.order * k.n + 1;
   b += (long long)(2 * restart + 3) * (k.dim == 2 ? m * m : m * m * m) * 8;

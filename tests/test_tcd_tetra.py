@@ -276,6 +276,16 @@ def test_tcd_matrices_and_steps_parity(ctx, name):
     for l in range(levels):
         assert rel(gpu.tcd_matrix(1, l), o.tcd_matrix(1, l)) < 1e-12
         assert rel(gpu.tcd_matrix(2, l), o.tcd_matrix(2, l)) < 1e-12
+    # the operator of the solver (sliced ELLPACK copy on the finest level):
+    # the system matrix on active rows, identity rows where Dirichlet rows
+    # hold assembled values
+    rp, col = o.structure(0)
+    na = o.info(0)["nactive"]
+    S = gpu.tcd_matrix(2, 0)
+    x = np.random.default_rng(2).standard_normal(len(rp) - 1)
+    want = np.array([S[rp[r]:rp[r + 1]] @ x[col[rp[r]:rp[r + 1]]] for r in range(len(rp) - 1)])
+    want[na:] = x[na:]
+    assert rel(gpu.apply(x), want) < 1e-13
 
 
 @pytest.mark.gpu
