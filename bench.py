@@ -208,6 +208,27 @@ def profile_traffic(kernel_tag):
 
 
 # ---------------------------------------------------------------------------
+def timed_hierarchies(pg, ctx, args, kw, levels):
+    """The hierarchy built on the host and on the GPU (DOF numbering and CSR
+    patterns of every level), both timed; the GPU-built one is checked
+    bit-exact against the host one and used for the run."""
+    t0 = time.perf_counter()
+    host = pg.Hierarchy(*args, **kw)
+    t_host = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    dev = pg.Hierarchy(*args, ctx=ctx, **kw)
+    t_dev = time.perf_counter() - t0
+    same = True
+    for lvl in range(levels):
+        ra, ca = host.pattern(lvl)
+        rb, cb = dev.pattern(lvl)
+        same = same and host.info(lvl) == dev.info(lvl) and np.array_equal(
+            host.dofs(lvl), dev.dofs(lvl)) and np.array_equal(ra, rb) and np.array_equal(ca, cb)
+    if not same:
+        raise RuntimeError("GPU-built hierarchy differs from the host one")
+    return dev, {"hierarchy_host_s": t_host, "hierarchy_device_s": t_dev, "bit_exact": same}
+
+
 def run_gpu(args):
     import torch
     import parmoon2022_gb300 as pg
@@ -218,7 +239,8 @@ def run_gpu(args):
     ctx = pg.Context(local)
     stream = torch.cuda.ExternalStream(ctx.stream(), device=local)
     LEVELS = w["levels"]
-    hier = pg.Hierarchy(w["dim"], w["order"], w["nref"], n_levels=LEVELS, roots=w["roots"])
+    hkw = dict(n_levels=LEVELS, roots=w["roots"])
+    hier, setup = timed_hierarchies(pg, ctx, (w["dim"], w["order"], w["nref"]), hkw, LEVELS)
     cd = pg.ConvectionDiffusion(ctx, hier)
     a = spec_assembly(pg, w)
     precs = w["precisions"]
@@ -371,6 +393,7 @@ def run_gpu(args):
                 "d2h_bytes_per_step": 8 * n + 8 * 4},
         "clocks": clk,
         "gpu_launches": launches,
+        "setup": setup,
     }
     if fp64_side:
         rel = float(np.max(np.abs(x_m - x_d)) / np.max(np.abs(x_d)))
@@ -419,8 +442,9 @@ def run_gpu_tcd(args):
     stream = torch.cuda.ExternalStream(ctx.stream(), device=local)
     L = TCD["levels"] - (1 if args.small else 0)
     nref = TCD["nref"] - (1 if args.small else 0)
-    hier = pg.Hierarchy(3, 2, nref, n_levels=L, roots=TCD["roots"], tetra=True,
-                        perturb=TCD["perturb"], seed=TCD["seed"])
+    hier, setup = timed_hierarchies(pg, ctx, (3, 2, nref),
+                                    dict(n_levels=L, roots=TCD["roots"], tetra=True,
+                                         perturb=TCD["perturb"], seed=TCD["seed"]), L)
     cd = pg.ConvectionDiffusion(ctx, hier)
     info = [cd.info(l) for l in range(L)]
     n = info[0]["ndof"]
@@ -545,7 +569,7 @@ def run_gpu_tcd(args):
         "cpu_baseline": cpu,
         "e2e": {"value": world / t_e2e, "unit": "steps/s", "h2d_bytes_per_step": 136 + 136,
                 "d2h_bytes_per_step": 8 * n + 8 * 4},
-        "clocks": clk, "gpu_launches": launches,
+        "clocks": clk, "gpu_launches": launches, "setup": setup,
     }))
 
 

@@ -149,6 +149,33 @@ int cdg_hierarchy_create(int dim, int order, int roots, int nref, int n_levels,
 int cdg_hierarchy_create_tetra(int order, int roots, int nref, int n_levels,
                                double perturb, unsigned long long seed,
                                cdg_hierarchy **out);
+/* the same hierarchies with the FE space numbering and the TStructure of every
+ * level built on the context's GPU (bit-exact with the host builders above) */
+int cdg_hierarchy_create_device(cdg_context *ctx, int dim, int order, int roots,
+                                int nref, int n_levels, int neumann_mask,
+                                cdg_hierarchy **out);
+int cdg_hierarchy_create_tetra_device(cdg_context *ctx, int order, int roots,
+                                      int nref, int n_levels, double perturb,
+                                      unsigned long long seed, cdg_hierarchy **out);
+/* TFESpace numbering on the GPU (TFESpace3D::ConstructSpace,
+ * src/FE/FESpace3D.C:186; TFESpace::compute_various_numbers,
+ * src/FE/FESpace.C:1863-2099): inner DOFs, then non-Dirichlet boundary DOFs,
+ * then Dirichlet DOFs, each class in order of first appearance over (cell,
+ * local DOF).  Cells of a structured mesh of the unit square / cube (DOFs on
+ * a lattice of the first cell's edge length / order); cell_type
+ * CDG_CELL_QUAD, CDG_CELL_HEXA or CDG_CELL_TETRA, verts as in
+ * cdg_problem_create_from_arrays; gdof receives n_cells * n_local_dofs */
+int cdg_space_number_device(cdg_context *ctx, int cell_type, int order,
+                            int neumann_mask, int n_cells, const double *verts,
+                            int *gdof, int *ndof, int *nactive);
+/* TStructure(space) on the GPU (src/Matrix/Structure.C:226-556): rows of
+ * every DOF of every cell containing the row's DOF, columns sorted, full rows
+ * for Dirichlet DOFs.  row_ptr receives ndof+1 offsets and *nnz the entry
+ * count in every case; col receives the columns when col_capacity >= *nnz,
+ * otherwise CDG_ERR_LIMIT (call again with a large enough buffer) */
+int cdg_structure_build_device(cdg_context *ctx, int n_cells, int n_local_dofs,
+                               int ndof, const int *gdof, int *row_ptr, int *col,
+                               long long col_capacity, long long *nnz);
 int cdg_hierarchy_destroy(cdg_hierarchy *h);
 /* info[0..5] = n_cells, n_local_dofs, n_dofs, n_active, nnz, verts_per_cell */
 int cdg_hierarchy_level_info(const cdg_hierarchy *h, int level, int *info);

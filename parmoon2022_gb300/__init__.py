@@ -42,6 +42,8 @@ EXPORTED = [
     "cdg_problem_apply", "cdg_problem_prolongate", "cdg_problem_restrict",
     "cdg_problem_precondition", "cdg_context_stream", "cdg_problem_time_kernel",
     "cdg_problem_errors_noalloc", "cdg_hierarchy_create_tetra", "cdg_problem_tcd_initialize",
+    "cdg_hierarchy_create_device", "cdg_hierarchy_create_tetra_device",
+    "cdg_space_number_device", "cdg_structure_build_device",
     "cdg_problem_tcd_step", "cdg_problem_get_tcd_matrix", "cdg_server_create",
     "cdg_server_destroy", "cdg_request_ndof", "cdg_server_submit", "cdg_server_wait",
     "cdg_server_counters",
@@ -133,6 +135,12 @@ def lib():
             "cdg_problem_errors_noalloc": [P, ctypes.POINTER(AssemblyParams), dp],
             "cdg_hierarchy_create_tetra": [ctypes.c_int] * 4 + [ctypes.c_double,
                                                                 ctypes.c_ulonglong, PP],
+            "cdg_hierarchy_create_device": [P] + [ctypes.c_int] * 6 + [PP],
+            "cdg_hierarchy_create_tetra_device": [P] + [ctypes.c_int] * 4 + [
+                ctypes.c_double, ctypes.c_ulonglong, PP],
+            "cdg_space_number_device": [P] + [ctypes.c_int] * 4 + [dp, ip, ip, ip],
+            "cdg_structure_build_device": [P] + [ctypes.c_int] * 3 + [
+                ip, ip, ip, ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong)],
             "cdg_problem_tcd_initialize": [P, ctypes.POINTER(AssemblyParams)],
             "cdg_problem_tcd_step": [P, ctypes.POINTER(AssemblyParams), ctypes.c_double,
                                      ctypes.POINTER(SolverParams), ctypes.POINTER(SolveStats)],
@@ -235,16 +243,23 @@ class Hierarchy:
     """Host setup: unit square/cube (roots^dim cells) refined nref times, the
     Q_order space and CSR pattern of each of n_levels levels (0 = finest).
     tetra=True: roots^3 cubes of 6 Kuhn tetrahedra, P_order, with the finest
-    interior vertices perturbed by perturb*h (seeded)."""
+    interior vertices perturbed by perturb*h (seeded).  ctx: number the DOFs
+    and build the patterns on that context's GPU instead of the host."""
 
     def __init__(self, dim, order, nref, n_levels=1, roots=1, neumann_mask=0, tetra=False,
-                 perturb=0.0, seed=0):
+                 perturb=0.0, seed=0, ctx=None):
         self.dim, self.order, self.nref, self.n_levels = dim, order, nref, n_levels
         self.tetra = tetra
         h = ctypes.c_void_p()
-        if tetra:
+        if tetra and ctx is not None:
+            _chk(lib().cdg_hierarchy_create_tetra_device(ctx.c, order, roots, nref, n_levels,
+                                                         perturb, seed, ctypes.byref(h)))
+        elif tetra:
             _chk(lib().cdg_hierarchy_create_tetra(order, roots, nref, n_levels, perturb, seed,
                                                   ctypes.byref(h)))
+        elif ctx is not None:
+            _chk(lib().cdg_hierarchy_create_device(ctx.c, dim, order, roots, nref, n_levels,
+                                                   neumann_mask, ctypes.byref(h)))
         else:
             _chk(lib().cdg_hierarchy_create(dim, order, roots, nref, n_levels, neumann_mask,
                                             ctypes.byref(h)))
@@ -279,6 +294,38 @@ class Hierarchy:
         col = np.zeros(i["nnz"], dtype=np.int32)
         _chk(lib().cdg_hierarchy_get_pattern(self.h, level, _ip(rp), _ip(col)))
         return rp, col
+
+
+CELL_QUAD, CELL_HEXA, CELL_TETRA = 2, 3, 4
+
+
+def space_number_device(ctx, cell_type, order, verts, neumann_mask=0):
+    """TFESpace numbering on the GPU: (gdof[ncells, nloc], ndof, nactive)."""
+    verts = np.ascontiguousarray(verts, dtype=np.float64)
+    nv = 8 if cell_type == CELL_HEXA else 4
+    dim = 2 if cell_type == CELL_QUAD else 3
+    ncells = verts.size // (nv * dim)
+    nloc = {(CELL_QUAD, 1): 4, (CELL_QUAD, 2): 9, (CELL_HEXA, 1): 8, (CELL_HEXA, 2): 27,
+            (CELL_TETRA, 1): 4, (CELL_TETRA, 2): 10}[(cell_type, order)]
+    g = np.zeros((ncells, nloc), dtype=np.int32)
+    nd = ctypes.c_int(0)
+    na = ctypes.c_int(0)
+    _chk(lib().cdg_space_number_device(ctx.c, cell_type, order, neumann_mask, ncells, _dp(verts),
+                                       _ip(g), ctypes.byref(nd), ctypes.byref(na)))
+    return g, nd.value, na.value
+
+
+def structure_build_device(ctx, gdof, ndof):
+    """TStructure on the GPU: (row_ptr, col)."""
+    gdof = np.ascontiguousarray(gdof, dtype=np.int32)
+    ncells, nloc = gdof.shape
+    rp = np.zeros(ndof + 1, dtype=np.int32)
+    nnz = ctypes.c_longlong(0)
+    cap = ncells * nloc * nloc
+    col = np.zeros(cap, dtype=np.int32)
+    _chk(lib().cdg_structure_build_device(ctx.c, ncells, nloc, ndof, _ip(gdof), _ip(rp), _ip(col),
+                                          cap, ctypes.byref(nnz)))
+    return rp, col[:nnz.value].copy()
 
 
 class Context:

@@ -96,8 +96,23 @@ int cdg_context_stream(cdg_context* c, void** stream) {
 // ---------------------------------------------------------------------------
 // host setup hierarchy
 // ---------------------------------------------------------------------------
+// numbering and pattern of one level: host (ctx == null) or device
+static int level_space_pattern(cdg_context* ctx, const Mesh& m, int order, int nmask, Space* s,
+                               Pattern* P) {
+  if (!ctx) {
+    *s = make_space(m, order, nmask);
+    *P = make_pattern(*s);
+    return CDG_OK;
+  }
+  CDG_CUDA(cudaSetDevice(ctx->device));
+  CDG_TRY(device_space(ctx, m, order, nmask, s));
+  P->nrows = s->ndof;
+  return device_pattern(ctx, m.ncells, s->nloc, s->ndof, s->gdof.data(), nullptr, &P->row_ptr,
+                        &P->col, nullptr, nullptr);
+}
+
 static int hierarchy_create(int dim, int order, int roots, int nref, int n_levels, int nmask,
-                            cdg_hierarchy** out) {
+                            cdg_hierarchy** out, cdg_context* ctx = nullptr) {
   if (!out || (dim != 2 && dim != 3) || (order != 1 && order != 2) || roots < 1 || nref < 0 ||
       n_levels < 1 || n_levels > nref + 1) {
     set_error("bad hierarchy arguments");
@@ -109,8 +124,14 @@ static int hierarchy_create(int dim, int order, int roots, int nref, int n_level
   h->order = order;
   for (int l = 0; l < n_levels; ++l) {
     h->mesh.push_back(make_refined_box(dim, roots, nref - l));
-    h->space.push_back(make_space(h->mesh.back(), order, nmask));
-    h->pattern.push_back(make_pattern(h->space.back()));
+    h->space.emplace_back();
+    h->pattern.emplace_back();
+    const int rc = level_space_pattern(ctx, h->mesh.back(), order, nmask, &h->space.back(),
+                                       &h->pattern.back());
+    if (rc != CDG_OK) {
+      delete h;
+      return rc;
+    }
   }
   h->mesh_nested = h->mesh;
   *out = h;
@@ -118,7 +139,8 @@ static int hierarchy_create(int dim, int order, int roots, int nref, int n_level
 }
 
 static int hierarchy_create_tetra(int order, int roots, int nref, int n_levels, double perturb,
-                                  unsigned long long seed, cdg_hierarchy** out) {
+                                  unsigned long long seed, cdg_hierarchy** out,
+                                  cdg_context* ctx = nullptr) {
   if (!out || (order != 1 && order != 2) || roots < 1 || nref < 0 || n_levels < 1 ||
       n_levels > nref + 1 || perturb < 0 || perturb >= 0.5) {
     set_error("bad tetrahedral hierarchy arguments");
@@ -130,8 +152,14 @@ static int hierarchy_create_tetra(int order, int roots, int nref, int n_levels, 
   h->order = order;
   for (int l = 0; l < n_levels; ++l) {
     h->mesh.push_back(make_kuhn_box(roots, nref - l));
-    h->space.push_back(make_space(h->mesh.back(), order, 0));
-    h->pattern.push_back(make_pattern(h->space.back()));
+    h->space.emplace_back();
+    h->pattern.emplace_back();
+    const int rc = level_space_pattern(ctx, h->mesh.back(), order, 0, &h->space.back(),
+                                       &h->pattern.back());
+    if (rc != CDG_OK) {
+      delete h;
+      return rc;
+    }
   }
   h->mesh_nested = h->mesh;
   if (perturb > 0) perturb_interior(h->mesh[0], 1.0 / (roots << nref), perturb, seed);
@@ -147,6 +175,79 @@ int cdg_hierarchy_create(int dim, int order, int roots, int nref, int n_levels, 
 int cdg_hierarchy_create_tetra(int order, int roots, int nref, int n_levels, double perturb,
                                unsigned long long seed, cdg_hierarchy** out) {
   API_GUARD(hierarchy_create_tetra(order, roots, nref, n_levels, perturb, seed, out));
+}
+
+int cdg_hierarchy_create_device(cdg_context* ctx, int dim, int order, int roots, int nref,
+                                int n_levels, int neumann_mask, cdg_hierarchy** out) {
+  if (!ctx) { set_error("null context"); return CDG_ERR_ARG; }
+  API_GUARD(hierarchy_create(dim, order, roots, nref, n_levels, neumann_mask, out, ctx));
+}
+
+int cdg_hierarchy_create_tetra_device(cdg_context* ctx, int order, int roots, int nref,
+                                      int n_levels, double perturb, unsigned long long seed,
+                                      cdg_hierarchy** out) {
+  if (!ctx) { set_error("null context"); return CDG_ERR_ARG; }
+  API_GUARD(hierarchy_create_tetra(order, roots, nref, n_levels, perturb, seed, out, ctx));
+}
+
+static int space_number_device(cdg_context* ctx, int cell_type, int order, int neumann_mask,
+                               int ncells, const double* verts, int* gdof, int* ndof,
+                               int* nactive) {
+  if (!ctx || !verts || !gdof || !ndof || !nactive || ncells < 1 || (order != 1 && order != 2) ||
+      (cell_type != CDG_CELL_QUAD && cell_type != CDG_CELL_HEXA && cell_type != CDG_CELL_TETRA)) {
+    set_error("bad arguments");
+    return CDG_ERR_ARG;
+  }
+  CDG_CUDA(cudaSetDevice(ctx->device));
+  Mesh m;
+  m.shape = cell_type == CDG_CELL_QUAD ? kQuad : cell_type == CDG_CELL_HEXA ? kHexa : kTetra;
+  m.dim = m.shape == kQuad ? 2 : 3;
+  m.nv = n_vertices(m.shape);
+  m.ncells = ncells;
+  m.verts.assign(verts, verts + (size_t)ncells * m.nv * m.dim);
+  Space s;
+  CDG_TRY(device_space(ctx, m, order, neumann_mask, &s));
+  std::memcpy(gdof, s.gdof.data(), s.gdof.size() * sizeof(int));
+  *ndof = s.ndof;
+  *nactive = s.nactive;
+  return CDG_OK;
+}
+
+int cdg_space_number_device(cdg_context* ctx, int cell_type, int order, int neumann_mask,
+                            int ncells, const double* verts, int* gdof, int* ndof, int* nactive) {
+  API_GUARD(space_number_device(ctx, cell_type, order, neumann_mask, ncells, verts, gdof, ndof,
+                                nactive));
+}
+
+static int structure_build_device(cdg_context* ctx, int ncells, int nloc, int ndof,
+                                  const int* gdof, int* row_ptr, int* col, long long capacity,
+                                  long long* nnz) {
+  if (!ctx || !gdof || !row_ptr || !nnz || ncells < 1 || nloc < 1 || nloc > kMaxLoc || ndof < 1) {
+    set_error("bad arguments");
+    return CDG_ERR_ARG;
+  }
+  for (long i = 0; i < (long)ncells * nloc; ++i)
+    if (gdof[i] < 0 || gdof[i] >= ndof) {
+      set_error("global DOF %d out of range at %ld", gdof[i], i);
+      return CDG_ERR_ARG;
+    }
+  CDG_CUDA(cudaSetDevice(ctx->device));
+  std::vector<int> rp, cl;
+  CDG_TRY(device_pattern(ctx, ncells, nloc, ndof, gdof, nullptr, &rp, &cl, nullptr, nullptr));
+  std::memcpy(row_ptr, rp.data(), rp.size() * sizeof(int));
+  *nnz = (long long)cl.size();
+  if (!col || capacity < (long long)cl.size()) {
+    set_error("column capacity %lld below nnz %lld", capacity, (long long)cl.size());
+    return CDG_ERR_LIMIT;
+  }
+  std::memcpy(col, cl.data(), cl.size() * sizeof(int));
+  return CDG_OK;
+}
+
+int cdg_structure_build_device(cdg_context* ctx, int ncells, int nloc, int ndof, const int* gdof,
+                               int* row_ptr, int* col, long long col_capacity, long long* nnz) {
+  API_GUARD(structure_build_device(ctx, ncells, nloc, ndof, gdof, row_ptr, col, col_capacity,
+                                   nnz));
 }
 
 int cdg_hierarchy_destroy(cdg_hierarchy* h) {

@@ -1162,6 +1162,7 @@ int check_device_error(cdg_context* ctx) {
     if (h & kErrZeroDiag) { set_error("zero entry on the diagonal (Jacobi)"); return CDG_ERR_ZERO_DIAG; }
     if (h & kErrSingular) { set_error("singular coarse matrix"); return CDG_ERR_SINGULAR; }
     if (h & kErrBreakdown) { set_error("Unhappy breakdown in flexible gmres"); return CDG_ERR_BREAKDOWN; }
+    if (h & kErrLattice) { set_error("a DOF lies off the lattice of the unit square / cube"); return CDG_ERR_ARG; }
     set_error("device error word %d", h);
     return CDG_ERR_CUDA;
   }

@@ -37,6 +37,7 @@ enum : int {
   kErrZeroDiag = 2,    // zero diagonal entry
   kErrSingular = 4,    // zero pivot in the coarse Gauss-Jordan
   kErrBreakdown = 8,   // FGMRES H(i+1,i) == 0
+  kErrLattice = 16,    // a DOF off the unit box lattice (device numbering)
 };
 
 constexpr int kRedSlots = 32;         // partial-sum rows (one per inner product)
@@ -194,6 +195,13 @@ inline int grid_for(long n, int block) {
 
 // host launchers implemented in the .cu files
 int upload_level(cdg_context* ctx, DevLevel& L);
+// FE space numbering and CSR pattern built on the device (bit-exact with
+// make_space / make_pattern); device_pattern takes gdof from the host or the
+// device and can hand over its device row_ptr / col
+int device_space(cdg_context* ctx, const Mesh& m, int order, int neumann_mask, Space* out);
+int device_pattern(cdg_context* ctx, int ncells, int nloc, int ndof, const int* gdof_host,
+                   const int* gdof_dev, std::vector<int>* row_ptr, std::vector<int>* col,
+                   int** col_dev_out, int** rp_dev_out);
 constexpr int kSellWindow = 256;    // rows sorted by length inside windows of this many rows
 constexpr int kSellMinRows = 32768; // smaller levels keep the CSR kernels (latency bound)
 constexpr int kSellMinWarps = 4096; // lanes per row doubled until a launch has this many warps

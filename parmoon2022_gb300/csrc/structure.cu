@@ -1,0 +1,573 @@
+// structure.cu -- FE space numbering and TStructure (CSR pattern) built on the
+// device, bit-exact with the host setup layer (make_space / make_pattern).
+//
+// Numbering (TFESpace3D::ConstructSpace + TFESpace::compute_various_numbers,
+// src/FE/FESpace3D.C:186, src/FE/FESpace.C:1863-2099): every (cell, local
+// DOF) names a lattice point of the structured mesh; points are numbered per
+// class (inner, non-Dirichlet boundary, Dirichlet last), each class in the
+// order of the point's first appearance over (cell, local DOF).  On the
+// device the first appearance of a point is an atomicMin over the flat index
+// cell * nloc + k (a deterministic result), and the numbers are a three-class
+// exclusive scan over the first appearances in flat order.
+//
+// Pattern (TStructure(space), src/Matrix/Structure.C:226-556, add_entry
+// :122-140, Sort :607-618): row r holds every DOF of every cell containing r,
+// columns sorted ascending, no duplicates, full rows for Dirichlet DOFs.  On
+// the device every incidence appends its cell's DOFs to the row (atomic
+// cursors, so the order is not fixed), then one CTA per row sorts its entries
+// in shared memory (bitonic) and keeps the distinct ones, which fixes the
+// result.  Row offsets are exclusive scans.
+#include <algorithm>
+#include <climits>
+#include <cmath>
+
+#include "common.cuh"
+
+namespace cdg {
+
+// ---------------------------------------------------------------------------
+// exclusive scan with K counters per element (tiles of 2048 elements)
+// ---------------------------------------------------------------------------
+constexpr int kScanThreads = 256;
+constexpr int kScanPer = 8;
+constexpr int kScanTile = kScanThreads * kScanPer;
+
+template <int K>
+__device__ void block_exclusive_scan(long long (&v)[K], long long (&total)[K]) {
+  __shared__ long long sh[kScanThreads / 32][K];
+  const int l = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    long long x = v[k];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long y = __shfl_up_sync(0xffffffffu, x, o);
+      if (l >= o) x += y;
+    }
+    if (l == 31) sh[w][k] = x;
+    v[k] = x - v[k];   // exclusive within the warp
+  }
+  __syncthreads();
+  if (w == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      long long x = l < kScanThreads / 32 ? sh[l][k] : 0;
+      const long long x0 = x;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const long long y = __shfl_up_sync(0xffffffffu, x, o);
+        if (l >= o) x += y;
+      }
+      if (l < kScanThreads / 32) sh[l][k] = x - x0;
+      if (l == kScanThreads / 32 - 1) total[k] = x;   // only lane 7 holds it
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < K; ++k) v[k] += sh[w][k];
+  __syncthreads();
+}
+
+// per-tile sums of f over the tile's elements
+template <int K, typename F>
+__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(long n, F f, long long* tile_sums) {
+  const long base = (long)blockIdx.x * kScanTile + (long)threadIdx.x * kScanPer;
+  long long s[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) s[k] = 0;
+  for (int e = 0; e < kScanPer; ++e) {
+    const long i = base + e;
+    if (i < n) {
+      long long v[K];
+      f(i, v);
+#pragma unroll
+      for (int k = 0; k < K; ++k) s[k] += v[k];
+    }
+  }
+  long long tot[K];
+  block_exclusive_scan<K>(s, tot);
+  __shared__ long long bt[K];
+  // the totals are in lane kScanThreads/32-1 of warp 0
+  if (threadIdx.x == kScanThreads / 32 - 1)
+#pragma unroll
+    for (int k = 0; k < K; ++k) bt[k] = tot[k];
+  __syncthreads();
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int k = 0; k < K; ++k) tile_sums[(size_t)blockIdx.x * K + k] = bt[k];
+}
+
+// exclusive scan of the tile sums in place (one CTA); totals[k] = grand total
+template <int K>
+__global__ void __launch_bounds__(kScanThreads) k_scan_top(int ntiles, long long* tile_sums,
+                                                           long long* totals) {
+  const int per = (ntiles + kScanThreads - 1) / kScanThreads;
+  const int b = threadIdx.x * per, e = min(ntiles, b + per);
+  long long s[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) s[k] = 0;
+  for (int t = b; t < e; ++t)
+#pragma unroll
+    for (int k = 0; k < K; ++k) s[k] += tile_sums[(size_t)t * K + k];
+  long long tot[K];
+  long long pre[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) pre[k] = s[k];
+  block_exclusive_scan<K>(pre, tot);
+  __shared__ long long bt[K];
+  if (threadIdx.x == kScanThreads / 32 - 1)
+#pragma unroll
+    for (int k = 0; k < K; ++k) bt[k] = tot[k];
+  for (int t = b; t < e; ++t)
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const long long v = tile_sums[(size_t)t * K + k];
+      tile_sums[(size_t)t * K + k] = pre[k];
+      pre[k] += v;
+    }
+  __syncthreads();
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int k = 0; k < K; ++k) totals[k] = bt[k];
+}
+
+// g(i, prefix) for every element, prefix = exclusive scan of f before i
+template <int K, typename F, typename G>
+__global__ void __launch_bounds__(kScanThreads) k_scan_apply(long n, F f, G g,
+                                                             const long long* tile_off) {
+  const long base = (long)blockIdx.x * kScanTile + (long)threadIdx.x * kScanPer;
+  long long v[kScanPer][K], s[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) s[k] = 0;
+#pragma unroll
+  for (int e = 0; e < kScanPer; ++e) {
+    const long i = base + e;
+    if (i < n) {
+      f(i, v[e]);
+    } else {
+#pragma unroll
+      for (int k = 0; k < K; ++k) v[e][k] = 0;
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) s[k] += v[e][k];
+  }
+  long long tot[K];
+  block_exclusive_scan<K>(s, tot);
+#pragma unroll
+  for (int k = 0; k < K; ++k) s[k] += tile_off[(size_t)blockIdx.x * K + k];
+#pragma unroll
+  for (int e = 0; e < kScanPer; ++e) {
+    const long i = base + e;
+    if (i < n) g(i, s);
+#pragma unroll
+    for (int k = 0; k < K; ++k) s[k] += v[e][k];
+  }
+}
+
+// scratch for the scans: tile sums + totals
+struct ScanScratch {
+  long long* tiles = nullptr;
+  long long* totals = nullptr;
+  int cap = 0;
+  ~ScanScratch() {
+    if (tiles) cudaFree(tiles);
+    if (totals) cudaFree(totals);
+  }
+};
+
+template <int K, typename F, typename G>
+static int device_scan(cdg_context* ctx, ScanScratch& sc, long n, F f, G g, long long* host_totals) {
+  const int ntiles = (int)std::max<long>(1, (n + kScanTile - 1) / kScanTile);
+  if (sc.cap < ntiles * K) {
+    if (sc.tiles) cudaFree(sc.tiles);
+    CDG_CUDA(cudaMalloc(&sc.tiles, (size_t)ntiles * K * sizeof(long long)));
+    sc.cap = ntiles * K;
+  }
+  if (!sc.totals) CDG_CUDA(cudaMalloc(&sc.totals, 8 * sizeof(long long)));
+  CDG_LAUNCH(ctx, (k_scan_tiles<K, F>), ntiles, kScanThreads, 0, n, f, sc.tiles);
+  CDG_LAUNCH(ctx, (k_scan_top<K>), 1, kScanThreads, 0, ntiles, sc.tiles, sc.totals);
+  CDG_LAUNCH(ctx, (k_scan_apply<K, F, G>), ntiles, kScanThreads, 0, n, f, g, sc.tiles);
+  if (host_totals) {
+    CDG_CUDA(cudaMemcpyAsync(host_totals, sc.totals, K * sizeof(long long),
+                             cudaMemcpyDeviceToHost, ctx->stream));
+    CDG_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
+  return CDG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// numbering
+// ---------------------------------------------------------------------------
+struct NumberingArgs {
+  int shape, dim, nl, nres, n1l, neumann_mask;
+  int comp[3][2];        // boundary component of the face x_a = side
+  double ref[kMaxLoc][3];
+};
+
+// lattice point and class of every (cell, local DOF); first appearance of
+// every point by atomicMin over the flat index
+__global__ void k_dof_keys(long n, NumberingArgs a, const double* __restrict__ verts,
+                           int* __restrict__ keys, signed char* __restrict__ cls,
+                           int* __restrict__ first, int* err) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
+       i += (long)gridDim.x * blockDim.x) {
+    const long c = i / a.nl;
+    const int k = (int)(i - c * a.nl);
+    const int nv = a.shape == kHexa ? 8 : 4;
+    const double* cv = verts + c * nv * a.dim;
+    const double* r = a.ref[k];
+    double x[3] = {0, 0, 0};
+    if (a.shape == kTetra) {
+      for (int d = 0; d < 3; ++d) {
+        double s = cv[d];
+        for (int q = 0; q < 3; ++q) s += r[q] * (cv[(q + 1) * 3 + d] - cv[d]);
+        x[d] = s;
+      }
+    } else {
+      const int e[3] = {1, 3, 4};
+      for (int d = 0; d < a.dim; ++d) {
+        double s = cv[d];
+        for (int q = 0; q < a.dim; ++q) s += 0.5 * (r[q] + 1.0) * (cv[e[q] * a.dim + d] - cv[d]);
+        x[d] = s;
+      }
+    }
+    long key = 0;
+    bool on = true;
+    for (int d = a.dim - 1; d >= 0; --d) {
+      const long li = lround(x[d] * a.nres);
+      on = on && li >= 0 && li <= a.nres;
+      key = key * a.n1l + li;
+    }
+    if (!on) {   // off the lattice: flag it, leave the point out
+      atomicOr(err, kErrLattice);
+      keys[i] = 0;
+      cls[i] = 0;
+      continue;
+    }
+    int cl = 0;
+    for (int d = 0; d < a.dim; ++d)
+      for (int side = 0; side < 2; ++side) {
+        if (fabs(x[d] - side) >= 1e-12) continue;
+        const int t = ((a.neumann_mask >> a.comp[d][side]) & 1) ? 1 : 2;
+        cl = max(cl, t);
+      }
+    keys[i] = (int)key;
+    cls[i] = (signed char)cl;
+    atomicMin(first + key, (int)i);
+  }
+}
+
+struct FirstClassCount {
+  const int* keys;
+  const signed char* cls;
+  const int* first;
+  __device__ void operator()(long i, long long (&v)[3]) const {
+    const bool f = first[keys[i]] == (int)i;
+    const int c = cls[i];
+    v[0] = f && c == 0;
+    v[1] = f && c == 1;
+    v[2] = f && c == 2;
+  }
+};
+
+struct FirstClassNumber {
+  const int* keys;
+  const signed char* cls;
+  const int* first;
+  int* num;
+  signed char* clsk;
+  __device__ void operator()(long i, const long long (&pre)[3]) const {
+    const int key = keys[i];
+    if (first[key] != (int)i) return;
+    const int c = cls[i];
+    num[key] = (int)pre[c];
+    clsk[key] = (signed char)c;
+  }
+};
+
+__global__ void k_gdof(long n, const int* __restrict__ keys, const int* __restrict__ num,
+                       const signed char* __restrict__ clsk, int off1, int off2,
+                       int* __restrict__ gdof) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
+       i += (long)gridDim.x * blockDim.x) {
+    const int key = keys[i];
+    const int c = clsk[key];
+    gdof[i] = (c == 0 ? 0 : c == 1 ? off1 : off2) + num[key];
+  }
+}
+
+__global__ void k_fill_int(long n, int* p, int v) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
+       i += (long)gridDim.x * blockDim.x)
+    p[i] = v;
+}
+
+// device buffers freed on scope exit
+template <typename T>
+struct DBuf {
+  T* p = nullptr;
+  ~DBuf() {
+    if (p) cudaFree(p);
+  }
+  int alloc(size_t n) {
+    CDG_CUDA(cudaMalloc((void**)&p, std::max<size_t>(n, 1) * sizeof(T)));
+    return CDG_OK;
+  }
+};
+
+static int fill_grid(cdg_context* ctx, long n) {
+  return (int)std::max<long>(1, std::min<long>((n + 255) / 256, (long)ctx->num_sms * 16));
+}
+
+int device_space(cdg_context* ctx, const Mesh& m, int order, int neumann_mask, Space* out) {
+  const int dim = m.dim, nl = n_local_dofs(m.shape, order);
+  if (m.ncells < 1) { set_error("empty mesh"); return CDG_ERR_ARG; }
+  double h = 0;
+  for (int a = 0; a < dim; ++a) h += std::fabs(m.verts[dim + a] - m.verts[a]);
+  if (!(h > 0) || order / h > 1e6) {
+    set_error("first cell edge of length %g: no lattice", h);
+    return CDG_ERR_ARG;
+  }
+  const long nres = std::lround(order / h);
+  const long n1l = nres + 1;
+  const double nk = dim == 2 ? (double)n1l * n1l : (double)n1l * n1l * n1l;
+  const long n = (long)m.ncells * nl;
+  if (nk >= 2147483647.0 || n >= 2147483647L) {
+    set_error("mesh too large for 32-bit lattice keys");
+    return CDG_ERR_LIMIT;
+  }
+  const long nkeys = (long)nk;
+  NumberingArgs a{};
+  a.shape = m.shape;
+  a.dim = dim;
+  a.nl = nl;
+  a.nres = (int)nres;
+  a.n1l = (int)n1l;
+  a.neumann_mask = neumann_mask;
+  for (int d = 0; d < dim; ++d)
+    for (int side = 0; side < 2; ++side) {
+      double probe[3] = {0.5, 0.5, 0.5};
+      probe[d] = side;
+      a.comp[d][side] = boundary_component(dim, probe);
+    }
+  for (int k = 0; k < nl; ++k) local_dof_ref_shape(m.shape, order, k, a.ref[k]);
+  cudaStream_t st = ctx->stream;
+  DBuf<double> verts;
+  DBuf<int> keys, first, num, gdof;
+  DBuf<signed char> cls, clsk;
+  CDG_TRY(verts.alloc(m.verts.size()));
+  CDG_TRY(keys.alloc(n));
+  CDG_TRY(cls.alloc(n));
+  CDG_TRY(first.alloc(nkeys));
+  CDG_TRY(num.alloc(nkeys));
+  CDG_TRY(clsk.alloc(nkeys));
+  CDG_TRY(gdof.alloc(n));
+  CDG_CUDA(cudaMemcpyAsync(verts.p, m.verts.data(), m.verts.size() * sizeof(double),
+                           cudaMemcpyHostToDevice, st));
+  CDG_LAUNCH(ctx, k_fill_int, fill_grid(ctx, nkeys), 256, 0, nkeys, first.p, INT_MAX);
+  CDG_LAUNCH(ctx, k_dof_keys, fill_grid(ctx, n), 256, 0, n, a, verts.p, keys.p, cls.p, first.p,
+             ctx->d_err);
+  CDG_TRY(check_device_error(ctx));
+  ScanScratch sc;
+  long long tot[3];
+  CDG_TRY((device_scan<3>(ctx, sc, n, FirstClassCount{keys.p, cls.p, first.p},
+                          FirstClassNumber{keys.p, cls.p, first.p, num.p, clsk.p}, tot)));
+  const int off1 = (int)tot[0], off2 = (int)(tot[0] + tot[1]);
+  CDG_LAUNCH(ctx, k_gdof, fill_grid(ctx, n), 256, 0, n, keys.p, num.p, clsk.p, off1, off2, gdof.p);
+  Space s;
+  s.dim = dim;
+  s.shape = m.shape;
+  s.order = order;
+  s.nloc = nl;
+  s.nactive = off2;
+  s.ndof = (int)(tot[0] + tot[1] + tot[2]);
+  s.gdof.resize(n);
+  CDG_CUDA(cudaMemcpyAsync(s.gdof.data(), gdof.p, n * sizeof(int), cudaMemcpyDeviceToHost, st));
+  CDG_CUDA(cudaStreamSynchronize(st));
+  CDG_TRY(check_device_error(ctx));
+  *out = std::move(s);
+  return CDG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// pattern
+// ---------------------------------------------------------------------------
+__global__ void k_row_count(long n, int nl, const int* __restrict__ gdof, int* __restrict__ cnt) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
+       i += (long)gridDim.x * blockDim.x)
+    atomicAdd(cnt + gdof[i], nl);
+}
+
+__global__ void k_row_max(int nrows, const int* __restrict__ cnt, int* __restrict__ mx) {
+  int m = 0;
+  for (long r = blockIdx.x * (long)blockDim.x + threadIdx.x; r < nrows;
+       r += (long)gridDim.x * blockDim.x)
+    m = max(m, cnt[r]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(mx, m);
+}
+
+struct CountOf {
+  const int* cnt;
+  __device__ void operator()(long i, long long (&v)[1]) const { v[0] = cnt[i]; }
+};
+struct WriteOffset64 {
+  long long* off;
+  __device__ void operator()(long i, const long long (&pre)[1]) const { off[i] = pre[0]; }
+};
+struct WriteOffset32 {
+  int* off;
+  __device__ void operator()(long i, const long long (&pre)[1]) const { off[i] = (int)pre[0]; }
+};
+
+// every incidence (cell, m) appends the cell's DOFs to row gdof[cell, m]
+__global__ void k_row_fill(long n, int nl, const int* __restrict__ gdof,
+                           const long long* __restrict__ tp, int* __restrict__ cursor,
+                           int* __restrict__ tmp) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
+       i += (long)gridDim.x * blockDim.x) {
+    const long c = i / nl;
+    const int r = gdof[i];
+    const long long at = tp[r] + atomicAdd(cursor + r, nl);
+    for (int k = 0; k < nl; ++k) tmp[at + k] = gdof[c * nl + k];
+  }
+}
+
+// one CTA per row: bitonic sort of the row's P (power of two) slots in
+// shared memory, distinct values written back to the row's start in order
+constexpr int kSortThreads = 128;
+__global__ void __launch_bounds__(kSortThreads)
+k_row_sort_unique(int nrows, int P, const long long* __restrict__ tp, const int* __restrict__ cnt,
+                  int* __restrict__ tmp, int* __restrict__ ucnt) {
+  extern __shared__ int s[];
+  __shared__ int wsum[kSortThreads / 32];
+  for (int r = blockIdx.x; r < nrows; r += gridDim.x) {
+    const int len = cnt[r];
+    int* row = tmp + tp[r];
+    for (int t = threadIdx.x; t < P; t += kSortThreads) s[t] = t < len ? row[t] : INT_MAX;
+    __syncthreads();
+    for (int k = 2; k <= P; k <<= 1)
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        for (int t = threadIdx.x; t < P; t += kSortThreads) {
+          const int u = t ^ j;
+          if (u > t) {
+            const int x = s[t], y = s[u];
+            const bool up = (t & k) == 0;
+            if ((x > y) == up) {
+              s[t] = y;
+              s[u] = x;
+            }
+          }
+        }
+        __syncthreads();
+      }
+    // distinct values: thread t owns slots [t*E, t*E+E)
+    const int E = P / kSortThreads;
+    const int b = threadIdx.x * E;
+    int mine = 0;
+    for (int q = b; q < b + E; ++q)
+      if (q < len && (q == 0 || s[q] != s[q - 1])) ++mine;
+    // block exclusive scan of `mine`
+    const int l = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int x = mine;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (l >= o) x += y;
+    }
+    if (l == 31) wsum[w] = x;
+    __syncthreads();
+    int wo = 0, total = 0;
+    for (int q = 0; q < kSortThreads / 32; ++q) {
+      if (q < w) wo += wsum[q];
+      total += wsum[q];
+    }
+    int at = wo + x - mine;
+    for (int q = b; q < b + E; ++q)
+      if (q < len && (q == 0 || s[q] != s[q - 1])) row[at++] = s[q];
+    if (threadIdx.x == 0) ucnt[r] = total;
+    __syncthreads();
+  }
+}
+
+// one warp per row: the distinct entries to their final place
+__global__ void k_row_copy(int nrows, const long long* __restrict__ tp, const int* __restrict__ tmp,
+                           const int* __restrict__ rp, int* __restrict__ col) {
+  const long wid = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5;
+  const int l = threadIdx.x & 31;
+  for (long r = wid; r < nrows; r += ((long)gridDim.x * blockDim.x) >> 5) {
+    const int b = rp[r], e = rp[r + 1];
+    const int* src = tmp + tp[r];
+    for (int q = b + l; q < e; q += 32) col[q] = src[q - b];
+  }
+}
+
+int device_pattern(cdg_context* ctx, int ncells, int nloc, int ndof, const int* gdof_host,
+                   const int* gdof_dev, std::vector<int>* row_ptr, std::vector<int>* col,
+                   int** col_dev_out, int** rp_dev_out) {
+  const long n = (long)ncells * nloc;
+  cudaStream_t st = ctx->stream;
+  DBuf<int> gd, cnt, cursor, tmp, ucnt, rp, cl, mx;
+  DBuf<long long> tp;
+  if (!gdof_dev) {
+    CDG_TRY(gd.alloc(n));
+    CDG_CUDA(cudaMemcpyAsync(gd.p, gdof_host, n * sizeof(int), cudaMemcpyHostToDevice, st));
+    gdof_dev = gd.p;
+  }
+  CDG_TRY(cnt.alloc((size_t)ndof + 1));
+  CDG_TRY(cursor.alloc((size_t)ndof + 1));
+  CDG_TRY(ucnt.alloc((size_t)ndof + 1));
+  CDG_TRY(tp.alloc((size_t)ndof + 1));
+  CDG_TRY(rp.alloc((size_t)ndof + 1));
+  CDG_TRY(mx.alloc(1));
+  CDG_CUDA(cudaMemsetAsync(cnt.p, 0, ((size_t)ndof + 1) * sizeof(int), st));
+  CDG_CUDA(cudaMemsetAsync(cursor.p, 0, ((size_t)ndof + 1) * sizeof(int), st));
+  CDG_CUDA(cudaMemsetAsync(mx.p, 0, sizeof(int), st));
+  CDG_LAUNCH(ctx, k_row_count, fill_grid(ctx, n), 256, 0, n, nloc, gdof_dev, cnt.p);
+  CDG_LAUNCH(ctx, k_row_max, fill_grid(ctx, ndof), 256, 0, ndof, cnt.p, mx.p);
+  ScanScratch sc;
+  long long tot[1];
+  CDG_TRY((device_scan<1>(ctx, sc, (long)ndof + 1, CountOf{cnt.p}, WriteOffset64{tp.p}, tot)));
+  int maxlen = 0;
+  CDG_CUDA(cudaMemcpyAsync(&maxlen, mx.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CDG_CUDA(cudaStreamSynchronize(st));
+  int P = kSortThreads;
+  while (P < maxlen) P <<= 1;
+  if (P > 16384) {
+    set_error("row of %d entries before merging: beyond the shared-memory sort", maxlen);
+    return CDG_ERR_LIMIT;
+  }
+  CDG_TRY(tmp.alloc((size_t)tot[0]));
+  CDG_LAUNCH(ctx, k_row_fill, fill_grid(ctx, n), 256, 0, n, nloc, gdof_dev, tp.p, cursor.p, tmp.p);
+  const int sgrid = (int)std::min<long>(ndof, (long)ctx->num_sms * 16);
+  if (P * sizeof(int) > 48 * 1024)
+    CDG_CUDA(cudaFuncSetAttribute(k_row_sort_unique, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)(P * sizeof(int))));
+  CDG_LAUNCH(ctx, k_row_sort_unique, std::max(1, sgrid), kSortThreads, P * sizeof(int), ndof, P,
+             tp.p, cnt.p, tmp.p, ucnt.p);
+  CDG_CUDA(cudaMemsetAsync(ucnt.p + ndof, 0, sizeof(int), st));
+  long long nnz[1];
+  CDG_TRY((device_scan<1>(ctx, sc, (long)ndof + 1, CountOf{ucnt.p}, WriteOffset32{rp.p}, nnz)));
+  if (nnz[0] >= 2147483647LL) { set_error("pattern beyond 32-bit offsets"); return CDG_ERR_LIMIT; }
+  CDG_TRY(cl.alloc((size_t)nnz[0]));
+  CDG_LAUNCH(ctx, k_row_copy, fill_grid(ctx, (long)ndof * 32), 256, 0, ndof, tp.p, tmp.p, rp.p,
+             cl.p);
+  if (row_ptr) {
+    row_ptr->resize((size_t)ndof + 1);
+    CDG_CUDA(cudaMemcpyAsync(row_ptr->data(), rp.p, ((size_t)ndof + 1) * sizeof(int),
+                             cudaMemcpyDeviceToHost, st));
+  }
+  if (col) {
+    col->resize((size_t)nnz[0]);
+    CDG_CUDA(cudaMemcpyAsync(col->data(), cl.p, (size_t)nnz[0] * sizeof(int),
+                             cudaMemcpyDeviceToHost, st));
+  }
+  CDG_CUDA(cudaStreamSynchronize(st));
+  CDG_TRY(check_device_error(ctx));
+  if (col_dev_out) { *col_dev_out = cl.p; cl.p = nullptr; }
+  if (rp_dev_out) { *rp_dev_out = rp.p; rp.p = nullptr; }
+  return CDG_OK;
+}
+
+}  // namespace cdg
