@@ -258,6 +258,35 @@ int cdg_problem_tcd_step(cdg_problem *p, const cdg_assembly_params *a, double ta
 int cdg_problem_get_tcd_matrix(cdg_problem *p, int level, int which,
                                double *values);
 
+/* ---- checkpoints (src/FE/CheckpointIO.C, src/Matrix/BlockVector.C) ---- */
+/* BlockVector::write_to_file (BlockVector.C:1064-1126): a text line with the
+ * entry count, then the n entries as raw native doubles.  A file that cannot
+ * be opened returns CDG_ERR_ARG (the reference prints a warning and returns) */
+int cdg_vector_write_file(const char *filename, const double *v, long long n);
+/* BlockVector::read_from_file (BlockVector.C:1075-1136): the first line must
+ * hold only the entry count (else CDG_ERR_ARG, "formatting error");
+ * n_expected > 0: the count must equal it (else CDG_ERR_ARG, "unexpected size
+ * to be read"), 0: any count up to capacity (beyond: CDG_ERR_LIMIT).
+ * *n_read receives the file's count whenever the first line parses */
+int cdg_vector_read_file(const char *filename, double *v, long long capacity,
+                         long long n_expected, long long *n_read);
+/* CheckpointIO file name: base, or base + "." + std::to_string(time) unless
+ * overwrite (CheckpointIO.C:68-93) */
+int cdg_checkpoint_file_name(const char *base, double time, int overwrite,
+                             char *out, long long capacity);
+/* the finest-level solution to / from a file in that format
+ * (ConvectionDiffusion: checkpoint_io.write / read, ConvectionDiffusion.C:162,307) */
+int cdg_problem_write_solution(cdg_problem *p, const char *filename);
+int cdg_problem_read_solution(cdg_problem *p, const char *filename);
+/* CheckpointIO::write(data, time_stepping_scheme) (CheckpointIO.C:68-93):
+ * writes the solution after every_n_steps completed steps, never at step 0,
+ * into the CheckpointIO file name; *written = 1 when a file was written.
+ * A restart is cdg_problem_tcd_initialize at the checkpoint's time followed
+ * by cdg_problem_read_solution (the reference reads the checkpoint over the
+ * interpolated initial condition, TimeConvectionDiffusion.C:112-149) */
+int cdg_problem_checkpoint(cdg_problem *p, const char *base, int step, double time,
+                           int every_n_steps, int overwrite, int *written);
+
 /* ---- data access (host buffers) ----------------------------------------- */
 int cdg_problem_level_info(const cdg_problem *p, int level, int *info);
 /* storage of the level's FP64 operator on the device (no reference

@@ -44,6 +44,8 @@ EXPORTED = [
     "cdg_problem_errors_noalloc", "cdg_hierarchy_create_tetra", "cdg_problem_tcd_initialize",
     "cdg_hierarchy_create_device", "cdg_hierarchy_create_tetra_device",
     "cdg_space_number_device", "cdg_structure_build_device",
+    "cdg_vector_write_file", "cdg_vector_read_file", "cdg_checkpoint_file_name",
+    "cdg_problem_write_solution", "cdg_problem_read_solution", "cdg_problem_checkpoint",
     "cdg_problem_tcd_step", "cdg_problem_get_tcd_matrix", "cdg_server_create",
     "cdg_server_destroy", "cdg_request_ndof", "cdg_server_submit", "cdg_server_wait",
     "cdg_server_counters",
@@ -139,6 +141,15 @@ def lib():
             "cdg_hierarchy_create_tetra_device": [P] + [ctypes.c_int] * 4 + [
                 ctypes.c_double, ctypes.c_ulonglong, PP],
             "cdg_space_number_device": [P] + [ctypes.c_int] * 4 + [dp, ip, ip, ip],
+            "cdg_vector_write_file": [ctypes.c_char_p, dp, ctypes.c_longlong],
+            "cdg_vector_read_file": [ctypes.c_char_p, dp, ctypes.c_longlong, ctypes.c_longlong,
+                                     ctypes.POINTER(ctypes.c_longlong)],
+            "cdg_checkpoint_file_name": [ctypes.c_char_p, ctypes.c_double, ctypes.c_int,
+                                         ctypes.c_char_p, ctypes.c_longlong],
+            "cdg_problem_write_solution": [P, ctypes.c_char_p],
+            "cdg_problem_read_solution": [P, ctypes.c_char_p],
+            "cdg_problem_checkpoint": [P, ctypes.c_char_p, ctypes.c_int, ctypes.c_double,
+                                       ctypes.c_int, ctypes.c_int, ip],
             "cdg_structure_build_device": [P] + [ctypes.c_int] * 3 + [
                 ip, ip, ip, ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong)],
             "cdg_problem_tcd_initialize": [P, ctypes.POINTER(AssemblyParams)],
@@ -296,7 +307,26 @@ class Hierarchy:
         return rp, col
 
 
-CELL_QUAD, CELL_HEXA, CELL_TETRA = 2, 3, 4
+def write_vector(filename, v):
+    """BlockVector::write_to_file format: count line, raw doubles."""
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    _chk(lib().cdg_vector_write_file(os.fsencode(filename), _dp(v), v.size))
+
+
+def read_vector(filename, n=0, capacity=None):
+    """BlockVector::read_from_file: n > 0 requires that many entries."""
+    cap = n if n > 0 else (capacity if capacity is not None else os.path.getsize(filename) // 8)
+    v = np.zeros(max(cap, 1))
+    got = ctypes.c_longlong(0)
+    _chk(lib().cdg_vector_read_file(os.fsencode(filename), _dp(v), cap, n, ctypes.byref(got)))
+    return v[:got.value].copy()
+
+
+def checkpoint_file_name(base, time, overwrite=False):
+    buf = ctypes.create_string_buffer(len(base) + 64)
+    _chk(lib().cdg_checkpoint_file_name(os.fsencode(base), time, int(overwrite), buf,
+                                        len(buf)))
+    return buf.value.decode()
 
 
 def space_number_device(ctx, cell_type, order, verts, neumann_mask=0):
@@ -415,6 +445,19 @@ class ConvectionDiffusion:
         _chk(lib().cdg_problem_level_info(self.p, level, _ip(a)))
         return dict(ncells=int(a[0]), nloc=int(a[1]), ndof=int(a[2]), nactive=int(a[3]),
                     nnz=int(a[4]), nv=int(a[5]))
+
+    def write_solution(self, filename):
+        _chk(lib().cdg_problem_write_solution(self.p, os.fsencode(filename)))
+
+    def read_solution(self, filename):
+        _chk(lib().cdg_problem_read_solution(self.p, os.fsencode(filename)))
+
+    def checkpoint(self, base, step, time, every_n_steps=1, overwrite=False):
+        """CheckpointIO::write(solution, time_stepping_scheme); True if written."""
+        w = np.zeros(1, dtype=np.int32)
+        _chk(lib().cdg_problem_checkpoint(self.p, os.fsencode(base), step, time, every_n_steps,
+                                          int(overwrite), _ip(w)))
+        return bool(w[0])
 
     def operator_layout(self, level=0):
         """lanes 0: CSR; else sliced ELLPACK with `lanes` lanes per row."""
