@@ -42,6 +42,7 @@ extern "C" {
 #define CDG_ERR_SINGULAR (-8)     /* singular coarse matrix                  */
 #define CDG_ERR_NO_DEVICE (-9)    /* no CUDA device                          */
 #define CDG_ERR_LIMIT (-10)       /* size beyond a documented maximum        */
+#define CDG_ERR_TIMEOUT (-11)     /* a bounded device-side wait ran out      */
 
 /* example ids: coefficient function + exact solution + boundary data of the
  * problem (the reference's Example_CD2D/Example_CD3D callbacks) */
@@ -289,12 +290,14 @@ int cdg_problem_checkpoint(cdg_problem *p, const char *base, int step, double ti
 
 /* ---- data access (host buffers) ----------------------------------------- */
 int cdg_problem_level_info(const cdg_problem *p, int level, int *info);
-/* storage of the level's FP64 operator on the device (no reference
- * counterpart: ParMooN keeps CSR only): *lanes = 0 for CSR, otherwise the
- * sliced ELLPACK copy with *lanes lanes per row and *slots stored entries
- * (padding included) */
+/* storage and kernels of the level's operators on the device (no reference
+ * counterpart: ParMooN keeps CSR only): *lanes = 0 for a CSR FP64 operator,
+ * otherwise the sliced ELLPACK copy with *lanes lanes per row and *slots
+ * stored entries (padding included); *smoother_chunk = 0 when the FP32
+ * smoother streams CSR through registers, otherwise the entries per chunk it
+ * stages through shared memory */
 int cdg_problem_operator_layout(const cdg_problem *p, int level, int *lanes,
-                                long long *slots);
+                                long long *slots, int *smoother_chunk);
 int cdg_problem_get_matrix(cdg_problem *p, int level, double *values);
 int cdg_problem_get_rhs(cdg_problem *p, int level, double *rhs);
 int cdg_problem_get_solution(cdg_problem *p, double *sol);

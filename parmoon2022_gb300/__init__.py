@@ -158,7 +158,7 @@ def lib():
             "cdg_problem_get_tcd_matrix": [P, ctypes.c_int, ctypes.c_int, dp],
             "cdg_problem_level_info": [P, ctypes.c_int, ip],
             "cdg_problem_operator_layout": [P, ctypes.c_int, ip,
-                                            ctypes.POINTER(ctypes.c_longlong)],
+                                            ctypes.POINTER(ctypes.c_longlong), ip],
             "cdg_problem_get_matrix": [P, ctypes.c_int, dp],
             "cdg_problem_get_rhs": [P, ctypes.c_int, dp],
             "cdg_problem_get_solution": [P, dp], "cdg_problem_set_solution": [P, dp],
@@ -460,11 +460,15 @@ class ConvectionDiffusion:
         return bool(w[0])
 
     def operator_layout(self, level=0):
-        """lanes 0: CSR; else sliced ELLPACK with `lanes` lanes per row."""
+        """lanes 0: CSR FP64 operator; else sliced ELLPACK with `lanes` lanes
+        per row.  smoother_chunk 0: FP32 smoother streams CSR through
+        registers; else entries per chunk staged through shared memory."""
         g = ctypes.c_int(0)
         t = ctypes.c_longlong(0)
-        _chk(lib().cdg_problem_operator_layout(self.p, level, ctypes.byref(g), ctypes.byref(t)))
-        return dict(lanes=g.value, slots=t.value)
+        c = ctypes.c_int(0)
+        _chk(lib().cdg_problem_operator_layout(self.p, level, ctypes.byref(g), ctypes.byref(t),
+                                               ctypes.byref(c)))
+        return dict(lanes=g.value, slots=t.value, smoother_chunk=c.value)
 
     def assemble(self, a):
         _chk(lib().cdg_problem_assemble(self.p, ctypes.byref(a)))

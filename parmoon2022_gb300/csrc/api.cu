@@ -306,6 +306,7 @@ static int finish_problem(cdg_context* ctx, cdg_problem* p, const std::vector<st
   for (auto& L : p->lev) {
     CDG_TRY(upload_level(ctx, L));
     CDG_TRY(build_sell(ctx, L));
+    CDG_TRY(build_bulk(ctx, L));
   }
   for (size_t l = 0; l + 1 < p->lev.size(); ++l) {
     DevLevel& F = p->lev[l];
@@ -617,14 +618,16 @@ static DevLevel* get_level(cdg_problem* p, int level) {
   return &p->lev[level];
 }
 
-int cdg_problem_operator_layout(const cdg_problem* p, int level, int* lanes, long long* slots) {
-  if (!p || level < 0 || level >= (int)p->lev.size() || !lanes || !slots) {
+int cdg_problem_operator_layout(const cdg_problem* p, int level, int* lanes, long long* slots,
+                                int* smoother_chunk) {
+  if (!p || level < 0 || level >= (int)p->lev.size() || !lanes || !slots || !smoother_chunk) {
     set_error("bad arguments");
     return CDG_ERR_ARG;
   }
   const DevLevel& L = p->lev[level];
   *lanes = L.sell_nslices ? L.sell_lanes : 0;
   *slots = L.sell_nslices ? L.sell_total : 0;
+  *smoother_chunk = L.bulk_nchunks ? L.bulk_chunk : 0;
   return CDG_OK;
 }
 

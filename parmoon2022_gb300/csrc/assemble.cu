@@ -969,11 +969,11 @@ int upload_level(cdg_context* ctx, DevLevel& L) {
   CDG_TRY(dalloc(&L.verts, nvd));
   CDG_TRY(dalloc(&L.gdof, (size_t)L.ncells * L.nloc));
   CDG_TRY(dalloc(&L.row_ptr, (size_t)L.ndof + 1));
-  CDG_TRY(dalloc(&L.col, (size_t)L.nnz));
+  CDG_TRY(dalloc(&L.col, (size_t)L.nnz + 4));   // + tail padding of the staged chunks
   CDG_TRY(dalloc(&L.slot, nsl));
   CDG_TRY(dalloc(&L.diag_slot, (size_t)L.ndof));
   CDG_TRY(dalloc(&L.val64, (size_t)L.nnz));
-  CDG_TRY(dalloc(&L.val32, (size_t)L.nnz));
+  CDG_TRY(dalloc(&L.val32, (size_t)L.nnz + 4));
   CDG_TRY(dalloc(&L.rhs, (size_t)L.ndof));
   CDG_TRY(dalloc(&L.sol, (size_t)L.ndof));
   CDG_TRY(dalloc(&L.invdiag64, (size_t)L.ndof));
@@ -1141,8 +1141,35 @@ int build_sell(cdg_context* ctx, DevLevel& L) {
   return CDG_OK;
 }
 
+// chunks of consecutive active rows with at most kBulkChunk entries each
+int build_bulk(cdg_context* ctx, DevLevel& L) {
+  if (L.nactive < kBulkMinRows) return CDG_OK;
+  int chunk = kBulkChunk;   // off by default: slower than k_spmv on GB300 (2-3.5x)
+  if (const char* e = getenv("CDG_BULK_CHUNK")) {   // 0: register-streaming kernels
+    const int c = atoi(e);
+    if (c == 0) return CDG_OK;
+    if (c == 256 || c == 512 || c == 1024) chunk = c;
+  }
+  if (chunk == 0) return CDG_OK;
+  const std::vector<int>& rp = L.pattern.row_ptr;
+  std::vector<int> cr(1, 0);
+  for (int r = 0; r < L.nactive; ++r) {
+    const int len = rp[r + 1] - rp[r];
+    if (len > chunk) return CDG_OK;             // a row beyond a chunk: keep CSR streaming
+    if (rp[r + 1] - rp[cr.back()] > chunk) cr.push_back(r);
+  }
+  cr.push_back(L.nactive);
+  CDG_TRY(dalloc(&L.bulk_row, cr.size()));
+  CDG_CUDA(cudaMemcpyAsync(L.bulk_row, cr.data(), cr.size() * sizeof(int), cudaMemcpyHostToDevice,
+                           ctx->stream));
+  CDG_CUDA(cudaStreamSynchronize(ctx->stream));
+  L.bulk_nchunks = (int)cr.size() - 1;
+  L.bulk_chunk = chunk;
+  return CDG_OK;
+}
+
 int free_level(DevLevel& L) {
-  void* ptrs[] = {L.sell_off, L.sell_row, L.sell_col, L.sell_val, L.sell_pos,L.verts, L.gdof, L.row_ptr, L.col, L.slot, L.diag_slot, L.val64, L.val32,
+  void* ptrs[] = {L.bulk_row, L.sell_off, L.sell_row, L.sell_col, L.sell_val, L.sell_pos,L.verts, L.gdof, L.row_ptr, L.col, L.slot, L.diag_slot, L.val64, L.val32,
                   L.rhs, L.sol, L.invdiag64, L.invdiag32, L.mg_rhs, L.mg_sol, L.mg_tmp,
                   L.mg_def, L.P_rp, L.P_col, L.P_val, L.P_val32, L.R_rp, L.R_col, L.R_val,
                   L.R_val32, L.coarse_inv, L.coarse_work, L.dc_rp, L.dc_col, L.dc_pos,
@@ -1163,6 +1190,7 @@ int check_device_error(cdg_context* ctx) {
     if (h & kErrSingular) { set_error("singular coarse matrix"); return CDG_ERR_SINGULAR; }
     if (h & kErrBreakdown) { set_error("Unhappy breakdown in flexible gmres"); return CDG_ERR_BREAKDOWN; }
     if (h & kErrLattice) { set_error("a DOF lies off the lattice of the unit square / cube"); return CDG_ERR_ARG; }
+    if (h & kErrTimeout) { set_error("a bounded wait for a staged copy ran out"); return CDG_ERR_TIMEOUT; }
     set_error("device error word %d", h);
     return CDG_ERR_CUDA;
   }

@@ -38,6 +38,7 @@ enum : int {
   kErrSingular = 4,    // zero pivot in the coarse Gauss-Jordan
   kErrBreakdown = 8,   // FGMRES H(i+1,i) == 0
   kErrLattice = 16,    // a DOF off the unit box lattice (device numbering)
+  kErrTimeout = 32,    // a bounded wait on a shared-memory barrier ran out
 };
 
 constexpr int kRedSlots = 32;         // partial-sum rows (one per inner product)
@@ -80,6 +81,14 @@ struct DevLevel {
   double* invdiag64 = nullptr;   // ndof
   float* invdiag32 = nullptr;    // ndof
   int rows_per_warp_hint = 1;    // SpMV shape (avg row length)
+  // FP32 smoothing / defect with the CSR stream staged through shared memory
+  // (opt-in, measured slower than the register-streaming kernels on GB300):
+  // active rows cut into chunks of at most kBulkChunk entries, chunk c =
+  // rows [bulk_row[c], bulk_row[c+1]); col and val32 carry 4 entries of tail
+  // padding so a chunk copy rounded out to 16 bytes stays inside them
+  int bulk_nchunks = 0;
+  int bulk_chunk = 0;            // entries per chunk at most
+  int* bulk_row = nullptr;       // nchunks+1
   // sliced ELLPACK copy of the FP64 matrix (the FGMRES operator, the FP64
   // multigrid smoother and defect) on levels of at least kSellMinRows rows:
   // G = sell_lanes lanes per row, slices of 32/G rows (one warp),
@@ -203,6 +212,10 @@ int device_pattern(cdg_context* ctx, int ncells, int nloc, int ndof, const int* 
                    const int* gdof_dev, std::vector<int>* row_ptr, std::vector<int>* col,
                    int** col_dev_out, int** rp_dev_out);
 constexpr int kSellWindow = 256;    // rows sorted by length inside windows of this many rows
+constexpr int kBulkChunk = 0;       // CSR entries per staged chunk; 0: off unless
+                                    // CDG_BULK_CHUNK (256, 512, 1024) asks for it
+constexpr int kBulkMinRows = 65536; // smaller levels keep the register-streaming kernels
+int build_bulk(cdg_context* ctx, DevLevel& L);
 constexpr int kSellMinRows = 32768; // smaller levels keep the CSR kernels (latency bound)
 constexpr int kSellMinWarps = 4096; // lanes per row doubled until a launch has this many warps
 int build_sell(cdg_context* ctx, DevLevel& L);
