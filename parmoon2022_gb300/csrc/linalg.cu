@@ -64,11 +64,15 @@ __device__ __forceinline__ T group_sum(T s) {
 //   MODE 0: y = A x
 //   MODE 1: y = b - A x                         (calculate_defect)
 //   MODE 2: y = x + w D^-1 (b - A x)            (JacobiSmoother::smooth)
+//   MODE 3: MODE 2, and y also in FP64 into z (block z at vector *di when di
+//           is given, and zcur): the last smoothing step of a mixed-precision
+//           cycle hands its result to the FP64 Krylov method directly
 template <typename T, int TPR, int UNR, int MODE>
 __global__ void __launch_bounds__(256)
 k_spmv(int n, int nactive, const int* __restrict__ rp, const int* __restrict__ col,
        const T* __restrict__ val, const T* __restrict__ x, const T* __restrict__ b,
-       const T* __restrict__ invd, T w, T* __restrict__ y) {
+       const T* __restrict__ invd, T w, T* __restrict__ y, double* __restrict__ z = nullptr,
+       const int* di = nullptr, double* __restrict__ zcur = nullptr) {
   const long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
   const int row = (int)(gt / TPR);
   const int sub = threadIdx.x % TPR;
@@ -80,7 +84,15 @@ k_spmv(int n, int nactive, const int* __restrict__ rp, const int* __restrict__ c
   if (row >= nactive) s = xr;
   if (MODE == 0) y[row] = s;
   else if (MODE == 1) y[row] = b[row] - s;
-  else y[row] = xr + w * (invd[row] * (b[row] - s));
+  else {
+    const T yr = xr + w * (invd[row] * (b[row] - s));
+    y[row] = yr;
+    if (MODE == 3) {
+      const double zr = (double)yr;
+      (di ? z + (size_t)(*di) * n : z)[row] = zr;
+      if (zcur) zcur[row] = zr;
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1017,6 +1029,21 @@ static int vec_grid(cdg_context* ctx, long n) {
   return (int)(g > cap ? cap : (g < 1 ? 1 : g));
 }
 
+// last smoothing step of the finest level with the FP64 hand-over (MODE 3)
+template <typename T>
+static int smooth_out(cdg_context* ctx, const DevLevel& L, const T* val, const T* x, const T* b,
+                      const T* invd, T w, T* y, double* z, const int* di, double* zcur) {
+  const int tpr = L.rows_per_warp_hint;
+  const int grid = (int)(((long)L.ndof * tpr + 255) / 256);
+  switch (tpr) {
+    case 2: CDG_LAUNCH(ctx, (k_spmv<T, 2, 8, 3>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y, z, di, zcur); break;
+    case 4: CDG_LAUNCH(ctx, (k_spmv<T, 4, 8, 3>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y, z, di, zcur); break;
+    case 8: CDG_LAUNCH(ctx, (k_spmv<T, 8, 8, 3>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y, z, di, zcur); break;
+    default: CDG_LAUNCH(ctx, (k_spmv<T, 16, 8, 3>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y, z, di, zcur); break;
+  }
+  return CDG_OK;
+}
+
 // sliced ELLPACK smoothing / defect on a multigrid level
 template <typename T, int MODE>
 static int sell_mg(cdg_context* ctx, const DevLevel& L, const T* val, const T* x, const T* b,
@@ -1076,6 +1103,31 @@ k_first_smooth(int n, int nactive, int with_dirichlet, const int* __restrict__ d
     } else {
       const T x0 = with_dirichlet ? b[i] : (T)0;
       x1[i] = x0 + w * (invd[i] * (b[i] - x0));
+    }
+  }
+}
+
+// the finest level's first smoothing step fused with the cycle's start
+// (Iteration_multigrid::apply copies the Krylov vector into the multigrid
+// rhs): rhs = v in T, and x1 as k_first_smooth computes it from that rhs,
+// reading the Dirichlet neighbours' rhs straight from v
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_first_smooth_init(int n, int nactive, const int* __restrict__ dc_rp,
+                    const int* __restrict__ dc_col, const int* __restrict__ dc_pos,
+                    const T* __restrict__ val, const double* __restrict__ v,
+                    const T* __restrict__ invd, T w, T* __restrict__ rhs, T* __restrict__ x1,
+                    const int* di) {
+  if (di) v += (size_t)(*di) * n;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const T bi = (T)v[i];
+    rhs[i] = bi;
+    if (i < nactive) {
+      T s = 0;
+      for (int k = dc_rp[i]; k < dc_rp[i + 1]; ++k) s += val[dc_pos[k]] * (T)v[dc_col[k]];
+      x1[i] = w * (invd[i] * (bi - s));
+    } else {
+      x1[i] = bi + w * (invd[i] * (bi - bi));
     }
   }
 }
@@ -1156,8 +1208,21 @@ static int mg_cycle(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s
   const int nl = s.multigrid_n_levels;
   auto lv = [&](int m) -> DevLevel& { return p->lev[nl - 1 - m]; };
   DevLevel& F = p->lev[0];
-  CDG_LAUNCH(ctx, k_mg_init<T>, vec_grid(ctx, F.ndof), 256, 0, F.ndof, F.nactive, v,
-             (T*)F.mg_rhs, (T*)F.mg_sol, di);
+  // with pre-smoothing on a finest level above the coarse solve, the first
+  // smoothing step also does the start (rhs = v, x0 = Dirichlet values)
+  const bool fused_start = nl > 1 && s.multigrid_n_pre_smooth > 0;
+  if (fused_start) {
+    CDG_LAUNCH(ctx, k_first_smooth_init<T>, vec_grid(ctx, F.ndof), 256, 0, F.ndof, F.nactive,
+               F.dc_rp, F.dc_col, F.dc_pos, Prec<T>::val(F), v, Prec<T>::invd(F),
+               (T)s.jacobi_damp, (T*)F.mg_rhs, (T*)F.mg_tmp, di);
+    std::swap(F.mg_sol, F.mg_tmp);
+  } else {
+    CDG_LAUNCH(ctx, k_mg_init<T>, vec_grid(ctx, F.ndof), 256, 0, F.ndof, F.nactive, v,
+               (T*)F.mg_rhs, (T*)F.mg_sol, di);
+  }
+  // the FP64 result of the last finest-level smoothing step goes to z directly
+  // (CSR smoother; the FP64 sliced smoother keeps the separate conversion)
+  bool z_written = false;
   std::vector<int> rec(nl, s.multigrid_cycle_type == 0 ? 1 : 2), seq;
   rec[nl - 1] = 1;
   seq.push_back(kDummy);
@@ -1179,12 +1244,27 @@ static int mg_cycle(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s
       }
       const bool from_below = seq[step - 1] == kUp;
       const int dir = seq[step];
-      if (from_below)
-        for (int i = 0; i < s.multigrid_n_post_smooth; ++i) CDG_TRY(smooth<T>(ctx, L, damp));
+      if (from_below) {
+        const bool hand_over = level == nl - 1 && dir == kEnd && !Prec<T>::has_sell(L) &&
+                               s.multigrid_n_post_smooth > 0;
+        for (int i = 0; i < s.multigrid_n_post_smooth; ++i) {
+          if (hand_over && i + 1 == s.multigrid_n_post_smooth) {
+            CDG_TRY(smooth_out<T>(ctx, L, Prec<T>::val(L), (const T*)L.mg_sol,
+                                  (const T*)L.mg_rhs, Prec<T>::invd(L), damp, (T*)L.mg_tmp, z,
+                                  di, zcur));
+            std::swap(L.mg_sol, L.mg_tmp);
+            z_written = true;
+          } else {
+            CDG_TRY(smooth<T>(ctx, L, damp));
+          }
+        }
+      }
       if (dir == kDown) {
         for (int i = 0; i < s.multigrid_n_pre_smooth; ++i) {
           // the start iterate is zero (finest: Dirichlet values) unless the
           // level was smoothed since its solution was last reset (W, F cycles)
+          if (i == 0 && level == nl - 1 && fused_start && !L.mg_visited)
+            continue;   // done by k_first_smooth_init
           if (i == 0 && !L.mg_visited)
             CDG_TRY(first_smooth<T>(ctx, L, damp, level == nl - 1));
           else
@@ -1193,9 +1273,13 @@ static int mg_cycle(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s
         L.mg_visited = true;
         CDG_TRY(defect<T>(ctx, L));
         DevLevel& C = lv(level - 1);
-        // coarse start iterate is set by the restriction target's consumer:
-        // the coarse solution starts from zero
-        CDG_CUDA(cudaMemsetAsync(C.mg_sol, 0, (size_t)C.ndof * sizeof(T), ctx->stream));
+        // the coarse solution starts from zero; a first smoothing step or the
+        // direct coarse solve overwrites it without reading it
+        const bool coarsest = level - 1 == 0;
+        const bool read_start = coarsest ? s.multigrid_smoother_coarse != 0
+                                         : s.multigrid_n_pre_smooth == 0;
+        if (read_start)
+          CDG_CUDA(cudaMemsetAsync(C.mg_sol, 0, (size_t)C.ndof * sizeof(T), ctx->stream));
         C.mg_visited = false;   // zero start iterate again: shortcut valid
         CDG_LAUNCH(ctx, (k_restrict<T, 8>), grid_for<int>((long)C.ndof * 8, 256), 256, 0,
                    C.ndof, C.nactive, L.R_rp, L.R_col, Prec<T>::R(L), (const T*)L.mg_def,
@@ -1209,8 +1293,9 @@ static int mg_cycle(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s
       }
     }
   }
-  CDG_LAUNCH(ctx, k_to_double<T>, vec_grid(ctx, F.ndof), 256, 0, F.ndof, (const T*)F.mg_sol, z,
-             di, zcur);
+  if (!z_written)
+    CDG_LAUNCH(ctx, k_to_double<T>, vec_grid(ctx, F.ndof), 256, 0, F.ndof, (const T*)F.mg_sol, z,
+               di, zcur);
   return CDG_OK;
 }
 
