@@ -1385,6 +1385,66 @@ static void neumann_edge(orc_problem *p, level_t *L, int cell, int j,
   }
 }
 
+/* Neumann boundary integral on a hexahedron face (Assemble3D.C:552-655,
+ * quadrilateral faces): g = eps * n.grad(u) with the outward unit normal n of
+ * the boundary component, tensor Gauss rule of degree 2p on [-1,1]^2 mapped
+ * bilinearly through the face's vertices, weight times |dx/ds x dx/dt| */
+static void neumann_face(orc_problem *p, level_t *L, int cell, int j, int comp,
+                         double *rhs) {
+  const orc_config *c = &p->cfg;
+  const double *cv = L->verts + (size_t)cell * L->nv * 3;
+  int nl = L->nloc;
+  int np = line_points_for_degree(2 * c->order);
+  double lx[10], lw[10];
+  gauss_legendre(np, lx, lw);
+  static const double nrm[6][3] = {{0, 0, -1}, {0, -1, 0}, {1, 0, 0},
+                                   {0, 1, 0},  {-1, 0, 0}, {0, 0, 1}};
+  double X[4][3];
+  for (int m = 0; m < 4; ++m)
+    for (int a = 0; a < 3; ++a) X[m][a] = cv[HEX_FACE[j][m] * 3 + a];
+  double c1[3], c2[3], c3[3];
+  for (int a = 0; a < 3; ++a) {
+    c1[a] = (-X[0][a] + X[1][a] + X[2][a] - X[3][a]) * 0.25;
+    c2[a] = (-X[0][a] - X[1][a] + X[2][a] + X[3][a]) * 0.25;
+    c3[a] = (X[0][a] - X[1][a] + X[2][a] - X[3][a]) * 0.25;
+  }
+  affine_t A;
+  cell_affine(3, cv, &A);
+  for (int l1 = 0; l1 < np; ++l1)
+    for (int l2 = 0; l2 < np; ++l2) {
+      double ps = lx[l1], pt = lx[l2];
+      double t0 = 0.5 * (ps + 1), t1 = 0.5 * (pt + 1);
+      double lc[4] = {(1 - t0) * (1 - t1), t0 * (1 - t1), t0 * t1, (1 - t0) * t1};
+      double x[3] = {0, 0, 0};
+      for (int m = 0; m < 4; ++m)
+        for (int a = 0; a < 3; ++a) x[a] += lc[m] * X[m][a];
+      double u[6];
+      exact_sol(c, x, u);
+      double g = c->eps * (nrm[comp][0] * u[1] + nrm[comp][1] * u[2] + nrm[comp][2] * u[3]);
+      double ta[3], tb[3];
+      for (int a = 0; a < 3; ++a) {
+        ta[a] = c1[a] + pt * c3[a];
+        tb[a] = c2[a] + ps * c3[a];
+      }
+      double nx = ta[1] * tb[2] - ta[2] * tb[1];
+      double ny = ta[2] * tb[0] - ta[0] * tb[2];
+      double nz = ta[0] * tb[1] - ta[1] * tb[0];
+      double sc = g * lw[l1] * lw[l2] * sqrt(nx * nx + ny * ny + nz * nz);
+      double xi[3];
+      for (int a = 0; a < 3; ++a) {
+        double t = 0;
+        for (int r = 0; r < 3; ++r) t += A.Jinv[a][r] * (x[r] - A.x0[r]);
+        xi[a] = t;
+      }
+      double ref[MAXLOC][NDER];
+      ref_basis(3, c->order, xi, ref);
+      for (int k = 0; k < nl; ++k) {
+        int d = L->gdof[cell * nl + k];
+        if (d < L->nactive) rhs[d] += sc * ref[k][0];
+      }
+    }
+}
+
 /* local mass matrix, TCDMass (CD_local_assembling_routines.C:156-167):
  * M_ij = int phi_i phi_j; with SUPG plus TCDMassSUPG (:261-321):
  * int delta (b . grad phi_i) phi_j */
@@ -1484,7 +1544,7 @@ static int assemble_into(orc_problem *p, int level, double *val, double *rhs,
     return 0;
   }
   /* boundary data: Dirichlet values by point evaluation at the nodes (nodal
-   * functionals of Q1/Q2), Neumann integrals (2D) */
+   * functionals of Q1/Q2), Neumann integrals over edges (2D) and faces (3D) */
   int nj = dim == 2 ? 4 : 6;
   for (int cell = 0; cell < L->ncells; ++cell) {
     const double *cv = L->verts + (size_t)cell * L->nv * dim;
@@ -1508,6 +1568,8 @@ static int assemble_into(orc_problem *p, int level, double *val, double *rhs,
         }
       } else if (dim == 2) {
         neumann_edge(p, L, cell, j, rhs);
+      } else {
+        neumann_face(p, L, cell, j, comp, rhs);
       }
     }
   }

@@ -661,7 +661,8 @@ __device__ int boundary_comp_d(int dim, const double* x) {
 //   phase 1  thread per cell: x0, J, |det J| (inverse and delta for SUPG)
 //   phase 2  (cell, quadrature point): w |det J| f(x_q)
 //   phase 3  (cell, local DOF): F_i = sum_q fw_q (phi_i + delta b.grad phi_i),
-//            Dirichlet values at the nodes, Neumann edge integrals (2D)
+//            Dirichlet values at the nodes, Neumann edge integrals (2D) and
+//            face integrals (hexahedra)
 constexpr int kRhsTile = 32;
 constexpr int kRhsGeo = 18;   // x0[3], J[9], |det|, delta, b'[3]
 
@@ -675,7 +676,7 @@ k_rhs(AsmCoefs k, int ncells, int nactive, const double* __restrict__ verts,
   __shared__ double fw[kRhsTile][128];
   const int tile0 = blockIdx.x * kRhsTile;
   const int nt = min(kRhsTile, ncells - tile0);
-  const bool need_inv = k.supg || (DIM == 2 && k.neumann_mask);
+  const bool need_inv = k.supg || k.neumann_mask;
   if (threadIdx.x < nt) {
     const int c = threadIdx.x;
     const double* cv = verts + (size_t)(tile0 + c) * NV * DIM;
@@ -789,6 +790,77 @@ k_rhs(AsmCoefs k, int ncells, int nactive, const double* __restrict__ verts,
           int n1 = k.order + 1;
           G += gval * hE * lw[l] * (v0[i % n1] * v1[i / n1]);
         }
+        F += G;
+      }
+    }
+    // Neumann data on boundary faces of hexahedra (Assemble3D.C:552-655):
+    // g = eps n.grad(u), tensor Gauss rule of degree 2p on [-1,1]^2 mapped
+    // bilinearly through the face's vertices, weight times |dx/ds x dx/dt|
+    if (DIM == 3 && k.neumann_mask && k.shape == kHexa) {
+      const double* cv = verts + (size_t)cell * NV * DIM;
+      const int hf[6][4] = {{0, 1, 2, 3}, {0, 4, 5, 1}, {1, 5, 6, 2},
+                            {2, 6, 7, 3}, {0, 3, 7, 4}, {4, 7, 6, 5}};
+      const double nrm[6][3] = {{0, 0, -1}, {0, -1, 0}, {1, 0, 0},
+                                {0, 1, 0},  {-1, 0, 0}, {0, 0, 1}};
+      Affine A;
+      cell_affine_s(k.shape, DIM, cv, A);
+      const int n1 = k.order + 1;
+      const int ia = i % n1, ib = (i / n1) % n1, ic = i / (n1 * n1);
+      double lx[3], lw[3];
+      if (n1 == 2) {
+        lx[0] = -0.57735026918962576451; lx[1] = 0.57735026918962576451;
+        lw[0] = lw[1] = 1.0;
+      } else {
+        lx[0] = -0.77459666924148337704; lx[1] = 0.0; lx[2] = 0.77459666924148337704;
+        lw[0] = lw[2] = 5.0 / 9.0; lw[1] = 8.0 / 9.0;
+      }
+      for (int j = 0; j < 6; ++j) {
+        double X[4][3], ctr[3] = {0, 0, 0};
+        for (int m = 0; m < 4; ++m)
+          for (int a = 0; a < 3; ++a) {
+            X[m][a] = cv[hf[j][m] * 3 + a];
+            ctr[a] += 0.25 * X[m][a];
+          }
+        const int comp = boundary_comp_d(3, ctr);
+        if (comp < 0 || !((k.neumann_mask >> comp) & 1)) continue;
+        double c1[3], c2[3], c3[3];
+        for (int a = 0; a < 3; ++a) {
+          c1[a] = (-X[0][a] + X[1][a] + X[2][a] - X[3][a]) * 0.25;
+          c2[a] = (-X[0][a] - X[1][a] + X[2][a] + X[3][a]) * 0.25;
+          c3[a] = (X[0][a] - X[1][a] + X[2][a] - X[3][a]) * 0.25;
+        }
+        double G = 0.0;
+        for (int l1 = 0; l1 < n1; ++l1)
+          for (int l2 = 0; l2 < n1; ++l2) {
+            const double ps = lx[l1], pt = lx[l2];
+            const double t0 = 0.5 * (ps + 1), t1 = 0.5 * (pt + 1);
+            const double lc[4] = {(1 - t0) * (1 - t1), t0 * (1 - t1), t0 * t1, (1 - t0) * t1};
+            double x[3] = {0, 0, 0};
+            for (int m = 0; m < 4; ++m)
+              for (int a = 0; a < 3; ++a) x[a] += lc[m] * X[m][a];
+            double u[6];
+            ex_exact(k, x, u);
+            const double gval =
+                k.eps * (nrm[comp][0] * u[1] + nrm[comp][1] * u[2] + nrm[comp][2] * u[3]);
+            double ta[3], tb[3];
+            for (int a = 0; a < 3; ++a) {
+              ta[a] = c1[a] + pt * c3[a];
+              tb[a] = c2[a] + ps * c3[a];
+            }
+            const double nx = ta[1] * tb[2] - ta[2] * tb[1];
+            const double ny = ta[2] * tb[0] - ta[0] * tb[2];
+            const double nz = ta[0] * tb[1] - ta[1] * tb[0];
+            double xi[3];
+            for (int a = 0; a < 3; ++a)
+              xi[a] = A.Ji[a][0] * (x[0] - A.x0[0]) + A.Ji[a][1] * (x[1] - A.x0[1]) +
+                      A.Ji[a][2] * (x[2] - A.x0[2]);
+            double v0[3], v1[3], v2[3];
+            line_basis_d(k.order, xi[0], v0);
+            line_basis_d(k.order, xi[1], v1);
+            line_basis_d(k.order, xi[2], v2);
+            G += gval * lw[l1] * lw[l2] * sqrt(nx * nx + ny * ny + nz * nz) *
+                 (v0[ia] * v1[ib] * v2[ic]);
+          }
         F += G;
       }
     }
@@ -1282,6 +1354,10 @@ static TermSet stiffness_set(const AsmCoefs& k) {
 
 static int check_coefs(const AsmCoefs& k) {
   if (k.nqp > 128) { set_error("quadrature rule too large"); return CDG_ERR_ARG; }
+  if (k.shape == kTetra && k.neumann_mask) {
+    set_error("Neumann boundaries on tetrahedral meshes are not supported");
+    return CDG_ERR_ARG;
+  }
   if (k.supg && k.linear_b) {
     set_error("SUPG with a convection field linear in x is not supported");
     return CDG_ERR_ARG;

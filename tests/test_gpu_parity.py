@@ -37,6 +37,9 @@ CASES = {
     "q2_3d_supg": (3, 2, 2, po.EX_POLYEXP, 1e-3, (0.57735026918962573, 0.57735026918962573,
                                                      0.57735026918962573), 0.0, True, 5, 0),
     "q2_3d_galerkin": (3, 2, 2, po.EX_SINE, 1.0, (0.0, 0.0, 0.0), 0.0, False, 2, 0),
+    # Neumann faces on hexahedra (x = 1 and z = 1; y = 0 alone)
+    "q1_3d_neumann": (3, 1, 3, po.EX_SINE, 0.1, (1.0, 0.3, -0.2), 1.0, False, 2, 36),
+    "q2_3d_neumann_supg": (3, 2, 2, po.EX_POLYEXP, 1e-3, (0.6, 0.64, 0.48), 0.0, True, 5, 2),
 }
 
 
