@@ -241,7 +241,9 @@ def run_gpu(args):
     LEVELS = w["levels"]
     hkw = dict(n_levels=LEVELS, roots=w["roots"])
     hier, setup = timed_hierarchies(pg, ctx, (w["dim"], w["order"], w["nref"]), hkw, LEVELS)
+    t0 = time.perf_counter()
     cd = pg.ConvectionDiffusion(ctx, hier)
+    setup["problem_create_s"] = time.perf_counter() - t0
     a = spec_assembly(pg, w)
     precs = w["precisions"]
     s_main = spec_solver(pg, w, precs[0])
@@ -451,7 +453,9 @@ def run_gpu_tcd(args):
     hier, setup = timed_hierarchies(pg, ctx, (3, 2, nref),
                                     dict(n_levels=L, roots=TCD["roots"], tetra=True,
                                          perturb=TCD["perturb"], seed=TCD["seed"]), L)
+    t0 = time.perf_counter()
     cd = pg.ConvectionDiffusion(ctx, hier)
+    setup["problem_create_s"] = time.perf_counter() - t0
     info = [cd.info(l) for l in range(L)]
     n = info[0]["ndof"]
     tau = TCD["tau"]

@@ -299,21 +299,51 @@ static int up(T** d, const std::vector<T>& h, cudaStream_t st) {
 }
 extern "C" {
 
+// CDG_SETUP_TIMING=1: print the seconds of each phase of problem creation
+struct PhaseClock {
+  bool on = getenv("CDG_SETUP_TIMING") != nullptr;
+  std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+  double acc[4] = {0, 0, 0, 0};
+  void lap(int k, cudaStream_t st) {
+    if (!on) return;
+    cudaStreamSynchronize(st);
+    const auto now = std::chrono::steady_clock::now();
+    acc[k] += std::chrono::duration<double>(now - t).count();
+    t = now;
+  }
+  ~PhaseClock() {
+    if (on)
+      fprintf(stderr, "problem setup: upload+slots %.3f s, sliced copy %.3f s, transfers %.3f s\n",
+              acc[0], acc[1], acc[2]);
+  }
+};
+
 static int finish_problem(cdg_context* ctx, cdg_problem* p, const std::vector<std::vector<int>>& parents,
                           const std::vector<Mesh>* nested) {
+  PhaseClock clk;
   CDG_CUDA(cudaMalloc(&p->d_zero_diag, sizeof(int)));
   CDG_CUDA(cudaMemsetAsync(p->d_zero_diag, 0, sizeof(int), ctx->stream));
   for (auto& L : p->lev) {
     CDG_TRY(upload_level(ctx, L));
+    clk.lap(0, ctx->stream);
     CDG_TRY(build_sell(ctx, L));
     CDG_TRY(build_bulk(ctx, L));
+    clk.lap(1, ctx->stream);
   }
   for (size_t l = 0; l + 1 < p->lev.size(); ++l) {
     DevLevel& F = p->lev[l];
     DevLevel& C = p->lev[l + 1];
-    HostCsr P, R;
     const Mesh& fm = nested ? (*nested)[l] : F.mesh;
     const Mesh& cm = nested ? (*nested)[l + 1] : C.mesh;
+    // on the device; the host builder stays for rows beyond the device sort
+    const int drc = device_transfer(ctx, fm, F.space, cm, C.space, parents[l].data(), F.gdof,
+                                    C.gdof, F);
+    if (drc == CDG_OK) {
+      clk.lap(2, ctx->stream);
+      continue;
+    }
+    if (drc != CDG_ERR_LIMIT) return drc;
+    HostCsr P, R;
     make_transfer(fm, F.space, cm, C.space, parents[l].data(), &P, &R);
     std::vector<float> pv(P.val.begin(), P.val.end()), rv(R.val.begin(), R.val.end());
     CDG_TRY(up(&F.P_rp, P.row_ptr, ctx->stream));
@@ -326,6 +356,7 @@ static int finish_problem(cdg_context* ctx, cdg_problem* p, const std::vector<st
     CDG_TRY(up(&F.R_val32, rv, ctx->stream));
     F.P_nnz = (int)P.col.size();
     F.R_nnz = (int)R.col.size();
+    clk.lap(2, ctx->stream);
   }
   CDG_CUDA(cudaStreamSynchronize(ctx->stream));
   return CDG_OK;

@@ -211,6 +211,12 @@ int device_space(cdg_context* ctx, const Mesh& m, int order, int neumann_mask, S
 int device_pattern(cdg_context* ctx, int ncells, int nloc, int ndof, const int* gdof_host,
                    const int* gdof_dev, std::vector<int>* row_ptr, std::vector<int>* col,
                    int** col_dev_out, int** rp_dev_out);
+// prolongation / restriction of the fine level F (the matrices of
+// make_transfer) built on the device into F.P_* / F.R_*; fm, cm: the nested
+// (unperturbed) meshes, parent: coarse cell of each fine cell (host)
+int device_transfer(cdg_context* ctx, const Mesh& fm, const Space& fs, const Mesh& cm,
+                    const Space& cs, const int* parent_host, const int* fgdof_dev,
+                    const int* cgdof_dev, DevLevel& F);
 constexpr int kSellWindow = 256;    // rows sorted by length inside windows of this many rows
 constexpr int kBulkChunk = 0;       // CSR entries per staged chunk; 0: off unless
                                     // CDG_BULK_CHUNK (256, 512, 1024) asks for it

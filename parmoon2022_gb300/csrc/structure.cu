@@ -315,6 +315,12 @@ struct DBuf {
   }
 };
 
+template <typename T>
+static int dalloc_raw(T** p, size_t n) {
+  CDG_CUDA(cudaMalloc((void**)p, std::max<size_t>(n, 1) * sizeof(T)));
+  return CDG_OK;
+}
+
 static int fill_grid(cdg_context* ctx, long n) {
   return (int)std::max<long>(1, std::min<long>((n + 255) / 256, (long)ctx->num_sms * 16));
 }
@@ -568,6 +574,405 @@ int device_pattern(cdg_context* ctx, int ncells, int nloc, int ndof, const int* 
   if (col_dev_out) { *col_dev_out = cl.p; cl.p = nullptr; }
   if (rp_dev_out) { *rp_dev_out = rp.p; rp.p = nullptr; }
   return CDG_OK;
+}
+
+
+// ---------------------------------------------------------------------------
+// grid transfer (GridTransfer::Prolongate / DefectRestriction with the child-
+// local matrices of GetProlongationMatrix3D, src/Multigrid/GridTransfer.C,
+// src/FE/FEDatabase.C:261-574) built on the device: the same matrices as
+// make_transfer -- row i of P holds, for every coarse DOF j, the value of the
+// parent's basis function j at fine node i, summed over the fine cells that
+// contain node i in (cell, local DOF) order and divided by their number; R is
+// the transpose with the fine indices of a row ascending
+// ---------------------------------------------------------------------------
+namespace {
+
+struct TransferArgs {
+  int shape, dim, p, nl, nv;
+  double ref[kMaxLoc][3];
+};
+
+__device__ void parent_basis_values(const TransferArgs& a, const double* __restrict__ cvf,
+                                    const double* __restrict__ cvc, int k, double* val) {
+  const int dim = a.dim;
+  double x0[3] = {0, 0, 0}, J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, Ji[3][3];
+  for (int r = 0; r < dim; ++r) x0[r] = cvc[r];
+  if (a.shape == kTetra) {
+    for (int q = 0; q < 3; ++q)
+      for (int r = 0; r < 3; ++r) J[r][q] = cvc[(q + 1) * 3 + r] - x0[r];
+  } else {
+    const int e[3] = {1, 3, 4};
+    for (int q = 0; q < dim; ++q)
+      for (int r = 0; r < dim; ++r) {
+        const double xa = cvc[r] + 1.0 * (cvc[e[q] * dim + r] - cvc[r]);
+        J[r][q] = (xa - x0[r]) / 2.0;
+      }
+  }
+  if (dim == 2) {
+    const double det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    Ji[0][0] = J[1][1] / det; Ji[0][1] = -J[0][1] / det;
+    Ji[1][0] = -J[1][0] / det; Ji[1][1] = J[0][0] / det;
+  } else {
+    const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+                       J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+                       J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        const int i1 = (j + 1) % 3, i2 = (j + 2) % 3, j1 = (i + 1) % 3, j2 = (i + 2) % 3;
+        Ji[i][j] = (J[i1][j1] * J[i2][j2] - J[i1][j2] * J[i2][j1]) / det;
+      }
+  }
+  // the fine node (fine cell's affine map) in the parent's reference cell
+  const double* r = a.ref[k];
+  double x[3] = {0, 0, 0};
+  if (a.shape == kTetra) {
+    for (int d = 0; d < 3; ++d) {
+      double s = cvf[d];
+      for (int q = 0; q < 3; ++q) s += r[q] * (cvf[(q + 1) * 3 + d] - cvf[d]);
+      x[d] = s;
+    }
+  } else {
+    const int e[3] = {1, 3, 4};
+    for (int d = 0; d < dim; ++d) {
+      double s = cvf[d];
+      for (int q = 0; q < dim; ++q) s += 0.5 * (r[q] + 1.0) * (cvf[e[q] * dim + d] - cvf[d]);
+      x[d] = s;
+    }
+  }
+  const double r0 = a.shape == kTetra ? 0.0 : -1.0;
+  double xi[3] = {0, 0, 0};
+  for (int q = 0; q < dim; ++q) {
+    double t = 0;
+    for (int rr = 0; rr < dim; ++rr) t += Ji[q][rr] * (x[rr] - x0[rr]);
+    xi[q] = r0 + t;
+  }
+  if (a.shape == kTetra) {
+    const double l[4] = {1.0 - xi[0] - xi[1] - xi[2], xi[0], xi[1], xi[2]};
+    if (a.p == 1) {
+      for (int q = 0; q < 4; ++q) val[q] = l[q];
+    } else {
+      const int va[10] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3};
+      const int vb[10] = {0, 1, 1, 2, 2, 2, 3, 3, 3, 3};
+      for (int q = 0; q < 10; ++q)
+        val[q] = va[q] == vb[q] ? l[va[q]] * (2.0 * l[va[q]] - 1.0) : 4.0 * l[va[q]] * l[vb[q]];
+    }
+    return;
+  }
+  const int n1 = a.p + 1;
+  double v[3][3];
+  for (int q = 0; q < dim; ++q) {
+    const double t = xi[q];
+    if (a.p == 1) {
+      v[q][0] = 0.5 * (1 - t); v[q][1] = 0.5 * (1 + t);
+    } else {
+      v[q][0] = 0.5 * t * (t - 1); v[q][1] = (1 - t) * (1 + t); v[q][2] = 0.5 * t * (t + 1);
+    }
+  }
+  for (int q = 0; q < a.nl; ++q) {
+    const int i0 = q % n1, i1 = (q / n1) % n1, i2 = q / (n1 * n1);
+    val[q] = dim == 2 ? v[0][i0] * v[1][i1] : v[0][i0] * v[1][i1] * v[2][i2];
+  }
+}
+
+constexpr double kTransferDrop = 1e-14;   // basis values below this are not entries
+
+__global__ void k_tr_count(long n, TransferArgs a, const double* __restrict__ fverts,
+                           const double* __restrict__ cverts, const int* __restrict__ parent,
+                           const int* __restrict__ fgdof, int* __restrict__ cnt,
+                           int* __restrict__ mult) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
+       i += (long)gridDim.x * blockDim.x) {
+    const long f = i / a.nl;
+    const int k = (int)(i - f * a.nl);
+    double val[kMaxLoc];
+    parent_basis_values(a, fverts + f * a.nv * a.dim, cverts + (long)parent[f] * a.nv * a.dim, k,
+                        val);
+    int nz = 0;
+    for (int q = 0; q < a.nl; ++q) nz += fabs(val[q]) >= kTransferDrop;
+    const int fi = fgdof[i];
+    atomicAdd(cnt + fi, nz);
+    atomicAdd(mult + fi, 1);
+  }
+}
+
+// entry key: coarse column in the high word, the flat source index (cell, local
+// DOF) in the low word, so a row sorted by key sums its duplicates in cell order
+__global__ void k_tr_fill(long n, TransferArgs a, const double* __restrict__ fverts,
+                          const double* __restrict__ cverts, const int* __restrict__ parent,
+                          const int* __restrict__ fgdof, const int* __restrict__ cgdof,
+                          const long long* __restrict__ tp, int* __restrict__ cursor,
+                          long long* __restrict__ key, double* __restrict__ tval) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
+       i += (long)gridDim.x * blockDim.x) {
+    const long f = i / a.nl;
+    const int k = (int)(i - f * a.nl);
+    const int c = parent[f];
+    double val[kMaxLoc];
+    parent_basis_values(a, fverts + f * a.nv * a.dim, cverts + (long)c * a.nv * a.dim, k, val);
+    const int fi = fgdof[i];
+    for (int q = 0; q < a.nl; ++q) {
+      if (fabs(val[q]) < kTransferDrop) continue;
+      const long long at = tp[fi] + atomicAdd(cursor + fi, 1);
+      key[at] = ((long long)cgdof[(long)c * a.nl + q] << 32) | (long long)(unsigned)i;
+      tval[at] = val[q];
+    }
+  }
+}
+
+// one CTA per segment: bitonic sort of the segment's (key, value) pairs
+constexpr int kPairThreads = 128;
+__global__ void __launch_bounds__(kPairThreads)
+k_seg_sort_pairs(int nseg, int P, const long long* __restrict__ off, const int* __restrict__ len,
+                 long long* __restrict__ key, double* __restrict__ val) {
+  extern __shared__ __align__(16) unsigned char pair_smem[];
+  long long* sk = reinterpret_cast<long long*>(pair_smem);
+  double* sv = reinterpret_cast<double*>(pair_smem + (size_t)P * sizeof(long long));
+  for (int s = blockIdx.x; s < nseg; s += gridDim.x) {
+    const int n = len[s];
+    long long* kk = key + off[s];
+    double* vv = val + off[s];
+    for (int t = threadIdx.x; t < P; t += kPairThreads) {
+      sk[t] = t < n ? kk[t] : LLONG_MAX;
+      sv[t] = t < n ? vv[t] : 0.0;
+    }
+    __syncthreads();
+    for (int k = 2; k <= P; k <<= 1)
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        for (int t = threadIdx.x; t < P; t += kPairThreads) {
+          const int u = t ^ j;
+          if (u > t) {
+            const long long x = sk[t], y = sk[u];
+            const bool up = (t & k) == 0;
+            if ((x > y) == up) {
+              sk[t] = y; sk[u] = x;
+              const double w = sv[t]; sv[t] = sv[u]; sv[u] = w;
+            }
+          }
+        }
+        __syncthreads();
+      }
+    for (int t = threadIdx.x; t < n; t += kPairThreads) {
+      kk[t] = sk[t];
+      vv[t] = sv[t];
+    }
+    __syncthreads();
+  }
+}
+
+// one thread per fine row: sum the runs of equal columns in order, divide by
+// the node's cell count, keep (column, value) compacted at the row's start
+__global__ void k_tr_combine(int nrows, const long long* __restrict__ tp, const int* __restrict__ cnt,
+                             const int* __restrict__ mult, long long* __restrict__ key,
+                             double* __restrict__ val, int* __restrict__ ucnt) {
+  for (long r = blockIdx.x * (long)blockDim.x + threadIdx.x; r < nrows;
+       r += (long)gridDim.x * blockDim.x) {
+    long long* kk = key + tp[r];
+    double* vv = val + tp[r];
+    const int n = cnt[r];
+    const double m = (double)mult[r];
+    int u = 0;
+    for (int q = 0; q < n;) {
+      const long long col = kk[q] >> 32;
+      double s = 0.0;
+      while (q < n && (kk[q] >> 32) == col) s += vv[q++];
+      kk[u] = col;
+      vv[u] = s / m;
+      ++u;
+    }
+    ucnt[r] = u;
+  }
+}
+
+__global__ void k_tr_copy_p(int nrows, const long long* __restrict__ tp, const long long* __restrict__ key,
+                            const double* __restrict__ val, const int* __restrict__ rp,
+                            int* __restrict__ col, double* __restrict__ pval,
+                            float* __restrict__ pval32, int* __restrict__ rcnt) {
+  for (long r = blockIdx.x * (long)blockDim.x + threadIdx.x; r < nrows;
+       r += (long)gridDim.x * blockDim.x) {
+    const long long* kk = key + tp[r];
+    const double* vv = val + tp[r];
+    const int b = rp[r], e = rp[r + 1];
+    for (int q = b; q < e; ++q) {
+      const int c = (int)kk[q - b];
+      col[q] = c;
+      pval[q] = vv[q - b];
+      pval32[q] = (float)vv[q - b];
+      atomicAdd(rcnt + c, 1);
+    }
+  }
+}
+
+__global__ void k_tr_fill_r(int nrows, const int* __restrict__ prp, const int* __restrict__ pcol,
+                            const double* __restrict__ pval, const int* __restrict__ rrp,
+                            int* __restrict__ rcur, long long* __restrict__ rkey,
+                            double* __restrict__ rval) {
+  for (long r = blockIdx.x * (long)blockDim.x + threadIdx.x; r < nrows;
+       r += (long)gridDim.x * blockDim.x)
+    for (int q = prp[r]; q < prp[r + 1]; ++q) {
+      const int c = pcol[q];
+      const int at = rrp[c] + atomicAdd(rcur + c, 1);
+      rkey[at] = r;
+      rval[at] = pval[q];
+    }
+}
+
+__global__ void k_tr_copy_r(long n, const long long* __restrict__ rkey,
+                            const double* __restrict__ rval, int* __restrict__ col,
+                            double* __restrict__ val, float* __restrict__ val32) {
+  for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n;
+       q += (long)gridDim.x * blockDim.x) {
+    col[q] = (int)rkey[q];
+    val[q] = rval[q];
+    val32[q] = (float)rval[q];
+  }
+}
+
+__global__ void k_lengths(int n, const int* __restrict__ rp, int* __restrict__ len,
+                          long long* __restrict__ off) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n;
+       i += (long)gridDim.x * blockDim.x) {
+    len[i] = rp[i + 1] - rp[i];
+    off[i] = rp[i];
+  }
+}
+
+int seg_sort(cdg_context* ctx, int nseg, int maxlen, const long long* off, const int* len,
+             long long* key, double* val) {
+  int P = kPairThreads;
+  while (P < maxlen) P <<= 1;
+  if (P > 4096) {
+    set_error("transfer row of %d entries beyond the shared-memory sort", maxlen);
+    return CDG_ERR_LIMIT;
+  }
+  const size_t smem = (size_t)P * (sizeof(long long) + sizeof(double));
+  if (smem > 48 * 1024)
+    CDG_CUDA(cudaFuncSetAttribute(k_seg_sort_pairs, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem));
+  const int grid = (int)std::max<long>(1, std::min<long>(nseg, (long)ctx->num_sms * 16));
+  CDG_LAUNCH(ctx, k_seg_sort_pairs, grid, kPairThreads, smem, nseg, P, off, len, key, val);
+  return CDG_OK;
+}
+
+int max_of(cdg_context* ctx, int n, const int* v, int* mx_dev, int* out) {
+  CDG_CUDA(cudaMemsetAsync(mx_dev, 0, sizeof(int), ctx->stream));
+  CDG_LAUNCH(ctx, k_row_max, fill_grid(ctx, n), 256, 0, n, v, mx_dev);
+  CDG_CUDA(cudaMemcpyAsync(out, mx_dev, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CDG_CUDA(cudaStreamSynchronize(ctx->stream));
+  return CDG_OK;
+}
+
+}  // namespace
+
+int device_transfer(cdg_context* ctx, const Mesh& fm, const Space& fs, const Mesh& cm,
+                    const Space& cs, const int* parent_host, const int* fgdof_dev,
+                    const int* cgdof_dev, DevLevel& F) {
+  const int nl = fs.nloc, nf = fs.ndof, nc = cs.ndof;
+  const long n = (long)fm.ncells * nl;
+  cudaStream_t st = ctx->stream;
+  TransferArgs a{};
+  a.shape = fm.shape;
+  a.dim = fm.dim;
+  a.p = fs.order;
+  a.nl = nl;
+  a.nv = fm.nv;
+  for (int k = 0; k < nl; ++k) local_dof_ref_shape(fm.shape, fs.order, k, a.ref[k]);
+  DBuf<double> fv, cv, tval, rval;
+  DBuf<int> parent, cnt, mult, cursor, ucnt, mx, rcnt, rcur, rlen;
+  DBuf<long long> tp, key, rkey, roff;
+  CDG_TRY(fv.alloc(fm.verts.size()));
+  CDG_TRY(cv.alloc(cm.verts.size()));
+  CDG_TRY(parent.alloc(fm.ncells));
+  CDG_TRY(cnt.alloc((size_t)nf + 1));
+  CDG_TRY(mult.alloc((size_t)nf + 1));
+  CDG_TRY(cursor.alloc((size_t)nf + 1));
+  CDG_TRY(ucnt.alloc((size_t)nf + 1));
+  CDG_TRY(tp.alloc((size_t)nf + 1));
+  CDG_TRY(mx.alloc(1));
+  CDG_CUDA(cudaMemcpyAsync(fv.p, fm.verts.data(), fm.verts.size() * sizeof(double),
+                           cudaMemcpyHostToDevice, st));
+  CDG_CUDA(cudaMemcpyAsync(cv.p, cm.verts.data(), cm.verts.size() * sizeof(double),
+                           cudaMemcpyHostToDevice, st));
+  CDG_CUDA(cudaMemcpyAsync(parent.p, parent_host, (size_t)fm.ncells * sizeof(int),
+                           cudaMemcpyHostToDevice, st));
+  CDG_CUDA(cudaMemsetAsync(cnt.p, 0, ((size_t)nf + 1) * sizeof(int), st));
+  CDG_CUDA(cudaMemsetAsync(mult.p, 0, ((size_t)nf + 1) * sizeof(int), st));
+  CDG_CUDA(cudaMemsetAsync(cursor.p, 0, ((size_t)nf + 1) * sizeof(int), st));
+  CDG_CUDA(cudaMemsetAsync(ucnt.p, 0, ((size_t)nf + 1) * sizeof(int), st));
+  CDG_LAUNCH(ctx, k_tr_count, fill_grid(ctx, n), 256, 0, n, a, fv.p, cv.p, parent.p, fgdof_dev,
+             cnt.p, mult.p);
+  ScanScratch sc;
+  long long tot[1];
+  CDG_TRY((device_scan<1>(ctx, sc, (long)nf + 1, CountOf{cnt.p}, WriteOffset64{tp.p}, tot)));
+  CDG_TRY(key.alloc((size_t)tot[0]));
+  CDG_TRY(tval.alloc((size_t)tot[0]));
+  CDG_LAUNCH(ctx, k_tr_fill, fill_grid(ctx, n), 256, 0, n, a, fv.p, cv.p, parent.p, fgdof_dev,
+             cgdof_dev, tp.p, cursor.p, key.p, tval.p);
+  int maxlen = 0;
+  CDG_TRY(max_of(ctx, nf, cnt.p, mx.p, &maxlen));
+  CDG_TRY(seg_sort(ctx, nf, maxlen, tp.p, cnt.p, key.p, tval.p));
+  CDG_LAUNCH(ctx, k_tr_combine, fill_grid(ctx, nf), 256, 0, nf, tp.p, cnt.p, mult.p, key.p,
+             tval.p, ucnt.p);
+  // P
+  long long pnnz[1];
+  int *prp = nullptr, *pcol = nullptr, *rrp = nullptr, *rcol = nullptr;
+  double *pval = nullptr, *rv = nullptr;
+  float *pval32 = nullptr, *rv32 = nullptr;
+  auto release = [&]() {
+    for (void* q : {(void*)prp, (void*)pcol, (void*)rrp, (void*)rcol, (void*)pval, (void*)rv,
+                    (void*)pval32, (void*)rv32})
+      if (q) cudaFree(q);
+  };
+  int rc = CDG_OK;
+  do {
+    if ((rc = dalloc_raw(&prp, (size_t)nf + 1)) != CDG_OK) break;
+    rc = device_scan<1>(ctx, sc, (long)nf + 1, CountOf{ucnt.p}, WriteOffset32{prp}, pnnz);
+    if (rc != CDG_OK) break;
+    if ((rc = dalloc_raw(&pcol, (size_t)pnnz[0])) != CDG_OK) break;
+    if ((rc = dalloc_raw(&pval, (size_t)pnnz[0])) != CDG_OK) break;
+    if ((rc = dalloc_raw(&pval32, (size_t)pnnz[0])) != CDG_OK) break;
+    if ((rc = rcnt.alloc((size_t)nc + 1)) != CDG_OK) break;
+    if ((rc = rcur.alloc((size_t)nc + 1)) != CDG_OK) break;
+    cudaMemsetAsync(rcnt.p, 0, ((size_t)nc + 1) * sizeof(int), st);
+    cudaMemsetAsync(rcur.p, 0, ((size_t)nc + 1) * sizeof(int), st);
+    CDG_LAUNCH(ctx, k_tr_copy_p, fill_grid(ctx, nf), 256, 0, nf, tp.p, key.p, tval.p, prp, pcol,
+               pval, pval32, rcnt.p);
+    // R = P^T, rows sorted by fine index
+    if ((rc = dalloc_raw(&rrp, (size_t)nc + 1)) != CDG_OK) break;
+    long long rnnz[1];
+    rc = device_scan<1>(ctx, sc, (long)nc + 1, CountOf{rcnt.p}, WriteOffset32{rrp}, rnnz);
+    if (rc != CDG_OK) break;
+    if ((rc = rkey.alloc((size_t)rnnz[0])) != CDG_OK) break;
+    if ((rc = rval.alloc((size_t)rnnz[0])) != CDG_OK) break;
+    CDG_LAUNCH(ctx, k_tr_fill_r, fill_grid(ctx, nf), 256, 0, nf, prp, pcol, pval, rrp, rcur.p,
+               rkey.p, rval.p);
+    if ((rc = rlen.alloc((size_t)nc + 1)) != CDG_OK) break;
+    if ((rc = roff.alloc((size_t)nc + 1)) != CDG_OK) break;
+    CDG_LAUNCH(ctx, k_lengths, fill_grid(ctx, nc), 256, 0, nc, rrp, rlen.p, roff.p);
+    int rmax = 0;
+    if ((rc = max_of(ctx, nc, rlen.p, mx.p, &rmax)) != CDG_OK) break;
+    if ((rc = seg_sort(ctx, nc, rmax, roff.p, rlen.p, rkey.p, rval.p)) != CDG_OK) break;
+    if ((rc = dalloc_raw(&rcol, (size_t)rnnz[0])) != CDG_OK) break;
+    if ((rc = dalloc_raw(&rv, (size_t)rnnz[0])) != CDG_OK) break;
+    if ((rc = dalloc_raw(&rv32, (size_t)rnnz[0])) != CDG_OK) break;
+    CDG_LAUNCH(ctx, k_tr_copy_r, fill_grid(ctx, rnnz[0]), 256, 0, rnnz[0], rkey.p, rval.p, rcol,
+               rv, rv32);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+      set_error("transfer build: %s", cudaGetErrorString(e));
+      rc = CDG_ERR_CUDA;
+      break;
+    }
+    if ((rc = check_device_error(ctx)) != CDG_OK) break;
+    F.P_rp = prp; F.P_col = pcol; F.P_val = pval; F.P_val32 = pval32;
+    F.R_rp = rrp; F.R_col = rcol; F.R_val = rv; F.R_val32 = rv32;
+    F.P_nnz = (int)pnnz[0];
+    F.R_nnz = (int)rnnz[0];
+    return CDG_OK;
+  } while (false);
+  cudaStreamSynchronize(st);
+  release();
+  return rc;
 }
 
 }  // namespace cdg
