@@ -1139,6 +1139,12 @@ int build_sell(cdg_context* ctx, DevLevel& L) {
     if (g == 0) return CDG_OK;                  // CSR kernels
     if (g == 1 || g == 2 || g == 4 || g == 8 || g == 16) G = g;
   }
+  // built on the device (the same layout); CDG_SELL_HOST=1 builds it here
+  if (!getenv("CDG_SELL_HOST")) {
+    const int rc = device_sell(ctx, L, G);
+    if (rc != CDG_ERR_LIMIT) return rc;
+    return CDG_OK;                              // positions beyond int: keep CSR
+  }
   const int R = 32 / G;                         // rows per slice
   const int nslices = (n + R - 1) / R;
   std::vector<int> order(n);

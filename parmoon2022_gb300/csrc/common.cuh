@@ -211,6 +211,9 @@ int device_space(cdg_context* ctx, const Mesh& m, int order, int neumann_mask, S
 int device_pattern(cdg_context* ctx, int ncells, int nloc, int ndof, const int* gdof_host,
                    const int* gdof_dev, std::vector<int>* row_ptr, std::vector<int>* col,
                    int** col_dev_out, int** rp_dev_out);
+// sliced ELLPACK layout of L with G lanes per row built on the device (the
+// layout of build_sell's host path); CDG_ERR_LIMIT: slots beyond 32-bit positions
+int device_sell(cdg_context* ctx, DevLevel& L, int G);
 // prolongation / restriction of the fine level F (the matrices of
 // make_transfer) built on the device into F.P_* / F.R_*; fm, cm: the nested
 // (unperturbed) meshes, parent: coarse cell of each fine cell (host)

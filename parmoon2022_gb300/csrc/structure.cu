@@ -975,4 +975,157 @@ int device_transfer(cdg_context* ctx, const Mesh& fm, const Space& fs, const Mes
   return rc;
 }
 
+
+// ---------------------------------------------------------------------------
+// sliced ELLPACK layout of the FP64 operator, built on the device with the
+// host builder's rules: rows stable-sorted by length (descending) inside
+// windows of kSellWindow rows, slices of 32/G rows, entry k of slice row i at
+// off[s] + 32 (k / G) + G i + k mod G, padding = own row with value 0,
+// non-active rows = identity (1 at the first slot)
+// ---------------------------------------------------------------------------
+namespace {
+
+__global__ void __launch_bounds__(kSellWindow)
+k_sell_order(int n, int na, const int* __restrict__ rp, int* __restrict__ order) {
+  __shared__ long long key[kSellWindow];
+  const int w0 = blockIdx.x * kSellWindow, t = threadIdx.x, r = w0 + t;
+  long long kv = LLONG_MAX;
+  if (r < n) {
+    const int len = r < na ? rp[r + 1] - rp[r] : 1;
+    kv = ((long long)(INT_MAX - len) << 32) | (long long)(unsigned)t;   // ties: row order
+  }
+  key[t] = kv;
+  __syncthreads();
+  for (int k = 2; k <= kSellWindow; k <<= 1)
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      const int u = t ^ j;
+      if (u > t) {
+        const long long x = key[t], y = key[u];
+        const bool up = (t & k) == 0;
+        if ((x > y) == up) {
+          key[t] = y;
+          key[u] = x;
+        }
+      }
+      __syncthreads();
+    }
+  if (w0 + t < n) order[w0 + t] = w0 + (int)(key[t] & 0xffffffffLL);
+}
+
+__global__ void k_sell_steps(int nslices, int R, int G, int n, int na, const int* __restrict__ rp,
+                             const int* __restrict__ order, int* __restrict__ srow,
+                             int* __restrict__ width) {
+  for (long s = blockIdx.x * (long)blockDim.x + threadIdx.x; s < nslices;
+       s += (long)gridDim.x * blockDim.x) {
+    int steps = 0;
+    for (int i = 0; i < R; ++i) {
+      const long idx = s * R + i;
+      int r = -1;
+      if (idx < n) {
+        r = order[idx];
+        const int len = r < na ? rp[r + 1] - rp[r] : 1;
+        steps = max(steps, (len + G - 1) / G);
+      }
+      srow[idx] = r;
+    }
+    width[s] = 32 * steps;
+  }
+}
+
+__global__ void k_sell_fill(int nslices, int R, int G, int na, const int* __restrict__ rp,
+                            const int* __restrict__ col, const long long* __restrict__ off,
+                            const int* __restrict__ srow, int* __restrict__ scol,
+                            int* __restrict__ pos, double* __restrict__ sval) {
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < (long)nslices * R;
+       t += (long)gridDim.x * blockDim.x) {
+    const long s = t / R;
+    const int i = (int)(t - s * R);
+    const int r = srow[t];
+    if (r < 0) continue;                          // padding row: column 0, value 0
+    const long long o = off[s];
+    const int slots = (int)((off[s + 1] - o) / 32) * G;
+    const int m = r < na ? rp[r + 1] - rp[r] : 0;
+    const int b = r < na ? rp[r] : 0;
+    for (int k = 0; k < slots; ++k) {
+      const long long q = o + 32LL * (k / G) + G * i + k % G;
+      if (k < m) {
+        scol[q] = col[b + k];
+        pos[b + k] = (int)q;
+      } else {
+        scol[q] = r;                              // padding: own row, value 0
+      }
+    }
+    if (r >= na) sval[o + G * i] = 1.0;           // identity row
+  }
+}
+
+struct SliceWidth {
+  const int* w;
+  __device__ void operator()(long i, long long (&v)[1]) const { v[0] = w[i]; }
+};
+
+}  // namespace
+
+int device_sell(cdg_context* ctx, DevLevel& L, int G) {
+  const int n = L.ndof, na = L.nactive;
+  const int R = 32 / G;
+  const int nslices = (n + R - 1) / R;
+  cudaStream_t st = ctx->stream;
+  DBuf<int> order, width;
+  CDG_TRY(order.alloc(n));
+  CDG_TRY(width.alloc((size_t)nslices + 1));
+  int *srow = nullptr, *scol = nullptr, *pos = nullptr;
+  long long* off = nullptr;
+  double* sval = nullptr;
+  auto release = [&]() {
+    for (void* q : {(void*)srow, (void*)scol, (void*)pos, (void*)off, (void*)sval})
+      if (q) cudaFree(q);
+  };
+  int rc = CDG_OK;
+  do {
+    if ((rc = dalloc_raw(&srow, (size_t)nslices * R)) != CDG_OK) break;
+    if ((rc = dalloc_raw(&off, (size_t)nslices + 1)) != CDG_OK) break;
+    CDG_LAUNCH(ctx, k_sell_order, (n + kSellWindow - 1) / kSellWindow, kSellWindow, 0, n, na,
+               L.row_ptr, order.p);
+    cudaMemsetAsync(width.p + nslices, 0, sizeof(int), st);
+    CDG_LAUNCH(ctx, k_sell_steps, fill_grid(ctx, nslices), 256, 0, nslices, R, G, n, na,
+               L.row_ptr, order.p, srow, width.p);
+    ScanScratch sc;
+    long long total[1];
+    rc = device_scan<1>(ctx, sc, (long)nslices + 1, SliceWidth{width.p}, WriteOffset64{off}, total);
+    if (rc != CDG_OK) break;
+    if (total[0] >= (1LL << 31)) {
+      set_error("sliced layout of %lld slots beyond 32-bit positions", total[0]);
+      rc = CDG_ERR_LIMIT;
+      break;
+    }
+    if ((rc = dalloc_raw(&scol, (size_t)total[0])) != CDG_OK) break;
+    if ((rc = dalloc_raw(&sval, (size_t)total[0])) != CDG_OK) break;
+    if ((rc = dalloc_raw(&pos, (size_t)L.nnz)) != CDG_OK) break;
+    cudaMemsetAsync(scol, 0, (size_t)total[0] * sizeof(int), st);
+    cudaMemsetAsync(sval, 0, (size_t)total[0] * sizeof(double), st);
+    cudaMemsetAsync(pos, 0xff, (size_t)L.nnz * sizeof(int), st);   // -1: no slot
+    CDG_LAUNCH(ctx, k_sell_fill, fill_grid(ctx, (long)nslices * R), 256, 0, nslices, R, G, na,
+               L.row_ptr, L.col, off, srow, scol, pos, sval);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+      set_error("sliced layout: %s", cudaGetErrorString(e));
+      rc = CDG_ERR_CUDA;
+      break;
+    }
+    L.sell_off = off;
+    L.sell_row = srow;
+    L.sell_col = scol;
+    L.sell_val = sval;
+    L.sell_pos = pos;
+    L.sell_nslices = nslices;
+    L.sell_lanes = G;
+    L.sell_total = total[0];
+    return CDG_OK;
+  } while (false);
+  cudaStreamSynchronize(st);
+  release();
+  return rc;
+}
+
 }  // namespace cdg

@@ -144,3 +144,22 @@ def test_tcd_system_on_sell_operator(ctx):
     prod = np.add.reduceat(S * x[col], rp[:-1])
     prod[na:] = x[na:]
     assert rel(gpu.apply(x), prod) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["q1_2d_n512", "q2_3d_n16"])
+def test_device_layout_equals_host_layout(ctx, name):
+    import os
+    out = []
+    for host in (True, False):
+        if host:
+            os.environ["CDG_SELL_HOST"] = "1"
+        try:
+            o, h, a, lanes = make(name, n_levels=1)
+            gpu = pg.ConvectionDiffusion(ctx, h)
+        finally:
+            os.environ.pop("CDG_SELL_HOST", None)
+        gpu.assemble(a)
+        x = np.random.default_rng(9).standard_normal(gpu.info(0)["ndof"])
+        out.append((gpu.operator_layout(0), gpu.apply(x)))
+    assert out[0][0] == out[1][0]
+    assert rel(out[1][1], out[0][1]) < 1e-14
