@@ -662,7 +662,9 @@ def run_gpu_serve(args):
     # warm the pools: one request of every mesh class (hierarchies, device
     # instances, captured graphs), not timed
     warm = [(d, o, n, 1e-2, (0.6, 0.8, 0.0)[:d], 0.5) for d, o, n in SERVE["classes"]]
+    t_cold = time.perf_counter()
     run_stream(pg, srv, warm, [0.0] * len(warm), "mixed")
+    t_cold = time.perf_counter() - t_cold
     c0 = srv.counters()
     clocks = ClockSampler(local)
     clocks.start()
@@ -748,6 +750,7 @@ def run_gpu_serve(args):
         "e2e": {"value": sat, "unit": "solves/s", "h2d_bytes_per_step": 400,
                 "d2h_bytes_per_step": int(8 * ndof_mean)},
         "clocks": clk, "gpu_launches": c1["launches"] - c0["launches"],
+        "cold_start_s": t_cold,
     }))
 
 

@@ -285,8 +285,16 @@ void worker(cdg_server* s, Slot* slot) {
         if (!mc->h) {
           int roots = 1, nref = 0;
           split_n(job->req.n, &roots, &nref);
-          rc = cdg_hierarchy_create(job->req.dim, job->req.order, roots, nref, job->key.levels,
-                                    job->req.a.neumann_mask, &mc->h);
+          // numbering, patterns (and, at instance creation, transfers and the
+          // sliced operator) built on this slot's GPU; CDG_SERVER_HOST_SETUP=1
+          // builds the hierarchy on the host
+          if (getenv("CDG_SERVER_HOST_SETUP"))
+            rc = cdg_hierarchy_create(job->req.dim, job->req.order, roots, nref,
+                                      job->key.levels, job->req.a.neumann_mask, &mc->h);
+          else
+            rc = cdg_hierarchy_create_device(slot->ctx, job->req.dim, job->req.order, roots,
+                                             nref, job->key.levels, job->req.a.neumann_mask,
+                                             &mc->h);
           if (rc == CDG_OK) {
             mc->bytes = estimate_bytes(mc->h, job->key.levels,
                                        std::max(1, job->req.s.gmres_restart));
