@@ -153,6 +153,7 @@ struct GmresState {
   // FGMRES iteration); rebuilt when the solver parameters or buffers change
   int* dstate = nullptr;     // [0] i (column), [1] j (iteration), [2] flag
   double* zcur = nullptr;    // n: z_i for the operator application
+  double* part = nullptr;    // block partial sums of the cooperative restart cycle
   cudaGraphExec_t exec = nullptr;
   cudaGraph_t graph = nullptr;
   cdg_solver_params key{};   // parameters the graph was captured with

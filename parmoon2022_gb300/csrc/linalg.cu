@@ -1424,7 +1424,7 @@ __global__ void k_update(int n, int k, const double* __restrict__ Z, const doubl
 }
 
 void free_gmres(GmresState& g) {
-  double* ptrs[] = {g.V, g.Z, g.w, g.H, g.cs, g.sn, g.s, g.y, g.scal, g.zcur};
+  double* ptrs[] = {g.V, g.Z, g.w, g.H, g.cs, g.sn, g.s, g.y, g.scal, g.zcur, g.part};
   for (double* q : ptrs)
     if (q) cudaFree(q);
   if (g.dstate) cudaFree(g.dstate);
@@ -1647,6 +1647,182 @@ static int read_state(cdg_context* ctx, const GmresState& g, int* st4, double* r
   return CDG_OK;
 }
 
+// ---------------------------------------------------------------------------
+// One FGMRES restart cycle with the Jacobi preconditioner as a single
+// cooperative kernel, for small systems: the iteration of iteration_body
+// (z_i = D^-1 v_i, w = A z_i, classical Gram-Schmidt, norm, Givens, test,
+// v_{i+1} = w / h_{i+1,i}) with three grid-wide barriers where the graph runs
+// seven dependent kernels.  A thread owns up to kCycleRows rows and keeps
+// their w in registers from the operator to the normalisation (one row per
+// thread measured best on GB300: 64^2 Q1, 387 iterations, 84.9 solves/s
+// against 68.8 with two rows, 57.2 with four and 58.9 for the graph).  The inner
+// products of a block are reduced through shared memory (one warp per
+// product); every block sums the blocks' partials in block order, so all
+// blocks hold the same values, run the Givens step and the convergence test
+// on their own copy of the rotations and take the same branch without a
+// further barrier.  Block 0 writes the shared state (H, rotations, s, the
+// residual and the loop state) for the back substitution on the host side.
+// ---------------------------------------------------------------------------
+constexpr int kCycleThreads = 256, kCycleRows = 1, kCycleMaxM = 64;
+constexpr int kCycleMaxRows = 65536;   // larger systems keep the graph-captured kernels
+
+__global__ void __launch_bounds__(kCycleThreads)
+k_fgmres_cycle_jacobi(int n, int nactive, int m, ConvParams cp, const int* __restrict__ rp,
+                      const int* __restrict__ col, const double* __restrict__ val,
+                      const double* __restrict__ invd, double* __restrict__ V,
+                      double* __restrict__ Z, double* __restrict__ H, double* __restrict__ cs,
+                      double* __restrict__ sn, double* __restrict__ s, double* __restrict__ scal,
+                      int* __restrict__ st, double* __restrict__ part, int* err) {
+  cgrp::grid_group grid = cgrp::this_grid();
+  __shared__ double tr[8][kCycleThreads + 1];
+  __shared__ double hc[kCycleMaxM + 2];
+  __shared__ double lcs[kCycleMaxM + 1], lsn[kCycleMaxM + 1], ls[kCycleMaxM + 2];
+  __shared__ double lli[2], red[kCycleThreads / 32], nrm_s;
+  __shared__ int dec[4];   // next i, next j, flag, continue
+  const int nb = gridDim.x, wp = threadIdx.x >> 5, l = threadIdx.x & 31;
+  const long nthr = (long)nb * kCycleThreads;
+  const long tid = blockIdx.x * (long)kCycleThreads + threadIdx.x;
+  double* part2 = part + (size_t)nb * (m + 1);   // norm partials
+  for (int k = threadIdx.x; k <= m; k += kCycleThreads) {
+    ls[k] = s[k];
+    lcs[k] = cs[k];
+    lsn[k] = sn[k];
+  }
+  if (threadIdx.x == 0) {
+    lli[0] = scal[4];
+    lli[1] = scal[5];
+  }
+  int i = st[0], j = st[1];
+  __syncthreads();
+  for (;;) {
+    // z_i = D^-1 v_i on the own rows (Iteration_jacobi::apply)
+#pragma unroll
+    for (int q = 0; q < kCycleRows; ++q) {
+      const long r = tid + q * nthr;
+      if (r < n) Z[(size_t)i * n + r] = V[(size_t)i * n + r] * invd[r];
+    }
+    grid.sync();
+    // w = A z_i (non-active rows: identity)
+    double wv[kCycleRows];
+#pragma unroll
+    for (int q = 0; q < kCycleRows; ++q) {
+      const long r = tid + q * nthr;
+      double a = 0.0;
+      if (r < nactive) {
+        for (int k = rp[r]; k < rp[r + 1]; ++k) a = fma(val[k], Z[(size_t)i * n + col[k]], a);
+      } else if (r < n) {
+        a = Z[(size_t)i * n + r];
+      }
+      wv[q] = a;
+    }
+    // block partials of (w, v_k), k <= i, eight products per pass
+    for (int k0 = 0; k0 <= i; k0 += 8) {
+      double a[8];
+#pragma unroll
+      for (int kk = 0; kk < 8; ++kk) a[kk] = 0.0;
+#pragma unroll
+      for (int q = 0; q < kCycleRows; ++q) {
+        const long r = tid + q * nthr;
+        if (r < n)
+#pragma unroll
+          for (int kk = 0; kk < 8; ++kk)
+            if (k0 + kk <= i) a[kk] = fma(wv[q], V[(size_t)(k0 + kk) * n + r], a[kk]);
+      }
+#pragma unroll
+      for (int kk = 0; kk < 8; ++kk) tr[kk][threadIdx.x] = a[kk];
+      __syncthreads();
+      if (k0 + wp <= i) {
+        double v = 0.0;
+#pragma unroll
+        for (int q = 0; q < kCycleThreads / 32; ++q) v += tr[wp][q * 32 + l];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (l == 0) part[(size_t)blockIdx.x * (m + 1) + k0 + wp] = v;
+      }
+      __syncthreads();
+    }
+    grid.sync();
+    // every block: h_k = sum of the block partials in block order
+    for (int k = threadIdx.x; k <= i; k += kCycleThreads) {
+      double v = 0.0;
+      for (int b = 0; b < nb; ++b) v += part[(size_t)b * (m + 1) + k];
+      hc[k] = v;
+    }
+    __syncthreads();
+    // w -= sum_k h_k v_k (k in order), norm partial
+    double nn = 0.0;
+#pragma unroll
+    for (int q = 0; q < kCycleRows; ++q) {
+      const long r = tid + q * nthr;
+      if (r < n) {
+        double w = wv[q];
+        for (int k = 0; k <= i; ++k) w = fma(-hc[k], V[(size_t)k * n + r], w);
+        wv[q] = w;
+        nn = fma(w, w, nn);
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) nn += __shfl_xor_sync(0xffffffffu, nn, o);
+    if (l == 0) red[wp] = nn;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double v = 0.0;
+      for (int q = 0; q < kCycleThreads / 32; ++q) v += red[q];
+      part2[blockIdx.x] = v;
+    }
+    grid.sync();
+    // every block: the norm, Givens, the test (k_fgmres_iter_check)
+    if (threadIdx.x == 0) {
+      double v = 0.0;
+      for (int b = 0; b < nb; ++b) v += part2[b];
+      const double nrm = sqrt(v);
+      nrm_s = nrm;
+      hc[i + 1] = nrm;
+      double resid = 0.0;
+      givens_column(i, hc, lcs, lsn, ls, &resid);
+      const int cv = conv_test(cp, lli, resid, j);
+      int flag = 0, ni = i, nj = j, cont = 0;
+      if (cv == 2) flag = 2;
+      else if (cv == 1) flag = 1;
+      else if (i + 1 == m) { flag = 3; nj = j + 1; }
+      else { ni = i + 1; nj = j + 1; cont = 1; }
+      if (nrm == 0.0) {   // H(i+1,i) == 0: unhappy breakdown (k_scale_inv)
+        cont = 0;
+        if (blockIdx.x == 0) atomicOr(err, kErrBreakdown);
+      }
+      dec[0] = ni; dec[1] = nj; dec[2] = flag; dec[3] = cont;
+      if (blockIdx.x == 0) {
+        for (int k = 0; k <= i + 1; ++k) H[(size_t)i * (m + 1) + k] = hc[k];
+        cs[i] = lcs[i];
+        sn[i] = lsn[i];
+        s[i] = ls[i];
+        s[i + 1] = ls[i + 1];
+        scal[0] = resid;
+        scal[2] = nrm;
+        scal[4] = lli[0];
+        scal[5] = lli[1];
+        st[0] = ni;
+        st[1] = nj;
+        st[2] = flag;
+      }
+    }
+    __syncthreads();
+    const double nrm = nrm_s;
+    if (nrm != 0.0) {
+      const double f = 1.0 / nrm;
+#pragma unroll
+      for (int q = 0; q < kCycleRows; ++q) {
+        const long r = tid + q * nthr;
+        if (r < n) V[(size_t)(i + 1) * n + r] = wv[q] * f;
+      }
+    }
+    if (!dec[3]) break;
+    i = dec[0];
+    j = dec[1];
+    __syncthreads();
+  }
+}
+
 constexpr int kGraphUnavailable = 1;   // internal: use the host loop
 
 static int fgmres_graph(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s,
@@ -1659,11 +1835,31 @@ static int fgmres_graph(cdg_context* ctx, cdg_problem* p, const cdg_solver_param
   double* beta_d = g.scal + 1;
   const int vg = vec_grid(ctx, n);
   const ConvParams cp = conv_params(s);
+  // small Jacobi-preconditioned systems: one cooperative kernel per restart
+  // cycle (CDG_FGMRES_CYCLE=0 keeps the graph)
+  int cycle_blocks = 0;
+  {
+    const char* ce = std::getenv("CDG_FGMRES_CYCLE");
+    const bool cycle_off = ce && ce[0] == '0';
+    int coop = 0, per_sm = 0;
+    if (!cycle_off && s.preconditioner == 1 && n <= kCycleMaxRows && m <= kCycleMaxM &&
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device) == cudaSuccess &&
+        coop &&
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fgmres_cycle_jacobi,
+                                                      kCycleThreads, 0) == cudaSuccess &&
+        per_sm > 0) {
+      const long per_block = (long)kCycleThreads * kCycleRows;
+      const long need = (n + per_block - 1) / per_block;
+      if (need <= (long)ctx->num_sms * per_sm) cycle_blocks = (int)std::max<long>(1, need);
+    }
+  }
   // a graph that cannot be built (capture rejected) falls back to the host loop
-  if (ensure_iteration_graph(ctx, p, s) != CDG_OK) {
+  if (!cycle_blocks && ensure_iteration_graph(ctx, p, s) != CDG_OK) {
     cudaGetLastError();
     return kGraphUnavailable;
   }
+  if (cycle_blocks && g.part == nullptr)
+    CDG_CUDA(cudaMalloc(&g.part, ((size_t)ctx->num_sms * 8 * (kCycleMaxM + 2)) * sizeof(double)));
   // r = b - A x; beta = ||r||; the test at iteration 0
   CDG_TRY(residual64(ctx, L, b, x, g.w));
   CDG_TRY(dot64(ctx, n, g.w, nullptr, beta_d, 0));
@@ -1680,10 +1876,26 @@ static int fgmres_graph(cdg_context* ctx, cdg_problem* p, const cdg_solver_param
   for (;;) {
     CDG_LAUNCH(ctx, k_scale_inv, vg, 256, 0, n, g.w, beta_d, g.V, ctx->d_err);
     CDG_LAUNCH(ctx, k_init_s, 1, 128, 0, m, beta_d, g.s);
-    CDG_CUDA(cudaGraphLaunch(g.exec, ctx->stream));
+    if (cycle_blocks) {
+      const int* rp = L.row_ptr;
+      const int* cl = L.col;
+      const double* vl = L.val64;
+      const double* di = L.invdiag64;
+      int na = L.nactive, nn = n, mm = m;
+      ConvParams cpp = cp;
+      void* args[] = {(void*)&nn,   (void*)&na,   (void*)&mm,    (void*)&cpp,  (void*)&rp,
+                      (void*)&cl,   (void*)&vl,   (void*)&di,    (void*)&g.V,  (void*)&g.Z,
+                      (void*)&g.H,  (void*)&g.cs, (void*)&g.sn,  (void*)&g.s,  (void*)&g.scal,
+                      (void*)&g.dstate, (void*)&g.part, (void*)&ctx->d_err};
+      CDG_CUDA(cudaLaunchCooperativeKernel((const void*)k_fgmres_cycle_jacobi, dim3(cycle_blocks),
+                                           dim3(kCycleThreads), args, 0, ctx->stream));
+      ctx->launches++;
+    } else {
+      CDG_CUDA(cudaGraphLaunch(g.exec, ctx->stream));
+    }
     CDG_TRY(read_state(ctx, g, sv, &resid));
     const int i = sv[0], j = sv[1], flag = sv[2];
-    ctx->launches += g.body_launches * (long long)(flag == 3 ? m : i + 1);
+    if (!cycle_blocks) ctx->launches += g.body_launches * (long long)(flag == 3 ? m : i + 1);
     CDG_TRY(check_device_error(ctx));
     if (flag == 2) {
       set_error("Execution of the code stopped because of solver divergence.");
