@@ -519,7 +519,12 @@ template <int NLOC> struct ShapeInfo {
   static constexpr int THREADS = S::EPB * S::LANES;
 };
 
-constexpr int kCellTile = 32;
+// cells per block: one thread per cell computes the factors while the block
+// waits, so larger tiles amortise that serial FP64 phase; with at least three
+// blocks per SM (register cap) another block contracts meanwhile.  Measured on
+// GB300: 663,552 P2 tetrahedra 3.36 ms (32 cells, 124 registers) -> 2.78 ms
+// (64 cells, 3 blocks/SM); 32^3 Q2 1.57 -> 1.46 ms
+constexpr int kCellTile = 64;
 
 // which reference tensors a launch contracts
 struct TermList {
@@ -527,7 +532,7 @@ struct TermList {
 };
 
 template <int DIM, int NLOC, int NTU>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 3)
 k_element_contract(AsmCoefs k, TermList tl, int mode, int all_rows, int ncells,
                    int nactive, const double* __restrict__ verts, const int* __restrict__ gdof,
                    const int* __restrict__ slot, const double* __restrict__ R,
