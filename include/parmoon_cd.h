@@ -54,6 +54,9 @@ extern "C" {
 #define CDG_EX_BUMP 5             /* f = 0, u = 0 on the boundary, initial
                                      condition exp(-|x-c|^2 / (2 sigma^2))    */
 #define CDG_EX_POLY1_T 6          /* u = (1+t)(1 + x + 2y (+3z)), in time     */
+#define CDG_EX_EXP_SIN 7          /* u = e^{sin 2 pi t} prod sin(2 pi x_i): the
+                                     TCD2D example 0 of the reference's tests
+                                     (include/Examples/TCD_2D/exp.h)          */
 
 /* local assembling + example: LocalAssembling<d>(db, ConvDiff, {}, coeffs,
  * disctype) with the TDatabase globals the CD routines read */

@@ -502,6 +502,23 @@ static void exact_sol(const orc_config *c, const double *x, double *u) {
     u[4] = p2 * qy * qz - 2 * p * qz - 2 * p * qy;
     break;
   }
+  case ORC_EX_EXP_SIN: {
+    /* u = e^{sin 2 pi t} prod sin(2 pi x_a): include/Examples/TCD_2D/exp.h
+       (exp_sin_cos, src/Examples/Example_TimeCD2D.C:12-15) */
+    double w = 2 * M_PI, e = exp(sin(w * c->t)), s[3] = {0, 0, 0}, co[3] = {0, 0, 0};
+    for (int a = 0; a < d; ++a) {
+      s[a] = sin(w * x[a]);
+      co[a] = cos(w * x[a]);
+    }
+    double p = d == 2 ? s[0] * s[1] : s[0] * s[1] * s[2];
+    u[0] = e * p;
+    u[1] = e * w * co[0] * s[1] * (d == 3 ? s[2] : 1.0);
+    u[2] = e * w * s[0] * co[1] * (d == 3 ? s[2] : 1.0);
+    if (d == 3) u[3] = e * w * s[0] * s[1] * co[2];
+    u[d + 1] = -d * w * w * e * p;
+    u[d + 2] = w * cos(w * c->t) * e * p;
+    break;
+  }
   case ORC_EX_POLY1:
   case ORC_EX_POLY1_T: {
     double sc = c->example == ORC_EX_POLY1_T ? 1 + c->t : 1.0;

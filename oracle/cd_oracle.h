@@ -26,7 +26,9 @@ enum {
   ORC_EX_CONST_F = 3,      /* f = 1, homogeneous Dirichlet, no exact solution  */
   ORC_EX_POLY1 = 4,        /* u = 1 + x + 2y (+3z): inside Q1, Dirichlet       */
   ORC_EX_BUMP = 5,         /* f = 0, u_D = 0, u0 = exp(-|x-c|^2/(2 s^2))       */
-  ORC_EX_POLY1_T = 6       /* u = (1+t)(1 + x + 2y (+3z))                      */
+  ORC_EX_POLY1_T = 6,      /* u = (1+t)(1 + x + 2y (+3z))                      */
+  ORC_EX_EXP_SIN = 7       /* u = e^{sin 2 pi t} prod sin(2 pi x_i) (TCD2D example 0,
+                              include/Examples/TCD_2D/exp.h)                   */
 };
 
 typedef struct {

@@ -26,7 +26,7 @@ ERRORS = {
     -5: "CDG_ERR_BREAKDOWN", -6: "CDG_ERR_ZERO_DIAG", -7: "CDG_ERR_PATTERN",
     -8: "CDG_ERR_SINGULAR", -9: "CDG_ERR_NO_DEVICE", -10: "CDG_ERR_LIMIT",
 }
-EX_SINE_LAPLACE, EX_SINE, EX_POLYEXP, EX_CONST_F, EX_POLY1, EX_BUMP, EX_POLY1_T = range(7)
+EX_SINE_LAPLACE, EX_SINE, EX_POLYEXP, EX_CONST_F, EX_POLY1, EX_BUMP, EX_POLY1_T, EX_EXP_SIN = range(8)
 CELL_QUAD, CELL_HEXA, CELL_TETRA = 2, 3, 4
 
 # every symbol include/parmoon_cd.h declares

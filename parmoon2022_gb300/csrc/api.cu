@@ -516,7 +516,7 @@ int cdg_problem_destroy(cdg_problem* p) {
 
 static int check_assembly_params(const cdg_problem* p, const cdg_assembly_params* a) {
   if (!p || !a) { set_error("null argument"); return CDG_ERR_ARG; }
-  if (a->example < 0 || a->example > CDG_EX_POLY1_T) { set_error("unknown example %d", a->example); return CDG_ERR_ARG; }
+  if (a->example < 0 || a->example > CDG_EX_EXP_SIN) { set_error("unknown example %d", a->example); return CDG_ERR_ARG; }
   if (a->example == CDG_EX_POLYEXP && p->dim != 3) { set_error("example needs 3D"); return CDG_ERR_ARG; }
   return CDG_OK;
 }

@@ -132,6 +132,21 @@ __device__ void ex_exact(const AsmCoefs& k, const double* x, double* u) {
     u[2] = px * (1 - 2 * x[1]) * qz;
     u[3] = px * qy * (1 - 2 * x[2]);
     u[4] = px2 * qy * qz - 2 * px * qz - 2 * px * qy;
+  } else if (k.example == CDG_EX_EXP_SIN) {
+    // e^{sin 2 pi t} prod sin(2 pi x_a) (include/Examples/TCD_2D/exp.h)
+    const double w = 2.0 * M_PI, e = exp(sin(w * k.t));
+    double sn[3], cs[3];
+    for (int a = 0; a < d; ++a) {
+      sn[a] = sin(w * x[a]);
+      cs[a] = cos(w * x[a]);
+    }
+    const double pr = d == 2 ? sn[0] * sn[1] : sn[0] * sn[1] * sn[2];
+    u[0] = e * pr;
+    u[1] = e * w * cs[0] * sn[1] * (d == 3 ? sn[2] : 1.0);
+    u[2] = e * w * sn[0] * cs[1] * (d == 3 ? sn[2] : 1.0);
+    if (d == 3) u[3] = e * w * sn[0] * sn[1] * cs[2];
+    u[d + 1] = -d * w * w * e * pr;
+    u[d + 2] = w * cos(w * k.t) * e * pr;
   } else if (k.example == CDG_EX_POLY1 || k.example == CDG_EX_POLY1_T) {
     const double s = k.example == CDG_EX_POLY1_T ? 1.0 + k.t : 1.0;
     const double q = 1 + x[0] + 2 * x[1] + (d == 3 ? 3 * x[2] : 0.0);

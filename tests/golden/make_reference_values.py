@@ -1,9 +1,10 @@
 """Extract the golden values the reference's own tests hold for the CD path.
 
 Reads (as text) test/cd2d_test.c++ (error norms of CD2D example 0 on the
-4x4 UnitSquare for Q1..Q8, tolerance 1e-11) and test/structure_test.c++
-(pattern counts of one-cell meshes), and writes reference_values.json next
-to this script.  Runs where the reference tree is present; the JSON is
+4x4 UnitSquare for Q1..Q8, tolerance 1e-11), test/tcd2d_test.c++ (L2 / H1
+errors of the Crank-Nicolson TCD2D example 0 after selected steps, Galerkin
+and SUPG, tolerance 1e-10) and test/structure_test.c++ (pattern counts of
+one-cell meshes), and writes reference_values.json next to this script.  Runs where the reference tree is present; the JSON is
 committed so the tests never need the reference itself.
 """
 import json
@@ -26,6 +27,21 @@ def cd2d_errors():
     return out, tol
 
 
+def tcd2d_errors():
+    src = open(os.path.join(REF, "test", "tcd2d_test.c++")).read()
+
+    def arr(name, conv):
+        m = re.search(name + r"\[nb_test\] = \{([^}]*)\};", src)
+        return [conv(v) for v in m.group(1).replace("\n", " ").split(",")]
+
+    steps = arr("iter_m", int)
+    tol = float(re.search(r"double eps = ([0-9.e+-]+);", src).group(1))
+    out = {}
+    for kind in ("galerkin", "supg"):
+        out[kind] = dict(L2=arr("L2_" + kind, float), H1=arr("H1_" + kind, float))
+    return steps, tol, out
+
+
 def structure_counts():
     src = open(os.path.join(REF, "test", "structure_test.c++")).read()
     body = src[src.index("std::array<unsigned int, 4> get_reference_values("):]
@@ -40,12 +56,21 @@ def structure_counts():
 
 if __name__ == "__main__":
     errs, tol = cd2d_errors()
+    tcd_steps, tcd_tol, tcd_errs = tcd2d_errors()
     data = {
         "cd2d_test": {
             "source": "test/cd2d_test.c++:42-145 (UnitSquare refined twice, example 0, "
                       "diffusion_coefficient 1, Neumann on boundary component 1)",
             "tolerance": tol,
             "errors": errs,
+        },
+        "tcd2d_test": {
+            "source": "test/tcd2d_test.c++:24-137 (UnitSquare refined 5 times, Q1, example 0 "
+                      "exp_sin_cos, diffusion 1, b = (1, -1), c = 1, Crank-Nicolson, "
+                      "tau 0.05, direct solver)",
+            "tolerance": tcd_tol,
+            "steps": tcd_steps,
+            "errors": tcd_errs,
         },
         "structure_test": {
             "source": "test/structure_test.c++:603-660 (one-cell UnitSquare_quad.mesh, no face integrals)",
