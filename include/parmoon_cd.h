@@ -57,6 +57,21 @@ extern "C" {
 #define CDG_EX_EXP_SIN 7          /* u = e^{sin 2 pi t} prod sin(2 pi x_i): the
                                      TCD2D example 0 of the reference's tests
                                      (include/Examples/TCD_2D/exp.h)          */
+#define CDG_EX_LINEAR_ST 8        /* u = 1 + 2x + 3ty (+ 4tz): linear in space
+                                     and time, example -2 of the TCD tests
+                                     (include/Examples/TCD_3D/
+                                     linear_space_time.h, TCD_2D/ the same
+                                     at z = 0)                                */
+#define CDG_EX_QUAD_ST 9          /* u = t^2 (x^2 + yz): quadratic space-time,
+                                     example -1 of the TCD3D tests
+                                     (include/Examples/TCD_3D/
+                                     quadratic_space_time.h)                  */
+
+/* time_discretization (TimeDiscretization, src/TimeDiscRoutines/
+ * TimeDiscretizations.C:36-50,117-215,422-475); zero is Crank-Nicolson */
+#define CDG_TIME_CRANK_NICOLSON 0
+#define CDG_TIME_BACKWARD_EULER 1
+#define CDG_TIME_BDF_TWO 2
 
 /* local assembling + example: LocalAssembling<d>(db, ConvDiff, {}, coeffs,
  * disctype) with the TDatabase globals the CD routines read */
@@ -81,6 +96,10 @@ typedef struct {
                            the time-dependent routines takes at
                            cdg_problem_tcd_initialize (each step uses its own
                            tau); ignored by the stationary problem          */
+  int time_discretization; /* CDG_TIME_*: the scheme of cdg_problem_tcd_step  */
+  int bdf_two_first_step;  /* bdf_two_first_step, the scheme of the first
+                              CDG_TIME_BDF_TWO step: 0 backward Euler (the
+                              reference's default), 1 Crank-Nicolson       */
 } cdg_assembly_params;
 
 /* Solver ParameterDatabase keys (src/Solver/Solver.C:26-209,
@@ -242,20 +261,28 @@ int cdg_problem_errors(cdg_problem *p, const cdg_assembly_params *a,
 int cdg_problem_errors_noalloc(cdg_problem *p, const cdg_assembly_params *a,
                                double *errors);
 
-/* ---- time-dependent CD: TimeConvectionDiffusion<d> with Crank-Nicolson -- */
+/* ---- time-dependent CD: TimeConvectionDiffusion<d> -------------------- */
 /* assemble_initial_time (src/System/TimeConvectionDiffusion.C:260-311): on
  * every level stiffness, mass and rhs at time a->t (Dirichlet rows assembled
  * in full); the finest solution becomes the interpolant of the example's
  * initial condition.  With SUPG (TCDStiffSUPG, TCDMassSUPG, TCDRhsSUPG,
  * src/General/CD_local_assembling_routines.C:184-387) the stabilisation
- * parameter uses theta1 * a->time_step, which must then be positive */
+ * parameter uses theta1 * a->time_step, which must then be positive; theta1
+ * is that of the first step of a->time_discretization.  Resets the step
+ * count (TimeDiscretization::current_step_ = 0). */
 int cdg_problem_tcd_initialize(cdg_problem *p, const cdg_assembly_params *a);
-/* one Crank-Nicolson step to time a->t = t_old + tau
- * (TimeConvectionDiffusion.C:315-450, TimeDiscretizations.C:117-283):
+/* one step to time a->t = t_old + tau of a->time_discretization
+ * (TimeConvectionDiffusion.C:315-450, TimeDiscretizations.C:117-283,422-475):
  * reassemble stiffness and rhs on every level (with SUPG the mass matrix too,
- * with the parameter of this tau), rhs = tau/2 (f_new + f_old) +
- * M u_old - tau/2 A u_old on active rows, system M + tau/2 A on active rows,
- * Dirichlet data at the new time, then Solver::solve warm-started from u_old */
+ * with the parameter theta1 * tau), then on active rows
+ *   Crank-Nicolson  rhs = tau/2 (f_new + f_old) + M u_old - tau/2 A u_old,
+ *                   system M + tau/2 A          (theta1 = 1/2)
+ *   backward Euler  rhs = tau f_new + M u_old, system M + tau A (theta1 = 1)
+ *   BDF2            rhs = 2/3 tau f_new + 4/3 M u_old - 1/3 M u_older,
+ *                   system M + 2/3 tau A        (theta1 = 2/3)
+ * where the first step after cdg_problem_tcd_initialize of BDF2 is taken by
+ * a->bdf_two_first_step; Dirichlet data at the new time, then Solver::solve
+ * warm-started from u_old */
 int cdg_problem_tcd_step(cdg_problem *p, const cdg_assembly_params *a, double tau,
                          const cdg_solver_params *s, cdg_solve_stats *stats);
 /* which: 0 stiffness A, 1 mass M, 2 system matrix (after a step) */

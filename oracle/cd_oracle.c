@@ -298,6 +298,7 @@ typedef struct {
   int lu_gen;       /* assembly generation the LU belongs to */
   /* time-dependent problem: stiffness, mass, rhs of this and the last step */
   double *tA, *tM, *tf, *tfold;
+  double *tu2;      /* BDF2: solution of the step before the last (finest level) */
 } level_t;
 
 struct orc_problem {
@@ -311,6 +312,7 @@ struct orc_problem {
   int asm_gen;      /* incremented by every orc_assemble */
   int tcd;          /* assembling for the time-dependent problem */
   double ttau;      /* THETA1 * CURRENTTIMESTEPLENGTH (Crank-Nicolson: tau/2) */
+  int tcd_step;     /* TimeDiscretization::current_step_ */
 };
 
 static int nverts(int dim) { return dim == 2 ? 4 : 8; }
@@ -517,6 +519,27 @@ static void exact_sol(const orc_config *c, const double *x, double *u) {
     if (d == 3) u[3] = e * w * s[0] * s[1] * co[2];
     u[d + 1] = -d * w * w * e * p;
     u[d + 2] = w * cos(w * c->t) * e * p;
+    break;
+  }
+  case ORC_EX_LINEAR_ST: {
+    /* include/Examples/TCD_3D/linear_space_time.h (TCD_2D: z = 0) */
+    double z = d == 3 ? x[2] : 0.0;
+    u[0] = 1 + 2 * x[0] + 3 * c->t * x[1] + 4 * c->t * z;
+    u[1] = 2;
+    u[2] = 3 * c->t;
+    if (d == 3) u[3] = 4 * c->t;
+    u[d + 2] = 3 * x[1] + 4 * z;
+    break;
+  }
+  case ORC_EX_QUAD_ST: {
+    /* include/Examples/TCD_3D/quadratic_space_time.h */
+    double z = d == 3 ? x[2] : 0.0, t2 = c->t * c->t, q = x[0] * x[0] + x[1] * z;
+    u[0] = t2 * q;
+    u[1] = 2 * x[0] * t2;
+    u[2] = z * t2;
+    if (d == 3) u[3] = x[1] * t2;
+    u[d + 1] = 2 * t2;
+    u[d + 2] = 2 * c->t * q;
     break;
   }
   case ORC_EX_POLY1:
@@ -1082,7 +1105,7 @@ void orc_destroy(orc_problem *p) {
     free(L->val); free(L->rhs); free(L->sol); free(L->diag);
     free(L->mg_rhs); free(L->mg_sol); free(L->mg_def);
     free(L->lu); free(L->piv);
-    free(L->tA); free(L->tM); free(L->tf); free(L->tfold);
+    free(L->tA); free(L->tM); free(L->tf); free(L->tfold); free(L->tu2);
   }
   free(p->lev);
   free(p);
@@ -2153,17 +2176,33 @@ static void ensure_tcd(level_t *L) {
   L->tfold = (double *)calloc(L->ndof, sizeof(double));
 }
 
+/* the scheme of step `step` (TimeDiscretization::set_time_disc_parameters,
+ * TimeDiscretizations.C:422-475): BDF2 takes its first step (and the initial
+ * assembly, step 0) by bdf_two_first_step; *theta1 = THETA1 */
+static int step_scheme(const orc_config *c, int step, double *theta1) {
+  int kind = c->time_disc;
+  if (kind == ORC_TIME_BDF_TWO && step <= 1)
+    kind = c->bdf_first == 1 ? ORC_TIME_CRANK_NICOLSON : ORC_TIME_BACKWARD_EULER;
+  *theta1 = kind == ORC_TIME_CRANK_NICOLSON ? 0.5 : kind == ORC_TIME_BACKWARD_EULER ? 1.0 : 2. / 3.;
+  return kind;
+}
+
 /* TimeConvectionDiffusion::assemble_initial_time (TimeConvectionDiffusion.C
  * call_assembling_routine with assemble_dirichlet_rows): stiffness, mass and
  * rhs at cfg.t on every level, old_rhs = rhs, then the initial condition
- * interpolated into the finest solution (every DOF) */
+ * interpolated into the finest solution (every DOF); solution_m2 =
+ * solution_m1 = solution (TimeConvectionDiffusion.C:306-310) */
 int orc_tcd_initialize(orc_problem *p) {
+  if (p->cfg.time_disc < 0 || p->cfg.time_disc > 2) FAIL("time discretization not supported");
   if (p->cfg.supg) {
     if (!(p->cfg.time_step > 0)) FAIL("SUPG for the time-dependent problem needs the time step");
     if (p->cfg.sdfem_type >= 9 && p->cfg.sdfem_type <= 12) FAIL("SDFEM_TYPE not supported");
   }
+  double theta1;
+  step_scheme(&p->cfg, 0, &theta1);
   p->tcd = 1;
-  p->ttau = 0.5 * p->cfg.time_step;
+  p->tcd_step = 0;
+  p->ttau = theta1 * p->cfg.time_step;
   for (int k = 0; k < p->nlev; ++k) {
     level_t *L = &p->lev[k];
     ensure_tcd(L);
@@ -2180,22 +2219,31 @@ int orc_tcd_initialize(orc_problem *p) {
       F->sol[F->gdof[cell * nl + k]] = initial_value(&p->cfg, x);
     }
   }
+  if (!F->tu2) F->tu2 = (double *)calloc(F->ndof, sizeof(double));
+  memcpy(F->tu2, F->sol, sizeof(double) * F->ndof);
   return 0;
 }
 
-/* one Crank-Nicolson step (TimeDiscretizations.C:171-189 rhs, :219-251
- * system matrix; TimeConvectionDiffusion::assemble / solve):
- *   rhs (active)     = tau/2 (f_new + f_old) + M u_old - tau/2 A u_old
- *   rhs (non-active) = f_new (Dirichlet data at t_new), copied into u
- *   S (active rows)  = tau/2 A + M, Dirichlet rows keep A
- * then FGMRES on S from u_old */
+/* one step of the scheme (TimeDiscretizations.C:117-189 rhs, :195-251 system
+ * matrix; TimeConvectionDiffusion::assemble / solve), on active rows
+ *   Crank-Nicolson: rhs = tau/2 f_new + tau/2 f_old + M u1 - tau/2 A u1,
+ *                   S = tau/2 A + M
+ *   backward Euler: rhs = tau f_new + M u1, S = tau A + M
+ *   BDF2:           rhs = (2/3 tau) f_new + 4/3 M u1 - 1/3 M u2,
+ *                   S = (2/3 tau) A + M
+ * (u1 the last solution, u2 the one before); non-active rows: rhs = f_new
+ * (Dirichlet data at t_new), copied into u, and S keeps the rows of A.  The
+ * SUPG parameter takes THETA1 * tau.  Then FGMRES on S from u1 */
 int orc_tcd_step(orc_problem *p, double t_new, double tau, const orc_solver_config *s,
                  int *iterations, double *residual, double *initial_residual) {
   if (!p->lev[0].tA) FAIL("call orc_tcd_initialize first");
   if (!(tau > 0)) FAIL("time step must be positive");
+  if (p->cfg.time_disc < 0 || p->cfg.time_disc > 2) FAIL("time discretization not supported");
+  double theta1;
+  const int kind = step_scheme(&p->cfg, ++p->tcd_step, &theta1);
   p->cfg.t = t_new;
   p->tcd = 1;
-  p->ttau = 0.5 * tau;
+  p->ttau = theta1 * tau;
   /* with SUPG the mass matrix is reassembled too (TimeConvectionDiffusion.C
    * assemble: TCDStiffMassRhs, assemble_both) */
   for (int k = 0; k < p->nlev; ++k) {
@@ -2203,30 +2251,40 @@ int orc_tcd_step(orc_problem *p, double t_new, double tau, const orc_solver_conf
     if (assemble_into(p, k, L->tA, L->tf, 1, p->cfg.supg ? L->tM : NULL)) return -1;
   }
   level_t *F = &p->lev[0];
-  double ht = 0.5 * tau;
+  const double c_new = kind == ORC_TIME_BDF_TWO ? (2. / 3.) * tau : theta1 * tau;
   for (int r = 0; r < F->ndof; ++r) {
     if (r < F->nactive) {
-      double sa = 0, sm = 0;
+      double sa = 0, sm = 0, sm2 = 0;
       for (int n = F->row_ptr[r]; n < F->row_ptr[r + 1]; ++n) {
         sa += F->tA[n] * F->sol[F->col[n]];
         sm += F->tM[n] * F->sol[F->col[n]];
+        sm2 += F->tM[n] * F->tu2[F->col[n]];
       }
-      double v = ht * F->tf[r];
-      v += ht * F->tfold[r];
-      v += sm;
-      v += -ht * sa;
+      double v = c_new * F->tf[r];
+      if (kind == ORC_TIME_CRANK_NICOLSON) {
+        v += c_new * F->tfold[r];
+        v += sm;
+        v += -c_new * sa;
+      } else if (kind == ORC_TIME_BDF_TWO) {
+        v += (4. / 3.) * sm;
+        v += (-1. / 3.) * sm2;
+      } else {
+        v += sm;
+      }
       F->rhs[r] = v;
     } else {
       F->rhs[r] = F->tf[r];
     }
   }
   memcpy(F->tfold, F->tf, sizeof(double) * F->ndof);
+  memcpy(F->tu2, F->sol, sizeof(double) * F->ndof);   /* solution_m2 = solution_m1 */
   for (int r = F->nactive; r < F->ndof; ++r) F->sol[r] = F->rhs[r];
+  const double factor = kind == ORC_TIME_BDF_TWO ? tau * (2. / 3.) : theta1 * tau;
   for (int k = 0; k < p->nlev; ++k) {
     level_t *L = &p->lev[k];
     int nae = L->row_ptr[L->nactive];
     for (int n = 0; n < L->nnz; ++n)
-      L->val[n] = n < nae ? L->tA[n] * ht + L->tM[n] : L->tA[n];
+      L->val[n] = n < nae ? L->tA[n] * factor + L->tM[n] : L->tA[n];
     for (int r = 0; r < L->ndof; ++r)
       for (int n = L->row_ptr[r]; n < L->row_ptr[r + 1]; ++n)
         if (L->col[n] == r) L->diag[r] = L->val[n];

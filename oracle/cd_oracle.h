@@ -27,9 +27,16 @@ enum {
   ORC_EX_POLY1 = 4,        /* u = 1 + x + 2y (+3z): inside Q1, Dirichlet       */
   ORC_EX_BUMP = 5,         /* f = 0, u_D = 0, u0 = exp(-|x-c|^2/(2 s^2))       */
   ORC_EX_POLY1_T = 6,      /* u = (1+t)(1 + x + 2y (+3z))                      */
-  ORC_EX_EXP_SIN = 7       /* u = e^{sin 2 pi t} prod sin(2 pi x_i) (TCD2D example 0,
+  ORC_EX_EXP_SIN = 7,      /* u = e^{sin 2 pi t} prod sin(2 pi x_i) (TCD2D example 0,
                               include/Examples/TCD_2D/exp.h)                   */
+  ORC_EX_LINEAR_ST = 8,    /* u = 1 + 2x + 3ty (+4tz) (TCD example -2,
+                              include/Examples/TCD_3D/linear_space_time.h)     */
+  ORC_EX_QUAD_ST = 9       /* u = t^2 (x^2 + yz) (TCD3D example -1,
+                              include/Examples/TCD_3D/quadratic_space_time.h)  */
 };
+
+/* TimeDiscretization schemes (src/TimeDiscRoutines/TimeDiscretizations.C) */
+enum { ORC_TIME_CRANK_NICOLSON = 0, ORC_TIME_BACKWARD_EULER = 1, ORC_TIME_BDF_TWO = 2 };
 
 typedef struct {
   int dim;             /* 2 or 3                                              */
@@ -52,6 +59,8 @@ typedef struct {
   double t;            /* time of f and the boundary data                     */
   double ic[4];        /* ORC_EX_BUMP centre and sigma                        */
   double time_step;    /* TIMESTEPLENGTH at orc_tcd_initialize (SUPG only)    */
+  int time_disc;       /* ORC_TIME_*                                          */
+  int bdf_first;       /* first BDF2 step: 0 backward Euler, 1 Crank-Nicolson */
 } orc_config;
 
 typedef struct {

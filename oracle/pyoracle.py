@@ -12,7 +12,9 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "libcd_oracle.so")
 
-EX_SINE_LAPLACE, EX_SINE, EX_POLYEXP, EX_CONST_F, EX_POLY1, EX_BUMP, EX_POLY1_T, EX_EXP_SIN = range(8)
+(EX_SINE_LAPLACE, EX_SINE, EX_POLYEXP, EX_CONST_F, EX_POLY1, EX_BUMP, EX_POLY1_T, EX_EXP_SIN,
+ EX_LINEAR_ST, EX_QUAD_ST) = range(10)
+TIME_SCHEMES = {"crank_nicolson": 0, "backward_euler": 1, "bdf_two": 2}
 
 
 class Config(ctypes.Structure):
@@ -27,6 +29,7 @@ class Config(ctypes.Structure):
         ("poly_degree", ctypes.c_int), ("tetra", ctypes.c_int),
         ("b_grad", ctypes.c_double * 9), ("t", ctypes.c_double),
         ("ic", ctypes.c_double * 4), ("time_step", ctypes.c_double),
+        ("time_disc", ctypes.c_int), ("bdf_first", ctypes.c_int),
     ]
 
 
@@ -109,7 +112,8 @@ def _ip(a):
 def make_config(dim, order, nref, example, eps=1.0, b=(0, 0, 0), c=0.0, freq=1.0,
                 supg=False, sdfem_type=2, delta0=1.0, delta1=1.0, cell_measure=0,
                 problem_linear=0, neumann_mask=0, poly_degree=0, tetra=False,
-                b_grad=None, t=0.0, ic=(0.5, 0.5, 0.5, 0.1), time_step=0.0):
+                b_grad=None, t=0.0, ic=(0.5, 0.5, 0.5, 0.1), time_step=0.0,
+                time_discretization="crank_nicolson", bdf_two_first_step="backward_euler"):
     cfg = Config()
     cfg.dim, cfg.order, cfg.nref, cfg.example = dim, order, nref, example
     cfg.eps = eps
@@ -126,6 +130,8 @@ def make_config(dim, order, nref, example, eps=1.0, b=(0, 0, 0), c=0.0, freq=1.0
             cfg.b_grad[i] = float(bg[i])
     cfg.t = t
     cfg.time_step = time_step
+    cfg.time_disc = TIME_SCHEMES[time_discretization]
+    cfg.bdf_first = 1 if bdf_two_first_step == "crank_nicolson" else 0
     for i in range(4):
         cfg.ic[i] = ic[i]
     return cfg

@@ -26,7 +26,10 @@ ERRORS = {
     -5: "CDG_ERR_BREAKDOWN", -6: "CDG_ERR_ZERO_DIAG", -7: "CDG_ERR_PATTERN",
     -8: "CDG_ERR_SINGULAR", -9: "CDG_ERR_NO_DEVICE", -10: "CDG_ERR_LIMIT",
 }
-EX_SINE_LAPLACE, EX_SINE, EX_POLYEXP, EX_CONST_F, EX_POLY1, EX_BUMP, EX_POLY1_T, EX_EXP_SIN = range(8)
+(EX_SINE_LAPLACE, EX_SINE, EX_POLYEXP, EX_CONST_F, EX_POLY1, EX_BUMP, EX_POLY1_T, EX_EXP_SIN,
+ EX_LINEAR_ST, EX_QUAD_ST) = range(10)
+# TimeDiscretization schemes (db["time_discretization"])
+TIME_SCHEMES = {"crank_nicolson": 0, "backward_euler": 1, "bdf_two": 2}
 CELL_QUAD, CELL_HEXA, CELL_TETRA = 2, 3, 4
 
 # every symbol include/parmoon_cd.h declares
@@ -66,7 +69,8 @@ class AssemblyParams(ctypes.Structure):
         ("cell_measure", ctypes.c_int), ("problem_linear", ctypes.c_int),
         ("neumann_mask", ctypes.c_int), ("poly_degree", ctypes.c_int),
         ("b_grad", ctypes.c_double * 9), ("t", ctypes.c_double), ("ic", ctypes.c_double * 4),
-        ("time_step", ctypes.c_double),
+        ("time_step", ctypes.c_double), ("time_discretization", ctypes.c_int),
+        ("bdf_two_first_step", ctypes.c_int),
     ]
 
 
@@ -201,9 +205,18 @@ def _ip(a):
 def assembly_params(example=EX_SINE, eps=1.0, b=(0.0, 0.0, 0.0), c=0.0, freq=1.0,
                     space_discretization_type="galerkin", sdfem_type=2, delta0=1.0, delta1=1.0,
                     cell_measure=0, problem_linear=0, neumann_mask=0, poly_degree=0,
-                    b_grad=None, t=0.0, ic=(0.0, 0.0, 0.0, 1.0), time_step=0.0):
-    """b_grad: 3x3 gradient of a convection field linear in x (row-major)."""
+                    b_grad=None, t=0.0, ic=(0.0, 0.0, 0.0, 1.0), time_step=0.0,
+                    time_discretization="crank_nicolson", bdf_two_first_step="backward_euler"):
+    """b_grad: 3x3 gradient of a convection field linear in x (row-major).
+    time_discretization: "crank_nicolson", "backward_euler" or "bdf_two";
+    bdf_two_first_step: "backward_euler" or "crank_nicolson"."""
     a = AssemblyParams()
+    if time_discretization not in TIME_SCHEMES:
+        raise ValueError("time discretization scheme %r is not supported" % (time_discretization,))
+    if bdf_two_first_step not in ("backward_euler", "crank_nicolson"):
+        raise ValueError("bdf_two_first_step %r" % (bdf_two_first_step,))
+    a.time_discretization = TIME_SCHEMES[time_discretization]
+    a.bdf_two_first_step = 1 if bdf_two_first_step == "crank_nicolson" else 0
     if b_grad is not None:
         g = np.asarray(b_grad, dtype=np.float64).reshape(-1)
         for i in range(9):
@@ -388,6 +401,41 @@ class Context:
 
     def __del__(self):
         self.close()
+
+
+class TimeErrors:
+    """Errors integrated over time, as TimeConvectionDiffusion::output
+    accumulates them (src/System/TimeConvectionDiffusion.C:936-966) and
+    get_errors returns them (:1179-1187): the trapezoidal rule in time for
+    L2(0,t;L2), L2(0,t;H1) (and L2(0,t;SUPG)), maxima for L_inf(0,t;L_inf) and
+    L_inf(0,t;L2).  The previous value starts at zero, so the first add()
+    counts half a step of the first error only."""
+
+    def __init__(self, supg=False):
+        self.supg = supg
+        self.errors = [0.0] * 8
+        self.t_linf = self.t_l2 = 0.0
+
+    def add(self, local, tau, t):
+        """local: ConvectionDiffusion.errors() at time t (L2, H1-semi, SD, DG, L_inf)."""
+        e = self.errors
+        e[0] += (local[0] * local[0] + e[1] * e[1]) * tau * 0.5
+        e[1] = local[0]
+        e[2] += (local[1] * local[1] + e[3] * e[3]) * tau * 0.5
+        e[3] = local[1]
+        if self.supg:
+            e[6] += (local[2] * local[2] + e[7] * e[7]) * tau * 0.5
+            e[7] = local[2]
+        if e[4] < local[4]:
+            e[4] = local[4]
+            self.t_linf = t
+        if e[5] < local[0]:
+            e[5] = local[0]
+            self.t_l2 = t
+
+    def get_errors(self):
+        """(L2(0,t;L2), L2(0,t;H1), L_inf(0,t;L_inf))"""
+        return (float(np.sqrt(self.errors[0])), float(np.sqrt(self.errors[2])), self.errors[4])
 
 
 class ConvectionDiffusion:

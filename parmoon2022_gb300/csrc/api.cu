@@ -516,7 +516,15 @@ int cdg_problem_destroy(cdg_problem* p) {
 
 static int check_assembly_params(const cdg_problem* p, const cdg_assembly_params* a) {
   if (!p || !a) { set_error("null argument"); return CDG_ERR_ARG; }
-  if (a->example < 0 || a->example > CDG_EX_EXP_SIN) { set_error("unknown example %d", a->example); return CDG_ERR_ARG; }
+  if (a->example < 0 || a->example > CDG_EX_QUAD_ST) { set_error("unknown example %d", a->example); return CDG_ERR_ARG; }
+  if (a->time_discretization < CDG_TIME_CRANK_NICOLSON || a->time_discretization > CDG_TIME_BDF_TWO) {
+    set_error("time discretization scheme %d is not supported", a->time_discretization);
+    return CDG_ERR_ARG;
+  }
+  if (a->bdf_two_first_step < 0 || a->bdf_two_first_step > 1) {
+    set_error("bdf_two_first_step %d: 0 backward Euler or 1 Crank-Nicolson", a->bdf_two_first_step);
+    return CDG_ERR_ARG;
+  }
   if (a->example == CDG_EX_POLYEXP && p->dim != 3) { set_error("example needs 3D"); return CDG_ERR_ARG; }
   return CDG_OK;
 }
@@ -597,13 +605,18 @@ int cdg_problem_tcd_initialize(cdg_problem* p, const cdg_assembly_params* a) {
   CDG_TRY(check_assembly_params(p, a));
   CDG_CUDA(cudaSetDevice(p->ctx->device));
   CDG_CUDA(cudaMemsetAsync(p->d_zero_diag, 0, sizeof(int), p->ctx->stream));
+  p->tcd_step = 0;
+  const TimeScheme ts = time_scheme(*a, 0);
   for (auto& L : p->lev) {
-    CDG_TRY(tcd_assemble_level(p->ctx, p, L, *a, true, a->time_step));
+    CDG_TRY(tcd_assemble_level(p->ctx, p, L, *a, true, ts.theta1 * a->time_step));
     // old_rhs = rhs
     CDG_CUDA(cudaMemcpyAsync(L.tcd_fold, L.tcd_f, (size_t)L.ndof * sizeof(double),
                              cudaMemcpyDeviceToDevice, p->ctx->stream));
   }
   CDG_TRY(tcd_interpolate(p->ctx, p, *a));
+  DevLevel& F = p->lev[0];
+  // solution_m2 = solution_m1 = the initial solution (TimeConvectionDiffusion.C:306-310)
+  CDG_TRY(tcd_start_history(p->ctx, F));
   return check_device_error(p->ctx);
 }
 
@@ -617,17 +630,19 @@ int cdg_problem_tcd_step(cdg_problem* p, const cdg_assembly_params* a, double ta
   auto t0 = std::chrono::steady_clock::now();
   cudaStream_t stm = p->ctx->stream;
   CDG_CUDA(cudaMemsetAsync(p->d_zero_diag, 0, sizeof(int), stm));
-  // reassemble stiffness and rhs on every level (the Galerkin mass is time
-  // independent; the SUPG mass is reassembled with this tau)
-  for (auto& L : p->lev) CDG_TRY(tcd_assemble_level(p->ctx, p, L, *a, false, tau));
+  const TimeScheme ts = time_scheme(*a, ++p->tcd_step);
   DevLevel& F = p->lev[0];
-  CDG_TRY(tcd_cn_rhs(p->ctx, F, tau));
+  // reassemble stiffness and rhs on every level (the Galerkin mass is time
+  // independent; the SUPG mass is reassembled with theta1 * tau)
+  for (auto& L : p->lev)
+    CDG_TRY(tcd_assemble_level(p->ctx, p, L, *a, false, ts.theta1 * tau));
+  CDG_TRY(tcd_rhs(p->ctx, F, ts, tau));
   // solution.copy_nonactive(rhs): Dirichlet data at the new time
   const int nd = F.ndof - F.nactive;
   if (nd > 0)
     CDG_CUDA(cudaMemcpyAsync(F.sol + F.nactive, F.rhs + F.nactive, (size_t)nd * sizeof(double),
                              cudaMemcpyDeviceToDevice, stm));
-  for (auto& L : p->lev) CDG_TRY(tcd_system(p->ctx, p, L, tau));
+  for (auto& L : p->lev) CDG_TRY(tcd_system(p->ctx, p, L, ts, tau));
   cdg_solve_stats local{};
   CDG_TRY(prepare_solver(p->ctx, p, *s));
   int rc = fgmres(p->ctx, p, *s, &local);

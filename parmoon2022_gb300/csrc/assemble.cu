@@ -147,6 +147,24 @@ __device__ void ex_exact(const AsmCoefs& k, const double* x, double* u) {
     if (d == 3) u[3] = e * w * sn[0] * sn[1] * cs[2];
     u[d + 1] = -d * w * w * e * pr;
     u[d + 2] = w * cos(w * k.t) * e * pr;
+  } else if (k.example == CDG_EX_LINEAR_ST) {
+    // 1 + 2x + 3ty (+ 4tz) (include/Examples/TCD_3D/linear_space_time.h)
+    const double z = d == 3 ? x[2] : 0.0;
+    u[0] = 1 + 2 * x[0] + 3 * k.t * x[1] + 4 * k.t * z;
+    u[1] = 2;
+    u[2] = 3 * k.t;
+    if (d == 3) u[3] = 4 * k.t;
+    u[d + 2] = 3 * x[1] + 4 * z;
+  } else if (k.example == CDG_EX_QUAD_ST) {
+    // t^2 (x^2 + yz) (include/Examples/TCD_3D/quadratic_space_time.h)
+    const double z = d == 3 ? x[2] : 0.0, t2 = k.t * k.t;
+    const double q = x[0] * x[0] + x[1] * z;
+    u[0] = t2 * q;
+    u[1] = 2 * x[0] * t2;
+    u[2] = z * t2;
+    if (d == 3) u[3] = x[1] * t2;
+    u[d + 1] = 2 * t2;
+    u[d + 2] = 2 * k.t * q;
   } else if (k.example == CDG_EX_POLY1 || k.example == CDG_EX_POLY1_T) {
     const double s = k.example == CDG_EX_POLY1_T ? 1.0 + k.t : 1.0;
     const double q = 1 + x[0] + 2 * x[1] + (d == 3 ? 3 * x[2] : 0.0);
@@ -998,50 +1016,68 @@ __global__ void k_interpolate(AsmCoefs k, int ncells, const double* __restrict__
   }
 }
 
-// Crank-Nicolson right-hand side (TimeDiscretizations.C:171-189):
-//   active rows:     tau/2 (f_new + f_old) + M u_old - tau/2 A u_old
-//   non-active rows: f_new (Dirichlet data, copy_nonactive)
-template <int TPR>
+// Right-hand side of one step (TimeDiscretization::prepare_rhs_from_time_disc,
+// TimeDiscretizations.C:117-189), on active rows
+//   Crank-Nicolson  c_new f_new + c_new f_old + M u - c_new A u   (c_new = tau/2)
+//   backward Euler  c_new f_new + M u                             (c_new = tau)
+//   BDF2            c_new f_new + 4/3 M u - 1/3 M u2              (c_new = 2/3 tau)
+// in the reference's order of additions; non-active rows take f_new (the
+// Dirichlet data, copy_nonactive).  Only the operands a scheme uses are read.
+template <int TPR, int KIND>
 __global__ void __launch_bounds__(256)
-k_cn_rhs(int n, int nactive, const int* __restrict__ rp, const int* __restrict__ col,
-         const double* __restrict__ Aval, const double* __restrict__ Mval,
-         const double* __restrict__ u, const double* __restrict__ fnew,
-         const double* __restrict__ fold, double half_tau, double* __restrict__ out) {
+k_tcd_rhs(int n, int nactive, const int* __restrict__ rp, const int* __restrict__ col,
+          const double* __restrict__ Aval, const double* __restrict__ Mval,
+          const double* __restrict__ u, const double* __restrict__ u2,
+          const double* __restrict__ fnew, const double* __restrict__ fold, double c_new,
+          double* __restrict__ out) {
+  constexpr bool kA = KIND == CDG_TIME_CRANK_NICOLSON, kU2 = KIND == CDG_TIME_BDF_TWO;
   const long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
   const int row = (int)(gt / TPR), sub = threadIdx.x % TPR;
-  double sa = 0.0, sm = 0.0;
+  double sa = 0.0, sm = 0.0, sm2 = 0.0;
   if (row < nactive) {
     const int e = rp[row + 1];
     for (int k = rp[row] + sub; k < e; k += TPR) {
-      const double x = __ldg(u + __ldg(col + k));
-      sa = fma(__ldcs(Aval + k), x, sa);
-      sm = fma(__ldcs(Mval + k), x, sm);
+      const int c = __ldg(col + k);
+      const double m = __ldcs(Mval + k);
+      const double x = __ldg(u + c);
+      sm = fma(m, x, sm);
+      if (kA) sa = fma(__ldcs(Aval + k), x, sa);
+      if (kU2) sm2 = fma(m, __ldg(u2 + c), sm2);
     }
   }
 #pragma unroll
   for (int o = TPR / 2; o > 0; o >>= 1) {
-    sa += __shfl_xor_sync(0xffffffffu, sa, o, TPR);
     sm += __shfl_xor_sync(0xffffffffu, sm, o, TPR);
+    if (kA) sa += __shfl_xor_sync(0xffffffffu, sa, o, TPR);
+    if (kU2) sm2 += __shfl_xor_sync(0xffffffffu, sm2, o, TPR);
   }
   if (row >= n || sub != 0) return;
   if (row < nactive) {
-    double r = half_tau * fnew[row];
-    r += half_tau * fold[row];
-    r += 1.0 * sm;
-    r += -half_tau * sa;
+    double r = c_new * fnew[row];
+    if (kA) {
+      r += c_new * fold[row];
+      r += 1.0 * sm;
+      r += -c_new * sa;
+    } else if (kU2) {
+      r += (4. / 3.) * sm;
+      r += (-1. / 3.) * sm2;
+    } else {
+      r += 1.0 * sm;
+    }
     out[row] = r;
   } else {
     out[row] = fnew[row];
   }
 }
 
-// system matrix (TimeDiscretizations.C:219-251): active rows tau/2 A + M,
-// non-active rows keep the assembled stiffness rows
-__global__ void k_cn_system(int nactive_entries, int nnz, const double* __restrict__ Aval,
-                            const double* __restrict__ Mval, double half_tau,
-                            double* __restrict__ S) {
+// system matrix (TimeDiscretization::prepare_system_matrix,
+// TimeDiscretizations.C:195-251): active rows theta1 tau A + M, non-active
+// rows keep the assembled stiffness rows
+__global__ void k_tcd_system(int nactive_entries, int nnz, const double* __restrict__ Aval,
+                             const double* __restrict__ Mval, double factor,
+                             double* __restrict__ S) {
   for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < nnz; t += (long)gridDim.x * blockDim.x)
-    S[t] = t < nactive_entries ? Aval[t] * half_tau + 1.0 * Mval[t] : Aval[t];
+    S[t] = t < nactive_entries ? Aval[t] * factor + 1.0 * Mval[t] : Aval[t];
 }
 
 // ---------------------------------------------------------------------------
@@ -1271,7 +1307,8 @@ int free_level(DevLevel& L) {
                   L.rhs, L.sol, L.invdiag64, L.invdiag32, L.mg_rhs, L.mg_sol, L.mg_tmp,
                   L.mg_def, L.P_rp, L.P_col, L.P_val, L.P_val32, L.R_rp, L.R_col, L.R_val,
                   L.R_val32, L.coarse_inv, L.coarse_work, L.dc_rp, L.dc_col, L.dc_pos,
-                  L.tcd_A, L.tcd_M, L.tcd_f, L.tcd_fold, L.dof_rp, L.dof_ent, L.rhs_loc};
+                  L.tcd_A, L.tcd_M, L.tcd_f, L.tcd_fold, L.tcd_u2, L.dof_rp, L.dof_ent,
+                  L.rhs_loc};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   return CDG_OK;
@@ -1546,15 +1583,15 @@ int tcd_interpolate(cdg_context* ctx, cdg_problem* p, const cdg_assembly_params&
 // parameter depends on theta1 * tau, and the mass matrix carries a SUPG term,
 // so it is reassembled with every step (TimeConvectionDiffusion.C:315-346).
 int tcd_assemble_level(cdg_context* ctx, cdg_problem* p, DevLevel& L,
-                       const cdg_assembly_params& a, bool with_mass, double tau) {
+                       const cdg_assembly_params& a, bool with_mass, double theta_tau) {
   CDG_TRY(ensure_tables(ctx, p));
   CDG_TRY(ensure_tcd(L));
   AsmCoefs k = make_coefs(a, L.shape, L.order);
   CDG_TRY(check_coefs(k));
   k.tcd = 1;
-  k.ttau = 0.5 * tau;
+  k.ttau = theta_tau;
   if (k.supg) {
-    if (!(tau > 0)) { set_error("SUPG for the time-dependent problem needs the time step"); return CDG_ERR_ARG; }
+    if (!(theta_tau > 0)) { set_error("SUPG for the time-dependent problem needs the time step"); return CDG_ERR_ARG; }
     if (k.sdfem_type >= 9 && k.sdfem_type <= 12) {
       set_error("SDFEM_TYPE %d (time-step dependent) is not supported", k.sdfem_type);
       return CDG_ERR_ARG;
@@ -1572,23 +1609,46 @@ int tcd_assemble_level(cdg_context* ctx, cdg_problem* p, DevLevel& L,
   return launch_rhs(ctx, k, L, L.tcd_f);
 }
 
-// rhs of the step into L.rhs from L.sol (u_old), tcd_f (new) and tcd_fold;
-// then tcd_fold <- tcd_f
-int tcd_cn_rhs(cdg_context* ctx, DevLevel& L, double tau) {
+// rhs of the step into L.rhs from L.sol (u_old), tcd_u2 (BDF2), tcd_f (new)
+// and tcd_fold; then tcd_fold <- tcd_f and tcd_u2 <- u_old (solution_m2 =
+// solution_m1, TimeConvectionDiffusion::solve)
+int tcd_rhs(cdg_context* ctx, DevLevel& L, TimeScheme ts, double tau) {
   const int tpr = 4;
-  int grid = (int)(((long)L.ndof * tpr + 255) / 256);
-  CDG_LAUNCH(ctx, k_cn_rhs<4>, grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, L.tcd_A,
-             L.tcd_M, L.sol, L.tcd_f, L.tcd_fold, 0.5 * tau, L.rhs);
+  const int grid = (int)(((long)L.ndof * tpr + 255) / 256);
+  const double c_new = ts.kind == CDG_TIME_BDF_TWO ? (2. / 3.) * tau : ts.theta1 * tau;
+  if (ts.kind == CDG_TIME_CRANK_NICOLSON)
+    CDG_LAUNCH(ctx, (k_tcd_rhs<4, CDG_TIME_CRANK_NICOLSON>), grid, 256, 0, L.ndof, L.nactive,
+               L.row_ptr, L.col, L.tcd_A, L.tcd_M, L.sol, nullptr, L.tcd_f, L.tcd_fold, c_new,
+               L.rhs);
+  else if (ts.kind == CDG_TIME_BACKWARD_EULER)
+    CDG_LAUNCH(ctx, (k_tcd_rhs<4, CDG_TIME_BACKWARD_EULER>), grid, 256, 0, L.ndof, L.nactive,
+               L.row_ptr, L.col, nullptr, L.tcd_M, L.sol, nullptr, L.tcd_f, nullptr, c_new,
+               L.rhs);
+  else
+    CDG_LAUNCH(ctx, (k_tcd_rhs<4, CDG_TIME_BDF_TWO>), grid, 256, 0, L.ndof, L.nactive,
+               L.row_ptr, L.col, nullptr, L.tcd_M, L.sol, L.tcd_u2, L.tcd_f, nullptr, c_new,
+               L.rhs);
   CDG_CUDA(cudaMemcpyAsync(L.tcd_fold, L.tcd_f, (size_t)L.ndof * sizeof(double),
+                           cudaMemcpyDeviceToDevice, ctx->stream));
+  CDG_CUDA(cudaMemcpyAsync(L.tcd_u2, L.sol, (size_t)L.ndof * sizeof(double),
                            cudaMemcpyDeviceToDevice, ctx->stream));
   return CDG_OK;
 }
 
-// system matrix into val64 (+ FP32 copy and inverse diagonals)
-int tcd_system(cdg_context* ctx, cdg_problem* p, DevLevel& L, double tau) {
+int tcd_start_history(cdg_context* ctx, DevLevel& L) {
+  if (!L.tcd_u2) CDG_TRY(dalloc(&L.tcd_u2, (size_t)L.ndof));
+  CDG_CUDA(cudaMemcpyAsync(L.tcd_u2, L.sol, (size_t)L.ndof * sizeof(double),
+                           cudaMemcpyDeviceToDevice, ctx->stream));
+  return CDG_OK;
+}
+
+// system matrix into val64 (+ FP32 copy and inverse diagonals); the factor is
+// TimeDiscretization::get_scale_factor: tau, tau/2, 2/3 tau
+int tcd_system(cdg_context* ctx, cdg_problem* p, DevLevel& L, TimeScheme ts, double tau) {
   const int nae = L.pattern.row_ptr[L.nactive];
+  const double factor = ts.kind == CDG_TIME_BDF_TWO ? tau * (2. / 3.) : ts.theta1 * tau;
   int g = (int)std::min<long>(((long)L.nnz + 255) / 256, (long)ctx->num_sms * 16);
-  CDG_LAUNCH(ctx, k_cn_system, g, 256, 0, nae, L.nnz, L.tcd_A, L.tcd_M, 0.5 * tau, L.val64);
+  CDG_LAUNCH(ctx, k_tcd_system, g, 256, 0, nae, L.nnz, L.tcd_A, L.tcd_M, factor, L.val64);
   return finish_matrix(ctx, p, L);
 }
 

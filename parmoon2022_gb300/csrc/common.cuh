@@ -125,12 +125,14 @@ struct DevLevel {
   int* P_rp = nullptr; int* P_col = nullptr; double* P_val = nullptr; float* P_val32 = nullptr;
   int* R_rp = nullptr; int* R_col = nullptr; double* R_val = nullptr; float* R_val32 = nullptr;
   int P_nnz = 0, R_nnz = 0;
-  // time-dependent CD (Crank-Nicolson): stiffness and mass values (the system
-  // M + tau/2 A lives in val64), rhs of the current and the previous step
+  // time-dependent CD: stiffness and mass values (the system M + theta1 tau A
+  // lives in val64), rhs of the current and the previous step, and the
+  // solution of the step before the last (finest level; BDF2 reads it)
   double* tcd_A = nullptr;
   double* tcd_M = nullptr;
   double* tcd_f = nullptr;
   double* tcd_fold = nullptr;
+  double* tcd_u2 = nullptr;
   // dense inverse of the active block (coarsest multigrid level)
   double* coarse_inv = nullptr;  // na*na
   double* coarse_work = nullptr; // 2 na^2 (Gauss-Jordan ping-pong) + pivots + column map
@@ -173,6 +175,7 @@ struct cdg_problem {
   int* d_zero_diag = nullptr;     // set by the assembly when a diagonal is 0
   int nterms = 0;
   int rt_order = -1;
+  int tcd_step = 0;               // TimeDiscretization::current_step_
 };
 
 struct cdg_hierarchy {
@@ -236,12 +239,30 @@ int assemble_level(cdg_context* ctx, cdg_problem* p, DevLevel& L,
 int check_device_error(cdg_context* ctx);
 int level_errors(cdg_context* ctx, cdg_problem* p, DevLevel& L,
                  const cdg_assembly_params& a, double* errors);
-// time-dependent CD (TimeConvectionDiffusion with Crank-Nicolson)
+// time-dependent CD (TimeConvectionDiffusion with the TimeDiscretization schemes)
 int tcd_interpolate(cdg_context* ctx, cdg_problem* p, const cdg_assembly_params& a);
 int tcd_assemble_level(cdg_context* ctx, cdg_problem* p, DevLevel& L,
-                       const cdg_assembly_params& a, bool with_mass, double tau);
-int tcd_cn_rhs(cdg_context* ctx, DevLevel& L, double tau);
-int tcd_system(cdg_context* ctx, cdg_problem* p, DevLevel& L, double tau);
+                       const cdg_assembly_params& a, bool with_mass, double theta_tau);
+// The scheme one step takes (TimeDiscretization::set_time_disc_parameters,
+// src/TimeDiscRoutines/TimeDiscretizations.C:422-475): step is the index of
+// the step (TimeDiscretization::current_step_ after the increment; 0 for the
+// initial assembly), and the first BDF2 step is taken by bdf_two_first_step.
+struct TimeScheme {
+  int kind;        // CDG_TIME_CRANK_NICOLSON, _BACKWARD_EULER or _BDF_TWO
+  double theta1;   // THETA1: 1/2, 1, 2/3
+};
+inline TimeScheme time_scheme(const cdg_assembly_params& a, int step) {
+  int kind = a.time_discretization;
+  if (kind == CDG_TIME_BDF_TWO && step <= 1)
+    kind = a.bdf_two_first_step == 1 ? CDG_TIME_CRANK_NICOLSON : CDG_TIME_BACKWARD_EULER;
+  const double theta1 = kind == CDG_TIME_CRANK_NICOLSON ? 0.5
+                        : kind == CDG_TIME_BACKWARD_EULER ? 1.0 : 2. / 3.;
+  return TimeScheme{kind, theta1};
+}
+int tcd_rhs(cdg_context* ctx, DevLevel& L, TimeScheme ts, double tau);
+// solution history: tcd_u2 (allocated on first use) <- the current solution
+int tcd_start_history(cdg_context* ctx, DevLevel& L);
+int tcd_system(cdg_context* ctx, cdg_problem* p, DevLevel& L, TimeScheme ts, double tau);
 
 // linear algebra (linalg.cu)
 int spmv_apply64(cdg_context* ctx, const DevLevel& L, const double* x, double* y);
