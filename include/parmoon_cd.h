@@ -166,20 +166,22 @@ int cdg_hierarchy_create(int dim, int order, int roots, int nref, int n_levels,
                          int neumann_mask, cdg_hierarchy **out);
 /* unit cube split into roots^3 cubes of 6 Kuhn tetrahedra, P1 or P2 (order),
  * refined nref times (regular refinement, children of cell c are the eight
- * cells 8c..8c+7 of the next level); perturb > 0 moves every interior vertex
+ * cells 8c..8c+7 of the next level); neumann_mask as above (bit k: boundary
+ * face k of the cube is Neumann); perturb > 0 moves every interior vertex
  * of the finest level by perturb*h*U(-1,1) per coordinate (seeded), as the
  * perturbed-tetrahedra configuration of TCD3D asks */
 int cdg_hierarchy_create_tetra(int order, int roots, int nref, int n_levels,
-                               double perturb, unsigned long long seed,
-                               cdg_hierarchy **out);
+                               int neumann_mask, double perturb,
+                               unsigned long long seed, cdg_hierarchy **out);
 /* the same hierarchies with the FE space numbering and the TStructure of every
  * level built on the context's GPU (bit-exact with the host builders above) */
 int cdg_hierarchy_create_device(cdg_context *ctx, int dim, int order, int roots,
                                 int nref, int n_levels, int neumann_mask,
                                 cdg_hierarchy **out);
 int cdg_hierarchy_create_tetra_device(cdg_context *ctx, int order, int roots,
-                                      int nref, int n_levels, double perturb,
-                                      unsigned long long seed, cdg_hierarchy **out);
+                                      int nref, int n_levels, int neumann_mask,
+                                      double perturb, unsigned long long seed,
+                                      cdg_hierarchy **out);
 /* TFESpace numbering on the GPU (TFESpace3D::ConstructSpace,
  * src/FE/FESpace3D.C:186; TFESpace::compute_various_numbers,
  * src/FE/FESpace.C:1863-2099): inner DOFs, then non-Dirichlet boundary DOFs,

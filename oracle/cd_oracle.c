@@ -1485,6 +1485,59 @@ static void neumann_face(orc_problem *p, level_t *L, int cell, int j, int comp,
     }
 }
 
+/* Neumann boundary integral on a tetrahedron face (Assemble3D.C:552-655,
+ * triangular faces, face j opposite vertex j): g = eps * n.grad(u) with the
+ * outward unit normal n of the boundary component at x = X0 + s (X1-X0) +
+ * t (X2-X0), weight times |(X1-X0) x (X2-X0)|.  The rule on the reference
+ * triangle is Gauss-Legendre in (sigma, tau) with p+1 points each, collapsed
+ * by s = sigma (1 - tau), t = tau with the factor (1 - tau): exact to degree
+ * 2p, as the reference's triangle rule of degree 2p is. */
+static void neumann_face_tet(orc_problem *p, level_t *L, int cell, int j, int comp,
+                             double *rhs) {
+  const orc_config *c = &p->cfg;
+  static const int TET_FACE[4][3] = {{1, 2, 3}, {0, 2, 3}, {0, 1, 3}, {0, 1, 2}};
+  static const double nrm[6][3] = {{0, 0, -1}, {0, -1, 0}, {1, 0, 0},
+                                   {0, 1, 0},  {-1, 0, 0}, {0, 0, 1}};
+  const double *cv = L->verts + (size_t)cell * 4 * 3;
+  int nl = L->nloc, np = c->order + 1;
+  double lx[10], lw[10];
+  gauss_legendre(np, lx, lw);
+  double X[3][3], e1[3], e2[3];
+  for (int m = 0; m < 3; ++m)
+    for (int a = 0; a < 3; ++a) X[m][a] = cv[TET_FACE[j][m] * 3 + a];
+  for (int a = 0; a < 3; ++a) {
+    e1[a] = X[1][a] - X[0][a];
+    e2[a] = X[2][a] - X[0][a];
+  }
+  double cx = e1[1] * e2[2] - e1[2] * e2[1];
+  double cy = e1[2] * e2[0] - e1[0] * e2[2];
+  double cz = e1[0] * e2[1] - e1[1] * e2[0];
+  double area2 = sqrt(cx * cx + cy * cy + cz * cz);
+  affine_t A;
+  cell_affine_s(p->shape, 3, cv, &A);
+  for (int l1 = 0; l1 < np; ++l1)
+    for (int l2 = 0; l2 < np; ++l2) {
+      double sg = 0.5 * (lx[l1] + 1), tau = 0.5 * (lx[l2] + 1);
+      double fs = sg * (1 - tau), ft = tau;
+      double w = 0.25 * lw[l1] * lw[l2] * (1 - tau);
+      double x[3], u[6], xi[3];
+      for (int a = 0; a < 3; ++a) x[a] = X[0][a] + fs * e1[a] + ft * e2[a];
+      exact_sol(c, x, u);
+      double g = c->eps * (nrm[comp][0] * u[1] + nrm[comp][1] * u[2] + nrm[comp][2] * u[3]);
+      for (int a = 0; a < 3; ++a) {
+        double t = 0;
+        for (int r = 0; r < 3; ++r) t += A.Jinv[a][r] * (x[r] - A.x0[r]);
+        xi[a] = t;
+      }
+      double ref[MAXLOC][NDER];
+      tet_basis(c->order, xi, ref);
+      for (int k = 0; k < nl; ++k) {
+        int d = L->gdof[cell * nl + k];
+        if (d < L->nactive) rhs[d] += g * w * area2 * ref[k][0];
+      }
+    }
+}
+
 /* local mass matrix, TCDMass (CD_local_assembling_routines.C:156-167):
  * M_ij = int phi_i phi_j; with SUPG plus TCDMassSUPG (:261-321):
  * int delta (b . grad phi_i) phi_j */
@@ -1569,7 +1622,8 @@ static int assemble_into(orc_problem *p, int level, double *val, double *rhs,
   }
   if (p->shape == 2) {
     /* tetrahedra: every non-active DOF is a Dirichlet node; value = nodal
-     * functional of P1/P2 = point value */
+     * functional of P1/P2 = point value; Neumann integrals over the faces
+     * that lie on a Neumann component */
     for (int cell = 0; cell < L->ncells; ++cell) {
       const double *cv = L->verts + (size_t)cell * L->nv * dim;
       for (int k = 0; k < nl; ++k) {
@@ -1579,6 +1633,15 @@ static int assemble_into(orc_problem *p, int level, double *val, double *rhs,
         dof_position_s(2, 3, c->order, cv, k, x);
         exact_sol(c, x, u);
         rhs[d] = u[0];
+      }
+      if (!c->neumann_mask) continue;
+      for (int j = 0; j < 4; ++j) {
+        double ctr[3] = {0, 0, 0};
+        for (int m = 0; m < 4; ++m)
+          if (m != j)
+            for (int a = 0; a < 3; ++a) ctr[a] += cv[m * 3 + a] / 3.0;
+        int comp = boundary_comp(3, ctr);
+        if (comp >= 0 && bc_type(c, comp) != 0) neumann_face_tet(p, L, cell, j, comp, rhs);
       }
     }
     return 0;

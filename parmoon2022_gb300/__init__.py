@@ -139,10 +139,10 @@ def lib():
                                            ctypes.POINTER(SolveStats)],
             "cdg_problem_errors": [P, ctypes.POINTER(AssemblyParams), dp],
             "cdg_problem_errors_noalloc": [P, ctypes.POINTER(AssemblyParams), dp],
-            "cdg_hierarchy_create_tetra": [ctypes.c_int] * 4 + [ctypes.c_double,
+            "cdg_hierarchy_create_tetra": [ctypes.c_int] * 5 + [ctypes.c_double,
                                                                 ctypes.c_ulonglong, PP],
             "cdg_hierarchy_create_device": [P] + [ctypes.c_int] * 6 + [PP],
-            "cdg_hierarchy_create_tetra_device": [P] + [ctypes.c_int] * 4 + [
+            "cdg_hierarchy_create_tetra_device": [P] + [ctypes.c_int] * 5 + [
                 ctypes.c_double, ctypes.c_ulonglong, PP],
             "cdg_space_number_device": [P] + [ctypes.c_int] * 4 + [dp, ip, ip, ip],
             "cdg_vector_write_file": [ctypes.c_char_p, dp, ctypes.c_longlong],
@@ -277,10 +277,11 @@ class Hierarchy:
         h = ctypes.c_void_p()
         if tetra and ctx is not None:
             _chk(lib().cdg_hierarchy_create_tetra_device(ctx.c, order, roots, nref, n_levels,
-                                                         perturb, seed, ctypes.byref(h)))
+                                                         neumann_mask, perturb, seed,
+                                                         ctypes.byref(h)))
         elif tetra:
-            _chk(lib().cdg_hierarchy_create_tetra(order, roots, nref, n_levels, perturb, seed,
-                                                  ctypes.byref(h)))
+            _chk(lib().cdg_hierarchy_create_tetra(order, roots, nref, n_levels, neumann_mask,
+                                                  perturb, seed, ctypes.byref(h)))
         elif ctx is not None:
             _chk(lib().cdg_hierarchy_create_device(ctx.c, dim, order, roots, nref, n_levels,
                                                    neumann_mask, ctypes.byref(h)))

@@ -138,11 +138,11 @@ static int hierarchy_create(int dim, int order, int roots, int nref, int n_level
   return CDG_OK;
 }
 
-static int hierarchy_create_tetra(int order, int roots, int nref, int n_levels, double perturb,
-                                  unsigned long long seed, cdg_hierarchy** out,
+static int hierarchy_create_tetra(int order, int roots, int nref, int n_levels, int nmask,
+                                  double perturb, unsigned long long seed, cdg_hierarchy** out,
                                   cdg_context* ctx = nullptr) {
   if (!out || (order != 1 && order != 2) || roots < 1 || nref < 0 || n_levels < 1 ||
-      n_levels > nref + 1 || perturb < 0 || perturb >= 0.5) {
+      n_levels > nref + 1 || perturb < 0 || perturb >= 0.5 || nmask < 0 || nmask > 63) {
     set_error("bad tetrahedral hierarchy arguments");
     return CDG_ERR_ARG;
   }
@@ -154,7 +154,7 @@ static int hierarchy_create_tetra(int order, int roots, int nref, int n_levels, 
     h->mesh.push_back(make_kuhn_box(roots, nref - l));
     h->space.emplace_back();
     h->pattern.emplace_back();
-    const int rc = level_space_pattern(ctx, h->mesh.back(), order, 0, &h->space.back(),
+    const int rc = level_space_pattern(ctx, h->mesh.back(), order, nmask, &h->space.back(),
                                        &h->pattern.back());
     if (rc != CDG_OK) {
       delete h;
@@ -172,9 +172,9 @@ int cdg_hierarchy_create(int dim, int order, int roots, int nref, int n_levels, 
   API_GUARD(hierarchy_create(dim, order, roots, nref, n_levels, neumann_mask, out));
 }
 
-int cdg_hierarchy_create_tetra(int order, int roots, int nref, int n_levels, double perturb,
-                               unsigned long long seed, cdg_hierarchy** out) {
-  API_GUARD(hierarchy_create_tetra(order, roots, nref, n_levels, perturb, seed, out));
+int cdg_hierarchy_create_tetra(int order, int roots, int nref, int n_levels, int neumann_mask,
+                               double perturb, unsigned long long seed, cdg_hierarchy** out) {
+  API_GUARD(hierarchy_create_tetra(order, roots, nref, n_levels, neumann_mask, perturb, seed, out));
 }
 
 int cdg_hierarchy_create_device(cdg_context* ctx, int dim, int order, int roots, int nref,
@@ -184,10 +184,11 @@ int cdg_hierarchy_create_device(cdg_context* ctx, int dim, int order, int roots,
 }
 
 int cdg_hierarchy_create_tetra_device(cdg_context* ctx, int order, int roots, int nref,
-                                      int n_levels, double perturb, unsigned long long seed,
-                                      cdg_hierarchy** out) {
+                                      int n_levels, int neumann_mask, double perturb,
+                                      unsigned long long seed, cdg_hierarchy** out) {
   if (!ctx) { set_error("null context"); return CDG_ERR_ARG; }
-  API_GUARD(hierarchy_create_tetra(order, roots, nref, n_levels, perturb, seed, out, ctx));
+  API_GUARD(hierarchy_create_tetra(order, roots, nref, n_levels, neumann_mask, perturb, seed,
+                                   out, ctx));
 }
 
 static int space_number_device(cdg_context* ctx, int cell_type, int order, int neumann_mask,

@@ -674,6 +674,17 @@ __device__ void line_basis_d(int p, double t, double* v) {
   }
 }
 
+// value of P1/P2 basis function i at reference point xi of the tetrahedron
+// (BF_C_T_P2_3D node order: vertices and edge midpoints by barycentric pairs)
+__device__ double tet_basis_val_d(int p, const double* xi, int i) {
+  const double l[4] = {1.0 - xi[0] - xi[1] - xi[2], xi[0], xi[1], xi[2]};
+  if (p == 1) return l[i];
+  const int va[10] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3};
+  const int vb[10] = {0, 1, 1, 2, 2, 2, 3, 3, 3, 3};
+  const int a = va[i], b = vb[i];
+  return a == b ? l[a] * (2.0 * l[a] - 1.0) : 4.0 * l[a] * l[b];
+}
+
 __device__ int boundary_comp_d(int dim, const double* x) {
   const double t = 1e-12;
   if (dim == 2) {
@@ -700,7 +711,7 @@ __device__ int boundary_comp_d(int dim, const double* x) {
 //   phase 2  (cell, quadrature point): w |det J| f(x_q)
 //   phase 3  (cell, local DOF): F_i = sum_q fw_q (phi_i + delta b.grad phi_i),
 //            Dirichlet values at the nodes, Neumann edge integrals (2D) and
-//            face integrals (hexahedra)
+//            face integrals (hexahedra, tetrahedra)
 constexpr int kRhsTile = 32;
 constexpr int kRhsGeo = 18;   // x0[3], J[9], |det|, delta, b'[3]
 
@@ -898,6 +909,66 @@ k_rhs(AsmCoefs k, int ncells, int nactive, const double* __restrict__ verts,
             line_basis_d(k.order, xi[2], v2);
             G += gval * lw[l1] * lw[l2] * sqrt(nx * nx + ny * ny + nz * nz) *
                  (v0[ia] * v1[ib] * v2[ic]);
+          }
+        F += G;
+      }
+    }
+    // Neumann data on boundary faces of tetrahedra (Assemble3D.C:552-655,
+    // triangular faces): g = eps n.grad(u) at x = X0 + s (X1-X0) + t (X2-X0),
+    // weight times |(X1-X0) x (X2-X0)|; the rule on the reference triangle
+    // is the collapsed Gauss rule with p+1 points per direction (degree 2p:
+    // s = sigma (1 - tau), t = tau, weight (1 - tau) w_sigma w_tau / 4)
+    if (DIM == 3 && k.neumann_mask && k.shape == kTetra) {
+      const double* cv = verts + (size_t)cell * NV * DIM;
+      const int tf[4][3] = {{1, 2, 3}, {0, 2, 3}, {0, 1, 3}, {0, 1, 2}};
+      const double nrm[6][3] = {{0, 0, -1}, {0, -1, 0}, {1, 0, 0},
+                                {0, 1, 0},  {-1, 0, 0}, {0, 0, 1}};
+      Affine A;
+      cell_affine_s(k.shape, DIM, cv, A);
+      const int n1 = k.order + 1;
+      double lx[3], lw[3];
+      if (n1 == 2) {
+        lx[0] = -0.57735026918962576451; lx[1] = 0.57735026918962576451;
+        lw[0] = lw[1] = 1.0;
+      } else {
+        lx[0] = -0.77459666924148337704; lx[1] = 0.0; lx[2] = 0.77459666924148337704;
+        lw[0] = lw[2] = 5.0 / 9.0; lw[1] = 8.0 / 9.0;
+      }
+      for (int j = 0; j < 4; ++j) {
+        double X[3][3], ctr[3] = {0, 0, 0};
+        for (int m = 0; m < 3; ++m)
+          for (int a = 0; a < 3; ++a) {
+            X[m][a] = cv[tf[j][m] * 3 + a];
+            ctr[a] += X[m][a] / 3.0;
+          }
+        const int comp = boundary_comp_d(3, ctr);
+        if (comp < 0 || !((k.neumann_mask >> comp) & 1)) continue;
+        double e1[3], e2[3];
+        for (int a = 0; a < 3; ++a) {
+          e1[a] = X[1][a] - X[0][a];
+          e2[a] = X[2][a] - X[0][a];
+        }
+        const double cx = e1[1] * e2[2] - e1[2] * e2[1];
+        const double cy = e1[2] * e2[0] - e1[0] * e2[2];
+        const double cz = e1[0] * e2[1] - e1[1] * e2[0];
+        const double area2 = sqrt(cx * cx + cy * cy + cz * cz);
+        double G = 0.0;
+        for (int l1 = 0; l1 < n1; ++l1)
+          for (int l2 = 0; l2 < n1; ++l2) {
+            const double sg = 0.5 * (lx[l1] + 1), ta = 0.5 * (lx[l2] + 1);
+            const double fs = sg * (1 - ta), ft = ta;
+            const double w = 0.25 * lw[l1] * lw[l2] * (1 - ta);
+            double x[3];
+            for (int a = 0; a < 3; ++a) x[a] = X[0][a] + fs * e1[a] + ft * e2[a];
+            double u[6];
+            ex_exact(k, x, u);
+            const double gval =
+                k.eps * (nrm[comp][0] * u[1] + nrm[comp][1] * u[2] + nrm[comp][2] * u[3]);
+            double xi[3];
+            for (int a = 0; a < 3; ++a)
+              xi[a] = A.Ji[a][0] * (x[0] - A.x0[0]) + A.Ji[a][1] * (x[1] - A.x0[1]) +
+                      A.Ji[a][2] * (x[2] - A.x0[2]);
+            G += gval * w * area2 * tet_basis_val_d(k.order, xi, i);
           }
         F += G;
       }
@@ -1417,10 +1488,6 @@ static TermSet stiffness_set(const AsmCoefs& k) {
 
 static int check_coefs(const AsmCoefs& k) {
   if (k.nqp > 128) { set_error("quadrature rule too large"); return CDG_ERR_ARG; }
-  if (k.shape == kTetra && k.neumann_mask) {
-    set_error("Neumann boundaries on tetrahedral meshes are not supported");
-    return CDG_ERR_ARG;
-  }
   if (k.supg && k.linear_b) {
     set_error("SUPG with a convection field linear in x is not supported");
     return CDG_ERR_ARG;

@@ -25,6 +25,8 @@ CASES = {
     "q2_3d_neumann": (3, 2, 2, 2, 1, 33, False, 0.0),
     "p1_tet": (3, 1, 2, 2, 2, 0, True, 0.0),
     "p2_tet_perturbed": (3, 2, 2, 2, 1, 0, True, 0.2),
+    "p1_tet_neumann": (3, 1, 2, 2, 2, 47, True, 0.0),
+    "p2_tet_neumann_perturbed": (3, 2, 2, 2, 1, 36, True, 0.2),
 }
 
 
