@@ -400,6 +400,24 @@ __device__ double block_sum(double v) {
   return r;  // valid in thread 0
 }
 
+// sum of p[start], p[start + stride], ... below n in that order, read from L2
+// (the block partials other blocks published before their __threadfence and
+// the counter update): the loads of eight terms are issued together, the
+// additions stay in index order
+__device__ __forceinline__ double sum_partials(const double* p, int start, int stride, int n) {
+  double v = 0.0;
+  int q = start;
+  for (; q + 7 * stride < n; q += 8 * stride) {
+    double t[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) t[u] = __ldcg(p + q + u * stride);
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v += t[u];
+  }
+  for (; q < n; q += stride) v += __ldcg(p + q);
+  return v;
+}
+
 template <int NT>
 __device__ void finalize_sum(double blocksum, double* partials, unsigned* cnt, double* out,
                              bool take_sqrt) {
@@ -413,8 +431,7 @@ __device__ void finalize_sum(double blocksum, double* partials, unsigned* cnt, d
   __syncthreads();
   if (!last) return;
   __threadfence();
-  double v = 0.0;
-  for (int i = threadIdx.x; i < (int)gridDim.x; i += NT) v += ((volatile double*)partials)[i];
+  double v = sum_partials(partials, threadIdx.x, NT, (int)gridDim.x);
   v = block_sum<NT>(v);
   if (threadIdx.x == 0) {
     *out = take_sqrt ? sqrt(v) : v;
@@ -509,9 +526,7 @@ k_multidot(int n, const double* __restrict__ w, const double* __restrict__ V, in
   __threadfence();
   // one warp per inner product, lanes stride over the block partials
   for (int j = wp; j < cnt; j += NT / 32) {
-    double v = 0.0;
-    for (int q = l; q < (int)gridDim.x; q += 32)
-      v += ((volatile double*)partials)[(size_t)j * gridDim.x + q];
+    double v = sum_partials(partials + (size_t)j * gridDim.x, l, 32, (int)gridDim.x);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     if (l == 0) out[j] = v;
@@ -522,8 +537,16 @@ k_multidot(int n, const double* __restrict__ w, const double* __restrict__ V, in
 // Givens rotations of Hessenberg column i (Utilities_gmres.C:60-88): apply
 // the previous rotations, generate and apply rotation i, rotate s, write
 // |s_{i+1}| to *resid
+__device__ void givens_column_s(int i, double* col, double* cs, double* sn, double& si,
+                                double& si1, double* resid);
 __device__ void givens_column(int i, double* col, double* cs, double* sn, double* s,
                               double* resid) {
+  givens_column_s(i, col, cs, sn, s[i], s[i + 1], resid);
+}
+
+// the same with s[i], s[i+1] passed by reference
+__device__ void givens_column_s(int i, double* col, double* cs, double* sn, double& si,
+                                double& si1, double* resid) {
   for (int k = 0; k < i; ++k) {
     double dx = col[k], dy = col[k + 1];
     col[k] = cs[k] * dx + sn[k] * dy;
@@ -546,10 +569,10 @@ __device__ void givens_column(int i, double* col, double* cs, double* sn, double
   sn[i] = sg;
   col[i] = c * dx + sg * dy;
   col[i + 1] = -sg * dx + c * dy;
-  double a = s[i], b = s[i + 1];
-  s[i] = c * a + sg * b;
-  s[i + 1] = -sg * a + c * b;
-  *resid = fabs(s[i + 1]);
+  double a = si, b = si1;
+  si = c * a + sg * b;
+  si1 = -sg * a + c * b;
+  *resid = fabs(si1);
 }
 
 // w -= sum_k H(k,i) v_k (k in order), H(i+1,i) = ||w||, then the Givens
@@ -592,15 +615,31 @@ k_cgs_update(int n, double* __restrict__ w, const double* __restrict__ V, int i,
   __syncthreads();
   if (!last) return;
   __threadfence();
-  double v = 0.0;
-  for (int q = threadIdx.x; q < (int)gridDim.x; q += 256) v += ((volatile double*)partials)[q];
-  v = block_sum<256>(v);
+  // the rotation state in shared memory: the serial Givens chain then waits on
+  // no global load (H(k,i) = -h[k] exactly)
+  __shared__ double scs[128], ssn[128], ss[2];
+  for (int j = threadIdx.x; j < i; j += 256) {
+    scs[j] = cs[j];
+    ssn[j] = sn[j];
+  }
+  if (threadIdx.x < 2) ss[threadIdx.x] = gs[i + threadIdx.x];
+  for (int j = threadIdx.x; j <= i; j += 256) h[j] = -h[j];   // back to H(k,i)
+  double v = sum_partials(partials, threadIdx.x, 256, (int)gridDim.x);
+  v = block_sum<256>(v);   // synchronises the block
   if (threadIdx.x == 0) {
     const double nrm = sqrt(v);
-    hcol[i + 1] = nrm;
     *norm_out = nrm;   // v_{i+1} = w / H(i+1,i) uses the value before rotation
     *counter = 0u;
-    givens_column(i, hcol, cs, sn, gs, resid);
+    h[i + 1] = nrm;
+    givens_column_s(i, h, scs, ssn, ss[0], ss[1], resid);   // on the staged copies
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j <= i + 1; j += 256) hcol[j] = h[j];
+  if (threadIdx.x == 0) {
+    cs[i] = scs[i];
+    sn[i] = ssn[i];
+    gs[i] = ss[0];
+    gs[i + 1] = ss[1];
   }
 }
 
