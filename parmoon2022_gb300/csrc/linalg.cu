@@ -1449,12 +1449,42 @@ __global__ void k_init_s(int m, const double* beta, double* s) {
 }
 
 // Hessenberg back substitution (Utilities_gmres.C:90-108)
-__global__ void k_backsolve(int k, int m, const double* H, const double* s, double* y) {
-  for (int i = 0; i <= k; ++i) y[i] = s[i];
-  for (int i = k; i >= 0; --i) {
-    y[i] /= H[(size_t)i * (m + 1) + i];
-    for (int j = i - 1; j >= 0; --j) y[j] -= H[(size_t)i * (m + 1) + j] * y[i];
+// y = R^{-1} s for the rotated Hessenberg columns 0..k (Utilities_gmres.C
+// Update): one block, columns and s staged in shared memory by one coalesced
+// pass, then the column sweep -- y_i /= R(i,i), y_j -= R(j,i) y_i for j < i in
+// parallel -- in the serial order of every y_j
+constexpr int kBacksolveThreads = 128;
+__global__ void __launch_bounds__(kBacksolveThreads)
+k_backsolve(int k, int m, const double* __restrict__ H, const double* __restrict__ s,
+            double* __restrict__ y) {
+  extern __shared__ double bs[];
+  double* ys = bs;               // k + 1
+  double* hs = bs + (k + 1);     // column i at hs[i * (k + 1)], rows 0..i
+  const int n1 = k + 1;
+  for (int t = threadIdx.x; t < n1 * n1; t += blockDim.x) {
+    const int i = t / n1, j = t - i * n1;
+    if (j <= i) hs[t] = H[(size_t)i * (m + 1) + j];
   }
+  for (int j = threadIdx.x; j < n1; j += blockDim.x) ys[j] = s[j];
+  __syncthreads();
+  for (int i = k; i >= 0; --i) {
+    if (threadIdx.x == 0) ys[i] /= hs[i * n1 + i];
+    __syncthreads();
+    const double yi = ys[i];
+    for (int j = threadIdx.x; j < i; j += blockDim.x) ys[j] -= hs[i * n1 + j] * yi;
+    __syncthreads();
+  }
+  for (int j = threadIdx.x; j < n1; j += blockDim.x) y[j] = ys[j];
+}
+
+static int launch_backsolve(cdg_context* ctx, int k, int m, const double* H, const double* s,
+                            double* y) {
+  const size_t smem = (size_t)(k + 1) * (k + 2) * sizeof(double);
+  // restarts up to 120: at most 120 * 121 doubles (the attribute is per device)
+  CDG_CUDA(cudaFuncSetAttribute(k_backsolve, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(120 * 121 * sizeof(double))));
+  CDG_LAUNCH(ctx, k_backsolve, 1, kBacksolveThreads, smem, k, m, H, s, y);
+  return CDG_OK;
 }
 
 // x += sum_j y_j z_j (accumulated from zero in order j = 0..k, then added)
@@ -1951,14 +1981,14 @@ static int fgmres_graph(cdg_context* ctx, cdg_problem* p, const cdg_solver_param
       return CDG_ERR_DIVERGED;
     }
     if (flag == 1) {
-      CDG_LAUNCH(ctx, k_backsolve, 1, 1, 0, i, m, g.H, g.s, g.y);
+      CDG_TRY(launch_backsolve(ctx, i, m, g.H, g.s, g.y));
       CDG_LAUNCH(ctx, k_update, vg, 256, 0, n, i, g.Z, g.y, x);
       st->iterations = j;
       st->residual = resid;
       return CDG_OK;
     }
     // end of the restart cycle: update x, new residual, test
-    CDG_LAUNCH(ctx, k_backsolve, 1, 1, 0, m - 1, m, g.H, g.s, g.y);
+    CDG_TRY(launch_backsolve(ctx, m - 1, m, g.H, g.s, g.y));
     CDG_LAUNCH(ctx, k_update, vg, 256, 0, n, m - 1, g.Z, g.y, x);
     CDG_TRY(residual64(ctx, L, b, x, g.w));
     CDG_TRY(dot64(ctx, n, g.w, nullptr, beta_d, 0));
@@ -2061,14 +2091,14 @@ int fgmres(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s, cdg_sol
         return CDG_ERR_DIVERGED;
       }
       if (cv) {
-        CDG_LAUNCH(ctx, k_backsolve, 1, 1, 0, i, m, g.H, g.s, g.y);
+        CDG_TRY(launch_backsolve(ctx, i, m, g.H, g.s, g.y));
         CDG_LAUNCH(ctx, k_update, vg, 256, 0, n, i, g.Z, g.y, x);
         st->iterations = j;
         st->residual = resid;
         return CDG_OK;
       }
     }
-    CDG_LAUNCH(ctx, k_backsolve, 1, 1, 0, m - 1, m, g.H, g.s, g.y);
+    CDG_TRY(launch_backsolve(ctx, m - 1, m, g.H, g.s, g.y));
     CDG_LAUNCH(ctx, k_update, vg, 256, 0, n, m - 1, g.Z, g.y, x);
     CDG_TRY(residual64(ctx, L, b, x, g.w));
     CDG_TRY(dot64(ctx, n, g.w, nullptr, beta_d, 0));
