@@ -312,6 +312,7 @@ struct orc_problem {
   int asm_gen;      /* incremented by every orc_assemble */
   int tcd;          /* assembling for the time-dependent problem */
   double ttau;      /* THETA1 * CURRENTTIMESTEPLENGTH (Crank-Nicolson: tau/2) */
+  double tau, theta1; /* CURRENTTIMESTEPLENGTH and THETA1 (SDFEM types 9-11) */
   int tcd_step;     /* TimeDiscretization::current_step_ */
 };
 
@@ -1218,8 +1219,8 @@ int orc_set_solution(orc_problem *p, const double *v) {
 /* local assembly                                                            */
 /* ------------------------------------------------------------------------ */
 /* Compute_SDFEM_delta (ConvDiff.C:269-495) for the steady types */
-static double sdfem_delta(const orc_config *c, double hK, double eps,
-                          const double *b, double react, double linfb) {
+static double sdfem_delta(const orc_config *c, double tau, double theta1, double hK,
+                          double eps, const double *b, double react, double linfb) {
   int d = c->dim;
   double delta0 = c->delta0, delta1 = c->delta1, delta = 0, alpha;
   if (fabs(eps) < 1e-20) eps = 1e-20;
@@ -1265,13 +1266,56 @@ static double sdfem_delta(const orc_config *c, double hK, double eps,
     delta *= delta0;
     if (delta < 0) delta = 0;
     break;
+  case 6: {
+    /* Franca/Valentin (2000) */
+    double r = reaction < 1e-20 ? 1e20 : reaction;
+    double alpha2;
+    alpha = 6 * eps / (h * h * r);
+    if (alpha <= 1) alpha = 1;
+    alpha2 = h * nb / (3 * eps);
+    if (alpha2 <= 1) alpha2 = 1;
+    delta = 1 / (r * h * h * alpha + 6 * eps * alpha2);
+    delta *= delta0 * h * h;
+    break;
+  }
   case 7:
     delta = delta0 * h * h / (4 * eps + 2 * h * nb + h * h * reaction);
     break;
+  /* the time-dependent estimates of John and Novo (tau = CURRENTTIMESTEPLENGTH,
+   * theta1 = THETA1) */
+  case 9:
+    delta = delta0 * tau;
+    break;
+  case 10:
+    eps /= (theta1 * tau);
+    delta = eps <= h ? delta0 * h : delta0 * h * h / eps;
+    break;
+  case 11:
+    nb /= tau;
+    delta = nb > 0 ? delta0 * h * sqrt(tau) / nb : 0;
+    break;
+  case 12: {
+    double c_inv = delta0;
+    double m = sqrt(3.0) * h / (8 * eps * c_inv);
+    m = m < 0.25 ? m : 0.25;
+    m *= h / (2. * sqrt(3.0) * c_inv);
+    delta = 100 * (m < 1. ? m : 1.);
+    break;
+  }
   default:
     delta = 0;
   }
   return delta;
+}
+
+/* Compute_SDFEM_delta throws for the types it does not have (3, above 12);
+ * 9-11 take the time step: time-dependent problem only */
+static int check_sdfem(const orc_config *c, int tcd) {
+  if (!c->supg) return 0;
+  int ty = c->sdfem_type;
+  if (ty < 0 || ty == 3 || ty > 12) FAIL("SDFEM_TYPE not implemented");
+  if (!tcd && ty >= 9 && ty <= 11) FAIL("SDFEM_TYPE depends on the time step");
+  return 0;
 }
 
 /* the stabilisation parameter of TCDStiffSUPG, TCDMassSUPG and TCDRhsSUPG
@@ -1290,11 +1334,12 @@ static double tcd_delta(const orc_problem *p, double hK, double eps, const doubl
     double bs[3] = {tt * b[0], tt * b[1], 0};
     double bb = fabs(bs[0]) > fabs(bs[1]) ? fabs(bs[0]) : fabs(bs[1]);
     if (ty != 2 && ty != 12)
-      delta = sdfem_delta(c, hK, tt * eps, bs, ty == 8 ? tt * react : 1.0 + tt * react, bb);
+      delta = sdfem_delta(c, p->tau, p->theta1, hK, tt * eps, bs,
+                          ty == 8 ? tt * react : 1.0 + tt * react, bb);
     else
-      delta = sdfem_delta(c, hK, eps, b, react, bb);
+      delta = sdfem_delta(c, p->tau, p->theta1, hK, eps, b, react, bb);
   } else {
-    delta = sdfem_delta(c, hK, eps, b, react, linfb);
+    delta = sdfem_delta(c, p->tau, p->theta1, hK, eps, b, react, linfb);
   }
   if (ty != 2 && ty != 9 && ty != 10 && ty != 11 && ty != 12) delta *= tt;
   return delta;
@@ -1367,7 +1412,7 @@ int orc_local_system(orc_problem *p, int level, int cell, double *Aloc,
       /* BilinearAssemble_SD<d> (ConvDiff.C:1886-1999); the time-dependent
        * TCDStiffSUPG / TCDRhsSUPG have the same form with their own delta */
       double delta = p->tcd ? tcd_delta(p, hK, eps, b, react, co[dim + 3])
-                            : sdfem_delta(c, hK, eps, b, react, co[dim + 3]);
+                            : sdfem_delta(c, 0.0, 0.0, hK, eps, b, react, co[dim + 3]);
       for (int i = 0; i < nl; ++i) {
         double bgradv = 0;
         for (int r = 0; r < dim; ++r) bgradv += b[r] * g[i][r];
@@ -1692,6 +1737,7 @@ static int assemble_level(orc_problem *p, int level) {
 }
 
 int orc_assemble(orc_problem *p) {
+  if (check_sdfem(&p->cfg, 0)) return -1;
   p->asm_gen++;
   p->tcd = 0;
   for (int k = 0; k < p->nlev; ++k)
@@ -2204,7 +2250,7 @@ int orc_errors(const orc_problem *p, double *errors) {
       double react = co[dim + 1];
       double bn = fmax(fabs(bb[0]), fabs(bb[1]));
       if (dim == 3) bn = fmax(bn, fabs(bb[2]));
-      double delta = sdfem_delta(c, hK, nu, bb, react, bn);
+      double delta = sdfem_delta(c, 0.0, 0.0, hK, nu, bb, react, bn);
       double w = p->qr.w[q] * fabs(A.det);
       double e0 = der[0] - u[0];
       e[0] += w * e0 * e0;
@@ -2259,13 +2305,15 @@ int orc_tcd_initialize(orc_problem *p) {
   if (p->cfg.time_disc < 0 || p->cfg.time_disc > 2) FAIL("time discretization not supported");
   if (p->cfg.supg) {
     if (!(p->cfg.time_step > 0)) FAIL("SUPG for the time-dependent problem needs the time step");
-    if (p->cfg.sdfem_type >= 9 && p->cfg.sdfem_type <= 12) FAIL("SDFEM_TYPE not supported");
   }
   double theta1;
   step_scheme(&p->cfg, 0, &theta1);
   p->tcd = 1;
   p->tcd_step = 0;
+  if (check_sdfem(&p->cfg, 1)) return -1;
   p->ttau = theta1 * p->cfg.time_step;
+  p->tau = p->cfg.time_step;
+  p->theta1 = theta1;
   for (int k = 0; k < p->nlev; ++k) {
     level_t *L = &p->lev[k];
     ensure_tcd(L);
@@ -2307,6 +2355,8 @@ int orc_tcd_step(orc_problem *p, double t_new, double tau, const orc_solver_conf
   p->cfg.t = t_new;
   p->tcd = 1;
   p->ttau = theta1 * tau;
+  p->tau = tau;
+  p->theta1 = theta1;
   /* with SUPG the mass matrix is reassembled too (TimeConvectionDiffusion.C
    * assemble: TCDStiffMassRhs, assemble_both) */
   for (int k = 0; k < p->nlev; ++k) {

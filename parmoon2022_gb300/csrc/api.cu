@@ -609,7 +609,7 @@ int cdg_problem_tcd_initialize(cdg_problem* p, const cdg_assembly_params* a) {
   p->tcd_step = 0;
   const TimeScheme ts = time_scheme(*a, 0);
   for (auto& L : p->lev) {
-    CDG_TRY(tcd_assemble_level(p->ctx, p, L, *a, true, ts.theta1 * a->time_step));
+    CDG_TRY(tcd_assemble_level(p->ctx, p, L, *a, true, ts.theta1, a->time_step));
     // old_rhs = rhs
     CDG_CUDA(cudaMemcpyAsync(L.tcd_fold, L.tcd_f, (size_t)L.ndof * sizeof(double),
                              cudaMemcpyDeviceToDevice, p->ctx->stream));
@@ -636,7 +636,7 @@ int cdg_problem_tcd_step(cdg_problem* p, const cdg_assembly_params* a, double ta
   // reassemble stiffness and rhs on every level (the Galerkin mass is time
   // independent; the SUPG mass is reassembled with theta1 * tau)
   for (auto& L : p->lev)
-    CDG_TRY(tcd_assemble_level(p->ctx, p, L, *a, false, ts.theta1 * tau));
+    CDG_TRY(tcd_assemble_level(p->ctx, p, L, *a, false, ts.theta1, tau));
   CDG_TRY(tcd_rhs(p->ctx, F, ts, tau));
   // solution.copy_nonactive(rhs): Dirichlet data at the new time
   const int nd = F.ndof - F.nactive;

@@ -45,6 +45,7 @@ struct AsmCoefs {
   double eps, b[3], bg[9], c, freq, delta0, delta1, t, ic[4];
   int tcd;        // time-dependent assembly (SUPG parameter of the TCD routines)
   double ttau;    // theta1 * time step (Crank-Nicolson: theta1 = 1/2)
+  double tau, theta1;   // CURRENTTIMESTEPLENGTH and THETA1 (SDFEM types 9-11)
 };
 
 static AsmCoefs make_coefs(const cdg_assembly_params& a, int shape, int order) {
@@ -57,6 +58,8 @@ static AsmCoefs make_coefs(const cdg_assembly_params& a, int shape, int order) {
   k.supg = a.supg;
   k.tcd = 0;
   k.ttau = 0.0;
+  k.tau = 0.0;
+  k.theta1 = 0.0;
   k.sdfem_type = a.sdfem_type;
   k.cell_measure = a.cell_measure;
   k.poly_degree = a.poly_degree > 0 ? a.poly_degree : order;
@@ -372,11 +375,40 @@ __device__ double sdfem_delta(const AsmCoefs& k, double h, double eps, const dou
       delta *= k.delta0;
       if (delta < 0) delta = 0;
       break;
+    case 6: {
+      // Franca/Valentin (2000)
+      double r = reaction < 1e-20 ? 1e20 : reaction;
+      alpha = 6 * eps / (h * h * r);
+      if (alpha <= 1) alpha = 1;
+      double alpha2 = h * nb / (3 * eps);
+      if (alpha2 <= 1) alpha2 = 1;
+      delta = 1 / (r * h * h * alpha + 6 * eps * alpha2);
+      delta *= k.delta0 * h * h;
+      break;
+    }
     case 7:
       delta = k.delta0 * h * h / (4 * eps + 2 * h * nb + h * h * reaction);
       break;
+    // the time-dependent estimates of John and Novo
+    case 9:
+      delta = k.delta0 * k.tau;
+      break;
+    case 10:
+      eps /= (k.theta1 * k.tau);   // the unscaled diffusion of the 2D routines
+      delta = eps <= h ? k.delta0 * h : k.delta0 * h * h / eps;
+      break;
+    case 11:
+      nb /= k.tau;
+      delta = nb > 0 ? k.delta0 * h * sqrt(k.tau) / nb : 0.0;
+      break;
+    case 12: {
+      const double c_inv = k.delta0;
+      delta = 100 * fmin(h / (2. * sqrt(3.0) * c_inv) *
+                             fmin(0.25, sqrt(3.0) * h / (8 * eps * c_inv)), 1.);
+      break;
+    }
     default:
-      delta = 0;
+      delta = 0;   // rejected before any launch
   }
   return delta;
 }
@@ -1488,6 +1520,19 @@ static TermSet stiffness_set(const AsmCoefs& k) {
 
 static int check_coefs(const AsmCoefs& k) {
   if (k.nqp > 128) { set_error("quadrature rule too large"); return CDG_ERR_ARG; }
+  if (k.supg) {
+    // Compute_SDFEM_delta (ConvDiff.C:290-487): types 0-2 and 4-12; 3 and the
+    // rest throw; 100 (a delta field of the finest level) is not taken here
+    const int ty = k.sdfem_type;
+    if (ty < 0 || ty == 3 || ty > 12) {
+      set_error("SDFEM_TYPE %d not implemented", ty);
+      return CDG_ERR_ARG;
+    }
+    if (!k.tcd && ty >= 9 && ty <= 11) {
+      set_error("SDFEM_TYPE %d depends on the time step: time-dependent problem only", ty);
+      return CDG_ERR_ARG;
+    }
+  }
   if (k.supg && k.linear_b) {
     set_error("SUPG with a convection field linear in x is not supported");
     return CDG_ERR_ARG;
@@ -1650,19 +1695,19 @@ int tcd_interpolate(cdg_context* ctx, cdg_problem* p, const cdg_assembly_params&
 // parameter depends on theta1 * tau, and the mass matrix carries a SUPG term,
 // so it is reassembled with every step (TimeConvectionDiffusion.C:315-346).
 int tcd_assemble_level(cdg_context* ctx, cdg_problem* p, DevLevel& L,
-                       const cdg_assembly_params& a, bool with_mass, double theta_tau) {
+                       const cdg_assembly_params& a, bool with_mass, double theta1,
+                       double tau) {
   CDG_TRY(ensure_tables(ctx, p));
   CDG_TRY(ensure_tcd(L));
   AsmCoefs k = make_coefs(a, L.shape, L.order);
-  CDG_TRY(check_coefs(k));
   k.tcd = 1;
-  k.ttau = theta_tau;
-  if (k.supg) {
-    if (!(theta_tau > 0)) { set_error("SUPG for the time-dependent problem needs the time step"); return CDG_ERR_ARG; }
-    if (k.sdfem_type >= 9 && k.sdfem_type <= 12) {
-      set_error("SDFEM_TYPE %d (time-step dependent) is not supported", k.sdfem_type);
-      return CDG_ERR_ARG;
-    }
+  k.theta1 = theta1;
+  k.tau = tau;
+  k.ttau = theta1 * tau;
+  CDG_TRY(check_coefs(k));
+  if (k.supg && !(k.ttau > 0)) {
+    set_error("SUPG for the time-dependent problem needs the time step");
+    return CDG_ERR_ARG;
   }
   cudaStream_t st = ctx->stream;
   CDG_CUDA(cudaMemsetAsync(L.tcd_A, 0, (size_t)L.nnz * sizeof(double), st));

@@ -242,7 +242,8 @@ int level_errors(cdg_context* ctx, cdg_problem* p, DevLevel& L,
 // time-dependent CD (TimeConvectionDiffusion with the TimeDiscretization schemes)
 int tcd_interpolate(cdg_context* ctx, cdg_problem* p, const cdg_assembly_params& a);
 int tcd_assemble_level(cdg_context* ctx, cdg_problem* p, DevLevel& L,
-                       const cdg_assembly_params& a, bool with_mass, double theta_tau);
+                       const cdg_assembly_params& a, bool with_mass, double theta1,
+                       double tau);
 // The scheme one step takes (TimeDiscretization::set_time_disc_parameters,
 // src/TimeDiscRoutines/TimeDiscretizations.C:422-475): step is the index of
 // the step (TimeDiscretization::current_step_ after the increment; 0 for the
