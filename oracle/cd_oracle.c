@@ -1218,13 +1218,81 @@ int orc_set_solution(orc_problem *p, const double *v) {
 /* ------------------------------------------------------------------------ */
 /* local assembly                                                            */
 /* ------------------------------------------------------------------------ */
-/* Compute_SDFEM_delta (ConvDiff.C:269-495) for the steady types */
-static double sdfem_delta(const orc_config *c, double tau, double theta1, double hK,
-                          double eps, const double *b, double react, double linfb) {
+/* Mesh_size_in_convection_direction (ConvDiff.C:26-254), CELL_MEASURE 4:
+ * the vertex functions of the cell fitted in physical coordinates --
+ * (1,x,y,xy) on quadrilaterals, (1,x,y,z) on tetrahedra,
+ * (1,x,y,z,xy,xz,yz,xyz) on hexahedra -- and h = 2|b| / sum_i |b . grad
+ * phi_i(barycentre)|, hK when the sum vanishes.  The inverse of the vertex
+ * system by Gauss-Jordan elimination with partial pivoting. */
+static double conv_hK(int shape, int dim, const double *cv, const double *b, double hK) {
+  int n = shape == 1 ? 8 : 4;   /* shape: 0 quadrilateral, 1 hexahedron, 2 tetrahedron */
+  double a[8][8], x[8][8], sc[3] = {0, 0, 0}, den = 0, nb = 0;
+  for (int i = 0; i < n; ++i) {
+    const double *v = cv + i * dim;
+    double px = v[0], py = v[1], pz = dim == 3 ? v[2] : 0.0;
+    double r[8] = {1, px, py, shape == 0 ? px * py : pz, px * py, px * pz, py * pz, px * py * pz};
+    sc[0] += px / n;
+    sc[1] += py / n;
+    sc[2] += pz / n;
+    for (int j = 0; j < n; ++j) {
+      a[i][j] = r[j];
+      x[i][j] = i == j;
+    }
+  }
+  for (int col = 0; col < n; ++col) {
+    int pr = col;
+    for (int r = col + 1; r < n; ++r)
+      if (fabs(a[r][col]) > fabs(a[pr][col])) pr = r;
+    if (a[pr][col] == 0.0) return hK;
+    for (int j = 0; j < n; ++j) {
+      double t = a[col][j]; a[col][j] = a[pr][j]; a[pr][j] = t;
+      t = x[col][j]; x[col][j] = x[pr][j]; x[pr][j] = t;
+    }
+    double ip = 1.0 / a[col][col];
+    for (int j = 0; j < n; ++j) {
+      a[col][j] *= ip;
+      x[col][j] *= ip;
+    }
+    for (int r = 0; r < n; ++r) {
+      if (r == col || a[r][col] == 0.0) continue;
+      double f = a[r][col];
+      for (int j = 0; j < n; ++j) {
+        a[r][j] -= f * a[col][j];
+        x[r][j] -= f * x[col][j];
+      }
+    }
+  }
+  for (int a2 = 0; a2 < dim; ++a2) nb += b[a2] * b[a2];
+  nb = sqrt(nb);
+  for (int i = 0; i < n; ++i) {
+    double g[3] = {0, 0, 0}, v = 0;
+    if (shape == 0) {
+      g[0] = x[1][i] + x[3][i] * sc[1];
+      g[1] = x[2][i] + x[3][i] * sc[0];
+    } else if (shape == 2) {
+      g[0] = x[1][i];
+      g[1] = x[2][i];
+      g[2] = x[3][i];
+    } else {
+      g[0] = x[1][i] + x[4][i] * sc[1] + x[5][i] * sc[2] + x[7][i] * sc[1] * sc[2];
+      g[1] = x[2][i] + x[4][i] * sc[0] + x[6][i] * sc[2] + x[7][i] * sc[0] * sc[2];
+      g[2] = x[3][i] + x[5][i] * sc[0] + x[6][i] * sc[1] + x[7][i] * sc[0] * sc[1];
+    }
+    for (int a2 = 0; a2 < dim; ++a2) v += b[a2] * g[a2];
+    den += fabs(v);
+  }
+  return den < 1e-10 ? hK : 2 * nb / den;
+}
+
+/* Compute_SDFEM_delta (ConvDiff.C:269-495); hK is the cell's Get_hK,
+ * replaced by the size in convection direction for CELL_MEASURE 4 */
+static double sdfem_delta(const orc_config *c, int shape, const double *cv, double tau,
+                          double theta1, double hK, double eps, const double *b, double react,
+                          double linfb) {
   int d = c->dim;
   double delta0 = c->delta0, delta1 = c->delta1, delta = 0, alpha;
   if (fabs(eps) < 1e-20) eps = 1e-20;
-  double h = hK;
+  double h = c->cell_measure == 4 ? conv_hK(shape, d, cv, b, hK) : hK;
   double nb = b[0] * b[0] + b[1] * b[1];
   if (d == 3) nb += b[2] * b[2];
   nb = sqrt(nb);
@@ -1324,8 +1392,8 @@ static int check_sdfem(const orc_config *c, int tcd) {
  * (reaction 1 + theta1 tau c, type 8: theta1 tau c); the L_inf norm of b is
  * always the scaled one in 2D.  Then delta *= theta1 * tau except for the
  * types 2, 9, 10, 11, 12. */
-static double tcd_delta(const orc_problem *p, double hK, double eps, const double *b,
-                        double react, double linfb) {
+static double tcd_delta(const orc_problem *p, const double *cv, double hK, double eps,
+                        const double *b, double react, double linfb) {
   const orc_config *c = &p->cfg;
   const double tt = p->ttau;
   const int ty = c->sdfem_type;
@@ -1334,12 +1402,12 @@ static double tcd_delta(const orc_problem *p, double hK, double eps, const doubl
     double bs[3] = {tt * b[0], tt * b[1], 0};
     double bb = fabs(bs[0]) > fabs(bs[1]) ? fabs(bs[0]) : fabs(bs[1]);
     if (ty != 2 && ty != 12)
-      delta = sdfem_delta(c, p->tau, p->theta1, hK, tt * eps, bs,
+      delta = sdfem_delta(c, p->shape, cv, p->tau, p->theta1, hK, tt * eps, bs,
                           ty == 8 ? tt * react : 1.0 + tt * react, bb);
     else
-      delta = sdfem_delta(c, p->tau, p->theta1, hK, eps, b, react, bb);
+      delta = sdfem_delta(c, p->shape, cv, p->tau, p->theta1, hK, eps, b, react, bb);
   } else {
-    delta = sdfem_delta(c, p->tau, p->theta1, hK, eps, b, react, linfb);
+    delta = sdfem_delta(c, p->shape, cv, p->tau, p->theta1, hK, eps, b, react, linfb);
   }
   if (ty != 2 && ty != 9 && ty != 10 && ty != 11 && ty != 12) delta *= tt;
   return delta;
@@ -1411,8 +1479,9 @@ int orc_local_system(orc_problem *p, int level, int cell, double *Aloc,
     if (c->supg) {
       /* BilinearAssemble_SD<d> (ConvDiff.C:1886-1999); the time-dependent
        * TCDStiffSUPG / TCDRhsSUPG have the same form with their own delta */
-      double delta = p->tcd ? tcd_delta(p, hK, eps, b, react, co[dim + 3])
-                            : sdfem_delta(c, 0.0, 0.0, hK, eps, b, react, co[dim + 3]);
+      double delta = p->tcd ? tcd_delta(p, cv, hK, eps, b, react, co[dim + 3])
+                            : sdfem_delta(c, p->shape, cv, 0.0, 0.0, hK, eps, b, react,
+                                          co[dim + 3]);
       for (int i = 0; i < nl; ++i) {
         double bgradv = 0;
         for (int r = 0; r < dim; ++r) bgradv += b[r] * g[i][r];
@@ -1606,7 +1675,7 @@ static void local_mass(orc_problem *p, level_t *L, int cell, double *Mloc) {
     affine_map(dim, &A, p->qr.xi[q], x);
     coeffs_at(c, x, co);
     double b[3] = {co[1], co[2], dim == 3 ? co[3] : 0};
-    double delta = tcd_delta(p, hK, co[0], b, co[dim + 1], co[dim + 3]);
+    double delta = tcd_delta(p, cv, hK, co[0], b, co[dim + 1], co[dim + 3]);
     for (int i = 0; i < nl; ++i) {
       double bgradv = 0;
       for (int r = 0; r < dim; ++r) {
@@ -2250,7 +2319,7 @@ int orc_errors(const orc_problem *p, double *errors) {
       double react = co[dim + 1];
       double bn = fmax(fabs(bb[0]), fabs(bb[1]));
       if (dim == 3) bn = fmax(bn, fabs(bb[2]));
-      double delta = sdfem_delta(c, 0.0, 0.0, hK, nu, bb, react, bn);
+      double delta = sdfem_delta(c, p->shape, cv, 0.0, 0.0, hK, nu, bb, react, bn);
       double w = p->qr.w[q] * fabs(A.det);
       double e0 = der[0] - u[0];
       e[0] += w * e0 * e0;

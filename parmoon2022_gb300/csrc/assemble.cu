@@ -330,10 +330,102 @@ __device__ double cell_hK(int dim, const double* __restrict__ cv, int measure, d
   return cell_hK_s(dim == 2 ? kQuad : kHexa, dim, cv, measure, det);
 }
 
-// Compute_SDFEM_delta (ConvDiff.C:269-495), steady types
-__device__ double sdfem_delta(const AsmCoefs& k, double h, double eps, const double* b,
-                              double react, double linfb) {
+// Mesh_size_in_convection_direction (ConvDiff.C:26-254), CELL_MEASURE 4: the
+// vertex functions of the cell fitted in physical coordinates -- (1,x,y,xy)
+// on quadrilaterals, (1,x,y,z) on tetrahedra, (1,x,y,z,xy,xz,yz,xyz) on
+// hexahedra -- and h = 2|b| / sum_i |b.grad phi_i(barycentre)|, hK when the
+// sum vanishes.  The inverse of the vertex system by Gauss-Jordan with
+// partial pivoting; column i holds the coefficients of phi_i.
+__device__ __noinline__ double conv_hK(int shape, int dim, const double* __restrict__ cv, const double* b,
+                          double hK) {
+  const int n = shape == kHexa ? 8 : 4;
+  double a[8][8], x[8][8], sc[3] = {0, 0, 0};
+#pragma unroll 1
+  for (int i = 0; i < n; ++i) {
+    const double* v = cv + i * dim;
+    const double px = v[0], py = v[1], pz = dim == 3 ? v[2] : 0.0;
+    sc[0] += px / n;
+    sc[1] += py / n;
+    sc[2] += pz / n;
+    double r[8] = {1, px, py, 0, 0, 0, 0, 0};
+    if (shape == kQuad) r[3] = px * py;
+    else r[3] = pz;
+    if (shape == kHexa) {
+      r[4] = px * py;
+      r[5] = px * pz;
+      r[6] = py * pz;
+      r[7] = px * py * pz;
+    }
+#pragma unroll 1
+    for (int j = 0; j < n; ++j) {
+      a[i][j] = r[j];
+      x[i][j] = i == j ? 1.0 : 0.0;
+    }
+  }
+#pragma unroll 1
+  for (int c = 0; c < n; ++c) {
+    int pr = c;
+#pragma unroll 1
+    for (int r = c + 1; r < n; ++r)
+      if (fabs(a[r][c]) > fabs(a[pr][c])) pr = r;
+    if (a[pr][c] == 0.0) return hK;
+#pragma unroll 1
+    for (int j = 0; j < n; ++j) {
+      double t = a[c][j]; a[c][j] = a[pr][j]; a[pr][j] = t;
+      t = x[c][j]; x[c][j] = x[pr][j]; x[pr][j] = t;
+    }
+    const double ip = 1.0 / a[c][c];
+#pragma unroll 1
+    for (int j = 0; j < n; ++j) {
+      a[c][j] *= ip;
+      x[c][j] *= ip;
+    }
+#pragma unroll 1
+    for (int r = 0; r < n; ++r) {
+      if (r == c) continue;
+      const double f = a[r][c];
+      if (f == 0.0) continue;
+#pragma unroll 1
+      for (int j = 0; j < n; ++j) {
+        a[r][j] -= f * a[c][j];
+        x[r][j] -= f * x[c][j];
+      }
+    }
+  }
+  double den = 0.0, nb = 0.0;
+#pragma unroll 1
+  for (int a2 = 0; a2 < dim; ++a2) nb += b[a2] * b[a2];
+  nb = sqrt(nb);
+#pragma unroll 1
+  for (int i = 0; i < n; ++i) {
+    double g[3];
+    if (shape == kQuad) {
+      g[0] = x[1][i] + x[3][i] * sc[1];
+      g[1] = x[2][i] + x[3][i] * sc[0];
+      g[2] = 0.0;
+    } else if (shape == kTetra) {
+      g[0] = x[1][i];
+      g[1] = x[2][i];
+      g[2] = x[3][i];
+    } else {
+      g[0] = x[1][i] + x[4][i] * sc[1] + x[5][i] * sc[2] + x[7][i] * sc[1] * sc[2];
+      g[1] = x[2][i] + x[4][i] * sc[0] + x[6][i] * sc[2] + x[7][i] * sc[0] * sc[2];
+      g[2] = x[3][i] + x[5][i] * sc[0] + x[6][i] * sc[1] + x[7][i] * sc[0] * sc[1];
+    }
+    double v = 0.0;
+#pragma unroll 1
+    for (int a2 = 0; a2 < dim; ++a2) v += b[a2] * g[a2];
+    den += fabs(v);
+  }
+  return den < 1e-10 ? hK : 2 * nb / den;
+}
+
+// Compute_SDFEM_delta (ConvDiff.C:269-495); h is the cell's Get_hK, replaced
+// by the size in convection direction for CELL_MEASURE 4
+__device__ double sdfem_delta(const AsmCoefs& k, const double* cv, double h, double eps,
+                              const double* b, double react, double linfb) {
   double delta = 0, alpha;
+  if (k.cell_measure == 4) h = conv_hK(k.shape, k.dim, cv, b, h);
   if (fabs(eps) < 1e-20) eps = 1e-20;
   double nb = b[0] * b[0] + b[1] * b[1];
   if (k.dim == 3) nb += b[2] * b[2];
@@ -418,7 +510,7 @@ __device__ double cell_delta(const AsmCoefs& k, const double* cv, const Affine& 
   double h = cell_hK_s(k.shape, k.dim, cv, k.cell_measure, A.det);
   double linfb = fmax(fabs(k.b[0]), fabs(k.b[1]));
   if (k.dim == 3) linfb = fmax(linfb, fabs(k.b[2]));
-  if (!k.tcd) return sdfem_delta(k, h, k.eps, k.b, k.c, linfb);
+  if (!k.tcd) return sdfem_delta(k, cv, h, k.eps, k.b, k.c, linfb);
   // TCDStiffSUPG / TCDMassSUPG / TCDRhsSUPG (CD_local_assembling_routines.C:
   // 184-387): in 2D the coefficients are scaled by theta1*tau first (except
   // SDFEM_TYPE 2 and 12, which keep them but take the scaled L_inf norm);
@@ -429,12 +521,12 @@ __device__ double cell_delta(const AsmCoefs& k, const double* cv, const Affine& 
     const double bs[3] = {k.ttau * k.b[0], k.ttau * k.b[1], 0.0};
     const double bb = fmax(fabs(bs[0]), fabs(bs[1]));
     if (ty != 2 && ty != 12)
-      delta = sdfem_delta(k, h, k.ttau * k.eps, bs,
+      delta = sdfem_delta(k, cv, h, k.ttau * k.eps, bs,
                           ty == 8 ? k.ttau * k.c : 1.0 + k.ttau * k.c, bb);
     else
-      delta = sdfem_delta(k, h, k.eps, k.b, k.c, bb);
+      delta = sdfem_delta(k, cv, h, k.eps, k.b, k.c, bb);
   } else {
-    delta = sdfem_delta(k, h, k.eps, k.b, k.c, linfb);
+    delta = sdfem_delta(k, cv, h, k.eps, k.b, k.c, linfb);
   }
   if (ty != 2 && ty != 9 && ty != 10 && ty != 11 && ty != 12) delta *= k.ttau;
   return delta;
@@ -1076,7 +1168,7 @@ k_errors(AsmCoefs k, int ncells, const double* __restrict__ verts, const int* __
       b_at(k, x, bx);
       double linfb = fmax(fabs(bx[0]), fabs(bx[1]));
       if (DIM == 3) linfb = fmax(linfb, fabs(bx[2]));
-      const double delta = sdfem_delta(k, hK, k.eps, bx, k.c, linfb);
+      const double delta = sdfem_delta(k, cv, hK, k.eps, bx, k.c, linfb);
       double w = tb.w[q] * adet;
       double e0 = uh - u[0];
       emax = fmax(emax, fabs(e0));
@@ -1829,7 +1921,7 @@ k_errors_noalloc(AsmCoefs k, LineRule rule, int ncells, const double* __restrict
     const double fv = lane < nl ? sol[gdof[(size_t)cell * nl + lane]] : 0.0;
     double linfb = fmax(fabs(k.b[0]), fabs(k.b[1]));
     if (DIM == 3) linfb = fmax(linfb, fabs(k.b[2]));
-    const double delta = sdfem_delta(k, hK, k.eps, k.b, k.c, linfb);
+    const double delta = sdfem_delta(k, cv, hK, k.eps, k.b, k.c, linfb);
     const int ki[3] = {lane % n1, (lane / n1) % n1, lane / (n1 * n1)};
     const int nq = DIM == 2 ? rule.n * rule.n : rule.n * rule.n * rule.n;
     for (int q = 0; q < nq; ++q) {

@@ -1,6 +1,7 @@
 """The SUPG parameter types of Compute_SDFEM_delta (ConvDiff.C:269-495)
 beyond the steady ones: 6 (Franca/Valentin), 9-11 (John/Novo, time step
-dependent) and 12, and the rejection of the types the reference throws on.
+dependent) and 12, the rejection of the types the reference throws on, and
+CELL_MEASURE 4 (Mesh_size_in_convection_direction, ConvDiff.C:26-254).
 
 CPU: on the unit cube of 4^3 equal cubes every cell has h_K = sqrt(3)/4
 (CELL_MEASURE 0), so each type gives one delta for all cells.  A Python
@@ -137,3 +138,77 @@ def test_cuda_rejects_unknown_and_stationary_time_step_types(ctx):
         assert e.value.code == -1
     # Galerkin ignores the type
     cd.assemble(pg.assembly_params(example=pg.EX_SINE, eps=EPS, b=B[:2], sdfem_type=3))
+
+
+# ---------------------------------------------------------------------------
+# CELL_MEASURE 4: mesh size in convection direction (ConvDiff.C:26-254)
+# ---------------------------------------------------------------------------
+def stationary_matrix(dim, order, measure, b, ty=2, delta0=1.0):
+    o = po.Problem(po.make_config(dim, order, 2, po.EX_SINE, eps=EPS, b=b, c=C, supg=True,
+                                  sdfem_type=ty, cell_measure=measure, delta0=delta0), 1)
+    o.assemble()
+    return o.matrix(0)
+
+
+def same(A, B):
+    return np.max(np.abs(A - B)) <= 1e-13 * np.max(np.abs(B))
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("ty", [2, 7])
+def test_oracle_convection_size_known_answers(built, dim, ty):
+    # cells of side s: for b along x the size in convection direction is the
+    # edge s (CELL_MEASURE 2); for b along the diagonal it is the diameter
+    # sqrt(2) s in 2D (CELL_MEASURE 0), and 2 s / sqrt(3) = 2/3 of the diameter
+    # in 3D, which SDFEM type 0 (delta = delta0 h / |b| here) turns into a
+    # factor 2/3 on delta0
+    axis = tuple([0.9] + [0.0] * (dim - 1))
+    assert same(stationary_matrix(dim, 1, 4, axis, ty), stationary_matrix(dim, 1, 2, axis, ty))
+    diag = tuple([0.6] * dim)
+    if dim == 2:
+        assert same(stationary_matrix(2, 1, 4, diag, ty), stationary_matrix(2, 1, 0, diag, ty))
+    else:
+        assert same(stationary_matrix(3, 1, 4, diag, 0, 0.9),
+                    stationary_matrix(3, 1, 0, diag, 0, 0.9 * 2 / 3))
+    # and differs from both for another direction
+    b = (0.9, 0.4, 0.2)[:dim]
+    A4 = stationary_matrix(dim, 1, 4, b, ty)
+    assert np.max(np.abs(A4 - stationary_matrix(dim, 1, 0, b, ty))) > 1e-10
+    assert np.max(np.abs(A4 - stationary_matrix(dim, 1, 2, b, ty))) > 1e-10
+
+
+@pytest.mark.gpu
+def test_cuda_convection_size_matches_oracle(ctx):
+    b3 = (0.9, 0.4, 0.2)
+    # perturbed P2 tetrahedra (irregular cells), stationary
+    h = pg.Hierarchy(3, 2, 2, tetra=True, perturb=0.2, seed=9)
+    lv = []
+    for lvl in range(h.n_levels):
+        rp, col = h.pattern(lvl)
+        i = h.info(lvl)
+        lv.append(dict(verts=h.mesh(lvl), gdof=h.dofs(lvl), ndof=i["ndof"],
+                       nactive=i["nactive"], row_ptr=rp, col=col))
+    o = po.Problem(po.make_config(3, 2, 0, po.EX_SINE, eps=EPS, b=b3, c=C, supg=True,
+                                  sdfem_type=2, cell_measure=4, tetra=True), arrays=lv)
+    o.assemble()
+    cd = pg.ConvectionDiffusion(ctx, h)
+    cd.assemble(pg.assembly_params(example=pg.EX_SINE, eps=EPS, b=b3, c=C,
+                                   space_discretization_type="supg", sdfem_type=2,
+                                   cell_measure=4))
+    assert rel(cd.matrix(0), o.matrix(0)) < 1e-12
+    assert rel(cd.rhs(0), o.rhs(0)) < 1e-12
+    # quadrilaterals, time-dependent (type 5, coefficients scaled by theta1 tau)
+    cfg = po.make_config(2, 2, 3, po.EX_EXP_SIN, eps=EPS, b=b3[:2], c=C, supg=True,
+                         sdfem_type=5, cell_measure=4, time_step=TAU)
+    o2 = po.Problem(cfg, 1)
+    cd2 = pg.ConvectionDiffusion(ctx, pg.Hierarchy(2, 2, 3))
+    a = lambda t: pg.assembly_params(example=pg.EX_EXP_SIN, eps=EPS, b=b3[:2], c=C, t=t,
+                                     space_discretization_type="supg", sdfem_type=5,
+                                     cell_measure=4, time_step=TAU)
+    o2.tcd_initialize()
+    cd2.tcd_initialize(a(0.0))
+    o2.tcd_step(TAU, TAU, po.make_solver("jacobi", max_it=500, restart=50, reduction=1e-12))
+    cd2.tcd_step(a(TAU), TAU, pg.solver_params("jacobi", max_n_iterations=500, gmres_restart=50,
+                                               residual_tolerance=0.0, residual_reduction=1e-12))
+    for which in (0, 1, 2):
+        assert rel(cd2.tcd_matrix(which, 0), o2.tcd_matrix(which, 0)) < 1e-12
