@@ -411,6 +411,41 @@ int cdg_problem_create(cdg_context* ctx, const cdg_hierarchy* h, cdg_problem** o
   API_GUARD(problem_create(ctx, h, out));
 }
 
+// the first quadrilateral (hexahedron) of the mesh that is not a parallelogram
+// (parallelepiped), -1 if all are: the library maps cells affinely
+// (QuadAffin / HexaAffin through vertices 0, 1, 3 (, 4)); the reference takes
+// TQuadBilinear / THexaTrilinear for the others, which are not built here
+static long first_non_affine_cell(const Mesh& m) {
+  if (m.shape == kTetra) return -1;
+  const int dim = m.dim, nv = m.nv;
+  // vertex = v0 + sum of the listed edge vectors (v1-v0, v3-v0, v4-v0)
+  static const int quad_chk[1][3] = {{2, 1, 3}};
+  static const int hexa_chk[4][4] = {{2, 1, 3, -1}, {5, 1, 4, -1}, {7, 3, 4, -1}, {6, 1, 3, 4}};
+  for (long c = 0; c < m.ncells; ++c) {
+    const double* v = &m.verts[(size_t)c * nv * dim];
+    double scale = 0.0;
+    for (int e : {1, 3, 4}) {
+      if (e >= nv) continue;
+      double l = 0.0;
+      for (int a = 0; a < dim; ++a) l += (v[e * dim + a] - v[a]) * (v[e * dim + a] - v[a]);
+      scale += std::sqrt(l);
+    }
+    const int nchk = m.shape == kQuad ? 1 : 4;
+    for (int k = 0; k < nchk; ++k) {
+      const int* t = m.shape == kQuad ? quad_chk[k] : hexa_chk[k];
+      double d2 = 0.0;
+      for (int a = 0; a < dim; ++a) {
+        double x = v[a];
+        for (int e = 1; e < (m.shape == kQuad ? 3 : 4); ++e)
+          if (t[e] >= 0) x += v[t[e] * dim + a] - v[a];
+        d2 += (v[t[0] * dim + a] - x) * (v[t[0] * dim + a] - x);
+      }
+      if (std::sqrt(d2) > 1e-10 * scale) return c;
+    }
+  }
+  return -1;
+}
+
 static int problem_from_arrays(cdg_context* ctx, int cell_type, int order, int nl, const int* n_cells,
                                const double* const* verts, const int* const* gn,
                                const int* n_dofs, const int* n_active, const int* const* rp,
@@ -446,6 +481,13 @@ static int problem_from_arrays(cdg_context* ctx, int cell_type, int order, int n
     L.mesh.nv = nv;
     L.mesh.ncells = n_cells[l];
     L.mesh.verts.assign(verts[l], verts[l] + (size_t)n_cells[l] * nv * dim);
+    const long bad = first_non_affine_cell(L.mesh);
+    if (bad >= 0) {
+      delete p;
+      set_error("cell %ld of level %d is not a %s: bilinear/trilinear reference maps are "
+                "not supported", bad, l, shape == kQuad ? "parallelogram" : "parallelepiped");
+      return CDG_ERR_ARG;
+    }
     L.space.dim = dim;
     L.space.shape = shape;
     L.space.order = order;

@@ -217,6 +217,27 @@ def test_from_arrays_equals_hierarchy(ctx):
     assert rel(g1.solution(), g2.solution()) < 1e-12
 
 
+@pytest.mark.parametrize("dim", [2, 3])
+def test_from_arrays_rejects_non_affine_cells(ctx, dim):
+    # the reference maps such cells with TQuadBilinear / THexaTrilinear, which
+    # are not built: the problem is refused instead of assembled wrongly
+    h = pg.Hierarchy(dim, 1, 2)
+    rp, col = h.pattern(0)
+    i = h.info(0)
+    v = h.mesh(0).copy()
+    lv = dict(verts=v, dofs=h.dofs(0), ndof=i["ndof"], nactive=i["nactive"], row_ptr=rp, col=col)
+    ct = pg.CELL_QUAD if dim == 2 else pg.CELL_HEXA
+    # a sheared (still affine) mesh is accepted
+    sh = v.copy()
+    sh[..., 0] += 0.3 * sh[..., 1]
+    pg.ConvectionDiffusion.from_arrays(ctx, ct, 1, [dict(lv, verts=sh)])
+    bad = v.copy()
+    bad[5, 2, 0] += 0.01 * (1.0 / 4)     # vertex 2 of cell 5 off the parallelogram
+    with pytest.raises(pg.CdgError) as e:
+        pg.ConvectionDiffusion.from_arrays(ctx, ct, 1, [dict(lv, verts=bad)])
+    assert e.value.code == -1 and "cell 5" in str(e.value)
+
+
 def test_errors_are_reported(ctx):
     # zero matrix (eps=b=c=0): Jacobi finds a zero diagonal, the reference
     # throws "zero entry on the diagonal"; here a status code comes back
