@@ -1732,7 +1732,9 @@ static int read_state(cdg_context* ctx, const GmresState& g, int* st4, double* r
 // seven dependent kernels.  A thread owns up to kCycleRows rows and keeps
 // their w in registers from the operator to the normalisation (one row per
 // thread measured best on GB300: 64^2 Q1, 387 iterations, 84.9 solves/s
-// against 68.8 with two rows, 57.2 with four and 58.9 for the graph).  The inner
+// against 68.8 with two rows, 57.2 with four and 58.9 for the graph; 64-thread
+// blocks over 67 SMs instead of 17 gave 69.3 against 91.9: the barriers, not
+// the FP64 work, bound an iteration of this size).  The inner
 // products of a block are reduced through shared memory (one warp per
 // product); every block sums the blocks' partials in block order, so all
 // blocks hold the same values, run the Givens step and the convergence test
