@@ -82,9 +82,11 @@ typedef struct {
   double c;             /* reaction                                           */
   double freq;          /* CDG_EX_SINE frequency                              */
   int supg;             /* space_discretization_type: 0 galerkin, 1 supg      */
-  int sdfem_type;       /* SDFEM_TYPE                                         */
+  int sdfem_type;       /* SDFEM_TYPE: 0-2, 4-12 (9-11 time-dependent only);
+                           others rejected with CDG_ERR_ARG                   */
   double delta0, delta1;/* DELTA0, DELTA1                                     */
-  int cell_measure;     /* CELL_MEASURE                                       */
+  int cell_measure;     /* CELL_MEASURE: 0 diameter, 1/3 sqrt(measure), 2
+                           shortest edge, 4 size in convection direction     */
   int problem_linear;   /* INTERNAL_PROBLEM_LINEAR (quadrature degree 2p)     */
   int neumann_mask;     /* bit k: boundary component k is Neumann             */
   int poly_degree;      /* INTERNAL_POLYNOMIAL_DEGREE (0: element order)      */
