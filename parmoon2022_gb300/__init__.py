@@ -25,6 +25,7 @@ ERRORS = {
     -1: "CDG_ERR_ARG", -2: "CDG_ERR_CUDA", -3: "CDG_ERR_OOM", -4: "CDG_ERR_DIVERGED",
     -5: "CDG_ERR_BREAKDOWN", -6: "CDG_ERR_ZERO_DIAG", -7: "CDG_ERR_PATTERN",
     -8: "CDG_ERR_SINGULAR", -9: "CDG_ERR_NO_DEVICE", -10: "CDG_ERR_LIMIT",
+    -11: "CDG_ERR_TIMEOUT",
 }
 (EX_SINE_LAPLACE, EX_SINE, EX_POLYEXP, EX_CONST_F, EX_POLY1, EX_BUMP, EX_POLY1_T, EX_EXP_SIN,
  EX_LINEAR_ST, EX_QUAD_ST) = range(10)

@@ -9,6 +9,7 @@ SolverConfig).
 """
 import ctypes
 import os
+import re
 import shutil
 import subprocess
 import tempfile
@@ -70,3 +71,31 @@ def test_ctypes_mirrors_match_the_header(which):
         assert ctypes.sizeof(py) == t[(cname, "sizeof")], cname
         for fname, _ in py._fields_:
             assert getattr(py, fname).offset == t[(cname, fname)], (cname, fname)
+
+
+def test_constants_match_the_headers():
+    # the C-ABI's #defines against the package's constants
+    hdr = open(os.path.join(ROOT, "include", "parmoon_cd.h")).read()
+    defs = {m.group(1): int(m.group(2)) for m in
+            re.finditer(r"#define CDG_(\w+) \(?(-?\d+)\)?", hdr)}
+    schemes = {"TIME_CRANK_NICOLSON": "crank_nicolson", "TIME_BACKWARD_EULER": "backward_euler",
+               "TIME_BDF_TWO": "bdf_two"}
+    seen = set()
+    for name, value in defs.items():
+        if name.startswith("EX_") or name.startswith("CELL_"):
+            assert getattr(pg, name) == value, name
+        elif name.startswith("ERR_"):
+            assert pg.ERRORS[value] == "CDG_" + name, name
+        elif name in schemes:
+            assert pg.TIME_SCHEMES[schemes[name]] == value, name
+        else:
+            continue
+        seen.add(name)
+    assert len([n for n in seen if n.startswith("EX_")]) == 10
+    assert len([n for n in seen if n.startswith("ERR_")]) == len(pg.ERRORS)
+    # the oracle's enumerations against pyoracle
+    ohdr = open(os.path.join(ROOT, "oracle", "cd_oracle.h")).read()
+    for m in re.finditer(r"ORC_(EX_\w+) = (\d+)", ohdr):
+        assert getattr(po, m.group(1)) == int(m.group(2)), m.group(1)
+    for m in re.finditer(r"ORC_(TIME_\w+) = (\d+)", ohdr):
+        assert po.TIME_SCHEMES[schemes[m.group(1)]] == int(m.group(2)), m.group(1)
