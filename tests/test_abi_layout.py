@@ -1,4 +1,4 @@
-"""The ctypes mirrors of the C structs match their headers.
+"""The ctypes mirrors of the C structs, constants and signatures match their headers.
 
 A small C program compiled with the host compiler against the header prints
 sizeof and every field's offsetof; the Python structures must agree field by
@@ -99,3 +99,23 @@ def test_constants_match_the_headers():
         assert getattr(po, m.group(1)) == int(m.group(2)), m.group(1)
     for m in re.finditer(r"ORC_(TIME_\w+) = (\d+)", ohdr):
         assert po.TIME_SCHEMES[schemes[m.group(1)]] == int(m.group(2)), m.group(1)
+
+
+def test_ctypes_signatures_match_the_prototypes(built):
+    # every function the package gives argtypes to takes as many parameters
+    # as its prototype in the header declares
+    hdr = open(os.path.join(ROOT, "include", "parmoon_cd.h")).read()
+    hdr = re.sub(r"/\*.*?\*/", " ", hdr, flags=re.S)
+    protos = {}
+    for m in re.finditer(r"(?:const char \*|int|long long)\s*(cdg_\w+)\(([^)]*)\);", hdr, re.S):
+        params = m.group(2).strip()
+        protos[m.group(1)] = 0 if params in ("", "void") else params.count(",") + 1
+    L = pg.lib()
+    checked = 0
+    for name, n in protos.items():
+        at = getattr(L, name).argtypes
+        if at is None:
+            continue
+        assert len(at) == n, (name, len(at), n)
+        checked += 1
+    assert checked >= 40
