@@ -101,15 +101,33 @@ def test_constants_match_the_headers():
         assert po.TIME_SCHEMES[schemes[m.group(1)]] == int(m.group(2)), m.group(1)
 
 
+def prototypes(path, prefix):
+    hdr = open(path).read()
+    hdr = re.sub(r"/\*.*?\*/", " ", hdr, flags=re.S)
+    protos = {}
+    pat = r"(?:const char \*|int|long long|void|orc_problem \*)\s*(%s\w+)\(([^)]*)\);" % prefix
+    for m in re.finditer(pat, hdr, re.S):
+        params = m.group(2).strip()
+        protos[m.group(1)] = 0 if params in ("", "void") else params.count(",") + 1
+    return protos
+
+
+def test_oracle_signatures_match_the_prototypes(built):
+    L = po.lib()
+    checked = 0
+    for name, n in prototypes(os.path.join(ROOT, "oracle", "cd_oracle.h"), "orc_").items():
+        at = getattr(L, name).argtypes
+        if at is None:
+            continue
+        assert len(at) == n, (name, len(at), n)
+        checked += 1
+    assert checked >= 10
+
+
 def test_ctypes_signatures_match_the_prototypes(built):
     # every function the package gives argtypes to takes as many parameters
     # as its prototype in the header declares
-    hdr = open(os.path.join(ROOT, "include", "parmoon_cd.h")).read()
-    hdr = re.sub(r"/\*.*?\*/", " ", hdr, flags=re.S)
-    protos = {}
-    for m in re.finditer(r"(?:const char \*|int|long long)\s*(cdg_\w+)\(([^)]*)\);", hdr, re.S):
-        params = m.group(2).strip()
-        protos[m.group(1)] = 0 if params in ("", "void") else params.count(",") + 1
+    protos = prototypes(os.path.join(ROOT, "include", "parmoon_cd.h"), "cdg_")
     L = pg.lib()
     checked = 0
     for name, n in protos.items():
