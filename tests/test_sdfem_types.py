@@ -212,3 +212,27 @@ def test_cuda_convection_size_matches_oracle(ctx):
                                                residual_tolerance=0.0, residual_reduction=1e-12))
     for which in (0, 1, 2):
         assert rel(cd2.tcd_matrix(which, 0), o2.tcd_matrix(which, 0)) < 1e-12
+
+
+def test_oracle_convection_size_kuhn_tetrahedra(built):
+    # on unperturbed Kuhn tetrahedra (cube side s) the P1 vertex gradients
+    # give h = s for b along x (the shortest edge, CELL_MEASURE 2) and
+    # h = sqrt(3) s for b along the cube diagonal (the longest edge, the
+    # diameter, CELL_MEASURE 0) in every one of the six orientations
+    h = pg.Hierarchy(3, 1, 2, tetra=True)
+    lv = []
+    for lvl in range(h.n_levels):
+        rp, col = h.pattern(lvl)
+        i = h.info(lvl)
+        lv.append(dict(verts=h.mesh(lvl), gdof=h.dofs(lvl), ndof=i["ndof"],
+                       nactive=i["nactive"], row_ptr=rp, col=col))
+
+    def mat(measure, b):
+        o = po.Problem(po.make_config(3, 1, 0, po.EX_SINE, eps=EPS, b=b, c=C, supg=True,
+                                      sdfem_type=2, cell_measure=measure, tetra=True), arrays=lv)
+        o.assemble()
+        return o.matrix(0)
+
+    assert same(mat(4, (0.9, 0.0, 0.0)), mat(2, (0.9, 0.0, 0.0)))
+    assert same(mat(4, (0.6, 0.6, 0.6)), mat(0, (0.6, 0.6, 0.6)))
+    assert np.max(np.abs(mat(4, (0.9, 0.4, 0.2)) - mat(0, (0.9, 0.4, 0.2)))) > 1e-10
