@@ -236,3 +236,45 @@ def test_oracle_convection_size_kuhn_tetrahedra(built):
     assert same(mat(4, (0.9, 0.0, 0.0)), mat(2, (0.9, 0.0, 0.0)))
     assert same(mat(4, (0.6, 0.6, 0.6)), mat(0, (0.6, 0.6, 0.6)))
     assert np.max(np.abs(mat(4, (0.9, 0.4, 0.2)) - mat(0, (0.9, 0.4, 0.2)))) > 1e-10
+
+
+def expected_delta_2d(ty, h):
+    # the 2D time-dependent routines scale the coefficients by theta1 tau
+    # first (reaction 1 + theta1 tau c), except for types 2 and 12
+    b = B[:2]
+    tt = THETA1 * TAU
+    nb = math.sqrt(sum(x * x for x in b))
+    es, nbs, rs = tt * EPS, tt * nb, 1.0 + tt * C
+    if ty == 6:
+        a1 = max(1.0, 6 * es / (h * h * rs))
+        a2 = max(1.0, h * nbs / (3 * es))
+        return D0 * h * h / (rs * h * h * a1 + 6 * es * a2) * tt
+    if ty == 7:
+        return D0 * h * h / (4 * es + 2 * h * nbs + h * h * rs) * tt
+    if ty == 10:
+        eu = es / tt
+        return D0 * h if eu <= h else D0 * h * h / eu
+    if ty == 11:
+        return D0 * h * math.sqrt(TAU) / (nbs / TAU)
+    if ty == 12:
+        return 100 * min(h / (2 * math.sqrt(3) * D0) * min(0.25, math.sqrt(3) * h / (8 * EPS * D0)),
+                         1.0)
+    raise ValueError(ty)
+
+
+def oracle_tcd_2d(ty, delta0):
+    cfg = po.make_config(2, 1, 2, po.EX_SINE, eps=EPS, b=B[:2], c=C, supg=True, sdfem_type=ty,
+                         delta0=delta0, time_step=TAU)
+    o = po.Problem(cfg, 1)
+    o.tcd_initialize()
+    o.tcd_step(TAU, TAU, po.make_solver("jacobi", max_it=500, restart=50, reduction=1e-10))
+    return o.tcd_matrix(2, 0), o.tcd_matrix(1, 0)
+
+
+@pytest.mark.parametrize("ty", [6, 7, 10, 11, 12])
+def test_oracle_delta_formula_2d_scaled_coefficients(built, ty):
+    d = expected_delta_2d(ty, math.sqrt(2) / 4)
+    S, M = oracle_tcd_2d(ty, D0)
+    S9, M9 = oracle_tcd_2d(9, d / TAU)
+    assert np.max(np.abs(S - S9)) <= 1e-13 * np.max(np.abs(S))
+    assert np.max(np.abs(M - M9)) <= 1e-13 * np.max(np.abs(M))
