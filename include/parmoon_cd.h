@@ -258,8 +258,12 @@ int cdg_problem_errors(cdg_problem *p, const cdg_assembly_params *a,
  * array of 16384 x 5 + 8 doubles (~640 KB) that every GPU loading the library
  * keeps until exit; it holds one partial sum row per 8 cells, so the finest
  * level may have at most 131,072 cells (larger: CDG_ERR_LIMIT, use
- * cdg_problem_errors).  The first call on a device looks up the array's
- * device address; make that first call before any stream capture.  All calls
+ * cdg_problem_errors).  It evaluates tensor-product bases only
+ * (quadrilaterals and hexahedra; tetrahedral levels get CDG_ERR_ARG).
+ * Otherwise it accepts what cdg_problem_errors accepts (every example, a
+ * convection field linear in x, any time a->t) and returns the same status
+ * for what that entry rejects.  The first call on a device looks up the
+ * array's device address; make that first call before any stream capture.  All calls
  * share the array: calls that overlap on the GPU (other streams, other host
  * threads) race and must be serialised by the caller. */
 int cdg_problem_errors_noalloc(cdg_problem *p, const cdg_assembly_params *a,

@@ -380,6 +380,7 @@ class Context:
         c = ctypes.c_void_p()
         _chk(lib().cdg_context_create(device, ctypes.byref(c)))
         self.c = c
+        self.device = device
         self._problems = weakref.WeakSet()   # destroyed before the context
 
     def synchronize(self):

@@ -18,6 +18,21 @@ void set_error(const char* fmt, ...) {
   vsnprintf(g_msg, sizeof g_msg, fmt, ap);
   va_end(ap);
 }
+
+int check_assembly_params(const cdg_problem* p, const cdg_assembly_params* a) {
+  if (!p || !a) { set_error("null argument"); return CDG_ERR_ARG; }
+  if (a->example < 0 || a->example > CDG_EX_QUAD_ST) { set_error("unknown example %d", a->example); return CDG_ERR_ARG; }
+  if (a->time_discretization < CDG_TIME_CRANK_NICOLSON || a->time_discretization > CDG_TIME_BDF_TWO) {
+    set_error("time discretization scheme %d is not supported", a->time_discretization);
+    return CDG_ERR_ARG;
+  }
+  if (a->bdf_two_first_step < 0 || a->bdf_two_first_step > 1) {
+    set_error("bdf_two_first_step %d: 0 backward Euler or 1 Crank-Nicolson", a->bdf_two_first_step);
+    return CDG_ERR_ARG;
+  }
+  if (a->example == CDG_EX_POLYEXP && p->dim != 3) { set_error("example needs 3D"); return CDG_ERR_ARG; }
+  return CDG_OK;
+}
 }  // namespace cdg
 
 using namespace cdg;
@@ -554,21 +569,6 @@ int cdg_problem_destroy(cdg_problem* p) {
   if (p->d_tables) cudaFree(p->d_tables);
   if (p->d_zero_diag) cudaFree(p->d_zero_diag);
   delete p;
-  return CDG_OK;
-}
-
-static int check_assembly_params(const cdg_problem* p, const cdg_assembly_params* a) {
-  if (!p || !a) { set_error("null argument"); return CDG_ERR_ARG; }
-  if (a->example < 0 || a->example > CDG_EX_QUAD_ST) { set_error("unknown example %d", a->example); return CDG_ERR_ARG; }
-  if (a->time_discretization < CDG_TIME_CRANK_NICOLSON || a->time_discretization > CDG_TIME_BDF_TWO) {
-    set_error("time discretization scheme %d is not supported", a->time_discretization);
-    return CDG_ERR_ARG;
-  }
-  if (a->bdf_two_first_step < 0 || a->bdf_two_first_step > 1) {
-    set_error("bdf_two_first_step %d: 0 backward Euler or 1 Crank-Nicolson", a->bdf_two_first_step);
-    return CDG_ERR_ARG;
-  }
-  if (a->example == CDG_EX_POLYEXP && p->dim != 3) { set_error("example needs 3D"); return CDG_ERR_ARG; }
   return CDG_OK;
 }
 

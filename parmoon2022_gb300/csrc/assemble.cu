@@ -1919,9 +1919,6 @@ k_errors_noalloc(AsmCoefs k, LineRule rule, int ncells, const double* __restrict
     const double hK = cell_hK(DIM, cv, k.cell_measure, A.det);
     const int nl = k.nloc, n1 = k.order + 1;
     const double fv = lane < nl ? sol[gdof[(size_t)cell * nl + lane]] : 0.0;
-    double linfb = fmax(fabs(k.b[0]), fabs(k.b[1]));
-    if (DIM == 3) linfb = fmax(linfb, fabs(k.b[2]));
-    const double delta = sdfem_delta(k, cv, hK, k.eps, k.b, k.c, linfb);
     const int ki[3] = {lane % n1, (lane / n1) % n1, lane / (n1 * n1)};
     const int nq = DIM == 2 ? rule.n * rule.n : rule.n * rule.n * rule.n;
     for (int q = 0; q < nq; ++q) {
@@ -1946,20 +1943,25 @@ k_errors_noalloc(AsmCoefs k, LineRule rule, int ncells, const double* __restrict
         double g[3] = {0, 0, 0};
         for (int r = 0; r < DIM; ++r)
           for (int a = 0; a < DIM; ++a) g[r] += A.Ji[a][r] * gr[a];
-        double x[3], u[6];
+        double x[3], u[6], bx[3];
         for (int r = 0; r < DIM; ++r) {
           double s = A.x0[r];
           for (int a = 0; a < DIM; ++a) s += A.J[r][a] * xi[a];
           x[r] = s;
         }
         ex_exact(k, x, u);
+        // convection (and with it delta) at the point: b may be linear in x
+        b_at(k, x, bx);
+        double linfb = fmax(fabs(bx[0]), fabs(bx[1]));
+        if (DIM == 3) linfb = fmax(linfb, fabs(bx[2]));
+        const double delta = sdfem_delta(k, cv, hK, k.eps, bx, k.c, linfb);
         const double w = wq * adet;
         const double e0 = uh - u[0];
         emax = fmax(emax, fabs(e0));
         const double e1 = g[0] - u[1], e2 = g[1] - u[2], e3 = DIM == 2 ? 0.0 : g[2] - u[3];
         e[0] += w * e0 * e0;
         e[1] += w * (e1 * e1 + e2 * e2 + e3 * e3);
-        const double e4 = k.b[0] * e1 + k.b[1] * e2 + (DIM == 3 ? k.b[2] * e3 : 0.0);
+        const double e4 = bx[0] * e1 + bx[1] * e2 + (DIM == 3 ? bx[2] * e3 : 0.0);
         e[2] += w * (k.eps * (e1 * e1 + e2 * e2 + e3 * e3) + k.c * e0 * e0 + delta * e4 * e4);
         e[3] += w * (k.eps * (e1 * e1 + e2 * e2 + e3 * e3) + (e4 + k.c * e0) * e0);
       }
@@ -2004,12 +2006,10 @@ static cudaError_t g_errors_noalloc_status[64];
 extern "C" int cdg_problem_errors_noalloc(cdg_problem* p, const cdg_assembly_params* a,
                                           double* errors) {
   using namespace cdg;
-  if (!p || !a || !errors) {
-    set_error("null argument");
-    return CDG_ERR_ARG;
-  }
-  if (a->example < 0 || a->example > CDG_EX_POLY1) {
-    set_error("unknown example %d", a->example);
+  // the same argument checks as cdg_problem_errors
+  CDG_TRY(check_assembly_params(p, a));
+  if (!errors) {
+    set_error("null output");
     return CDG_ERR_ARG;
   }
   cdg_context* ctx = p->ctx;

@@ -237,6 +237,8 @@ int build_slots(cdg_context* ctx, DevLevel& L);
 int assemble_level(cdg_context* ctx, cdg_problem* p, DevLevel& L,
                    const cdg_assembly_params& a);
 int check_device_error(cdg_context* ctx);
+// argument checks of every entry point that takes assembly parameters
+int check_assembly_params(const cdg_problem* p, const cdg_assembly_params* a);
 int level_errors(cdg_context* ctx, cdg_problem* p, DevLevel& L,
                  const cdg_assembly_params& a, double* errors);
 // time-dependent CD (TimeConvectionDiffusion with the TimeDiscretization schemes)

@@ -4,15 +4,21 @@ Reads (as text) test/cd2d_test.c++ (error norms of CD2D example 0 on the
 4x4 UnitSquare for Q1..Q8, tolerance 1e-11), test/tcd2d_test.c++ (L2 / H1
 errors of the Crank-Nicolson TCD2D example 0 after selected steps, Galerkin
 and SUPG, tolerance 1e-10) and test/structure_test.c++ (pattern counts of
-one-cell meshes), and writes reference_values.json next to this script.  Runs where the reference tree is present; the JSON is
-committed so the tests never need the reference itself.
+one-cell meshes), and writes reference_values.json next to this script.
+
+    python tests/golden/make_reference_values.py <path of the ParMooN2022 source tree>
+
+Runs where the reference tree is present; the JSON is committed so the tests
+never need the reference itself.
 """
 import json
 import os
 import re
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit("usage: make_reference_values.py <ParMooN2022 source tree>")
+REF = sys.argv[1]
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 

@@ -16,6 +16,8 @@ import parmoon2022_gb300 as pg
 
 pytestmark = pytest.mark.gpu
 
+ROT = ((0.0, -1.0, 0.0), (1.0, 0.0, 0.0), (0.0, 0.0, 0.0))
+
 
 def _noalloc(cd, a):
     e = np.zeros(5)
@@ -24,16 +26,22 @@ def _noalloc(cd, a):
     return rc, e
 
 
-@pytest.mark.parametrize("dim,order,nref,example,eps,b,c,supg", [
-    (2, 1, 6, pg.EX_SINE, 1e-2, (1.0, 0.5), 1.0, False),
-    (2, 2, 4, pg.EX_SINE, 1e-3, (1.0, 0.5), 0.5, True),
-    (3, 2, 3, pg.EX_POLYEXP, 1e-3, (0.57735, 0.57735, 0.57735), 0.0, True),
+@pytest.mark.parametrize("dim,order,nref,kw", [
+    (2, 1, 6, dict(example=pg.EX_SINE, eps=1e-2, b=(1.0, 0.5), c=1.0)),
+    (2, 2, 4, dict(example=pg.EX_SINE, eps=1e-3, b=(1.0, 0.5), c=0.5,
+                   space_discretization_type="supg", sdfem_type=2)),
+    (3, 2, 3, dict(example=pg.EX_POLYEXP, eps=1e-3, b=(0.57735, 0.57735, 0.57735),
+                   space_discretization_type="supg", sdfem_type=5, cell_measure=2,
+                   problem_linear=1)),
+    # a convection field linear in x: b and delta change from point to point
+    (2, 2, 4, dict(example=pg.EX_SINE, eps=1e-2, b=(0.5, -0.5), b_grad=ROT, c=0.5)),
+    (3, 1, 3, dict(example=pg.EX_SINE, eps=1e-2, b=(0.5, -0.5, 0.2), b_grad=ROT, c=0.3)),
+    # a time-dependent example at t = 0.3 (its exact solution depends on t)
+    (2, 2, 4, dict(example=pg.EX_EXP_SIN, eps=1.0, b=(1.0, -1.0), c=1.0, t=0.3)),
 ])
-def test_noalloc_errors_match_allocating_entry(ctx, dim, order, nref, example, eps, b, c, supg):
+def test_noalloc_errors_match_allocating_entry(ctx, dim, order, nref, kw):
     cd = pg.ConvectionDiffusion(ctx, pg.Hierarchy(dim, order, nref, n_levels=1))
-    a = pg.assembly_params(example=example, eps=eps, b=b, c=c,
-                           space_discretization_type="supg" if supg else "galerkin",
-                           sdfem_type=2)
+    a = pg.assembly_params(**kw)
     cd.assemble(a)
     cd.solve(pg.solver_params("jacobi", max_n_iterations=300, gmres_restart=50,
                               residual_tolerance=0.0, residual_reduction=1e-8))
@@ -42,6 +50,39 @@ def test_noalloc_errors_match_allocating_entry(ctx, dim, order, nref, example, e
         rc, got = _noalloc(cd, a)
         assert rc == 0, pg.lib().cdg_last_error().decode()
         assert np.allclose(got, want, rtol=1e-12, atol=0.0), (got, want)
+    cd.close()
+
+
+def test_noalloc_leaves_device_memory_unchanged(ctx):
+    torch = pytest.importorskip("torch")
+    cd = pg.ConvectionDiffusion(ctx, pg.Hierarchy(3, 2, 3, n_levels=1))
+    a = pg.assembly_params(example=pg.EX_SINE, eps=1e-2, b=(1.0, 0.3, -0.2), c=0.5)
+    cd.assemble(a)
+    rc, _ = _noalloc(cd, a)        # first call on the device: the array's address
+    assert rc == 0
+    ctx.synchronize()
+    free0 = torch.cuda.mem_get_info(ctx.device)[0]
+    for _ in range(3):
+        rc, _ = _noalloc(cd, a)
+        assert rc == 0
+    ctx.synchronize()
+    assert torch.cuda.mem_get_info(ctx.device)[0] == free0
+    cd.close()
+
+
+def test_noalloc_rejects_what_the_allocating_entry_rejects(ctx):
+    cd = pg.ConvectionDiffusion(ctx, pg.Hierarchy(2, 1, 3, n_levels=1))
+    for bad in (dict(example=pg.EX_POLYEXP),             # a 3D example on a 2D problem
+                dict(example=42),
+                dict(example=pg.EX_SINE, time_discretization="crank_nicolson")):
+        a = pg.assembly_params(**bad)
+        if bad.get("time_discretization"):
+            a.time_discretization = 7
+        rc, _ = _noalloc(cd, a)
+        e = np.zeros(5)
+        rc_alloc = pg.lib().cdg_problem_errors(cd.p, ctypes.byref(a),
+                                               e.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+        assert rc == rc_alloc == -1, (bad, rc, rc_alloc)
     cd.close()
 
 
