@@ -353,6 +353,23 @@ int cdg_problem_prolongate(cdg_problem *p, int fine_level, const double *xc,
 /* GridTransfer::DefectRestriction (fine_level -> fine_level+1) */
 int cdg_problem_restrict(cdg_problem *p, int fine_level, const double *df,
                          double *rc);
+/* y = A x with the FP32 copy of a level's operator that the mixed-precision
+ * multigrid smooths with (JacobiSmoother's BlockFEMatrix::apply, identity on
+ * non-active rows), host float buffers of n_dofs entries.  variant 0: CSR
+ * kernel; 1: matrix-free kernel (Q2 hexahedra after a stationary assembly,
+ * the element matrices applied from per-cell factors or, on uniform levels,
+ * from one shared element matrix).  Parity access for the multigrid kernels. */
+int cdg_problem_apply32(cdg_problem *p, int level, int variant, const float *x,
+                        float *y);
+/* the FP32 multigrid kernel chosen for a level (no counterpart in the
+ * reference, which has one kernel): *choice -1 not chosen yet (no
+ * mixed-precision multigrid solve so far, or a level without a matrix-free
+ * operator), 0 CSR, 1 matrix-free.  The choice is made once per level at
+ * the first mixed-precision solve by timing one smoothing step of each
+ * kernel (CUDA events); ms (may be NULL) receives those two times in
+ * milliseconds (0 when the choice was fixed by CDG_MATFREE=0/1 in the
+ * environment). */
+int cdg_problem_tuning(cdg_problem *p, int level, int *choice, double *ms);
 /* one preconditioner application z = M^-1 v (Iteration_multigrid::apply or
  * Iteration_jacobi::apply) */
 int cdg_problem_precondition(cdg_problem *p, const cdg_solver_params *s,

@@ -52,7 +52,7 @@ EXPORTED = [
     "cdg_problem_write_solution", "cdg_problem_read_solution", "cdg_problem_checkpoint",
     "cdg_problem_tcd_step", "cdg_problem_get_tcd_matrix", "cdg_server_create",
     "cdg_server_destroy", "cdg_request_ndof", "cdg_server_submit", "cdg_server_wait",
-    "cdg_server_counters",
+    "cdg_server_counters", "cdg_problem_apply32", "cdg_problem_tuning",
 ]
 
 
@@ -169,6 +169,9 @@ def lib():
             "cdg_problem_get_solution": [P, dp], "cdg_problem_set_solution": [P, dp],
             "cdg_problem_get_slots": [P, ctypes.c_int, ip],
             "cdg_problem_apply": [P, ctypes.c_int, dp, dp],
+            "cdg_problem_tuning": [P, ctypes.c_int, ip, dp],
+            "cdg_problem_apply32": [P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float),
+                                    ctypes.POINTER(ctypes.c_float)],
             "cdg_problem_prolongate": [P, ctypes.c_int, dp, dp],
             "cdg_problem_restrict": [P, ctypes.c_int, dp, dp],
             "cdg_problem_precondition": [P, ctypes.POINTER(SolverParams), dp, dp],
@@ -593,6 +596,24 @@ class ConvectionDiffusion:
         x = np.ascontiguousarray(x, dtype=np.float64)
         y = np.zeros_like(x)
         _chk(lib().cdg_problem_apply(self.p, level, _dp(x), _dp(y)))
+        return y
+
+    def tuning(self, level=0):
+        """(choice, (ms_csr, ms_matfree)): the FP32 multigrid kernel of a
+        level (-1 not chosen, 0 CSR, 1 matrix-free) and the tuner's times."""
+        c = ctypes.c_int(0)
+        ms = np.zeros(2)
+        _chk(lib().cdg_problem_tuning(self.p, level, ctypes.byref(c), _dp(ms)))
+        return c.value, (float(ms[0]), float(ms[1]))
+
+    def apply32(self, x, level=0, variant=0):
+        """y = A x with the FP32 multigrid operator of a level: variant 0 the
+        CSR kernel, 1 the matrix-free kernel (Q2 hexahedra)."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.zeros_like(x)
+        fp = ctypes.POINTER(ctypes.c_float)
+        _chk(lib().cdg_problem_apply32(self.p, level, variant, x.ctypes.data_as(fp),
+                                       y.ctypes.data_as(fp)))
         return y
 
     def prolongate(self, xc, fine_level=0):

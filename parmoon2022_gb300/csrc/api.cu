@@ -798,6 +798,43 @@ int cdg_problem_apply(cdg_problem* p, int level, const double* x, double* y) {
   return d2h(p->ctx, y, dy.d, (size_t)L->ndof * sizeof(double));
 }
 
+int cdg_problem_tuning(cdg_problem* p, int level, int* choice, double* ms) {
+  DevLevel* L = get_level(p, level);
+  if (!L || !choice) { set_error("bad arguments"); return CDG_ERR_ARG; }
+  *choice = L->mf_mode;
+  if (ms) {
+    ms[0] = L->tuned_ms[0];
+    ms[1] = L->tuned_ms[1];
+  }
+  return CDG_OK;
+}
+
+int cdg_problem_apply32(cdg_problem* p, int level, int variant, const float* x, float* y) {
+  DevLevel* L = get_level(p, level);
+  if (!L || !x || !y || variant < 0 || variant > 1) { set_error("bad arguments"); return CDG_ERR_ARG; }
+  if (variant == 1 && !L->mf_valid) {
+    set_error("no matrix-free operator on level %d (Q2 hexahedra after a stationary assembly)",
+              level);
+    return CDG_ERR_ARG;
+  }
+  CDG_CUDA(cudaSetDevice(p->ctx->device));
+  const size_t n = (size_t)std::max(L->ndof, 1);
+  float *dx = nullptr, *dy = nullptr;
+  CDG_CUDA(cudaMalloc(&dx, n * sizeof(float)));
+  int rc = CDG_OK;
+  if (cudaMalloc(&dy, n * sizeof(float)) != cudaSuccess) rc = CDG_ERR_OOM;
+  if (rc == CDG_OK &&
+      cudaMemcpyAsync(dx, x, (size_t)L->ndof * sizeof(float), cudaMemcpyHostToDevice,
+                      p->ctx->stream) != cudaSuccess)
+    rc = CDG_ERR_CUDA;
+  if (rc == CDG_OK) rc = apply32(p->ctx, *L, variant, dx, dy);
+  if (rc == CDG_OK) rc = d2h(p->ctx, y, dy, (size_t)L->ndof * sizeof(float));
+  cudaFree(dx);
+  if (dy) cudaFree(dy);
+  if (rc == CDG_ERR_OOM) set_error("out of device memory");
+  return rc;
+}
+
 int cdg_problem_prolongate(cdg_problem* p, int fine, const double* xc, double* xf) {
   DevLevel* F = get_level(p, fine);
   DevLevel* C = get_level(p, fine + 1);

@@ -608,6 +608,92 @@ __device__ void cell_factors(const AsmCoefs& k, const double* __restrict__ cv, d
     }
 }
 
+// the factors of the stationary operator of every cell in FP32, for the
+// matrix-free multigrid operator of Q2 hexahedral levels (matfree.cu)
+__global__ void k_mf_factors(AsmCoefs k, int ncells, const double* __restrict__ verts,
+                             float* __restrict__ fac) {
+  const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= ncells) return;
+  static_assert(Terms<3>::NT == kMfFactors, "factor layout of the matrix-free operator");
+  double g[Terms<3>::NT];
+  cell_factors<3>(k, verts + (size_t)cell * 8 * 3, g, 0);
+  for (int t = 0; t < Terms<3>::NT; ++t) fac[(size_t)cell * kMfFactors + t] = (float)g[t];
+}
+
+// Position of every (cell, local DOF) result in the DOF-major array the
+// matrix-free gather sums: the entries of active row r occupy
+// [dof_rp[r], dof_rp[r+1]) in the order of dof_ent; -1 for non-active DOFs
+// (identity rows, never summed)
+__global__ void k_mf_pos(int nactive, const int* __restrict__ dof_rp,
+                         const int* __restrict__ dof_ent, int* __restrict__ pos) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nactive) return;
+  for (int e = dof_rp[r]; e < dof_rp[r + 1]; ++e) pos[dof_ent[e]] = e;
+}
+
+// Cells of a refined hexahedral hierarchy carry rotated and reflected local
+// frames.  Where every cell is a translate of cell 0 (a uniform mesh, or one
+// affine image of it), R = J_0^-1 J_c is a signed permutation: the node of
+// cell c at reference point xi sits at R xi in cell 0's frame, so in that
+// order the cell has cell 0's element matrix.  Per cell: the DOFs and the
+// gather positions in cell 0's order (gdof_c, pos_c); any cell without such
+// an R sets *nonuniform (its own order kept).
+__global__ void k_mf_canon(int ncells, const double* __restrict__ verts,
+                           const int* __restrict__ gdof, const int* __restrict__ pos,
+                           int* __restrict__ gdof_c, int* __restrict__ pos_c,
+                           int* __restrict__ nonuniform) {
+  const int cell = blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= ncells) return;
+  Affine A0, Ac;
+  cell_affine(3, verts, A0);
+  cell_affine(3, verts + (size_t)cell * 8 * 3, Ac);
+  int R[3][3];
+  bool ok = true;
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) {
+      double r = 0.0;
+      for (int q = 0; q < 3; ++q) r += A0.Ji[a][q] * Ac.J[q][b];
+      const double ri = rint(r);
+      if (fabs(r - ri) > 1e-9 || fabs(ri) > 1.0) ok = false;
+      R[a][b] = (int)ri;
+    }
+  for (int a = 0; a < 3 && ok; ++a) {
+    int nr = 0, nc = 0;
+    for (int b = 0; b < 3; ++b) {
+      nr += R[a][b] != 0;
+      nc += R[b][a] != 0;
+    }
+    if (nr != 1 || nc != 1) ok = false;
+  }
+  const size_t o = (size_t)cell * 27;
+  for (int k = 0; k < 27; ++k) {
+    const int xi[3] = {k % 3 - 1, (k / 3) % 3 - 1, k / 9 - 1};
+    int m = k;
+    if (ok) {
+      int xp[3];
+      for (int a = 0; a < 3; ++a) xp[a] = R[a][0] * xi[0] + R[a][1] * xi[1] + R[a][2] * xi[2];
+      m = (xp[0] + 1) + 3 * (xp[1] + 1) + 9 * (xp[2] + 1);
+    }
+    gdof_c[o + m] = gdof[o + k];
+    pos_c[o + m] = pos[o + k];
+  }
+  if (!ok) atomicOr(nonuniform, 1);
+}
+
+// element matrix of cell 0 in FP32, transposed (AeT[j*27 + i] = A_ij): the
+// matrix of every cell of a uniform level, A = sum_t g_t R_t in FP64
+__global__ void k_mf_element(AsmCoefs k, const double* __restrict__ verts,
+                             const double* __restrict__ R, float* __restrict__ AeT) {
+  __shared__ double g0[Terms<3>::NT];
+  if (threadIdx.x == 0) cell_factors<3>(k, verts, g0, 0);
+  __syncthreads();
+  for (int e = threadIdx.x; e < 27 * 27; e += blockDim.x) {
+    double a = 0.0;
+    for (int t = 0; t < Terms<3>::NT; ++t) a += g0[t] * R[(size_t)t * 729 + e];
+    AeT[(e % 27) * 27 + e / 27] = (float)a;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // coupling -> CSR slot map (replaces the reference's linear row search)
 // ---------------------------------------------------------------------------
@@ -737,8 +823,17 @@ __global__ void k_finish_matrix(int n, int nnz, const int* __restrict__ dslot,
                                 const double* __restrict__ val, float* __restrict__ val32,
                                 double* __restrict__ invd, float* __restrict__ invd32,
                                 const int* __restrict__ sell_pos, double* __restrict__ sell_val,
+                                int ndc, const int* __restrict__ dc_pos,
+                                double* __restrict__ dc_val, float* __restrict__ dc_val32,
                                 int* err) {
   long stride = (long)gridDim.x * blockDim.x;
+  // couplings of active rows to non-active columns, contiguous per row (the
+  // first smoothing step reads them without the CSR slot indirection)
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < ndc; t += stride) {
+    const double v = val[dc_pos[t]];
+    dc_val[t] = v;
+    dc_val32[t] = (float)v;
+  }
   for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < nnz; t += stride) {
     const double v = val[t];
     val32[t] = (float)v;
@@ -1324,6 +1419,9 @@ int upload_level(cdg_context* ctx, DevLevel& L) {
     CDG_TRY(dalloc(&L.dc_rp, rp.size()));
     CDG_TRY(dalloc(&L.dc_col, dcol.size()));
     CDG_TRY(dalloc(&L.dc_pos, dpos.size()));
+    CDG_TRY(dalloc(&L.dc_val64, dpos.size()));
+    CDG_TRY(dalloc(&L.dc_val32, dpos.size()));
+    L.dc_n = (int)dpos.size();
     CDG_CUDA(cudaMemcpyAsync(L.dc_rp, rp.data(), rp.size() * sizeof(int), cudaMemcpyHostToDevice, st));
     if (!dcol.empty()) {
       CDG_CUDA(cudaMemcpyAsync(L.dc_col, dcol.data(), dcol.size() * sizeof(int),
@@ -1503,7 +1601,8 @@ int free_level(DevLevel& L) {
                   L.mg_def, L.P_rp, L.P_col, L.P_val, L.P_val32, L.R_rp, L.R_col, L.R_val,
                   L.R_val32, L.coarse_inv, L.coarse_work, L.dc_rp, L.dc_col, L.dc_pos,
                   L.tcd_A, L.tcd_M, L.tcd_f, L.tcd_fold, L.tcd_u2, L.dof_rp, L.dof_ent,
-                  L.rhs_loc};
+                  L.rhs_loc, L.mf_fac, L.mf_y, L.mf_ae, L.mf_gdof, L.mf_pos, L.mf_pos_c,
+                  L.dc_val64, L.dc_val32};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   return CDG_OK;
@@ -1705,7 +1804,8 @@ static int launch_rhs(cdg_context* ctx, const AsmCoefs& k, DevLevel& L, double* 
 static int finish_matrix(cdg_context* ctx, cdg_problem* p, DevLevel& L) {
   int g = (int)std::min<long>(((long)std::max(L.nnz, L.ndof) + 255) / 256, (long)ctx->num_sms * 16);
   CDG_LAUNCH(ctx, k_finish_matrix, g, 256, 0, L.ndof, L.nnz, L.diag_slot, L.val64, L.val32,
-             L.invdiag64, L.invdiag32, L.sell_pos, L.sell_val, p->d_zero_diag);
+             L.invdiag64, L.invdiag32, L.sell_pos, L.sell_val, L.dc_n, L.dc_pos, L.dc_val64,
+             L.dc_val32, p->d_zero_diag);
   return CDG_OK;
 }
 
@@ -1718,6 +1818,43 @@ int assemble_level(cdg_context* ctx, cdg_problem* p, DevLevel& L, const cdg_asse
   CDG_CUDA(cudaMemsetAsync(L.val64, 0, (size_t)L.nnz * sizeof(double), st));
   CDG_CUDA(cudaMemsetAsync(L.rhs, 0, (size_t)L.ndof * sizeof(double), st));
   CDG_TRY(contract(ctx, k, L, p->d_tables, stiffness_set(k), false, L.val64));
+  // the matrix-free FP32 operator takes the same factors (the SUPG term set
+  // has no linear-convection terms, so that combination keeps the CSR path)
+  L.mf_valid = 0;
+  if (mf_eligible(L) && L.mf_mode != 0 && !(k.supg && k.linear_b)) {
+    CDG_TRY(mf_ensure(L));
+    if (L.mf_geo < 0) {
+      // once per level: gather positions, and the cells' frames relative to cell 0
+      CDG_CUDA(cudaMemsetAsync(L.mf_pos, 0xff, (size_t)L.ncells * 27 * sizeof(int), st));
+      CDG_LAUNCH(ctx, k_mf_pos, grid_for<int>(L.nactive, 256), 256, 0, L.nactive, L.dof_rp,
+                 L.dof_ent, L.mf_pos);
+      int* flag = nullptr;
+      CDG_CUDA(cudaMalloc(&flag, sizeof(int)));
+      int nonuni = 1;
+      cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int), st);
+      if (e == cudaSuccess) {
+        k_mf_canon<<<grid_for<int>(L.ncells, 128), 128, 0, st>>>(
+            L.ncells, L.verts, L.gdof, L.mf_pos, L.mf_gdof, L.mf_pos_c, flag);
+        ++ctx->launches;
+        e = cudaGetLastError();
+      }
+      if (e == cudaSuccess) e = cudaMemcpyAsync(&nonuni, flag, sizeof(int), cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      cudaFree(flag);
+      CDG_CUDA(e);
+      L.mf_geo = nonuni ? 0 : 1;
+    }
+    // constant coefficients on translated cells: one element matrix;
+    // otherwise per-cell factors for the sum-factorised kernel
+    L.mf_uniform = L.mf_geo == 1 && !k.linear_b ? 1 : 0;
+    if (L.mf_uniform)
+      CDG_LAUNCH(ctx, k_mf_element, 1, 256, 0, k, L.verts, p->d_tables, L.mf_ae);
+    else
+      CDG_LAUNCH(ctx, k_mf_factors, grid_for<int>(L.ncells, 128), 128, 0, k, L.ncells, L.verts,
+                 L.mf_fac);
+    L.mf_valid = 1;
+    L.mf_lin = k.linear_b;
+  }
   int nd = L.ndof - L.nactive;
   if (nd > 0)
     CDG_LAUNCH(ctx, k_dirichlet_rows, grid_for<int>(nd, 256), 256, 0, L.ndof, L.nactive,
@@ -1791,6 +1928,7 @@ int tcd_assemble_level(cdg_context* ctx, cdg_problem* p, DevLevel& L,
                        double tau) {
   CDG_TRY(ensure_tables(ctx, p));
   CDG_TRY(ensure_tcd(L));
+  L.mf_valid = 0;   // the FP32 operator becomes the time-dependent system
   AsmCoefs k = make_coefs(a, L.shape, L.order);
   k.tcd = 1;
   k.theta1 = theta1;

@@ -41,6 +41,7 @@ enum : int {
   kErrTimeout = 32,    // a bounded wait on a shared-memory barrier ran out
 };
 
+constexpr int kMfFactors = 40;        // per-cell factors of the matrix-free Q2 operator
 constexpr int kRedSlots = 32;         // partial-sum rows (one per inner product)
 constexpr int kRedMaxBlocks = 1024;   // partial sums per reduction
 
@@ -113,6 +114,9 @@ struct DevLevel {
   int* dc_rp = nullptr;
   int* dc_col = nullptr;
   int* dc_pos = nullptr;
+  double* dc_val64 = nullptr;    // their values (refreshed with the FP32 copy)
+  float* dc_val32 = nullptr;
+  int dc_n = 0;
   // multigrid work vectors (double or float, per precision)
   void* mg_rhs = nullptr;
   void* mg_sol = nullptr;
@@ -133,6 +137,25 @@ struct DevLevel {
   double* tcd_f = nullptr;
   double* tcd_fold = nullptr;
   double* tcd_u2 = nullptr;
+  // matrix-free FP32 operator of Q2 hexahedral levels (matfree.cu): the
+  // per-cell factors of A_cell = sum_t g_t R_t in FP32 (cells x kMfFactors)
+  // and the local results of one application, DOF-major (the entries of
+  // active row r at [dof_rp[r], dof_rp[r+1]), cells x 27 at most).  mf_valid:
+  // the factors belong to the operator the FP32 multigrid uses (stationary
+  // assembly); mf_mode: -1 not yet chosen, 0 CSR kernels, 1 matrix-free
+  float* mf_fac = nullptr;
+  float* mf_y = nullptr;
+  int mf_valid = 0;
+  int mf_lin = 0;                // factors of a convection field linear in x
+  int mf_mode = -1;
+  float* mf_ae = nullptr;        // 27 x 27 element matrix of a uniform level (transposed)
+  int* mf_pos = nullptr;         // cells x 27: position of (cell, local DOF) in mf_y, -1 non-active
+  int* mf_gdof = nullptr;        // cells x 27: DOFs in cell 0's local order
+  int* mf_pos_c = nullptr;       // cells x 27: mf_pos in cell 0's local order
+  int mf_geo = -1;               // every cell a translate of cell 0 (-1: not checked)
+  int mf_uniform = 0;            // the last assembly has one element matrix for all cells
+  int mf_blocks_per_sm = 0;      // grid cap of the cell kernel (0: one cell per warp)
+  float tuned_ms[2] = {0.f, 0.f};   // tuner's smoothing-step times: CSR, matrix-free
   // dense inverse of the active block (coarsest multigrid level)
   double* coarse_inv = nullptr;  // na*na
   double* coarse_work = nullptr; // 2 na^2 (Gauss-Jordan ping-pong) + pivots + column map
@@ -237,6 +260,15 @@ int build_slots(cdg_context* ctx, DevLevel& L);
 int assemble_level(cdg_context* ctx, cdg_problem* p, DevLevel& L,
                    const cdg_assembly_params& a);
 int check_device_error(cdg_context* ctx);
+// matrix-free FP32 operator of Q2 hexahedral levels (matfree.cu); mode as
+// k_spmv: 0 y = Ax, 1 y = b - Ax, 2 Jacobi step, 3 Jacobi step + FP64 copy
+bool mf_eligible(const DevLevel& L);
+int mf_ensure(DevLevel& L);
+int mf_apply(cdg_context* ctx, const DevLevel& L, int mode, const float* x, const float* b,
+             const float* invd, float w, float* y, double* z = nullptr, const int* di = nullptr,
+             double* zcur = nullptr);
+// y = A x with the FP32 multigrid operator of a level: 0 CSR, 1 matrix-free
+int apply32(cdg_context* ctx, const DevLevel& L, int variant, const float* x, float* y);
 // argument checks of every entry point that takes assembly parameters
 int check_assembly_params(const cdg_problem* p, const cdg_assembly_params* a);
 int level_errors(cdg_context* ctx, cdg_problem* p, DevLevel& L,

@@ -17,6 +17,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <type_traits>
 
 #include "common.cuh"
 
@@ -1058,6 +1059,7 @@ template <> struct Prec<double> {
   static const double* sell(const DevLevel& L) { return L.sell_val; }
   static bool has_sell(const DevLevel& L) { return L.sell_nslices > 0; }
   static const double* invd(const DevLevel& L) { return L.invdiag64; }
+  static const double* dcv(const DevLevel& L) { return L.dc_val64; }
   static const double* P(const DevLevel& L) { return L.P_val; }
   static const double* R(const DevLevel& L) { return L.R_val; }
 };
@@ -1066,6 +1068,7 @@ template <> struct Prec<float> {
   static const float* sell(const DevLevel&) { return nullptr; }
   static bool has_sell(const DevLevel&) { return false; }   // CSR measured faster in FP32
   static const float* invd(const DevLevel& L) { return L.invdiag32; }
+  static const float* dcv(const DevLevel& L) { return L.dc_val32; }
   static const float* P(const DevLevel& L) { return L.P_val32; }
   static const float* R(const DevLevel& L) { return L.R_val32; }
 };
@@ -1076,10 +1079,19 @@ static int vec_grid(cdg_context* ctx, long n) {
   return (int)(g > cap ? cap : (g < 1 ? 1 : g));
 }
 
+// the FP32 multigrid applies a level's operator matrix-free where the level
+// has valid cell factors and the tuner chose that kernel (matfree.cu)
+template <typename T>
+static bool mf_on(const DevLevel& L) {
+  return std::is_same<T, float>::value && L.mf_valid && L.mf_mode == 1;
+}
+
 // last smoothing step of the finest level with the FP64 hand-over (MODE 3)
 template <typename T>
 static int smooth_out(cdg_context* ctx, const DevLevel& L, const T* val, const T* x, const T* b,
                       const T* invd, T w, T* y, double* z, const int* di, double* zcur) {
+  if constexpr (std::is_same<T, float>::value)
+    if (mf_on<T>(L)) return mf_apply(ctx, L, 3, x, b, invd, w, y, z, di, zcur);
   const int tpr = L.rows_per_warp_hint;
   const int grid = (int)(((long)L.ndof * tpr + 255) / 256);
   switch (tpr) {
@@ -1122,6 +1134,14 @@ static int mg_spmv(cdg_context* ctx, const DevLevel& L, const double* val, const
 
 template <typename T>
 static int smooth(cdg_context* ctx, DevLevel& L, T damp) {
+  if constexpr (std::is_same<T, float>::value) {
+    if (mf_on<T>(L)) {
+      CDG_TRY(mf_apply(ctx, L, 2, (const float*)L.mg_sol, (const float*)L.mg_rhs, L.invdiag32,
+                       damp, (float*)L.mg_tmp));
+      std::swap(L.mg_sol, L.mg_tmp);
+      return CDG_OK;
+    }
+  }
   if (Prec<T>::has_sell(L))
     CDG_TRY((sell_mg<T, 2>(ctx, L, Prec<T>::sell(L), (const T*)L.mg_sol, (const T*)L.mg_rhs,
                            Prec<T>::invd(L), damp, (T*)L.mg_tmp)));
@@ -1138,14 +1158,13 @@ static int smooth(cdg_context* ctx, DevLevel& L, T damp) {
 template <typename T>
 __global__ void __launch_bounds__(256)
 k_first_smooth(int n, int nactive, int with_dirichlet, const int* __restrict__ dc_rp,
-               const int* __restrict__ dc_col, const int* __restrict__ dc_pos,
-               const T* __restrict__ val, const T* __restrict__ b, const T* __restrict__ invd,
-               T w, T* __restrict__ x1) {
+               const int* __restrict__ dc_col, const T* __restrict__ dcv,
+               const T* __restrict__ b, const T* __restrict__ invd, T w, T* __restrict__ x1) {
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     if (i < nactive) {
       T s = 0;
       if (with_dirichlet)
-        for (int k = dc_rp[i]; k < dc_rp[i + 1]; ++k) s += val[dc_pos[k]] * b[dc_col[k]];
+        for (int k = dc_rp[i]; k < dc_rp[i + 1]; ++k) s += dcv[k] * b[dc_col[k]];
       x1[i] = w * (invd[i] * (b[i] - s));
     } else {
       const T x0 = with_dirichlet ? b[i] : (T)0;
@@ -1161,17 +1180,16 @@ k_first_smooth(int n, int nactive, int with_dirichlet, const int* __restrict__ d
 template <typename T>
 __global__ void __launch_bounds__(256)
 k_first_smooth_init(int n, int nactive, const int* __restrict__ dc_rp,
-                    const int* __restrict__ dc_col, const int* __restrict__ dc_pos,
-                    const T* __restrict__ val, const double* __restrict__ v,
-                    const T* __restrict__ invd, T w, T* __restrict__ rhs, T* __restrict__ x1,
-                    const int* di) {
+                    const int* __restrict__ dc_col, const T* __restrict__ dcv,
+                    const double* __restrict__ v, const T* __restrict__ invd, T w,
+                    T* __restrict__ rhs, T* __restrict__ x1, const int* di) {
   if (di) v += (size_t)(*di) * n;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     const T bi = (T)v[i];
     rhs[i] = bi;
     if (i < nactive) {
       T s = 0;
-      for (int k = dc_rp[i]; k < dc_rp[i + 1]; ++k) s += val[dc_pos[k]] * (T)v[dc_col[k]];
+      for (int k = dc_rp[i]; k < dc_rp[i + 1]; ++k) s += dcv[k] * (T)v[dc_col[k]];
       x1[i] = w * (invd[i] * (bi - s));
     } else {
       x1[i] = bi + w * (invd[i] * (bi - bi));
@@ -1182,7 +1200,7 @@ k_first_smooth_init(int n, int nactive, const int* __restrict__ dc_rp,
 template <typename T>
 static int first_smooth(cdg_context* ctx, DevLevel& L, T damp, bool finest) {
   CDG_LAUNCH(ctx, k_first_smooth<T>, vec_grid(ctx, L.ndof), 256, 0, L.ndof, L.nactive,
-             finest ? 1 : 0, L.dc_rp, L.dc_col, L.dc_pos, Prec<T>::val(L), (const T*)L.mg_rhs,
+             finest ? 1 : 0, L.dc_rp, L.dc_col, Prec<T>::dcv(L), (const T*)L.mg_rhs,
              Prec<T>::invd(L), damp, (T*)L.mg_tmp);
   std::swap(L.mg_sol, L.mg_tmp);
   return CDG_OK;
@@ -1190,6 +1208,10 @@ static int first_smooth(cdg_context* ctx, DevLevel& L, T damp, bool finest) {
 
 template <typename T>
 static int defect(cdg_context* ctx, DevLevel& L) {
+  if constexpr (std::is_same<T, float>::value)
+    if (mf_on<T>(L))
+      return mf_apply(ctx, L, 1, (const float*)L.mg_sol, (const float*)L.mg_rhs, nullptr, 0.f,
+                      (float*)L.mg_def);
   if (Prec<T>::has_sell(L))
     return sell_mg<T, 1>(ctx, L, Prec<T>::sell(L), (const T*)L.mg_sol, (const T*)L.mg_rhs,
                          nullptr, (T)0, (T*)L.mg_def);
@@ -1260,7 +1282,7 @@ static int mg_cycle(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s
   const bool fused_start = nl > 1 && s.multigrid_n_pre_smooth > 0;
   if (fused_start) {
     CDG_LAUNCH(ctx, k_first_smooth_init<T>, vec_grid(ctx, F.ndof), 256, 0, F.ndof, F.nactive,
-               F.dc_rp, F.dc_col, F.dc_pos, Prec<T>::val(F), v, Prec<T>::invd(F),
+               F.dc_rp, F.dc_col, Prec<T>::dcv(F), v, Prec<T>::invd(F),
                (T)s.jacobi_damp, (T*)F.mg_rhs, (T*)F.mg_tmp, di);
     std::swap(F.mg_sol, F.mg_tmp);
   } else {
@@ -1360,6 +1382,14 @@ int ensure_mg_vectors(cdg_context* ctx, DevLevel& L, int elem) {
   return CDG_OK;
 }
 
+// y = A x with the FP32 multigrid operator of a level (identity on
+// non-active rows): variant 0 the CSR kernel, 1 the matrix-free kernel
+int apply32(cdg_context* ctx, const DevLevel& L, int variant, const float* x, float* y) {
+  if (variant == 1) return mf_apply(ctx, L, 0, x, nullptr, nullptr, 0.f, y);
+  return spmv_t<float, 0>(ctx, L, L.val32, x, (const float*)nullptr, (const float*)nullptr, 0.f,
+                          y);
+}
+
 int smooth32_once(cdg_context* ctx, DevLevel& L, float damp) {
   CDG_TRY(ensure_mg_vectors(ctx, L, (int)sizeof(float)));
   return smooth<float>(ctx, L, damp);
@@ -1368,6 +1398,43 @@ int smooth32_once(cdg_context* ctx, DevLevel& L, float damp) {
 int defect32_once(cdg_context* ctx, DevLevel& L) {
   CDG_TRY(ensure_mg_vectors(ctx, L, (int)sizeof(float)));
   return defect<float>(ctx, L);
+}
+
+// Per-level kernel choice of the FP32 multigrid, made once per level by
+// timing (CUDA events on the context stream, the level's own vectors): the
+// CSR smoothing step against the matrix-free one.  CDG_MATFREE=0 / =1 in the
+// environment fixes the choice instead.
+static int tune_level(cdg_context* ctx, cdg_problem* p, DevLevel& L) {
+  if (!L.mf_valid || L.mf_mode >= 0) return CDG_OK;
+  const char* env = getenv("CDG_MATFREE");
+  if (env && (env[0] == '0' || env[0] == '1')) {
+    L.mf_mode = env[0] - '0';
+    p->alloc_gen++;
+    return CDG_OK;
+  }
+  cudaEvent_t e0, e1;
+  CDG_CUDA(cudaEventCreate(&e0));
+  CDG_CUDA(cudaEventCreate(&e1));
+  float t[2] = {0.f, 0.f};
+  int rc = CDG_OK;
+  for (int mode = 0; mode < 2 && rc == CDG_OK; ++mode) {
+    L.mf_mode = mode;
+    for (int r = 0; r < 3 && rc == CDG_OK; ++r) rc = smooth<float>(ctx, L, 0.8f);
+    if (rc != CDG_OK) break;
+    cudaEventRecord(e0, ctx->stream);
+    for (int r = 0; r < 10 && rc == CDG_OK; ++r) rc = smooth<float>(ctx, L, 0.8f);
+    cudaEventRecord(e1, ctx->stream);
+    cudaEventSynchronize(e1);
+    cudaEventElapsedTime(&t[mode], e0, e1);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  CDG_TRY(rc);
+  L.mf_mode = t[1] < t[0] ? 1 : 0;
+  L.tuned_ms[0] = t[0] / 10;
+  L.tuned_ms[1] = t[1] / 10;
+  p->alloc_gen++;   // the captured iteration graph holds the kernels of the old choice
+  return CDG_OK;
 }
 
 int prepare_solver(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s) {
@@ -1391,6 +1458,8 @@ int prepare_solver(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s)
   }
   const int elem = s.precision == 1 ? (int)sizeof(float) : (int)sizeof(double);
   for (int k = 0; k < nl; ++k) CDG_TRY(ensure_mg_vectors(ctx, p->lev[k], elem));
+  if (s.precision == 1)
+    for (int k = 0; k + 1 < nl; ++k) CDG_TRY(tune_level(ctx, p, p->lev[k]));
   if (s.multigrid_smoother_coarse == 0) {
     CDG_TRY(coarse_inverse(ctx, p->lev[nl - 1]));
     CDG_TRY(check_device_error(ctx));
@@ -1657,7 +1726,9 @@ static unsigned long long graph_generation(const cdg_problem* p) {
   unsigned long long gen = p->alloc_gen * 1000003ull + (unsigned long long)(uintptr_t)p->ctx;
   for (const DevLevel& L : p->lev)
     gen = gen * 1000003ull + (unsigned long long)L.realloc_count * 7919ull +
-          (unsigned long long)(uintptr_t)L.coarse_inv;
+          (unsigned long long)(uintptr_t)L.coarse_inv +
+          (unsigned long long)(L.mf_valid * 4 + L.mf_uniform * 2 + (L.mf_mode == 1 ? 1 : 0)) *
+              104729ull;
   return gen;
 }
 

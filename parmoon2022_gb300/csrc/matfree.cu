@@ -1,0 +1,328 @@
+// matfree.cu -- matrix-free FP32 operator of the multigrid levels on Q2
+// hexahedra (JacobiSmoother::smooth / calculate_defect without the CSR
+// matrix, src/Multigrid/JacobiSmoother.C:21-29).
+//
+// The assembled element matrix of an affine hexahedron with cell-constant
+// coefficients is A_cell = sum_t g_t R_t (the contraction in assemble.cu):
+// 40 per-cell factors g_t (diffusion + SUPG gradient pairs, convection,
+// reaction, convection linear in x, SUPG reaction, SUPG diffusion-Hessian)
+// times exact reference integrals R_t.  Two kernels apply it:
+//
+// k_mf_uniform: where every cell is a translate of cell 0 and the
+// coefficients are constant (uniform meshes and their affine images), the
+// cells' DOFs are listed in cell 0's local frame once per level, and all
+// cells share cell 0's 27 x 27 element matrix, kept in registers (one row per
+// lane): 27 multiply-adds per lane and cell.
+//
+// k_mf_cell: any affine hexahedra.  Every integrand of a Q2 cell is a
+// polynomial of degree <= 5 per direction, so the 3-point Gauss rule per
+// direction reproduces R_t exactly, and A_cell u is applied by sum
+// factorisation: values, gradients and Hessians of u at the 27 Gauss points
+// by 1D passes (B, B', B'' along each direction), four test fields per point
+// from the factors, and three transposed 1D passes back to the 27 local DOFs
+// -- about 3.3k FP32 multiply-adds per cell.  One warp per cell, lane = Gauss
+// point / local DOF (27 of 32 lanes); the 1D passes exchange values through
+// per-warp shared memory (only __syncwarp, no block barrier).
+//
+// Both write each local result to its position in a DOF-major array (the
+// entries of active row r contiguous, in the fixed (cell, local DOF) order of
+// the rhs gather); k_mf_gather sums a row's range (deterministic, no atomics)
+// and applies the smoothing / defect update.  Non-active rows act as identity
+// rows, as in the CSR kernels.
+#include "common.cuh"
+
+namespace cdg {
+
+namespace {
+
+constexpr int kMfWarps = 8;            // cells in flight per block
+constexpr int kMfBuf = 10;             // per-warp 32-float exchange buffers
+constexpr float kGs = 0.7745966692414834f;   // sqrt(3/5), 3-point Gauss point
+
+// 1D Q2 Lagrange basis on [-1, 1] (nodes -1, 0, 1; local index i):
+// phi_0 = (t^2 - t)/2, phi_1 = 1 - t^2, phi_2 = (t^2 + t)/2,
+// phi'_i = (t - 1/2, -2t, t + 1/2), phi''_i = (1, -2, 1),
+// at the Gauss points t_q = (-sqrt(3/5), 0, sqrt(3/5))
+__device__ __forceinline__ float gpt(int q) { return (float)(q - 1) * kGs; }
+__device__ __forceinline__ float phi(int i, float t) {
+  const float t2 = t * t;
+  return i == 0 ? 0.5f * (t2 - t) : (i == 1 ? 1.0f - t2 : 0.5f * (t2 + t));
+}
+__device__ __forceinline__ float dphi(int i, float t) {
+  return i == 0 ? t - 0.5f : (i == 1 ? -2.0f * t : t + 0.5f);
+}
+__device__ __forceinline__ float gw(int q) { return q == 1 ? 8.0f / 9.0f : 5.0f / 9.0f; }
+
+// row q of B / B' (values at point q) and column i (basis i at all points)
+struct Line {
+  float br[3], dr[3];   // B[q][.], B'[q][.] for this lane's q
+  float bc[3], dc[3];   // B[.][i], B'[.][i] for this lane's i
+};
+__device__ __forceinline__ Line make_line(int l) {
+  Line L;
+  const float t = gpt(l);
+  for (int i = 0; i < 3; ++i) {
+    L.br[i] = phi(i, t);
+    L.dr[i] = dphi(i, t);
+    L.bc[i] = phi(l, gpt(i));
+    L.dc[i] = dphi(l, gpt(i));
+  }
+  return L;
+}
+
+__device__ __forceinline__ float dot3(const float* a, float x0, float x1, float x2) {
+  return fmaf(a[2], x2, fmaf(a[1], x1, a[0] * x0));
+}
+
+// factor offsets (the Terms<3> order of assemble.cu)
+constexpr int kS = 0, kC = 6, kM = 9, kL = 10, kD = 19, kT = 22;
+
+template <bool LIN>
+__global__ void __launch_bounds__(kMfWarps * 32)
+k_mf_cell(int ncells, const int* __restrict__ gdof, const int* __restrict__ pos,
+          const float* __restrict__ fac, const float* __restrict__ x,
+          float* __restrict__ ycell) {
+  __shared__ float sb[kMfWarps][kMfBuf][32];
+  __shared__ float sf[kMfWarps][kMfFactors];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const bool act = lane < 27;
+  const int l0 = lane % 3, l1 = (lane / 3) % 3, l2 = act ? lane / 9 : 0;
+  const Line X0 = make_line(l0), X1 = make_line(l1), X2 = make_line(l2);
+  const float wq = gw(l0) * gw(l1) * gw(l2);
+  float (*B)[32] = sb[warp];
+  float* F = sf[warp];
+  for (int cell = blockIdx.x * kMfWarps + warp; cell < ncells; cell += gridDim.x * kMfWarps) {
+    // factors and local values (lane = local DOF)
+    const float* fc = fac + (size_t)cell * kMfFactors;
+    F[lane] = __ldg(fc + lane);
+    if (lane < kMfFactors - 32) F[32 + lane] = __ldg(fc + 32 + lane);
+    if (act) B[0][lane] = __ldg(x + __ldg(gdof + (size_t)cell * 27 + lane));
+    __syncwarp();
+    // direction 0: lane (q0, i1, i2)
+    if (act) {
+      const float* u = &B[0][3 * l1 + 9 * l2];
+      const float u0 = u[0], u1 = u[1], u2 = u[2];
+      B[1][lane] = dot3(X0.br, u0, u1, u2);
+      B[2][lane] = dot3(X0.dr, u0, u1, u2);
+      B[3][lane] = u0 - 2.0f * u1 + u2;
+    }
+    __syncwarp();
+    // direction 1: lane (q0, q1, i2)
+    if (act) {
+      const int o = l0 + 9 * l2;
+      const float a0 = B[1][o], a1 = B[1][o + 3], a2 = B[1][o + 6];
+      const float d0 = B[2][o], d1 = B[2][o + 3], d2 = B[2][o + 6];
+      const float h0 = B[3][o], h1 = B[3][o + 3], h2 = B[3][o + 6];
+      B[4][lane] = dot3(X1.br, a0, a1, a2);   // B B
+      B[5][lane] = dot3(X1.br, d0, d1, d2);   // B' B
+      B[6][lane] = dot3(X1.dr, a0, a1, a2);   // B B'
+      B[7][lane] = dot3(X1.br, h0, h1, h2);   // B'' B
+      B[8][lane] = a0 - 2.0f * a1 + a2;       // B B''
+      B[9][lane] = dot3(X1.dr, d0, d1, d2);   // B' B'
+    }
+    __syncwarp();
+    // direction 2 and the point values: lane (q0, q1, q2)
+    if (act) {
+      const int o = l0 + 3 * l1;
+      float c[6][3];
+#pragma unroll
+      for (int k = 0; k < 6; ++k)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) c[k][j] = B[4 + k][o + 9 * j];
+      const float u = dot3(X2.br, c[0][0], c[0][1], c[0][2]);
+      const float u_2 = dot3(X2.dr, c[0][0], c[0][1], c[0][2]);
+      const float u_22 = c[0][0] - 2.0f * c[0][1] + c[0][2];
+      const float u_0 = dot3(X2.br, c[1][0], c[1][1], c[1][2]);
+      const float u_02 = dot3(X2.dr, c[1][0], c[1][1], c[1][2]);
+      const float u_1 = dot3(X2.br, c[2][0], c[2][1], c[2][2]);
+      const float u_12 = dot3(X2.dr, c[2][0], c[2][1], c[2][2]);
+      const float u_00 = dot3(X2.br, c[3][0], c[3][1], c[3][2]);
+      const float u_11 = dot3(X2.br, c[4][0], c[4][1], c[4][2]);
+      const float u_01 = dot3(X2.br, c[5][0], c[5][1], c[5][2]);
+      const float g[3] = {u_0, u_1, u_2};
+      const float h[6] = {u_00, u_01, u_02, u_11, u_12, u_22};   // pair order (00,01,02,11,12,22)
+      float f0 = F[kM] * u;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) f0 = fmaf(F[kC + a], g[a], f0);
+      if (LIN) {
+        const float xi[3] = {gpt(l0), gpt(l1), gpt(l2)};
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+          const float s = fmaf(F[kL + 3 * a + 2], xi[2],
+                               fmaf(F[kL + 3 * a + 1], xi[1], F[kL + 3 * a] * xi[0]));
+          f0 = fmaf(s, g[a], f0);
+        }
+      }
+      // symmetric K from the six pair factors
+      const float K00 = F[kS], K01 = F[kS + 1], K02 = F[kS + 2], K11 = F[kS + 3],
+                  K12 = F[kS + 4], K22 = F[kS + 5];
+      float f1 = fmaf(K02, u_2, fmaf(K01, u_1, K00 * u_0));
+      float f2 = fmaf(K12, u_2, fmaf(K11, u_1, K01 * u_0));
+      float f3 = fmaf(K22, u_2, fmaf(K12, u_1, K02 * u_0));
+      f1 = fmaf(F[kD], u, f1);
+      f2 = fmaf(F[kD + 1], u, f2);
+      f3 = fmaf(F[kD + 2], u, f3);
+#pragma unroll
+      for (int s = 0; s < 6; ++s) {
+        f1 = fmaf(F[kT + 3 * s], h[s], f1);
+        f2 = fmaf(F[kT + 3 * s + 1], h[s], f2);
+        f3 = fmaf(F[kT + 3 * s + 2], h[s], f3);
+      }
+      // buffers 0..3 are free: this phase reads 4..9 only
+      B[0][lane] = wq * f0;
+      B[1][lane] = wq * f1;
+      B[2][lane] = wq * f2;
+      B[3][lane] = wq * f3;
+    }
+    __syncwarp();
+    // transposed direction 2: lane (q0, q1, i2)
+    if (act) {
+      const int o = l0 + 3 * l1;
+      float g[4][3];
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) g[k][j] = B[k][o + 9 * j];
+      B[4][lane] = dot3(X2.bc, g[0][0], g[0][1], g[0][2]);   // value path
+      B[5][lane] = dot3(X2.bc, g[1][0], g[1][1], g[1][2]);   // d/dxi_0 path
+      B[6][lane] = dot3(X2.bc, g[2][0], g[2][1], g[2][2]);   // d/dxi_1 path
+      B[7][lane] = dot3(X2.dc, g[3][0], g[3][1], g[3][2]);   // d/dxi_2 path
+    }
+    __syncwarp();
+    // transposed direction 1: lane (q0, i1, i2)
+    if (act) {
+      const int o = l0 + 9 * l2;
+      const float p00 = B[4][o], p01 = B[4][o + 3], p02 = B[4][o + 6];
+      const float p10 = B[5][o], p11 = B[5][o + 3], p12 = B[5][o + 6];
+      const float p20 = B[6][o], p21 = B[6][o + 3], p22 = B[6][o + 6];
+      const float p30 = B[7][o], p31 = B[7][o + 3], p32 = B[7][o + 6];
+      B[0][lane] = dot3(X1.bc, p00 + p30, p01 + p31, p02 + p32) + dot3(X1.dc, p20, p21, p22);
+      B[1][lane] = dot3(X1.bc, p10, p11, p12);
+    }
+    __syncwarp();
+    // transposed direction 0: lane (i0, i1, i2) = local DOF
+    if (act) {
+      const int o = 3 * l1 + 9 * l2;
+      const float y = dot3(X0.bc, B[0][o], B[0][o + 1], B[0][o + 2]) +
+                      dot3(X0.dc, B[1][o], B[1][o + 1], B[1][o + 2]);
+      const int ps = __ldg(pos + (size_t)cell * 27 + lane);
+      if (ps >= 0) ycell[ps] = y;
+    }
+    __syncwarp();   // buffers 0, 1 and the factors are rewritten for the next cell
+  }
+}
+
+// A uniform level (every cell a translate of cell 0, constant coefficients):
+// with each cell's DOFs in cell 0's local order (gdof_c, pos_c), all cells
+// share cell 0's element matrix.  Lane m keeps row m of the 27 x 27 FP32
+// matrix in registers for the whole launch; per cell it gathers one local
+// value, broadcasts the 27 values by shuffles and forms its row's product
+// -- 27 multiply-adds per lane in place of the sum-factorised ~124 and the
+// shared-memory passes -- and stores it at its gather position
+__global__ void __launch_bounds__(256)
+k_mf_uniform(int ncells, const int* __restrict__ gdof_c, const int* __restrict__ pos_c,
+             const float* __restrict__ AeT, const float* __restrict__ x,
+             float* __restrict__ ycell) {
+  const int lane = threadIdx.x & 31;
+  const int il = lane < 27 ? lane : 26;
+  float a[27];
+#pragma unroll
+  for (int j = 0; j < 27; ++j) a[j] = __ldg(AeT + j * 27 + il);
+  const int nw = gridDim.x * (blockDim.x >> 5);
+  for (int cell = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); cell < ncells;
+       cell += nw) {
+    const size_t o = (size_t)cell * 27;
+    float xv = 0.f;
+    int ps = -1;
+    if (lane < 27) {
+      xv = __ldg(x + __ldg(gdof_c + o + lane));
+      ps = __ldg(pos_c + o + lane);
+    }
+    float y = 0.f;
+#pragma unroll
+    for (int j = 0; j < 27; ++j) y = fmaf(a[j], __shfl_sync(0xffffffffu, xv, j), y);
+    if (ps >= 0) ycell[ps] = y;
+  }
+}
+
+// per-row update from the local results (a contiguous range per active
+// row), in the modes of k_spmv:
+//   0: y = A x, 1: y = b - A x, 2: y = x + w D^-1 (b - A x),
+//   3: mode 2, and y also in FP64 into z (block *di when given) and zcur
+template <int MODE>
+__global__ void __launch_bounds__(256)
+k_mf_gather(int n, int nactive, const int* __restrict__ dof_rp,
+            const float* __restrict__ ycell, const float* __restrict__ x,
+            const float* __restrict__ b, const float* __restrict__ invd, float w,
+            float* __restrict__ y, double* __restrict__ z, const int* di,
+            double* __restrict__ zcur) {
+  const int row = blockIdx.x * blockDim.x + threadIdx.x;
+  if (row >= n) return;
+  const float xr = x[row];
+  float s;
+  if (row < nactive) {
+    s = 0.f;
+    const int e1 = dof_rp[row + 1];
+    for (int e = dof_rp[row]; e < e1; ++e) s += ycell[e];
+  } else {
+    s = xr;
+  }
+  if (MODE == 0) {
+    y[row] = s;
+  } else if (MODE == 1) {
+    y[row] = b[row] - s;
+  } else {
+    const float yr = xr + w * (invd[row] * (b[row] - s));
+    y[row] = yr;
+    if (MODE == 3) {
+      const double zr = (double)yr;
+      (di ? z + (size_t)(*di) * n : z)[row] = zr;
+      if (zcur) zcur[row] = zr;
+    }
+  }
+}
+
+}  // namespace
+
+bool mf_eligible(const DevLevel& L) { return L.shape == kHexa && L.order == 2; }
+
+int mf_ensure(DevLevel& L) {
+  if (L.mf_fac) return CDG_OK;
+  CDG_CUDA(cudaMalloc(&L.mf_fac, (size_t)L.ncells * kMfFactors * sizeof(float)));
+  CDG_CUDA(cudaMalloc(&L.mf_y, (size_t)L.ncells * 27 * sizeof(float)));
+  CDG_CUDA(cudaMalloc(&L.mf_ae, 27 * 27 * sizeof(float)));
+  CDG_CUDA(cudaMalloc(&L.mf_pos, (size_t)L.ncells * 27 * sizeof(int)));
+  CDG_CUDA(cudaMalloc(&L.mf_gdof, (size_t)L.ncells * 27 * sizeof(int)));
+  CDG_CUDA(cudaMalloc(&L.mf_pos_c, (size_t)L.ncells * 27 * sizeof(int)));
+  return CDG_OK;
+}
+
+int mf_apply(cdg_context* ctx, const DevLevel& L, int mode, const float* x, const float* b,
+             const float* invd, float w, float* y, double* z, const int* di, double* zcur) {
+  if (!L.mf_valid) {
+    set_error("matrix-free operator used without valid cell factors");
+    return CDG_ERR_ARG;
+  }
+  const int cblocks = (L.ncells + kMfWarps - 1) / kMfWarps;
+  const int cap = ctx->num_sms * L.mf_blocks_per_sm;
+  const int grid = cap > 0 && cblocks > cap ? cap : cblocks;
+  if (L.mf_uniform)
+    CDG_LAUNCH(ctx, k_mf_uniform, grid, kMfWarps * 32, 0, L.ncells, L.mf_gdof, L.mf_pos_c,
+               L.mf_ae, x, L.mf_y);
+  else if (L.mf_lin)
+    CDG_LAUNCH(ctx, k_mf_cell<true>, grid, kMfWarps * 32, 0, L.ncells, L.gdof, L.mf_pos,
+               L.mf_fac, x, L.mf_y);
+  else
+    CDG_LAUNCH(ctx, k_mf_cell<false>, grid, kMfWarps * 32, 0, L.ncells, L.gdof, L.mf_pos,
+               L.mf_fac, x, L.mf_y);
+  const int g2 = (L.ndof + 255) / 256;
+  switch (mode) {
+    case 0: CDG_LAUNCH(ctx, k_mf_gather<0>, g2, 256, 0, L.ndof, L.nactive, L.dof_rp, L.mf_y, x, b, invd, w, y, z, di, zcur); break;
+    case 1: CDG_LAUNCH(ctx, k_mf_gather<1>, g2, 256, 0, L.ndof, L.nactive, L.dof_rp, L.mf_y, x, b, invd, w, y, z, di, zcur); break;
+    case 2: CDG_LAUNCH(ctx, k_mf_gather<2>, g2, 256, 0, L.ndof, L.nactive, L.dof_rp, L.mf_y, x, b, invd, w, y, z, di, zcur); break;
+    default: CDG_LAUNCH(ctx, k_mf_gather<3>, g2, 256, 0, L.ndof, L.nactive, L.dof_rp, L.mf_y, x, b, invd, w, y, z, di, zcur); break;
+  }
+  return CDG_OK;
+}
+
+}  // namespace cdg

@@ -1,0 +1,168 @@
+"""Matrix-free FP32 operator of the Q2 hexahedral multigrid levels.
+
+The mixed-precision multigrid smooths with an FP32 copy of each level's
+operator (JacobiSmoother::smooth, src/Multigrid/JacobiSmoother.C:21-29).  On
+Q2 hexahedra that operator can also be applied without the CSR matrix: by sum
+factorisation from per-cell factors, or, where all cells are translates of
+one cell and the coefficients are constant, from one shared element matrix.
+Bars:
+
+  * the matrix-free product equals the FP32 CSR product and the oracle's FP64
+    product (BlockFEMatrix::apply) to FP32 rounding (2e-5 relative to the
+    largest entry of the active rows; identity on the non-active rows), on
+    every level, for SUPG, Galerkin and a convection field linear in x, on
+    uniform and sheared (still affine) meshes;
+  * a mixed-precision solve with the matrix-free smoother reaches the same
+    1e-10 residual reduction as with the CSR smoother, within two FGMRES
+    iterations of it, with the solution equal to the oracle's to 1e-8 and
+    L2/H1 errors equal to 3 significant digits;
+  * the per-level kernel choice of the tuner is reported and gives the same
+    solve within those bars.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import parmoon2022_gb300 as pg
+import pyoracle as po
+
+pytestmark = pytest.mark.gpu
+
+S3 = 0.57735026918962573
+ROT = ((0.0, -1.0, 0.0), (1.0, 0.0, 0.0), (0.0, 0.0, 0.0))
+
+CASES = {
+    # name: (nref, levels, kwargs shared by the oracle config and the assembly)
+    "supg_polyexp": (3, 2, dict(example=po.EX_POLYEXP, eps=1e-3, b=(S3, S3, S3), c=0.0,
+                                supg=True, sdfem_type=5, cell_measure=2, problem_linear=1)),
+    "supg_sine_sdfem2": (3, 2, dict(example=po.EX_SINE, eps=1e-4, b=(1.0, 0.25, 0.1), c=0.2,
+                                    supg=True, sdfem_type=2)),
+    "galerkin_sine": (3, 2, dict(example=po.EX_SINE, eps=0.1, b=(1.0, 0.3, -0.2), c=0.5)),
+    "galerkin_linear_b": (2, 2, dict(example=po.EX_SINE, eps=1e-2, b=(0.5, -0.5, 0.2),
+                                     b_grad=ROT, c=0.3)),
+}
+
+
+def rel(x, y):
+    return float(np.max(np.abs(x - y)) / max(np.max(np.abs(y)), 1e-300))
+
+
+def gpu_params(kw):
+    return pg.assembly_params(
+        example=kw["example"], eps=kw["eps"], b=kw["b"], c=kw["c"], b_grad=kw.get("b_grad"),
+        space_discretization_type="supg" if kw.get("supg") else "galerkin",
+        sdfem_type=kw.get("sdfem_type", 2), cell_measure=kw.get("cell_measure", 0),
+        problem_linear=kw.get("problem_linear", 0))
+
+
+def oracle_cfg(nref, kw):
+    ok = {k: v for k, v in kw.items() if k != "example"}
+    return po.make_config(3, 2, nref, kw["example"], **ok)
+
+
+def sheared_pair(ctx, nref, levels, kw):
+    """the unit-cube hierarchy with x += 0.3 y: parallelepiped (affine) cells"""
+    h = pg.Hierarchy(3, 2, nref, n_levels=levels)
+    lv = []
+    for l in range(levels):
+        rp, col = h.pattern(l)
+        i = h.info(l)
+        v = h.mesh(l).copy()
+        v[..., 0] += 0.3 * v[..., 1]
+        lv.append(dict(verts=v, dofs=h.dofs(l), gdof=h.dofs(l), ndof=i["ndof"],
+                       nactive=i["nactive"], row_ptr=rp, col=col))
+    gpu = pg.ConvectionDiffusion.from_arrays(ctx, pg.CELL_HEXA, 2, lv)
+    o = po.Problem(oracle_cfg(0, kw), arrays=lv)
+    return gpu, o
+
+
+@pytest.mark.parametrize("sheared", [False, True])
+@pytest.mark.parametrize("name", list(CASES))
+def test_matrix_free_operator_parity(ctx, name, sheared):
+    nref, levels, kw = CASES[name]
+    if sheared:
+        gpu, o = sheared_pair(ctx, nref, levels, kw)
+    else:
+        gpu = pg.ConvectionDiffusion(ctx, pg.Hierarchy(3, 2, nref, n_levels=levels))
+        o = po.Problem(oracle_cfg(nref, kw), levels)
+    gpu.assemble(gpu_params(kw))
+    o.assemble()
+    rng = np.random.default_rng(5)
+    for lvl in range(levels):
+        na = gpu.info(lvl)["nactive"]
+        x = rng.standard_normal(gpu.info(lvl)["ndof"]).astype(np.float32)
+        y_csr = gpu.apply32(x, lvl, 0)
+        y_mf = gpu.apply32(x, lvl, 1)
+        y_ref = o.apply(x.astype(np.float64), lvl)
+        # active rows (the operator proper), relative to their largest entry
+        assert rel(y_mf[:na], y_csr[:na]) < 2e-5, (lvl, rel(y_mf[:na], y_csr[:na]))
+        assert rel(y_mf[:na], y_ref[:na]) < 2e-5, (lvl, rel(y_mf[:na], y_ref[:na]))
+        # non-active rows are identity rows
+        assert np.array_equal(y_mf[na:], x[na:])
+    gpu.close()
+
+
+def test_matrix_free_needs_a_stationary_hexahedral_assembly(ctx):
+    h = pg.Hierarchy(2, 2, 3)
+    gpu = pg.ConvectionDiffusion(ctx, h)
+    gpu.assemble(pg.assembly_params(example=pg.EX_SINE, eps=1.0))
+    with pytest.raises(pg.CdgError) as e:
+        gpu.apply32(np.zeros(h.info(0)["ndof"], np.float32), 0, 1)
+    assert e.value.code == -1
+    gpu.close()
+
+
+def mixed_solver(levels):
+    return pg.solver_params("multigrid", precision="mixed", max_n_iterations=500,
+                            gmres_restart=30, residual_tolerance=0.0, residual_reduction=1e-10,
+                            multigrid_n_levels=levels, multigrid_n_pre_smooth=2,
+                            multigrid_n_post_smooth=2, jacobi_damp=0.8)
+
+
+def solve_with(ctx, nref, levels, kw, env):
+    old = os.environ.get("CDG_MATFREE")
+    if env is None:
+        os.environ.pop("CDG_MATFREE", None)
+    else:
+        os.environ["CDG_MATFREE"] = env
+    try:
+        gpu = pg.ConvectionDiffusion(ctx, pg.Hierarchy(3, 2, nref, n_levels=levels))
+        a = gpu_params(kw)
+        gpu.assemble(a)
+        st = gpu.solve(mixed_solver(levels))
+        out = dict(st=st, x=gpu.solution(), e=gpu.errors(a),
+                   choice=[gpu.tuning(l)[0] for l in range(levels)])
+        gpu.close()
+        return out
+    finally:
+        if old is None:
+            os.environ.pop("CDG_MATFREE", None)
+        else:
+            os.environ["CDG_MATFREE"] = old
+
+
+@pytest.mark.parametrize("name", ["supg_polyexp", "galerkin_sine"])
+def test_mixed_solve_with_matrix_free_smoother(ctx, name):
+    nref, _, kw = CASES[name]
+    levels = 3
+    o = po.Problem(oracle_cfg(nref, kw), levels)
+    o.assemble()
+    it_o, res_o, ini_o = o.solve(po.make_solver("multigrid", max_it=500, restart=30,
+                                                reduction=1e-10, mg_levels=levels, n_pre=2,
+                                                n_post=2, jacobi_damp=0.8))
+    assert res_o <= 1e-10 * ini_o
+    x_o, e_o = o.solution(), o.errors()
+    csr = solve_with(ctx, nref, levels, kw, "0")
+    mf = solve_with(ctx, nref, levels, kw, "1")
+    tuned = solve_with(ctx, nref, levels, kw, None)
+    assert csr["choice"][:2] == [0, 0] and mf["choice"][:2] == [1, 1]
+    assert all(c in (0, 1) for c in tuned["choice"][:levels - 1])
+    for r in (csr, mf, tuned):
+        st = r["st"]
+        assert st.residual <= 1e-10 * st.initial_residual
+        assert abs(st.iterations - csr["st"].iterations) <= 2
+        assert abs(st.iterations - it_o) <= 3
+        assert rel(r["x"], x_o) < 1e-8
+        for k in (0, 1):
+            assert abs(r["e"][k] - e_o[k]) <= 5e-4 * e_o[k]
