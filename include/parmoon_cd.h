@@ -353,6 +353,33 @@ int cdg_problem_prolongate(cdg_problem *p, int fine_level, const double *xc,
 /* GridTransfer::DefectRestriction (fine_level -> fine_level+1) */
 int cdg_problem_restrict(cdg_problem *p, int fine_level, const double *df,
                          double *rc);
+/* ---- coefficients from the caller (the reference's CoeffFct2D/3D) ------ */
+/* An Example_CD2D/3D built from coefficient callbacks
+ * (include/Examples/Example_CD2D.h:67-71) has
+ *   CoeffFct2D/3D(n_points, x, y[, z], params, coeffs)
+ * (include/General/Constants.h:43-47), called by LocalAssembling on the
+ * quadrature points of every cell.  Here the caller asks for the points of a
+ * level, evaluates its callback on them and hands the values back:
+ *
+ * cdg_problem_quadrature_points: *nqp = points per cell of the rule the
+ * assembly uses for a (the rule by degree of the reference's
+ * QuadratureFormulaDatabase, as for the built-in examples); x (may be NULL to
+ * query *nqp) receives n_cells * nqp * dim physical coordinates,
+ * x[(cell * nqp + q) * dim + r].
+ *
+ * cdg_problem_assemble_coefficients: assembles the matrix and rhs of one
+ * level (Galerkin, or SUPG with delta per point from the point's
+ * coefficients, Compute_SDFEM_delta) from coeffs[(cell * nqp + q) * (dim + 3)
+ * + k], k = 0 eps, 1..dim b, dim+1 c, dim+2 f -- the reference's
+ * coefficient vector layout (src/AssembleRoutines/ConvDiff.C:1858-1863).
+ * Dirichlet values come from a->example's boundary data; Neumann parts are
+ * rejected (CDG_ERR_ARG).  Call it once per multigrid level, as the
+ * reference assembles every level; such levels keep the CSR multigrid
+ * kernels. */
+int cdg_problem_quadrature_points(cdg_problem *p, const cdg_assembly_params *a,
+                                  int level, int *nqp, double *x);
+int cdg_problem_assemble_coefficients(cdg_problem *p, const cdg_assembly_params *a,
+                                      int level, const double *coeffs);
 /* y = A x with the FP32 copy of a level's operator that the mixed-precision
  * multigrid smooths with (JacobiSmoother's BlockFEMatrix::apply, identity on
  * non-active rows), host float buffers of n_dofs entries.  variant 0: CSR

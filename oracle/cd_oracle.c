@@ -140,7 +140,66 @@ static void make_tet_rule(int n, quad_rule *q) {
         q->w[q->nqp++] = 0.125 * w[i] * w[j] * w[k] * (1 - u) * (1 - u) * (1 - v);
       }
 }
-static int tet_points_for_degree(int deg) { return (deg + 4) / 2; }
+/* QuadratureFormulaDatabase.C:30-37: degree <= 2 P2Tetra, 3-4 P4Tetra, 5-6
+ * P5Tetra; the rules of QuadFormula.C (P4Tetra :1693, P5Tetra :1739) are
+ * Keast's symmetric rules (Comput. Methods Appl. Mech. Engrg. 55 (1986)
+ * 339-348), written here as orbits in barycentric coordinates: kind 1 the
+ * centroid, 4 the permutations of (a,b,b,b), 6 those of (a,a,b,b); w per
+ * point.  Degrees above 6 fall back to the collapsed Gauss rule. */
+typedef struct { int kind; double a, b, w; } tet_orbit;
+
+static void tet_orbit_add(const tet_orbit *o, quad_rule *q) {
+  double l[4];
+  if (o->kind == 1) {
+    for (int i = 0; i < 4; ++i) l[i] = 0.25;
+    q->xi[q->nqp][0] = l[1]; q->xi[q->nqp][1] = l[2]; q->xi[q->nqp][2] = l[3];
+    q->w[q->nqp++] = o->w;
+    return;
+  }
+  for (int i = 0; i < 4; ++i)
+    for (int j = (o->kind == 4 ? i : i + 1); j < (o->kind == 4 ? i + 1 : 4); ++j) {
+      for (int m = 0; m < 4; ++m) l[m] = o->b;
+      l[i] = o->a;
+      l[j] = o->a;
+      q->xi[q->nqp][0] = l[1]; q->xi[q->nqp][1] = l[2]; q->xi[q->nqp][2] = l[3];
+      q->w[q->nqp++] = o->w;
+    }
+}
+
+static int tet_points_for_degree(int deg) {
+  if (deg <= 2) return 102;
+  if (deg <= 4) return 104;
+  if (deg <= 6) return 105;
+  return (deg + 4) / 2;
+}
+
+static void make_tet_rule_by_code(int code, quad_rule *q) {
+  if (code < 100) {
+    make_tet_rule(code, q);
+    return;
+  }
+  q->nqp = 0;
+  if (code == 102) {
+    const tet_orbit o = {4, 0.585410196624968454461376050311,
+                         0.138196601125010515179541316563, 1.0 / 24.0};
+    tet_orbit_add(&o, q);
+  } else if (code == 104) {
+    const tet_orbit o[3] = {
+        {1, 0.25, 0.25, -74.0 / 5625.0},
+        {4, 11.0 / 14.0, 1.0 / 14.0, 343.0 / 45000.0},
+        {6, 0.399403576166799204996102147462, 0.100596423833200795003897852538,
+         56.0 / 2250.0}};
+    for (int i = 0; i < 3; ++i) tet_orbit_add(&o[i], q);
+  } else {
+    const tet_orbit o[4] = {
+        {4, 0.0, 1.0 / 3.0, 0.602678571428571428571428571428571e-2},
+        {1, 0.25, 0.25, 0.302836780970891758063769725577305e-1},
+        {4, 8.0 / 11.0, 1.0 / 11.0, 0.116452490860289694108936091443380e-1},
+        {6, 0.665501535736642982398804642263025e-1, 0.433449846426335701760119535773697,
+         0.109491415613864593456430191124068e-1}};
+    for (int i = 0; i < 4; ++i) tet_orbit_add(&o[i], q);
+  }
+}
 
 /* ------------------------------------------------------------------------ */
 /* Lagrange tensor basis Q1/Q2, derivatives up to order 2                    */
@@ -314,6 +373,9 @@ struct orc_problem {
   double ttau;      /* THETA1 * CURRENTTIMESTEPLENGTH (Crank-Nicolson: tau/2) */
   double tau, theta1; /* CURRENTTIMESTEPLENGTH and THETA1 (SDFEM types 9-11) */
   int tcd_step;     /* TimeDiscretization::current_step_ */
+  /* coefficients supplied per (cell, quadrature point) by the caller, the
+   * reference's CoeffFct contract; NULL: the example's coefficients */
+  const double *coef_in;
 };
 
 static int nverts(int dim) { return dim == 2 ? 4 : 8; }
@@ -1165,7 +1227,7 @@ orc_problem *orc_create_from_arrays(const orc_config *cfg, int n_levels,
   int nterms = cfg->problem_linear ? 2 : 3;
   if (p->shape == 2) {
     p->nqp1 = tet_points_for_degree(nterms * cfg->order);
-    make_tet_rule(p->nqp1, &p->qr);
+    make_tet_rule_by_code(p->nqp1, &p->qr);
   } else {
     p->nqp1 = gauss_points_for_degree(nterms * cfg->order);
     make_rule(dim, p->nqp1, &p->qr);
@@ -1458,7 +1520,19 @@ int orc_local_system(orc_problem *p, int level, int cell, double *Aloc,
     double x[3];
     affine_map(dim, &A, p->qr.xi[q], x);
     double co[8];
-    coeffs_at(c, x, co);
+    if (p->coef_in) {
+      /* CoeffFct values at this point: eps, b, c, f; the L_inf norm of b that
+       * Compute_SDFEM_delta takes is formed here, as ConvDiff.C:1858-1863
+       * lays out the coefficient vector */
+      const double *ci = p->coef_in + ((size_t)cell * p->qr.nqp + q) * (dim + 3);
+      double binf = 0;
+      for (int k = 0; k < dim + 3; ++k) co[k] = ci[k];
+      for (int a = 0; a < dim; ++a)
+        if (fabs(ci[1 + a]) > binf) binf = fabs(ci[1 + a]);
+      co[dim + 3] = binf;
+    } else {
+      coeffs_at(c, x, co);
+    }
     double Mult = p->qr.w[q] * adet;
     double eps = co[0], b[3] = {co[1], co[2], dim == 3 ? co[3] : 0};
     double react = co[dim + 1], f = co[dim + 2];
@@ -1803,6 +1877,37 @@ static int assemble_level(orc_problem *p, int level) {
     for (int n = L->row_ptr[r]; n < L->row_ptr[r + 1]; ++n)
       if (L->col[n] == r) L->diag[r] = L->val[n];
   return 0;
+}
+
+/* physical coordinates of the quadrature points of every cell of a level,
+ * x[(cell * nqp + q) * dim + r] (the points orc_local_system integrates at) */
+int orc_quadrature_points(const orc_problem *p, int level, int *nqp, double *x) {
+  if (level < 0 || level >= p->nlev) FAIL("level out of range");
+  const level_t *L = &p->lev[level];
+  const int dim = p->cfg.dim;
+  *nqp = p->qr.nqp;
+  if (!x) return 0;
+  for (int cell = 0; cell < L->ncells; ++cell) {
+    affine_t A;
+    cell_affine_s(p->shape, dim, L->verts + (size_t)cell * L->nv * dim, &A);
+    for (int q = 0; q < p->qr.nqp; ++q)
+      affine_map(dim, &A, p->qr.xi[q], x + ((size_t)cell * p->qr.nqp + q) * dim);
+  }
+  return 0;
+}
+
+/* ConvectionDiffusion::assemble of one level with the coefficients given per
+ * (cell, quadrature point), co[(cell * nqp + q) * (dim + 3) + k]: k = 0 eps,
+ * 1..dim b, dim+1 c, dim+2 f (the CoeffFct2D/3D output,
+ * include/General/Constants.h:43-47); boundary values from the example */
+int orc_assemble_coefficients(orc_problem *p, int level, const double *co) {
+  if (level < 0 || level >= p->nlev) FAIL("level out of range");
+  if (check_sdfem(&p->cfg, 0)) return -1;
+  p->asm_gen++;
+  p->coef_in = co;
+  int rc = assemble_level(p, level);
+  p->coef_in = NULL;
+  return rc;
 }
 
 int orc_assemble(orc_problem *p) {

@@ -116,6 +116,13 @@ int orc_set_solution(orc_problem *p, const double *sol);
 
 /* ConvectionDiffusion<d>::assemble over all levels */
 int orc_assemble(orc_problem *p);
+/* quadrature points of every cell of a level (physical coordinates,
+ * x[(cell * nqp + q) * dim + r]); x == NULL returns *nqp only */
+int orc_quadrature_points(const orc_problem *p, int level, int *nqp, double *x);
+/* assemble one level with coefficients per (cell, quadrature point):
+ * co[(cell * nqp + q) * (dim + 3) + k], k = 0 eps, 1..dim b, dim+1 c,
+ * dim+2 f (CoeffFct2D/3D, include/General/Constants.h:43-47) */
+int orc_assemble_coefficients(orc_problem *p, int level, const double *co);
 /* local matrix and rhs of one cell of one level (before scatter) */
 int orc_local_system(orc_problem *p, int level, int cell, double *A, double *f);
 /* y = A x on active rows, identity on non-active rows (BlockFEMatrix::apply) */

@@ -93,6 +93,8 @@ def lib():
             ("orc_tcd_step", [P, ctypes.c_double, ctypes.c_double,
                               ctypes.POINTER(SolverConfig), ip, dp, dp]),
             ("orc_get_tcd_matrix", [P, ctypes.c_int, ctypes.c_int, dp]),
+            ("orc_quadrature_points", [P, ctypes.c_int, ip, dp]),
+            ("orc_assemble_coefficients", [P, ctypes.c_int, dp]),
         ]:
             f = getattr(L, name)
             f.restype = ctypes.c_int
@@ -286,6 +288,21 @@ class Problem:
         e = np.zeros(5)
         self._chk(lib().orc_errors(self.h, _dp(e)))
         return e
+
+    def quadrature_points(self, level=0):
+        """(ncells, nqp, dim) physical quadrature points of a level"""
+        nq = np.zeros(1, dtype=np.int32)
+        self._chk(lib().orc_quadrature_points(self.h, level, _ip(nq), None))
+        i = self.info(level)
+        x = np.zeros((i["ncells"], int(nq[0]), self.cfg.dim))
+        self._chk(lib().orc_quadrature_points(self.h, level, _ip(nq), _dp(x)))
+        return x
+
+    def assemble_coefficients(self, level, coeffs):
+        """assemble one level with coeffs (ncells, nqp, dim + 3): eps, b, c, f
+        per quadrature point"""
+        co = np.ascontiguousarray(coeffs, dtype=np.float64)
+        self._chk(lib().orc_assemble_coefficients(self.h, level, _dp(co)))
 
     def tcd_initialize(self):
         self._chk(lib().orc_tcd_initialize(self.h))

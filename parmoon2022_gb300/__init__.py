@@ -53,6 +53,7 @@ EXPORTED = [
     "cdg_problem_tcd_step", "cdg_problem_get_tcd_matrix", "cdg_server_create",
     "cdg_server_destroy", "cdg_request_ndof", "cdg_server_submit", "cdg_server_wait",
     "cdg_server_counters", "cdg_problem_apply32", "cdg_problem_tuning",
+    "cdg_problem_quadrature_points", "cdg_problem_assemble_coefficients",
 ]
 
 
@@ -170,6 +171,10 @@ def lib():
             "cdg_problem_get_slots": [P, ctypes.c_int, ip],
             "cdg_problem_apply": [P, ctypes.c_int, dp, dp],
             "cdg_problem_tuning": [P, ctypes.c_int, ip, dp],
+            "cdg_problem_quadrature_points": [P, ctypes.POINTER(AssemblyParams), ctypes.c_int,
+                                              ip, dp],
+            "cdg_problem_assemble_coefficients": [P, ctypes.POINTER(AssemblyParams),
+                                                  ctypes.c_int, dp],
             "cdg_problem_apply32": [P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float),
                                     ctypes.POINTER(ctypes.c_float)],
             "cdg_problem_prolongate": [P, ctypes.c_int, dp, dp],
@@ -453,6 +458,7 @@ class ConvectionDiffusion:
         _chk(lib().cdg_problem_create(ctx.c, hierarchy.h, ctypes.byref(p)))
         self.p = p
         self.n_levels = hierarchy.n_levels
+        self.dim = hierarchy.dim
         ctx._problems.add(self)
 
     @classmethod
@@ -462,6 +468,7 @@ class ConvectionDiffusion:
         (ncells,nloc), ndof, nactive, row_ptr, col, optional parent."""
         self = cls.__new__(cls)
         self.ctx, self.hier, self.n_levels = ctx, None, len(levels)
+        self.dim = 2 if cell_type == CELL_QUAD else 3
         n = len(levels)
         keep = []
 
@@ -597,6 +604,24 @@ class ConvectionDiffusion:
         y = np.zeros_like(x)
         _chk(lib().cdg_problem_apply(self.p, level, _dp(x), _dp(y)))
         return y
+
+    def quadrature_points(self, a, level=0):
+        """(ncells, nqp, dim): physical quadrature points of a level, where the
+        caller evaluates its coefficient function"""
+        nq = ctypes.c_int(0)
+        _chk(lib().cdg_problem_quadrature_points(self.p, ctypes.byref(a), level,
+                                                 ctypes.byref(nq), None))
+        i = self.info(level)
+        x = np.zeros((i["ncells"], nq.value, self.dim))
+        _chk(lib().cdg_problem_quadrature_points(self.p, ctypes.byref(a), level,
+                                                 ctypes.byref(nq), _dp(x)))
+        return x
+
+    def assemble_coefficients(self, a, level, coeffs):
+        """assemble one level from coeffs (ncells, nqp, dim + 3): eps, b, c, f
+        at every quadrature point (the reference's CoeffFct output)"""
+        co = np.ascontiguousarray(coeffs, dtype=np.float64)
+        _chk(lib().cdg_problem_assemble_coefficients(self.p, ctypes.byref(a), level, _dp(co)))
 
     def tuning(self, level=0):
         """(choice, (ms_csr, ms_matfree)): the FP32 multigrid kernel of a

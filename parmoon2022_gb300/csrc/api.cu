@@ -798,6 +798,25 @@ int cdg_problem_apply(cdg_problem* p, int level, const double* x, double* y) {
   return d2h(p->ctx, y, dy.d, (size_t)L->ndof * sizeof(double));
 }
 
+int cdg_problem_quadrature_points(cdg_problem* p, const cdg_assembly_params* a, int level,
+                                  int* nqp, double* x) {
+  CDG_TRY(check_assembly_params(p, a));
+  DevLevel* L = get_level(p, level);
+  if (!L || !nqp) { set_error("bad arguments"); return CDG_ERR_ARG; }
+  return level_quadrature_points(*L, *a, nqp, x);
+}
+
+int cdg_problem_assemble_coefficients(cdg_problem* p, const cdg_assembly_params* a, int level,
+                                      const double* coeffs) {
+  CDG_TRY(check_assembly_params(p, a));
+  DevLevel* L = get_level(p, level);
+  if (!L || !coeffs) { set_error("bad arguments"); return CDG_ERR_ARG; }
+  CDG_CUDA(cudaSetDevice(p->ctx->device));
+  CDG_CUDA(cudaMemsetAsync(p->d_zero_diag, 0, sizeof(int), p->ctx->stream));
+  CDG_TRY(assemble_level_coefficients(p->ctx, p, *L, *a, coeffs));
+  return check_device_error(p->ctx);
+}
+
 int cdg_problem_tuning(cdg_problem* p, int level, int* choice, double* ms) {
   DevLevel* L = get_level(p, level);
   if (!L || !choice) { set_error("bad arguments"); return CDG_ERR_ARG; }

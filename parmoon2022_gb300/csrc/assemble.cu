@@ -81,8 +81,8 @@ static AsmCoefs make_coefs(const cdg_assembly_params& a, int shape, int order) {
   const int nterms = a.problem_linear ? 2 : 3;
   const int deg = nterms * order;
   if (shape == kTetra) {
-    k.nqp1 = tetra_points_for_degree(deg);
-    k.nqp = k.nqp1 * k.nqp1 * k.nqp1;
+    k.nqp1 = tetra_points_for_degree(deg);   // the reference's rule by degree
+    k.nqp = tetra_rule_size(k.nqp1);
   } else {
     k.nqp1 = gauss_points_for_degree(deg);
     k.nqp = k.dim == 2 ? k.nqp1 * k.nqp1 : k.nqp1 * k.nqp1 * k.nqp1;
@@ -1801,6 +1801,171 @@ static int launch_rhs(cdg_context* ctx, const AsmCoefs& k, DevLevel& L, double* 
   return CDG_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Assembly with coefficients given per (cell, quadrature point): the
+// reference's per-point loop for a CoeffFct2D/3D example (GetLocalForms,
+// BilinearAssembleGalerkin and BilinearAssemble_SD, ConvDiff.C:1776-1999,
+// with Compute_SDFEM_delta taking the point's coefficients).  The contraction
+// above needs cell-constant coefficients; this kernel takes any field.  One
+// block per cell (grid-stride), 128 threads: the physical basis values of a
+// point (value, gradient, Laplacian through the affine map) go to shared
+// memory, every thread accumulates its entries of the local matrix over the
+// points, and the entries of active rows are added into the CSR values
+// through the slot map.  coef[(cell * nqp + q) * (DIM + 3) + k]: k = 0 eps,
+// 1..DIM b, DIM+1 c, DIM+2 f.
+// ---------------------------------------------------------------------------
+struct QpTables {
+  const double* w;      // nqp
+  const double* xi;     // nqp * 3
+  const double* val;    // nqp * nloc
+  const double* grad;   // nqp * dim * nloc
+  const double* hess;   // nqp * nsym * nloc (pairs (00,01,11) / (00,01,02,11,12,22))
+  int nqp;
+};
+
+constexpr int kCoefThreads = 128;
+
+template <int DIM>
+__global__ void __launch_bounds__(kCoefThreads)
+k_coef_element(AsmCoefs k, int ncells, int nactive, const double* __restrict__ verts,
+               const int* __restrict__ gdof, const int* __restrict__ slot, QpTables tb,
+               const double* __restrict__ coef, double* __restrict__ val,
+               double* __restrict__ rhs, double* __restrict__ loc) {
+  constexpr int NSYM = DIM == 2 ? 3 : 6;
+  constexpr int NACC = (kMaxLoc * kMaxLoc + kCoefThreads - 1) / kCoefThreads;
+  __shared__ double ph[kMaxLoc][DIM + 2];   // phi, grad phi (physical), laplacian
+  __shared__ double cq[DIM + 5];            // eps, b, c, f, delta, w |det J|
+  __shared__ Affine A;
+  __shared__ double hK;
+  const int NV = k.shape == kHexa ? 8 : 4;
+  const int nl = k.nloc, ne = nl * nl, tid = threadIdx.x;
+  for (int cell = blockIdx.x; cell < ncells; cell += gridDim.x) {
+    const double* cv = verts + (size_t)cell * NV * DIM;
+    if (tid == 0) {
+      cell_affine_s(k.shape, DIM, cv, A);
+      hK = cell_hK_s(k.shape, DIM, cv, k.cell_measure, A.det);
+    }
+    __syncthreads();
+    double acc[NACC], facc = 0.0;
+#pragma unroll
+    for (int m = 0; m < NACC; ++m) acc[m] = 0.0;
+    for (int q = 0; q < tb.nqp; ++q) {
+      if (tid < nl) {
+        const int i = tid;
+        ph[i][0] = tb.val[q * nl + i];
+        for (int r = 0; r < DIM; ++r) {
+          double s = 0.0;
+          for (int a = 0; a < DIM; ++a) s += A.Ji[a][r] * tb.grad[(q * DIM + a) * nl + i];
+          ph[i][1 + r] = s;
+        }
+        // Laplacian of the affine image: sum_r J^-T H J^-1 (r, r)
+        double H[3][3];
+        int pr = 0;
+        for (int a = 0; a < DIM; ++a)
+          for (int b = a; b < DIM; ++b) {
+            H[a][b] = H[b][a] = tb.hess[(q * NSYM + pr) * nl + i];
+            ++pr;
+          }
+        double l = 0.0;
+        for (int r = 0; r < DIM; ++r)
+          for (int a = 0; a < DIM; ++a)
+            for (int b = 0; b < DIM; ++b) l += A.Ji[a][r] * A.Ji[b][r] * H[a][b];
+        ph[i][DIM + 1] = l;
+      } else if (tid == 32) {
+        const double* ci = coef + ((size_t)cell * tb.nqp + q) * (DIM + 3);
+        double bq[3] = {0.0, 0.0, 0.0}, linfb = 0.0;
+        for (int a = 0; a < DIM + 3; ++a) cq[a] = ci[a];
+        for (int a = 0; a < DIM; ++a) {
+          bq[a] = ci[1 + a];
+          linfb = fmax(linfb, fabs(bq[a]));
+        }
+        cq[DIM + 3] = k.supg ? sdfem_delta(k, cv, hK, ci[0], bq, ci[DIM + 1], linfb) : 0.0;
+        cq[DIM + 4] = tb.w[q] * fabs(A.det);
+      }
+      __syncthreads();
+      const double eps = cq[0], c = cq[DIM + 1], f = cq[DIM + 2], delta = cq[DIM + 3];
+      const double mult = cq[DIM + 4];
+#pragma unroll
+      for (int m = 0; m < NACC; ++m) {
+        const int e = tid + m * kCoefThreads;
+        if (e >= ne) break;
+        const int i = e / nl, j = e - i * nl;
+        double gg = 0.0, bgj = 0.0, bgi = 0.0;
+        for (int r = 0; r < DIM; ++r) {
+          gg += ph[i][1 + r] * ph[j][1 + r];
+          bgj += cq[1 + r] * ph[j][1 + r];
+          bgi += cq[1 + r] * ph[i][1 + r];
+        }
+        // Galerkin: eps grad phi_j . grad phi_i + (b . grad phi_j) phi_i + c phi_j phi_i
+        double v = eps * gg + bgj * ph[i][0] + c * ph[j][0] * ph[i][0];
+        // SUPG: delta (-eps lap phi_j + b . grad phi_j + c phi_j) (b . grad phi_i)
+        if (delta != 0.0) v += delta * bgi * (-eps * ph[j][DIM + 1] + bgj + c * ph[j][0]);
+        acc[m] = fma(mult, v, acc[m]);
+      }
+      if (tid < nl) {
+        double bgi = 0.0;
+        for (int r = 0; r < DIM; ++r) bgi += cq[1 + r] * ph[tid][1 + r];
+        facc = fma(mult * f, ph[tid][0] + delta * bgi, facc);
+      }
+      __syncthreads();   // ph and cq are rewritten for the next point
+    }
+#pragma unroll
+    for (int m = 0; m < NACC; ++m) {
+      const int e = tid + m * kCoefThreads;
+      if (e >= ne) break;
+      const int row = gdof[(size_t)cell * nl + e / nl];
+      if (row < nactive) atomicAdd(val + slot[(size_t)cell * ne + e], acc[m]);
+    }
+    if (tid < nl) {
+      const int row = gdof[(size_t)cell * nl + tid];
+      loc[(size_t)cell * nl + tid] = facc;
+      if (row >= nactive) {
+        // Dirichlet value at the node from the example's boundary data
+        double r[3], x[3], u[6];
+        ref_node_s(k.shape, DIM, k.order, tid, r);
+        for (int rr = 0; rr < DIM; ++rr) {
+          double sx = A.x0[rr];
+          for (int a = 0; a < DIM; ++a) sx += A.J[rr][a] * r[a];
+          x[rr] = sx;
+        }
+        ex_exact(k, x, u);
+        rhs[row] = u[0];
+      }
+    }
+    __syncthreads();   // A and hK are rewritten for the next cell
+  }
+}
+
+static RefTables coef_tables(const DevLevel& L, const AsmCoefs& k, std::vector<double>* hess) {
+  RefTables t = make_ref_tables(L.dim, L.order, k.nqp1, L.shape);
+  const int nl = t.nloc, ns = L.dim == 2 ? 3 : 6;
+  hess->assign((size_t)t.nqp * ns * nl, 0.0);
+  std::vector<double> v(nl), g(3 * nl), h(6 * nl);
+  for (int q = 0; q < t.nqp; ++q) {
+    if (L.shape == kTetra)
+      tetra_basis_point(L.order, &t.xi[3 * q], v.data(), g.data(), h.data());
+    else
+      ref_basis_point(L.dim, L.order, &t.xi[3 * q], v.data(), g.data(), h.data());
+    for (int s2 = 0; s2 < ns; ++s2)
+      for (int i = 0; i < nl; ++i) (*hess)[((size_t)q * ns + s2) * nl + i] = h[(size_t)s2 * nl + i];
+  }
+  return t;
+}
+
+int level_quadrature_points(const DevLevel& L, const cdg_assembly_params& a, int* nqp,
+                            double* x) {
+  AsmCoefs k = make_coefs(a, L.shape, L.order);
+  RefTables t = make_ref_tables(L.dim, L.order, k.nqp1, L.shape);
+  *nqp = t.nqp;
+  if (!x) return CDG_OK;
+  const int nv = L.mesh.nv, dim = L.dim;
+  for (int c = 0; c < L.ncells; ++c)
+    for (int q = 0; q < t.nqp; ++q)
+      cell_point(L.shape, dim, &L.mesh.verts[(size_t)c * nv * dim], &t.xi[3 * q],
+                 x + ((size_t)c * t.nqp + q) * dim);
+  return CDG_OK;
+}
+
 static int finish_matrix(cdg_context* ctx, cdg_problem* p, DevLevel& L) {
   int g = (int)std::min<long>(((long)std::max(L.nnz, L.ndof) + 255) / 256, (long)ctx->num_sms * 16);
   CDG_LAUNCH(ctx, k_finish_matrix, g, 256, 0, L.ndof, L.nnz, L.diag_slot, L.val64, L.val32,
@@ -1864,6 +2029,71 @@ int assemble_level(cdg_context* ctx, cdg_problem* p, DevLevel& L, const cdg_asse
     CDG_LAUNCH(ctx, k_copy_nonactive, grid_for<int>(nd, 256), 256, 0, L.ndof, L.nactive, L.rhs,
                L.sol);
   return finish_matrix(ctx, p, L);
+}
+
+// one level with coefficients per (cell, quadrature point) (the generic
+// CoeffFct path); the matrix-free operator is not used for such a level
+int assemble_level_coefficients(cdg_context* ctx, cdg_problem* p, DevLevel& L,
+                                const cdg_assembly_params& a, const double* coef_host) {
+  AsmCoefs k = make_coefs(a, L.shape, L.order);
+  CDG_TRY(check_coefs(k));
+  if (k.neumann_mask) {
+    set_error("Neumann boundary parts take their data from the example; the per-point "
+              "coefficient assembly handles Dirichlet boundaries only");
+    return CDG_ERR_ARG;
+  }
+  std::vector<double> hess;
+  RefTables t = coef_tables(L, k, &hess);
+  const int ncoef = L.dim + 3;
+  const size_t ncoefs = (size_t)L.ncells * t.nqp * ncoef;
+  const size_t ntab = t.w.size() + t.xi.size() + t.val.size() + t.grad.size() + hess.size();
+  cudaStream_t st = ctx->stream;
+  double* buf = nullptr;
+  CDG_TRY(dalloc(&buf, ntab + ncoefs));
+  double* d = buf;
+  QpTables tb;
+  auto put = [&](const std::vector<double>& v) {
+    cudaMemcpyAsync(d, v.data(), v.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+    const double* r = d;
+    d += v.size();
+    return r;
+  };
+  tb.w = put(t.w);
+  tb.xi = put(t.xi);
+  tb.val = put(t.val);
+  tb.grad = put(t.grad);
+  tb.hess = put(hess);
+  tb.nqp = t.nqp;
+  cudaError_t e = cudaMemcpyAsync(d, coef_host, ncoefs * sizeof(double), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) {
+    cudaFree(buf);
+    CDG_CUDA(e);
+  }
+  L.mf_valid = 0;
+  CDG_CUDA(cudaMemsetAsync(L.val64, 0, (size_t)L.nnz * sizeof(double), st));
+  CDG_CUDA(cudaMemsetAsync(L.rhs, 0, (size_t)L.ndof * sizeof(double), st));
+  const int g = std::max(1, std::min(L.ncells, ctx->num_sms * 8));
+  if (L.dim == 2)
+    CDG_LAUNCH(ctx, k_coef_element<2>, g, kCoefThreads, 0, k, L.ncells, L.nactive, L.verts,
+               L.gdof, L.slot, tb, d, L.val64, L.rhs, L.rhs_loc);
+  else
+    CDG_LAUNCH(ctx, k_coef_element<3>, g, kCoefThreads, 0, k, L.ncells, L.nactive, L.verts,
+               L.gdof, L.slot, tb, d, L.val64, L.rhs, L.rhs_loc);
+  const int nd = L.ndof - L.nactive;
+  if (nd > 0)
+    CDG_LAUNCH(ctx, k_dirichlet_rows, grid_for<int>(nd, 256), 256, 0, L.ndof, L.nactive,
+               L.diag_slot, L.val64);
+  if (L.nactive > 0)
+    CDG_LAUNCH(ctx, k_rhs_gather, (int)std::min<long>((L.nactive + 255) / 256, (long)ctx->num_sms * 16),
+               256, 0, L.nactive, L.dof_rp, L.dof_ent, L.rhs_loc, L.rhs);
+  if (nd > 0)
+    CDG_LAUNCH(ctx, k_copy_nonactive, grid_for<int>(nd, 256), 256, 0, L.ndof, L.nactive, L.rhs,
+               L.sol);
+  CDG_TRY(finish_matrix(ctx, p, L));
+  e = cudaStreamSynchronize(st);   // the tables and coefficients are released
+  cudaFree(buf);
+  CDG_CUDA(e);
+  return CDG_OK;
 }
 
 int level_errors(cdg_context* ctx, cdg_problem* p, DevLevel& L, const cdg_assembly_params& a,

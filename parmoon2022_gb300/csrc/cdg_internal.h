@@ -85,9 +85,12 @@ struct RefTables {
   std::vector<double> grad; // nqp * dim * nloc  d_a phi
 };
 RefTables make_ref_tables(int dim, int order, int nqp1, int shape);
-// points per direction of the collapsed Gauss rule that integrates degree
-// `degree` exactly on the reference tetrahedron
+// the reference tetrahedron's quadrature rule for `degree` (above kTetraRule:
+// the reference's Keast rule, kTetraRule + its degree; else points per
+// direction of a collapsed Gauss rule)
+constexpr int kTetraRule = 100;
 int tetra_points_for_degree(int degree);
+int tetra_rule_size(int code);   // points of that rule
 
 void ref_basis_point(int dim, int order, const double* xi, double* val,
                      double* grad /* dim*nloc */, double* hess /* sym */);

@@ -269,6 +269,12 @@ int mf_apply(cdg_context* ctx, const DevLevel& L, int mode, const float* x, cons
              double* zcur = nullptr);
 // y = A x with the FP32 multigrid operator of a level: 0 CSR, 1 matrix-free
 int apply32(cdg_context* ctx, const DevLevel& L, int variant, const float* x, float* y);
+// generic coefficients (CoeffFct): quadrature points of a level (host) and the
+// assembly with eps, b, c, f per (cell, point)
+int level_quadrature_points(const DevLevel& L, const cdg_assembly_params& a, int* nqp,
+                            double* x);
+int assemble_level_coefficients(cdg_context* ctx, cdg_problem* p, DevLevel& L,
+                                const cdg_assembly_params& a, const double* coef_host);
 // argument checks of every entry point that takes assembly parameters
 int check_assembly_params(const cdg_problem* p, const cdg_assembly_params* a);
 int level_errors(cdg_context* ctx, cdg_problem* p, DevLevel& L,

@@ -207,12 +207,91 @@ void ref_basis_point(int dim, int p, const double* xi, double* val, double* grad
   }
 }
 
+// Quadrature on the reference tetrahedron by degree, as the reference picks it
+// (QuadratureFormulaDatabase.C:30-37): degree <= 2 P2Tetra, 3-4 P4Tetra, 5-6
+// P5Tetra (QuadFormula.C:1693,1739) -- Keast's symmetric rules (P. Keast,
+// Moderate-degree tetrahedral quadrature formulas, Comput. Methods Appl. Mech.
+// Engrg. 55 (1986) 339-348) with 4, 11 and 15 points.  They are returned as
+// the code kTetraRule + degree of the rule; degrees above 6 (no element here
+// needs them) take the collapsed Gauss rule below with (degree + 4) / 2
+// points per direction.
+int tetra_points_for_degree(int degree) {
+  if (degree <= 2) return kTetraRule + 2;
+  if (degree <= 4) return kTetraRule + 4;
+  if (degree <= 6) return kTetraRule + 5;
+  return (degree + 4) / 2;
+}
+
+int tetra_rule_size(int code) {
+  if (code == kTetraRule + 2) return 4;
+  if (code == kTetraRule + 4) return 11;
+  if (code == kTetraRule + 5) return 15;
+  return code * code * code;
+}
+
+namespace {
+// one orbit of a symmetric rule in barycentric coordinates (l0, l1, l2, l3):
+// kind 1 the centroid, kind 4 the permutations of (a, b, b, b), kind 6 those
+// of (a, a, b, b); w the weight of each point (the weights sum to 1/6)
+struct TetOrbit {
+  int kind;
+  double a, b, w;
+};
+void add_orbit(const TetOrbit& o, std::vector<double>& pts, std::vector<double>& wts) {
+  auto put = [&](const double l[4]) {
+    pts.push_back(l[1]);
+    pts.push_back(l[2]);
+    pts.push_back(l[3]);
+    wts.push_back(o.w);
+  };
+  if (o.kind == 1) {
+    const double l[4] = {0.25, 0.25, 0.25, 0.25};
+    put(l);
+  } else if (o.kind == 4) {
+    for (int i = 0; i < 4; ++i) {
+      double l[4] = {o.b, o.b, o.b, o.b};
+      l[i] = o.a;
+      put(l);
+    }
+  } else {
+    for (int i = 0; i < 4; ++i)
+      for (int j = i + 1; j < 4; ++j) {
+        double l[4] = {o.b, o.b, o.b, o.b};
+        l[i] = l[j] = o.a;
+        put(l);
+      }
+  }
+}
+}  // namespace
+
+static void keast_rule(int degree, std::vector<double>& pts, std::vector<double>& wts) {
+  pts.clear();
+  wts.clear();
+  if (degree == 2) {
+    add_orbit({4, 0.585410196624968454461376050311, 0.138196601125010515179541316563,
+               1.0 / 24.0}, pts, wts);
+  } else if (degree == 4) {
+    add_orbit({1, 0.25, 0.25, -74.0 / 5625.0}, pts, wts);
+    add_orbit({4, 11.0 / 14.0, 1.0 / 14.0, 343.0 / 45000.0}, pts, wts);
+    add_orbit({6, 0.399403576166799204996102147462, 0.100596423833200795003897852538,
+               56.0 / 2250.0}, pts, wts);
+  } else {
+    add_orbit({4, 0.0, 1.0 / 3.0, 0.602678571428571428571428571428571e-2}, pts, wts);
+    add_orbit({1, 0.25, 0.25, 0.302836780970891758063769725577305e-1}, pts, wts);
+    add_orbit({4, 8.0 / 11.0, 1.0 / 11.0, 0.116452490860289694108936091443380e-1}, pts, wts);
+    add_orbit({6, 0.665501535736642982398804642263025e-1, 0.433449846426335701760119535773697,
+               0.109491415613864593456430191124068e-1}, pts, wts);
+  }
+}
+
 // collapsed (Duffy) Gauss rule on the reference tetrahedron with n points per
 // direction: xi = u, eta = v (1-u), zeta = w (1-u)(1-v), exact for degree
-// <= 2n-3
-int tetra_points_for_degree(int degree) { return (degree + 4) / 2; }
-
+// <= 2n-3 (the exact reference tensors take it with n = 5)
 static void tetra_rule(int n, std::vector<double>& pts, std::vector<double>& wts) {
+  if (n > kTetraRule) {
+    keast_rule(n - kTetraRule, pts, wts);
+    return;
+  }
   double x[kMaxQp1], w[kMaxQp1];
   gauss_legendre(n, x, w);
   pts.clear();

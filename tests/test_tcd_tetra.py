@@ -52,6 +52,64 @@ def test_oracle_tet_mass_sums_to_volume(built, order):
     assert abs(o.tcd_matrix(1).sum() - 1.0) < 1e-12
 
 
+# the reference's tetrahedral rules by degree (QuadratureFormulaDatabase.C:30-37;
+# QuadFormula.C:1693 P4Tetra, :1739 P5Tetra): Keast's symmetric rules, as
+# orbits in barycentric coordinates (kind, a, b, weight per point)
+KEAST = {
+    2: [(4, 0.585410196624968454461376050311, 0.138196601125010515179541316563, 1 / 24)],
+    4: [(1, 0.25, 0.25, -74 / 5625), (4, 11 / 14, 1 / 14, 343 / 45000),
+        (6, 0.399403576166799204996102147462, 0.100596423833200795003897852538, 56 / 2250)],
+    5: [(4, 0.0, 1 / 3, 0.602678571428571428571428571428571e-2),
+        (1, 0.25, 0.25, 0.302836780970891758063769725577305e-1),
+        (4, 8 / 11, 1 / 11, 0.116452490860289694108936091443380e-1),
+        (6, 0.665501535736642982398804642263025e-1, 0.433449846426335701760119535773697,
+         0.109491415613864593456430191124068e-1)],
+}
+
+
+def keast_points(deg):
+    pts = []
+    for kind, a, b, w in KEAST[deg]:
+        if kind == 1:
+            pts.append(((0.25,) * 4, w))
+        for i in range(4):
+            for j in range(i, 4):
+                if (kind == 4 and j == i) or (kind == 6 and j > i):
+                    l = [b] * 4
+                    l[i] = l[j] = a
+                    pts.append((tuple(l), w))
+    return pts
+
+
+@pytest.mark.parametrize("deg", [2, 4, 5])
+def test_keast_rules_exact_to_their_degree(deg):
+    from math import factorial
+    pts = keast_points(deg)
+    assert len(pts) == {2: 4, 4: 11, 5: 15}[deg]
+    for a in range(deg + 1):
+        for b in range(deg + 1 - a):
+            for c in range(deg + 1 - a - b):
+                q = sum(w * l[1] ** a * l[2] ** b * l[3] ** c for l, w in pts)
+                exact = factorial(a) * factorial(b) * factorial(c) / factorial(a + b + c + 3)
+                assert abs(q - exact) < 1e-15
+
+
+@pytest.mark.parametrize("order,linear,deg", [(1, 1, 2), (1, 0, 4), (2, 1, 4), (2, 0, 5)])
+def test_oracle_uses_the_reference_tet_rules(built, order, linear, deg):
+    # one reference-shaped tetrahedron: physical = reference coordinates
+    nl = 4 if order == 1 else 10
+    lv = [dict(verts=np.array([[[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]]], dtype=float),
+               gdof=np.arange(nl, dtype=np.int32)[None, :], ndof=nl, nactive=nl,
+               row_ptr=np.arange(0, nl * nl + 1, nl, dtype=np.int32),
+               col=np.tile(np.arange(nl, dtype=np.int32), nl))]
+    o = po.Problem(po.make_config(3, order, 0, po.EX_SINE, tetra=True, problem_linear=linear),
+                   arrays=lv)
+    x = o.quadrature_points(0)[0]
+    want = sorted(tuple(round(v, 12) for v in l[1:]) for l, _ in keast_points(deg))
+    got = sorted(tuple(round(v, 12) for v in p) for p in x)
+    assert got == want
+
+
 def test_oracle_tet_p2_reproduces_linear_solution(built):
     # u = 1 + x + 2y + 3z lies in P2: Galerkin gives the interpolant
     h = pg.Hierarchy(3, 2, 1, roots=2, tetra=True, perturb=0.2, seed=5)
