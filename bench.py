@@ -59,7 +59,7 @@ STATIONARY = {
         b=(1 / np.sqrt(3.0),) * 3, c=0.0, supg=True, sdfem_type=5, delta0=1.0, cell_measure=2,
         problem_linear=1, quadrature="3x3x3 Gauss", sdfem="type 5, delta=h/(2|b|), h=edge length",
         precond="multigrid", restart=30, n_pre=2, n_post=2, damp=0.8, precisions=("mixed", "fp64"),
-        cpu_sample=None, profile_tag="k_spmv_f32_jacobi_q2_32"),
+        cpu_sample=None, profile_tag="k_sell_f64_cd3d_q2_32"),
     "cd2d_q1_64": dict(
         workload="CD2D 64^2 Q1 Galerkin eps=1e-2 b=(1,.5) c=1 u=sin(pi x)sin(pi y), "
                  "FGMRES(50)+Jacobi FP64 to 1e-10",
@@ -77,7 +77,7 @@ STATIONARY = {
         # omega 0.5: with 0.8 the Jacobi smoother amplifies high modes of this
         # convection-dominated Q2 SUPG operator and FGMRES stagnates
         precond="multigrid", restart=30, n_pre=3, n_post=3, damp=0.5, precisions=("mixed", "fp64"),
-        cpu_sample=dict(roots=3, nref=3, levels=4), profile_tag="k_spmv_f32_jacobi_q2_96"),
+        cpu_sample=dict(roots=3, nref=3, levels=4), profile_tag="k_sell_f64_cd3d_q2_96"),
 }
 
 
@@ -208,10 +208,18 @@ def profile_traffic(kernel_tag):
 
 
 # ---------------------------------------------------------------------------
+EXTRA = {"on": False}   # a short record run embedded in the headline line
+
+
 def timed_hierarchies(pg, ctx, args, kw, levels):
     """The hierarchy built on the host and on the GPU (DOF numbering and CSR
     patterns of every level), both timed; the GPU-built one is checked
     bit-exact against the host one and used for the run."""
+    if EXTRA["on"]:
+        t0 = time.perf_counter()
+        dev = pg.Hierarchy(*args, ctx=ctx, **kw)
+        return dev, {"hierarchy_device_s": time.perf_counter() - t0,
+                     "bit_exact": "not checked in the embedded record run"}
     t0 = time.perf_counter()
     host = pg.Hierarchy(*args, **kw)
     t_host = time.perf_counter() - t0
@@ -349,19 +357,43 @@ def run_gpu(args):
     bytes_spmv64 = 12 * nnz0 + 4 * (n + 1) + 8 * 2 * n
     peak, peak_kind = measured_peak_hbm()
     mg = w["precond"] == "multigrid"
-    if mg:
-        chunk = cd.operator_layout(0)["smoother_chunk"]
-        tpr = 8 if nnz0 / n > 32 else 4
-        rl_kernel = ("k_spmv_bulk<%d,%d,2> (Jacobi smoothing, finest level, %d-entry chunks "
-                     "staged by cp.async.bulk)" % (8192 // chunk, tpr, chunk)) if chunk else (
-                     "k_spmv<float,%d,8,2> (Jacobi smoothing, finest level)" % tpr)
-        achieved = bytes_smooth / (ms_smooth * 1e-3) / 1e9
-        rl_bytes = bytes_smooth
-    else:
-        rl_kernel = "k_spmv<double,...,0> (FP64 operator, finest level)"
-        achieved = bytes_spmv64 / (ms_spmv64 * 1e-3) / 1e9
-        rl_bytes = bytes_spmv64
+    lay = cd.operator_layout(0)
+    # roofline kernel: the FP64 operator w = A z of the finest level, the one
+    # kernel on the path that streams an assembled matrix from HBM every
+    # FGMRES iteration (sliced ELLPACK copy where the level has one)
+    rl_kernel = ("k_sell<double,%d,8,0> (FP64 operator, finest level, sliced ELLPACK)"
+                 % lay["lanes"]) if lay["lanes"] else \
+        "k_spmv<double,...,0> (FP64 operator, finest level, CSR)"
+    achieved = bytes_spmv64 / (ms_spmv64 * 1e-3) / 1e9
+    rl_bytes = bytes_spmv64
     traffic = profile_traffic(w["profile_tag"])
+    smoother, tuning = None, None
+    if mg:
+        # the FP32 smoothing step of every multigrid level as the tuner chose
+        # it (CSR or matrix-free), with the tuner's timings of both kernels
+        tuning = []
+        for l in range(LEVELS - 1):
+            c, (t_csr, t_mf) = cd.tuning(l)
+            tuning.append({"level": l, "dofs": info[l]["ndof"],
+                           "kernel": {-1: "csr (no matrix-free operator)", 0: "csr",
+                                      1: "matrix-free"}[c],
+                           "ms_csr": t_csr, "ms_matrix_free": t_mf})
+        if cd.tuning(0)[0] == 1:
+            nc0 = info[0]["ncells"]
+            # gdof_c + pos_c + results (written, read), row ranges, x, b, D^-1, x'
+            mf_bytes = 4 * 27 * nc0 * 4 + 4 * (info[0]["nactive"] + 1) + 4 * 4 * n
+            smoother = {"kernel": "k_mf_uniform + k_mf_gather<2> (matrix-free Jacobi step, "
+                                  "finest level, one element matrix)",
+                        "bound": "latency (dependent L2 gathers); neither FP32 issue nor HBM",
+                        "ms": ms_smooth, "bytes": mf_bytes,
+                        "achieved_gbs": mf_bytes / (ms_smooth * 1e-3) / 1e9,
+                        "fp32_gflop": 2 * 729 * nc0 / 1e9,
+                        "csr_step_ms": cd.tuning(0)[1][0], "csr_bytes": bytes_smooth}
+        else:
+            smoother = {"kernel": "k_spmv<float,8,8,2> (CSR Jacobi step, finest level)",
+                        "bound": "hbm", "ms": ms_smooth, "bytes": bytes_smooth,
+                        "achieved_gbs": bytes_smooth / (ms_smooth * 1e-3) / 1e9,
+                        "frac": bytes_smooth / (ms_smooth * 1e-3) / 1e9 / peak}
 
     t_step_m = max_over_ranks(dist, sum(per_m) / len(per_m) / 1e3)
     if fp64_side:
@@ -392,6 +424,8 @@ def run_gpu(args):
         "assembly_ms": t_asm * 1e3,
         "kernels_ms": {"jacobi_smooth_f32_L0": ms_smooth, "spmv_f64_L0": ms_spmv64,
                        "element_contract_f64_L0": ms_contract},
+        "smoother": smoother,
+        "tuning": tuning,
         "roofline": {"bound": "hbm", "kernel": rl_kernel, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                      "algorithmic_bytes": rl_bytes, "traffic": traffic},
@@ -410,7 +444,32 @@ def run_gpu(args):
         line["fp64"] = {"value": world / t_step_d, "ms_per_step": t_step_d * 1e3,
                         "iterations": st_d[-1].iterations}
         line["mixed_over_fp64"] = t_step_d / t_step_m
+    if args.workload == "cd3d_q2_32" and world == 1 and not EXTRA["on"] and not args.no_extra:
+        line["extra_workloads"] = extra_workloads()
     print(json.dumps(line))
+
+
+def extra_workloads():
+    """The other workloads as short child runs of this script (3 timed steps,
+    no CPU sample), each line embedded as reported; the headline numbers above
+    are measured before any of them starts."""
+    out = {}
+    for wl, steps in (("cd2d_q1_64", 5), ("tcd3d_p2_48", 5), ("cd3d_q2_96", 3), ("serve", 0)):
+        cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--workload", wl, "--skip-cpu",
+               "--extra"]
+        if steps:
+            cmd += ["--steps", str(steps), "--warmup", "3"]
+        t0 = time.perf_counter()
+        try:
+            r = subprocess.run(cmd, capture_output=True, text=True, timeout=600)
+            lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+            rec = json.loads(lines[-1]) if r.returncode == 0 and lines else {
+                "error": "rc %d: %s" % (r.returncode, r.stderr.strip().splitlines()[-1:])}
+        except Exception as e:  # a failed record run must not lose the headline line
+            rec = {"error": repr(e)}
+        rec["wall_s"] = time.perf_counter() - t0
+        out[wl] = rec
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -670,10 +729,12 @@ def run_gpu_serve(args):
     clocks.start()
     sweep = []
     rng = np.random.default_rng(SERVE["seed"])
-    for k, lam in enumerate(SERVE["rates"]):
+    rates = (100, 500, 2000) if EXTRA["on"] else SERVE["rates"]
+    secs = 1.5 if EXTRA["on"] else SERVE["seconds_per_rate"]
+    for k, lam in enumerate(rates):
         # about seconds_per_rate of arrivals, at most 2500 requests per rate
-        # (8,160 requests over the sweep)
-        cnt = int(min(2500, max(40, lam * SERVE["seconds_per_rate"])))
+        # (8,160 requests over the full sweep)
+        cnt = int(min(2500, max(40, lam * secs)))
         qs = serve_stream(cnt, SERVE["seed"] + k)
         arrivals = np.cumsum(rng.exponential(1.0 / lam, cnt))
         wall, res = run_stream(pg, srv, qs, arrivals, "mixed")
@@ -728,7 +789,10 @@ def run_gpu_serve(args):
     if rank != 0:
         return
     cpu = cpu_baseline_serve() if not args.skip_cpu else None
-    top = sweep[-1]
+    # latency at the highest offered rate the server keeps up with (beyond
+    # saturation the queue, not the solve, sets the latency)
+    kept = [e for e in sweep if e["solves_per_s"] >= 0.9 * e["rate"]]
+    top = kept[-1] if kept else sweep[0]
     ndof_mean = float(np.mean([(o * n + 1) ** d for d, o, n, *_ in base_q]))
     print(json.dumps({
         "metric": SERVE_METRIC, "value": sat, "unit": "solves/s", "n_gpus": world,
@@ -738,7 +802,8 @@ def run_gpu_serve(args):
         "config": {"workload": SERVE_WORKLOAD, "slots": SERVE["slots"],
                    "classes": len(SERVE["classes"]), "mean_dofs": ndof_mean,
                    "l2": "mixed sizes; no flush", "parallelism": "single GPU, %d streams" % SERVE["slots"]},
-        "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"], "sweep": sweep,
+        "p50_ms": top["p50_ms"], "p99_ms": top["p99_ms"], "latency_at_rate": top["rate"],
+        "sweep": sweep,
         "one_at_a_time": {"fp64_solves_per_s": one["fp64"], "mixed_solves_per_s": one["mixed"]},
         "served_over_one_at_a_time_fp64": sat / one["fp64"],
         "server": {k: c1[k] - c0.get(k, 0) if k in ("completed", "launches", "evictions") else c1[k]
@@ -1023,7 +1088,11 @@ def main():
                     help="serve: concurrent request slots (default 8)")
     ap.add_argument("--small", action="store_true",
                     help="with --profile: the 24^3x6 tetrahedral mesh (for detailed captures)")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="headline only: no embedded record runs of the other workloads")
+    ap.add_argument("--extra", action="store_true", help=argparse.SUPPRESS)
     args = ap.parse_args()
+    EXTRA["on"] = args.extra
     if args.warmup < 3 and args.impl != "reference":
         args.warmup = 3
     if args.impl == "reference":

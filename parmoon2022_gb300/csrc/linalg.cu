@@ -1017,7 +1017,10 @@ static int coarse_inverse(cdg_context* ctx, DevLevel& C) {
   // the block in shared memory where cooperative launches are unavailable.
   // Measured on GB300: grid-wide 0.54 ms (125 rows) / 2.25 ms (343 rows), one
   // CTA 2.2 ms (125, one SM's FP64 pipe), a 16-CTA cluster with the rows in
-  // distributed shared memory 0.71 / 3.56 ms (barriers per pivot step)
+  // distributed shared memory 0.71 / 3.56 ms (barriers per pivot step), a
+  // blocked variant (panels of 4-32 pivot columns factored in one CTA, then a
+  // rank-b update of the other columns by all SMs) 2.8-4.3 ms for 343 rows:
+  // the panel steps run on one SM's FP64 pipe
   int coop = 0, per_sm = 0;
   CDG_CUDA(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device));
   CDG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gj_coop, 256, 0));
@@ -1402,13 +1405,17 @@ int defect32_once(cdg_context* ctx, DevLevel& L) {
 
 // Per-level kernel choice of the FP32 multigrid, made once per level by
 // timing (CUDA events on the context stream, the level's own vectors): the
-// CSR smoothing step against the matrix-free one.  CDG_MATFREE=0 / =1 in the
-// environment fixes the choice instead.
-static int tune_level(cdg_context* ctx, cdg_problem* p, DevLevel& L) {
+// CSR smoothing step against the matrix-free one.  CDG_MATFREE in the
+// environment fixes the choice instead: "0" / "1" for every level, or one
+// digit per level from the finest ("100": matrix-free on level 0 only) --
+// under a profiler, whose per-launch overhead distorts the timing
+static int tune_level(cdg_context* ctx, cdg_problem* p, DevLevel& L, int level) {
   if (!L.mf_valid || L.mf_mode >= 0) return CDG_OK;
   const char* env = getenv("CDG_MATFREE");
   if (env && (env[0] == '0' || env[0] == '1')) {
-    L.mf_mode = env[0] - '0';
+    const size_t len = strlen(env);
+    const char c = len > 1 ? (level < (int)len ? env[level] : '0') : env[0];
+    L.mf_mode = c == '1' ? 1 : 0;
     p->alloc_gen++;
     return CDG_OK;
   }
@@ -1459,7 +1466,7 @@ int prepare_solver(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s)
   const int elem = s.precision == 1 ? (int)sizeof(float) : (int)sizeof(double);
   for (int k = 0; k < nl; ++k) CDG_TRY(ensure_mg_vectors(ctx, p->lev[k], elem));
   if (s.precision == 1)
-    for (int k = 0; k + 1 < nl; ++k) CDG_TRY(tune_level(ctx, p, p->lev[k]));
+    for (int k = 0; k + 1 < nl; ++k) CDG_TRY(tune_level(ctx, p, p->lev[k], k));
   if (s.multigrid_smoother_coarse == 0) {
     CDG_TRY(coarse_inverse(ctx, p->lev[nl - 1]));
     CDG_TRY(check_device_error(ctx));
