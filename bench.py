@@ -254,19 +254,26 @@ def run_gpu(args):
     setup["problem_create_s"] = time.perf_counter() - t0
     a = spec_assembly(pg, w)
     precs = w["precisions"]
+    cd64 = cd
+    if precs[0] == "mixed":
+        # the mixed solve's intermediate multigrid levels are FP32-only:
+        # assembled on the tensor cores; the FP64 side runs on its own problem
+        cd.set_fp32_tensor_levels(True)
+        cd64 = pg.ConvectionDiffusion(ctx, hier)
     s_main = spec_solver(pg, w, precs[0])
     s_fp64 = spec_solver(pg, w, "fp64")
     info = [cd.info(l) for l in range(LEVELS)]
     n = info[0]["ndof"]
 
-    def step(s):
-        cd.set_solution(None)   # start iterate 0 on the device (assemble sets Dirichlet values)
-        cd.assemble(a)
-        return cd.solve(s)
+    def step(s, prob=None):
+        prob = prob or cd
+        prob.set_solution(None)   # start iterate 0 on the device (assemble sets Dirichlet values)
+        prob.assemble(a)
+        return prob.solve(s)
 
-    def timed(s, k, w_):
+    def timed(s, k, w_, prob=None):
         for _ in range(w_):
-            step(s)
+            step(s, prob)
         barrier(dist)
         torch.cuda.synchronize()
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
@@ -275,7 +282,7 @@ def run_gpu(args):
         stats = []
         for i in range(k):
             ev[i][0].record(stream)
-            stats.append(step(s))
+            stats.append(step(s, prob))
             ev[i][1].record(stream)
         torch.cuda.synchronize()
         barrier(dist)
@@ -305,9 +312,9 @@ def run_gpu(args):
     fp64_side = len(precs) > 1
     if fp64_side:
         # side by side: all-FP64 GPU solve of the same problem
-        per_d, st_d, _ = timed(s_fp64, max(2, min(args.steps, 5)), 1)
-        err_d = cd.errors(a)
-        x_d = cd.solution()
+        per_d, st_d, _ = timed(s_fp64, max(2, min(args.steps, 5)), 1, cd64)
+        err_d = cd64.errors(a)
+        x_d = cd64.solution()
     # assembly only (all levels, FP64)
     for _ in range(2):
         cd.assemble(a)
@@ -373,10 +380,12 @@ def run_gpu(args):
         # it (CSR or matrix-free), with the tuner's timings of both kernels
         tuning = []
         for l in range(LEVELS - 1):
-            c, (t_csr, t_mf) = cd.tuning(l)
+            c, (t_csr, t_mf), (lanes, cap) = cd.tuning_detail(l)
             tuning.append({"level": l, "dofs": info[l]["ndof"],
-                           "kernel": {-1: "csr (no matrix-free operator)", 0: "csr",
-                                      1: "matrix-free"}[c],
+                           "kernel": {-2: "not tuned", -1: "csr (no matrix-free operator)",
+                                      0: "csr", 1: "matrix-free"}[c],
+                           "csr_lanes_per_row": lanes,
+                           "matrix_free_blocks_per_sm": cap if c == 1 else None,
                            "ms_csr": t_csr, "ms_matrix_free": t_mf})
         if cd.tuning(0)[0] == 1:
             nc0 = info[0]["ncells"]

@@ -388,15 +388,33 @@ int cdg_problem_assemble_coefficients(cdg_problem *p, const cdg_assembly_params 
  * from one shared element matrix).  Parity access for the multigrid kernels. */
 int cdg_problem_apply32(cdg_problem *p, int level, int variant, const float *x,
                         float *y);
-/* the FP32 multigrid kernel chosen for a level (no counterpart in the
- * reference, which has one kernel): *choice -1 not chosen yet (no
- * mixed-precision multigrid solve so far, or a level without a matrix-free
- * operator), 0 CSR, 1 matrix-free.  The choice is made once per level at
- * the first mixed-precision solve by timing one smoothing step of each
- * kernel (CUDA events); ms (may be NULL) receives those two times in
- * milliseconds (0 when the choice was fixed by CDG_MATFREE=0/1 in the
- * environment). */
-int cdg_problem_tuning(cdg_problem *p, int level, int *choice, double *ms);
+/* Operators used only in FP32 on tensor cores (no counterpart in the
+ * reference, which assembles every level in double).  enable = 1: the next
+ * assemblies form the matrices of the levels between the finest and the
+ * coarsest -- which the mixed-precision multigrid uses only as FP32 copies
+ * -- by a tcgen05 contraction of the cell factors with the reference
+ * tensors, split TF32 with FP32 accumulation (FP32-level accuracy), instead
+ * of the FP64 contraction.  Their FP64 values are formed when something
+ * needs them (an FP64 multigrid solve, cdg_problem_get_matrix,
+ * cdg_problem_apply), from the parameters of their last assembly.
+ * Stationary assembly only (cdg_problem_assemble); SUPG with a convection
+ * field linear in x keeps the FP64 path. */
+int cdg_problem_set_fp32_tensor_levels(cdg_problem *p, int enable);
+/* the FP32 values the multigrid smooths with (nnz floats, CSR order) */
+int cdg_problem_get_matrix32(cdg_problem *p, int level, float *v);
+/* the FP32 multigrid schedule chosen for a level (no counterpart in the
+ * reference, which has one kernel).  At the first mixed-precision multigrid
+ * solve every level above the coarsest is tuned once by timing one smoothing
+ * step of each candidate (CUDA events): CSR lanes per row 2/4/8/16, and on Q2
+ * hexahedra with a matrix-free operator its grid (one cell per warp, or 4 / 8
+ * blocks per SM) and then CSR against matrix-free.  *choice: -2 not tuned
+ * yet, -1 CSR (no matrix-free operator), 0 CSR, 1 matrix-free; shape (may be
+ * NULL): [0] FP32 CSR lanes per row, [1] matrix-free blocks per SM (0: one
+ * cell per warp); ms (may be NULL): the best CSR and the best matrix-free
+ * step in milliseconds (0 where not timed).  CDG_TUNE=0 in the environment
+ * keeps the untuned defaults; CDG_MATFREE, CDG_TPR32 and CDG_MF_CAP (one
+ * value, or one per level from the finest, comma-separated) fix choices. */
+int cdg_problem_tuning(cdg_problem *p, int level, int *choice, int *shape, double *ms);
 /* one preconditioner application z = M^-1 v (Iteration_multigrid::apply or
  * Iteration_jacobi::apply) */
 int cdg_problem_precondition(cdg_problem *p, const cdg_solver_params *s,

@@ -54,6 +54,7 @@ EXPORTED = [
     "cdg_server_destroy", "cdg_request_ndof", "cdg_server_submit", "cdg_server_wait",
     "cdg_server_counters", "cdg_problem_apply32", "cdg_problem_tuning",
     "cdg_problem_quadrature_points", "cdg_problem_assemble_coefficients",
+    "cdg_problem_set_fp32_tensor_levels", "cdg_problem_get_matrix32",
 ]
 
 
@@ -170,7 +171,9 @@ def lib():
             "cdg_problem_get_solution": [P, dp], "cdg_problem_set_solution": [P, dp],
             "cdg_problem_get_slots": [P, ctypes.c_int, ip],
             "cdg_problem_apply": [P, ctypes.c_int, dp, dp],
-            "cdg_problem_tuning": [P, ctypes.c_int, ip, dp],
+            "cdg_problem_tuning": [P, ctypes.c_int, ip, ip, dp],
+            "cdg_problem_set_fp32_tensor_levels": [P, ctypes.c_int],
+            "cdg_problem_get_matrix32": [P, ctypes.c_int, ctypes.POINTER(ctypes.c_float)],
             "cdg_problem_quadrature_points": [P, ctypes.POINTER(AssemblyParams), ctypes.c_int,
                                               ip, dp],
             "cdg_problem_assemble_coefficients": [P, ctypes.POINTER(AssemblyParams),
@@ -623,13 +626,31 @@ class ConvectionDiffusion:
         co = np.ascontiguousarray(coeffs, dtype=np.float64)
         _chk(lib().cdg_problem_assemble_coefficients(self.p, ctypes.byref(a), level, _dp(co)))
 
+    def set_fp32_tensor_levels(self, enable=True):
+        """levels between the finest and the coarsest assembled FP32-only by
+        the tensor-core contraction (their FP64 values formed on demand)"""
+        _chk(lib().cdg_problem_set_fp32_tensor_levels(self.p, 1 if enable else 0))
+
+    def matrix32(self, level=0):
+        v = np.zeros(self.info(level)["nnz"], dtype=np.float32)
+        _chk(lib().cdg_problem_get_matrix32(self.p, level,
+                                            v.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return v
+
     def tuning(self, level=0):
         """(choice, (ms_csr, ms_matfree)): the FP32 multigrid kernel of a
-        level (-1 not chosen, 0 CSR, 1 matrix-free) and the tuner's times."""
+        level (-2 not tuned yet, -1 CSR without a matrix-free operator, 0 CSR,
+        1 matrix-free) and the tuner's best times of both kinds."""
+        c, ms = self.tuning_detail(level)[:2]
+        return c, ms
+
+    def tuning_detail(self, level=0):
+        """(choice, (ms_csr, ms_matfree), (csr_lanes_per_row, mf_blocks_per_sm))"""
         c = ctypes.c_int(0)
+        sh = np.zeros(2, dtype=np.int32)
         ms = np.zeros(2)
-        _chk(lib().cdg_problem_tuning(self.p, level, ctypes.byref(c), _dp(ms)))
-        return c.value, (float(ms[0]), float(ms[1]))
+        _chk(lib().cdg_problem_tuning(self.p, level, ctypes.byref(c), _ip(sh), _dp(ms)))
+        return c.value, (float(ms[0]), float(ms[1])), (int(sh[0]), int(sh[1]))
 
     def apply32(self, x, level=0, variant=0):
         """y = A x with the FP32 multigrid operator of a level: variant 0 the

@@ -574,7 +574,15 @@ int cdg_problem_destroy(cdg_problem* p) {
 
 static int assemble_all(cdg_problem* p, const cdg_assembly_params* a) {
   CDG_CUDA(cudaMemsetAsync(p->d_zero_diag, 0, sizeof(int), p->ctx->stream));
-  for (auto& L : p->lev) CDG_TRY(assemble_level(p->ctx, p, L, *a));
+  const size_t nl = p->lev.size();
+  for (size_t l = 0; l < nl; ++l) {
+    // with the option, the levels between the finest and the coarsest (FP32
+    // operators of the mixed-precision multigrid) come from the tensor cores
+    if (p->tc_levels && l > 0 && l + 1 < nl)
+      CDG_TRY(assemble_level_tc(p->ctx, p, p->lev[l], *a));
+    else
+      CDG_TRY(assemble_level(p->ctx, p, p->lev[l], *a));
+  }
   return CDG_OK;
 }
 
@@ -737,7 +745,20 @@ static int d2h(cdg_context* ctx, void* h, const void* d, size_t bytes) {
 int cdg_problem_get_matrix(cdg_problem* p, int level, double* v) {
   DevLevel* L = get_level(p, level);
   if (!L || !v) return CDG_ERR_ARG;
+  CDG_CUDA(cudaSetDevice(p->ctx->device));
+  CDG_TRY(ensure_fp64(p->ctx, p, *L));
   return d2h(p->ctx, v, L->val64, (size_t)L->nnz * sizeof(double));
+}
+int cdg_problem_get_matrix32(cdg_problem* p, int level, float* v) {
+  DevLevel* L = get_level(p, level);
+  if (!L || !v) { set_error("bad arguments"); return CDG_ERR_ARG; }
+  CDG_CUDA(cudaSetDevice(p->ctx->device));
+  return d2h(p->ctx, v, L->val32, (size_t)L->nnz * sizeof(float));
+}
+int cdg_problem_set_fp32_tensor_levels(cdg_problem* p, int enable) {
+  if (!p || enable < 0 || enable > 1) { set_error("bad arguments"); return CDG_ERR_ARG; }
+  p->tc_levels = enable;
+  return CDG_OK;
 }
 int cdg_problem_get_tcd_matrix(cdg_problem* p, int level, int which, double* v) {
   DevLevel* L = get_level(p, level);
@@ -791,6 +812,8 @@ static int h2d_tmp(DevBuf& b, const double* h, size_t n, cudaStream_t st) {
 int cdg_problem_apply(cdg_problem* p, int level, const double* x, double* y) {
   DevLevel* L = get_level(p, level);
   if (!L || !x || !y) return CDG_ERR_ARG;
+  CDG_CUDA(cudaSetDevice(p->ctx->device));
+  CDG_TRY(ensure_fp64(p->ctx, p, *L));
   DevBuf dx, dy;
   CDG_TRY(h2d_tmp(dx, x, L->ndof, p->ctx->stream));
   CDG_TRY(h2d_tmp(dy, nullptr, L->ndof, p->ctx->stream));
@@ -817,10 +840,14 @@ int cdg_problem_assemble_coefficients(cdg_problem* p, const cdg_assembly_params*
   return check_device_error(p->ctx);
 }
 
-int cdg_problem_tuning(cdg_problem* p, int level, int* choice, double* ms) {
+int cdg_problem_tuning(cdg_problem* p, int level, int* choice, int* shape, double* ms) {
   DevLevel* L = get_level(p, level);
   if (!L || !choice) { set_error("bad arguments"); return CDG_ERR_ARG; }
-  *choice = L->mf_mode;
+  *choice = L->tuned ? L->mf_mode : -2;
+  if (shape) {
+    shape[0] = L->tpr32 ? L->tpr32 : L->rows_per_warp_hint;
+    shape[1] = L->mf_blocks_per_sm;
+  }
   if (ms) {
     ms[0] = L->tuned_ms[0];
     ms[1] = L->tuned_ms[1];
@@ -902,6 +929,7 @@ int cdg_problem_time_kernel(cdg_problem* p, const cdg_assembly_params* a, int ke
     return CDG_ERR_ARG;
   }
   cdg_context* ctx = p->ctx;
+  if (kernel == 1 || kernel == 2) CDG_TRY(ensure_fp64(ctx, p, *L));
   cudaEvent_t e0, e1;
   CDG_CUDA(cudaEventCreate(&e0));
   CDG_CUDA(cudaEventCreate(&e1));

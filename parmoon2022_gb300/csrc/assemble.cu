@@ -695,6 +695,215 @@ __global__ void k_mf_element(AsmCoefs k, const double* __restrict__ verts,
 }
 
 // ---------------------------------------------------------------------------
+// Element matrices on the tensor pipe, for operators used only in FP32 (the
+// mixed-precision multigrid's levels between the finest and the coarsest):
+// A(cells x entries) = G(cells x terms) R(terms x entries), the contraction
+// of the FP64 kernel above, as one tcgen05 GEMM tile per 128 cells.  G and R
+// are split into TF32 pairs (x = hi + lo), and D = Ghi Rhi + Ghi Rlo + Glo Rhi
+// accumulates in FP32 in tensor memory: FP32-level accuracy (the lo*lo term,
+// ~2^-22 of the product, is dropped).  Operands are staged in shared memory
+// in the no-swizzle K-major layout (core matrices of 8 rows x 16 bytes,
+// 128 B each; the next core along K at +128 B, along rows at +KP/4 * 128 B);
+// one thread issues the MMAs (M = 128, N <= 256, K = 8 per instruction), a
+// commit arrives on an mbarrier whose wait is bounded, and 16 warps read the
+// tile back with tcgen05.ld (four per tensor-memory lane quarter, each a
+// quarter of the columns) and add the entries of active rows into the FP32
+// CSR values through the slot map.
+// ---------------------------------------------------------------------------
+constexpr int kTcCells = 128;
+constexpr int kTcThreads = 512;      // four warps per tensor-memory lane quarter
+constexpr long kTcSpin = 1L << 26;   // mbarrier polls before the wait counts as lost
+
+__device__ __forceinline__ unsigned tc_smem(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ float tc_tf32(float x) {
+  unsigned r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+// float index of element (row, k) in the no-swizzle K-major layout with kg
+// core matrices along K
+__device__ __forceinline__ int tc_off(int row, int k, int kg) {
+  return ((row >> 3) * kg + (k >> 2)) * 32 + (row & 7) * 4 + (k & 3);
+}
+__device__ __forceinline__ unsigned long long tc_desc(unsigned addr, unsigned lbo, unsigned sbo) {
+  unsigned long long d = (unsigned long long)((addr & 0x3FFFF) >> 4);
+  d |= (unsigned long long)(lbo >> 4) << 16;
+  d |= (unsigned long long)(sbo >> 4) << 32;
+  d |= 1ull << 46;   // descriptor version; base offset 0, no swizzle
+  return d;
+}
+
+template <int DIM, int NLOC>
+__global__ void __launch_bounds__(kTcThreads)
+k_tc_contract(AsmCoefs k, int ncells, int nactive, const double* __restrict__ verts,
+              const int* __restrict__ gdof, const int* __restrict__ slot,
+              const double* __restrict__ R, float* __restrict__ val32, int* err) {
+  using TT = Terms<DIM>;
+  constexpr int NE = NLOC * NLOC;
+  constexpr int KP = (TT::NT + 7) / 8 * 8;   // terms padded to the MMA's K step
+  constexpr int KG = KP / 4;                  // core matrices along K
+  constexpr int NV = DIM == 2 ? 4 : (NLOC == 4 || NLOC == 10 ? 4 : 8);
+  extern __shared__ __align__(1024) float tsm[];
+  float* Ahi = tsm;                    // kTcCells x KP
+  float* Alo = Ahi + kTcCells * KP;
+  float* Bhi = Alo + kTcCells * KP;    // 256 x KP
+  float* Blo = Bhi + 256 * KP;
+  __shared__ __align__(8) unsigned long long mbar;
+  __shared__ unsigned tbase;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int c0 = blockIdx.x * kTcCells;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 256;"
+                 ::"r"(tc_smem(&tbase)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(&mbar)));
+  if (tid < kTcCells) {
+    // the cell's factors (FP64) as TF32 pairs, one row per thread
+    double g[TT::NT];
+    const int cell = c0 + tid;
+    if (cell < ncells)
+      cell_factors<DIM>(k, verts + (size_t)cell * NV * DIM, g, 0);
+    else
+      for (int t = 0; t < TT::NT; ++t) g[t] = 0.0;
+    for (int t = 0; t < KP; ++t) {
+      const double x = t < TT::NT ? g[t] : 0.0;
+      const float hi = tc_tf32((float)x);
+      Ahi[tc_off(tid, t, KG)] = hi;
+      Alo[tc_off(tid, t, KG)] = tc_tf32((float)(x - (double)hi));
+    }
+  }
+  // this thread's cell in the epilogue: tensor-memory lane quarter warp % 4,
+  // columns interleaved over the four warps of that quarter
+  const int quarter = warp & 3, colgrp = warp >> 2;
+  const int row = 32 * quarter + lane;
+  const int ecell = c0 + row;
+  unsigned active = 0;   // bit i: local row i is an active DOF
+  if (ecell < ncells)
+    for (int i = 0; i < NLOC; ++i)
+      if (gdof[(size_t)ecell * NLOC + i] < nactive) active |= 1u << i;
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  const unsigned sbo = KG * 128;
+  unsigned phase = 0;
+  bool ok = true;
+  for (int n0 = 0; n0 < NE; n0 += 256) {
+    const int nv = min(256, NE - n0);          // valid entries in this tile
+    const int nt = (nv + 15) / 16 * 16;        // MMA N (multiple of 16 for M = 128)
+    for (int e = tid; e < nt * KP; e += kTcThreads) {
+      const int n = e / KP, t = e - n * KP;
+      const double x = (n < nv && t < TT::NT) ? R[(size_t)t * NE + n0 + n] : 0.0;
+      const float hi = tc_tf32((float)x);
+      Bhi[tc_off(n, t, KG)] = hi;
+      Blo[tc_off(n, t, KG)] = tc_tf32((float)(x - (double)hi));
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const unsigned tmem = tbase;
+    if (tid == 0) {
+      // D f32, A and B tf32, both K-major, N >> 3 at bit 17, M >> 4 at bit 24
+      const unsigned idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((unsigned)(nt >> 3) << 17) |
+                             ((unsigned)(kTcCells >> 4) << 24);
+      const float* As[3] = {Ahi, Ahi, Alo};
+      const float* Bs[3] = {Bhi, Blo, Bhi};
+      int acc = 0;
+      for (int sp = 0; sp < 3; ++sp)
+        for (int ks = 0; ks < KP / 8; ++ks) {
+          const unsigned long long ad = tc_desc(tc_smem(As[sp]) + ks * 256, 128, sbo);
+          const unsigned long long bd = tc_desc(tc_smem(Bs[sp]) + ks * 256, 128, sbo);
+          asm volatile(
+              "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+              "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+              ::"r"(tmem), "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+          acc = 1;
+        }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                   ::"r"(tc_smem(&mbar)) : "memory");
+    }
+    unsigned done = 0;
+    for (long it = 0; it < kTcSpin && !done; ++it)
+      asm volatile(
+          "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+          "selp.u32 %0, 1, 0, p;\n\t}"
+          : "=r"(done) : "r"(tc_smem(&mbar)), "r"(phase) : "memory");
+    phase ^= 1u;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (!done) {
+      ok = false;
+      if (lane == 0) atomicOr(err, kErrTimeout);
+    }
+    // uniform over the block: a lost wait in any warp ends the tile loop below
+    if (__syncthreads_or(!ok)) {
+      ok = false;
+      break;
+    }
+    for (int cc = 16 * colgrp; cc < nt; cc += 64) {
+      unsigned r[16];
+      const unsigned addr = tmem + ((unsigned)(32 * quarter) << 16) + cc;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
+          "%13,%14,%15}, [%16];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+            "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+            "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          : "r"(addr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (ecell < ncells) {
+        int sl[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int e = n0 + cc + j;
+          sl[j] = (cc + j < nv && ((active >> (e / NLOC)) & 1u))
+                      ? __ldg(slot + (size_t)ecell * NE + e) : -1;
+        }
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+          if (sl[j] >= 0) atomicAdd(val32 + sl[j], __uint_as_float(r[j]));
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();   // tensor memory and the B tile are reused by the next tile
+  }
+  if (!ok) {
+    // a lost wait: give the MMAs in flight another bounded wait before the
+    // tensor memory is released
+    unsigned done = 0;
+    for (long it = 0; it < kTcSpin && !done; ++it)
+      asm volatile(
+          "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+          "selp.u32 %0, 1, 0, p;\n\t}"
+          : "=r"(done) : "r"(tc_smem(&mbar)), "r"(phase ^ 1u) : "memory");
+  }
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 256;" ::"r"(tbase));
+}
+
+__global__ void k_dirichlet_rows32(int n, int nactive, const int* __restrict__ dslot,
+                                   float* __restrict__ val) {
+  const int r = nactive + blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < n) val[dslot[r]] = 1.0f;
+}
+
+// inverse diagonal and the Dirichlet-coupling values of an FP32-only level
+__global__ void k_finish_matrix32(int n, const int* __restrict__ dslot,
+                                  const float* __restrict__ val32, float* __restrict__ invd32,
+                                  int ndc, const int* __restrict__ dc_pos,
+                                  float* __restrict__ dc_val32, int* err) {
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < ndc; t += stride)
+    dc_val32[t] = val32[dc_pos[t]];
+  for (long r = blockIdx.x * (long)blockDim.x + threadIdx.x; r < n; r += stride) {
+    const float d = val32[dslot[r]];
+    if (d == 0.0f) atomicOr(err, kErrZeroDiag);
+    invd32[r] = d == 0.0f ? 0.0f : 1.0f / d;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // coupling -> CSR slot map (replaces the reference's linear row search)
 // ---------------------------------------------------------------------------
 __global__ void k_build_slots(int ncells, int nloc, const int* __restrict__ gdof,
@@ -1974,17 +2183,10 @@ static int finish_matrix(cdg_context* ctx, cdg_problem* p, DevLevel& L) {
   return CDG_OK;
 }
 
-int assemble_level(cdg_context* ctx, cdg_problem* p, DevLevel& L, const cdg_assembly_params& a) {
-  CDG_TRY(ensure_tables(ctx, p));
-  AsmCoefs k = make_coefs(a, L.shape, L.order);
-  CDG_TRY(check_coefs(k));
+// the matrix-free FP32 operator takes the same factors (the SUPG term set
+// has no linear-convection terms, so that combination keeps the CSR path)
+static int mf_prepare(cdg_context* ctx, cdg_problem* p, DevLevel& L, const AsmCoefs& k) {
   cudaStream_t st = ctx->stream;
-  // block->reset(), rhs.reset()
-  CDG_CUDA(cudaMemsetAsync(L.val64, 0, (size_t)L.nnz * sizeof(double), st));
-  CDG_CUDA(cudaMemsetAsync(L.rhs, 0, (size_t)L.ndof * sizeof(double), st));
-  CDG_TRY(contract(ctx, k, L, p->d_tables, stiffness_set(k), false, L.val64));
-  // the matrix-free FP32 operator takes the same factors (the SUPG term set
-  // has no linear-convection terms, so that combination keeps the CSR path)
   L.mf_valid = 0;
   if (mf_eligible(L) && L.mf_mode != 0 && !(k.supg && k.linear_b)) {
     CDG_TRY(mf_ensure(L));
@@ -2020,6 +2222,19 @@ int assemble_level(cdg_context* ctx, cdg_problem* p, DevLevel& L, const cdg_asse
     L.mf_valid = 1;
     L.mf_lin = k.linear_b;
   }
+  return CDG_OK;
+}
+
+int assemble_level(cdg_context* ctx, cdg_problem* p, DevLevel& L, const cdg_assembly_params& a) {
+  CDG_TRY(ensure_tables(ctx, p));
+  AsmCoefs k = make_coefs(a, L.shape, L.order);
+  CDG_TRY(check_coefs(k));
+  cudaStream_t st = ctx->stream;
+  // block->reset(), rhs.reset()
+  CDG_CUDA(cudaMemsetAsync(L.val64, 0, (size_t)L.nnz * sizeof(double), st));
+  CDG_CUDA(cudaMemsetAsync(L.rhs, 0, (size_t)L.ndof * sizeof(double), st));
+  CDG_TRY(contract(ctx, k, L, p->d_tables, stiffness_set(k), false, L.val64));
+  CDG_TRY(mf_prepare(ctx, p, L, k));
   int nd = L.ndof - L.nactive;
   if (nd > 0)
     CDG_LAUNCH(ctx, k_dirichlet_rows, grid_for<int>(nd, 256), 256, 0, L.ndof, L.nactive,
@@ -2028,7 +2243,64 @@ int assemble_level(cdg_context* ctx, cdg_problem* p, DevLevel& L, const cdg_asse
   if (nd > 0)
     CDG_LAUNCH(ctx, k_copy_nonactive, grid_for<int>(nd, 256), 256, 0, L.ndof, L.nactive, L.rhs,
                L.sol);
+  L.fp64_stale = 0;
   return finish_matrix(ctx, p, L);
+}
+
+template <int DIM, int NLOC>
+static int launch_tc(cdg_context* ctx, const AsmCoefs& k, DevLevel& L, const double* R) {
+  constexpr int KP = (Terms<DIM>::NT + 7) / 8 * 8;
+  const size_t smem = (size_t)(kTcCells + 256) * KP * 2 * sizeof(float);
+  CDG_CUDA(cudaFuncSetAttribute(k_tc_contract<DIM, NLOC>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  CDG_LAUNCH(ctx, (k_tc_contract<DIM, NLOC>), (L.ncells + kTcCells - 1) / kTcCells, kTcThreads,
+             smem, k, L.ncells, L.nactive, L.verts, L.gdof, L.slot, R, L.val32, ctx->d_err);
+  return CDG_OK;
+}
+
+// A level whose operator is used only in FP32 (mixed-precision multigrid,
+// between the finest and the coarsest level): its FP32 values from the
+// tensor-core contraction, rhs and Dirichlet data as in assemble_level.  The
+// FP64 values are not formed; ensure_fp64 forms them when something needs
+// them (an FP64 solve, the matrix getter, the FP64 operator).
+int assemble_level_tc(cdg_context* ctx, cdg_problem* p, DevLevel& L,
+                      const cdg_assembly_params& a) {
+  CDG_TRY(ensure_tables(ctx, p));
+  AsmCoefs k = make_coefs(a, L.shape, L.order);
+  CDG_TRY(check_coefs(k));
+  if (k.supg && k.linear_b) return assemble_level(ctx, p, L, a);   // terms differ: FP64 path
+  cudaStream_t st = ctx->stream;
+  CDG_CUDA(cudaMemsetAsync(L.val32, 0, (size_t)L.nnz * sizeof(float), st));
+  CDG_CUDA(cudaMemsetAsync(L.rhs, 0, (size_t)L.ndof * sizeof(double), st));
+  int rc = CDG_ERR_ARG;
+  if (L.shape == kHexa && L.nloc == 27) rc = launch_tc<3, 27>(ctx, k, L, p->d_tables);
+  else if (L.shape == kHexa && L.nloc == 8) rc = launch_tc<3, 8>(ctx, k, L, p->d_tables);
+  else if (L.shape == kQuad && L.nloc == 9) rc = launch_tc<2, 9>(ctx, k, L, p->d_tables);
+  else if (L.shape == kQuad && L.nloc == 4) rc = launch_tc<2, 4>(ctx, k, L, p->d_tables);
+  else if (L.shape == kTetra && L.nloc == 10) rc = launch_tc<3, 10>(ctx, k, L, p->d_tables);
+  else if (L.shape == kTetra && L.nloc == 4) rc = launch_tc<3, 4>(ctx, k, L, p->d_tables);
+  else set_error("unsupported element");
+  CDG_TRY(rc);
+  CDG_TRY(mf_prepare(ctx, p, L, k));
+  const int nd = L.ndof - L.nactive;
+  if (nd > 0)
+    CDG_LAUNCH(ctx, k_dirichlet_rows32, grid_for<int>(nd, 256), 256, 0, L.ndof, L.nactive,
+               L.diag_slot, L.val32);
+  CDG_TRY(launch_rhs(ctx, k, L, L.rhs));
+  if (nd > 0)
+    CDG_LAUNCH(ctx, k_copy_nonactive, grid_for<int>(nd, 256), 256, 0, L.ndof, L.nactive, L.rhs,
+               L.sol);
+  const int g = (int)std::min<long>(((long)L.ndof + 255) / 256, (long)ctx->num_sms * 16);
+  CDG_LAUNCH(ctx, k_finish_matrix32, g, 256, 0, L.ndof, L.diag_slot, L.val32, L.invdiag32,
+             L.dc_n, L.dc_pos, L.dc_val32, p->d_zero_diag);
+  L.fp64_stale = 1;
+  L.last_a = a;
+  return CDG_OK;
+}
+
+int ensure_fp64(cdg_context* ctx, cdg_problem* p, DevLevel& L) {
+  if (!L.fp64_stale) return CDG_OK;
+  return assemble_level(ctx, p, L, L.last_a);
 }
 
 // one level with coefficients per (cell, quadrature point) (the generic
@@ -2070,6 +2342,7 @@ int assemble_level_coefficients(cdg_context* ctx, cdg_problem* p, DevLevel& L,
     CDG_CUDA(e);
   }
   L.mf_valid = 0;
+  L.fp64_stale = 0;
   CDG_CUDA(cudaMemsetAsync(L.val64, 0, (size_t)L.nnz * sizeof(double), st));
   CDG_CUDA(cudaMemsetAsync(L.rhs, 0, (size_t)L.ndof * sizeof(double), st));
   const int g = std::max(1, std::min(L.ncells, ctx->num_sms * 8));
@@ -2159,6 +2432,7 @@ int tcd_assemble_level(cdg_context* ctx, cdg_problem* p, DevLevel& L,
   CDG_TRY(ensure_tables(ctx, p));
   CDG_TRY(ensure_tcd(L));
   L.mf_valid = 0;   // the FP32 operator becomes the time-dependent system
+  L.fp64_stale = 0;
   AsmCoefs k = make_coefs(a, L.shape, L.order);
   k.tcd = 1;
   k.theta1 = theta1;

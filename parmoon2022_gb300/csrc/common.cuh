@@ -155,6 +155,12 @@ struct DevLevel {
   int mf_geo = -1;               // every cell a translate of cell 0 (-1: not checked)
   int mf_uniform = 0;            // the last assembly has one element matrix for all cells
   int mf_blocks_per_sm = 0;      // grid cap of the cell kernel (0: one cell per warp)
+  int tpr32 = 0;                 // FP32 CSR lanes per row (0: rows_per_warp_hint)
+  // FP32 values from the tensor-core contraction, FP64 values not formed
+  // (assemble_level_tc); last_a assembles them on demand (ensure_fp64)
+  int fp64_stale = 0;
+  cdg_assembly_params last_a{};
+  int tuned = 0;                 // the tuner has run on this level
   float tuned_ms[2] = {0.f, 0.f};   // tuner's smoothing-step times: CSR, matrix-free
   // dense inverse of the active block (coarsest multigrid level)
   double* coarse_inv = nullptr;  // na*na
@@ -199,6 +205,7 @@ struct cdg_problem {
   int nterms = 0;
   int rt_order = -1;
   int tcd_step = 0;               // TimeDiscretization::current_step_
+  int tc_levels = 0;              // levels 1 .. n-2 assembled FP32-only on tensor cores
 };
 
 struct cdg_hierarchy {
@@ -275,6 +282,10 @@ int level_quadrature_points(const DevLevel& L, const cdg_assembly_params& a, int
                             double* x);
 int assemble_level_coefficients(cdg_context* ctx, cdg_problem* p, DevLevel& L,
                                 const cdg_assembly_params& a, const double* coef_host);
+// FP32-only level from the tensor-core contraction, and its FP64 values on demand
+int assemble_level_tc(cdg_context* ctx, cdg_problem* p, DevLevel& L,
+                      const cdg_assembly_params& a);
+int ensure_fp64(cdg_context* ctx, cdg_problem* p, DevLevel& L);
 // argument checks of every entry point that takes assembly parameters
 int check_assembly_params(const cdg_problem* p, const cdg_assembly_params* a);
 int level_errors(cdg_context* ctx, cdg_problem* p, DevLevel& L,

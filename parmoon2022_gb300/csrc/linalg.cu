@@ -279,7 +279,7 @@ static int spmv_bulk_any(cdg_context* ctx, const DevLevel& L, const float* val, 
 template <typename T, int MODE>
 static int spmv_t(cdg_context* ctx, const DevLevel& L, const T* val, const T* x, const T* b,
                   const T* invd, T w, T* y) {
-  const int tpr = L.rows_per_warp_hint;
+  const int tpr = std::is_same<T, float>::value && L.tpr32 ? L.tpr32 : L.rows_per_warp_hint;
   long threads = (long)L.ndof * tpr;
   int grid = (int)((threads + 255) / 256);
   switch (tpr) {
@@ -1095,7 +1095,7 @@ static int smooth_out(cdg_context* ctx, const DevLevel& L, const T* val, const T
                       const T* invd, T w, T* y, double* z, const int* di, double* zcur) {
   if constexpr (std::is_same<T, float>::value)
     if (mf_on<T>(L)) return mf_apply(ctx, L, 3, x, b, invd, w, y, z, di, zcur);
-  const int tpr = L.rows_per_warp_hint;
+  const int tpr = std::is_same<T, float>::value && L.tpr32 ? L.tpr32 : L.rows_per_warp_hint;
   const int grid = (int)(((long)L.ndof * tpr + 255) / 256);
   switch (tpr) {
     case 2: CDG_LAUNCH(ctx, (k_spmv<T, 2, 8, 3>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y, z, di, zcur); break;
@@ -1155,6 +1155,32 @@ static int smooth(cdg_context* ctx, DevLevel& L, T damp) {
   return CDG_OK;
 }
 
+// sum_k dcv[k] * x[col[k]] over a row's couplings to non-active columns, in k
+// order; the loads of eight terms are issued together (a boundary row has up
+// to ~45 such couplings, and one thread walks them)
+template <typename T, typename X>
+__device__ __forceinline__ T dirichlet_coupling(int k, int ke, const int* __restrict__ col,
+                                                const T* __restrict__ dcv,
+                                                const X* __restrict__ x) {
+  T s = 0;
+  for (; k + 8 <= ke; k += 8) {
+    T a[8];
+    int c[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      a[u] = dcv[k + u];
+      c[u] = col[k + u];
+    }
+    T xv[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) xv[u] = (T)x[c[u]];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) s += a[u] * xv[u];
+  }
+  for (; k < ke; ++k) s += dcv[k] * (T)x[col[k]];
+  return s;
+}
+
 // first smoothing step from x0 = 0 on active rows and x0 = b on non-active
 // rows (zero there on coarse levels): A x0 on an active row only involves its
 // non-active columns, so the step needs no full SpMV
@@ -1166,8 +1192,7 @@ k_first_smooth(int n, int nactive, int with_dirichlet, const int* __restrict__ d
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     if (i < nactive) {
       T s = 0;
-      if (with_dirichlet)
-        for (int k = dc_rp[i]; k < dc_rp[i + 1]; ++k) s += dcv[k] * b[dc_col[k]];
+      if (with_dirichlet) s = dirichlet_coupling(dc_rp[i], dc_rp[i + 1], dc_col, dcv, b);
       x1[i] = w * (invd[i] * (b[i] - s));
     } else {
       const T x0 = with_dirichlet ? b[i] : (T)0;
@@ -1191,8 +1216,7 @@ k_first_smooth_init(int n, int nactive, const int* __restrict__ dc_rp,
     const T bi = (T)v[i];
     rhs[i] = bi;
     if (i < nactive) {
-      T s = 0;
-      for (int k = dc_rp[i]; k < dc_rp[i + 1]; ++k) s += dcv[k] * (T)v[dc_col[k]];
+      const T s = dirichlet_coupling(dc_rp[i], dc_rp[i + 1], dc_col, dcv, v);
       x1[i] = w * (invd[i] * (bi - s));
     } else {
       x1[i] = bi + w * (invd[i] * (bi - bi));
@@ -1403,45 +1427,116 @@ int defect32_once(cdg_context* ctx, DevLevel& L) {
   return defect<float>(ctx, L);
 }
 
-// Per-level kernel choice of the FP32 multigrid, made once per level by
-// timing (CUDA events on the context stream, the level's own vectors): the
-// CSR smoothing step against the matrix-free one.  CDG_MATFREE in the
-// environment fixes the choice instead: "0" / "1" for every level, or one
-// digit per level from the finest ("100": matrix-free on level 0 only) --
-// under a profiler, whose per-launch overhead distorts the timing
+// per-level value of an environment override: one value for every level, or
+// one per level from the finest ("8,4,4"; digits without commas for 0/1
+// switches, "100"); -1 when unset
+static int env_level(const char* name, int level) {
+  const char* e = getenv(name);
+  if (!e || !*e) return -1;
+  if (!strchr(e, ',')) {
+    const size_t len = strlen(e);
+    if (len > 1 && (e[0] == '0' || e[0] == '1') && strspn(e, "01") == len)
+      return level < (int)len ? e[level] - '0' : 0;
+    return atoi(e);
+  }
+  const char* q = e;
+  for (int l = 0; l < level && q; ++l) {
+    q = strchr(q, ',');
+    if (q) ++q;
+  }
+  return q && *q ? atoi(q) : -1;
+}
+
+// Per-level kernel schedule of the FP32 multigrid, chosen once per level by
+// timing one smoothing step of each candidate (CUDA events on the context
+// stream, the level's own vectors, 3 warm-up + 10 timed steps):
+//   * CSR: lanes per row 2 / 4 / 8 / 16 (those with 8 * lanes >= a quarter of
+//     the mean row length);
+//   * matrix-free (Q2 hexahedra): grid of one cell per warp, or 4 / 8 blocks
+//     per SM walking the cells;
+// and the faster of the best CSR and the best matrix-free step.  The grid
+// size and, for a given lane count, the loop unrolling do not change any
+// result; the lane count and the kernel kind change FP32 rounding only.
+// Environment overrides (a profiler's per-launch overhead distorts timing):
+// CDG_MATFREE (0/1), CDG_TPR32 (lanes), CDG_MF_CAP (blocks per SM).
 static int tune_level(cdg_context* ctx, cdg_problem* p, DevLevel& L, int level) {
-  if (!L.mf_valid || L.mf_mode >= 0) return CDG_OK;
-  const char* env = getenv("CDG_MATFREE");
-  if (env && (env[0] == '0' || env[0] == '1')) {
-    const size_t len = strlen(env);
-    const char c = len > 1 ? (level < (int)len ? env[level] : '0') : env[0];
-    L.mf_mode = c == '1' ? 1 : 0;
-    p->alloc_gen++;
+  if (L.tuned) return CDG_OK;
+  L.tuned = 1;
+  p->alloc_gen++;   // the captured iteration graph holds the kernels of the old choice
+  const char* off = getenv("CDG_TUNE");
+  if (off && off[0] == '0') {   // untuned defaults: CSR, lanes by mean row length
+    L.mf_mode = 0;
     return CDG_OK;
   }
   cudaEvent_t e0, e1;
   CDG_CUDA(cudaEventCreate(&e0));
   CDG_CUDA(cudaEventCreate(&e1));
-  float t[2] = {0.f, 0.f};
   int rc = CDG_OK;
-  for (int mode = 0; mode < 2 && rc == CDG_OK; ++mode) {
-    L.mf_mode = mode;
+  auto time_step = [&](float* ms) {
     for (int r = 0; r < 3 && rc == CDG_OK; ++r) rc = smooth<float>(ctx, L, 0.8f);
-    if (rc != CDG_OK) break;
+    if (rc != CDG_OK) return;
     cudaEventRecord(e0, ctx->stream);
     for (int r = 0; r < 10 && rc == CDG_OK; ++r) rc = smooth<float>(ctx, L, 0.8f);
     cudaEventRecord(e1, ctx->stream);
     cudaEventSynchronize(e1);
-    cudaEventElapsedTime(&t[mode], e0, e1);
+    cudaEventElapsedTime(ms, e0, e1);
+    *ms /= 10;
+  };
+  const int mf_env = env_level("CDG_MATFREE", level);
+  const int tpr_env = env_level("CDG_TPR32", level);
+  const int cap_env = env_level("CDG_MF_CAP", level);
+  // CSR lanes per row (not for the opt-in staged kernel, which has its own)
+  L.mf_mode = 0;
+  if (tpr_env == 2 || tpr_env == 4 || tpr_env == 8 || tpr_env == 16) {
+    L.tpr32 = tpr_env;
+  } else if (mf_env != 1 && !L.bulk_nchunks) {
+    const double avg = L.ndof ? (double)L.nnz / L.ndof : 1.0;
+    float best = 1e30f;
+    int bt = L.rows_per_warp_hint;
+    for (int t : {2, 4, 8, 16}) {
+      if (8.0 * t < avg / 4 || (t == 2 && avg > 32)) continue;
+      L.tpr32 = t;
+      float ms = 0.f;
+      time_step(&ms);
+      if (rc != CDG_OK) break;
+      if (ms < best) {
+        best = ms;
+        bt = t;
+      }
+    }
+    L.tpr32 = bt;
+    L.tuned_ms[0] = best;
   }
+  // matrix-free grid, then the faster kind
+  if (rc == CDG_OK && L.mf_valid && mf_env != 0) {
+    L.mf_mode = 1;
+    if (cap_env >= 0) {
+      L.mf_blocks_per_sm = cap_env;
+    } else {
+      float best = 1e30f;
+      int bc = 0;
+      for (int cap : {0, 4, 8}) {
+        L.mf_blocks_per_sm = cap;
+        float ms = 0.f;
+        time_step(&ms);
+        if (rc != CDG_OK) break;
+        if (ms < best) {
+          best = ms;
+          bc = cap;
+        }
+      }
+      L.mf_blocks_per_sm = bc;
+      L.tuned_ms[1] = best;
+    }
+    if (mf_env != 1 && !(L.tuned_ms[1] < L.tuned_ms[0])) {
+      L.mf_mode = 0;
+      L.mf_blocks_per_sm = 0;   // unused by the CSR kernel
+    }
+  }
+  if (!L.mf_valid) L.mf_mode = -1;   // no matrix-free operator on this level
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  CDG_TRY(rc);
-  L.mf_mode = t[1] < t[0] ? 1 : 0;
-  L.tuned_ms[0] = t[0] / 10;
-  L.tuned_ms[1] = t[1] / 10;
-  p->alloc_gen++;   // the captured iteration graph holds the kernels of the old choice
-  return CDG_OK;
+  return rc;
 }
 
 int prepare_solver(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s) {
@@ -1464,9 +1559,14 @@ int prepare_solver(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s)
     return CDG_ERR_ARG;
   }
   const int elem = s.precision == 1 ? (int)sizeof(float) : (int)sizeof(double);
+  // FP64 values of FP32-only levels where this solve needs them: every level
+  // of an FP64 multigrid, the coarse inverse's level otherwise
+  for (int k = 0; k < nl; ++k)
+    if (s.precision == 0 || k == nl - 1) CDG_TRY(ensure_fp64(ctx, p, p->lev[k]));
   for (int k = 0; k < nl; ++k) CDG_TRY(ensure_mg_vectors(ctx, p->lev[k], elem));
   if (s.precision == 1)
     for (int k = 0; k + 1 < nl; ++k) CDG_TRY(tune_level(ctx, p, p->lev[k], k));
+
   if (s.multigrid_smoother_coarse == 0) {
     CDG_TRY(coarse_inverse(ctx, p->lev[nl - 1]));
     CDG_TRY(check_device_error(ctx));

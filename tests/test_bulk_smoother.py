@@ -46,9 +46,9 @@ def problem(ctx, name, chunk):
 
 @pytest.mark.parametrize("name", list(CASES))
 def test_staged_cycle_bit_identical(ctx, name, monkeypatch):
-    # both kernels stream the CSR matrix: keep the tuner from choosing the
-    # matrix-free operator on Q2 hexahedral levels
-    monkeypatch.setenv("CDG_MATFREE", "0")
+    # both kernels stream the CSR matrix with the default lanes per row: the
+    # tuner (matrix-free operator, other lane counts) stays off
+    monkeypatch.setenv("CDG_TUNE", "0")
     outs = []
     for chunk in (0, 256, 512, 1024):
         cd, levels = problem(ctx, name, chunk)

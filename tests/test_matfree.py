@@ -166,3 +166,64 @@ def test_mixed_solve_with_matrix_free_smoother(ctx, name):
         assert rel(r["x"], x_o) < 1e-8
         for k in (0, 1):
             assert abs(r["e"][k] - e_o[k]) <= 5e-4 * e_o[k]
+
+
+def test_tuned_schedule_reproduced_by_its_settings(ctx, monkeypatch):
+    # the tuner's choices (kernel, lanes per row, matrix-free grid) fixed
+    # through the environment reproduce the tuned schedule and solve (the
+    # FP64 element scatter adds with atomics, so two assemblies agree to
+    # round-off, not bit for bit); the untuned defaults give the same solve
+    # within the mixed-precision bars
+    nref, _, kw = CASES["supg_polyexp"]
+    levels = 3
+    for name in ("CDG_MATFREE", "CDG_TPR32", "CDG_MF_CAP", "CDG_TUNE"):
+        monkeypatch.delenv(name, raising=False)
+
+    def run():
+        gpu = pg.ConvectionDiffusion(ctx, pg.Hierarchy(3, 2, nref, n_levels=levels))
+        a = gpu_params(kw)
+        gpu.assemble(a)
+        st = gpu.solve(mixed_solver(levels))
+        det = [gpu.tuning_detail(l) for l in range(levels - 1)]
+        x = gpu.solution()
+        gpu.close()
+        return st, x, det
+
+    st_t, x_t, det = run()
+    assert all(d[0] in (0, 1) for d in det)
+    monkeypatch.setenv("CDG_MATFREE", ",".join(str(d[0]) for d in det))
+    monkeypatch.setenv("CDG_TPR32", ",".join(str(d[2][0]) for d in det))
+    monkeypatch.setenv("CDG_MF_CAP", ",".join(str(d[2][1]) for d in det))
+    st_f, x_f, det_f = run()
+    assert [d[0] for d in det_f] == [d[0] for d in det]
+    assert [d[2] for d in det_f] == [d[2] for d in det]
+    assert st_f.iterations == st_t.iterations
+    assert rel(x_f, x_t) < 1e-10
+    for name in ("CDG_MATFREE", "CDG_TPR32", "CDG_MF_CAP"):
+        monkeypatch.delenv(name)
+    monkeypatch.setenv("CDG_TUNE", "0")
+    st_d, x_d, det_d = run()
+    assert all(d[0] == 0 for d in det_d)
+    assert abs(st_d.iterations - st_t.iterations) <= 2
+    assert rel(x_d, x_t) < 1e-8
+
+
+def test_matrix_free_grid_does_not_change_results(ctx, monkeypatch):
+    # one cell per warp or 4 / 8 blocks per SM walking the cells: the same
+    # matrix-free products, bit for bit (the operator of a uniform level comes
+    # from cell 0's factors and is summed per row in a fixed order)
+    nref, levels, kw = CASES["supg_polyexp"]
+    x = None
+    outs = []
+    for cap in ("0", "4", "8"):
+        monkeypatch.setenv("CDG_MATFREE", "1")
+        monkeypatch.setenv("CDG_MF_CAP", cap)
+        gpu = pg.ConvectionDiffusion(ctx, pg.Hierarchy(3, 2, nref, n_levels=levels))
+        gpu.assemble(gpu_params(kw))
+        if x is None:
+            x = np.random.default_rng(8).standard_normal(gpu.info(0)["ndof"]).astype(np.float32)
+        gpu.precondition(mixed_solver(levels), x.astype(np.float64))   # runs the tuner
+        assert gpu.tuning_detail(0)[0] == 1 and gpu.tuning_detail(0)[2][1] == int(cap)
+        outs.append(gpu.apply32(x, 0, 1))
+        gpu.close()
+    assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[0], outs[2])
