@@ -385,7 +385,10 @@ int cdg_problem_assemble_coefficients(cdg_problem *p, const cdg_assembly_params 
  * non-active rows), host float buffers of n_dofs entries.  variant 0: CSR
  * kernel; 1: matrix-free kernel (Q2 hexahedra after a stationary assembly,
  * the element matrices applied from per-cell factors or, on uniform levels,
- * from one shared element matrix).  Parity access for the multigrid kernels. */
+ * from one shared element matrix in one launch per product); 2: the
+ * matrix-free product as two launches (cell products, then the row sums),
+ * which the one-launch form equals bit for bit.  Parity access for the
+ * multigrid kernels. */
 int cdg_problem_apply32(cdg_problem *p, int level, int variant, const float *x,
                         float *y);
 /* Operators used only in FP32 on tensor cores (no counterpart in the
@@ -407,10 +410,11 @@ int cdg_problem_get_matrix32(cdg_problem *p, int level, float *v);
  * solve every level above the coarsest is tuned once by timing one smoothing
  * step of each candidate (CUDA events): CSR lanes per row 2/4/8/16, and on Q2
  * hexahedra with a matrix-free operator its grid (one cell per warp, or 4 / 8
- * blocks per SM) and then CSR against matrix-free.  *choice: -2 not tuned
+ * blocks per SM; uniform levels sweep in one launch of one block per 256
+ * rows) and then CSR against matrix-free.  *choice: -2 not tuned
  * yet, -1 CSR (no matrix-free operator), 0 CSR, 1 matrix-free; shape (may be
  * NULL): [0] FP32 CSR lanes per row, [1] matrix-free blocks per SM (0: one
- * cell per warp); ms (may be NULL): the best CSR and the best matrix-free
+ * cell per warp, -1: the one-launch sweep); ms (may be NULL): the best CSR and the best matrix-free
  * step in milliseconds (0 where not timed).  CDG_TUNE=0 in the environment
  * keeps the untuned defaults; CDG_MATFREE, CDG_TPR32 and CDG_MF_CAP (one
  * value, or one per level from the finest, comma-separated) fix choices. */

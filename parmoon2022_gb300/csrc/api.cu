@@ -77,6 +77,14 @@ int cdg_context_create(int device, cdg_context** out) {
   CDG_CUDA(cudaMalloc(&c->d_cnt, kRedSlots * sizeof(unsigned)));
   CDG_CUDA(cudaMemset(c->d_cnt, 0, kRedSlots * sizeof(unsigned)));
   CDG_CUDA(cudaMallocHost(&c->h_pinned, 64 * sizeof(double)));
+  {
+    // off by default: measured on GB300 (32^3 Q2 mixed step) the
+    // graph-launched FGMRES iteration took 42.9 ms per solve with it and
+    // 40.4 ms without, although single kernels repeated back to back gained
+    // (matrix-free smoothing step 16.4 -> 11.7 us)
+    const char* e = std::getenv("CDG_PDL");
+    c->pdl = (e && e[0] == '1') ? 1 : 0;
+  }
   *out = c;
   return CDG_OK;
 }
@@ -857,8 +865,8 @@ int cdg_problem_tuning(cdg_problem* p, int level, int* choice, int* shape, doubl
 
 int cdg_problem_apply32(cdg_problem* p, int level, int variant, const float* x, float* y) {
   DevLevel* L = get_level(p, level);
-  if (!L || !x || !y || variant < 0 || variant > 1) { set_error("bad arguments"); return CDG_ERR_ARG; }
-  if (variant == 1 && !L->mf_valid) {
+  if (!L || !x || !y || variant < 0 || variant > 2) { set_error("bad arguments"); return CDG_ERR_ARG; }
+  if (variant >= 1 && !L->mf_valid) {
     set_error("no matrix-free operator on level %d (Q2 hexahedra after a stationary assembly)",
               level);
     return CDG_ERR_ARG;

@@ -1811,6 +1811,7 @@ int free_level(DevLevel& L) {
                   L.R_val32, L.coarse_inv, L.coarse_work, L.dc_rp, L.dc_col, L.dc_pos,
                   L.tcd_A, L.tcd_M, L.tcd_f, L.tcd_fold, L.tcd_u2, L.dof_rp, L.dof_ent,
                   L.rhs_loc, L.mf_fac, L.mf_y, L.mf_ae, L.mf_gdof, L.mf_pos, L.mf_pos_c,
+                  L.mf_tile_rp, L.mf_tile_gdof, L.mf_ent_loc,
                   L.dc_val64, L.dc_val32};
   for (void* q : ptrs)
     if (q) cudaFree(q);
@@ -2210,6 +2211,7 @@ static int mf_prepare(cdg_context* ctx, cdg_problem* p, DevLevel& L, const AsmCo
       cudaFree(flag);
       CDG_CUDA(e);
       L.mf_geo = nonuni ? 0 : 1;
+      if (L.mf_geo == 1) CDG_TRY(mf_build_tiles(ctx, L));
     }
     // constant coefficients on translated cells: one element matrix;
     // otherwise per-cell factors for the sum-factorised kernel

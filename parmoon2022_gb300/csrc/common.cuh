@@ -42,6 +42,8 @@ enum : int {
 };
 
 constexpr int kMfFactors = 40;        // per-cell factors of the matrix-free Q2 operator
+constexpr int kMfTileRows = 256;      // rows (threads) per tile of the one-launch sweep
+constexpr int kMfCellStride = 28;     // floats per tile cell in shared memory (16-byte rows)
 constexpr int kRedSlots = 32;         // partial-sum rows (one per inner product)
 constexpr int kRedMaxBlocks = 1024;   // partial sums per reduction
 
@@ -56,6 +58,8 @@ struct cdg_context {
   unsigned* d_cnt = nullptr;      // kRedSlots last-block counters
   double* h_pinned = nullptr;     // 64 doubles of pinned readback space
   long long launches = 0;
+  // programmatic dependent launch of the solver kernels (CDG_PDL=1: on)
+  int pdl = 0;
 };
 
 namespace cdg {
@@ -155,6 +159,17 @@ struct DevLevel {
   int mf_geo = -1;               // every cell a translate of cell 0 (-1: not checked)
   int mf_uniform = 0;            // the last assembly has one element matrix for all cells
   int mf_blocks_per_sm = 0;      // grid cap of the cell kernel (0: one cell per warp)
+  // one-launch sweep of a uniform level (k_mf_fused): rows cut into tiles of
+  // kMfTileRows; tile t recomputes the cells mf_tile_rp[t] .. mf_tile_rp[t+1]
+  // of the tile cell list, whose DOFs in cell 0's local order (kMfCellStride
+  // per cell, the last one padding) are mf_tile_gdof[kMfCellStride * c ..];
+  // entry e of the DOF-major order reads its local result at mf_ent_loc[e]
+  // (tile cell * kMfCellStride + local DOF) of the tile's shared memory
+  int mf_ntiles = 0;
+  int mf_tile_maxcells = 0;
+  int* mf_tile_rp = nullptr;
+  int* mf_tile_gdof = nullptr;
+  int* mf_ent_loc = nullptr;
   int tpr32 = 0;                 // FP32 CSR lanes per row (0: rows_per_warp_hint)
   // FP32 values from the tensor-core contraction, FP64 values not formed
   // (assemble_level_tc); last_a assembles them on demand (ensure_fp64)
@@ -236,6 +251,46 @@ inline int grid_for(long n, int block) {
     }                                                                          \
   } while (0)
 
+// Programmatic dependent launch: a solver kernel launched with
+// CDG_LAUNCH_PDL may be scheduled while its predecessor on the stream is
+// still running, so its blocks are resident when the predecessor ends instead
+// of being launched then.  Every such kernel starts with pdl_enter(): it waits
+// until the predecessor grid has completed and its memory is visible (so
+// nothing is read or written before then), and only then allows its own
+// successor to be scheduled -- at most two grids are in flight, and the chain
+// of waits keeps every earlier kernel complete.  Outside a programmatic
+// launch both instructions do nothing.
+__device__ __forceinline__ void pdl_enter() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+#define CDG_LAUNCH_PDL(ctx, kernel, grid, block, smem, ...)                    \
+  do {                                                                         \
+    cudaError_t le_;                                                           \
+    if ((ctx)->pdl) {                                                          \
+      cudaLaunchConfig_t cfg_ = {};                                            \
+      cfg_.gridDim = dim3(grid);                                               \
+      cfg_.blockDim = dim3(block);                                             \
+      cfg_.dynamicSmemBytes = (smem);                                          \
+      cfg_.stream = (ctx)->stream;                                             \
+      cudaLaunchAttribute at_[1];                                              \
+      at_[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;          \
+      at_[0].val.programmaticStreamSerializationAllowed = 1;                   \
+      cfg_.attrs = at_;                                                        \
+      cfg_.numAttrs = 1;                                                       \
+      le_ = cudaLaunchKernelEx(&cfg_, kernel, __VA_ARGS__);                    \
+    } else {                                                                   \
+      kernel<<<(grid), (block), (smem), (ctx)->stream>>>(__VA_ARGS__);         \
+      le_ = cudaGetLastError();                                                \
+    }                                                                          \
+    (ctx)->launches++;                                                         \
+    if (le_ != cudaSuccess) {                                                  \
+      cdg::set_error("launch %s: %s", #kernel, cudaGetErrorString(le_));       \
+      return CDG_ERR_CUDA;                                                     \
+    }                                                                          \
+  } while (0)
+
 // host launchers implemented in the .cu files
 int upload_level(cdg_context* ctx, DevLevel& L);
 // FE space numbering and CSR pattern built on the device (bit-exact with
@@ -270,11 +325,14 @@ int check_device_error(cdg_context* ctx);
 // matrix-free FP32 operator of Q2 hexahedral levels (matfree.cu); mode as
 // k_spmv: 0 y = Ax, 1 y = b - Ax, 2 Jacobi step, 3 Jacobi step + FP64 copy
 bool mf_eligible(const DevLevel& L);
+// tiles of the one-launch sweep of a uniform level (once per level)
+int mf_build_tiles(cdg_context* ctx, DevLevel& L);
 int mf_ensure(DevLevel& L);
 int mf_apply(cdg_context* ctx, const DevLevel& L, int mode, const float* x, const float* b,
              const float* invd, float w, float* y, double* z = nullptr, const int* di = nullptr,
-             double* zcur = nullptr);
+             double* zcur = nullptr, int two_kernel = 0);
 // y = A x with the FP32 multigrid operator of a level: 0 CSR, 1 matrix-free
+// (one launch on uniform levels), 2 the two-kernel matrix-free product
 int apply32(cdg_context* ctx, const DevLevel& L, int variant, const float* x, float* y);
 // generic coefficients (CoeffFct): quadrature points of a level (host) and the
 // assembly with eps, b, c, f per (cell, point)

@@ -74,6 +74,7 @@ k_spmv(int n, int nactive, const int* __restrict__ rp, const int* __restrict__ c
        const T* __restrict__ val, const T* __restrict__ x, const T* __restrict__ b,
        const T* __restrict__ invd, T w, T* __restrict__ y, double* __restrict__ z = nullptr,
        const int* di = nullptr, double* __restrict__ zcur = nullptr) {
+  pdl_enter();
   const long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
   const int row = (int)(gt / TPR);
   const int sub = threadIdx.x % TPR;
@@ -154,6 +155,7 @@ k_spmv_bulk(int n, int nactive, int nchunks, int stage, const int* __restrict__ 
             const int* __restrict__ rp, const int* __restrict__ col, const float* __restrict__ val,
             const float* __restrict__ x, const float* __restrict__ b,
             const float* __restrict__ invd, float w, float* __restrict__ y, int* err) {
+  pdl_enter();
   extern __shared__ __align__(16) unsigned char bulk_smem[];
   __shared__ __align__(8) unsigned long long bars[WARPS][2];
   const int wp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -246,7 +248,7 @@ static int launch_bulk(cdg_context* ctx, const DevLevel& L, const float* val, co
                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     configured_device = ctx->device;
   }
-  CDG_LAUNCH(ctx, (k_spmv_bulk<WARPS, TPR, MODE>), ctx->num_sms, WARPS * 32, smem, L.ndof,
+  CDG_LAUNCH_PDL(ctx, (k_spmv_bulk<WARPS, TPR, MODE>), ctx->num_sms, WARPS * 32, smem, L.ndof,
              L.nactive, L.bulk_nchunks, stage, L.bulk_row, L.row_ptr, L.col, val, x, b, invd, w, y,
              ctx->d_err);
   return CDG_OK;
@@ -283,10 +285,14 @@ static int spmv_t(cdg_context* ctx, const DevLevel& L, const T* val, const T* x,
   long threads = (long)L.ndof * tpr;
   int grid = (int)((threads + 255) / 256);
   switch (tpr) {
-    case 2: CDG_LAUNCH(ctx, (k_spmv<T, 2, 8, MODE>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y); break;
-    case 4: CDG_LAUNCH(ctx, (k_spmv<T, 4, 8, MODE>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y); break;
-    case 8: CDG_LAUNCH(ctx, (k_spmv<T, 8, 8, MODE>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y); break;
-    default: CDG_LAUNCH(ctx, (k_spmv<T, 16, 8, MODE>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y); break;
+    case 2: CDG_LAUNCH_PDL(ctx, (k_spmv<T, 2, 8, MODE>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y,
+                             (double*)nullptr, (const int*)nullptr, (double*)nullptr); break;
+    case 4: CDG_LAUNCH_PDL(ctx, (k_spmv<T, 4, 8, MODE>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y,
+                             (double*)nullptr, (const int*)nullptr, (double*)nullptr); break;
+    case 8: CDG_LAUNCH_PDL(ctx, (k_spmv<T, 8, 8, MODE>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y,
+                             (double*)nullptr, (const int*)nullptr, (double*)nullptr); break;
+    default: CDG_LAUNCH_PDL(ctx, (k_spmv<T, 16, 8, MODE>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y,
+                             (double*)nullptr, (const int*)nullptr, (double*)nullptr); break;
   }
   return CDG_OK;
 }
@@ -301,6 +307,7 @@ __global__ void __launch_bounds__(256)
 k_sell(int nslices, const long long* __restrict__ off, const int* __restrict__ srow,
        const int* __restrict__ scol, const T* __restrict__ sval, const T* __restrict__ x,
        const T* __restrict__ b, const T* __restrict__ invd, T w, T* __restrict__ y) {
+  pdl_enter();
   const int slice = (int)((blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
   if (slice >= nslices) return;              // warp-uniform
@@ -340,10 +347,10 @@ static int sell64_g(cdg_context* ctx, const DevLevel& L, const double* x, const 
   const int grid = (int)(((long)L.sell_nslices * 32 + 255) / 256);
   const double steps = (double)L.nnz / L.ndof / G;
   if (steps >= 24)
-    CDG_LAUNCH(ctx, (k_sell<double, G, 8, MODE>), grid, 256, 0, L.sell_nslices, L.sell_off,
+    CDG_LAUNCH_PDL(ctx, (k_sell<double, G, 8, MODE>), grid, 256, 0, L.sell_nslices, L.sell_off,
                L.sell_row, L.sell_col, L.sell_val, x, b, (const double*)nullptr, 0.0, y);
   else
-    CDG_LAUNCH(ctx, (k_sell<double, G, 4, MODE>), grid, 256, 0, L.sell_nslices, L.sell_off,
+    CDG_LAUNCH_PDL(ctx, (k_sell<double, G, 4, MODE>), grid, 256, 0, L.sell_nslices, L.sell_off,
                L.sell_row, L.sell_col, L.sell_val, x, b, (const double*)nullptr, 0.0, y);
   return CDG_OK;
 }
@@ -367,8 +374,9 @@ int spmv_apply64(cdg_context* ctx, const DevLevel& L, const double* x, double* y
   if (L.sell_nslices) return sell64<0>(ctx, L, x, nullptr, y);
   if (L.rows_per_warp_hint == 8) {
     int grid = (int)(((long)L.ndof * 4 + 255) / 256);
-    CDG_LAUNCH(ctx, (k_spmv<double, 4, 16, 0>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr,
-               L.col, L.val64, x, (const double*)nullptr, (const double*)nullptr, 0.0, y);
+    CDG_LAUNCH_PDL(ctx, (k_spmv<double, 4, 16, 0>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr,
+               L.col, L.val64, x, (const double*)nullptr, (const double*)nullptr, 0.0, y,
+                   (double*)nullptr, (const int*)nullptr, (double*)nullptr);
     return CDG_OK;
   }
   return spmv_t<double, 0>(ctx, L, L.val64, x, nullptr, nullptr, 0.0, y);
@@ -445,6 +453,7 @@ template <int MODE>
 __global__ void __launch_bounds__(256)
 k_dot(int n, const double* __restrict__ a, const double* __restrict__ b, double* partials,
       unsigned* cnt, double* out) {
+  pdl_enter();
   double s = 0.0;
   for (long i = blockIdx.x * 256L + threadIdx.x; i < n; i += (long)gridDim.x * 256)
     s += MODE == 0 ? a[i] * b[i] : a[i] * a[i];
@@ -457,6 +466,7 @@ k_dot(int n, const double* __restrict__ a, const double* __restrict__ b, double*
 __global__ void __launch_bounds__(256)
 k_mgs(int n, double* __restrict__ w, const double* __restrict__ vk, const double* hk,
       const double* __restrict__ vnext, double* partials, unsigned* cnt, double* out) {
+  pdl_enter();
   const double h = -(*hk);
   double s = 0.0;
   for (long i = blockIdx.x * 256L + threadIdx.x; i < n; i += (long)gridDim.x * 256) {
@@ -476,6 +486,7 @@ __global__ void __launch_bounds__(NT)
 k_multidot(int n, const double* __restrict__ w, const double* __restrict__ V, int k0, int cnt,
            double* partials, unsigned* counter, double* out, const int* di = nullptr,
            int hstride = 0) {
+  pdl_enter();
   static_assert(NT == 256, "one reducing warp per inner product of a group of 8");
   if (di) {
     // graph-captured loop: inner products k0 .. min(k0 + 32, i + 1) of column i
@@ -583,6 +594,7 @@ k_cgs_update(int n, double* __restrict__ w, const double* __restrict__ V, int i,
              double* __restrict__ hcol, double* partials, unsigned* counter, double* cs,
              double* sn, double* gs, double* resid, double* norm_out, const int* di = nullptr,
              int hstride = 0) {
+  pdl_enter();
   __shared__ double h[128];
   __shared__ bool last;
   if (di) {
@@ -656,9 +668,9 @@ int dot64(cdg_context* ctx, int n, const double* a, const double* b, double* out
   double* part = ctx->d_red + (size_t)slot * kRedMaxBlocks;
   unsigned* cnt = ctx->d_cnt + slot;
   if (b)
-    CDG_LAUNCH(ctx, k_dot<0>, red_grid(ctx, n), 256, 0, n, a, b, part, cnt, out);
+    CDG_LAUNCH_PDL(ctx, k_dot<0>, red_grid(ctx, n), 256, 0, n, a, b, part, cnt, out);
   else
-    CDG_LAUNCH(ctx, k_dot<1>, red_grid(ctx, n), 256, 0, n, a, a, part, cnt, out);
+    CDG_LAUNCH_PDL(ctx, k_dot<1>, red_grid(ctx, n), 256, 0, n, a, a, part, cnt, out);
   return CDG_OK;
 }
 
@@ -669,6 +681,7 @@ int dot64(cdg_context* ctx, int n, const double* a, const double* b, double* out
 // dst is the basis vector (*di + 1) of the block dst (graph-captured loop)
 __global__ void k_scale_inv(int n, const double* __restrict__ src, const double* s,
                             double* __restrict__ dst, int* err, const int* di = nullptr) {
+  pdl_enter();
   if (di) dst += (size_t)(*di + 1) * n;
   const double d = *s;
   if (d == 0.0) {
@@ -683,6 +696,7 @@ __global__ void k_scale_inv(int n, const double* __restrict__ src, const double*
 // c = a .* b; di != null: a and c are vector *di of their blocks, c2 gets a copy
 __global__ void k_mul(int n, const double* __restrict__ a, const double* __restrict__ b,
                       double* __restrict__ c, const int* di = nullptr, double* c2 = nullptr) {
+  pdl_enter();
   if (di) {
     a += (size_t)(*di) * n;
     c += (size_t)(*di) * n;
@@ -697,6 +711,7 @@ __global__ void k_mul(int n, const double* __restrict__ a, const double* __restr
 // c = a (no preconditioner), same indexing as k_mul
 __global__ void k_copy_idx(int n, const double* __restrict__ a, double* __restrict__ c,
                            const int* di, double* c2) {
+  pdl_enter();
   if (di) {
     a += (size_t)(*di) * n;
     c += (size_t)(*di) * n;
@@ -710,6 +725,7 @@ __global__ void k_copy_idx(int n, const double* __restrict__ a, double* __restri
 template <typename T>
 __global__ void k_mg_init(int n, int nactive, const double* __restrict__ v, T* __restrict__ rhs,
                           T* __restrict__ sol, const int* di = nullptr) {
+  pdl_enter();
   if (di) v += (size_t)(*di) * n;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     T r = (T)v[i];
@@ -721,6 +737,7 @@ __global__ void k_mg_init(int n, int nactive, const double* __restrict__ v, T* _
 template <typename T>
 __global__ void k_to_double(int n, const T* __restrict__ a, double* __restrict__ b,
                             const int* di = nullptr, double* b2 = nullptr) {
+  pdl_enter();
   if (di) b += (size_t)(*di) * n;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     const double v = (double)a[i];
@@ -736,6 +753,7 @@ __global__ void __launch_bounds__(256)
 k_prolong(int nf, int nactive_f, const int* __restrict__ rp, const int* __restrict__ col,
           const T* __restrict__ val, const T* __restrict__ xc, T* __restrict__ xf, T damp,
           int add) {
+  pdl_enter();
   const long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
   const int i = (int)(gt / TPR), sub = threadIdx.x % TPR;
   T s = 0;
@@ -751,6 +769,7 @@ template <typename T, int TPR>
 __global__ void __launch_bounds__(256)
 k_restrict(int nc, int nactive_c, const int* __restrict__ rp, const int* __restrict__ col,
            const T* __restrict__ val, const T* __restrict__ df, T* __restrict__ rc, int mask) {
+  pdl_enter();
   const long gt = blockIdx.x * (long)blockDim.x + threadIdx.x;
   const int j = (int)(gt / TPR), sub = threadIdx.x % TPR;
   T s = 0;
@@ -762,6 +781,7 @@ k_restrict(int nc, int nactive_c, const int* __restrict__ rp, const int* __restr
 
 template <typename T>
 __global__ void k_coarse_init(int n, int na, const T* __restrict__ b, T* __restrict__ x) {
+  pdl_enter();
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
     x[i] = i < na ? (T)0 : b[i];
 }
@@ -770,6 +790,7 @@ __global__ void k_coarse_init(int n, int na, const T* __restrict__ b, T* __restr
 template <typename T>
 __global__ void k_coarse_apply(int na, const double* __restrict__ inv, const T* __restrict__ d,
                                T* __restrict__ x) {
+  pdl_enter();
   const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, l = threadIdx.x & 31;
   if (row >= na) return;
   double s = 0.0;
@@ -791,6 +812,7 @@ __global__ void k_coarse_apply(int na, const double* __restrict__ inv, const T* 
 // ---------------------------------------------------------------------------
 __global__ void k_extract_dense(int na, const int* __restrict__ rp, const int* __restrict__ col,
                                 const double* __restrict__ val, double* __restrict__ M) {
+  pdl_enter();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= na) return;
   for (int k = rp[i]; k < rp[i + 1]; ++k)
@@ -855,6 +877,7 @@ __device__ __forceinline__ bool gj_step(int na, int k, const double* __restrict_
 __global__ void __launch_bounds__(256)
 k_gj_step(int na, int k, const double* __restrict__ Min, double* __restrict__ Mout,
           int* __restrict__ perm, int* err) {
+  pdl_enter();
   __shared__ double sv[8];
   __shared__ int si[8];
   gj_step(na, k, Min, Mout, perm, err, sv, si);
@@ -862,6 +885,7 @@ k_gj_step(int na, int k, const double* __restrict__ Min, double* __restrict__ Mo
 
 // column exchanges in reverse pivot order: inv[:, j] = M[:, q[j]]
 __global__ void k_gj_colmap(int na, const int* __restrict__ perm, int* __restrict__ q) {
+  pdl_enter();
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
   for (int j = 0; j < na; ++j) q[j] = j;
   for (int k = na - 1; k >= 0; --k) {
@@ -873,6 +897,7 @@ __global__ void k_gj_colmap(int na, const int* __restrict__ perm, int* __restric
 
 __global__ void k_gj_unpermute(int na, const double* __restrict__ M, const int* __restrict__ q,
                                double* __restrict__ inv) {
+  pdl_enter();
   for (int i = blockIdx.x; i < na; i += gridDim.x)
     for (int j = threadIdx.x; j < na; j += blockDim.x)
       inv[(size_t)i * na + j] = M[(size_t)i * na + q[j]];
@@ -882,6 +907,7 @@ __global__ void k_gj_unpermute(int na, const double* __restrict__ M, const int* 
 // every block sees the same pivot, so all blocks leave together on a zero pivot
 __global__ void __launch_bounds__(256)
 k_gj_coop(int na, double* A, double* B, int* perm, int* q, double* inv, int* err) {
+  pdl_enter();
   __shared__ double sv[8];
   __shared__ int si[8];
   cgrp::grid_group grid = cgrp::this_grid();
@@ -915,6 +941,7 @@ constexpr int kGjSmemThreads = 1024;
 
 __global__ void __launch_bounds__(kGjSmemThreads)
 k_gj_smem(int na, const double* __restrict__ Ain, double* __restrict__ inv, int* err) {
+  pdl_enter();
   extern __shared__ double sm[];
   double* a = sm;                       // na * na
   double* prow = a + (size_t)na * na;   // na
@@ -1012,7 +1039,7 @@ static int coarse_inverse(cdg_context* ctx, DevLevel& C) {
   int* perm = (int*)(C.coarse_work + 2 * sz);
   int* q = perm + na;
   CDG_CUDA(cudaMemsetAsync(A, 0, sz * sizeof(double), ctx->stream));
-  CDG_LAUNCH(ctx, k_extract_dense, grid_for<int>(na, 128), 128, 0, na, C.row_ptr, C.col, C.val64, A);
+  CDG_LAUNCH_PDL(ctx, k_extract_dense, grid_for<int>(na, 128), 128, 0, na, C.row_ptr, C.col, C.val64, A);
   // the grid-wide kernel (a pivot step costs one grid sync); one CTA holding
   // the block in shared memory where cooperative launches are unavailable.
   // Measured on GB300: grid-wide 0.54 ms (125 rows) / 2.25 ms (343 rows), one
@@ -1031,7 +1058,7 @@ static int coarse_inverse(cdg_context* ctx, DevLevel& C) {
   const size_t smem = gj_smem_bytes(na);
   if (!(coop && per_sm > 0) && smem <= 220 * 1024) {
     CDG_CUDA(cudaFuncSetAttribute(k_gj_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    CDG_LAUNCH(ctx, k_gj_smem, 1, kGjSmemThreads, smem, na, A, C.coarse_inv, ctx->d_err);
+    CDG_LAUNCH_PDL(ctx, k_gj_smem, 1, kGjSmemThreads, smem, na, A, C.coarse_inv, ctx->d_err);
     return CDG_OK;
   }
   if (coop && per_sm > 0 && g >= 1) {
@@ -1045,11 +1072,11 @@ static int coarse_inverse(cdg_context* ctx, DevLevel& C) {
   }
   for (int k = 0; k < na; ++k) {
     int gg = std::min(na, ctx->num_sms * 4);
-    CDG_LAUNCH(ctx, k_gj_step, gg, 256, 0, na, k, A, B, perm, ctx->d_err);
+    CDG_LAUNCH_PDL(ctx, k_gj_step, gg, 256, 0, na, k, A, B, perm, ctx->d_err);
     std::swap(A, B);
   }
-  CDG_LAUNCH(ctx, k_gj_colmap, 1, 32, 0, na, perm, q);
-  CDG_LAUNCH(ctx, k_gj_unpermute, std::min(na, ctx->num_sms * 4), 256, 0, na, A, q, C.coarse_inv);
+  CDG_LAUNCH_PDL(ctx, k_gj_colmap, 1, 32, 0, na, perm, q);
+  CDG_LAUNCH_PDL(ctx, k_gj_unpermute, std::min(na, ctx->num_sms * 4), 256, 0, na, A, q, C.coarse_inv);
   return CDG_OK;
 }
 
@@ -1098,10 +1125,10 @@ static int smooth_out(cdg_context* ctx, const DevLevel& L, const T* val, const T
   const int tpr = std::is_same<T, float>::value && L.tpr32 ? L.tpr32 : L.rows_per_warp_hint;
   const int grid = (int)(((long)L.ndof * tpr + 255) / 256);
   switch (tpr) {
-    case 2: CDG_LAUNCH(ctx, (k_spmv<T, 2, 8, 3>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y, z, di, zcur); break;
-    case 4: CDG_LAUNCH(ctx, (k_spmv<T, 4, 8, 3>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y, z, di, zcur); break;
-    case 8: CDG_LAUNCH(ctx, (k_spmv<T, 8, 8, 3>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y, z, di, zcur); break;
-    default: CDG_LAUNCH(ctx, (k_spmv<T, 16, 8, 3>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y, z, di, zcur); break;
+    case 2: CDG_LAUNCH_PDL(ctx, (k_spmv<T, 2, 8, 3>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y, z, di, zcur); break;
+    case 4: CDG_LAUNCH_PDL(ctx, (k_spmv<T, 4, 8, 3>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y, z, di, zcur); break;
+    case 8: CDG_LAUNCH_PDL(ctx, (k_spmv<T, 8, 8, 3>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y, z, di, zcur); break;
+    default: CDG_LAUNCH_PDL(ctx, (k_spmv<T, 16, 8, 3>), grid, 256, 0, L.ndof, L.nactive, L.row_ptr, L.col, val, x, b, invd, w, y, z, di, zcur); break;
   }
   return CDG_OK;
 }
@@ -1112,11 +1139,11 @@ static int sell_mg(cdg_context* ctx, const DevLevel& L, const T* val, const T* x
                    const T* invd, T w, T* y) {
   const int grid = (int)(((long)L.sell_nslices * 32 + 255) / 256);
   switch (L.sell_lanes) {
-    case 1: CDG_LAUNCH(ctx, (k_sell<T, 1, 8, MODE>), grid, 256, 0, L.sell_nslices, L.sell_off, L.sell_row, L.sell_col, val, x, b, invd, w, y); break;
-    case 2: CDG_LAUNCH(ctx, (k_sell<T, 2, 8, MODE>), grid, 256, 0, L.sell_nslices, L.sell_off, L.sell_row, L.sell_col, val, x, b, invd, w, y); break;
-    case 4: CDG_LAUNCH(ctx, (k_sell<T, 4, 8, MODE>), grid, 256, 0, L.sell_nslices, L.sell_off, L.sell_row, L.sell_col, val, x, b, invd, w, y); break;
-    case 8: CDG_LAUNCH(ctx, (k_sell<T, 8, 8, MODE>), grid, 256, 0, L.sell_nslices, L.sell_off, L.sell_row, L.sell_col, val, x, b, invd, w, y); break;
-    default: CDG_LAUNCH(ctx, (k_sell<T, 16, 8, MODE>), grid, 256, 0, L.sell_nslices, L.sell_off, L.sell_row, L.sell_col, val, x, b, invd, w, y); break;
+    case 1: CDG_LAUNCH_PDL(ctx, (k_sell<T, 1, 8, MODE>), grid, 256, 0, L.sell_nslices, L.sell_off, L.sell_row, L.sell_col, val, x, b, invd, w, y); break;
+    case 2: CDG_LAUNCH_PDL(ctx, (k_sell<T, 2, 8, MODE>), grid, 256, 0, L.sell_nslices, L.sell_off, L.sell_row, L.sell_col, val, x, b, invd, w, y); break;
+    case 4: CDG_LAUNCH_PDL(ctx, (k_sell<T, 4, 8, MODE>), grid, 256, 0, L.sell_nslices, L.sell_off, L.sell_row, L.sell_col, val, x, b, invd, w, y); break;
+    case 8: CDG_LAUNCH_PDL(ctx, (k_sell<T, 8, 8, MODE>), grid, 256, 0, L.sell_nslices, L.sell_off, L.sell_row, L.sell_col, val, x, b, invd, w, y); break;
+    default: CDG_LAUNCH_PDL(ctx, (k_sell<T, 16, 8, MODE>), grid, 256, 0, L.sell_nslices, L.sell_off, L.sell_row, L.sell_col, val, x, b, invd, w, y); break;
   }
   return CDG_OK;
 }
@@ -1189,6 +1216,7 @@ __global__ void __launch_bounds__(256)
 k_first_smooth(int n, int nactive, int with_dirichlet, const int* __restrict__ dc_rp,
                const int* __restrict__ dc_col, const T* __restrict__ dcv,
                const T* __restrict__ b, const T* __restrict__ invd, T w, T* __restrict__ x1) {
+  pdl_enter();
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     if (i < nactive) {
       T s = 0;
@@ -1211,6 +1239,7 @@ k_first_smooth_init(int n, int nactive, const int* __restrict__ dc_rp,
                     const int* __restrict__ dc_col, const T* __restrict__ dcv,
                     const double* __restrict__ v, const T* __restrict__ invd, T w,
                     T* __restrict__ rhs, T* __restrict__ x1, const int* di) {
+  pdl_enter();
   if (di) v += (size_t)(*di) * n;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     const T bi = (T)v[i];
@@ -1226,7 +1255,7 @@ k_first_smooth_init(int n, int nactive, const int* __restrict__ dc_rp,
 
 template <typename T>
 static int first_smooth(cdg_context* ctx, DevLevel& L, T damp, bool finest) {
-  CDG_LAUNCH(ctx, k_first_smooth<T>, vec_grid(ctx, L.ndof), 256, 0, L.ndof, L.nactive,
+  CDG_LAUNCH_PDL(ctx, k_first_smooth<T>, vec_grid(ctx, L.ndof), 256, 0, L.ndof, L.nactive,
              finest ? 1 : 0, L.dc_rp, L.dc_col, Prec<T>::dcv(L), (const T*)L.mg_rhs,
              Prec<T>::invd(L), damp, (T*)L.mg_tmp);
   std::swap(L.mg_sol, L.mg_tmp);
@@ -1249,7 +1278,7 @@ static int defect(cdg_context* ctx, DevLevel& L) {
 // update_solution_in_finer_grid: fine.sol += damp * P coarse.sol on actives
 template <typename T>
 static int prolong_correct(cdg_context* ctx, DevLevel& F, DevLevel& C, T damp) {
-  CDG_LAUNCH(ctx, (k_prolong<T, 2>), grid_for<int>((long)F.ndof * 2, 256), 256, 0, F.ndof,
+  CDG_LAUNCH_PDL(ctx, (k_prolong<T, 2>), grid_for<int>((long)F.ndof * 2, 256), 256, 0, F.ndof,
              F.nactive, F.P_rp, F.P_col, Prec<T>::P(F), (const T*)C.mg_sol, (T*)F.mg_sol, damp, 1);
   return CDG_OK;
 }
@@ -1258,10 +1287,10 @@ template <typename T>
 static int coarse_solve(cdg_context* ctx, DevLevel& C, const cdg_solver_params& s) {
   if (s.multigrid_smoother_coarse == 0) {
     // direct_solve: x = A^-1 rhs (idempotent, one application suffices)
-    CDG_LAUNCH(ctx, k_coarse_init<T>, vec_grid(ctx, C.ndof), 256, 0, C.ndof, C.nactive,
+    CDG_LAUNCH_PDL(ctx, k_coarse_init<T>, vec_grid(ctx, C.ndof), 256, 0, C.ndof, C.nactive,
                (const T*)C.mg_rhs, (T*)C.mg_sol);
     CDG_TRY(defect<T>(ctx, C));
-    CDG_LAUNCH(ctx, k_coarse_apply<T>, grid_for<int>((long)C.nactive * 32, 256), 256, 0,
+    CDG_LAUNCH_PDL(ctx, k_coarse_apply<T>, grid_for<int>((long)C.nactive * 32, 256), 256, 0,
                C.nactive, C.coarse_inv, (const T*)C.mg_def, (T*)C.mg_sol);
     return CDG_OK;
   }
@@ -1308,12 +1337,12 @@ static int mg_cycle(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s
   // smoothing step also does the start (rhs = v, x0 = Dirichlet values)
   const bool fused_start = nl > 1 && s.multigrid_n_pre_smooth > 0;
   if (fused_start) {
-    CDG_LAUNCH(ctx, k_first_smooth_init<T>, vec_grid(ctx, F.ndof), 256, 0, F.ndof, F.nactive,
+    CDG_LAUNCH_PDL(ctx, k_first_smooth_init<T>, vec_grid(ctx, F.ndof), 256, 0, F.ndof, F.nactive,
                F.dc_rp, F.dc_col, Prec<T>::dcv(F), v, Prec<T>::invd(F),
                (T)s.jacobi_damp, (T*)F.mg_rhs, (T*)F.mg_tmp, di);
     std::swap(F.mg_sol, F.mg_tmp);
   } else {
-    CDG_LAUNCH(ctx, k_mg_init<T>, vec_grid(ctx, F.ndof), 256, 0, F.ndof, F.nactive, v,
+    CDG_LAUNCH_PDL(ctx, k_mg_init<T>, vec_grid(ctx, F.ndof), 256, 0, F.ndof, F.nactive, v,
                (T*)F.mg_rhs, (T*)F.mg_sol, di);
   }
   // the FP64 result of the last finest-level smoothing step goes to z directly
@@ -1377,7 +1406,7 @@ static int mg_cycle(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s
         if (read_start)
           CDG_CUDA(cudaMemsetAsync(C.mg_sol, 0, (size_t)C.ndof * sizeof(T), ctx->stream));
         C.mg_visited = false;   // zero start iterate again: shortcut valid
-        CDG_LAUNCH(ctx, (k_restrict<T, 8>), grid_for<int>((long)C.ndof * 8, 256), 256, 0,
+        CDG_LAUNCH_PDL(ctx, (k_restrict<T, 8>), grid_for<int>((long)C.ndof * 8, 256), 256, 0,
                    C.ndof, C.nactive, L.R_rp, L.R_col, Prec<T>::R(L), (const T*)L.mg_def,
                    (T*)C.mg_rhs, 1);
         level -= 1;
@@ -1390,7 +1419,7 @@ static int mg_cycle(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s
     }
   }
   if (!z_written)
-    CDG_LAUNCH(ctx, k_to_double<T>, vec_grid(ctx, F.ndof), 256, 0, F.ndof, (const T*)F.mg_sol, z,
+    CDG_LAUNCH_PDL(ctx, k_to_double<T>, vec_grid(ctx, F.ndof), 256, 0, F.ndof, (const T*)F.mg_sol, z,
                di, zcur);
   return CDG_OK;
 }
@@ -1412,7 +1441,9 @@ int ensure_mg_vectors(cdg_context* ctx, DevLevel& L, int elem) {
 // y = A x with the FP32 multigrid operator of a level (identity on
 // non-active rows): variant 0 the CSR kernel, 1 the matrix-free kernel
 int apply32(cdg_context* ctx, const DevLevel& L, int variant, const float* x, float* y) {
-  if (variant == 1) return mf_apply(ctx, L, 0, x, nullptr, nullptr, 0.f, y);
+  if (variant >= 1)
+    return mf_apply(ctx, L, 0, x, nullptr, nullptr, 0.f, y, nullptr, nullptr, nullptr,
+                    variant == 2 ? 1 : 0);
   return spmv_t<float, 0>(ctx, L, L.val32, x, (const float*)nullptr, (const float*)nullptr, 0.f,
                           y);
 }
@@ -1510,8 +1541,14 @@ static int tune_level(cdg_context* ctx, cdg_problem* p, DevLevel& L, int level) 
   // matrix-free grid, then the faster kind
   if (rc == CDG_OK && L.mf_valid && mf_env != 0) {
     L.mf_mode = 1;
-    if (cap_env >= 0) {
+    if (L.mf_uniform && L.mf_ntiles > 0) {
+      // the one-launch sweep has one block per row tile: no grid to choose
+      // (reported as -1)
+      L.mf_blocks_per_sm = -1;
+      time_step(&L.tuned_ms[1]);
+    } else if (cap_env >= 0) {
       L.mf_blocks_per_sm = cap_env;
+      time_step(&L.tuned_ms[1]);
     } else {
       float best = 1e30f;
       int bc = 0;
@@ -1581,7 +1618,7 @@ int precondition(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s, c
                  double* z, const int* di, double* zcur) {
   DevLevel& F = p->lev[0];
   if (s.preconditioner == 1) {
-    CDG_LAUNCH(ctx, k_mul, vec_grid(ctx, F.ndof), 256, 0, F.ndof, v, F.invdiag64, z, di, zcur);
+    CDG_LAUNCH_PDL(ctx, k_mul, vec_grid(ctx, F.ndof), 256, 0, F.ndof, v, F.invdiag64, z, di, zcur);
     return CDG_OK;
   }
   if (s.preconditioner == 2) {
@@ -1589,7 +1626,7 @@ int precondition(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s, c
     return mg_cycle<double>(ctx, p, s, v, z, di, zcur);
   }
   if (di) {
-    CDG_LAUNCH(ctx, k_copy_idx, vec_grid(ctx, F.ndof), 256, 0, F.ndof, v, z, di, zcur);
+    CDG_LAUNCH_PDL(ctx, k_copy_idx, vec_grid(ctx, F.ndof), 256, 0, F.ndof, v, z, di, zcur);
     return CDG_OK;
   }
   CDG_CUDA(cudaMemcpyAsync(z, v, (size_t)F.ndof * sizeof(double), cudaMemcpyDeviceToDevice,
@@ -1599,14 +1636,14 @@ int precondition(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s, c
 
 int prolongate64(cdg_context* ctx, const DevLevel& F, const double* xc, double* xf,
                  int add_actives_only, double damp) {
-  CDG_LAUNCH(ctx, (k_prolong<double, 2>), grid_for<int>((long)F.ndof * 2, 256), 256, 0, F.ndof,
+  CDG_LAUNCH_PDL(ctx, (k_prolong<double, 2>), grid_for<int>((long)F.ndof * 2, 256), 256, 0, F.ndof,
              F.nactive, F.P_rp, F.P_col, F.P_val, xc, xf, damp, add_actives_only);
   return CDG_OK;
 }
 
 int restrict64(cdg_context* ctx, const DevLevel& F, const DevLevel& C, const double* df,
                double* rc) {
-  CDG_LAUNCH(ctx, (k_restrict<double, 8>), grid_for<int>((long)C.ndof * 8, 256), 256, 0,
+  CDG_LAUNCH_PDL(ctx, (k_restrict<double, 8>), grid_for<int>((long)C.ndof * 8, 256), 256, 0,
              C.ndof, C.nactive, F.R_rp, F.R_col, F.R_val, df, rc, 0);
   return CDG_OK;
 }
@@ -1616,11 +1653,13 @@ int restrict64(cdg_context* ctx, const DevLevel& F, const DevLevel& C, const dou
 // ---------------------------------------------------------------------------
 __global__ void k_givens(int i, int m, double* H, double* cs, double* sn, double* s,
                          double* resid) {
+  pdl_enter();
   givens_column(i, H + (size_t)i * (m + 1), cs, sn, s, resid);
 }
 
 // s = (beta, 0, ..., 0)
 __global__ void k_init_s(int m, const double* beta, double* s) {
+  pdl_enter();
   for (int i = threadIdx.x; i <= m; i += blockDim.x) s[i] = i == 0 ? *beta : 0.0;
 }
 
@@ -1633,6 +1672,7 @@ constexpr int kBacksolveThreads = 128;
 __global__ void __launch_bounds__(kBacksolveThreads)
 k_backsolve(int k, int m, const double* __restrict__ H, const double* __restrict__ s,
             double* __restrict__ y) {
+  pdl_enter();
   extern __shared__ double bs[];
   double* ys = bs;               // k + 1
   double* hs = bs + (k + 1);     // column i at hs[i * (k + 1)], rows 0..i
@@ -1659,13 +1699,14 @@ static int launch_backsolve(cdg_context* ctx, int k, int m, const double* H, con
   // restarts up to 120: at most 120 * 121 doubles (the attribute is per device)
   CDG_CUDA(cudaFuncSetAttribute(k_backsolve, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)(120 * 121 * sizeof(double))));
-  CDG_LAUNCH(ctx, k_backsolve, 1, kBacksolveThreads, smem, k, m, H, s, y);
+  CDG_LAUNCH_PDL(ctx, k_backsolve, 1, kBacksolveThreads, smem, k, m, H, s, y);
   return CDG_OK;
 }
 
 // x += sum_j y_j z_j (accumulated from zero in order j = 0..k, then added)
 __global__ void k_update(int n, int k, const double* __restrict__ Z, const double* __restrict__ y,
                          double* __restrict__ x) {
+  pdl_enter();
   __shared__ double ys[128];
   for (int j = threadIdx.x; j <= k; j += blockDim.x) ys[j] = y[j];
   __syncthreads();
@@ -1770,6 +1811,7 @@ __device__ int conv_test(const ConvParams& c, double* li, double res, int it) {
 // st: [0] column i, [1] iteration j, [2] flag (0 run, 1 converged,
 // 2 diverged, 3 end of the restart cycle)
 __global__ void k_fgmres_start(ConvParams c, int* st, const double* beta, double* li) {
+  pdl_enter();
   st[0] = 0;
   st[1] = 1;
   st[2] = conv_test(c, li, *beta, 0);
@@ -1777,6 +1819,7 @@ __global__ void k_fgmres_start(ConvParams c, int* st, const double* beta, double
 
 __global__ void k_fgmres_iter_check(ConvParams c, int* st, const double* resid, double* li,
                                     cudaGraphConditionalHandle h) {
+  pdl_enter();
   const int i = st[0], j = st[1];
   const int cv = conv_test(c, li, *resid, j);
   unsigned cont = 0;
@@ -1797,6 +1840,7 @@ __global__ void k_fgmres_iter_check(ConvParams c, int* st, const double* resid, 
 
 // after a full cycle: the test with the last estimate at iteration j
 __global__ void k_fgmres_restart_check(ConvParams c, int* st, const double* resid, double* li) {
+  pdl_enter();
   st[2] = conv_test(c, li, *resid, st[1]);
   st[0] = 0;
 }
@@ -1817,12 +1861,12 @@ static int iteration_body(cdg_context* ctx, cdg_problem* p, const cdg_solver_par
   CDG_TRY(spmv_apply64(ctx, L, g.zcur, g.w));
   const int mg = std::min(red_grid(ctx, n), ctx->num_sms * 2);
   for (int k0 = 0; k0 < m; k0 += 32)
-    CDG_LAUNCH(ctx, k_multidot<256>, mg, 256, 0, n, g.w, g.V, k0, 0, ctx->d_red,
+    CDG_LAUNCH_PDL(ctx, k_multidot<256>, mg, 256, 0, n, g.w, g.V, k0, 0, ctx->d_red,
                ctx->d_cnt + 1, g.H, di, m + 1);
-  CDG_LAUNCH(ctx, k_cgs_update, red_grid(ctx, n), 256, 0, n, g.w, g.V, 0, g.H, ctx->d_red,
+  CDG_LAUNCH_PDL(ctx, k_cgs_update, red_grid(ctx, n), 256, 0, n, g.w, g.V, 0, g.H, ctx->d_red,
              ctx->d_cnt, g.cs, g.sn, g.s, g.scal + 0, g.scal + 2, di, m + 1);
-  CDG_LAUNCH(ctx, k_scale_inv, vec_grid(ctx, n), 256, 0, n, g.w, g.scal + 2, g.V, ctx->d_err, di);
-  CDG_LAUNCH(ctx, k_fgmres_iter_check, 1, 1, 0, conv_params(s), g.dstate, g.scal + 0,
+  CDG_LAUNCH_PDL(ctx, k_scale_inv, vec_grid(ctx, n), 256, 0, n, g.w, g.scal + 2, g.V, ctx->d_err, di);
+  CDG_LAUNCH_PDL(ctx, k_fgmres_iter_check, 1, 1, 0, conv_params(s), g.dstate, g.scal + 0,
              g.scal + 4, h);
   return CDG_OK;
 }
@@ -1930,6 +1974,7 @@ k_fgmres_cycle_jacobi(int n, int nactive, int m, ConvParams cp, const int* __res
                       double* __restrict__ Z, double* __restrict__ H, double* __restrict__ cs,
                       double* __restrict__ sn, double* __restrict__ s, double* __restrict__ scal,
                       int* __restrict__ st, double* __restrict__ part, int* err) {
+  pdl_enter();
   cgrp::grid_group grid = cgrp::this_grid();
   __shared__ double tr[8][kCycleThreads + 1];
   __shared__ double hc[kCycleMaxM + 2];
@@ -2110,17 +2155,27 @@ static int fgmres_graph(cdg_context* ctx, cdg_problem* p, const cdg_solver_param
       if (need <= (long)ctx->num_sms * per_sm) cycle_blocks = (int)std::max<long>(1, need);
     }
   }
-  // a graph that cannot be built (capture rejected) falls back to the host loop
-  if (!cycle_blocks && ensure_iteration_graph(ctx, p, s) != CDG_OK) {
-    cudaGetLastError();
-    return kGraphUnavailable;
+  // a graph that cannot be built (capture rejected) falls back to the host
+  // loop; one whose programmatic launch edges are rejected is built without
+  if (!cycle_blocks) {
+    int rc = ensure_iteration_graph(ctx, p, s);
+    if (rc != CDG_OK && ctx->pdl) {
+      cudaGetLastError();
+      ctx->pdl = 0;
+      rc = ensure_iteration_graph(ctx, p, s);
+      ctx->pdl = 1;
+    }
+    if (rc != CDG_OK) {
+      cudaGetLastError();
+      return kGraphUnavailable;
+    }
   }
   if (cycle_blocks && g.part == nullptr)
     CDG_CUDA(cudaMalloc(&g.part, ((size_t)ctx->num_sms * 8 * (kCycleMaxM + 2)) * sizeof(double)));
   // r = b - A x; beta = ||r||; the test at iteration 0
   CDG_TRY(residual64(ctx, L, b, x, g.w));
   CDG_TRY(dot64(ctx, n, g.w, nullptr, beta_d, 0));
-  CDG_LAUNCH(ctx, k_fgmres_start, 1, 1, 0, cp, g.dstate, beta_d, g.scal + 4);
+  CDG_LAUNCH_PDL(ctx, k_fgmres_start, 1, 1, 0, cp, g.dstate, beta_d, g.scal + 4);
   int sv[4];
   double beta = 0;
   CDG_CUDA(cudaMemcpyAsync(sv, g.dstate, 4 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -2131,8 +2186,9 @@ static int fgmres_graph(cdg_context* ctx, cdg_problem* p, const cdg_solver_param
   if (sv[2] != 0) return CDG_OK;
   double resid = beta;
   for (;;) {
-    CDG_LAUNCH(ctx, k_scale_inv, vg, 256, 0, n, g.w, beta_d, g.V, ctx->d_err);
-    CDG_LAUNCH(ctx, k_init_s, 1, 128, 0, m, beta_d, g.s);
+    CDG_LAUNCH_PDL(ctx, k_scale_inv, vg, 256, 0, n, g.w, beta_d, g.V, ctx->d_err,
+                   (const int*)nullptr);
+    CDG_LAUNCH_PDL(ctx, k_init_s, 1, 128, 0, m, beta_d, g.s);
     if (cycle_blocks) {
       const int* rp = L.row_ptr;
       const int* cl = L.col;
@@ -2162,17 +2218,17 @@ static int fgmres_graph(cdg_context* ctx, cdg_problem* p, const cdg_solver_param
     }
     if (flag == 1) {
       CDG_TRY(launch_backsolve(ctx, i, m, g.H, g.s, g.y));
-      CDG_LAUNCH(ctx, k_update, vg, 256, 0, n, i, g.Z, g.y, x);
+      CDG_LAUNCH_PDL(ctx, k_update, vg, 256, 0, n, i, g.Z, g.y, x);
       st->iterations = j;
       st->residual = resid;
       return CDG_OK;
     }
     // end of the restart cycle: update x, new residual, test
     CDG_TRY(launch_backsolve(ctx, m - 1, m, g.H, g.s, g.y));
-    CDG_LAUNCH(ctx, k_update, vg, 256, 0, n, m - 1, g.Z, g.y, x);
+    CDG_LAUNCH_PDL(ctx, k_update, vg, 256, 0, n, m - 1, g.Z, g.y, x);
     CDG_TRY(residual64(ctx, L, b, x, g.w));
     CDG_TRY(dot64(ctx, n, g.w, nullptr, beta_d, 0));
-    CDG_LAUNCH(ctx, k_fgmres_restart_check, 1, 1, 0, cp, g.dstate, g.scal + 0, g.scal + 4);
+    CDG_LAUNCH_PDL(ctx, k_fgmres_restart_check, 1, 1, 0, cp, g.dstate, g.scal + 0, g.scal + 4);
     CDG_TRY(read_state(ctx, g, sv, &resid));
     if (sv[2] == 2) {
       set_error("Execution of the code stopped because of solver divergence.");
@@ -2225,8 +2281,9 @@ int fgmres(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s, cdg_sol
   int j = 1;
   const int vg = vec_grid(ctx, n);
   while (j <= s.max_n_iterations) {
-    CDG_LAUNCH(ctx, k_scale_inv, vg, 256, 0, n, g.w, beta_d, g.V, ctx->d_err);
-    CDG_LAUNCH(ctx, k_init_s, 1, 128, 0, m, beta_d, g.s);
+    CDG_LAUNCH_PDL(ctx, k_scale_inv, vg, 256, 0, n, g.w, beta_d, g.V, ctx->d_err,
+                   (const int*)nullptr);
+    CDG_LAUNCH_PDL(ctx, k_init_s, 1, 128, 0, m, beta_d, g.s);
     int i;
     for (i = 0; i < m && j <= s.max_n_iterations; ++i, ++j) {
       double* vi = g.V + (size_t)i * n;
@@ -2239,27 +2296,29 @@ int fgmres(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s, cdg_sol
         for (int k0 = 0; k0 <= i; k0 += 32) {
           int cnt = std::min(32, i + 1 - k0);
           // two blocks per SM: several elements per thread, fewer FP64 reductions
-          CDG_LAUNCH(ctx, k_multidot<256>, std::min(red_grid(ctx, n), ctx->num_sms * 2), 256, 0,
-                     n, g.w, g.V, k0, cnt, ctx->d_red, ctx->d_cnt + 1, col + k0);
+          CDG_LAUNCH_PDL(ctx, k_multidot<256>, std::min(red_grid(ctx, n), ctx->num_sms * 2), 256, 0,
+                     n, g.w, g.V, k0, cnt, ctx->d_red, ctx->d_cnt + 1, col + k0,
+                     (const int*)nullptr, 0);
         }
-        CDG_LAUNCH(ctx, k_cgs_update, red_grid(ctx, n), 256, 0, n, g.w, g.V, i, col,
-                   ctx->d_red, ctx->d_cnt, g.cs, g.sn, g.s, resid_d, g.scal + 2);
-        CDG_LAUNCH(ctx, k_scale_inv, vg, 256, 0, n, g.w, g.scal + 2,
-                   g.V + (size_t)(i + 1) * n, ctx->d_err);
+        CDG_LAUNCH_PDL(ctx, k_cgs_update, red_grid(ctx, n), 256, 0, n, g.w, g.V, i, col,
+                   ctx->d_red, ctx->d_cnt, g.cs, g.sn, g.s, resid_d, g.scal + 2,
+                   (const int*)nullptr, 0);
+        CDG_LAUNCH_PDL(ctx, k_scale_inv, vg, 256, 0, n, g.w, g.scal + 2,
+                   g.V + (size_t)(i + 1) * n, ctx->d_err, (const int*)nullptr);
       } else {
         // modified: dot and update interleaved (sequential build)
         CDG_TRY(dot64(ctx, n, g.w, g.V, col + 0, 0));
         for (int k = 0; k <= i; ++k) {
           const double* vk = g.V + (size_t)k * n;
           const double* vn = (k < i) ? g.V + (size_t)(k + 1) * n : nullptr;
-          CDG_LAUNCH(ctx, k_mgs, red_grid(ctx, n), 256, 0, n, g.w, vk, col + k, vn,
+          CDG_LAUNCH_PDL(ctx, k_mgs, red_grid(ctx, n), 256, 0, n, g.w, vk, col + k, vn,
                      ctx->d_red, ctx->d_cnt, col + k + 1);
         }
       }
       if (s.gram_schmidt != 0) {
-        CDG_LAUNCH(ctx, k_scale_inv, vg, 256, 0, n, g.w, col + i + 1,
-                   g.V + (size_t)(i + 1) * n, ctx->d_err);
-        CDG_LAUNCH(ctx, k_givens, 1, 1, 0, i, m, g.H, g.cs, g.sn, g.s, resid_d);
+        CDG_LAUNCH_PDL(ctx, k_scale_inv, vg, 256, 0, n, g.w, col + i + 1,
+                   g.V + (size_t)(i + 1) * n, ctx->d_err, (const int*)nullptr);
+        CDG_LAUNCH_PDL(ctx, k_givens, 1, 1, 0, i, m, g.H, g.cs, g.sn, g.s, resid_d);
       }
       CDG_TRY(read_scalar(ctx, resid_d, &resid));
       CDG_TRY(check_device_error(ctx));
@@ -2272,14 +2331,14 @@ int fgmres(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s, cdg_sol
       }
       if (cv) {
         CDG_TRY(launch_backsolve(ctx, i, m, g.H, g.s, g.y));
-        CDG_LAUNCH(ctx, k_update, vg, 256, 0, n, i, g.Z, g.y, x);
+        CDG_LAUNCH_PDL(ctx, k_update, vg, 256, 0, n, i, g.Z, g.y, x);
         st->iterations = j;
         st->residual = resid;
         return CDG_OK;
       }
     }
     CDG_TRY(launch_backsolve(ctx, m - 1, m, g.H, g.s, g.y));
-    CDG_LAUNCH(ctx, k_update, vg, 256, 0, n, m - 1, g.Z, g.y, x);
+    CDG_LAUNCH_PDL(ctx, k_update, vg, 256, 0, n, m - 1, g.Z, g.y, x);
     CDG_TRY(residual64(ctx, L, b, x, g.w));
     CDG_TRY(dot64(ctx, n, g.w, nullptr, beta_d, 0));
     CDG_TRY(read_scalar(ctx, beta_d, &beta));

@@ -29,6 +29,10 @@
 // the rhs gather); k_mf_gather sums a row's range (deterministic, no atomics)
 // and applies the smoothing / defect update.  Non-active rows act as identity
 // rows, as in the CSR kernels.
+#include <algorithm>
+#include <cstdlib>
+#include <vector>
+
 #include "common.cuh"
 
 namespace cdg {
@@ -38,6 +42,8 @@ namespace {
 constexpr int kMfWarps = 8;            // cells in flight per block
 constexpr int kMfBuf = 10;             // per-warp 32-float exchange buffers
 constexpr float kGs = 0.7745966692414834f;   // sqrt(3/5), 3-point Gauss point
+constexpr int kMfGather = 12;          // cell values per thread and batch (one-launch sweep)
+constexpr int kMfRowRegs = 8;          // entries of a row held in registers (a Q2 vertex: 8 cells)
 
 // 1D Q2 Lagrange basis on [-1, 1] (nodes -1, 0, 1; local index i):
 // phi_0 = (t^2 - t)/2, phi_1 = 1 - t^2, phi_2 = (t^2 + t)/2,
@@ -82,6 +88,7 @@ __global__ void __launch_bounds__(kMfWarps * 32)
 k_mf_cell(int ncells, const int* __restrict__ gdof, const int* __restrict__ pos,
           const float* __restrict__ fac, const float* __restrict__ x,
           float* __restrict__ ycell) {
+  pdl_enter();
   __shared__ float sb[kMfWarps][kMfBuf][32];
   __shared__ float sf[kMfWarps][kMfFactors];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -223,6 +230,7 @@ __global__ void __launch_bounds__(256)
 k_mf_uniform(int ncells, const int* __restrict__ gdof_c, const int* __restrict__ pos_c,
              const float* __restrict__ AeT, const float* __restrict__ x,
              float* __restrict__ ycell) {
+  pdl_enter();
   const int lane = threadIdx.x & 31;
   const int il = lane < 27 ? lane : 26;
   float a[27];
@@ -256,6 +264,7 @@ k_mf_gather(int n, int nactive, const int* __restrict__ dof_rp,
             const float* __restrict__ b, const float* __restrict__ invd, float w,
             float* __restrict__ y, double* __restrict__ z, const int* di,
             double* __restrict__ zcur) {
+  pdl_enter();
   const int row = blockIdx.x * blockDim.x + threadIdx.x;
   if (row >= n) return;
   const float xr = x[row];
@@ -282,7 +291,205 @@ k_mf_gather(int n, int nactive, const int* __restrict__ dof_rp,
   }
 }
 
+// One launch per sweep on a uniform level: the product and the row update of
+// k_mf_uniform + k_mf_gather with the local results kept in shared memory.
+// Block t owns rows [256 t, 256 t + 256) and recomputes every cell that
+// touches them (the cells of neighbouring tiles are computed again, about 2.5
+// times the cells on a 32^3 Q2 level): (1) the cells' x values, cell-major,
+// 28 floats per cell, from the tile's DOF list; (2) a warp per cell, lane m
+// forms row m of the element product from the 27 values (seven broadcast
+// 16-byte loads) and writes it over the cell's x values; (3) a thread per row
+// sums its entries in the DOF-major order.  The same multiply-adds in the
+// same order as the two-kernel path: the results agree bit for bit.
+// (Measured on GB300, 32^3 Q2 finest level: 14.4 us per Jacobi step against
+// 16.4 us for the two kernels; forming only the (cell, row) products the
+// tile's rows need, grouped by row, cut the instructions by a quarter but
+// took 16.4 us: its 16-byte loads of different cells conflict in shared
+// memory where the warp-per-cell loads broadcast.)
+template <int MODE>
+__global__ void __launch_bounds__(kMfTileRows)
+k_mf_fused(int n, int nactive, const int* __restrict__ tile_rp,
+           const int* __restrict__ tile_gdof, const float* __restrict__ AeT,
+           const int* __restrict__ dof_rp, const int* __restrict__ ent_loc,
+           const float* __restrict__ x, const float* __restrict__ b,
+           const float* __restrict__ invd, float w, float* __restrict__ y,
+           double* __restrict__ z, const int* di, double* __restrict__ zcur) {
+  pdl_enter();
+  extern __shared__ float4 s_cell4[];
+  float* s_cell = reinterpret_cast<float*>(s_cell4);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int c0 = tile_rp[blockIdx.x], nc = tile_rp[blockIdx.x + 1] - c0;
+  const int row = blockIdx.x * kMfTileRows + tid;
+  // the row's entries (up to kMfRowRegs slots in registers) are fetched
+  // while the cell values arrive
+  int e0 = 0, e1 = 0;
+  if (row < nactive) {
+    e0 = __ldg(dof_rp + row);
+    e1 = __ldg(dof_rp + row + 1);
+  }
+  // (1) the tile's DOF list, coalesced, in batches of kMfGather entries per
+  // thread: every load of a batch is issued before the first one is used
+  const int* tg = tile_gdof + (size_t)c0 * kMfCellStride;
+  const int ne = nc * kMfCellStride;
+  for (int base = 0; base < ne; base += kMfGather * kMfTileRows) {
+    int g[kMfGather];
+#pragma unroll
+    for (int k = 0; k < kMfGather; ++k) {
+      const int q = base + k * kMfTileRows + tid;
+      g[k] = q < ne ? __ldg(tg + q) : -1;
+    }
+#pragma unroll
+    for (int k = 0; k < kMfGather; ++k) {
+      const int q = base + k * kMfTileRows + tid;
+      if (q < ne) s_cell[q] = __ldg(x + g[k]);
+    }
+  }
+  int slot[kMfRowRegs];
+#pragma unroll
+  for (int k = 0; k < kMfRowRegs; ++k) slot[k] = e0 + k < e1 ? __ldg(ent_loc + e0 + k) : 0;
+  float xr = 0.f, br = 0.f, dr = 0.f;
+  if (row < n) {
+    xr = x[row];
+    if (MODE >= 1) br = b[row];
+    if (MODE >= 2) dr = invd[row];
+  }
+  const int il = lane < 27 ? lane : 26;
+  float a[27];
+#pragma unroll
+  for (int j = 0; j < 27; ++j) a[j] = __ldg(AeT + j * 27 + il);
+  __syncthreads();
+  // (2) element products, a warp per cell, lane m = row m of the element matrix
+  for (int cl = warp; cl < nc; cl += kMfTileRows / 32) {
+    const float4* xc = s_cell4 + cl * (kMfCellStride / 4);
+    float acc = 0.f;
+#pragma unroll
+    for (int jj = 0; jj < 7; ++jj) {
+      const float4 v = xc[jj];
+      acc = fmaf(a[4 * jj], v.x, acc);
+      acc = fmaf(a[4 * jj + 1], v.y, acc);
+      acc = fmaf(a[4 * jj + 2], v.z, acc);
+      if (jj < 6) acc = fmaf(a[4 * jj + 3], v.w, acc);
+    }
+    __syncwarp();
+    if (lane < 27) s_cell[cl * kMfCellStride + lane] = acc;
+  }
+  __syncthreads();
+  // (3) the row sums and the update
+  if (row >= n) return;
+  float s;
+  if (row < nactive) {
+    s = 0.f;
+#pragma unroll
+    for (int k = 0; k < kMfRowRegs; ++k)
+      if (e0 + k < e1) s += s_cell[slot[k]];
+    for (int e = e0 + kMfRowRegs; e < e1; ++e) s += s_cell[__ldg(ent_loc + e)];
+  } else {
+    s = xr;
+  }
+  if (MODE == 0) {
+    y[row] = s;
+  } else if (MODE == 1) {
+    y[row] = br - s;
+  } else {
+    const float yr = xr + w * (dr * (br - s));
+    y[row] = yr;
+    if (MODE == 3) {
+      const double zr = (double)yr;
+      (di ? z + (size_t)(*di) * n : z)[row] = zr;
+      if (zcur) zcur[row] = zr;
+    }
+  }
+}
+
 }  // namespace
+
+// Tiles of the one-launch sweep, from the DOF-major positions of the cells'
+// local DOFs in cell 0's frame (mf_pos_c): tile t lists the cells that own an
+// entry of its active rows in first-use order (their DOFs padded to
+// kMfCellStride), and every entry gets the shared-memory slot of its (tile
+// cell, local DOF).  Levels whose largest tile does not fit one block's
+// shared memory keep the two-kernel sweep, as do all levels when
+// CDG_MF_FUSED=0 is set at the first assembly.
+int mf_build_tiles(cdg_context* ctx, DevLevel& L) {
+  L.mf_ntiles = 0;
+  const int n = L.ndof, na = L.nactive, nc = L.ncells;
+  const char* off = std::getenv("CDG_MF_FUSED");   // 0: keep the two-kernel sweep
+  if (na == 0 || nc == 0 || (off && off[0] == '0')) return CDG_OK;
+  std::vector<int> rp(na + 1), posc((size_t)nc * 27), gdc((size_t)nc * 27);
+  CDG_CUDA(cudaMemcpyAsync(rp.data(), L.dof_rp, rp.size() * sizeof(int), cudaMemcpyDeviceToHost,
+                           ctx->stream));
+  CDG_CUDA(cudaMemcpyAsync(posc.data(), L.mf_pos_c, posc.size() * sizeof(int),
+                           cudaMemcpyDeviceToHost, ctx->stream));
+  CDG_CUDA(cudaMemcpyAsync(gdc.data(), L.mf_gdof, gdc.size() * sizeof(int),
+                           cudaMemcpyDeviceToHost, ctx->stream));
+  CDG_CUDA(cudaStreamSynchronize(ctx->stream));
+  const int nent = rp[na];
+  std::vector<int> ent_cell(nent, -1), ent_i(nent, 0);
+  for (int c = 0; c < nc; ++c)
+    for (int i = 0; i < 27; ++i) {
+      const int e = posc[(size_t)c * 27 + i];
+      if (e < 0) continue;
+      if (e >= nent || ent_cell[e] >= 0) {
+        set_error("matrix-free positions are not a permutation of the DOF-major entries");
+        return CDG_ERR_ARG;
+      }
+      ent_cell[e] = c;
+      ent_i[e] = i;
+    }
+  const int ntiles = (n + kMfTileRows - 1) / kMfTileRows;
+  std::vector<int> trp(ntiles + 1, 0), tcells, loc(nent), mark(nc, -1), local(nc, 0);
+  tcells.reserve((size_t)nc * 3);
+  int maxc = 0;
+  for (int t = 0; t < ntiles; ++t) {
+    const int ra = std::min(t * kMfTileRows, na), rb = std::min((t + 1) * kMfTileRows, na);
+    const int start = (int)tcells.size();
+    for (int e = rp[ra]; e < rp[rb]; ++e) {
+      const int c = ent_cell[e];
+      if (c < 0) {
+        set_error("matrix-free positions leave a DOF-major entry unset");
+        return CDG_ERR_ARG;
+      }
+      if (mark[c] != t) {
+        mark[c] = t;
+        local[c] = (int)tcells.size() - start;
+        tcells.push_back(c);
+      }
+      loc[e] = local[c] * kMfCellStride + ent_i[e];
+    }
+    trp[t + 1] = (int)tcells.size();
+    maxc = std::max(maxc, trp[t + 1] - start);
+  }
+  const size_t smem = (size_t)maxc * kMfCellStride * sizeof(float);
+  if (smem > 200 * 1024) return CDG_OK;
+  // the tile cells' DOFs in cell 0's order, padded with the cell's first DOF
+  std::vector<int> tg(tcells.size() * kMfCellStride);
+  for (size_t c = 0; c < tcells.size(); ++c)
+    for (int i = 0; i < kMfCellStride; ++i)
+      tg[c * kMfCellStride + i] = gdc[(size_t)tcells[c] * 27 + (i < 27 ? i : 0)];
+  if (!L.mf_tile_rp) {
+    CDG_CUDA(cudaMalloc(&L.mf_tile_rp, trp.size() * sizeof(int)));
+    CDG_CUDA(cudaMalloc(&L.mf_tile_gdof, std::max<size_t>(1, tg.size()) * sizeof(int)));
+    CDG_CUDA(cudaMalloc(&L.mf_ent_loc, std::max(1, nent) * sizeof(int)));
+  }
+  CDG_CUDA(cudaMemcpyAsync(L.mf_tile_rp, trp.data(), trp.size() * sizeof(int),
+                           cudaMemcpyHostToDevice, ctx->stream));
+  if (!tg.empty())
+    CDG_CUDA(cudaMemcpyAsync(L.mf_tile_gdof, tg.data(), tg.size() * sizeof(int),
+                             cudaMemcpyHostToDevice, ctx->stream));
+  if (nent > 0)
+    CDG_CUDA(cudaMemcpyAsync(L.mf_ent_loc, loc.data(), (size_t)nent * sizeof(int),
+                             cudaMemcpyHostToDevice, ctx->stream));
+  CDG_CUDA(cudaStreamSynchronize(ctx->stream));   // host vectors go out of scope
+  if (smem > 48 * 1024) {
+    CDG_CUDA(cudaFuncSetAttribute(k_mf_fused<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CDG_CUDA(cudaFuncSetAttribute(k_mf_fused<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CDG_CUDA(cudaFuncSetAttribute(k_mf_fused<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CDG_CUDA(cudaFuncSetAttribute(k_mf_fused<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  }
+  L.mf_tile_maxcells = maxc;
+  L.mf_ntiles = ntiles;
+  return CDG_OK;
+}
 
 bool mf_eligible(const DevLevel& L) { return L.shape == kHexa && L.order == 2; }
 
@@ -298,29 +505,41 @@ int mf_ensure(DevLevel& L) {
 }
 
 int mf_apply(cdg_context* ctx, const DevLevel& L, int mode, const float* x, const float* b,
-             const float* invd, float w, float* y, double* z, const int* di, double* zcur) {
+             const float* invd, float w, float* y, double* z, const int* di, double* zcur,
+             int two_kernel) {
   if (!L.mf_valid) {
     set_error("matrix-free operator used without valid cell factors");
     return CDG_ERR_ARG;
+  }
+  if (L.mf_uniform && L.mf_ntiles > 0 && !two_kernel) {
+    const int g = L.mf_ntiles;
+    const size_t sm = (size_t)L.mf_tile_maxcells * kMfCellStride * sizeof(float);
+    switch (mode) {
+      case 0: CDG_LAUNCH_PDL(ctx, k_mf_fused<0>, g, kMfTileRows, sm, L.ndof, L.nactive, L.mf_tile_rp, L.mf_tile_gdof, L.mf_ae, L.dof_rp, L.mf_ent_loc, x, b, invd, w, y, z, di, zcur); break;
+      case 1: CDG_LAUNCH_PDL(ctx, k_mf_fused<1>, g, kMfTileRows, sm, L.ndof, L.nactive, L.mf_tile_rp, L.mf_tile_gdof, L.mf_ae, L.dof_rp, L.mf_ent_loc, x, b, invd, w, y, z, di, zcur); break;
+      case 2: CDG_LAUNCH_PDL(ctx, k_mf_fused<2>, g, kMfTileRows, sm, L.ndof, L.nactive, L.mf_tile_rp, L.mf_tile_gdof, L.mf_ae, L.dof_rp, L.mf_ent_loc, x, b, invd, w, y, z, di, zcur); break;
+      default: CDG_LAUNCH_PDL(ctx, k_mf_fused<3>, g, kMfTileRows, sm, L.ndof, L.nactive, L.mf_tile_rp, L.mf_tile_gdof, L.mf_ae, L.dof_rp, L.mf_ent_loc, x, b, invd, w, y, z, di, zcur); break;
+    }
+    return CDG_OK;
   }
   const int cblocks = (L.ncells + kMfWarps - 1) / kMfWarps;
   const int cap = ctx->num_sms * L.mf_blocks_per_sm;
   const int grid = cap > 0 && cblocks > cap ? cap : cblocks;
   if (L.mf_uniform)
-    CDG_LAUNCH(ctx, k_mf_uniform, grid, kMfWarps * 32, 0, L.ncells, L.mf_gdof, L.mf_pos_c,
+    CDG_LAUNCH_PDL(ctx, k_mf_uniform, grid, kMfWarps * 32, 0, L.ncells, L.mf_gdof, L.mf_pos_c,
                L.mf_ae, x, L.mf_y);
   else if (L.mf_lin)
-    CDG_LAUNCH(ctx, k_mf_cell<true>, grid, kMfWarps * 32, 0, L.ncells, L.gdof, L.mf_pos,
+    CDG_LAUNCH_PDL(ctx, k_mf_cell<true>, grid, kMfWarps * 32, 0, L.ncells, L.gdof, L.mf_pos,
                L.mf_fac, x, L.mf_y);
   else
-    CDG_LAUNCH(ctx, k_mf_cell<false>, grid, kMfWarps * 32, 0, L.ncells, L.gdof, L.mf_pos,
+    CDG_LAUNCH_PDL(ctx, k_mf_cell<false>, grid, kMfWarps * 32, 0, L.ncells, L.gdof, L.mf_pos,
                L.mf_fac, x, L.mf_y);
   const int g2 = (L.ndof + 255) / 256;
   switch (mode) {
-    case 0: CDG_LAUNCH(ctx, k_mf_gather<0>, g2, 256, 0, L.ndof, L.nactive, L.dof_rp, L.mf_y, x, b, invd, w, y, z, di, zcur); break;
-    case 1: CDG_LAUNCH(ctx, k_mf_gather<1>, g2, 256, 0, L.ndof, L.nactive, L.dof_rp, L.mf_y, x, b, invd, w, y, z, di, zcur); break;
-    case 2: CDG_LAUNCH(ctx, k_mf_gather<2>, g2, 256, 0, L.ndof, L.nactive, L.dof_rp, L.mf_y, x, b, invd, w, y, z, di, zcur); break;
-    default: CDG_LAUNCH(ctx, k_mf_gather<3>, g2, 256, 0, L.ndof, L.nactive, L.dof_rp, L.mf_y, x, b, invd, w, y, z, di, zcur); break;
+    case 0: CDG_LAUNCH_PDL(ctx, k_mf_gather<0>, g2, 256, 0, L.ndof, L.nactive, L.dof_rp, L.mf_y, x, b, invd, w, y, z, di, zcur); break;
+    case 1: CDG_LAUNCH_PDL(ctx, k_mf_gather<1>, g2, 256, 0, L.ndof, L.nactive, L.dof_rp, L.mf_y, x, b, invd, w, y, z, di, zcur); break;
+    case 2: CDG_LAUNCH_PDL(ctx, k_mf_gather<2>, g2, 256, 0, L.ndof, L.nactive, L.dof_rp, L.mf_y, x, b, invd, w, y, z, di, zcur); break;
+    default: CDG_LAUNCH_PDL(ctx, k_mf_gather<3>, g2, 256, 0, L.ndof, L.nactive, L.dof_rp, L.mf_y, x, b, invd, w, y, z, di, zcur); break;
   }
   return CDG_OK;
 }

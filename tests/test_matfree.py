@@ -209,12 +209,14 @@ def test_tuned_schedule_reproduced_by_its_settings(ctx, monkeypatch):
 
 
 def test_matrix_free_grid_does_not_change_results(ctx, monkeypatch):
-    # one cell per warp or 4 / 8 blocks per SM walking the cells: the same
-    # matrix-free products, bit for bit (the operator of a uniform level comes
-    # from cell 0's factors and is summed per row in a fixed order)
+    # two-kernel sweep with one cell per warp or 4 / 8 blocks per SM walking
+    # the cells: the same matrix-free products, bit for bit (the operator of a
+    # uniform level comes from cell 0's factors and is summed per row in a
+    # fixed order)
     nref, levels, kw = CASES["supg_polyexp"]
     x = None
     outs = []
+    monkeypatch.setenv("CDG_MF_FUSED", "0")
     for cap in ("0", "4", "8"):
         monkeypatch.setenv("CDG_MATFREE", "1")
         monkeypatch.setenv("CDG_MF_CAP", cap)
@@ -227,3 +229,51 @@ def test_matrix_free_grid_does_not_change_results(ctx, monkeypatch):
         outs.append(gpu.apply32(x, 0, 1))
         gpu.close()
     assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[0], outs[2])
+
+
+@pytest.mark.parametrize("sheared", [False, True])
+@pytest.mark.parametrize("name", ["supg_polyexp", "supg_sine_sdfem2", "galerkin_sine"])
+def test_one_launch_sweep_equals_two_kernel_product(ctx, name, sheared):
+    # uniform levels apply the shared element matrix in one launch per sweep
+    # (row tiles recomputing their cells in shared memory); the product
+    # equals the two-launch form (cell products to memory, then row sums)
+    # bit for bit, and the oracle's FP64 product to FP32 rounding
+    nref, levels, kw = CASES[name]
+    if sheared:
+        gpu, o = sheared_pair(ctx, nref, levels, kw)
+    else:
+        gpu = pg.ConvectionDiffusion(ctx, pg.Hierarchy(3, 2, nref, n_levels=levels))
+        o = po.Problem(oracle_cfg(nref, kw), levels)
+    gpu.assemble(gpu_params(kw))
+    o.assemble()
+    rng = np.random.default_rng(11)
+    for lvl in range(levels):
+        na = gpu.info(lvl)["nactive"]
+        x = rng.standard_normal(gpu.info(lvl)["ndof"]).astype(np.float32)
+        y1 = gpu.apply32(x, lvl, 1)
+        y2 = gpu.apply32(x, lvl, 2)
+        assert np.array_equal(y1, y2), lvl
+        assert rel(y1[:na], o.apply(x.astype(np.float64), lvl)[:na]) < 2e-5
+    gpu.close()
+
+
+def test_one_launch_sweep_in_solves(ctx, monkeypatch):
+    # the mixed solve with the one-launch sweep against the two-kernel sweep
+    # (CDG_MF_FUSED=0): the same iterations and solution (the FP64 finest
+    # operators of two assemblies differ in round-off only)
+    nref, _, kw = CASES["supg_polyexp"]
+    levels = 3
+    monkeypatch.setenv("CDG_MATFREE", "1")
+    out = []
+    for fused in ("1", "0"):
+        monkeypatch.setenv("CDG_MF_FUSED", fused)
+        gpu = pg.ConvectionDiffusion(ctx, pg.Hierarchy(3, 2, nref, n_levels=levels))
+        a = gpu_params(kw)
+        gpu.assemble(a)
+        st = gpu.solve(mixed_solver(levels))
+        assert st.residual <= 1e-10 * st.initial_residual
+        out.append((st.iterations, gpu.solution(), gpu.tuning_detail(0)))
+        gpu.close()
+    assert out[0][2][2][1] == -1 and out[1][2][2][1] != -1
+    assert abs(out[0][0] - out[1][0]) <= 1
+    assert rel(out[0][1], out[1][1]) < 1e-10
