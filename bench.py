@@ -773,12 +773,15 @@ def run_gpu_serve(args):
     # (each server first runs the same 200 requests untimed, so its pool
     # holds the instances the timed pass needs: steady state, not setup)
     one = {}
+    # (per-launch batching off: every request on the slot's stream)
+    os.environ["CDG_SERVER_BATCH"] = "0"
     for prec in ("fp64", "mixed"):
         s1 = pg.Server(local, n_slots=1)
         run_stream(pg, s1, base_q, [0.0] * len(base_q), prec)
         wall, res = run_stream(pg, s1, base_q, [0.0] * len(base_q), prec)
         one[prec] = len(base_q) / wall
         s1.close()
+    del os.environ["CDG_SERVER_BATCH"]
     # saturated concurrent throughput on the same 200 requests
     s8 = pg.Server(local, n_slots=SERVE["slots"])
     run_stream(pg, s8, base_q, [0.0] * len(base_q), "mixed")
@@ -823,8 +826,9 @@ def run_gpu_serve(args):
         "sweep": sweep,
         "one_at_a_time": {"fp64_solves_per_s": one["fp64"], "mixed_solves_per_s": one["mixed"]},
         "served_over_one_at_a_time_fp64": sat / one["fp64"],
-        "server": {k: c1[k] - c0.get(k, 0) if k in ("completed", "launches", "evictions") else c1[k]
-                   for k in c1},
+        "server": {k: c1[k] - c0.get(k, 0)
+                   if k in ("completed", "launches", "evictions", "batch_launches", "batched")
+                   else c1[k] for k in c1},
         "roofline": {"bound": "hbm", "kernel": rl_kernel,
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "algorithmic_bytes": bytes_smooth, "traffic": None},

@@ -246,6 +246,27 @@ int cdg_problem_assemble_solve(cdg_problem *p, const cdg_assembly_params *a,
                                const cdg_solver_params *s,
                                const double *solution_in, double *rhs_out,
                                double *solution_out, cdg_solve_stats *stats);
+
+/* Many small solves in one launch (the served form's batch; no counterpart
+ * in the reference, which solves one problem per ConvectionDiffusion::solve
+ * call, src/Solver/Iteration_gmres.C:430-620 with Multigrid.C:157-410).  Each
+ * problem (assembled, its solution holding the start iterate) is prepared on
+ * its own context's stream (FP32 copies, coarse inverse, Krylov buffers);
+ * then one kernel on ctx's stream runs one block per problem: FGMRES(m) in
+ * FP64 with the FP32 multigrid V-cycle, every operation under block
+ * barriers, and each block stops on its own convergence test.  Problems must
+ * be distinct, on ctx's device, at most 20000 DOFs, and params[q] must ask
+ * for precision 1 (mixed), multigrid (2 to 12 levels, V-cycle, at least one
+ * pre-smoothing step, direct coarse solve with at most 2048 active coarse
+ * DOFs), classical Gram-Schmidt and gmres_restart <= 64; otherwise
+ * CDG_ERR_ARG and nothing runs.  status[q] receives CDG_OK,
+ * CDG_ERR_DIVERGED or CDG_ERR_BREAKDOWN as cdg_problem_solve would return;
+ * stats[q] the iterations and residuals (seconds: the whole call).  The
+ * solutions stay on the device (cdg_problem_get_solution).  Results equal a
+ * cdg_problem_solve of the same problem to round-off. */
+int cdg_solve_batched(cdg_context *ctx, int count, cdg_problem *const *problems,
+                      const cdg_solver_params *params, int *status,
+                      cdg_solve_stats *stats);
 /* ConvectionDiffusion<d>::output error norms against the example's exact
  * solution: errors[0..4] = L2, H1-semi, SD, DG(volume), L_inf */
 int cdg_problem_errors(cdg_problem *p, const cdg_assembly_params *a,
@@ -446,7 +467,11 @@ int cdg_problem_time_kernel(cdg_problem *p, const cdg_assembly_params *a,
  * n_slots workers each own a stream; a request waits in the queue until a
  * slot is free and its problem instance fits the HBM budget (idle instances
  * are evicted least recently used first), then assemble + solve run on the
- * slot's stream, overlapping with the other slots' work on the device. */
+ * slot's stream, overlapping with the other slots' work on the device.  A
+ * small request that cdg_solve_batched takes is assembled on its slot and
+ * then solved by a batcher thread together with every other such request
+ * handed over since the batcher's previous launch (one launch, one block per
+ * request); its result's slot is then n_slots. */
 typedef struct cdg_server cdg_server;
 
 typedef struct {
@@ -486,6 +511,10 @@ int cdg_server_wait(cdg_server *srv, long long ticket, double timeout_seconds,
  * [8] budget bytes, [9] peak concurrent running, [10] kernel launches of all
  * slots, [11] mesh classes seen */
 int cdg_server_counters(cdg_server *srv, long long *c12);
+/* per-launch batching of small requests (the batcher thread): [0] launches,
+ * [1] requests solved in them, [2] 1 when batching is on (CDG_SERVER_BATCH
+ * unset or not 0 at server creation) */
+int cdg_server_batch_counters(cdg_server *srv, long long *c3);
 
 #ifdef __cplusplus
 }

@@ -54,7 +54,8 @@ EXPORTED = [
     "cdg_server_destroy", "cdg_request_ndof", "cdg_server_submit", "cdg_server_wait",
     "cdg_server_counters", "cdg_problem_apply32", "cdg_problem_tuning",
     "cdg_problem_quadrature_points", "cdg_problem_assemble_coefficients",
-    "cdg_problem_set_fp32_tensor_levels", "cdg_problem_get_matrix32",
+    "cdg_problem_set_fp32_tensor_levels", "cdg_problem_get_matrix32", "cdg_solve_batched",
+    "cdg_server_batch_counters",
 ]
 
 
@@ -192,6 +193,9 @@ def lib():
             "cdg_server_submit": [P, ctypes.POINTER(Request), dp, ctypes.POINTER(ctypes.c_longlong)],
             "cdg_server_wait": [P, ctypes.c_longlong, ctypes.c_double, ctypes.POINTER(Result)],
             "cdg_server_counters": [P, ctypes.POINTER(ctypes.c_longlong)],
+            "cdg_solve_batched": [P, ctypes.c_int, PP, ctypes.POINTER(SolverParams), ip,
+                                  ctypes.POINTER(SolveStats)],
+            "cdg_server_batch_counters": [P, ctypes.POINTER(ctypes.c_longlong)],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -708,6 +712,22 @@ def request_ndof(r):
     return nd.value
 
 
+def solve_batched(ctx, problems, params):
+    """Solve assembled problems in one launch, one block per problem (the
+    served form's batch): returns [(status, SolveStats)] in order.  params is
+    one SolverParams for all or one per problem."""
+    n = len(problems)
+    if not isinstance(params, (list, tuple)):
+        params = [params] * n
+    arr = (ctypes.c_void_p * max(n, 1))(*[pr.p.value if hasattr(pr.p, "value") else pr.p
+                                          for pr in problems])
+    sp = (SolverParams * max(n, 1))(*params)
+    st = (ctypes.c_int * max(n, 1))()
+    stats = (SolveStats * max(n, 1))()
+    _chk(lib().cdg_solve_batched(ctx.c, n, arr, sp, st, stats))
+    return [(st[q], stats[q]) for q in range(n)]
+
+
 class Server:
     """n_slots workers on one GPU; requests are admitted as slots free up and
     their problem instances fit the HBM budget (bytes; 0 = 80 % of free)."""
@@ -742,7 +762,11 @@ class Server:
     def counters(self):
         c = (ctypes.c_longlong * 12)()
         _chk(lib().cdg_server_counters(self.h, c))
-        return dict(zip(self.COUNTERS, list(c)))
+        b = (ctypes.c_longlong * 3)()
+        _chk(lib().cdg_server_batch_counters(self.h, b))
+        out = dict(zip(self.COUNTERS, list(c)))
+        out.update(batch_launches=b[0], batched=b[1], batching=b[2])
+        return out
 
     def close(self):
         if getattr(self, "h", None):

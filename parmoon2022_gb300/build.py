@@ -16,7 +16,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libparmoon_cd.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["setup.cpp", "assemble.cu", "linalg.cu", "api.cu", "server.cpp", "structure.cu",
-           "checkpoint.cpp", "matfree.cu"]
+           "checkpoint.cpp", "matfree.cu", "batch.cu"]
 
 
 def nvcc():

@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <vector>
 
 #include "common.cuh"
 
@@ -97,6 +98,8 @@ int cdg_context_destroy(cdg_context* c) {
   cudaFree(c->d_red);
   cudaFree(c->d_cnt);
   cudaFreeHost(c->h_pinned);
+  if (c->batch_host) cudaFreeHost(c->batch_host);
+  if (c->batch_dev) cudaFree(c->batch_dev);
   cudaStreamDestroy(c->stream);
   delete c;
   return CDG_OK;
@@ -620,6 +623,58 @@ int cdg_problem_solve(cdg_problem* p, const cdg_solver_params* s, cdg_solve_stat
   local.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   if (st) *st = local;
   return rc;
+}
+
+int cdg_solve_batched(cdg_context* ctx, int count, cdg_problem* const* probs,
+                      const cdg_solver_params* params, int* status, cdg_solve_stats* stats) {
+  if (!ctx || count < 0 || (count > 0 && (!probs || !params || !status || !stats))) {
+    set_error("bad arguments");
+    return CDG_ERR_ARG;
+  }
+  for (int q = 0; q < count; ++q) {
+    cdg_problem* p = probs[q];
+    if (!p || !p->ctx || p->ctx->device != ctx->device) {
+      set_error("problem %d is null or on another device", q);
+      return CDG_ERR_ARG;
+    }
+    CDG_TRY(check_solver_params(p, &params[q]));
+    const char* why = nullptr;
+    if (!batch_eligible(p, params[q], &why)) {
+      set_error("problem %d: %s", q, why);
+      return CDG_ERR_ARG;
+    }
+    for (int r = 0; r < q; ++r)
+      if (probs[r] == p) {
+        set_error("problem %d appears twice in the batch", q);
+        return CDG_ERR_ARG;
+      }
+  }
+  CDG_CUDA(cudaSetDevice(ctx->device));
+  auto t0 = std::chrono::steady_clock::now();
+  cudaEvent_t ev = nullptr;
+  for (int q = 0; q < count; ++q) {
+    cdg_problem* p = probs[q];
+    CDG_TRY(batch_prepare(p->ctx, p, params[q]));
+    if (p->ctx->stream != ctx->stream) {
+      if (!ev) CDG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+      CDG_CUDA(cudaEventRecord(ev, p->ctx->stream));
+      CDG_CUDA(cudaStreamWaitEvent(ctx->stream, ev, 0));
+    }
+  }
+  std::vector<BatchResult> res((size_t)std::max(count, 1));
+  int rc = batch_launch(ctx, probs, params, count, res.data());
+  if (ev) cudaEventDestroy(ev);
+  if (rc != CDG_OK) return rc;
+  const double secs =
+      std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  for (int q = 0; q < count; ++q) {
+    status[q] = res[q].status;
+    stats[q].iterations = res[q].iterations;
+    stats[q].residual = res[q].residual;
+    stats[q].initial_residual = res[q].initial;
+    stats[q].seconds = secs;
+  }
+  return CDG_OK;
 }
 
 int cdg_problem_assemble_solve(cdg_problem* p, const cdg_assembly_params* a,

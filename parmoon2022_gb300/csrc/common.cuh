@@ -44,6 +44,11 @@ enum : int {
 constexpr int kMfFactors = 40;        // per-cell factors of the matrix-free Q2 operator
 constexpr int kMfTileRows = 256;      // rows (threads) per tile of the one-launch sweep
 constexpr int kMfCellStride = 28;     // floats per tile cell in shared memory (16-byte rows)
+// batched solver (batch.cu): one block per request
+constexpr int kBatchMaxLevels = 12;
+constexpr int kBatchMaxRestart = 64;
+constexpr int kBatchMaxDofs = 20000;    // larger requests keep the stream-level solver
+constexpr int kBatchMaxCoarse = 2048;   // active DOFs of the coarsest level
 constexpr int kRedSlots = 32;         // partial-sum rows (one per inner product)
 constexpr int kRedMaxBlocks = 1024;   // partial sums per reduction
 
@@ -60,6 +65,10 @@ struct cdg_context {
   long long launches = 0;
   // programmatic dependent launch of the solver kernels (CDG_PDL=1: on)
   int pdl = 0;
+  // request descriptors and results of the batched solver (pinned / device)
+  void* batch_host = nullptr;
+  void* batch_dev = nullptr;
+  size_t batch_host_bytes = 0;
 };
 
 namespace cdg {
@@ -325,6 +334,17 @@ int check_device_error(cdg_context* ctx);
 // matrix-free FP32 operator of Q2 hexahedral levels (matfree.cu); mode as
 // k_spmv: 0 y = Ax, 1 y = b - Ax, 2 Jacobi step, 3 Jacobi step + FP64 copy
 bool mf_eligible(const DevLevel& L);
+// batched solver (batch.cu): requests a launch can take (why: the reason
+// when not), and one launch over prepared problems on ctx's stream
+struct BatchResult {
+  int status, iterations;
+  double residual, initial;
+};
+bool batch_eligible(const cdg_problem* p, const cdg_solver_params& s, const char** why);
+int batch_launch(cdg_context* ctx, cdg_problem* const* probs, const cdg_solver_params* params,
+                 int count, BatchResult* results);
+// prepare_solver and the Krylov buffers of a problem (linalg.cu)
+int batch_prepare(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s);
 // tiles of the one-launch sweep of a uniform level (once per level)
 int mf_build_tiles(cdg_context* ctx, DevLevel& L);
 int mf_ensure(DevLevel& L);

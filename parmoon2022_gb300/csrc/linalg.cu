@@ -20,6 +20,7 @@
 #include <type_traits>
 
 #include "common.cuh"
+#include "solver_dev.cuh"
 
 namespace cgrp = cooperative_groups;
 
@@ -546,45 +547,11 @@ k_multidot(int n, const double* __restrict__ w, const double* __restrict__ V, in
   if (threadIdx.x == 0) *counter = 0u;
 }
 
-// Givens rotations of Hessenberg column i (Utilities_gmres.C:60-88): apply
-// the previous rotations, generate and apply rotation i, rotate s, write
-// |s_{i+1}| to *resid
-__device__ void givens_column_s(int i, double* col, double* cs, double* sn, double& si,
-                                double& si1, double* resid);
+// Givens rotations of Hessenberg column i (Utilities_gmres.C:60-88):
+// givens_column_s in solver_dev.cuh, with s[i], s[i+1] in an array here
 __device__ void givens_column(int i, double* col, double* cs, double* sn, double* s,
                               double* resid) {
   givens_column_s(i, col, cs, sn, s[i], s[i + 1], resid);
-}
-
-// the same with s[i], s[i+1] passed by reference
-__device__ void givens_column_s(int i, double* col, double* cs, double* sn, double& si,
-                                double& si1, double* resid) {
-  for (int k = 0; k < i; ++k) {
-    double dx = col[k], dy = col[k + 1];
-    col[k] = cs[k] * dx + sn[k] * dy;
-    col[k + 1] = -sn[k] * dx + cs[k] * dy;
-  }
-  double dx = col[i], dy = col[i + 1], c, sg;
-  if (dy == 0.0) {
-    c = 1.0;
-    sg = 0.0;
-  } else if (fabs(dy) > fabs(dx)) {
-    double t = dx / dy;
-    sg = 1.0 / sqrt(1.0 + t * t);
-    c = t * sg;
-  } else {
-    double t = dy / dx;
-    c = 1.0 / sqrt(1.0 + t * t);
-    sg = t * c;
-  }
-  cs[i] = c;
-  sn[i] = sg;
-  col[i] = c * dx + sg * dy;
-  col[i + 1] = -sg * dx + c * dy;
-  double a = si, b = si1;
-  si = c * a + sg * b;
-  si1 = -sg * a + c * b;
-  *resid = fabs(si1);
 }
 
 // w -= sum_k H(k,i) v_k (k in order), H(i+1,i) = ||w||, then the Givens
@@ -1749,6 +1716,11 @@ static int ensure_gmres(cdg_problem* p, int n, int m) {
   return CDG_OK;
 }
 
+int batch_prepare(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s) {
+  CDG_TRY(prepare_solver(ctx, p, s));
+  return ensure_gmres(p, p->lev[0].ndof, s.gmres_restart);
+}
+
 struct LoopInfo {
   double initial = 0, previous = 0;
 };
@@ -1784,30 +1756,6 @@ static int read_scalar(cdg_context* ctx, const double* d, double* h) {
 // converged) runs on the device and ends the loop, so the host waits once
 // per restart cycle instead of once per iteration
 // ---------------------------------------------------------------------------
-struct ConvParams {
-  double tol, red, div;
-  int min_it, max_it, m;
-};
-
-// IterativeMethod::converged (IterativeMethod.h:83-163): 0 continue, 1 stop,
-// 2 diverged; li[0] initial, li[1] previous residual
-__device__ int conv_test(const ConvParams& c, double* li, double res, int it) {
-  if (it == 0) {
-    li[0] = res;
-    li[1] = res;
-  }
-  const bool small = res < c.tol;
-  const bool red = res < c.red * li[0];
-  const bool enough = it >= c.min_it;
-  const bool stag = res > 1e10 * li[1];
-  const bool div = res > c.div * li[0];
-  bool conv = (small || red || stag || div) && enough;
-  if (it == c.max_it) conv = true;
-  li[1] = res;
-  if (div) return 2;
-  return conv ? 1 : 0;
-}
-
 // st: [0] column i, [1] iteration j, [2] flag (0 run, 1 converged,
 // 2 diverged, 3 end of the restart cycle)
 __global__ void k_fgmres_start(ConvParams c, int* st, const double* beta, double* li) {

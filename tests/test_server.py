@@ -135,3 +135,34 @@ def test_budget_admission_and_eviction(ctx):
     assert c["evictions"] > 0
     assert c["resident_bytes"] <= c["budget_bytes"]
     srv.close()
+
+
+@pytest.mark.gpu
+def test_small_requests_are_batched_per_launch(ctx, monkeypatch):
+    # every request of the mix is small enough for the batched solver (cap
+    # raised to its limit): with batching on they are solved in launches of
+    # one block per request (the result's slot is n_slots), and each result
+    # equals the same request served with batching off (every request on its
+    # slot's stream)
+    reqs = mix_requests(1)
+    monkeypatch.setenv("CDG_SERVER_BATCH_DOFS", "20000")
+    monkeypatch.setenv("CDG_SERVER_BATCH", "0")
+    plain = pg.Server(0, n_slots=4)
+    ref = [plain.wait(t) for t in [plain.submit(r) for r in reqs]]
+    c = plain.counters()
+    assert c["batching"] == 0 and c["batched"] == 0
+    plain.close()
+    monkeypatch.delenv("CDG_SERVER_BATCH")
+    srv = pg.Server(0, n_slots=4)
+    out = [srv.wait(t) for t in [srv.submit(r) for r in reqs]]
+    c = srv.counters()
+    assert c["batching"] == 1 and c["batched"] == len(reqs)
+    assert 1 <= c["batch_launches"] <= len(reqs)
+    assert c["completed"] == len(reqs) and c["failed"] == 0
+    for (r0, x0), (r1, x1) in zip(ref, out):
+        assert r0.status == 0 and r1.status == 0
+        assert r1.slot == 4
+        assert r1.stats.residual <= 1e-10 * r1.stats.initial_residual * 1.0001
+        assert abs(r1.stats.iterations - r0.stats.iterations) <= 1
+        assert np.max(np.abs(x1 - x0)) <= 1e-8 * np.max(np.abs(x0))
+    srv.close()
