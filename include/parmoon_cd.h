@@ -166,6 +166,13 @@ int cdg_context_stream(cdg_context *ctx, void **stream);
  * Structure.C:226-618; GridTransfer.C:29-410) */
 int cdg_hierarchy_create(int dim, int order, int roots, int nref, int n_levels,
                          int neumann_mask, cdg_hierarchy **out);
+/* move the finest level's interior vertices of a hierarchy by amplitude * h
+ * in every coordinate (uniform, seeded; h = 1 / cells per direction), after
+ * numbering: quadrilaterals and hexahedra become general (non-parallelogram,
+ * non-parallelepiped) cells, mapped by the reference's bilinear / trilinear
+ * maps (TQuadBilinear, THexaTrilinear); the coarser levels and the grid
+ * transfers keep the nested positions.  amplitude in [0, 0.5). */
+int cdg_hierarchy_perturb(cdg_hierarchy *h, double amplitude, unsigned long long seed);
 /* unit cube split into roots^3 cubes of 6 Kuhn tetrahedra, P1 or P2 (order),
  * refined nref times (regular refinement, children of cell c are the eight
  * cells 8c..8c+7 of the next level); neumann_mask as above (bit k: boundary

@@ -826,8 +826,148 @@ static void cell_affine_s(int shape, int dim, const double *cv, affine_t *A) {
   A->Jinv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
 }
 
+/* TQuadrangle::CheckQuad (Quadrangle.C:119-128) and THexahedron::CheckHexa
+ * (Hexahedron.C:196-235): 1 when a quadrilateral is not a parallelogram (a
+ * hexahedron not a parallelepiped, "Brick"); the reference maps those cells
+ * by TQuadBilinear / THexaTrilinear (FESpace.C:83-84 picks the _M elements
+ * for them) and the others affinely */
+static int cell_is_multilinear(int shape, int dim, const double *cv) {
+  if (shape == 2) return 0;
+  if (dim == 2) {
+    double t1 = cv[0] - cv[2] + cv[4] - cv[6];
+    double t2 = cv[1] - cv[3] + cv[5] - cv[7];
+    return fabs(t1) > 1e-8 || fabs(t2) > 1e-8;
+  }
+  for (int a = 0; a < 3; ++a) {
+#define X(i) cv[3 * (i) + a]
+    double t1 = fabs(X(0) - X(1) - X(3) + X(2) + X(4) - X(5) - X(7) + X(6));
+    double t2 = fabs(X(0) - X(1) + X(3) - X(2) - X(4) + X(5) - X(7) + X(6));
+    double t3 = fabs(X(0) + X(1) - X(3) - X(2) - X(4) - X(5) + X(7) + X(6));
+    double t4 = fabs(-X(0) + X(1) + X(3) - X(2) + X(4) - X(5) - X(7) + X(6));
+#undef X
+    if (t1 + t2 + t3 + t4 >= 1e-8) return 1;
+  }
+  return 0;
+}
+
+/* the bilinear / trilinear map at a reference point (TQuadBilinear::SetCell,
+ * QuadBilinear.C:243-263, GetOrigValues :87-129; THexaTrilinear::SetCell,
+ * HexaTrilinear.C:225-270, GetOrigValues): x(xi), J = dx/dxi, its inverse
+ * and determinant in the affine_t layout; c[r][k] the map's coefficients */
+static void multilinear_coeffs(int dim, const double *cv, double c[3][8]) {
+  for (int r = 0; r < dim; ++r) {
+    if (dim == 2) {
+      double v0 = cv[r], v1 = cv[2 + r], v2 = cv[4 + r], v3 = cv[6 + r];
+      c[r][0] = (v0 + v1 + v2 + v3) * 0.25;
+      c[r][1] = (-v0 + v1 + v2 - v3) * 0.25;
+      c[r][2] = (-v0 - v1 + v2 + v3) * 0.25;
+      c[r][3] = (v0 - v1 + v2 - v3) * 0.25;
+    } else {
+      double v[8];
+      for (int i = 0; i < 8; ++i) v[i] = cv[3 * i + r];
+      c[r][0] = (v[0] + v[1] + v[3] + v[2] + v[4] + v[5] + v[7] + v[6]) * 0.125;
+      c[r][1] = (-v[0] + v[1] - v[3] + v[2] - v[4] + v[5] - v[7] + v[6]) * 0.125;
+      c[r][2] = (-v[0] - v[1] + v[3] + v[2] - v[4] - v[5] + v[7] + v[6]) * 0.125;
+      c[r][3] = (-v[0] - v[1] - v[3] - v[2] + v[4] + v[5] + v[7] + v[6]) * 0.125;
+      c[r][4] = (v[0] - v[1] - v[3] + v[2] + v[4] - v[5] - v[7] + v[6]) * 0.125;
+      c[r][5] = (v[0] - v[1] + v[3] - v[2] - v[4] + v[5] - v[7] + v[6]) * 0.125;
+      c[r][6] = (v[0] + v[1] - v[3] - v[2] - v[4] - v[5] + v[7] + v[6]) * 0.125;
+      c[r][7] = (-v[0] + v[1] + v[3] - v[2] + v[4] - v[5] - v[7] + v[6]) * 0.125;
+    }
+  }
+}
+
+static void multilinear_at(int dim, const double *cv, const double *xi, affine_t *P) {
+  double c[3][8];
+  multilinear_coeffs(dim, cv, c);
+  double (*J)[3] = P->J;
+  if (dim == 2) {
+    double s = xi[0], t = xi[1];
+    for (int r = 0; r < 2; ++r) {
+      P->x0[r] = c[r][0] + c[r][1] * s + c[r][2] * t + c[r][3] * s * t;
+      J[r][0] = c[r][1] + c[r][3] * t;
+      J[r][1] = c[r][2] + c[r][3] * s;
+    }
+    P->det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    P->Jinv[0][0] = J[1][1] / P->det; P->Jinv[0][1] = -J[0][1] / P->det;
+    P->Jinv[1][0] = -J[1][0] / P->det; P->Jinv[1][1] = J[0][0] / P->det;
+    return;
+  }
+  double s = xi[0], t = xi[1], u = xi[2];
+  for (int r = 0; r < 3; ++r) {
+    P->x0[r] = c[r][0] + c[r][1] * s + c[r][2] * t + c[r][3] * u + c[r][4] * s * t +
+               c[r][5] * s * u + c[r][6] * t * u + c[r][7] * s * t * u;
+    J[r][0] = c[r][1] + c[r][4] * t + c[r][5] * u + c[r][7] * t * u;
+    J[r][1] = c[r][2] + c[r][4] * s + c[r][6] * u + c[r][7] * s * u;
+    J[r][2] = c[r][3] + c[r][5] * s + c[r][6] * t + c[r][7] * s * t;
+  }
+  double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) -
+               J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+               J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+  P->det = det;
+  P->Jinv[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) / det;
+  P->Jinv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
+  P->Jinv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
+  P->Jinv[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) / det;
+  P->Jinv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
+  P->Jinv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
+  P->Jinv[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) / det;
+  P->Jinv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
+  P->Jinv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+}
+
+/* second derivatives through the bilinear map
+ * (TQuadBilinear::GetOrigAllDerivatives, QuadBilinear.C:131-205): the 5 x 5
+ * matrix G taking (u_x, u_y, u_xx, u_xy, u_yy) to (u_xi, u_eta, u_xixi,
+ * u_xieta, u_etaeta) is inverted by Gaussian elimination with partial pivoting
+ * (SolveMultipleSystemsNew solves G X = I the same way); lw = rows 2 + 4 of
+ * G^-1: the Laplacian of a function from its reference derivatives */
+static void bilinear_lap_weights(const double *cv, const double *xi, double *lw) {
+  double c[3][8];
+  multilinear_coeffs(2, cv, c);
+  double s = xi[0], t = xi[1];
+  double xx = c[0][1] + c[0][3] * t, yx = c[1][1] + c[1][3] * t;
+  double xe = c[0][2] + c[0][3] * s, ye = c[1][2] + c[1][3] * s;
+  double G[5][10] = {{xx, yx, 0, 0, 0}, {xe, ye, 0, 0, 0},
+                     {0, 0, xx * xx, 2 * xx * yx, yx * yx},
+                     {c[0][3], c[1][3], xx * xe, yx * xe + xx * ye, yx * ye},
+                     {0, 0, xe * xe, 2 * xe * ye, ye * ye}};
+  for (int i = 0; i < 5; ++i) G[i][5 + i] = 1.0;
+  for (int col = 0; col < 5; ++col) {
+    int pr = col;
+    for (int i = col + 1; i < 5; ++i)
+      if (fabs(G[i][col]) > fabs(G[pr][col])) pr = i;
+    if (pr != col)
+      for (int j = 0; j < 10; ++j) {
+        double tmp = G[col][j];
+        G[col][j] = G[pr][j];
+        G[pr][j] = tmp;
+      }
+    double inv = 1.0 / G[col][col];
+    for (int j = 0; j < 10; ++j) G[col][j] *= inv;
+    for (int i = 0; i < 5; ++i) {
+      if (i == col) continue;
+      double f = G[i][col];
+      if (f != 0.0)
+        for (int j = 0; j < 10; ++j) G[i][j] -= f * G[col][j];
+    }
+  }
+  for (int k = 0; k < 5; ++k) lw[k] = G[2][5 + k] + G[4][5 + k];
+}
+
+/* TQuadrangle::GetMeasure (Quadrangle.C:102-117): two triangles */
+static double quad_measure(const double *cv) {
+  double x1 = cv[0], y1 = cv[1], x2 = cv[2], y2 = cv[3], x3 = cv[4], y3 = cv[5], x4 = cv[6],
+         y4 = cv[7];
+  return 0.5 * fabs(x2 * y3 - x3 * y2 - x1 * y3 + x3 * y1 + x1 * y2 - x2 * y1) +
+         0.5 * fabs(x4 * y3 - x3 * y4 - x1 * y3 + x3 * y1 + x1 * y4 - x4 * y1);
+}
+
 /* Tetrahedron.C:64-113 (diameter = longest edge, shortest edge) */
 static double cell_hK_s(int shape, int dim, const double *cv, int measure) {
+  if (shape != 2 && dim == 2 && (measure == 1 || measure == 3) &&
+      cell_is_multilinear(shape, dim, cv))
+    return sqrt(quad_measure(cv));
   if (shape != 2) return cell_hK(dim, cv, measure);
   if (measure == 1 || measure == 3) {
     affine_t A;
@@ -1481,6 +1621,15 @@ int orc_local_system(orc_problem *p, int level, int cell, double *Aloc,
   level_t *L = &p->lev[level];
   int dim = c->dim, nl = L->nloc;
   const double *cv = L->verts + (size_t)cell * L->nv * dim;
+  /* affine map per cell, or the bilinear / trilinear map at every point */
+  const int multi = cell_is_multilinear(p->shape, dim, cv);
+  if (multi && dim == 3 && (c->supg || p->tcd)) {
+    /* THexaTrilinear::GetOrigAllDerivatives (HexaTrilinear.C:185-222) throws */
+    FAIL("SUPG needs second derivatives on trilinear hexahedra");
+  }
+  if (multi && (p->tcd || c->neumann_mask || (dim == 3 && c->cell_measure != 0 &&
+                                               c->cell_measure != 2)))
+    FAIL("multilinear cells: stationary, Dirichlet, CELL_MEASURE 0/2 in 3D");
   affine_t A;
   cell_affine_s(p->shape, dim, cv, &A);
   double adet = fabs(A.det);
@@ -1490,6 +1639,12 @@ int orc_local_system(orc_problem *p, int level, int cell, double *Aloc,
   double ref[MAXLOC][NDER];
   int nh = dim == 2 ? 3 : 6;
   for (int q = 0; q < p->qr.nqp; ++q) {
+    double lw[5] = {0, 0, 0, 0, 0};
+    if (multi) {
+      multilinear_at(dim, cv, p->qr.xi[q], &A);
+      adet = fabs(A.det);
+      if (dim == 2) bilinear_lap_weights(cv, p->qr.xi[q], lw);
+    }
     basis_s(p->shape, dim, c->order, p->qr.xi[q], ref);
     /* GetOrigValues: physical derivatives */
     double u[MAXLOC], g[MAXLOC][3], lap[MAXLOC];
@@ -1511,14 +1666,25 @@ int orc_local_system(orc_problem *p, int level, int cell, double *Aloc,
       }
       (void)nh;
       double l = 0;
-      for (int r = 0; r < dim; ++r)
-        for (int a = 0; a < dim; ++a)
-          for (int b2 = 0; b2 < dim; ++b2)
-            l += A.Jinv[a][r] * A.Jinv[b2][r] * H[a][b2];
+      if (multi) {
+        /* (u_xi, u_eta, u_xixi, u_xieta, u_etaeta) through G^-1; the
+         * trilinear case takes no second derivatives (Galerkin only) */
+        if (dim == 2)
+          l = lw[0] * ref[k][1] + lw[1] * ref[k][2] + lw[2] * H[0][0] + lw[3] * H[0][1] +
+              lw[4] * H[1][1];
+      } else {
+        for (int r = 0; r < dim; ++r)
+          for (int a = 0; a < dim; ++a)
+            for (int b2 = 0; b2 < dim; ++b2)
+              l += A.Jinv[a][r] * A.Jinv[b2][r] * H[a][b2];
+      }
       lap[k] = l;
     }
     double x[3];
-    affine_map(dim, &A, p->qr.xi[q], x);
+    if (multi)
+      for (int r = 0; r < dim; ++r) x[r] = A.x0[r];
+    else
+      affine_map(dim, &A, p->qr.xi[q], x);
     double co[8];
     if (p->coef_in) {
       /* CoeffFct values at this point: eps, b, c, f; the L_inf norm of b that
@@ -1793,7 +1959,7 @@ static int assemble_into(orc_problem *p, int level, double *val, double *rhs,
   if (mval) memset(mval, 0, sizeof(double) * L->nnz);
   double Aloc[MAXLOC * MAXLOC], floc[MAXLOC], Mloc[MAXLOC * MAXLOC];
   for (int cell = 0; cell < L->ncells; ++cell) {
-    orc_local_system(p, level, cell, Aloc, floc);
+    if (orc_local_system(p, level, cell, Aloc, floc)) return -1;
     if (mval) local_mass(p, L, cell, Mloc);
     const int *dof = L->gdof + cell * nl;
     for (int m = 0; m < nl; ++m) {
@@ -1851,9 +2017,19 @@ static int assemble_into(orc_problem *p, int level, double *val, double *rhs,
       if (bc_type(c, comp) == 0) {
         int idx[MAXLOC];
         int n = joint_dofs(dim, c->order, j, idx);
+        const int multi = cell_is_multilinear(p->shape, dim, cv);
         for (int m = 0; m < n; ++m) {
           double x[3], u[6];
-          dof_position(dim, c->order, cv, idx[m], x);
+          if (multi) {
+            /* the nodal functional's point on the bilinear / trilinear cell */
+            double r[3];
+            affine_t P;
+            local_dof_ref(dim, c->order, idx[m], r);
+            multilinear_at(dim, cv, r, &P);
+            for (int a = 0; a < dim; ++a) x[a] = P.x0[a];
+          } else {
+            dof_position(dim, c->order, cv, idx[m], x);
+          }
           exact_sol(c, x, u);
           rhs[L->gdof[cell * nl + idx[m]]] = u[0];
         }
@@ -1888,10 +2064,19 @@ int orc_quadrature_points(const orc_problem *p, int level, int *nqp, double *x) 
   *nqp = p->qr.nqp;
   if (!x) return 0;
   for (int cell = 0; cell < L->ncells; ++cell) {
+    const double *cv = L->verts + (size_t)cell * L->nv * dim;
     affine_t A;
-    cell_affine_s(p->shape, dim, L->verts + (size_t)cell * L->nv * dim, &A);
-    for (int q = 0; q < p->qr.nqp; ++q)
-      affine_map(dim, &A, p->qr.xi[q], x + ((size_t)cell * p->qr.nqp + q) * dim);
+    cell_affine_s(p->shape, dim, cv, &A);
+    const int multi = cell_is_multilinear(p->shape, dim, cv);
+    for (int q = 0; q < p->qr.nqp; ++q) {
+      double *xq = x + ((size_t)cell * p->qr.nqp + q) * dim;
+      if (multi) {
+        multilinear_at(dim, cv, p->qr.xi[q], &A);
+        for (int r = 0; r < dim; ++r) xq[r] = A.x0[r];
+      } else {
+        affine_map(dim, &A, p->qr.xi[q], xq);
+      }
+    }
   }
   return 0;
 }
@@ -2395,10 +2580,12 @@ int orc_errors(const orc_problem *p, double *errors) {
     const double *cv = L->verts + (size_t)cell * L->nv * dim;
     affine_t A;
     cell_affine_s(p->shape, dim, cv, &A);
+    const int multi = cell_is_multilinear(p->shape, dim, cv);
     double hK = cell_hK_s(p->shape, dim, cv, c->cell_measure);
     double fv[MAXLOC];
     for (int k = 0; k < nl; ++k) fv[k] = L->sol[L->gdof[cell * nl + k]];
     for (int q = 0; q < p->qr.nqp; ++q) {
+      if (multi) multilinear_at(dim, cv, p->qr.xi[q], &A);
       double ref[MAXLOC][NDER];
       basis_s(p->shape, dim, c->order, p->qr.xi[q], ref);
       double der[4] = {0, 0, 0, 0};
@@ -2415,7 +2602,10 @@ int orc_errors(const orc_problem *p, double *errors) {
         der[1 + r] = s;
       }
       double x[3], u[6], co[8];
-      affine_map(dim, &A, p->qr.xi[q], x);
+      if (multi)
+        for (int r = 0; r < dim; ++r) x[r] = A.x0[r];
+      else
+        affine_map(dim, &A, p->qr.xi[q], x);
       exact_sol(c, x, u);
       coeffs_at(c, x, co);
       double le = fabs(u[0] - der[0]);

@@ -55,7 +55,7 @@ EXPORTED = [
     "cdg_server_counters", "cdg_problem_apply32", "cdg_problem_tuning",
     "cdg_problem_quadrature_points", "cdg_problem_assemble_coefficients",
     "cdg_problem_set_fp32_tensor_levels", "cdg_problem_get_matrix32", "cdg_solve_batched",
-    "cdg_server_batch_counters",
+    "cdg_server_batch_counters", "cdg_hierarchy_perturb",
 ]
 
 
@@ -196,6 +196,7 @@ def lib():
             "cdg_solve_batched": [P, ctypes.c_int, PP, ctypes.POINTER(SolverParams), ip,
                                   ctypes.POINTER(SolveStats)],
             "cdg_server_batch_counters": [P, ctypes.POINTER(ctypes.c_longlong)],
+            "cdg_hierarchy_perturb": [P, ctypes.c_double, ctypes.c_ulonglong],
         }
         for name, args in sig.items():
             f = getattr(L, name)
@@ -282,8 +283,10 @@ def solver_params(preconditioner="jacobi", max_n_iterations=100, min_n_iteration
 class Hierarchy:
     """Host setup: unit square/cube (roots^dim cells) refined nref times, the
     Q_order space and CSR pattern of each of n_levels levels (0 = finest).
-    tetra=True: roots^3 cubes of 6 Kuhn tetrahedra, P_order, with the finest
-    interior vertices perturbed by perturb*h (seeded).  ctx: number the DOFs
+    tetra=True: roots^3 cubes of 6 Kuhn tetrahedra, P_order.  perturb > 0:
+    the finest interior vertices moved by up to perturb*h (seeded); on
+    quadrilaterals and hexahedra the cells become general (bilinear /
+    trilinear maps).  ctx: number the DOFs
     and build the patterns on that context's GPU instead of the host."""
 
     def __init__(self, dim, order, nref, n_levels=1, roots=1, neumann_mask=0, tetra=False,
@@ -305,6 +308,9 @@ class Hierarchy:
             _chk(lib().cdg_hierarchy_create(dim, order, roots, nref, n_levels, neumann_mask,
                                             ctypes.byref(h)))
         self.h = h
+        if not tetra and perturb > 0:
+            # general quadrilaterals / hexahedra on the finest level
+            _chk(lib().cdg_hierarchy_perturb(h, perturb, seed))
 
     def __del__(self):
         if getattr(self, "h", None):

@@ -198,6 +198,23 @@ int cdg_hierarchy_create(int dim, int order, int roots, int nref, int n_levels, 
   API_GUARD(hierarchy_create(dim, order, roots, nref, n_levels, neumann_mask, out));
 }
 
+int cdg_hierarchy_perturb(cdg_hierarchy* h, double amplitude, unsigned long long seed) {
+  if (!h || h->mesh.empty() || amplitude < 0 || amplitude >= 0.5) {
+    set_error("bad arguments (amplitude in [0, 0.5))");
+    return CDG_ERR_ARG;
+  }
+  Mesh& m = h->mesh[0];
+  // cells per direction of the unit square / cube (6 tetrahedra per cube)
+  const double cubes = (double)m.ncells / (m.shape == kTetra ? 6.0 : 1.0);
+  const long n = std::lround(std::pow(cubes, 1.0 / m.dim));
+  if (n < 1) {
+    set_error("empty mesh");
+    return CDG_ERR_ARG;
+  }
+  if (amplitude > 0) perturb_interior(m, 1.0 / (double)n, amplitude, seed);
+  return CDG_OK;
+}
+
 int cdg_hierarchy_create_tetra(int order, int roots, int nref, int n_levels, int neumann_mask,
                                double perturb, unsigned long long seed, cdg_hierarchy** out) {
   API_GUARD(hierarchy_create_tetra(order, roots, nref, n_levels, neumann_mask, perturb, seed, out));
@@ -345,11 +362,41 @@ struct PhaseClock {
   }
 };
 
+// the first quadrilateral of the mesh that is not a parallelogram
+// (hexahedron not a parallelepiped), -1 if all are, by the reference's shape
+// tests (TQuadrangle::CheckQuad, Quadrangle.C:119-128: |x0 - x1 + x2 - x3| >
+// 1e-8 in a coordinate; THexahedron::CheckHexa, Hexahedron.C:196-235: a
+// Brick when the four bilinear-term combinations sum below 1e-8 in every
+// coordinate).  The reference maps such cells with TQuadBilinear /
+// THexaTrilinear; their levels are assembled per point here.
+static long first_non_affine_cell(const Mesh& m) {
+  if (m.shape == kTetra) return -1;
+  const int dim = m.dim, nv = m.nv;
+  for (long c = 0; c < m.ncells; ++c) {
+    const double* v = &m.verts[(size_t)c * nv * dim];
+    if (m.shape == kQuad) {
+      for (int a = 0; a < 2; ++a)
+        if (std::fabs(v[a] - v[2 + a] + v[4 + a] - v[6 + a]) > 1e-8) return c;
+      continue;
+    }
+    for (int a = 0; a < 3; ++a) {
+      auto x = [&](int i) { return v[3 * i + a]; };
+      const double t1 = std::fabs(x(0) - x(1) - x(3) + x(2) + x(4) - x(5) - x(7) + x(6));
+      const double t2 = std::fabs(x(0) - x(1) + x(3) - x(2) - x(4) + x(5) - x(7) + x(6));
+      const double t3 = std::fabs(x(0) + x(1) - x(3) - x(2) - x(4) - x(5) + x(7) + x(6));
+      const double t4 = std::fabs(-x(0) + x(1) + x(3) - x(2) + x(4) - x(5) - x(7) + x(6));
+      if (t1 + t2 + t3 + t4 >= 1e-8) return c;
+    }
+  }
+  return -1;
+}
+
 static int finish_problem(cdg_context* ctx, cdg_problem* p, const std::vector<std::vector<int>>& parents,
                           const std::vector<Mesh>* nested) {
   PhaseClock clk;
   CDG_CUDA(cudaMalloc(&p->d_zero_diag, sizeof(int)));
   CDG_CUDA(cudaMemsetAsync(p->d_zero_diag, 0, sizeof(int), ctx->stream));
+  for (auto& L : p->lev) L.multilinear = first_non_affine_cell(L.mesh) >= 0 ? 1 : 0;
   for (auto& L : p->lev) {
     CDG_TRY(upload_level(ctx, L));
     clk.lap(0, ctx->stream);
@@ -437,40 +484,6 @@ int cdg_problem_create(cdg_context* ctx, const cdg_hierarchy* h, cdg_problem** o
   API_GUARD(problem_create(ctx, h, out));
 }
 
-// the first quadrilateral (hexahedron) of the mesh that is not a parallelogram
-// (parallelepiped), -1 if all are: the library maps cells affinely
-// (QuadAffin / HexaAffin through vertices 0, 1, 3 (, 4)); the reference takes
-// TQuadBilinear / THexaTrilinear for the others, which are not built here
-static long first_non_affine_cell(const Mesh& m) {
-  if (m.shape == kTetra) return -1;
-  const int dim = m.dim, nv = m.nv;
-  // vertex = v0 + sum of the listed edge vectors (v1-v0, v3-v0, v4-v0)
-  static const int quad_chk[1][3] = {{2, 1, 3}};
-  static const int hexa_chk[4][4] = {{2, 1, 3, -1}, {5, 1, 4, -1}, {7, 3, 4, -1}, {6, 1, 3, 4}};
-  for (long c = 0; c < m.ncells; ++c) {
-    const double* v = &m.verts[(size_t)c * nv * dim];
-    double scale = 0.0;
-    for (int e : {1, 3, 4}) {
-      if (e >= nv) continue;
-      double l = 0.0;
-      for (int a = 0; a < dim; ++a) l += (v[e * dim + a] - v[a]) * (v[e * dim + a] - v[a]);
-      scale += std::sqrt(l);
-    }
-    const int nchk = m.shape == kQuad ? 1 : 4;
-    for (int k = 0; k < nchk; ++k) {
-      const int* t = m.shape == kQuad ? quad_chk[k] : hexa_chk[k];
-      double d2 = 0.0;
-      for (int a = 0; a < dim; ++a) {
-        double x = v[a];
-        for (int e = 1; e < (m.shape == kQuad ? 3 : 4); ++e)
-          if (t[e] >= 0) x += v[t[e] * dim + a] - v[a];
-        d2 += (v[t[0] * dim + a] - x) * (v[t[0] * dim + a] - x);
-      }
-      if (std::sqrt(d2) > 1e-10 * scale) return c;
-    }
-  }
-  return -1;
-}
 
 static int problem_from_arrays(cdg_context* ctx, int cell_type, int order, int nl, const int* n_cells,
                                const double* const* verts, const int* const* gn,
@@ -507,13 +520,6 @@ static int problem_from_arrays(cdg_context* ctx, int cell_type, int order, int n
     L.mesh.nv = nv;
     L.mesh.ncells = n_cells[l];
     L.mesh.verts.assign(verts[l], verts[l] + (size_t)n_cells[l] * nv * dim);
-    const long bad = first_non_affine_cell(L.mesh);
-    if (bad >= 0) {
-      delete p;
-      set_error("cell %ld of level %d is not a %s: bilinear/trilinear reference maps are "
-                "not supported", bad, l, shape == kQuad ? "parallelogram" : "parallelepiped");
-      return CDG_ERR_ARG;
-    }
     L.space.dim = dim;
     L.space.shape = shape;
     L.space.order = order;
@@ -589,7 +595,7 @@ static int assemble_all(cdg_problem* p, const cdg_assembly_params* a) {
   for (size_t l = 0; l < nl; ++l) {
     // with the option, the levels between the finest and the coarsest (FP32
     // operators of the mixed-precision multigrid) come from the tensor cores
-    if (p->tc_levels && l > 0 && l + 1 < nl)
+    if (p->tc_levels && l > 0 && l + 1 < nl && !p->lev[l].multilinear)
       CDG_TRY(assemble_level_tc(p->ctx, p, p->lev[l], *a));
     else
       CDG_TRY(assemble_level(p->ctx, p, p->lev[l], *a));

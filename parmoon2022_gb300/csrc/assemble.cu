@@ -280,6 +280,117 @@ __device__ void cell_affine_s(int shape, int dim, const double* __restrict__ cv,
   invert_J(dim, A);
 }
 
+// Multilinear reference maps of quadrilaterals that are not parallelograms
+// and hexahedra that are not parallelepipeds (TQuadBilinear::SetCell,
+// QuadBilinear.C:243-263; THexaTrilinear::SetCell, HexaTrilinear.C:225-270):
+// x_r(xi) = c0 + c1 xi + c2 eta + c3 xi eta (2D), c0 + c1 xi + c2 eta +
+// c3 zeta + c4 xi eta + c5 xi zeta + c6 eta zeta + c7 xi eta zeta (3D), the
+// coefficients from the vertices in the reference cells' order
+struct MultiMap {
+  double c[3][8];
+};
+
+__device__ void multilinear_coeffs(int dim, const double* __restrict__ cv, MultiMap& M) {
+  if (dim == 2) {
+    for (int r = 0; r < 2; ++r) {
+      const double v0 = cv[r], v1 = cv[2 + r], v2 = cv[4 + r], v3 = cv[6 + r];
+      M.c[r][0] = (v0 + v1 + v2 + v3) * 0.25;
+      M.c[r][1] = (-v0 + v1 + v2 - v3) * 0.25;
+      M.c[r][2] = (-v0 - v1 + v2 + v3) * 0.25;
+      M.c[r][3] = (v0 - v1 + v2 - v3) * 0.25;
+    }
+    return;
+  }
+  for (int r = 0; r < 3; ++r) {
+    double v[8];
+    for (int i = 0; i < 8; ++i) v[i] = cv[3 * i + r];
+    M.c[r][0] = (v[0] + v[1] + v[3] + v[2] + v[4] + v[5] + v[7] + v[6]) * 0.125;
+    M.c[r][1] = (-v[0] + v[1] - v[3] + v[2] - v[4] + v[5] - v[7] + v[6]) * 0.125;
+    M.c[r][2] = (-v[0] - v[1] + v[3] + v[2] - v[4] - v[5] + v[7] + v[6]) * 0.125;
+    M.c[r][3] = (-v[0] - v[1] - v[3] - v[2] + v[4] + v[5] + v[7] + v[6]) * 0.125;
+    M.c[r][4] = (v[0] - v[1] - v[3] + v[2] + v[4] - v[5] - v[7] + v[6]) * 0.125;
+    M.c[r][5] = (v[0] - v[1] + v[3] - v[2] - v[4] + v[5] - v[7] + v[6]) * 0.125;
+    M.c[r][6] = (v[0] + v[1] - v[3] - v[2] - v[4] - v[5] + v[7] + v[6]) * 0.125;
+    M.c[r][7] = (-v[0] + v[1] + v[3] - v[2] + v[4] - v[5] - v[7] + v[6]) * 0.125;
+  }
+}
+
+// the map at a reference point: P.x0 = x(xi), P.J = dx/dxi, P.Ji, P.det
+// (GetOrigFromRef / GetOrigValues of the two maps)
+__device__ void multilinear_at(int dim, const MultiMap& M, const double* xi, Affine& P) {
+  if (dim == 2) {
+    const double s = xi[0], t = xi[1];
+    for (int r = 0; r < 2; ++r) {
+      const double* c = M.c[r];
+      P.x0[r] = c[0] + c[1] * s + c[2] * t + c[3] * s * t;
+      P.J[r][0] = c[1] + c[3] * t;
+      P.J[r][1] = c[2] + c[3] * s;
+    }
+  } else {
+    const double s = xi[0], t = xi[1], u = xi[2];
+    for (int r = 0; r < 3; ++r) {
+      const double* c = M.c[r];
+      P.x0[r] = c[0] + c[1] * s + c[2] * t + c[3] * u + c[4] * s * t + c[5] * s * u +
+                c[6] * t * u + c[7] * s * t * u;
+      P.J[r][0] = c[1] + c[4] * t + c[5] * u + c[7] * t * u;
+      P.J[r][1] = c[2] + c[4] * s + c[6] * u + c[7] * s * u;
+      P.J[r][2] = c[3] + c[5] * s + c[6] * t + c[7] * s * t;
+    }
+  }
+  invert_J(dim, P);
+}
+
+// Laplacian weights of a bilinear quadrilateral at a point
+// (TQuadBilinear::GetOrigAllDerivatives, QuadBilinear.C:131-181): with
+// G the 5 x 5 matrix taking the physical derivatives (u_x, u_y, u_xx, u_xy,
+// u_yy) to the reference ones (u_xi, u_eta, u_xixi, u_xieta, u_etaeta), the
+// physical ones are G^-1 times the reference ones, and lap u = (row 2 + row 4
+// of G^-1) . (u_xi, u_eta, u_xixi, u_xieta, u_etaeta).  G^-1 by Gaussian
+// elimination with partial pivoting (the reference's SolveMultipleSystemsNew
+// solves G X = I the same way)
+__device__ void bilinear_lap_weights(const MultiMap& M, const double* xi, double* lw) {
+  const double s = xi[0], t = xi[1];
+  const double xx = M.c[0][1] + M.c[0][3] * t, yx = M.c[1][1] + M.c[1][3] * t;   // d/dxi
+  const double xe = M.c[0][2] + M.c[0][3] * s, ye = M.c[1][2] + M.c[1][3] * s;   // d/deta
+  double G[5][10];
+  const double row[5][5] = {{xx, yx, 0.0, 0.0, 0.0},
+                            {xe, ye, 0.0, 0.0, 0.0},
+                            {0.0, 0.0, xx * xx, 2.0 * xx * yx, yx * yx},
+                            {M.c[0][3], M.c[1][3], xx * xe, yx * xe + xx * ye, yx * ye},
+                            {0.0, 0.0, xe * xe, 2.0 * xe * ye, ye * ye}};
+  for (int i = 0; i < 5; ++i)
+    for (int j = 0; j < 10; ++j) G[i][j] = j < 5 ? row[i][j] : (j - 5 == i ? 1.0 : 0.0);
+  for (int col = 0; col < 5; ++col) {
+    int pr = col;
+    for (int i = col + 1; i < 5; ++i)
+      if (fabs(G[i][col]) > fabs(G[pr][col])) pr = i;
+    if (pr != col)
+      for (int j = 0; j < 10; ++j) {
+        const double tmp = G[col][j];
+        G[col][j] = G[pr][j];
+        G[pr][j] = tmp;
+      }
+    const double inv = 1.0 / G[col][col];
+    for (int j = 0; j < 10; ++j) G[col][j] *= inv;
+    for (int i = 0; i < 5; ++i) {
+      if (i == col) continue;
+      const double f = G[i][col];
+      if (f != 0.0)
+        for (int j = 0; j < 10; ++j) G[i][j] -= f * G[col][j];
+    }
+  }
+  for (int k = 0; k < 5; ++k) lw[k] = G[2][5 + k] + G[4][5 + k];
+}
+
+// area of a quadrilateral from its two triangles (TQuadrangle::GetMeasure,
+// Quadrangle.C:102-117): the cell measure of a bilinear cell
+__device__ double quad_measure(const double* __restrict__ cv) {
+  const double x1 = cv[0], y1 = cv[1], x2 = cv[2], y2 = cv[3], x3 = cv[4], y3 = cv[5],
+               x4 = cv[6], y4 = cv[7];
+  return 0.5 * fabs(x2 * y3 - x3 * y2 - x1 * y3 + x3 * y1 + x1 * y2 - x2 * y1) +
+         0.5 * fabs(x4 * y3 - x3 * y4 - x1 * y3 + x3 * y1 + x1 * y4 - x4 * y1);
+}
+
 // quadrilateral / hexahedron form used by the fixed-scratch error norms
 __device__ void cell_affine(int dim, const double* __restrict__ cv, Affine& A) {
   cell_affine_s(dim == 2 ? kQuad : kHexa, dim, cv, A);
@@ -1434,17 +1545,24 @@ __global__ void k_copy_nonactive(int n, int nactive, const double* __restrict__ 
 template <int DIM>
 __global__ void __launch_bounds__(256)
 k_errors(AsmCoefs k, int ncells, const double* __restrict__ verts, const int* __restrict__ gdof,
-         const double* __restrict__ sol, RhsTables tb, double* __restrict__ acc,
+         const double* __restrict__ sol, RhsTables tb, int multi, double* __restrict__ acc,
          unsigned long long* __restrict__ linf) {
   const int NV = k.shape == kHexa ? 8 : 4;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int cell = blockIdx.x * 8 + warp;
   if (cell >= ncells) return;
   const double* cv = verts + (size_t)cell * NV * DIM;
+  // the cell's affine map, or its multilinear map evaluated at every point
   Affine A;
-  cell_affine_s(k.shape, DIM, cv, A);
-  const double adet = fabs(A.det);
-  const double hK = cell_hK_s(k.shape, DIM, cv, k.cell_measure, A.det);
+  MultiMap MM;
+  double hK;
+  if (multi) {
+    multilinear_coeffs(DIM, cv, MM);
+    hK = cell_hK_s(k.shape, DIM, cv, k.cell_measure, DIM == 2 ? quad_measure(cv) * 0.25 : 0.0);
+  } else {
+    cell_affine_s(k.shape, DIM, cv, A);
+    hK = cell_hK_s(k.shape, DIM, cv, k.cell_measure, A.det);
+  }
   const int nl = k.nloc;
   double fv = lane < nl ? sol[gdof[(size_t)cell * nl + lane]] : 0.0;
   double e[4] = {0, 0, 0, 0}, emax = 0.0;
@@ -1459,15 +1577,21 @@ k_errors(AsmCoefs k, int ncells, const double* __restrict__ verts, const int* __
       for (int a = 0; a < DIM; ++a) gr[a] += __shfl_xor_sync(0xffffffffu, gr[a], o);
     }
     if (lane == 0) {
+      double x[3], u[6], bx[3];
+      if (multi) {
+        multilinear_at(DIM, MM, tb.xi + q * 3, A);
+        for (int r = 0; r < DIM; ++r) x[r] = A.x0[r];
+      } else {
+        for (int r = 0; r < DIM; ++r) {
+          double s = A.x0[r];
+          for (int a = 0; a < DIM; ++a) s += A.J[r][a] * tb.xi[q * 3 + a];
+          x[r] = s;
+        }
+      }
+      const double adet = fabs(A.det);
       double g[3] = {0, 0, 0};
       for (int r = 0; r < DIM; ++r)
         for (int a = 0; a < DIM; ++a) g[r] += A.Ji[a][r] * gr[a];
-      double x[3], u[6], bx[3];
-      for (int r = 0; r < DIM; ++r) {
-        double s = A.x0[r];
-        for (int a = 0; a < DIM; ++a) s += A.J[r][a] * tb.xi[q * 3 + a];
-        x[r] = s;
-      }
       ex_exact(k, x, u);
       b_at(k, x, bx);
       double linfb = fmax(fabs(bx[0]), fabs(bx[1]));
@@ -2035,31 +2159,53 @@ struct QpTables {
 
 constexpr int kCoefThreads = 128;
 
+// src 0: coef[(cell * nqp + q) * (DIM + 3) + k] from the caller (k = 0 eps,
+// 1..DIM b, DIM+1 c, DIM+2 f); src 1: the example's eps, b(x), c, f(x) at
+// the physical point.  multi: the cells' multilinear maps, evaluated at every
+// point (J, J^-1, |det J|, the physical point and, in 2D, the Laplacian
+// through the bilinear map's second derivatives); otherwise one affine map
+// per cell.
 template <int DIM>
 __global__ void __launch_bounds__(kCoefThreads)
 k_coef_element(AsmCoefs k, int ncells, int nactive, const double* __restrict__ verts,
                const int* __restrict__ gdof, const int* __restrict__ slot, QpTables tb,
-               const double* __restrict__ coef, double* __restrict__ val,
+               const double* __restrict__ coef, int src, int multi, double* __restrict__ val,
                double* __restrict__ rhs, double* __restrict__ loc) {
   constexpr int NSYM = DIM == 2 ? 3 : 6;
   constexpr int NACC = (kMaxLoc * kMaxLoc + kCoefThreads - 1) / kCoefThreads;
   __shared__ double ph[kMaxLoc][DIM + 2];   // phi, grad phi (physical), laplacian
   __shared__ double cq[DIM + 5];            // eps, b, c, f, delta, w |det J|
-  __shared__ Affine A;
+  __shared__ Affine A;                      // the cell's affine map, or the point's
+  __shared__ MultiMap MM;
+  __shared__ double lw[5];
   __shared__ double hK;
   const int NV = k.shape == kHexa ? 8 : 4;
   const int nl = k.nloc, ne = nl * nl, tid = threadIdx.x;
   for (int cell = blockIdx.x; cell < ncells; cell += gridDim.x) {
     const double* cv = verts + (size_t)cell * NV * DIM;
     if (tid == 0) {
-      cell_affine_s(k.shape, DIM, cv, A);
-      hK = cell_hK_s(k.shape, DIM, cv, k.cell_measure, A.det);
+      if (multi) {
+        multilinear_coeffs(DIM, cv, MM);
+        // measure-based cell sizes take the cell's area (two triangles in 2D)
+        const double det = DIM == 2 ? quad_measure(cv) * 0.25 : 0.0;
+        hK = cell_hK_s(k.shape, DIM, cv, k.cell_measure, det);
+      } else {
+        cell_affine_s(k.shape, DIM, cv, A);
+        hK = cell_hK_s(k.shape, DIM, cv, k.cell_measure, A.det);
+      }
     }
     __syncthreads();
     double acc[NACC], facc = 0.0;
 #pragma unroll
     for (int m = 0; m < NACC; ++m) acc[m] = 0.0;
     for (int q = 0; q < tb.nqp; ++q) {
+      if (multi) {
+        if (tid == 64) {
+          multilinear_at(DIM, MM, tb.xi + q * 3, A);
+          if (DIM == 2 && k.supg) bilinear_lap_weights(MM, tb.xi + q * 3, lw);
+        }
+        __syncthreads();
+      }
       if (tid < nl) {
         const int i = tid;
         ph[i][0] = tb.val[q * nl + i];
@@ -2068,28 +2214,52 @@ k_coef_element(AsmCoefs k, int ncells, int nactive, const double* __restrict__ v
           for (int a = 0; a < DIM; ++a) s += A.Ji[a][r] * tb.grad[(q * DIM + a) * nl + i];
           ph[i][1 + r] = s;
         }
-        // Laplacian of the affine image: sum_r J^-T H J^-1 (r, r)
-        double H[3][3];
-        int pr = 0;
-        for (int a = 0; a < DIM; ++a)
-          for (int b = a; b < DIM; ++b) {
-            H[a][b] = H[b][a] = tb.hess[(q * NSYM + pr) * nl + i];
-            ++pr;
-          }
         double l = 0.0;
-        for (int r = 0; r < DIM; ++r)
+        if (multi) {
+          // bilinear map: lap = lw . (u_xi, u_eta, u_xixi, u_xieta, u_etaeta);
+          // trilinear maps (Galerkin only) need none
+          if (DIM == 2 && k.supg) {
+            const double rd[5] = {tb.grad[(q * DIM) * nl + i], tb.grad[(q * DIM + 1) * nl + i],
+                                  tb.hess[(q * NSYM) * nl + i], tb.hess[(q * NSYM + 1) * nl + i],
+                                  tb.hess[(q * NSYM + 2) * nl + i]};
+            for (int a = 0; a < 5; ++a) l += lw[a] * rd[a];
+          }
+        } else {
+          // Laplacian of the affine image: sum_r J^-T H J^-1 (r, r)
+          double H[3][3];
+          int pr = 0;
           for (int a = 0; a < DIM; ++a)
-            for (int b = 0; b < DIM; ++b) l += A.Ji[a][r] * A.Ji[b][r] * H[a][b];
+            for (int b = a; b < DIM; ++b) {
+              H[a][b] = H[b][a] = tb.hess[(q * NSYM + pr) * nl + i];
+              ++pr;
+            }
+          for (int r = 0; r < DIM; ++r)
+            for (int a = 0; a < DIM; ++a)
+              for (int b = 0; b < DIM; ++b) l += A.Ji[a][r] * A.Ji[b][r] * H[a][b];
+        }
         ph[i][DIM + 1] = l;
       } else if (tid == 32) {
-        const double* ci = coef + ((size_t)cell * tb.nqp + q) * (DIM + 3);
         double bq[3] = {0.0, 0.0, 0.0}, linfb = 0.0;
-        for (int a = 0; a < DIM + 3; ++a) cq[a] = ci[a];
-        for (int a = 0; a < DIM; ++a) {
-          bq[a] = ci[1 + a];
-          linfb = fmax(linfb, fabs(bq[a]));
+        if (src == 0) {
+          const double* ci = coef + ((size_t)cell * tb.nqp + q) * (DIM + 3);
+          for (int a = 0; a < DIM + 3; ++a) cq[a] = ci[a];
+          for (int a = 0; a < DIM; ++a) bq[a] = ci[1 + a];
+        } else {
+          double x[3] = {0.0, 0.0, 0.0};
+          for (int r = 0; r < DIM; ++r) {
+            double sx = A.x0[r];
+            if (!multi)
+              for (int a = 0; a < DIM; ++a) sx += A.J[r][a] * tb.xi[q * 3 + a];
+            x[r] = sx;
+          }
+          b_at(k, x, bq);
+          cq[0] = k.eps;
+          for (int a = 0; a < DIM; ++a) cq[1 + a] = bq[a];
+          cq[DIM + 1] = k.c;
+          cq[DIM + 2] = ex_source(k, x);
         }
-        cq[DIM + 3] = k.supg ? sdfem_delta(k, cv, hK, ci[0], bq, ci[DIM + 1], linfb) : 0.0;
+        for (int a = 0; a < DIM; ++a) linfb = fmax(linfb, fabs(bq[a]));
+        cq[DIM + 3] = k.supg ? sdfem_delta(k, cv, hK, cq[0], bq, cq[DIM + 1], linfb) : 0.0;
         cq[DIM + 4] = tb.w[q] * fabs(A.det);
       }
       __syncthreads();
@@ -2117,7 +2287,7 @@ k_coef_element(AsmCoefs k, int ncells, int nactive, const double* __restrict__ v
         for (int r = 0; r < DIM; ++r) bgi += cq[1 + r] * ph[tid][1 + r];
         facc = fma(mult * f, ph[tid][0] + delta * bgi, facc);
       }
-      __syncthreads();   // ph and cq are rewritten for the next point
+      __syncthreads();   // ph, cq and the point's map are rewritten for the next point
     }
 #pragma unroll
     for (int m = 0; m < NACC; ++m) {
@@ -2133,16 +2303,22 @@ k_coef_element(AsmCoefs k, int ncells, int nactive, const double* __restrict__ v
         // Dirichlet value at the node from the example's boundary data
         double r[3], x[3], u[6];
         ref_node_s(k.shape, DIM, k.order, tid, r);
-        for (int rr = 0; rr < DIM; ++rr) {
-          double sx = A.x0[rr];
-          for (int a = 0; a < DIM; ++a) sx += A.J[rr][a] * r[a];
-          x[rr] = sx;
+        if (multi) {
+          Affine P;
+          multilinear_at(DIM, MM, r, P);
+          for (int rr = 0; rr < DIM; ++rr) x[rr] = P.x0[rr];
+        } else {
+          for (int rr = 0; rr < DIM; ++rr) {
+            double sx = A.x0[rr];
+            for (int a = 0; a < DIM; ++a) sx += A.J[rr][a] * r[a];
+            x[rr] = sx;
+          }
         }
         ex_exact(k, x, u);
         rhs[row] = u[0];
       }
     }
-    __syncthreads();   // A and hK are rewritten for the next cell
+    __syncthreads();   // A, MM and hK are rewritten for the next cell
   }
 }
 
@@ -2170,9 +2346,14 @@ int level_quadrature_points(const DevLevel& L, const cdg_assembly_params& a, int
   if (!x) return CDG_OK;
   const int nv = L.mesh.nv, dim = L.dim;
   for (int c = 0; c < L.ncells; ++c)
-    for (int q = 0; q < t.nqp; ++q)
-      cell_point(L.shape, dim, &L.mesh.verts[(size_t)c * nv * dim], &t.xi[3 * q],
-                 x + ((size_t)c * t.nqp + q) * dim);
+    for (int q = 0; q < t.nqp; ++q) {
+      const double* cv = &L.mesh.verts[(size_t)c * nv * dim];
+      double* xq = x + ((size_t)c * t.nqp + q) * dim;
+      if (L.multilinear)
+        cell_point_multilinear(dim, cv, &t.xi[3 * q], xq);
+      else
+        cell_point(L.shape, dim, cv, &t.xi[3 * q], xq);
+    }
   return CDG_OK;
 }
 
@@ -2227,10 +2408,16 @@ static int mf_prepare(cdg_context* ctx, cdg_problem* p, DevLevel& L, const AsmCo
   return CDG_OK;
 }
 
+static int pointwise_assembly(cdg_context* ctx, cdg_problem* p, DevLevel& L, const AsmCoefs& k,
+                              const double* coef_host);
+
 int assemble_level(cdg_context* ctx, cdg_problem* p, DevLevel& L, const cdg_assembly_params& a) {
   CDG_TRY(ensure_tables(ctx, p));
   AsmCoefs k = make_coefs(a, L.shape, L.order);
   CDG_TRY(check_coefs(k));
+  // cells with multilinear maps: the reference's per-point assembly with the
+  // example's coefficients (the contraction needs one Jacobian per cell)
+  if (L.multilinear) return pointwise_assembly(ctx, p, L, k, nullptr);
   cudaStream_t st = ctx->stream;
   // block->reset(), rhs.reset()
   CDG_CUDA(cudaMemsetAsync(L.val64, 0, (size_t)L.nnz * sizeof(double), st));
@@ -2307,19 +2494,44 @@ int ensure_fp64(cdg_context* ctx, cdg_problem* p, DevLevel& L) {
 
 // one level with coefficients per (cell, quadrature point) (the generic
 // CoeffFct path); the matrix-free operator is not used for such a level
-int assemble_level_coefficients(cdg_context* ctx, cdg_problem* p, DevLevel& L,
-                                const cdg_assembly_params& a, const double* coef_host) {
-  AsmCoefs k = make_coefs(a, L.shape, L.order);
-  CDG_TRY(check_coefs(k));
+// what the multilinear (per-point) path takes: Dirichlet boundaries; on
+// trilinear hexahedra no second derivatives (THexaTrilinear::
+// GetOrigAllDerivatives, HexaTrilinear.C:185-222, throws) and the cell sizes
+// from vertex distances (CELL_MEASURE 0 or 2)
+int check_multilinear(const DevLevel& L, const AsmCoefs& k) {
+  if (!L.multilinear) return CDG_OK;
   if (k.neumann_mask) {
-    set_error("Neumann boundary parts take their data from the example; the per-point "
-              "coefficient assembly handles Dirichlet boundaries only");
+    set_error("cells with multilinear maps: Dirichlet boundaries only");
     return CDG_ERR_ARG;
   }
+  if (L.dim == 3 && k.supg) {
+    set_error("SUPG needs second derivatives on trilinear hexahedra, which are not "
+              "transformed (the reference throws here as well)");
+    return CDG_ERR_ARG;
+  }
+  if (L.dim == 3 && k.cell_measure != 0 && k.cell_measure != 2) {
+    set_error("trilinear hexahedra take CELL_MEASURE 0 or 2");
+    return CDG_ERR_ARG;
+  }
+  return CDG_OK;
+}
+
+// per-point assembly of a level (k_coef_element): coefficients from the
+// caller (coef_host, CoeffFct values at level_quadrature_points) or, with
+// coef_host null, from the example at the physical points; each level's
+// affine or multilinear cell maps
+static int pointwise_assembly(cdg_context* ctx, cdg_problem* p, DevLevel& L, const AsmCoefs& k,
+                              const double* coef_host) {
+  if (k.neumann_mask) {
+    set_error("the per-point assembly (CoeffFct coefficients, multilinear cells) handles "
+              "Dirichlet boundaries only");
+    return CDG_ERR_ARG;
+  }
+  CDG_TRY(check_multilinear(L, k));
   std::vector<double> hess;
   RefTables t = coef_tables(L, k, &hess);
   const int ncoef = L.dim + 3;
-  const size_t ncoefs = (size_t)L.ncells * t.nqp * ncoef;
+  const size_t ncoefs = coef_host ? (size_t)L.ncells * t.nqp * ncoef : 0;
   const size_t ntab = t.w.size() + t.xi.size() + t.val.size() + t.grad.size() + hess.size();
   cudaStream_t st = ctx->stream;
   double* buf = nullptr;
@@ -2338,22 +2550,26 @@ int assemble_level_coefficients(cdg_context* ctx, cdg_problem* p, DevLevel& L,
   tb.grad = put(t.grad);
   tb.hess = put(hess);
   tb.nqp = t.nqp;
-  cudaError_t e = cudaMemcpyAsync(d, coef_host, ncoefs * sizeof(double), cudaMemcpyHostToDevice, st);
-  if (e != cudaSuccess) {
-    cudaFree(buf);
-    CDG_CUDA(e);
+  if (coef_host) {
+    cudaError_t e = cudaMemcpyAsync(d, coef_host, ncoefs * sizeof(double),
+                                    cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) {
+      cudaFree(buf);
+      CDG_CUDA(e);
+    }
   }
   L.mf_valid = 0;
   L.fp64_stale = 0;
   CDG_CUDA(cudaMemsetAsync(L.val64, 0, (size_t)L.nnz * sizeof(double), st));
   CDG_CUDA(cudaMemsetAsync(L.rhs, 0, (size_t)L.ndof * sizeof(double), st));
   const int g = std::max(1, std::min(L.ncells, ctx->num_sms * 8));
+  const int src = coef_host ? 0 : 1;
   if (L.dim == 2)
     CDG_LAUNCH(ctx, k_coef_element<2>, g, kCoefThreads, 0, k, L.ncells, L.nactive, L.verts,
-               L.gdof, L.slot, tb, d, L.val64, L.rhs, L.rhs_loc);
+               L.gdof, L.slot, tb, d, src, L.multilinear, L.val64, L.rhs, L.rhs_loc);
   else
     CDG_LAUNCH(ctx, k_coef_element<3>, g, kCoefThreads, 0, k, L.ncells, L.nactive, L.verts,
-               L.gdof, L.slot, tb, d, L.val64, L.rhs, L.rhs_loc);
+               L.gdof, L.slot, tb, d, src, L.multilinear, L.val64, L.rhs, L.rhs_loc);
   const int nd = L.ndof - L.nactive;
   if (nd > 0)
     CDG_LAUNCH(ctx, k_dirichlet_rows, grid_for<int>(nd, 256), 256, 0, L.ndof, L.nactive,
@@ -2365,16 +2581,24 @@ int assemble_level_coefficients(cdg_context* ctx, cdg_problem* p, DevLevel& L,
     CDG_LAUNCH(ctx, k_copy_nonactive, grid_for<int>(nd, 256), 256, 0, L.ndof, L.nactive, L.rhs,
                L.sol);
   CDG_TRY(finish_matrix(ctx, p, L));
-  e = cudaStreamSynchronize(st);   // the tables and coefficients are released
+  cudaError_t e = cudaStreamSynchronize(st);   // the tables and coefficients are released
   cudaFree(buf);
   CDG_CUDA(e);
   return CDG_OK;
+}
+
+int assemble_level_coefficients(cdg_context* ctx, cdg_problem* p, DevLevel& L,
+                                const cdg_assembly_params& a, const double* coef_host) {
+  AsmCoefs k = make_coefs(a, L.shape, L.order);
+  CDG_TRY(check_coefs(k));
+  return pointwise_assembly(ctx, p, L, k, coef_host);
 }
 
 int level_errors(cdg_context* ctx, cdg_problem* p, DevLevel& L, const cdg_assembly_params& a,
                  double* errors) {
   AsmCoefs k = make_coefs(a, L.shape, L.order);
   if (k.nqp > 128) { set_error("quadrature rule too large"); return CDG_ERR_ARG; }
+  CDG_TRY(check_multilinear(L, k));
   RhsTables tb;
   CDG_TRY(get_rhs_tables(ctx, L.shape, L.order, k.nqp1, &tb));
   double* acc = nullptr;
@@ -2383,10 +2607,10 @@ int level_errors(cdg_context* ctx, cdg_problem* p, DevLevel& L, const cdg_assemb
   unsigned long long* lm = (unsigned long long*)(acc + 4);
   if (L.dim == 2)
     CDG_LAUNCH(ctx, k_errors<2>, grid_for<int>(L.ncells, 8), 256, 0, k, L.ncells, L.verts,
-               L.gdof, L.sol, tb, acc, lm);
+               L.gdof, L.sol, tb, L.multilinear, acc, lm);
   else
     CDG_LAUNCH(ctx, k_errors<3>, grid_for<int>(L.ncells, 8), 256, 0, k, L.ncells, L.verts,
-               L.gdof, L.sol, tb, acc, lm);
+               L.gdof, L.sol, tb, L.multilinear, acc, lm);
   double h[5];
   CDG_CUDA(cudaMemcpyAsync(h, acc, 5 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CDG_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -2431,6 +2655,11 @@ int tcd_interpolate(cdg_context* ctx, cdg_problem* p, const cdg_assembly_params&
 int tcd_assemble_level(cdg_context* ctx, cdg_problem* p, DevLevel& L,
                        const cdg_assembly_params& a, bool with_mass, double theta1,
                        double tau) {
+  if (L.multilinear) {
+    set_error("the time-dependent problem takes affine cells (parallelograms, "
+              "parallelepipeds, tetrahedra)");
+    return CDG_ERR_ARG;
+  }
   CDG_TRY(ensure_tables(ctx, p));
   CDG_TRY(ensure_tcd(L));
   L.mf_valid = 0;   // the FP32 operator becomes the time-dependent system
@@ -2658,6 +2887,11 @@ extern "C" int cdg_problem_errors_noalloc(cdg_problem* p, const cdg_assembly_par
   }
   cdg_context* ctx = p->ctx;
   DevLevel& L = p->lev[0];
+  if (L.multilinear) {
+    set_error("cdg_problem_errors_noalloc maps cells affinely; use cdg_problem_errors on "
+              "meshes with multilinear cells");
+    return CDG_ERR_ARG;
+  }
   if (L.shape == kTetra) {
     set_error("cdg_problem_errors_noalloc evaluates tensor-product bases only "
               "(quadrilaterals, hexahedra); use cdg_problem_errors");

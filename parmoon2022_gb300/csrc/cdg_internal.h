@@ -99,6 +99,7 @@ void local_dof_ref(int dim, int order, int k, double* r);
 void local_dof_ref_shape(int shape, int order, int k, double* r);
 // x = affine map of the cell (QuadAffin / HexaAffin / TetraAffin) at r
 void cell_point(int shape, int dim, const double* cv, const double* r, double* x);
+void cell_point_multilinear(int dim, const double* cv, const double* r, double* x);
 
 // ---------------------------------------------------------------------------
 // setup: structured meshes, DOF numbering, pattern, grid transfer

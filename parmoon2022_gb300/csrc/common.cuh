@@ -77,6 +77,10 @@ namespace cdg {
 struct DevLevel {
   int dim = 2, shape = kQuad, order = 1, nloc = 4, nv = 4;
   int ncells = 0, ndof = 0, nactive = 0, nnz = 0;
+  // some cell is a quadrilateral that is not a parallelogram (hexahedron not
+  // a parallelepiped): the level is assembled per point through the cells'
+  // bilinear / trilinear maps (TQuadBilinear, THexaTrilinear)
+  int multilinear = 0;
   // host copies of the inputs (info queries, transfers)
   Mesh mesh;
   Space space;

@@ -491,7 +491,9 @@ int mf_build_tiles(cdg_context* ctx, DevLevel& L) {
   return CDG_OK;
 }
 
-bool mf_eligible(const DevLevel& L) { return L.shape == kHexa && L.order == 2; }
+bool mf_eligible(const DevLevel& L) {
+  return L.shape == kHexa && L.order == 2 && !L.multilinear;
+}
 
 int mf_ensure(DevLevel& L) {
   if (L.mf_fac) return CDG_OK;

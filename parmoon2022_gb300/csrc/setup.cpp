@@ -167,6 +167,21 @@ void cell_point(int shape, int dim, const double* cv, const double* r, double* x
   }
 }
 
+// TQuadBilinear / THexaTrilinear::GetOrigFromRef: x = sum_v x_v N_v(r) with
+// the Q1 vertex functions (vertices 0-3 counterclockwise at zeta = -1, 4-7
+// above them); equal to the affine map on parallelograms / parallelepipeds
+void cell_point_multilinear(int dim, const double* cv, const double* r, double* x) {
+  static const int sg[8][3] = {{-1, -1, -1}, {1, -1, -1}, {1, 1, -1}, {-1, 1, -1},
+                               {-1, -1, 1},  {1, -1, 1},  {1, 1, 1},  {-1, 1, 1}};
+  const int nv = dim == 2 ? 4 : 8;
+  for (int c = 0; c < dim; ++c) x[c] = 0.0;
+  for (int v = 0; v < nv; ++v) {
+    double n = 1.0;
+    for (int a = 0; a < dim; ++a) n *= 0.5 * (1.0 + sg[v][a] * r[a]);
+    for (int c = 0; c < dim; ++c) x[c] += n * cv[v * dim + c];
+  }
+}
+
 // hess: symmetric pairs (a<=b) in order (00,01,11) / (00,01,02,11,12,22)
 void ref_basis_point(int dim, int p, const double* xi, double* val, double* grad,
                      double* hess) {

@@ -218,24 +218,36 @@ def test_from_arrays_equals_hierarchy(ctx):
 
 
 @pytest.mark.parametrize("dim", [2, 3])
-def test_from_arrays_rejects_non_affine_cells(ctx, dim):
-    # the reference maps such cells with TQuadBilinear / THexaTrilinear, which
-    # are not built: the problem is refused instead of assembled wrongly
+def test_from_arrays_maps_non_affine_cells_multilinearly(ctx, dim):
+    # a cell off the parallelogram (parallelepiped) is mapped as the
+    # reference maps it, by TQuadBilinear / THexaTrilinear: the level is
+    # assembled per point through the cells' multilinear maps and equals the
+    # oracle's matrix and rhs; sheared (still affine) meshes keep the
+    # contraction
     h = pg.Hierarchy(dim, 1, 2)
     rp, col = h.pattern(0)
     i = h.info(0)
     v = h.mesh(0).copy()
-    lv = dict(verts=v, dofs=h.dofs(0), ndof=i["ndof"], nactive=i["nactive"], row_ptr=rp, col=col)
+    lv = dict(verts=v, dofs=h.dofs(0), gdof=h.dofs(0), ndof=i["ndof"], nactive=i["nactive"],
+              row_ptr=rp, col=col)
     ct = pg.CELL_QUAD if dim == 2 else pg.CELL_HEXA
-    # a sheared (still affine) mesh is accepted
-    sh = v.copy()
-    sh[..., 0] += 0.3 * sh[..., 1]
-    pg.ConvectionDiffusion.from_arrays(ctx, ct, 1, [dict(lv, verts=sh)])
+    a = pg.assembly_params(example=pg.EX_SINE, eps=0.05, b=(1.0, 0.4, -0.3)[:dim], c=0.5)
+    cfg = po.make_config(dim, 1, 0, po.EX_SINE, eps=0.05, b=(1.0, 0.4, -0.3)[:dim], c=0.5)
     bad = v.copy()
     bad[5, 2, 0] += 0.01 * (1.0 / 4)     # vertex 2 of cell 5 off the parallelogram
-    with pytest.raises(pg.CdgError) as e:
-        pg.ConvectionDiffusion.from_arrays(ctx, ct, 1, [dict(lv, verts=bad)])
-    assert e.value.code == -1 and "cell 5" in str(e.value)
+    for verts in (v + 0.0, bad):
+        if verts is not bad:
+            verts[..., 0] += 0.3 * verts[..., 1]
+        gpu = pg.ConvectionDiffusion.from_arrays(ctx, ct, 1, [dict(lv, verts=verts)])
+        gpu.assemble(a)
+        o = po.Problem(cfg, arrays=[dict(lv, verts=verts)])
+        o.assemble()
+        assert rel(gpu.matrix(0), o.matrix(0)) < 1e-12
+        # active rows (the sheared mesh's boundary nodes lie off the unit
+        # square, where the oracle finds no boundary part to take values from)
+        na = i["nactive"]
+        assert rel(gpu.rhs(0)[:na], o.rhs(0)[:na]) < 1e-12
+        gpu.close()
 
 
 def test_errors_are_reported(ctx):
