@@ -1006,9 +1006,96 @@ def _worker_tcd(q):
     q.put(dt * 912673 / nd)
 
 
+BATCH_CLASSES = [(2, 1, 4, 3), (2, 2, 4, 3), (3, 1, 3, 2)]   # (dim, order, nref, levels)
+BATCH_METRIC = "batched small CD solves/s (one block per request, one launch)"
+
+
+def run_gpu_batch(args):
+    """Many small stationary solves in one launch (cdg_solve_batched) against
+    the same problems solved one at a time by the stream-level solver.  A
+    step is one launch over K = 2 x SMs requests of one class (host
+    preparation of the K problems included, assembly not); the headline class
+    is 2D Q1 16^2 (289 DOFs), the served mix's smallest."""
+    import torch
+    import parmoon2022_gb300 as pg
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    ctx = pg.Context(local)
+    nsm = torch.cuda.get_device_properties(local).multi_processor_count
+    K = 2 * nsm
+    rng = np.random.default_rng(17)
+    records = []
+    for dim, order, nref, levels in BATCH_CLASSES:
+        h = pg.Hierarchy(dim, order, nref, n_levels=levels)
+        probs, params_ = [], []
+        for q in range(K):
+            d = rng.standard_normal(dim)
+            d /= np.linalg.norm(d)
+            a = pg.assembly_params(example=pg.EX_CONST_F, eps=float(10 ** rng.uniform(-2, 0)),
+                                   b=tuple(d * rng.uniform(0, 1)), c=float(rng.uniform(0, 1)),
+                                   space_discretization_type="supg", sdfem_type=2)
+            cd = pg.ConvectionDiffusion(ctx, h)
+            cd.assemble(a)
+            probs.append(cd)
+            params_.append(pg.solver_params(
+                "multigrid", precision="mixed", max_n_iterations=500, gmres_restart=30,
+                residual_tolerance=0.0, residual_reduction=1e-10, multigrid_n_levels=levels,
+                multigrid_n_pre_smooth=2, multigrid_n_post_smooth=2, jacobi_damp=0.5))
+        x0 = [p.solution() for p in probs]
+        walls, its, launches = [], [], []
+        for step in range(args.warmup + args.steps):
+            for p, x in zip(probs, x0):
+                p.set_solution(x)
+            ctx.synchronize()
+            l0 = ctx.launches()
+            t0 = time.perf_counter()
+            out = pg.solve_batched(ctx, probs, params_)
+            t = time.perf_counter() - t0
+            launches.append(ctx.launches() - l0)
+            assert all(s == 0 and st.residual <= 1e-10 * st.initial_residual for s, st in out)
+            if step >= args.warmup:
+                walls.append(t)
+                its.append(float(np.mean([st.iterations for _, st in out])))
+        # the same problems one at a time (stream-level solver), 32 of them
+        t_one = []
+        for p, x, sp in list(zip(probs, x0, params_))[:32]:
+            p.set_solution(x)
+            ctx.synchronize()
+            t0 = time.perf_counter()
+            p.solve(sp)
+            t_one.append(time.perf_counter() - t0)
+        wall = float(np.median(walls))
+        records.append({"class": "%dD Q%d %d^%d" % (dim, order, 2 ** nref, dim),
+                        "dofs": probs[0].info(0)["ndof"], "requests_per_launch": K,
+                        "launch_ms": wall * 1e3, "solves_per_s": K / wall,
+                        "one_at_a_time_solves_per_s": 1.0 / float(np.mean(t_one)),
+                        "iterations_mean": float(np.mean(its)),
+                        "launches_per_step": int(launches[-1])})
+        for p in probs:
+            p.close()
+    if rank != 0:
+        return
+    head = records[0]
+    print(json.dumps({
+        "metric": BATCH_METRIC, "value": head["solves_per_s"], "unit": "solves/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": head["launch_ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64 FGMRES + f32 multigrid (mixed)", "data": "synthetic",
+        "config": {"workload": "batched: K = 2 x SMs small SUPG CD requests per launch, "
+                               "f = 1, eps log-U[1e-2,1], random b, c; FGMRES(30) + MG "
+                               "V(2,2) omega .5 to 1e-10", "l2": "small problems; no flush"},
+        "classes": records,
+        "batched_over_one_at_a_time": head["solves_per_s"] / head["one_at_a_time_solves_per_s"],
+        "gpu_launches": head["launches_per_step"] * args.steps}))
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
+        return
+    if args.workload == "batch":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference solves one "
+                          "problem per call; see --workload serve for its one-at-a-time rate"}))
         return
     tcd = args.workload == "tcd3d_p2_48"
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -1102,7 +1189,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--skip-cpu", action="store_true", help="omit the CPU-baseline sample")
     ap.add_argument("--workload", default="cd3d_q2_32",
-                    choices=["cd3d_q2_32", "tcd3d_p2_48", "cd2d_q1_64", "cd3d_q2_96", "serve"])
+                    choices=["cd3d_q2_32", "tcd3d_p2_48", "cd2d_q1_64", "cd3d_q2_96", "serve",
+                             "batch"])
     ap.add_argument("--profile", action="store_true",
                     help="run one bracketed step for an ncu capture and exit")
     ap.add_argument("--slots", type=int, default=0,
@@ -1122,6 +1210,8 @@ def main():
         run_gpu_tcd(args)
     elif args.workload == "serve":
         run_gpu_serve(args)
+    elif args.workload == "batch":
+        run_gpu_batch(args)
     else:
         run_gpu(args)
 

@@ -658,9 +658,10 @@ int cdg_solve_batched(cdg_context* ctx, int count, cdg_problem* const* probs,
   CDG_CUDA(cudaSetDevice(ctx->device));
   auto t0 = std::chrono::steady_clock::now();
   cudaEvent_t ev = nullptr;
+  std::vector<int> inl((size_t)std::max(count, 1), 0);
   for (int q = 0; q < count; ++q) {
     cdg_problem* p = probs[q];
-    CDG_TRY(batch_prepare(p->ctx, p, params[q]));
+    CDG_TRY(batch_prepare(p->ctx, p, params[q], &inl[q]));
     if (p->ctx->stream != ctx->stream) {
       if (!ev) CDG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
       CDG_CUDA(cudaEventRecord(ev, p->ctx->stream));
@@ -668,7 +669,7 @@ int cdg_solve_batched(cdg_context* ctx, int count, cdg_problem* const* probs,
     }
   }
   std::vector<BatchResult> res((size_t)std::max(count, 1));
-  int rc = batch_launch(ctx, probs, params, count, res.data());
+  int rc = batch_launch(ctx, probs, params, inl.data(), count, res.data());
   if (ev) cudaEventDestroy(ev);
   if (rc != CDG_OK) return rc;
   const double secs =

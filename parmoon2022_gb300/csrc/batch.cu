@@ -73,7 +73,14 @@ struct BJob {
   double* Z;
   double* w;
   double* H;
-  const double* cinv;   // coarsest level: dense inverse of the active block
+  double* cinv;         // coarsest level: dense inverse of the active block
+  const int* zero_diag; // the problem's zero-diagonal flag (set by its assembly)
+  // coarse block inverted by k_batch_coarse (cinline), from the coarsest
+  // level's FP64 CSR rows
+  int cinline, cna;
+  const int* c_rp;
+  const int* c_col;
+  const double* c_val;
 };
 
 // deterministic block sum (warp trees, then the warps' sums in order); every
@@ -277,9 +284,110 @@ __device__ void b_vcycle(const BJob& J, const double* v, double* z, float** sol,
   }
 }
 
-__global__ void __launch_bounds__(kBatchThreads)
-k_batch_solve(const BJob* __restrict__ jobs, BatchResult* __restrict__ out) {
+// The coarse direct solve's inverse of every small coarse block of the batch
+// (DirectSmoother, DirectSmoother.C:25-42; the dense block inverted as
+// k_gj_smem does: Gauss-Jordan with partial pivoting, the first row of
+// maximal |a_ik| as pivot, in shared memory, then the column exchanges in
+// reverse pivot order), one block per request; cstat[q] = kErrSingular on a
+// zero pivot
+constexpr int kCoarseThreads = 256;
+
+__global__ void __launch_bounds__(kCoarseThreads)
+k_batch_coarse(const BJob* __restrict__ jobs, int* __restrict__ cstat) {
   const BJob& J = jobs[blockIdx.x];
+  const int na = J.cna, tid = threadIdx.x, nt = kCoarseThreads;
+  if (tid == 0) cstat[blockIdx.x] = 0;
+  if (!J.cinline || na == 0) return;
+  extern __shared__ double s_gj[];
+  double* a = s_gj;                     // na * na
+  double* prow = a + (size_t)na * na;   // na
+  double* colk = prow + na;             // na
+  int* perm = (int*)(colk + na);        // na
+  int* q = perm + na;                   // na
+  __shared__ double wv[kCoarseThreads / 32];
+  __shared__ int wi[kCoarseThreads / 32];
+  __shared__ int s_p;
+  __shared__ double s_piv;
+  const int lane = tid & 31, w = tid >> 5;
+  for (int t = tid; t < na * na; t += nt) a[t] = 0.0;
+  __syncthreads();
+  for (int i = tid; i < na; i += nt)
+    for (int k = J.c_rp[i]; k < J.c_rp[i + 1]; ++k)
+      if (J.c_col[k] < na) a[(size_t)i * na + J.c_col[k]] = J.c_val[k];
+  __syncthreads();
+  for (int k = 0; k < na; ++k) {
+    double best = -1.0;
+    int bi = k;
+    for (int i = k + tid; i < na; i += nt) {
+      const double v = fabs(a[(size_t)i * na + k]);
+      if (v > best) { best = v; bi = i; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double v = __shfl_xor_sync(0xffffffffu, best, o);
+      const int vi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (v > best || (v == best && vi < bi)) { best = v; bi = vi; }
+    }
+    if (lane == 0) { wv[w] = best; wi[w] = bi; }
+    __syncthreads();
+    if (tid == 0) {
+      double b = wv[0];
+      int p = wi[0];
+      for (int u = 1; u < nt / 32; ++u)
+        if (wv[u] > b || (wv[u] == b && wi[u] < p)) { b = wv[u]; p = wi[u]; }
+      s_p = p;
+      s_piv = a[(size_t)p * na + k];
+      perm[k] = p;
+    }
+    __syncthreads();
+    const int p = s_p;
+    const double piv = s_piv;
+    if (piv == 0.0) {
+      if (tid == 0) cstat[blockIdx.x] = kErrSingular;
+      return;   // uniform: every thread read the same pivot
+    }
+    const double rpiv = 1.0 / piv;
+    for (int j = tid; j < na; j += nt) prow[j] = j == k ? rpiv : a[(size_t)p * na + j] * rpiv;
+    for (int i = tid; i < na; i += nt) colk[i] = a[(size_t)(i == p ? k : i) * na + k];
+    __syncthreads();
+    for (int t = tid; t < na * na; t += nt) {
+      const int i = t / na, j = t - i * na;
+      if (i == k) continue;
+      const double f = colk[i];
+      const double old = a[(size_t)(i == p ? k : i) * na + j];
+      a[t] = j == k ? -f * rpiv : fma(-f, prow[j], old);
+    }
+    __syncthreads();
+    for (int j = tid; j < na; j += nt) a[(size_t)k * na + j] = prow[j];
+    __syncthreads();
+  }
+  if (tid == 0) {
+    for (int j = 0; j < na; ++j) q[j] = j;
+    for (int k = na - 1; k >= 0; --k) {
+      const int t = q[k];
+      q[k] = q[perm[k]];
+      q[perm[k]] = t;
+    }
+  }
+  __syncthreads();
+  for (int t = tid; t < na * na; t += nt) {
+    const int i = t / na, j = t - (t / na) * na;
+    J.cinv[t] = a[(size_t)i * na + q[j]];
+  }
+}
+
+__global__ void __launch_bounds__(kBatchThreads)
+k_batch_solve(const BJob* __restrict__ jobs, const int* __restrict__ cstat,
+              BatchResult* __restrict__ out) {
+  const BJob& J = jobs[blockIdx.x];
+  // a zero diagonal found by the assembly (Iteration_jacobi.C:14-28 throws)
+  // or a singular coarse block: nothing to iterate
+  if (*J.zero_diag || cstat[blockIdx.x]) {
+    if (threadIdx.x == 0)
+      out[blockIdx.x] = BatchResult{*J.zero_diag ? CDG_ERR_ZERO_DIAG : CDG_ERR_SINGULAR, 0,
+                                    0.0, 0.0};
+    return;
+  }
   __shared__ double red[kBatchWarps];
   __shared__ double part[kBatchWarps][kBatchMaxRestart + 1];
   __shared__ double hcol[kBatchMaxRestart + 2], cs[kBatchMaxRestart + 1],
@@ -484,9 +592,10 @@ bool batch_eligible(const cdg_problem* p, const cdg_solver_params& s, const char
 }
 
 int batch_launch(cdg_context* ctx, cdg_problem* const* probs, const cdg_solver_params* params,
-                 int count, BatchResult* results) {
+                 const int* inline_coarse, int count, BatchResult* results) {
   if (count <= 0) return CDG_OK;
   std::vector<BJob> jobs(count);
+  int max_cna = 0;
   for (int q = 0; q < count; ++q) {
     cdg_problem* p = probs[q];
     const cdg_solver_params& s = params[q];
@@ -534,24 +643,48 @@ int batch_launch(cdg_context* ctx, cdg_problem* const* probs, const cdg_solver_p
     J.Z = p->gm.Z;
     J.w = p->gm.w;
     J.H = p->gm.H;
-    J.cinv = p->lev[J.nl - 1].coarse_inv;
+    const DevLevel& Cl = p->lev[J.nl - 1];
+    J.cinv = Cl.coarse_inv;
+    J.zero_diag = p->d_zero_diag;
+    J.cinline = inline_coarse[q];
+    J.cna = Cl.nactive;
+    J.c_rp = Cl.row_ptr;
+    J.c_col = Cl.col;
+    J.c_val = Cl.val64;
+    if (J.cinline) max_cna = std::max(max_cna, Cl.nactive);
   }
+  // descriptors, results, coarse status (16-byte aligned pieces)
   const size_t jb = (size_t)count * sizeof(BJob), rb = (size_t)count * sizeof(BatchResult);
-  if (ctx->batch_host_bytes < jb + rb) {
+  const size_t cb = ((size_t)count * sizeof(int) + 15) / 16 * 16;
+  if (ctx->batch_host_bytes < jb + rb + cb) {
     if (ctx->batch_host) cudaFreeHost(ctx->batch_host);
     if (ctx->batch_dev) cudaFree(ctx->batch_dev);
     ctx->batch_host = nullptr;
     ctx->batch_dev = nullptr;
     ctx->batch_host_bytes = 0;
-    CDG_CUDA(cudaMallocHost(&ctx->batch_host, jb + rb));
-    CDG_CUDA(cudaMalloc(&ctx->batch_dev, jb + rb));
-    ctx->batch_host_bytes = jb + rb;
+    CDG_CUDA(cudaMallocHost(&ctx->batch_host, jb + rb + cb));
+    CDG_CUDA(cudaMalloc(&ctx->batch_dev, jb + rb + cb));
+    ctx->batch_host_bytes = jb + rb + cb;
   }
   char* hb = (char*)ctx->batch_host;
   char* db = (char*)ctx->batch_dev;
   std::memcpy(hb, jobs.data(), jb);
   CDG_CUDA(cudaMemcpyAsync(db, hb, jb, cudaMemcpyHostToDevice, ctx->stream));
-  CDG_LAUNCH(ctx, k_batch_solve, count, kBatchThreads, 0, (const BJob*)db, (BatchResult*)(db + jb));
+  int* cstat = (int*)(db + jb + rb);
+  const size_t csm = (size_t)max_cna * max_cna * sizeof(double) +
+                     2 * (size_t)max_cna * sizeof(double) + 2 * (size_t)max_cna * sizeof(int);
+  static const bool attr_set = [] {
+    return cudaFuncSetAttribute(k_batch_coarse, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)((size_t)kBatchSmemCoarse * kBatchSmemCoarse * 8 +
+                                      4 * kBatchSmemCoarse * 8)) == cudaSuccess;
+  }();
+  if (!attr_set) {
+    set_error("shared memory of the batched coarse inverse");
+    return CDG_ERR_CUDA;
+  }
+  CDG_LAUNCH(ctx, k_batch_coarse, count, kCoarseThreads, csm, (const BJob*)db, cstat);
+  CDG_LAUNCH(ctx, k_batch_solve, count, kBatchThreads, 0, (const BJob*)db, (const int*)cstat,
+             (BatchResult*)(db + jb));
   CDG_CUDA(cudaMemcpyAsync(hb + jb, db + jb, rb, cudaMemcpyDeviceToHost, ctx->stream));
   CDG_CUDA(cudaStreamSynchronize(ctx->stream));
   std::memcpy(results, hb + jb, rb);

@@ -49,6 +49,7 @@ constexpr int kBatchMaxLevels = 12;
 constexpr int kBatchMaxRestart = 64;
 constexpr int kBatchMaxDofs = 20000;    // larger requests keep the stream-level solver
 constexpr int kBatchMaxCoarse = 2048;   // active DOFs of the coarsest level
+constexpr int kBatchSmemCoarse = 96;    // coarse blocks inverted inside the batch (shared memory)
 constexpr int kRedSlots = 32;         // partial-sum rows (one per inner product)
 constexpr int kRedMaxBlocks = 1024;   // partial sums per reduction
 
@@ -346,9 +347,11 @@ struct BatchResult {
 };
 bool batch_eligible(const cdg_problem* p, const cdg_solver_params& s, const char** why);
 int batch_launch(cdg_context* ctx, cdg_problem* const* probs, const cdg_solver_params* params,
-                 int count, BatchResult* results);
-// prepare_solver and the Krylov buffers of a problem (linalg.cu)
-int batch_prepare(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s);
+                 const int* inline_coarse, int count, BatchResult* results);
+// the buffers and coarse inverse a batched solve reads (linalg.cu);
+// *inline_coarse: the coarse block is inverted by the batch's coarse launch
+int batch_prepare(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s,
+                  int* inline_coarse);
 // tiles of the one-launch sweep of a uniform level (once per level)
 int mf_build_tiles(cdg_context* ctx, DevLevel& L);
 int mf_ensure(DevLevel& L);

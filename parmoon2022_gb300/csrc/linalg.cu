@@ -1716,9 +1716,35 @@ static int ensure_gmres(cdg_problem* p, int n, int m) {
   return CDG_OK;
 }
 
-int batch_prepare(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s) {
-  CDG_TRY(prepare_solver(ctx, p, s));
-  return ensure_gmres(p, p->lev[0].ndof, s.gmres_restart);
+// what the batched solver needs of a problem, without synchronising: FP64
+// values of the levels it reads in FP64 (finest, coarsest), FP32 multigrid
+// vectors, Krylov buffers, and the coarse inverse -- formed here only for a
+// coarse block above kBatchSmemCoarse rows (*inline_coarse = 0); smaller
+// ones are inverted by the batch's own coarse launch (the zero-diagonal test
+// then runs in the solve kernel, on the problem's flag)
+int batch_prepare(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s,
+                  int* inline_coarse) {
+  const int nl = s.multigrid_n_levels;
+  if (nl < 2 || nl > (int)p->lev.size()) {
+    set_error("multigrid_n_levels=%d but the problem has %d levels", nl, (int)p->lev.size());
+    return CDG_ERR_ARG;
+  }
+  CDG_TRY(ensure_fp64(ctx, p, p->lev[0]));
+  CDG_TRY(ensure_fp64(ctx, p, p->lev[nl - 1]));
+  for (int k = 0; k < nl; ++k) CDG_TRY(ensure_mg_vectors(ctx, p->lev[k], (int)sizeof(float)));
+  CDG_TRY(ensure_gmres(p, p->lev[0].ndof, s.gmres_restart));
+  DevLevel& C = p->lev[nl - 1];
+  const int na = C.nactive;
+  C.coarse_na = na;
+  if (na <= kBatchSmemCoarse) {
+    if (!C.coarse_inv && na > 0)
+      CDG_CUDA(cudaMalloc(&C.coarse_inv, (size_t)na * na * sizeof(double)));
+    *inline_coarse = 1;
+    return CDG_OK;
+  }
+  *inline_coarse = 0;
+  CDG_TRY(coarse_inverse(ctx, C));
+  return check_device_error(ctx);
 }
 
 struct LoopInfo {

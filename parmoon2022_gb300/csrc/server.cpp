@@ -92,6 +92,7 @@ struct Job {
   // the slot's stream
   Instance* inst = nullptr;
   cudaEvent_t ready = nullptr;
+  int inline_coarse = 0;   // coarse block inverted inside the batch
 };
 
 struct Slot {
@@ -250,7 +251,7 @@ int run_job(cdg_server* s, Slot* slot, Job* job, Instance* inst) {
   CDG_TRY(cdg_problem_set_solution(p, nullptr));
   CDG_TRY(cdg_problem_assemble(p, &job->req.a));
   if (s->batch && p->lev[0].ndof <= s->batch_max_dofs && batch_eligible(p, job->req.s, nullptr)) {
-    CDG_TRY(batch_prepare(slot->ctx, p, job->req.s));
+    CDG_TRY(batch_prepare(slot->ctx, p, job->req.s, &job->inline_coarse));
     if (!job->ready) CDG_CUDA(cudaEventCreateWithFlags(&job->ready, cudaEventDisableTiming));
     CDG_CUDA(cudaEventRecord(job->ready, slot->ctx->stream));
     job->inst = inst;
@@ -286,6 +287,7 @@ void batcher(cdg_server* s, int id) {
   std::vector<Job*> jobs;
   std::vector<cdg_problem*> probs;
   std::vector<cdg_solver_params> params;
+  std::vector<int> inl;
   std::vector<BatchResult> res;
   std::unique_lock<std::mutex> lk(s->mu);
   for (;;) {
@@ -297,14 +299,17 @@ void batcher(cdg_server* s, int id) {
     cudaStream_t st = bctx->stream;
     probs.clear();
     params.clear();
+    inl.clear();
     for (Job* j : jobs) {
       cudaStreamWaitEvent(st, j->ready, 0);
       probs.push_back(j->inst->p);
       params.push_back(j->req.s);
+      inl.push_back(j->inline_coarse);
     }
     res.assign(jobs.size(), BatchResult{CDG_OK, 0, 0.0, 0.0});
     const auto t0 = Clock::now();
-    int rc = batch_launch(bctx, probs.data(), params.data(), (int)jobs.size(), res.data());
+    int rc = batch_launch(bctx, probs.data(), params.data(), inl.data(), (int)jobs.size(),
+                          res.data());
     for (size_t q = 0; q < jobs.size() && rc == CDG_OK; ++q) {
       const DevLevel& F = jobs[q]->inst->p->lev[0];
       if (cudaMemcpyAsync(jobs[q]->out, F.sol, (size_t)F.ndof * sizeof(double),

@@ -122,3 +122,17 @@ def test_ineligible_requests_are_rejected(ctx):
         pg.solve_batched(ctx, [cd, cd], [params(q[3])] * 2)
     assert e.value.code == -1
     cd.close()
+
+
+def test_statuses_per_request(ctx):
+    # a zero diagonal (eps = b = c = 0: the reference's Jacobi throws "zero
+    # entry on the diagonal") ends that request with its status; the others
+    # in the launch still solve
+    good = make(ctx, REQS[0])
+    zero = pg.ConvectionDiffusion(ctx, pg.Hierarchy(2, 1, 4, n_levels=3))
+    zero.assemble(pg.assembly_params(example=pg.EX_CONST_F, eps=0.0))
+    out = pg.solve_batched(ctx, [good, zero], [params(3), params(3)])
+    assert out[0][0] == 0 and out[0][1].residual <= 1e-10 * out[0][1].initial_residual
+    assert out[1][0] == -6 and out[1][1].iterations == 0
+    good.close()
+    zero.close()
