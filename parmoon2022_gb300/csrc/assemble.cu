@@ -1749,6 +1749,14 @@ int upload_level(cdg_context* ctx, DevLevel& L) {
         }
       rp[r + 1] = (int)dcol.size();
     }
+    std::vector<int> rows;
+    for (int r = 0; r < L.nactive; ++r)
+      if (rp[r + 1] > rp[r]) rows.push_back(r);
+    L.dc_nrows = (int)rows.size();
+    CDG_TRY(dalloc(&L.dc_rows, std::max<size_t>(rows.size(), 1)));
+    if (!rows.empty())
+      CDG_CUDA(cudaMemcpyAsync(L.dc_rows, rows.data(), rows.size() * sizeof(int),
+                               cudaMemcpyHostToDevice, st));
     CDG_TRY(dalloc(&L.dc_rp, rp.size()));
     CDG_TRY(dalloc(&L.dc_col, dcol.size()));
     CDG_TRY(dalloc(&L.dc_pos, dpos.size()));
@@ -1936,7 +1944,7 @@ int free_level(DevLevel& L) {
                   L.tcd_A, L.tcd_M, L.tcd_f, L.tcd_fold, L.tcd_u2, L.dof_rp, L.dof_ent,
                   L.rhs_loc, L.mf_fac, L.mf_y, L.mf_ae, L.mf_gdof, L.mf_pos, L.mf_pos_c,
                   L.mf_tile_rp, L.mf_tile_gdof, L.mf_ent_loc,
-                  L.dc_val64, L.dc_val32};
+                  L.dc_val64, L.dc_val32, L.dc_rows};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   return CDG_OK;

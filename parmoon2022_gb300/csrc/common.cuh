@@ -135,6 +135,8 @@ struct DevLevel {
   double* dc_val64 = nullptr;    // their values (refreshed with the FP32 copy)
   float* dc_val32 = nullptr;
   int dc_n = 0;
+  int* dc_rows = nullptr;        // the active rows with couplings, increasing
+  int dc_nrows = 0;
   // multigrid work vectors (double or float, per precision)
   void* mg_rhs = nullptr;
   void* mg_sol = nullptr;

@@ -1199,24 +1199,48 @@ k_first_smooth(int n, int nactive, int with_dirichlet, const int* __restrict__ d
 // the finest level's first smoothing step fused with the cycle's start
 // (Iteration_multigrid::apply copies the Krylov vector into the multigrid
 // rhs): rhs = v in T, and x1 as k_first_smooth computes it from that rhs,
-// reading the Dirichlet neighbours' rhs straight from v
+// reading the Dirichlet neighbours' rhs straight from v.  Blocks below
+// row_blocks take a row per thread (rows without couplings to non-active
+// columns complete there); the others take the rows of dc_rows, 8 lanes per
+// row over its couplings (up to ~45 on a Q2 boundary layer, which one thread
+// walked in sequence while the rest of its warp waited)
+constexpr int kDcLanes = 8;
+
 template <typename T>
 __global__ void __launch_bounds__(256)
-k_first_smooth_init(int n, int nactive, const int* __restrict__ dc_rp,
-                    const int* __restrict__ dc_col, const T* __restrict__ dcv,
-                    const double* __restrict__ v, const T* __restrict__ invd, T w,
-                    T* __restrict__ rhs, T* __restrict__ x1, const int* di) {
+k_first_smooth_init(int n, int nactive, int row_blocks, int ndc, const int* __restrict__ dc_rows,
+                    const int* __restrict__ dc_rp, const int* __restrict__ dc_col,
+                    const T* __restrict__ dcv, const double* __restrict__ v,
+                    const T* __restrict__ invd, T w, T* __restrict__ rhs, T* __restrict__ x1,
+                    const int* di) {
   pdl_enter();
   if (di) v += (size_t)(*di) * n;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+  if ((int)blockIdx.x < row_blocks) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
     const T bi = (T)v[i];
     rhs[i] = bi;
     if (i < nactive) {
-      const T s = dirichlet_coupling(dc_rp[i], dc_rp[i + 1], dc_col, dcv, v);
-      x1[i] = w * (invd[i] * (bi - s));
+      if (dc_rp[i] == dc_rp[i + 1]) x1[i] = w * (invd[i] * (bi - (T)0));
     } else {
       x1[i] = bi + w * (invd[i] * (bi - bi));
     }
+    return;
+  }
+  const int g = ((int)blockIdx.x - row_blocks) * (blockDim.x / kDcLanes) + threadIdx.x / kDcLanes;
+  const int l = threadIdx.x % kDcLanes;
+  T s = 0;
+  int r = -1;
+  if (g < ndc) {
+    r = dc_rows[g];
+    const int k1 = dc_rp[r + 1];
+    for (int k = dc_rp[r] + l; k < k1; k += kDcLanes) s += dcv[k] * (T)v[dc_col[k]];
+  }
+#pragma unroll
+  for (int o = kDcLanes / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (r >= 0 && l == 0) {
+    const T bi = (T)v[r];
+    x1[r] = w * (invd[r] * (bi - s));
   }
 }
 
@@ -1304,8 +1328,10 @@ static int mg_cycle(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s
   // smoothing step also does the start (rhs = v, x0 = Dirichlet values)
   const bool fused_start = nl > 1 && s.multigrid_n_pre_smooth > 0;
   if (fused_start) {
-    CDG_LAUNCH_PDL(ctx, k_first_smooth_init<T>, vec_grid(ctx, F.ndof), 256, 0, F.ndof, F.nactive,
-               F.dc_rp, F.dc_col, Prec<T>::dcv(F), v, Prec<T>::invd(F),
+    const int rb = (F.ndof + 255) / 256;
+    const int db = (F.dc_nrows + 256 / kDcLanes - 1) / (256 / kDcLanes);
+    CDG_LAUNCH_PDL(ctx, k_first_smooth_init<T>, rb + db, 256, 0, F.ndof, F.nactive, rb,
+               F.dc_nrows, F.dc_rows, F.dc_rp, F.dc_col, Prec<T>::dcv(F), v, Prec<T>::invd(F),
                (T)s.jacobi_damp, (T*)F.mg_rhs, (T*)F.mg_tmp, di);
     std::swap(F.mg_sol, F.mg_tmp);
   } else {
