@@ -389,12 +389,13 @@ def run_gpu(args):
                            "ms_csr": t_csr, "ms_matrix_free": t_mf})
         if cd.tuning(0)[0] == 1:
             nc0 = info[0]["ncells"]
-            if cd.tuning_detail(0)[2][1] == -1:
+            if cd.tuning_detail(0)[2][1] < 0:
                 # one launch: gdof_c + entry slots, row ranges, x, b, D^-1, x'
                 # (the cells recomputed by neighbouring tiles hit L2)
                 mf_bytes = 2 * 27 * nc0 * 4 + 4 * (info[0]["nactive"] + 1) + 4 * 4 * n
-                mf_kernel = ("k_mf_fused<2> (one-launch matrix-free Jacobi step, finest "
-                             "level, one element matrix, 256-row tiles)")
+                mf_kernel = ("k_mf_fused<2,%d> (one-launch matrix-free Jacobi step, finest "
+                             "level, one element matrix, 256-row tiles)"
+                             % -cd.tuning_detail(0)[2][1])
             else:
                 # gdof_c + pos_c + results (written, read), row ranges, x, b, D^-1, x'
                 mf_bytes = 4 * 27 * nc0 * 4 + 4 * (info[0]["nactive"] + 1) + 4 * 4 * n

@@ -442,7 +442,8 @@ int cdg_problem_get_matrix32(cdg_problem *p, int level, float *v);
  * rows) and then CSR against matrix-free.  *choice: -2 not tuned
  * yet, -1 CSR (no matrix-free operator), 0 CSR, 1 matrix-free; shape (may be
  * NULL): [0] FP32 CSR lanes per row, [1] matrix-free blocks per SM (0: one
- * cell per warp, -1: the one-launch sweep); ms (may be NULL): the best CSR and the best matrix-free
+ * cell per warp; -4, -5, -6: the one-launch sweep compiled for that many
+ * resident blocks per SM); ms (may be NULL): the best CSR and the best matrix-free
  * step in milliseconds (0 where not timed).  CDG_TUNE=0 in the environment
  * keeps the untuned defaults; CDG_MATFREE, CDG_TPR32 and CDG_MF_CAP (one
  * value, or one per level from the finest, comma-separated) fix choices. */

@@ -182,6 +182,7 @@ struct DevLevel {
   // entry e of the DOF-major order reads its local result at mf_ent_loc[e]
   // (tile cell * kMfCellStride + local DOF) of the tile's shared memory
   int mf_ntiles = 0;
+  int mf_fused_minb = 4;         // resident blocks per SM the sweep is compiled for (4, 5, 6)
   int mf_tile_maxcells = 0;
   int* mf_tile_rp = nullptr;
   int* mf_tile_gdof = nullptr;

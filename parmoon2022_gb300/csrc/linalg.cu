@@ -1535,10 +1535,29 @@ static int tune_level(cdg_context* ctx, cdg_problem* p, DevLevel& L, int level) 
   if (rc == CDG_OK && L.mf_valid && mf_env != 0) {
     L.mf_mode = 1;
     if (L.mf_uniform && L.mf_ntiles > 0) {
-      // the one-launch sweep has one block per row tile: no grid to choose
-      // (reported as -1)
-      L.mf_blocks_per_sm = -1;
-      time_step(&L.tuned_ms[1]);
+      // the one-launch sweep has one block per row tile; its register budget
+      // (4, 5 or 6 resident blocks per SM) is timed, reported as -blocks
+      const int mb_env = env_level("CDG_MF_MINB", level);
+      if (mb_env >= 4 && mb_env <= 6) {
+        L.mf_fused_minb = mb_env;
+        time_step(&L.tuned_ms[1]);
+      } else {
+        float best = 1e30f;
+        int bm = 4;
+        for (int mb : {4, 5, 6}) {
+          L.mf_fused_minb = mb;
+          float ms = 0.f;
+          time_step(&ms);
+          if (rc != CDG_OK) break;
+          if (ms < best) {
+            best = ms;
+            bm = mb;
+          }
+        }
+        L.mf_fused_minb = bm;
+        L.tuned_ms[1] = best;
+      }
+      L.mf_blocks_per_sm = -L.mf_fused_minb;
     } else if (cap_env >= 0) {
       L.mf_blocks_per_sm = cap_env;
       time_step(&L.tuned_ms[1]);

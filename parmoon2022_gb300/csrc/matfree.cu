@@ -306,8 +306,8 @@ k_mf_gather(int n, int nactive, const int* __restrict__ dof_rp,
 // tile's rows need, grouped by row, cut the instructions by a quarter but
 // took 16.4 us: its 16-byte loads of different cells conflict in shared
 // memory where the warp-per-cell loads broadcast.)
-template <int MODE>
-__global__ void __launch_bounds__(kMfTileRows)
+template <int MODE, int MINB>
+__global__ void __launch_bounds__(kMfTileRows, MINB)
 k_mf_fused(int n, int nactive, const int* __restrict__ tile_rp,
            const int* __restrict__ tile_gdof, const float* __restrict__ AeT,
            const int* __restrict__ dof_rp, const int* __restrict__ ent_loc,
@@ -403,6 +403,35 @@ k_mf_fused(int n, int nactive, const int* __restrict__ tile_rp,
 
 }  // namespace
 
+// the sweep's register budget: 4, 5 or 6 resident blocks per SM (64, 48 or
+// 40 registers; the tuner times them, L.mf_fused_minb)
+template <int MINB>
+static int fused_smem_attr(int smem) {
+  CDG_CUDA(cudaFuncSetAttribute(k_mf_fused<0, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  CDG_CUDA(cudaFuncSetAttribute(k_mf_fused<1, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  CDG_CUDA(cudaFuncSetAttribute(k_mf_fused<2, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  CDG_CUDA(cudaFuncSetAttribute(k_mf_fused<3, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  return CDG_OK;
+}
+
+template <int MODE>
+static int fused_launch(cdg_context* ctx, const DevLevel& L, int g, size_t sm, const float* x,
+                        const float* b, const float* invd, float w, float* y, double* z,
+                        const int* di, double* zcur) {
+  switch (L.mf_fused_minb) {
+    case 5:
+      CDG_LAUNCH_PDL(ctx, (k_mf_fused<MODE, 5>), g, kMfTileRows, sm, L.ndof, L.nactive, L.mf_tile_rp, L.mf_tile_gdof, L.mf_ae, L.dof_rp, L.mf_ent_loc, x, b, invd, w, y, z, di, zcur);
+      break;
+    case 6:
+      CDG_LAUNCH_PDL(ctx, (k_mf_fused<MODE, 6>), g, kMfTileRows, sm, L.ndof, L.nactive, L.mf_tile_rp, L.mf_tile_gdof, L.mf_ae, L.dof_rp, L.mf_ent_loc, x, b, invd, w, y, z, di, zcur);
+      break;
+    default:
+      CDG_LAUNCH_PDL(ctx, (k_mf_fused<MODE, 4>), g, kMfTileRows, sm, L.ndof, L.nactive, L.mf_tile_rp, L.mf_tile_gdof, L.mf_ae, L.dof_rp, L.mf_ent_loc, x, b, invd, w, y, z, di, zcur);
+      break;
+  }
+  return CDG_OK;
+}
+
 // Tiles of the one-launch sweep, from the DOF-major positions of the cells'
 // local DOFs in cell 0's frame (mf_pos_c): tile t lists the cells that own an
 // entry of its active rows in first-use order (their DOFs padded to
@@ -481,10 +510,9 @@ int mf_build_tiles(cdg_context* ctx, DevLevel& L) {
                              cudaMemcpyHostToDevice, ctx->stream));
   CDG_CUDA(cudaStreamSynchronize(ctx->stream));   // host vectors go out of scope
   if (smem > 48 * 1024) {
-    CDG_CUDA(cudaFuncSetAttribute(k_mf_fused<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    CDG_CUDA(cudaFuncSetAttribute(k_mf_fused<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    CDG_CUDA(cudaFuncSetAttribute(k_mf_fused<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    CDG_CUDA(cudaFuncSetAttribute(k_mf_fused<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CDG_TRY(fused_smem_attr<4>((int)smem));
+    CDG_TRY(fused_smem_attr<5>((int)smem));
+    CDG_TRY(fused_smem_attr<6>((int)smem));
   }
   L.mf_tile_maxcells = maxc;
   L.mf_ntiles = ntiles;
@@ -517,12 +545,11 @@ int mf_apply(cdg_context* ctx, const DevLevel& L, int mode, const float* x, cons
     const int g = L.mf_ntiles;
     const size_t sm = (size_t)L.mf_tile_maxcells * kMfCellStride * sizeof(float);
     switch (mode) {
-      case 0: CDG_LAUNCH_PDL(ctx, k_mf_fused<0>, g, kMfTileRows, sm, L.ndof, L.nactive, L.mf_tile_rp, L.mf_tile_gdof, L.mf_ae, L.dof_rp, L.mf_ent_loc, x, b, invd, w, y, z, di, zcur); break;
-      case 1: CDG_LAUNCH_PDL(ctx, k_mf_fused<1>, g, kMfTileRows, sm, L.ndof, L.nactive, L.mf_tile_rp, L.mf_tile_gdof, L.mf_ae, L.dof_rp, L.mf_ent_loc, x, b, invd, w, y, z, di, zcur); break;
-      case 2: CDG_LAUNCH_PDL(ctx, k_mf_fused<2>, g, kMfTileRows, sm, L.ndof, L.nactive, L.mf_tile_rp, L.mf_tile_gdof, L.mf_ae, L.dof_rp, L.mf_ent_loc, x, b, invd, w, y, z, di, zcur); break;
-      default: CDG_LAUNCH_PDL(ctx, k_mf_fused<3>, g, kMfTileRows, sm, L.ndof, L.nactive, L.mf_tile_rp, L.mf_tile_gdof, L.mf_ae, L.dof_rp, L.mf_ent_loc, x, b, invd, w, y, z, di, zcur); break;
+      case 0: return fused_launch<0>(ctx, L, g, sm, x, b, invd, w, y, z, di, zcur);
+      case 1: return fused_launch<1>(ctx, L, g, sm, x, b, invd, w, y, z, di, zcur);
+      case 2: return fused_launch<2>(ctx, L, g, sm, x, b, invd, w, y, z, di, zcur);
+      default: return fused_launch<3>(ctx, L, g, sm, x, b, invd, w, y, z, di, zcur);
     }
-    return CDG_OK;
   }
   const int cblocks = (L.ncells + kMfWarps - 1) / kMfWarps;
   const int cap = ctx->num_sms * L.mf_blocks_per_sm;
