@@ -266,3 +266,20 @@ def test_errors_are_reported(ctx):
     gpu.assemble(pg.assembly_params(example=pg.EX_SINE, eps=1.0))
     st = gpu.solve(pg.solver_params("jacobi", residual_tolerance=0.0, residual_reduction=1e-8))
     assert st.residual < 1e-8 * st.initial_residual
+
+
+def test_assembly_reproducible_to_roundoff(ctx):
+    # the element scatter adds FP64 entries with atomics: two assemblies of
+    # the same problem agree to round-off (not necessarily bit for bit); the
+    # rhs is gathered in a fixed order and is bit-identical
+    h = pg.Hierarchy(3, 2, 3, n_levels=2)
+    a = pg.assembly_params(example=pg.EX_POLYEXP, eps=1e-3, b=(0.577, 0.577, 0.577),
+                           space_discretization_type="supg", sdfem_type=5, cell_measure=2)
+    m = []
+    for _ in range(2):
+        cd = pg.ConvectionDiffusion(ctx, h)
+        cd.assemble(a)
+        m.append((cd.matrix(0), cd.rhs(0)))
+        cd.close()
+    assert rel(m[0][0], m[1][0]) <= 1e-14
+    assert np.array_equal(m[0][1], m[1][1])
