@@ -769,10 +769,12 @@ def run_gpu_serve(args):
     clk = clocks.stop()
     c1 = srv.counters()
     srv.close()
-    # one-at-a-time FP64 (and mixed) on the same requests, back to back
-    base_q = serve_stream(200, SERVE["seed"] + 99)
-    # (each server first runs the same 200 requests untimed, so its pool
-    # holds the instances the timed pass needs: steady state, not setup)
+    # one-at-a-time FP64 (and mixed) on the same requests, back to back;
+    # 600 requests (~1.7 s one at a time) so that the concurrent pass's
+    # start and tail are a small part of it
+    base_q = serve_stream(600, SERVE["seed"] + 99)
+    # (each server first runs the same requests untimed, so its pool holds
+    # the instances the timed pass needs: steady state, not setup)
     one = {}
     # (per-launch batching off: every request on the slot's stream)
     os.environ["CDG_SERVER_BATCH"] = "0"
@@ -783,7 +785,7 @@ def run_gpu_serve(args):
         one[prec] = len(base_q) / wall
         s1.close()
     del os.environ["CDG_SERVER_BATCH"]
-    # saturated concurrent throughput on the same 200 requests
+    # saturated concurrent throughput on the same requests
     s8 = pg.Server(local, n_slots=SERVE["slots"])
     run_stream(pg, s8, base_q, [0.0] * len(base_q), "mixed")
     wall, _ = run_stream(pg, s8, base_q, [0.0] * len(base_q), "mixed")

@@ -12,6 +12,22 @@
 #include "common.cuh"
 
 namespace cdg {
+// the context's stream recreated at the device's highest priority (the
+// request server's small requests and batched launches: their short,
+// latency-bound kernels are scheduled ahead of large requests' blocks)
+int cdg_context_high_priority(cdg_context* c) {
+  if (!c) { set_error("null context"); return CDG_ERR_ARG; }
+  int least = 0, greatest = 0;
+  CDG_CUDA(cudaSetDevice(c->device));
+  CDG_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+  CDG_CUDA(cudaStreamSynchronize(c->stream));
+  cudaStream_t st = nullptr;
+  CDG_CUDA(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, greatest));
+  cudaStreamDestroy(c->stream);
+  c->stream = st;
+  return CDG_OK;
+}
+
 static thread_local char g_msg[512] = "";
 void set_error(const char* fmt, ...) {
   va_list ap;

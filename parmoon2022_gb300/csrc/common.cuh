@@ -342,6 +342,8 @@ int check_device_error(cdg_context* ctx);
 // matrix-free FP32 operator of Q2 hexahedral levels (matfree.cu); mode as
 // k_spmv: 0 y = Ax, 1 y = b - Ax, 2 Jacobi step, 3 Jacobi step + FP64 copy
 bool mf_eligible(const DevLevel& L);
+// a context's stream at the device's highest priority (api.cu)
+int cdg_context_high_priority(cdg_context* c);
 // batched solver (batch.cu): requests a launch can take (why: the reason
 // when not), and one launch over prepared problems on ctx's stream
 struct BatchResult {

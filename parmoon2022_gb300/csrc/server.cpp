@@ -46,6 +46,8 @@ namespace {
 using Clock = std::chrono::steady_clock;
 constexpr double kHeadPatience = 2.0;   // seconds before the queue head blocks others
 constexpr int kBatchers = 4;            // batched launches in flight
+constexpr int kServerPrioDofs = 20000;  // requests up to this size run on high-priority
+                                        // streams (CDG_SERVER_PRIORITY=0: none)
 // requests batched per launch up to this size (CDG_SERVER_BATCH_DOFS
 // overrides, at most the batched solver's kBatchMaxDofs).  Measured on GB300
 // (200 requests of the served mix, saturated, 8 slots): 597 solves/s without
@@ -98,6 +100,7 @@ struct Job {
 struct Slot {
   int id = 0;
   cdg_context* ctx = nullptr;
+  cdg_context* hi = nullptr;   // the same slot's high-priority stream (small requests)
   std::thread th;
 };
 
@@ -171,6 +174,7 @@ struct cdg_server {
   // whatever has been handed over when they are free (a long launch does not
   // hold back the next one)
   bool batch = true;
+  bool prio = true;
   int batch_max_dofs = kServerBatchDofs;
   std::vector<cdg_context*> bctx;
   std::vector<std::thread> batchers;
@@ -247,13 +251,16 @@ void destroy_instances(cdg_context* ctx, std::vector<Instance*>& v) {
 // here, < 0 an error
 int run_job(cdg_server* s, Slot* slot, Job* job, Instance* inst) {
   cdg_problem* p = inst->p;
-  p->ctx = slot->ctx;   // the problem's work goes to this slot's stream
+  // the problem's work goes to this slot's stream; small requests to its
+  // high-priority one
+  cdg_context* ctx = s->prio && p->lev[0].ndof <= kServerPrioDofs ? slot->hi : slot->ctx;
+  p->ctx = ctx;
   CDG_TRY(cdg_problem_set_solution(p, nullptr));
   CDG_TRY(cdg_problem_assemble(p, &job->req.a));
   if (s->batch && p->lev[0].ndof <= s->batch_max_dofs && batch_eligible(p, job->req.s, nullptr)) {
-    CDG_TRY(batch_prepare(slot->ctx, p, job->req.s, &job->inline_coarse));
+    CDG_TRY(batch_prepare(ctx, p, job->req.s, &job->inline_coarse));
     if (!job->ready) CDG_CUDA(cudaEventCreateWithFlags(&job->ready, cudaEventDisableTiming));
-    CDG_CUDA(cudaEventRecord(job->ready, slot->ctx->stream));
+    CDG_CUDA(cudaEventRecord(job->ready, ctx->stream));
     job->inst = inst;
     return 1;
   }
@@ -497,13 +504,19 @@ int cdg_server_create(int device, int n_slots, long long budget, cdg_server** ou
     const char* e = getenv("CDG_SERVER_BATCH");
     s->batch = !(e && e[0] == '0');
   }
+  {
+    const char* e = getenv("CDG_SERVER_PRIORITY");
+    s->prio = !(e && e[0] == '0');
+  }
   if (s->batch) {
     const char* e = getenv("CDG_SERVER_BATCH_DOFS");
     if (e) s->batch_max_dofs = std::min(atoi(e), kBatchMaxDofs);
     for (int i = 0; i < kBatchers; ++i) {
       cdg_context* c = nullptr;
-      const int rc = cdg_context_create(device, &c);
+      int rc = cdg_context_create(device, &c);
+      if (rc == CDG_OK && s->prio) rc = cdg_context_high_priority(c);
       if (rc != CDG_OK) {
+        if (c) cdg_context_destroy(c);
         for (cdg_context* x : s->bctx) cdg_context_destroy(x);
         return rc;
       }
@@ -514,8 +527,15 @@ int cdg_server_create(int device, int n_slots, long long budget, cdg_server** ou
     std::unique_ptr<Slot> sl(new Slot());
     sl->id = i;
     int rc = cdg_context_create(device, &sl->ctx);
+    if (rc == CDG_OK) rc = cdg_context_create(device, &sl->hi);
+    if (rc == CDG_OK && s->prio) rc = cdg_context_high_priority(sl->hi);
     if (rc != CDG_OK) {
-      for (auto& x : s->slots) cdg_context_destroy(x->ctx);
+      if (sl->ctx) cdg_context_destroy(sl->ctx);
+      if (sl->hi) cdg_context_destroy(sl->hi);
+      for (auto& x : s->slots) {
+        cdg_context_destroy(x->ctx);
+        cdg_context_destroy(x->hi);
+      }
       for (cdg_context* x : s->bctx) cdg_context_destroy(x);
       return rc;
     }
@@ -548,7 +568,10 @@ int cdg_server_destroy(cdg_server* s) {
   }
   for (auto& kv : s->classes)
     if (kv.second->h) cdg_hierarchy_destroy(kv.second->h);
-  for (auto& sl : s->slots) cdg_context_destroy(sl->ctx);
+  for (auto& sl : s->slots) {
+    cdg_context_destroy(sl->ctx);
+    cdg_context_destroy(sl->hi);
+  }
   for (cdg_context* x : s->bctx) cdg_context_destroy(x);
   for (auto& kv : s->jobs)
     if (kv.second->ready) cudaEventDestroy(kv.second->ready);
@@ -615,7 +638,8 @@ int cdg_server_counters(cdg_server* s, long long* c) {
   c[8] = s->budget;
   c[9] = s->peak_running;
   long long launches = 0;
-  for (auto& sl : s->slots) launches += cdg_context_launch_count(sl->ctx);
+  for (auto& sl : s->slots)
+    launches += cdg_context_launch_count(sl->ctx) + cdg_context_launch_count(sl->hi);
   for (cdg_context* x : s->bctx) launches += cdg_context_launch_count(x);
   c[10] = launches;
   c[11] = (long long)s->classes.size();
