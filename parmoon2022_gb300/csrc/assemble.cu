@@ -752,20 +752,21 @@ __global__ void k_mf_pos(int nactive, const int* __restrict__ dof_rp,
 __global__ void k_mf_canon(int ncells, const double* __restrict__ verts,
                            const int* __restrict__ gdof, const int* __restrict__ pos,
                            int* __restrict__ gdof_c, int* __restrict__ pos_c,
-                           int* __restrict__ nonuniform) {
+                           int* __restrict__ loc_c, int* __restrict__ nonuniform) {
   const int cell = blockIdx.x * blockDim.x + threadIdx.x;
   if (cell >= ncells) return;
   Affine A0, Ac;
   cell_affine(3, verts, A0);
   cell_affine(3, verts + (size_t)cell * 8 * 3, Ac);
   int R[3][3];
-  bool ok = true;
+  bool ok = true, exact = true;
   for (int a = 0; a < 3; ++a)
     for (int b = 0; b < 3; ++b) {
       double r = 0.0;
       for (int q = 0; q < 3; ++q) r += A0.Ji[a][q] * Ac.J[q][b];
       const double ri = rint(r);
       if (fabs(r - ri) > 1e-9 || fabs(ri) > 1.0) ok = false;
+      if (fabs(r - ri) > 1e-13) exact = false;
       R[a][b] = (int)ri;
     }
   for (int a = 0; a < 3 && ok; ++a) {
@@ -787,8 +788,47 @@ __global__ void k_mf_canon(int ncells, const double* __restrict__ verts,
     }
     gdof_c[o + m] = gdof[o + k];
     pos_c[o + m] = pos[o + k];
+    loc_c[o + m] = k;
   }
-  if (!ok) atomicOr(nonuniform, 1);
+  // bit 0: not translates within 1e-9 (the FP32 operator's test); bit 1: not
+  // within 1e-13 (the FP64 matrix from one element matrix must equal the
+  // per-cell contraction to round-off)
+  if (!ok) atomicOr(nonuniform, 3);
+  else if (!exact) atomicOr(nonuniform, 2);
+}
+
+// A uniform level's FP64 matrix: every cell's element matrix is cell 0's
+// (Ae = sum_t g_t R_t of cell 0, in its local order) with the cell's local
+// DOFs listed in cell 0's frame, so one FP64 element matrix is formed and
+// scattered into the CSR values through the slot map (entry (i, j) of cell 0's
+// frame goes to the cell's local pair (loc_c[i], loc_c[j])), in place of
+// ~22k FP64 multiply-adds per cell in the contraction; rows of non-active
+// DOFs are skipped as in the contraction
+__global__ void k_uniform_element64(AsmCoefs k, const double* __restrict__ verts,
+                                    const double* __restrict__ R, double* __restrict__ Ae) {
+  __shared__ double g0[Terms<3>::NT];
+  if (threadIdx.x == 0) cell_factors<3>(k, verts, g0, 0);
+  __syncthreads();
+  // the factors outside the operator's term set are zero (no SUPG: delta
+  // terms; constant b: the linear-convection block)
+  for (int e = threadIdx.x; e < 27 * 27; e += blockDim.x) {
+    double a = 0.0;
+    for (int t = 0; t < Terms<3>::NT; ++t) a += g0[t] * R[(size_t)t * 729 + e];
+    Ae[e] = a;
+  }
+}
+
+__global__ void __launch_bounds__(256)
+k_uniform_scatter(long n, int nactive, const int* __restrict__ gdof, const int* __restrict__ slot,
+                  const int* __restrict__ loc_c, const double* __restrict__ Ae,
+                  double* __restrict__ val) {
+  for (long t = blockIdx.x * 256L + threadIdx.x; t < n; t += (long)gridDim.x * 256) {
+    const long cell = t / 729;
+    const int e = (int)(t - cell * 729), i = e / 27, j = e - i * 27;
+    const int li = __ldg(loc_c + cell * 27 + i), lj = __ldg(loc_c + cell * 27 + j);
+    if (__ldg(gdof + cell * 27 + li) >= nactive) continue;
+    atomicAdd(val + __ldg(slot + cell * 729 + li * 27 + lj), __ldg(Ae + e));
+  }
 }
 
 // element matrix of cell 0 in FP32, transposed (AeT[j*27 + i] = A_ij): the
@@ -1943,7 +1983,7 @@ int free_level(DevLevel& L) {
                   L.R_val32, L.coarse_inv, L.coarse_work, L.dc_rp, L.dc_col, L.dc_pos,
                   L.tcd_A, L.tcd_M, L.tcd_f, L.tcd_fold, L.tcd_u2, L.dof_rp, L.dof_ent,
                   L.rhs_loc, L.mf_fac, L.mf_y, L.mf_ae, L.mf_gdof, L.mf_pos, L.mf_pos_c,
-                  L.mf_tile_rp, L.mf_tile_gdof, L.mf_ent_loc,
+                  L.mf_tile_rp, L.mf_tile_gdof, L.mf_ent_loc, L.mf_loc, L.ue64,
                   L.dc_val64, L.dc_val32, L.dc_rows};
   for (void* q : ptrs)
     if (q) cudaFree(q);
@@ -2375,33 +2415,51 @@ static int finish_matrix(cdg_context* ctx, cdg_problem* p, DevLevel& L) {
 
 // the matrix-free FP32 operator takes the same factors (the SUPG term set
 // has no linear-convection terms, so that combination keeps the CSR path)
-static int mf_prepare(cdg_context* ctx, cdg_problem* p, DevLevel& L, const AsmCoefs& k) {
+// once per Q2 hexahedral level: the DOF-major positions of the cells' local
+// DOFs and the cells' frames relative to cell 0 (L.mf_geo = 1: every cell a
+// translate of cell 0 once its DOFs are listed in cell 0's frame)
+static int mf_geometry(cdg_context* ctx, DevLevel& L) {
+  if (L.mf_geo >= 0) return CDG_OK;
   cudaStream_t st = ctx->stream;
+  CDG_TRY(mf_ensure(L));
+  CDG_CUDA(cudaMemsetAsync(L.mf_pos, 0xff, (size_t)L.ncells * 27 * sizeof(int), st));
+  CDG_LAUNCH(ctx, k_mf_pos, grid_for<int>(L.nactive, 256), 256, 0, L.nactive, L.dof_rp,
+             L.dof_ent, L.mf_pos);
+  int* flag = nullptr;
+  CDG_CUDA(cudaMalloc(&flag, sizeof(int)));
+  int nonuni = 1;
+  cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int), st);
+  if (e == cudaSuccess) {
+    k_mf_canon<<<grid_for<int>(L.ncells, 128), 128, 0, st>>>(
+        L.ncells, L.verts, L.gdof, L.mf_pos, L.mf_gdof, L.mf_pos_c, L.mf_loc, flag);
+    ++ctx->launches;
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&nonuni, flag, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(flag);
+  CDG_CUDA(e);
+  L.mf_geo = (nonuni & 1) ? 0 : 1;
+  L.mf_geo_exact = nonuni == 0 ? 1 : 0;
+  if (L.mf_geo == 1) CDG_TRY(mf_build_tiles(ctx, L));
+  return CDG_OK;
+}
+
+// the FP64 operator of a uniform level (every cell a translate of cell 0,
+// constant coefficients): one element matrix scattered (CDG_UNIFORM_FP64=0
+// keeps the per-cell contraction); false when the level does not qualify
+static bool uniform_fp64(const DevLevel& L, const AsmCoefs& k) {
+  const char* e = std::getenv("CDG_UNIFORM_FP64");
+  const bool off = e && e[0] == '0';
+  return !off && mf_eligible(L) && L.mf_geo_exact == 1 && !k.linear_b;
+}
+
+// the matrix-free FP32 operator takes the same factors (the SUPG term set
+// has no linear-convection terms, so that combination keeps the CSR path)
+static int mf_prepare(cdg_context* ctx, cdg_problem* p, DevLevel& L, const AsmCoefs& k) {
   L.mf_valid = 0;
   if (mf_eligible(L) && L.mf_mode != 0 && !(k.supg && k.linear_b)) {
-    CDG_TRY(mf_ensure(L));
-    if (L.mf_geo < 0) {
-      // once per level: gather positions, and the cells' frames relative to cell 0
-      CDG_CUDA(cudaMemsetAsync(L.mf_pos, 0xff, (size_t)L.ncells * 27 * sizeof(int), st));
-      CDG_LAUNCH(ctx, k_mf_pos, grid_for<int>(L.nactive, 256), 256, 0, L.nactive, L.dof_rp,
-                 L.dof_ent, L.mf_pos);
-      int* flag = nullptr;
-      CDG_CUDA(cudaMalloc(&flag, sizeof(int)));
-      int nonuni = 1;
-      cudaError_t e = cudaMemsetAsync(flag, 0, sizeof(int), st);
-      if (e == cudaSuccess) {
-        k_mf_canon<<<grid_for<int>(L.ncells, 128), 128, 0, st>>>(
-            L.ncells, L.verts, L.gdof, L.mf_pos, L.mf_gdof, L.mf_pos_c, flag);
-        ++ctx->launches;
-        e = cudaGetLastError();
-      }
-      if (e == cudaSuccess) e = cudaMemcpyAsync(&nonuni, flag, sizeof(int), cudaMemcpyDeviceToHost, st);
-      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-      cudaFree(flag);
-      CDG_CUDA(e);
-      L.mf_geo = nonuni ? 0 : 1;
-      if (L.mf_geo == 1) CDG_TRY(mf_build_tiles(ctx, L));
-    }
+    CDG_TRY(mf_geometry(ctx, L));
     // constant coefficients on translated cells: one element matrix;
     // otherwise per-cell factors for the sum-factorised kernel
     L.mf_uniform = L.mf_geo == 1 && !k.linear_b ? 1 : 0;
@@ -2430,7 +2488,15 @@ int assemble_level(cdg_context* ctx, cdg_problem* p, DevLevel& L, const cdg_asse
   // block->reset(), rhs.reset()
   CDG_CUDA(cudaMemsetAsync(L.val64, 0, (size_t)L.nnz * sizeof(double), st));
   CDG_CUDA(cudaMemsetAsync(L.rhs, 0, (size_t)L.ndof * sizeof(double), st));
-  CDG_TRY(contract(ctx, k, L, p->d_tables, stiffness_set(k), false, L.val64));
+  if (mf_eligible(L)) CDG_TRY(mf_geometry(ctx, L));
+  if (uniform_fp64(L, k)) {
+    CDG_LAUNCH(ctx, k_uniform_element64, 1, 256, 0, k, L.verts, p->d_tables, L.ue64);
+    const long n = (long)L.ncells * 729;
+    CDG_LAUNCH(ctx, k_uniform_scatter, (int)std::min<long>((n + 255) / 256, (long)ctx->num_sms * 32),
+               256, 0, n, L.nactive, L.gdof, L.slot, L.mf_loc, L.ue64, L.val64);
+  } else {
+    CDG_TRY(contract(ctx, k, L, p->d_tables, stiffness_set(k), false, L.val64));
+  }
   CDG_TRY(mf_prepare(ctx, p, L, k));
   int nd = L.ndof - L.nactive;
   if (nd > 0)

@@ -172,7 +172,10 @@ struct DevLevel {
   int* mf_pos = nullptr;         // cells x 27: position of (cell, local DOF) in mf_y, -1 non-active
   int* mf_gdof = nullptr;        // cells x 27: DOFs in cell 0's local order
   int* mf_pos_c = nullptr;       // cells x 27: mf_pos in cell 0's local order
+  int* mf_loc = nullptr;         // cells x 27: the cell's local index of cell 0's index i
+  double* ue64 = nullptr;        // 27 x 27 FP64 element matrix of a uniform level
   int mf_geo = -1;               // every cell a translate of cell 0 (-1: not checked)
+  int mf_geo_exact = 0;          // ... to 1e-13 (the FP64 matrix from one element matrix)
   int mf_uniform = 0;            // the last assembly has one element matrix for all cells
   int mf_blocks_per_sm = 0;      // grid cap of the cell kernel (0: one cell per warp)
   // one-launch sweep of a uniform level (k_mf_fused): rows cut into tiles of

@@ -531,6 +531,8 @@ int mf_ensure(DevLevel& L) {
   CDG_CUDA(cudaMalloc(&L.mf_pos, (size_t)L.ncells * 27 * sizeof(int)));
   CDG_CUDA(cudaMalloc(&L.mf_gdof, (size_t)L.ncells * 27 * sizeof(int)));
   CDG_CUDA(cudaMalloc(&L.mf_pos_c, (size_t)L.ncells * 27 * sizeof(int)));
+  CDG_CUDA(cudaMalloc(&L.mf_loc, (size_t)L.ncells * 27 * sizeof(int)));
+  CDG_CUDA(cudaMalloc(&L.ue64, 27 * 27 * sizeof(double)));
   return CDG_OK;
 }
 

@@ -279,3 +279,23 @@ def test_one_launch_sweep_in_solves(ctx, monkeypatch):
     assert out[0][2][2][1] in (-4, -5, -6) and out[1][2][2][1] >= 0
     assert abs(out[0][0] - out[1][0]) <= 1
     assert rel(out[0][1], out[1][1]) < 1e-10
+
+
+@pytest.mark.parametrize("name", ["supg_polyexp", "supg_sine_sdfem2", "galerkin_sine"])
+def test_uniform_fp64_matrix_equals_the_contraction(ctx, monkeypatch, name):
+    # on a uniform level the FP64 matrix is one element matrix scattered
+    # through the cells' frames; it equals the per-cell contraction
+    # (CDG_UNIFORM_FP64=0) to round-off and the oracle to 1e-12
+    nref, levels, kw = CASES[name]
+    o = po.Problem(oracle_cfg(nref, kw), levels)
+    o.assemble()
+    mats = []
+    for flag in ("1", "0"):
+        monkeypatch.setenv("CDG_UNIFORM_FP64", flag)
+        gpu = pg.ConvectionDiffusion(ctx, pg.Hierarchy(3, 2, nref, n_levels=levels))
+        gpu.assemble(gpu_params(kw))
+        mats.append([gpu.matrix(l) for l in range(levels)])
+        gpu.close()
+    for l in range(levels):
+        assert rel(mats[0][l], mats[1][l]) < 1e-14
+        assert rel(mats[0][l], o.matrix(l)) < 1e-12
