@@ -136,3 +136,23 @@ def test_statuses_per_request(ctx):
     assert out[1][0] == -6 and out[1][1].iterations == 0
     good.close()
     zero.close()
+
+
+def test_batched_tetrahedra(ctx):
+    # the batched solver is element-agnostic (CSR levels, transfers, coarse
+    # inverse): P2 tetrahedra with moved vertices against the stream solver
+    a = pg.assembly_params(example=pg.EX_SINE, eps=0.1, b=(1.0, 0.3, -0.2), c=1.0)
+    h = pg.Hierarchy(3, 2, 2, n_levels=2, tetra=True, perturb=0.15, seed=4)
+    s = params(2)
+    cd = pg.ConvectionDiffusion(ctx, h)
+    cd.assemble(a)
+    st = cd.solve(s)
+    x0 = cd.solution()
+    cd.close()
+    cd = pg.ConvectionDiffusion(ctx, h)
+    cd.assemble(a)
+    (status, sb), = pg.solve_batched(ctx, [cd], [s])
+    assert status == 0 and sb.residual <= 1e-10 * sb.initial_residual
+    assert abs(sb.iterations - st.iterations) <= 1
+    assert rel(cd.solution(), x0) < 1e-8
+    cd.close()
