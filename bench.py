@@ -389,7 +389,14 @@ def run_gpu(args):
                            "ms_csr": t_csr, "ms_matrix_free": t_mf})
         if cd.tuning(0)[0] == 1:
             nc0 = info[0]["ncells"]
-            if cd.tuning_detail(0)[2][1] < 0:
+            if cd.tuning_detail(0)[2][1] <= -100:
+                # stencil sweep: lattice map, x, b, D^-1, x' (the halo's
+                # re-reads of map and x hit L2); the eight stencils are 3 KB
+                zt = -100 - cd.tuning_detail(0)[2][1]
+                mf_bytes = 4 * n + 4 * 4 * n
+                mf_kernel = ("k_mf_stencil<2,%d> (lattice stencil Jacobi step, finest level, "
+                             "eight 125-point stencils from one element matrix)" % zt)
+            elif cd.tuning_detail(0)[2][1] < 0:
                 # one launch: gdof_c + entry slots, row ranges, x, b, D^-1, x'
                 # (the cells recomputed by neighbouring tiles hit L2)
                 mf_bytes = 2 * 27 * nc0 * 4 + 4 * (info[0]["nactive"] + 1) + 4 * 4 * n
@@ -405,7 +412,10 @@ def run_gpu(args):
                         "bound": "latency (dependent L2 gathers); neither FP32 issue nor HBM",
                         "ms": ms_smooth, "bytes": mf_bytes,
                         "achieved_gbs": mf_bytes / (ms_smooth * 1e-3) / 1e9,
-                        "fp32_gflop": 2 * 729 * nc0 / 1e9,
+                        # multiply-adds formed: 729 per cell (tiles), or
+                        # 25 (dx, dy) x 3 or 5 dz per lattice point (stencil)
+                        "fp32_gflop": (2 * 100 * info[0]["nactive"] if "stencil" in mf_kernel
+                                       else 2 * 729 * nc0) / 1e9,
                         "csr_step_ms": cd.tuning(0)[1][0], "csr_bytes": bytes_smooth}
         else:
             smoother = {"kernel": "k_spmv<float,8,8,2> (CSR Jacobi step, finest level)",

@@ -415,8 +415,11 @@ int cdg_problem_assemble_coefficients(cdg_problem *p, const cdg_assembly_params 
  * the element matrices applied from per-cell factors or, on uniform levels,
  * from one shared element matrix in one launch per product); 2: the
  * matrix-free product as two launches (cell products, then the row sums),
- * which the one-launch form equals bit for bit.  Parity access for the
- * multigrid kernels. */
+ * which the one-launch form equals bit for bit; 3: the lattice stencil
+ * sweep (uniform Q2 levels whose DOFs fill a lattice with Dirichlet data on
+ * the whole boundary: each active row one of eight 125-point stencils summed
+ * from the element matrix; CDG_ERR_ARG on other levels).  Parity access for
+ * the multigrid kernels. */
 int cdg_problem_apply32(cdg_problem *p, int level, int variant, const float *x,
                         float *y);
 /* Operators used only in FP32 on tensor cores (no counterpart in the
@@ -439,14 +442,18 @@ int cdg_problem_get_matrix32(cdg_problem *p, int level, float *v);
  * step of each candidate (CUDA events): CSR lanes per row 2/4/8/16, and on Q2
  * hexahedra with a matrix-free operator its grid (one cell per warp, or 4 / 8
  * blocks per SM; uniform levels sweep in one launch of one block per 256
- * rows) and then CSR against matrix-free.  *choice: -2 not tuned
+ * rows, or, on a lattice with Dirichlet data on the whole boundary, by the
+ * stencil sweep with 4 or 8 lattice points per thread) and then CSR against
+ * matrix-free.  *choice: -2 not tuned
  * yet, -1 CSR (no matrix-free operator), 0 CSR, 1 matrix-free; shape (may be
  * NULL): [0] FP32 CSR lanes per row, [1] matrix-free blocks per SM (0: one
  * cell per warp; -4, -5, -6: the one-launch sweep compiled for that many
- * resident blocks per SM); ms (may be NULL): the best CSR and the best matrix-free
+ * resident blocks per SM; -104, -108: the stencil sweep with 4 or 8 points
+ * per thread); ms (may be NULL): the best CSR and the best matrix-free
  * step in milliseconds (0 where not timed).  CDG_TUNE=0 in the environment
- * keeps the untuned defaults; CDG_MATFREE, CDG_TPR32 and CDG_MF_CAP (one
- * value, or one per level from the finest, comma-separated) fix choices. */
+ * keeps the untuned defaults; CDG_MATFREE, CDG_TPR32, CDG_MF_CAP, CDG_MF_MINB
+ * and CDG_MF_STENCIL (0: no stencil sweep, 4 or 8: that sweep; one value, or
+ * one per level from the finest, comma-separated) fix choices. */
 int cdg_problem_tuning(cdg_problem *p, int level, int *choice, int *shape, double *ms);
 /* one preconditioner application z = M^-1 v (Iteration_multigrid::apply or
  * Iteration_jacobi::apply) */

@@ -665,7 +665,9 @@ class ConvectionDiffusion:
     def apply32(self, x, level=0, variant=0):
         """y = A x with the FP32 multigrid operator of a level: variant 0 the
         CSR kernel, 1 the matrix-free kernel (Q2 hexahedra; one launch on
-        uniform levels), 2 the two-launch matrix-free product."""
+        uniform levels), 2 the two-launch matrix-free product, 3 the lattice
+        stencil sweep (uniform Q2 lattices with Dirichlet data on the whole
+        boundary)."""
         x = np.ascontiguousarray(x, dtype=np.float32)
         y = np.zeros_like(x)
         fp = ctypes.POINTER(ctypes.c_float)

@@ -943,7 +943,7 @@ int cdg_problem_tuning(cdg_problem* p, int level, int* choice, int* shape, doubl
 
 int cdg_problem_apply32(cdg_problem* p, int level, int variant, const float* x, float* y) {
   DevLevel* L = get_level(p, level);
-  if (!L || !x || !y || variant < 0 || variant > 2) { set_error("bad arguments"); return CDG_ERR_ARG; }
+  if (!L || !x || !y || variant < 0 || variant > 3) { set_error("bad arguments"); return CDG_ERR_ARG; }
   if (variant >= 1 && !L->mf_valid) {
     set_error("no matrix-free operator on level %d (Q2 hexahedra after a stationary assembly)",
               level);

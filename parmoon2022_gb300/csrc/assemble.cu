@@ -1984,7 +1984,7 @@ int free_level(DevLevel& L) {
                   L.tcd_A, L.tcd_M, L.tcd_f, L.tcd_fold, L.tcd_u2, L.dof_rp, L.dof_ent,
                   L.rhs_loc, L.mf_fac, L.mf_y, L.mf_ae, L.mf_gdof, L.mf_pos, L.mf_pos_c,
                   L.mf_tile_rp, L.mf_tile_gdof, L.mf_ent_loc, L.mf_loc, L.ue64,
-                  L.dc_val64, L.dc_val32, L.dc_rows};
+                  L.dc_val64, L.dc_val32, L.dc_rows, L.st_map, L.st_coef};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   return CDG_OK;
@@ -2413,11 +2413,10 @@ static int finish_matrix(cdg_context* ctx, cdg_problem* p, DevLevel& L) {
   return CDG_OK;
 }
 
-// the matrix-free FP32 operator takes the same factors (the SUPG term set
-// has no linear-convection terms, so that combination keeps the CSR path)
 // once per Q2 hexahedral level: the DOF-major positions of the cells' local
 // DOFs and the cells' frames relative to cell 0 (L.mf_geo = 1: every cell a
-// translate of cell 0 once its DOFs are listed in cell 0's frame)
+// translate of cell 0 once its DOFs are listed in cell 0's frame); on such
+// levels the one-launch sweep's tiles and the DOF lattice of the stencil sweep
 static int mf_geometry(cdg_context* ctx, DevLevel& L) {
   if (L.mf_geo >= 0) return CDG_OK;
   cudaStream_t st = ctx->stream;
@@ -2441,7 +2440,10 @@ static int mf_geometry(cdg_context* ctx, DevLevel& L) {
   CDG_CUDA(e);
   L.mf_geo = (nonuni & 1) ? 0 : 1;
   L.mf_geo_exact = nonuni == 0 ? 1 : 0;
-  if (L.mf_geo == 1) CDG_TRY(mf_build_tiles(ctx, L));
+  if (L.mf_geo == 1) {
+    CDG_TRY(mf_build_tiles(ctx, L));
+    CDG_TRY(mf_build_lattice(ctx, L));
+  }
   return CDG_OK;
 }
 
@@ -2463,9 +2465,10 @@ static int mf_prepare(cdg_context* ctx, cdg_problem* p, DevLevel& L, const AsmCo
     // constant coefficients on translated cells: one element matrix;
     // otherwise per-cell factors for the sum-factorised kernel
     L.mf_uniform = L.mf_geo == 1 && !k.linear_b ? 1 : 0;
-    if (L.mf_uniform)
+    if (L.mf_uniform) {
       CDG_LAUNCH(ctx, k_mf_element, 1, 256, 0, k, L.verts, p->d_tables, L.mf_ae);
-    else
+      CDG_TRY(mf_stencil_coef(ctx, L));
+    } else
       CDG_LAUNCH(ctx, k_mf_factors, grid_for<int>(L.ncells, 128), 128, 0, k, L.ncells, L.verts,
                  L.mf_fac);
     L.mf_valid = 1;

@@ -190,6 +190,17 @@ struct DevLevel {
   int* mf_tile_rp = nullptr;
   int* mf_tile_gdof = nullptr;
   int* mf_ent_loc = nullptr;
+  // lattice stencil sweep of a uniform level (k_mf_stencil): the DOFs sit on
+  // the points of an st_dims[0] x st_dims[1] x st_dims[2] lattice in cell 0's
+  // axes (st_map: lattice point, x fastest -> DOF), every active DOF is an
+  // interior point, so each active row is one of eight 125-point stencils
+  // (by the parities of its point); st_coef holds them (kStCoef floats,
+  // formed from the element matrix at each assembly); st_zt: the tuner's
+  // choice (0: not used, 4 or 8 lattice points per thread along z)
+  int st_dims[3] = {0, 0, 0};
+  int* st_map = nullptr;
+  float* st_coef = nullptr;
+  int st_zt = 0;
   int tpr32 = 0;                 // FP32 CSR lanes per row (0: rows_per_warp_hint)
   // FP32 values from the tensor-core contraction, FP64 values not formed
   // (assemble_level_tc); last_a assembles them on demand (ensure_fp64)
@@ -362,12 +373,24 @@ int batch_prepare(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s,
                   int* inline_coarse);
 // tiles of the one-launch sweep of a uniform level (once per level)
 int mf_build_tiles(cdg_context* ctx, DevLevel& L);
+// the DOF lattice of a uniform level for the stencil sweep (once per level;
+// leaves st_dims zero where the level is not a full lattice with active
+// DOFs exactly at its interior points), and the stencils of the element
+// matrix in L.mf_ae (each assembly)
+int mf_build_lattice(cdg_context* ctx, DevLevel& L);
+int mf_stencil_coef(cdg_context* ctx, DevLevel& L);
 int mf_ensure(DevLevel& L);
+// the kernel form of a matrix-free application: as the tuner chose
+// (stencil, one-launch tiles or two kernels), the two-kernel product, the
+// one-launch tile sweep (two kernels where the level has no tiles), the
+// lattice stencil sweep
+enum { kMfAsTuned = 0, kMfTwoKernel = 1, kMfOneLaunch = 2, kMfStencil = 3 };
 int mf_apply(cdg_context* ctx, const DevLevel& L, int mode, const float* x, const float* b,
              const float* invd, float w, float* y, double* z = nullptr, const int* di = nullptr,
-             double* zcur = nullptr, int two_kernel = 0);
+             double* zcur = nullptr, int form = kMfAsTuned);
 // y = A x with the FP32 multigrid operator of a level: 0 CSR, 1 matrix-free
-// (one launch on uniform levels), 2 the two-kernel matrix-free product
+// (one launch on uniform levels), 2 the two-kernel matrix-free product,
+// 3 the lattice stencil sweep
 int apply32(cdg_context* ctx, const DevLevel& L, int variant, const float* x, float* y);
 // generic coefficients (CoeffFct): quadrature points of a level (host) and the
 // assembly with eps, b, c, f per (cell, point)

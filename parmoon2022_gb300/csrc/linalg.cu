@@ -1436,7 +1436,7 @@ int ensure_mg_vectors(cdg_context* ctx, DevLevel& L, int elem) {
 int apply32(cdg_context* ctx, const DevLevel& L, int variant, const float* x, float* y) {
   if (variant >= 1)
     return mf_apply(ctx, L, 0, x, nullptr, nullptr, 0.f, y, nullptr, nullptr, nullptr,
-                    variant == 2 ? 1 : 0);
+                    variant == 3 ? kMfStencil : (variant == 2 ? kMfTwoKernel : kMfOneLaunch));
   return spmv_t<float, 0>(ctx, L, L.val32, x, (const float*)nullptr, (const float*)nullptr, 0.f,
                           y);
 }
@@ -1478,11 +1478,15 @@ static int env_level(const char* name, int level) {
 //     the mean row length);
 //   * matrix-free (Q2 hexahedra): grid of one cell per warp, or 4 / 8 blocks
 //     per SM walking the cells;
+//   * on a uniform lattice with Dirichlet data on the whole boundary, the
+//     stencil sweep with 8 or 4 lattice points per thread against the best
+//     of the above;
 // and the faster of the best CSR and the best matrix-free step.  The grid
 // size and, for a given lane count, the loop unrolling do not change any
 // result; the lane count and the kernel kind change FP32 rounding only.
 // Environment overrides (a profiler's per-launch overhead distorts timing):
-// CDG_MATFREE (0/1), CDG_TPR32 (lanes), CDG_MF_CAP (blocks per SM).
+// CDG_MATFREE (0/1), CDG_TPR32 (lanes), CDG_MF_CAP (blocks per SM),
+// CDG_MF_MINB (4/5/6), CDG_MF_STENCIL (0, or 4/8 points per thread).
 static int tune_level(cdg_context* ctx, cdg_problem* p, DevLevel& L, int level) {
   if (L.tuned) return CDG_OK;
   L.tuned = 1;
@@ -1532,9 +1536,16 @@ static int tune_level(cdg_context* ctx, cdg_problem* p, DevLevel& L, int level) 
     L.tuned_ms[0] = best;
   }
   // matrix-free grid, then the faster kind
+  L.st_zt = 0;
+  const int st_env = env_level("CDG_MF_STENCIL", level);
+  const bool lattice = L.mf_uniform && L.st_dims[0] > 0;
   if (rc == CDG_OK && L.mf_valid && mf_env != 0) {
     L.mf_mode = 1;
-    if (L.mf_uniform && L.mf_ntiles > 0) {
+    if (lattice && (st_env == 4 || st_env == 8)) {
+      L.st_zt = st_env;
+      L.mf_blocks_per_sm = -100 - st_env;
+      time_step(&L.tuned_ms[1]);
+    } else if (L.mf_uniform && L.mf_ntiles > 0) {
       // the one-launch sweep has one block per row tile; its register budget
       // (4, 5 or 6 resident blocks per SM) is timed, reported as -blocks
       const int mb_env = env_level("CDG_MF_MINB", level);
@@ -1577,9 +1588,32 @@ static int tune_level(cdg_context* ctx, cdg_problem* p, DevLevel& L, int level) 
       L.mf_blocks_per_sm = bc;
       L.tuned_ms[1] = best;
     }
+    // the stencil sweep (4 or 8 lattice points per thread along z) against
+    // the best tile or cell sweep
+    if (rc == CDG_OK && lattice && st_env != 0 && L.st_zt == 0) {
+      float best = 1e30f;
+      int bz = 0;
+      for (int zt : {8, 4}) {
+        L.st_zt = zt;
+        float ms = 0.f;
+        time_step(&ms);
+        if (rc != CDG_OK) break;
+        if (ms < best) {
+          best = ms;
+          bz = zt;
+        }
+      }
+      L.st_zt = 0;
+      if (rc == CDG_OK && best < L.tuned_ms[1]) {
+        L.st_zt = bz;
+        L.tuned_ms[1] = best;
+        L.mf_blocks_per_sm = -100 - bz;
+      }
+    }
     if (mf_env != 1 && !(L.tuned_ms[1] < L.tuned_ms[0])) {
       L.mf_mode = 0;
       L.mf_blocks_per_sm = 0;   // unused by the CSR kernel
+      L.st_zt = 0;
     }
   }
   if (!L.mf_valid) L.mf_mode = -1;   // no matrix-free operator on this level

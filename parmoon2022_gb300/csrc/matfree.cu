@@ -401,6 +401,212 @@ k_mf_fused(int n, int nactive, const int* __restrict__ tile_rp,
   }
 }
 
+// ---------------------------------------------------------------------------
+// Lattice stencil sweep of a uniform level.  The DOFs of a uniform Q2 mesh
+// sit on a lattice of half-cell spacing; a point with odd coordinate d lies
+// inside one cell along d, one with even coordinate on the face between two,
+// so an active row (an interior point) couples to the points within 1 (odd)
+// or 2 (even) along each direction, with the sum over the cells around the
+// point of the element matrix entries: one of eight 125-point stencils,
+// chosen by the parities of the point (zeros outside the couplings).
+//
+// Block: 32 (x) x kStTY (y) lattice columns of ZT points along z, starting
+// at odd z; the x values of the block's points and a halo of two are staged
+// in shared memory through the lattice map (z innermost, a 12-float column
+// per (x, y): three conflict-free 16-byte loads), one staged point or so per
+// thread.  Five threads share a column, one per stencil plane dy: per dx
+// each loads its column and the eight z coefficients of its (x, y) parity
+// (odd z points couple to dz = -1..1, even ones to -2..2) and adds to its ZT
+// partial sums (32 multiply-adds per 5 shared loads); the planes' partials
+// meet in shared memory and are summed in plane order.  The b and D^-1 of
+// the rows a thread finishes are loaded before the products.  Rows of
+// non-active DOFs (identity) are taken by the blocks past the lattice tiles.
+// ---------------------------------------------------------------------------
+constexpr int kStTX = 32, kStTY = 4, kStDY = 5;
+constexpr int kStThreads = kStTX * kStTY * kStDY;   // 640
+constexpr int kStXS = kStTX + 4, kStYS = kStTY + 4, kStZS = 12;
+constexpr int kStCoef = 4 * 25 * 8;   // (x, y parity) x (dy, dx) x 8 z slots
+constexpr int kStBatch = 6;           // staged points per thread (one batch)
+
+// the row update of the k_spmv modes from the row sum s, with the row's b
+// and D^-1 already loaded
+template <int MODE>
+__device__ __forceinline__ void st_finish(int row, int n, float xr, float s, float br, float dr,
+                                          float w, float* __restrict__ y,
+                                          double* __restrict__ z, const int* di,
+                                          double* __restrict__ zcur) {
+  if (MODE == 0) {
+    y[row] = s;
+  } else if (MODE == 1) {
+    y[row] = br - s;
+  } else {
+    const float yr = xr + w * (dr * (br - s));
+    y[row] = yr;
+    if (MODE == 3) {
+      const double zr = (double)yr;
+      (di ? z + (size_t)(*di) * n : z)[row] = zr;
+      if (zcur) zcur[row] = zr;
+    }
+  }
+}
+
+// the eight stencils from the element matrix (A(row, col) = AeT[col * 27 +
+// row], local index ix + 3 iy + 9 iz in cell 0's frame).  Entry t: slot
+// s = t % 8 (0..2: odd z, dz = -1..1; 3..7: even z, dz = -2..2), offsets
+// dx, dy = (t / 8) % 25 as (dx + 2) + 5 (dy + 2), parities cls = t / 200 as
+// (x odd) + 2 (y odd).  Summed in FP64 over the cells around the point in a
+// fixed order, rounded once.
+__global__ void k_st_coef(const float* __restrict__ AeT, float* __restrict__ coef) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= kStCoef) return;
+  const int s = t % 8, pair = t / 8, dxy = pair % 25, cls = pair / 25;
+  const int par[3] = {cls & 1, cls >> 1, s < 3 ? 1 : 0};
+  const int off[3] = {dxy % 5 - 2, dxy / 5 - 2, s < 3 ? s - 1 : s - 5};
+  double a = 0.0;
+  for (int c = 0; c < 8; ++c) {
+    int r[3], q[3];
+    bool ok = true;
+    for (int d = 0; d < 3; ++d) {
+      const int side = (c >> d) & 1;
+      if (par[d]) {
+        if (side) ok = false;   // one cell along d
+        r[d] = 1;
+      } else {
+        r[d] = side ? 2 : 0;    // the cell below (local 2) or above (local 0)
+      }
+      q[d] = r[d] + off[d];
+      if (q[d] < 0 || q[d] > 2) ok = false;
+    }
+    if (!ok) continue;
+    const int row = r[0] + 3 * r[1] + 9 * r[2], col = q[0] + 3 * q[1] + 9 * q[2];
+    a += (double)AeT[col * 27 + row];
+  }
+  coef[t] = (float)a;
+}
+
+template <int MODE, int ZT>
+__global__ void __launch_bounds__(kStThreads)
+k_mf_stencil(int n, int nactive, int lx, int ly, int lz, int bx, int by, int nst,
+             const int* __restrict__ lmap, const float* __restrict__ coef,
+             const float* __restrict__ x, const float* __restrict__ b,
+             const float* __restrict__ invd, float w, float* __restrict__ y,
+             double* __restrict__ z, const int* di, double* __restrict__ zcur) {
+  static_assert(ZT % 4 == 0 && ZT + 4 <= kStZS, "z column of ZT points and a halo of two");
+  constexpr int NO = ZT * kStTY * kStTX;   // points of the block
+  static_assert(NO <= 2 * kStThreads, "two finished points per thread at most");
+  pdl_enter();
+  __shared__ __align__(16) float s_x[kStYS * kStXS * kStZS];
+  __shared__ __align__(16) float s_c[kStCoef];
+  __shared__ float s_p[kStDY * NO];
+  __shared__ int s_g[NO];
+  const int tid = threadIdx.x;
+  if ((int)blockIdx.x >= nst) {
+    const int row = nactive + ((int)blockIdx.x - nst) * kStThreads + tid;
+    if (row < n) {
+      const float xr = x[row];
+      st_finish<MODE>(row, n, xr, xr, MODE >= 1 ? b[row] : 0.f, MODE >= 2 ? invd[row] : 0.f, w,
+                      y, z, di, zcur);
+    }
+    return;
+  }
+  const int bxi = (int)blockIdx.x % bx, rest = (int)blockIdx.x / bx;
+  const int X0 = 1 + bxi * kStTX, Y0 = 1 + (rest % by) * kStTY, Z0 = 1 + (rest / by) * ZT;
+  for (int i = tid; i < kStCoef; i += kStThreads) s_c[i] = __ldg(coef + i);
+  // stage the tile: every lattice map load, then every x value
+  constexpr int NP = kStXS * kStYS * (ZT + 4);
+  static_assert(NP <= kStBatch * kStThreads, "one staging batch");
+  {
+    int g[kStBatch];
+#pragma unroll
+    for (int k = 0; k < kStBatch; ++k) {
+      const int q = k * kStThreads + tid;
+      g[k] = -1;
+      if (q < NP) {
+        const int qx = q % kStXS, r = q / kStXS, qy = r % kStYS, qz = r / kStYS;
+        const int ax = X0 - 2 + qx, ay = Y0 - 2 + qy, az = Z0 - 2 + qz;
+        if (ax >= 0 && ax < lx && ay >= 0 && ay < ly && az >= 0 && az < lz)
+          g[k] = __ldg(lmap + ((size_t)az * ly + ay) * lx + ax);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kStBatch; ++k) {
+      const int q = k * kStThreads + tid;
+      if (q < NP) {
+        const int qx = q % kStXS, r = q / kStXS, qy = r % kStYS, qz = r / kStYS;
+        s_x[(qy * kStXS + qx) * kStZS + qz] = g[k] >= 0 ? __ldg(x + g[k]) : 0.f;
+        const int ix = qx - 2, iy = qy - 2, iz = qz - 2;
+        if (ix >= 0 && ix < kStTX && iy >= 0 && iy < kStTY && iz >= 0 && iz < ZT)
+          s_g[(iz * kStTY + iy) * kStTX + ix] = g[k];
+      }
+    }
+  }
+  __syncthreads();
+  // the points this thread finishes (o = tid, tid + kStThreads): their rows'
+  // b and D^-1 are in flight during the products
+  int orow[2] = {-1, -1};
+  float ob[2] = {0.f, 0.f}, od[2] = {0.f, 0.f};
+#pragma unroll
+  for (int u = 0; u < 2; ++u) {
+    const int o = tid + u * kStThreads;
+    if (o < NO) {
+      const int k = o / (kStTY * kStTX), ty = (o / kStTX) % kStTY, tx = o % kStTX;
+      if (X0 + tx <= lx - 2 && Y0 + ty <= ly - 2 && Z0 + k <= lz - 2) {
+        orow[u] = s_g[o];
+        if (MODE >= 1) ob[u] = __ldg(b + orow[u]);
+        if (MODE >= 2) od[u] = __ldg(invd + orow[u]);
+      }
+    }
+  }
+  const int tx = tid % kStTX, ty = (tid / kStTX) % kStTY, dy = tid / (kStTX * kStTY);
+  const int ax = X0 + tx, ay = Y0 + ty;
+  const float* cb = s_c + ((ax & 1) | ((ay & 1) << 1)) * 200 + dy * 40;
+  float acc[ZT];
+#pragma unroll
+  for (int k = 0; k < ZT; ++k) acc[k] = 0.f;
+#pragma unroll
+  for (int dx = 0; dx < 5; ++dx) {
+    const float4* cp = reinterpret_cast<const float4*>(s_x + ((ty + dy) * kStXS + tx + dx) * kStZS);
+    float col[ZT + 4];
+#pragma unroll
+    for (int j = 0; j < (ZT + 4) / 4; ++j) {
+      const float4 v = cp[j];
+      col[4 * j] = v.x;
+      col[4 * j + 1] = v.y;
+      col[4 * j + 2] = v.z;
+      col[4 * j + 3] = v.w;
+    }
+    const float4 c0 = *reinterpret_cast<const float4*>(cb + dx * 8);
+    const float4 c1 = *reinterpret_cast<const float4*>(cb + dx * 8 + 4);
+#pragma unroll
+    for (int k = 0; k < ZT; k += 2) {
+      // lattice z = Z0 + k is odd: dz = -1, 0, 1 at col[k + 2 + dz]
+      acc[k] = fmaf(c0.x, col[k + 1], acc[k]);
+      acc[k] = fmaf(c0.y, col[k + 2], acc[k]);
+      acc[k] = fmaf(c0.z, col[k + 3], acc[k]);
+      // z = Z0 + k + 1 is even: dz = -2 .. 2 at col[k + 3 + dz]
+      acc[k + 1] = fmaf(c0.w, col[k + 1], acc[k + 1]);
+      acc[k + 1] = fmaf(c1.x, col[k + 2], acc[k + 1]);
+      acc[k + 1] = fmaf(c1.y, col[k + 3], acc[k + 1]);
+      acc[k + 1] = fmaf(c1.z, col[k + 4], acc[k + 1]);
+      acc[k + 1] = fmaf(c1.w, col[k + 5], acc[k + 1]);
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < ZT; ++k) s_p[dy * NO + (k * kStTY + ty) * kStTX + tx] = acc[k];
+  __syncthreads();
+#pragma unroll
+  for (int u = 0; u < 2; ++u) {
+    if (orow[u] < 0) continue;
+    const int o = tid + u * kStThreads;
+    const int k = o / (kStTY * kStTX), oy = (o / kStTX) % kStTY, ox = o % kStTX;
+    float sum = s_p[o];
+#pragma unroll
+    for (int d = 1; d < kStDY; ++d) sum += s_p[d * NO + o];
+    const float xr = s_x[((oy + 2) * kStXS + ox + 2) * kStZS + k + 2];
+    st_finish<MODE>(orow[u], n, xr, sum, ob[u], od[u], w, y, z, di, zcur);
+  }
+}
+
 }  // namespace
 
 // the sweep's register budget: 4, 5 or 6 resident blocks per SM (64, 48 or
@@ -519,6 +725,135 @@ int mf_build_tiles(cdg_context* ctx, DevLevel& L) {
   return CDG_OK;
 }
 
+// The DOF lattice of a uniform level, from the cells' DOFs in cell 0's frame
+// (mf_gdof): cells sharing a face-centre DOF are neighbours along that
+// face's axis, so a walk from cell 0 places every cell at integer offsets;
+// local DOF (ix, iy, iz) of the cell at offset o sits at lattice point
+// 2 o + (ix, iy, iz).  The stencil sweep needs a full box of cells, one DOF
+// per lattice point and the active DOFs exactly at the interior points
+// (Dirichlet data on the whole boundary); any level that is not such a
+// lattice keeps st_dims zero.
+int mf_build_lattice(cdg_context* ctx, DevLevel& L) {
+  L.st_dims[0] = L.st_dims[1] = L.st_dims[2] = 0;
+  const int nc = L.ncells, n = L.ndof, na = L.nactive;
+  if (nc == 0 || na == 0 || L.mf_geo != 1) return CDG_OK;
+  std::vector<int> gdc((size_t)nc * 27);
+  CDG_CUDA(cudaMemcpyAsync(gdc.data(), L.mf_gdof, gdc.size() * sizeof(int),
+                           cudaMemcpyDeviceToHost, ctx->stream));
+  CDG_CUDA(cudaStreamSynchronize(ctx->stream));
+  // face-centre local DOFs: -x, +x, -y, +y, -z, +z
+  static const int kFace[6] = {12, 14, 10, 16, 4, 22};
+  std::vector<int> fa(n, -1), fb(n, -1);   // the (cell, face) holders of a DOF
+  for (int c = 0; c < nc; ++c)
+    for (int f = 0; f < 6; ++f) {
+      const int g = gdc[(size_t)c * 27 + kFace[f]];
+      if (g < 0 || g >= n) return CDG_OK;
+      if (fa[g] < 0) fa[g] = c * 6 + f;
+      else if (fb[g] < 0) fb[g] = c * 6 + f;
+      else return CDG_OK;   // a face-centre DOF in three cells
+    }
+  std::vector<int> off((size_t)nc * 3, 0), seen(nc, 0), queue;
+  queue.reserve(nc);
+  queue.push_back(0);
+  seen[0] = 1;
+  for (size_t h = 0; h < queue.size(); ++h) {
+    const int c = queue[h];
+    for (int f = 0; f < 6; ++f) {
+      const int g = gdc[(size_t)c * 27 + kFace[f]];
+      const int other = fa[g] == c * 6 + f ? fb[g] : fa[g];
+      if (other < 0) continue;   // boundary face
+      const int c2 = other / 6, f2 = other % 6;
+      if (f2 != (f ^ 1)) return CDG_OK;   // not a translate across the face
+      int o[3] = {off[(size_t)c * 3], off[(size_t)c * 3 + 1], off[(size_t)c * 3 + 2]};
+      o[f / 2] += (f & 1) ? 1 : -1;
+      if (seen[c2]) {
+        for (int d = 0; d < 3; ++d)
+          if (off[(size_t)c2 * 3 + d] != o[d]) return CDG_OK;
+        continue;
+      }
+      seen[c2] = 1;
+      for (int d = 0; d < 3; ++d) off[(size_t)c2 * 3 + d] = o[d];
+      queue.push_back(c2);
+    }
+  }
+  if ((int)queue.size() != nc) return CDG_OK;   // not connected through faces
+  int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  for (int c = 0; c < nc; ++c)
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = std::min(lo[d], off[(size_t)c * 3 + d]);
+      hi[d] = std::max(hi[d], off[(size_t)c * 3 + d]);
+    }
+  long ld[3], npts = 1, ncb = 1;
+  for (int d = 0; d < 3; ++d) {
+    ld[d] = 2L * (hi[d] - lo[d] + 1) + 1;
+    npts *= ld[d];
+    ncb *= hi[d] - lo[d] + 1;
+  }
+  if (ncb != nc || npts != n) return CDG_OK;   // not a full box, or not one DOF per point
+  std::vector<int> map((size_t)npts, -1), inv(n, -1);
+  for (int c = 0; c < nc; ++c)
+    for (int m = 0; m < 27; ++m) {
+      const long px = 2L * (off[(size_t)c * 3] - lo[0]) + m % 3;
+      const long py = 2L * (off[(size_t)c * 3 + 1] - lo[1]) + (m / 3) % 3;
+      const long pz = 2L * (off[(size_t)c * 3 + 2] - lo[2]) + m / 9;
+      const long idx = (pz * ld[1] + py) * ld[0] + px;
+      const int g = gdc[(size_t)c * 27 + m];
+      if (g < 0 || g >= n) return CDG_OK;
+      if (map[idx] >= 0 && map[idx] != g) return CDG_OK;
+      if (inv[g] >= 0 && inv[g] != idx) return CDG_OK;
+      map[idx] = g;
+      inv[g] = (int)idx;
+    }
+  for (long idx = 0; idx < npts; ++idx) {
+    if (map[idx] < 0) return CDG_OK;
+    const long px = idx % ld[0], py = (idx / ld[0]) % ld[1], pz = idx / (ld[0] * ld[1]);
+    const bool interior = px > 0 && px < ld[0] - 1 && py > 0 && py < ld[1] - 1 && pz > 0 &&
+                          pz < ld[2] - 1;
+    if (interior != (map[idx] < na)) return CDG_OK;
+  }
+  if (L.st_map) cudaFree(L.st_map);
+  L.st_map = nullptr;
+  CDG_CUDA(cudaMalloc(&L.st_map, (size_t)npts * sizeof(int)));
+  if (!L.st_coef) CDG_CUDA(cudaMalloc(&L.st_coef, kStCoef * sizeof(float)));
+  CDG_CUDA(cudaMemcpyAsync(L.st_map, map.data(), (size_t)npts * sizeof(int),
+                           cudaMemcpyHostToDevice, ctx->stream));
+  CDG_CUDA(cudaStreamSynchronize(ctx->stream));   // the host map goes out of scope
+  for (int d = 0; d < 3; ++d) L.st_dims[d] = (int)ld[d];
+  return CDG_OK;
+}
+
+int mf_stencil_coef(cdg_context* ctx, DevLevel& L) {
+  if (L.st_dims[0] == 0) return CDG_OK;
+  CDG_LAUNCH(ctx, k_st_coef, (kStCoef + 255) / 256, 256, 0, L.mf_ae, L.st_coef);
+  return CDG_OK;
+}
+
+template <int MODE, int ZT>
+static int stencil_launch(cdg_context* ctx, const DevLevel& L, const float* x, const float* b,
+                          const float* invd, float w, float* y, double* z, const int* di,
+                          double* zcur) {
+  const int lx = L.st_dims[0], ly = L.st_dims[1], lz = L.st_dims[2];
+  const int bx = (lx - 2 + kStTX - 1) / kStTX, by = (ly - 2 + kStTY - 1) / kStTY;
+  const int bz = (lz - 2 + ZT - 1) / ZT;
+  const int nst = bx * by * bz;
+  const int nb = nst + (L.ndof - L.nactive + kStThreads - 1) / kStThreads;
+  CDG_LAUNCH_PDL(ctx, (k_mf_stencil<MODE, ZT>), nb, kStThreads, 0, L.ndof, L.nactive, lx, ly,
+                 lz, bx, by, nst, L.st_map, L.st_coef, x, b, invd, w, y, z, di, zcur);
+  return CDG_OK;
+}
+
+template <int ZT>
+static int stencil_mode(cdg_context* ctx, const DevLevel& L, int mode, const float* x,
+                        const float* b, const float* invd, float w, float* y, double* z,
+                        const int* di, double* zcur) {
+  switch (mode) {
+    case 0: return stencil_launch<0, ZT>(ctx, L, x, b, invd, w, y, z, di, zcur);
+    case 1: return stencil_launch<1, ZT>(ctx, L, x, b, invd, w, y, z, di, zcur);
+    case 2: return stencil_launch<2, ZT>(ctx, L, x, b, invd, w, y, z, di, zcur);
+    default: return stencil_launch<3, ZT>(ctx, L, x, b, invd, w, y, z, di, zcur);
+  }
+}
+
 bool mf_eligible(const DevLevel& L) {
   return L.shape == kHexa && L.order == 2 && !L.multilinear;
 }
@@ -538,12 +873,21 @@ int mf_ensure(DevLevel& L) {
 
 int mf_apply(cdg_context* ctx, const DevLevel& L, int mode, const float* x, const float* b,
              const float* invd, float w, float* y, double* z, const int* di, double* zcur,
-             int two_kernel) {
+             int form) {
   if (!L.mf_valid) {
     set_error("matrix-free operator used without valid cell factors");
     return CDG_ERR_ARG;
   }
-  if (L.mf_uniform && L.mf_ntiles > 0 && !two_kernel) {
+  const bool lattice = L.mf_uniform && L.st_dims[0] > 0;
+  if (form == kMfStencil && !lattice) {
+    set_error("the level is not a uniform lattice with Dirichlet data on its whole boundary");
+    return CDG_ERR_ARG;
+  }
+  if (lattice && (form == kMfStencil || (form == kMfAsTuned && L.st_zt > 0))) {
+    if (L.st_zt == 4) return stencil_mode<4>(ctx, L, mode, x, b, invd, w, y, z, di, zcur);
+    return stencil_mode<8>(ctx, L, mode, x, b, invd, w, y, z, di, zcur);
+  }
+  if (L.mf_uniform && L.mf_ntiles > 0 && form != kMfTwoKernel) {
     const int g = L.mf_ntiles;
     const size_t sm = (size_t)L.mf_tile_maxcells * kMfCellStride * sizeof(float);
     switch (mode) {

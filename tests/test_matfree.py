@@ -17,7 +17,11 @@ Bars:
     iterations of it, with the solution equal to the oracle's to 1e-8 and
     L2/H1 errors equal to 3 significant digits;
   * the per-level kernel choice of the tuner is reported and gives the same
-    solve within those bars.
+    solve within those bars;
+  * on a uniform lattice with Dirichlet data on the whole boundary the
+    stencil sweep (eight 125-point stencils summed from the element matrix)
+    equals the CSR and the oracle's products to FP32 rounding and solves
+    within one iteration of the tile sweep; other levels refuse it.
 """
 import os
 
@@ -176,7 +180,8 @@ def test_tuned_schedule_reproduced_by_its_settings(ctx, monkeypatch):
     # within the mixed-precision bars
     nref, _, kw = CASES["supg_polyexp"]
     levels = 3
-    for name in ("CDG_MATFREE", "CDG_TPR32", "CDG_MF_CAP", "CDG_MF_MINB", "CDG_TUNE"):
+    for name in ("CDG_MATFREE", "CDG_TPR32", "CDG_MF_CAP", "CDG_MF_MINB", "CDG_MF_STENCIL",
+                 "CDG_TUNE"):
         monkeypatch.delenv(name, raising=False)
 
     def run():
@@ -193,15 +198,19 @@ def test_tuned_schedule_reproduced_by_its_settings(ctx, monkeypatch):
     assert all(d[0] in (0, 1) for d in det)
     monkeypatch.setenv("CDG_MATFREE", ",".join(str(d[0]) for d in det))
     monkeypatch.setenv("CDG_TPR32", ",".join(str(d[2][0]) for d in det))
-    # grid cap (two-launch sweep) or register budget (one-launch sweep, -blocks)
+    # grid cap (two-launch sweep), register budget (one-launch sweep, -blocks)
+    # or points per thread (stencil sweep, -100 - points)
     monkeypatch.setenv("CDG_MF_CAP", ",".join(str(max(d[2][1], 0)) for d in det))
-    monkeypatch.setenv("CDG_MF_MINB", ",".join(str(-d[2][1] if d[2][1] < 0 else 4) for d in det))
+    monkeypatch.setenv("CDG_MF_MINB", ",".join(str(-d[2][1] if -6 <= d[2][1] <= -4 else 4)
+                                               for d in det))
+    monkeypatch.setenv("CDG_MF_STENCIL", ",".join(str(-100 - d[2][1] if d[2][1] <= -100 else 0)
+                                                  for d in det))
     st_f, x_f, det_f = run()
     assert [d[0] for d in det_f] == [d[0] for d in det]
     assert [d[2] for d in det_f] == [d[2] for d in det]
     assert st_f.iterations == st_t.iterations
     assert rel(x_f, x_t) < 1e-10
-    for name in ("CDG_MATFREE", "CDG_TPR32", "CDG_MF_CAP", "CDG_MF_MINB"):
+    for name in ("CDG_MATFREE", "CDG_TPR32", "CDG_MF_CAP", "CDG_MF_MINB", "CDG_MF_STENCIL"):
         monkeypatch.delenv(name)
     monkeypatch.setenv("CDG_TUNE", "0")
     st_d, x_d, det_d = run()
@@ -219,6 +228,7 @@ def test_matrix_free_grid_does_not_change_results(ctx, monkeypatch):
     x = None
     outs = []
     monkeypatch.setenv("CDG_MF_FUSED", "0")
+    monkeypatch.setenv("CDG_MF_STENCIL", "0")
     for cap in ("0", "4", "8"):
         monkeypatch.setenv("CDG_MATFREE", "1")
         monkeypatch.setenv("CDG_MF_CAP", cap)
@@ -266,6 +276,7 @@ def test_one_launch_sweep_in_solves(ctx, monkeypatch):
     nref, _, kw = CASES["supg_polyexp"]
     levels = 3
     monkeypatch.setenv("CDG_MATFREE", "1")
+    monkeypatch.setenv("CDG_MF_STENCIL", "0")
     out = []
     for fused in ("1", "0"):
         monkeypatch.setenv("CDG_MF_FUSED", fused)
@@ -299,3 +310,95 @@ def test_uniform_fp64_matrix_equals_the_contraction(ctx, monkeypatch, name):
     for l in range(levels):
         assert rel(mats[0][l], mats[1][l]) < 1e-14
         assert rel(mats[0][l], o.matrix(l)) < 1e-12
+
+
+@pytest.mark.parametrize("sheared", [False, True])
+@pytest.mark.parametrize("name", ["supg_polyexp", "supg_sine_sdfem2", "galerkin_sine"])
+def test_stencil_sweep_operator(ctx, name, sheared):
+    # every active row of a uniform lattice is one of eight 125-point
+    # stencils (by the parities of its lattice point) summed from the element
+    # matrix: the stencil product equals the CSR product and the oracle's
+    # FP64 product to FP32 rounding on every level, identity on non-active rows
+    nref, levels, kw = CASES[name]
+    if sheared:
+        gpu, o = sheared_pair(ctx, nref, levels, kw)
+    else:
+        gpu = pg.ConvectionDiffusion(ctx, pg.Hierarchy(3, 2, nref, n_levels=levels))
+        o = po.Problem(oracle_cfg(nref, kw), levels)
+    gpu.assemble(gpu_params(kw))
+    o.assemble()
+    rng = np.random.default_rng(13)
+    for lvl in range(levels):
+        na = gpu.info(lvl)["nactive"]
+        x = rng.standard_normal(gpu.info(lvl)["ndof"]).astype(np.float32)
+        y3 = gpu.apply32(x, lvl, 3)
+        y0 = gpu.apply32(x, lvl, 0)
+        assert rel(y3[:na], y0[:na]) < 2e-5, (lvl, rel(y3[:na], y0[:na]))
+        assert rel(y3[:na], o.apply(x.astype(np.float64), lvl)[:na]) < 2e-5
+        assert np.array_equal(y3[na:], x[na:])
+    gpu.close()
+
+
+@pytest.mark.parametrize("sheared", [False, True])
+def test_stencil_sweep_on_several_tiles(ctx, sheared):
+    # a 32^3 Q2 lattice (65^3 points: two tiles along x, the last one partly
+    # outside, z tiles ending at the boundary) against the CSR product
+    kw = CASES["supg_polyexp"][2]
+    if sheared:
+        gpu, _ = sheared_pair(ctx, 5, 1, kw)
+    else:
+        gpu = pg.ConvectionDiffusion(ctx, pg.Hierarchy(3, 2, 5, n_levels=1))
+    gpu.assemble(gpu_params(kw))
+    na, n = gpu.info(0)["nactive"], gpu.info(0)["ndof"]
+    x = np.random.default_rng(17).standard_normal(n).astype(np.float32)
+    y3, y0 = gpu.apply32(x, 0, 3), gpu.apply32(x, 0, 0)
+    assert rel(y3[:na], y0[:na]) < 2e-5
+    assert np.array_equal(y3[na:], x[na:])
+    # deterministic: the same product twice
+    assert np.array_equal(gpu.apply32(x, 0, 3), y3)
+    gpu.close()
+
+
+def test_stencil_sweep_needs_a_dirichlet_lattice(ctx):
+    # active DOFs on the boundary (Neumann faces) break the interior-stencil
+    # rows; moved vertices leave no matrix-free operator: both refuse
+    kw = CASES["galerkin_sine"][2]
+    for h, a in ((pg.Hierarchy(3, 2, 2, neumann_mask=36),
+                  pg.assembly_params(example=pg.EX_SINE, eps=0.1, b=(1.0, 0.3, -0.2), c=0.5,
+                                     neumann_mask=36)),
+                 (pg.Hierarchy(3, 2, 2, perturb=0.2, seed=3), gpu_params(kw))):
+        gpu = pg.ConvectionDiffusion(ctx, h)
+        gpu.assemble(a)
+        x = np.ones(gpu.info(0)["ndof"], np.float32)
+        if a.neumann_mask:
+            gpu.apply32(x, 0, 1)   # the tile sweep takes the level
+        with pytest.raises(pg.CdgError) as e:
+            gpu.apply32(x, 0, 3)
+        assert e.value.code == -1
+        gpu.close()
+
+
+def test_stencil_sweep_in_solves(ctx, monkeypatch):
+    # mixed solves with the stencil sweep on the finest level (8 and 4 lattice
+    # points per thread) against the one-launch tile sweep: within one
+    # iteration, the solutions to 1e-8 (the sweeps differ in FP32 rounding)
+    nref, _, kw = CASES["supg_polyexp"]
+    nref, levels = 4, 3
+    monkeypatch.setenv("CDG_MATFREE", "1,0,0")
+    out = []
+    for st_env in ("8", "4", "0"):
+        monkeypatch.setenv("CDG_MF_STENCIL", st_env)
+        gpu = pg.ConvectionDiffusion(ctx, pg.Hierarchy(3, 2, nref, n_levels=levels))
+        a = gpu_params(kw)
+        gpu.assemble(a)
+        st = gpu.solve(mixed_solver(levels))
+        assert st.residual <= 1e-10 * st.initial_residual
+        out.append((st.iterations, gpu.solution(), gpu.tuning_detail(0), gpu.errors(a)))
+        gpu.close()
+    assert out[0][2][2][1] == -108 and out[1][2][2][1] == -104
+    assert out[2][2][2][1] in (-4, -5, -6)
+    for it, x, _, e in out[:2]:
+        assert abs(it - out[2][0]) <= 1
+        assert rel(x, out[2][1]) < 1e-8
+        for k in (0, 1):
+            assert abs(e[k] - out[2][3][k]) <= 5e-4 * out[2][3][k]
