@@ -413,7 +413,7 @@ k_mf_fused(int n, int nactive, const int* __restrict__ tile_rp,
 // Block: 32 (x) x kStTY (y) lattice columns of ZT points along z, starting
 // at odd z; the x values of the block's points and a halo of two are staged
 // in shared memory through the lattice map (z innermost, a 12-float column
-// per (x, y): three conflict-free 16-byte loads), one staged point or so per
+// per (x, y): three conflict-free 16-byte loads), a staged column per
 // thread.  Five threads share a column, one per stencil plane dy: per dx
 // each loads its column and the eight z coefficients of its (x, y) parity
 // (odd z points couple to dz = -1..1, even ones to -2..2) and adds to its ZT
@@ -426,7 +426,6 @@ constexpr int kStTX = 32, kStTY = 4, kStDY = 5;
 constexpr int kStThreads = kStTX * kStTY * kStDY;   // 640
 constexpr int kStXS = kStTX + 4, kStYS = kStTY + 4, kStZS = 12;
 constexpr int kStCoef = 4 * 25 * 8;   // (x, y parity) x (dy, dx) x 8 z slots
-constexpr int kStBatch = 6;           // staged points per thread (one batch)
 
 // the row update of the k_spmv modes from the row sum s, with the row's b
 // and D^-1 already loaded
@@ -485,7 +484,7 @@ __global__ void k_st_coef(const float* __restrict__ AeT, float* __restrict__ coe
 }
 
 template <int MODE, int ZT>
-__global__ void __launch_bounds__(kStThreads)
+__global__ void __launch_bounds__(kStThreads, 2)
 k_mf_stencil(int n, int nactive, int lx, int ly, int lz, int bx, int by, int nst,
              const int* __restrict__ lmap, const float* __restrict__ coef,
              const float* __restrict__ x, const float* __restrict__ b,
@@ -512,32 +511,33 @@ k_mf_stencil(int n, int nactive, int lx, int ly, int lz, int bx, int by, int nst
   const int bxi = (int)blockIdx.x % bx, rest = (int)blockIdx.x / bx;
   const int X0 = 1 + bxi * kStTX, Y0 = 1 + (rest % by) * kStTY, Z0 = 1 + (rest / by) * ZT;
   for (int i = tid; i < kStCoef; i += kStThreads) s_c[i] = __ldg(coef + i);
-  // stage the tile: every lattice map load, then every x value
-  constexpr int NP = kStXS * kStYS * (ZT + 4);
-  static_assert(NP <= kStBatch * kStThreads, "one staging batch");
-  {
-    int g[kStBatch];
+  // stage the tile: a thread per (x, y) column of the tile and its halo
+  // loads the column's ZT + 4 lattice map entries, then their x values, and
+  // stores the column as 16-byte words (conflict-free, as the loads below)
+  constexpr int NCOL = kStXS * kStYS;
+  static_assert(NCOL <= kStThreads, "one staged column per thread");
+  if (tid < NCOL) {
+    const int qx = tid % kStXS, qy = tid / kStXS;
+    const int ax = X0 - 2 + qx, ay = Y0 - 2 + qy;
+    const bool in = ax >= 0 && ax < lx && ay >= 0 && ay < ly;
+    const int* mp = lmap + (in ? (size_t)ay * lx + ax : 0);
+    const size_t plane = (size_t)lx * ly;
+    int g[ZT + 4];
 #pragma unroll
-    for (int k = 0; k < kStBatch; ++k) {
-      const int q = k * kStThreads + tid;
-      g[k] = -1;
-      if (q < NP) {
-        const int qx = q % kStXS, r = q / kStXS, qy = r % kStYS, qz = r / kStYS;
-        const int ax = X0 - 2 + qx, ay = Y0 - 2 + qy, az = Z0 - 2 + qz;
-        if (ax >= 0 && ax < lx && ay >= 0 && ay < ly && az >= 0 && az < lz)
-          g[k] = __ldg(lmap + ((size_t)az * ly + ay) * lx + ax);
-      }
+    for (int qz = 0; qz < ZT + 4; ++qz) {
+      const int az = Z0 - 2 + qz;
+      g[qz] = in && az >= 0 && az < lz ? __ldg(mp + (size_t)az * plane) : -1;
     }
+    float v[ZT + 4];
 #pragma unroll
-    for (int k = 0; k < kStBatch; ++k) {
-      const int q = k * kStThreads + tid;
-      if (q < NP) {
-        const int qx = q % kStXS, r = q / kStXS, qy = r % kStYS, qz = r / kStYS;
-        s_x[(qy * kStXS + qx) * kStZS + qz] = g[k] >= 0 ? __ldg(x + g[k]) : 0.f;
-        const int ix = qx - 2, iy = qy - 2, iz = qz - 2;
-        if (ix >= 0 && ix < kStTX && iy >= 0 && iy < kStTY && iz >= 0 && iz < ZT)
-          s_g[(iz * kStTY + iy) * kStTX + ix] = g[k];
-      }
+    for (int qz = 0; qz < ZT + 4; ++qz) v[qz] = g[qz] >= 0 ? __ldg(x + g[qz]) : 0.f;
+    float4* dst = reinterpret_cast<float4*>(s_x + (qy * kStXS + qx) * kStZS);
+#pragma unroll
+    for (int j = 0; j < (ZT + 4) / 4; ++j)
+      dst[j] = make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+    if (qx >= 2 && qx < 2 + kStTX && qy >= 2 && qy < 2 + kStTY) {
+#pragma unroll
+      for (int k = 0; k < ZT; ++k) s_g[(k * kStTY + qy - 2) * kStTX + qx - 2] = g[k + 2];
     }
   }
   __syncthreads();
@@ -563,8 +563,12 @@ k_mf_stencil(int n, int nactive, int lx, int ly, int lz, int bx, int by, int nst
   float acc[ZT];
 #pragma unroll
   for (int k = 0; k < ZT; ++k) acc[k] = 0.f;
+  // a point at odd y couples to dy = -1..1 only: the planes dy = +-2 of such
+  // rows (whole warps: a warp is one (y, dy)) have zero coefficients
+  const bool plane = !((ay & 1) && (dy == 0 || dy == 4));
 #pragma unroll
   for (int dx = 0; dx < 5; ++dx) {
+    if (!plane) break;
     const float4* cp = reinterpret_cast<const float4*>(s_x + ((ty + dy) * kStXS + tx + dx) * kStZS);
     float col[ZT + 4];
 #pragma unroll
