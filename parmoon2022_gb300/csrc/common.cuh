@@ -66,6 +66,8 @@ struct cdg_context {
   long long launches = 0;
   // programmatic dependent launch of the solver kernels (CDG_PDL=1: on)
   int pdl = 0;
+  // the runtime refused a cooperative launch inside the captured FGMRES loop
+  int coop_graph_failed = 0;
   // request descriptors and results of the batched solver (pinned / device)
   void* batch_host = nullptr;
   void* batch_dev = nullptr;
@@ -235,6 +237,7 @@ struct GmresState {
   cudaGraph_t graph = nullptr;
   cdg_solver_params key{};   // parameters the graph was captured with
   unsigned long long key_gen = 0;
+  int coop = -1;             // the graph's Gram-Schmidt: 1 the cooperative step, 0 three kernels
   long long body_launches = 0;   // kernels per iteration
 };
 

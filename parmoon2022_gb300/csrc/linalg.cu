@@ -623,12 +623,169 @@ k_cgs_update(int n, double* __restrict__ w, const double* __restrict__ V, int i,
   }
 }
 
+// One classical Gram-Schmidt step of FGMRES column i in one cooperative
+// launch of one block per SM: the inner products (w, v_k), k <= i
+// (Iteration_gmres.C:515-527), w -= sum_k H(k,i) v_k, H(i+1,i) = ||w||, the
+// Givens step of column i and v_{i+1} = w / H(i+1,i) -- the work of
+// k_multidot, k_cgs_update and k_scale_inv, with three grid-wide barriers in
+// place of two launches and two single-block sums of every block's
+// partials.  Inner product k is summed over the blocks' partials (in block
+// order) by block k mod nb; the norm by every block, in block order, so all
+// blocks hold the same value.  i from *di when di is given (graph-captured
+// loop), else i_host.
+__global__ void __launch_bounds__(256)
+k_cgs_coop(int n, double* __restrict__ w, double* __restrict__ V, int i_host, const int* di,
+           int hstride, double* __restrict__ H, double* __restrict__ part, int normoff,
+           double* cs, double* sn, double* gs, double* resid, double* norm_out, int* err) {
+  cgrp::grid_group grid = cgrp::this_grid();
+  __shared__ double tr[8][257];
+  __shared__ double h[128];
+  __shared__ double scs[128], ssn[128], ss[2], nrm_s;
+  const int i = di ? *di : i_host;
+  const int nb = gridDim.x, wp = threadIdx.x >> 5, l = threadIdx.x & 31;
+  const long stride = (long)nb * 256;
+  double* hcol = H + (size_t)i * hstride;
+  // (1) block partials of the inner products, eight per pass over w
+  for (int j0 = 0; j0 <= i; j0 += 8) {
+    double a[8];
+#pragma unroll
+    for (int jj = 0; jj < 8; ++jj) a[jj] = 0.0;
+    for (long t = blockIdx.x * 256L + threadIdx.x; t < n; t += stride) {
+      const double wt = w[t];
+#pragma unroll
+      for (int jj = 0; jj < 8; ++jj)
+        if (j0 + jj <= i) a[jj] = fma(wt, __ldcg(V + (size_t)(j0 + jj) * n + t), a[jj]);
+    }
+#pragma unroll
+    for (int jj = 0; jj < 8; ++jj) tr[jj][threadIdx.x] = a[jj];
+    __syncthreads();
+    if (j0 + wp <= i) {
+      double v = 0.0;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) v += tr[wp][q * 32 + l];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (l == 0) part[(size_t)(j0 + wp) * nb + blockIdx.x] = v;
+    }
+    __syncthreads();
+  }
+  grid.sync();
+  // (2) H(k,i): inner product k over the blocks, by block k mod nb
+  for (int k = blockIdx.x; k <= i; k += nb) {
+    double v = 0.0;
+    for (int b = threadIdx.x; b < nb; b += 256) v += __ldcg(part + (size_t)k * nb + b);
+    v = block_sum<256>(v);
+    if (threadIdx.x == 0) hcol[k] = v;
+  }
+  grid.sync();
+  // (3) w -= sum_k H(k,i) v_k (k in order), block partial of ||w||^2
+  for (int k = threadIdx.x; k <= i; k += 256) h[k] = -__ldcg(hcol + k);
+  __syncthreads();
+  double s = 0.0;
+  for (long t = blockIdx.x * 256L + threadIdx.x; t < n; t += stride) {
+    double wt = w[t];
+    int j = 0;
+    for (; j + 7 <= i; j += 8) {
+      double a[8];
+#pragma unroll
+      for (int jj = 0; jj < 8; ++jj) a[jj] = __ldcg(V + (size_t)(j + jj) * n + t);
+#pragma unroll
+      for (int jj = 0; jj < 8; ++jj) wt = fma(h[j + jj], a[jj], wt);
+    }
+    for (; j <= i; ++j) wt = fma(h[j], __ldcg(V + (size_t)j * n + t), wt);
+    w[t] = wt;
+    s += wt * wt;
+  }
+  s = block_sum<256>(s);
+  if (threadIdx.x == 0) part[normoff + blockIdx.x] = s;
+  grid.sync();
+  // (4) ||w|| (every block, block order), v_{i+1} = w / ||w||
+  double v = 0.0;
+  for (int b = threadIdx.x; b < nb; b += 256) v += __ldcg(part + normoff + b);
+  v = block_sum<256>(v);
+  if (threadIdx.x == 0) nrm_s = sqrt(v);
+  __syncthreads();
+  const double nrm = nrm_s;
+  if (nrm == 0.0) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(err, kErrBreakdown);
+  } else {
+    const double f = 1.0 / nrm;
+    double* vn = V + (size_t)(i + 1) * n;
+    for (long t = blockIdx.x * 256L + threadIdx.x; t < n; t += stride) vn[t] = w[t] * f;
+  }
+  if (blockIdx.x != 0) return;
+  // the Givens step of column i (Utilities_gmres.C:60-88) on block 0's
+  // copies of the rotations
+  for (int j = threadIdx.x; j < i; j += 256) {
+    scs[j] = cs[j];
+    ssn[j] = sn[j];
+  }
+  if (threadIdx.x < 2) ss[threadIdx.x] = gs[i + threadIdx.x];
+  for (int j = threadIdx.x; j <= i; j += 256) h[j] = -h[j];   // back to H(k,i)
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    *norm_out = nrm;
+    h[i + 1] = nrm;
+    givens_column_s(i, h, scs, ssn, ss[0], ss[1], resid);
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j <= i + 1; j += 256) hcol[j] = h[j];
+  if (threadIdx.x == 0) {
+    cs[i] = scs[i];
+    sn[i] = ssn[i];
+    gs[i] = ss[0];
+    gs[i + 1] = ss[1];
+  }
+}
+
 static int red_grid(cdg_context* ctx, int n) {
   int g = (n + 255) / 256;
   int cap = ctx->num_sms * 4;
   if (g > cap) g = cap;
   if (g > kRedMaxBlocks) g = kRedMaxBlocks;
   return g < 1 ? 1 : g;
+}
+
+// the cooperative Gram-Schmidt step (k_cgs_coop), an option
+// (CDG_CGS_COOP=1 in the environment) for large systems: cooperative
+// launches supported, at least kCgsCoopRows rows (the served requests run on
+// several streams at once), the partials fit the reduction buffer.  Off by
+// default: measured on GB300 (32^3 Q2, 148 iterations per solve) the three
+// grid-wide barriers cost more than the two launches and the two
+// single-block sums they replace (mixed step 35.9 against 34.5 ms, FP64
+// 72.9 against 70.9 ms).
+constexpr int kCgsCoopRows = 100000;
+
+static bool cgs_coop_on(cdg_context* ctx, int n, int m) {
+  const char* e = std::getenv("CDG_CGS_COOP");
+  if (!e || e[0] != '1') return false;
+  int coop = 0;
+  if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device) != cudaSuccess)
+    return false;
+  return coop && n >= kCgsCoopRows &&
+         (size_t)(m + 2) * ctx->num_sms <= (size_t)kRedSlots * kRedMaxBlocks;
+}
+
+static int cgs_coop(cdg_context* ctx, GmresState& g, int n, int m, int i_host, const int* di) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(ctx->num_sms);
+  cfg.blockDim = dim3(256);
+  cfg.stream = ctx->stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  const cudaError_t e =
+      cudaLaunchKernelEx(&cfg, k_cgs_coop, n, g.w, g.V, i_host, di, m + 1, g.H, ctx->d_red,
+                         (m + 1) * ctx->num_sms, g.cs, g.sn, g.s, g.scal + 0, g.scal + 2,
+                         ctx->d_err);
+  ctx->launches++;
+  if (e != cudaSuccess) {
+    set_error("launch k_cgs_coop: %s", cudaGetErrorString(e));
+    return CDG_ERR_CUDA;
+  }
+  return CDG_OK;
 }
 
 int dot64(cdg_context* ctx, int n, const double* a, const double* b, double* out, int slot) {
@@ -1912,13 +2069,18 @@ static int iteration_body(cdg_context* ctx, cdg_problem* p, const cdg_solver_par
   int* di = g.dstate;
   CDG_TRY(precondition(ctx, p, s, g.V, g.Z, di, g.zcur));
   CDG_TRY(spmv_apply64(ctx, L, g.zcur, g.w));
-  const int mg = std::min(red_grid(ctx, n), ctx->num_sms * 2);
-  for (int k0 = 0; k0 < m; k0 += 32)
-    CDG_LAUNCH_PDL(ctx, k_multidot<256>, mg, 256, 0, n, g.w, g.V, k0, 0, ctx->d_red,
-               ctx->d_cnt + 1, g.H, di, m + 1);
-  CDG_LAUNCH_PDL(ctx, k_cgs_update, red_grid(ctx, n), 256, 0, n, g.w, g.V, 0, g.H, ctx->d_red,
-             ctx->d_cnt, g.cs, g.sn, g.s, g.scal + 0, g.scal + 2, di, m + 1);
-  CDG_LAUNCH_PDL(ctx, k_scale_inv, vec_grid(ctx, n), 256, 0, n, g.w, g.scal + 2, g.V, ctx->d_err, di);
+  if (g.coop) {
+    CDG_TRY(cgs_coop(ctx, g, n, m, 0, di));
+  } else {
+    const int mg = std::min(red_grid(ctx, n), ctx->num_sms * 2);
+    for (int k0 = 0; k0 < m; k0 += 32)
+      CDG_LAUNCH_PDL(ctx, k_multidot<256>, mg, 256, 0, n, g.w, g.V, k0, 0, ctx->d_red,
+                 ctx->d_cnt + 1, g.H, di, m + 1);
+    CDG_LAUNCH_PDL(ctx, k_cgs_update, red_grid(ctx, n), 256, 0, n, g.w, g.V, 0, g.H, ctx->d_red,
+               ctx->d_cnt, g.cs, g.sn, g.s, g.scal + 0, g.scal + 2, di, m + 1);
+    CDG_LAUNCH_PDL(ctx, k_scale_inv, vec_grid(ctx, n), 256, 0, n, g.w, g.scal + 2, g.V,
+                   ctx->d_err, di);
+  }
   CDG_LAUNCH_PDL(ctx, k_fgmres_iter_check, 1, 1, 0, conv_params(s), g.dstate, g.scal + 0,
              g.scal + 4, h);
   return CDG_OK;
@@ -1936,10 +2098,30 @@ static unsigned long long graph_generation(const cdg_problem* p) {
   return gen;
 }
 
+static int capture_iteration_graph(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s,
+                                   unsigned long long gen, int coop);
+
+// the captured loop with the cooperative Gram-Schmidt step where it applies;
+// a runtime that cannot capture or instantiate a cooperative launch inside
+// the conditional node gets the three kernels (remembered per context)
 static int ensure_iteration_graph(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s) {
   GmresState& g = p->gm;
   const unsigned long long gen = graph_generation(p);
-  if (g.exec && g.key_gen == gen && std::memcmp(&g.key, &s, sizeof(s)) == 0) return CDG_OK;
+  const int coop =
+      !ctx->coop_graph_failed && cgs_coop_on(ctx, p->lev[0].ndof, s.gmres_restart) ? 1 : 0;
+  if (g.exec && g.key_gen == gen && g.coop == coop && std::memcmp(&g.key, &s, sizeof(s)) == 0)
+    return CDG_OK;
+  const int rc = capture_iteration_graph(ctx, p, s, gen, coop);
+  if (rc == CDG_OK || !coop) return rc;
+  cudaGetLastError();
+  ctx->coop_graph_failed = 1;
+  return capture_iteration_graph(ctx, p, s, gen, 0);
+}
+
+static int capture_iteration_graph(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s,
+                                   unsigned long long gen, int coop) {
+  GmresState& g = p->gm;
+  g.coop = coop;
   if (g.exec) cudaGraphExecDestroy(g.exec);
   if (g.graph) cudaGraphDestroy(g.graph);
   g.exec = nullptr;
@@ -2333,6 +2515,7 @@ int fgmres(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s, cdg_sol
   if (converged(s, li, resid, 0)) return CDG_OK;
   int j = 1;
   const int vg = vec_grid(ctx, n);
+  const bool coop = s.gram_schmidt == 0 && cgs_coop_on(ctx, n, m);
   while (j <= s.max_n_iterations) {
     CDG_LAUNCH_PDL(ctx, k_scale_inv, vg, 256, 0, n, g.w, beta_d, g.V, ctx->d_err,
                    (const int*)nullptr);
@@ -2344,7 +2527,11 @@ int fgmres(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s, cdg_sol
       double* col = g.H + (size_t)i * (m + 1);
       CDG_TRY(precondition(ctx, p, s, vi, zi));
       CDG_TRY(spmv_apply64(ctx, L, zi, g.w));
-      if (s.gram_schmidt == 0) {
+      if (s.gram_schmidt == 0 && coop) {
+        // classical, the inner products, updates, norm, Givens step and
+        // normalisation in one cooperative launch
+        CDG_TRY(cgs_coop(ctx, g, n, m, i, (const int*)nullptr));
+      } else if (s.gram_schmidt == 0) {
         // classical: all inner products, then all updates and the norm
         for (int k0 = 0; k0 <= i; k0 += 32) {
           int cnt = std::min(32, i + 1 - k0);
