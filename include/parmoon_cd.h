@@ -364,6 +364,16 @@ int cdg_problem_level_info(const cdg_problem *p, int level, int *info);
  * stages through shared memory */
 int cdg_problem_operator_layout(const cdg_problem *p, int level, int *lanes,
                                 long long *slots, int *smoother_chunk);
+/* The DOF lattice of a uniform Q2 hexahedral level (no counterpart in the
+ * reference): dims[0..2] its extents in cell 0's axes (0 when the level is
+ * not a full lattice with Dirichlet data on its whole boundary, or before
+ * its first assembly); *transfer the grid transfer to the next coarser
+ * level: -1 not decided yet (decided at the first multigrid solve or
+ * transfer call after both levels are assembled, with CDG_LAT_TRANSFER=1 in
+ * the environment; otherwise the CSR matrices are used), 0 the CSR
+ * matrices, 1 the lattice kernels (tensor-product Q2 interpolation, every
+ * row of P checked against it; slower than the CSR kernels on GB300). */
+int cdg_problem_lattice(const cdg_problem *p, int level, int *dims, int *transfer);
 int cdg_problem_get_matrix(cdg_problem *p, int level, double *values);
 int cdg_problem_get_rhs(cdg_problem *p, int level, double *rhs);
 int cdg_problem_get_solution(cdg_problem *p, double *sol);

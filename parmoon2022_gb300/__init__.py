@@ -41,7 +41,8 @@ EXPORTED = [
     "cdg_hierarchy_get_dofs", "cdg_hierarchy_get_pattern", "cdg_problem_create",
     "cdg_problem_create_from_arrays", "cdg_problem_destroy", "cdg_problem_assemble",
     "cdg_problem_solve", "cdg_problem_assemble_solve", "cdg_problem_errors",
-    "cdg_problem_level_info", "cdg_problem_operator_layout", "cdg_problem_get_matrix", "cdg_problem_get_rhs",
+    "cdg_problem_level_info", "cdg_problem_operator_layout", "cdg_problem_lattice",
+    "cdg_problem_get_matrix", "cdg_problem_get_rhs",
     "cdg_problem_get_solution", "cdg_problem_set_solution", "cdg_problem_get_slots",
     "cdg_problem_apply", "cdg_problem_prolongate", "cdg_problem_restrict",
     "cdg_problem_precondition", "cdg_context_stream", "cdg_problem_time_kernel",
@@ -167,6 +168,7 @@ def lib():
             "cdg_problem_level_info": [P, ctypes.c_int, ip],
             "cdg_problem_operator_layout": [P, ctypes.c_int, ip,
                                             ctypes.POINTER(ctypes.c_longlong), ip],
+            "cdg_problem_lattice": [P, ctypes.c_int, ip, ip],
             "cdg_problem_get_matrix": [P, ctypes.c_int, dp],
             "cdg_problem_get_rhs": [P, ctypes.c_int, dp],
             "cdg_problem_get_solution": [P, dp], "cdg_problem_set_solution": [P, dp],
@@ -543,6 +545,15 @@ class ConvectionDiffusion:
         _chk(lib().cdg_problem_operator_layout(self.p, level, ctypes.byref(g), ctypes.byref(t),
                                                ctypes.byref(c)))
         return dict(lanes=g.value, slots=t.value, smoother_chunk=c.value)
+
+    def lattice(self, level=0):
+        """dims: the DOF lattice of a uniform Q2 hexahedral level (zeros where
+        there is none); transfer: the grid transfer to the next coarser level
+        (-1 undecided, 0 CSR matrices, 1 lattice kernels)."""
+        d = (ctypes.c_int * 3)()
+        t = ctypes.c_int(0)
+        _chk(lib().cdg_problem_lattice(self.p, level, d, ctypes.byref(t)))
+        return dict(dims=tuple(d), transfer=t.value)
 
     def assemble(self, a):
         _chk(lib().cdg_problem_assemble(self.p, ctypes.byref(a)))

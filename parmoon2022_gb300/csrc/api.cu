@@ -814,6 +814,17 @@ int cdg_problem_operator_layout(const cdg_problem* p, int level, int* lanes, lon
   return CDG_OK;
 }
 
+int cdg_problem_lattice(const cdg_problem* p, int level, int* dims, int* transfer) {
+  if (!p || level < 0 || level >= (int)p->lev.size() || !dims || !transfer) {
+    set_error("bad arguments");
+    return CDG_ERR_ARG;
+  }
+  const DevLevel& L = p->lev[level];
+  for (int d = 0; d < 3; ++d) dims[d] = L.st_dims[d];
+  *transfer = L.lt_state;
+  return CDG_OK;
+}
+
 int cdg_problem_level_info(const cdg_problem* p, int level, int* info) {
   if (!p || level < 0 || level >= (int)p->lev.size() || !info) { set_error("bad level"); return CDG_ERR_ARG; }
   const DevLevel& L = p->lev[level];
@@ -974,7 +985,8 @@ int cdg_problem_prolongate(cdg_problem* p, int fine, const double* xc, double* x
   DevBuf dc, df;
   CDG_TRY(h2d_tmp(dc, xc, C->ndof, p->ctx->stream));
   CDG_TRY(h2d_tmp(df, nullptr, F->ndof, p->ctx->stream));
-  CDG_TRY(prolongate64(p->ctx, *F, dc.d, df.d, 0, 0.0));
+  CDG_TRY(lattice_transfer_setup(p->ctx, *F, *C));
+  CDG_TRY(prolongate64(p->ctx, *F, *C, dc.d, df.d, 0, 0.0));
   return d2h(p->ctx, xf, df.d, (size_t)F->ndof * sizeof(double));
 }
 
@@ -985,6 +997,7 @@ int cdg_problem_restrict(cdg_problem* p, int fine, const double* dfine, double* 
   DevBuf df, dc;
   CDG_TRY(h2d_tmp(df, dfine, F->ndof, p->ctx->stream));
   CDG_TRY(h2d_tmp(dc, nullptr, C->ndof, p->ctx->stream));
+  CDG_TRY(lattice_transfer_setup(p->ctx, *F, *C));
   CDG_TRY(restrict64(p->ctx, *F, *C, df.d, dc.d));
   return d2h(p->ctx, rc, dc.d, (size_t)C->ndof * sizeof(double));
 }

@@ -203,6 +203,13 @@ struct DevLevel {
   int* st_map = nullptr;
   float* st_coef = nullptr;
   int st_zt = 0;
+  // lattice grid transfer to the next coarser level (both uniform lattices,
+  // P checked against the tensor-product Q2 interpolation): -1 not checked,
+  // 0 CSR transfers, 1 lattice kernels with lt_perm / lt_sign / lt_t2 (fine
+  // axis d runs along coarse axis lt_perm[d]; coarse half-unit coordinate
+  // lt_t2[k] + lt_sign[d] * p_d)
+  int lt_state = -1;
+  int lt_perm[3] = {0, 1, 2}, lt_sign[3] = {1, 1, 1}, lt_t2[3] = {0, 0, 0};
   int tpr32 = 0;                 // FP32 CSR lanes per row (0: rows_per_warp_hint)
   // FP32 values from the tensor-core contraction, FP64 values not formed
   // (assemble_level_tc); last_a assembles them on demand (ensure_fp64)
@@ -382,6 +389,9 @@ int mf_build_tiles(cdg_context* ctx, DevLevel& L);
 // matrix in L.mf_ae (each assembly)
 int mf_build_lattice(cdg_context* ctx, DevLevel& L);
 int mf_stencil_coef(cdg_context* ctx, DevLevel& L);
+// lattice grid transfers between F and C = the next coarser level (once per
+// pair, after both are assembled; an option: CDG_LAT_TRANSFER=1)
+int lattice_transfer_setup(cdg_context* ctx, DevLevel& F, const DevLevel& C);
 int mf_ensure(DevLevel& L);
 // the kernel form of a matrix-free application: as the tuner chose
 // (stencil, one-launch tiles or two kernels), the two-kernel product, the
@@ -441,8 +451,8 @@ int residual64(cdg_context* ctx, const DevLevel& L, const double* b, const doubl
                double* r);
 int dot64(cdg_context* ctx, int n, const double* a, const double* b, double* out,
           int slot);
-int prolongate64(cdg_context* ctx, const DevLevel& F, const double* xc, double* xf,
-                 int add_actives_only, double damp);
+int prolongate64(cdg_context* ctx, const DevLevel& F, const DevLevel& C, const double* xc,
+                 double* xf, int add_actives_only, double damp);
 int restrict64(cdg_context* ctx, const DevLevel& F, const DevLevel& C, const double* df,
                double* rc);
 int precondition(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s,

@@ -903,6 +903,305 @@ k_restrict(int nc, int nactive_c, const int* __restrict__ rp, const int* __restr
   rc[j] = s;
 }
 
+// ---------------------------------------------------------------------------
+// Grid transfers on nested uniform Q2 lattices.  The averaged child-local
+// interpolation of GridTransfer::Prolongate (GridTransfer.C:29-410) on a
+// refined uniform Q2 mesh is a tensor product of 1D interpolations: a fine
+// point at coarse half-unit coordinate U takes coarse node U/2 (U even) or,
+// inside coarse cell c = U div 4, the Q2 basis at the quarter points:
+// (3/8, 3/4, -1/8) on nodes 2c, 2c+1, 2c+2 for U = 4c+1, reversed for 4c+3.
+// The restriction is its transpose.  The kernels gather through the lattice
+// maps instead of streaming P and R; lattice_transfer_setup checks every row
+// of the level's P against these weights once.  An option (CDG_LAT_TRANSFER=1
+// in the environment): measured on GB300 (32^3 Q2 mixed step, ncu launch
+// list) the gathers and per-tap index arithmetic take 21.9 us per
+// restriction and 16.1 us per prolongation against 6.2 and 7.8 us for the
+// CSR kernels, which stream each row's few entries.
+// ---------------------------------------------------------------------------
+struct LatMap {
+  int lf[3], lc[3];            // fine / coarse lattice extents (own axes)
+  int perm[3], sign[3], t2[3];
+  // per fine axis d: the coarse axis's half-unit offset and lattice stride
+  int t2f[3], csf[3];
+};
+
+// the coarse taps of half-unit coordinate U along one axis
+__device__ __forceinline__ int lat_taps(int U, int* q, double* w) {
+  if ((U & 1) == 0) {
+    q[0] = U >> 1;
+    w[0] = 1.0;
+    q[1] = q[2] = q[0];
+    w[1] = w[2] = 0.0;
+    return 1;
+  }
+  const int c2 = (U >> 2) * 2;
+  q[0] = c2;
+  q[1] = c2 + 1;
+  q[2] = c2 + 2;
+  const bool first = (U & 3) == 1;
+  w[0] = first ? 0.375 : -0.125;
+  w[1] = 0.75;
+  w[2] = first ? -0.125 : 0.375;
+  return 3;
+}
+
+// fine lattice point idx: per fine axis d its taps (count, coarse node,
+// weight); the coarse lattice index of a tap is sum_d q_d * csf[d]
+__device__ __forceinline__ void lat_fine_taps(const LatMap& M, long idx, int* nt, int (*q)[3],
+                                              double (*w)[3]) {
+  const int p[3] = {(int)(idx % M.lf[0]), (int)((idx / M.lf[0]) % M.lf[1]),
+                    (int)(idx / ((long)M.lf[0] * M.lf[1]))};
+#pragma unroll
+  for (int d = 0; d < 3; ++d) nt[d] = lat_taps(M.t2f[d] + M.sign[d] * p[d], q[d], w[d]);
+}
+
+// tap j of one axis at half-unit coordinate U: coarse node and weight
+// (prolongation: 1 tap at an even U, else the three quarter-point weights)
+template <typename T>
+__device__ __forceinline__ void lat_prolong_tap(int U, int j, int& q, T& w) {
+  if ((U & 1) == 0) {
+    q = U >> 1;
+    w = (T)1;
+    return;
+  }
+  q = (U >> 2) * 2 + j;
+  const bool first = (U & 3) == 1;
+  w = j == 1 ? (T)0.75 : ((j == 0) == first ? (T)0.375 : (T)-0.125);
+}
+
+// x_f[i] += damp * (P x_c)[i] on fine actives, or x_f = P x_c (add == 0);
+// a thread per fine point, its 1 to 27 taps decoded from a flat index
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_lat_prolong(LatMap M, int nactive_f, const int* __restrict__ mapf, const int* __restrict__ mapc,
+              const T* __restrict__ xc, T* __restrict__ xf, T damp, int add) {
+  pdl_enter();
+  const long nf = (long)M.lf[0] * M.lf[1] * M.lf[2];
+  const long idx = blockIdx.x * 256L + threadIdx.x;
+  if (idx >= nf) return;
+  const int row = __ldg(mapf + idx);
+  if (add && row >= nactive_f) return;
+  const int p0 = (int)(idx % M.lf[0]), p1 = (int)((idx / M.lf[0]) % M.lf[1]),
+            p2 = (int)(idx / ((long)M.lf[0] * M.lf[1]));
+  const int U0 = M.t2f[0] + M.sign[0] * p0, U1 = M.t2f[1] + M.sign[1] * p1,
+            U2 = M.t2f[2] + M.sign[2] * p2;
+  const int n0 = (U0 & 1) ? 3 : 1, n1 = (U1 & 1) ? 3 : 1, n2 = (U2 & 1) ? 3 : 1;
+  const int nt = n0 * n1 * n2;
+  T s = 0;
+#pragma unroll 3
+  for (int t = 0; t < nt; ++t) {
+    const int a = t % n0, r = t / n0, b = r % n1, c = r / n1;
+    int qa, qb, qc;
+    T wa, wb, wc;
+    lat_prolong_tap<T>(U0, a, qa, wa);
+    lat_prolong_tap<T>(U1, b, qb, wb);
+    lat_prolong_tap<T>(U2, c, qc, wc);
+    const long ci = (long)qa * M.csf[0] + (long)qb * M.csf[1] + (long)qc * M.csf[2];
+    s += ((wc * wb) * wa) * xc[__ldg(mapc + ci)];
+  }
+  if (!add) xf[row] = s;
+  else xf[row] += damp * s;
+}
+
+// r_c = P^T d_f on every coarse lattice point; coarse non-actives zeroed
+// when mask.  Along its coarse axis a node q takes the fine points at
+// half-unit offsets -3, -1, 0, 1, 3 (q even: weights -1/8, 3/8, 1, 3/8,
+// -1/8) or -1, 0, 1 (q odd: 3/4, 1, 3/4); kLatLanes lanes per coarse point
+// share its up to 125 taps and add their sums by shuffles
+constexpr int kLatLanes = 8;
+
+template <typename T>
+__device__ __forceinline__ int lat_restrict_tap(int qk, int j, T& w) {
+  if (qk & 1) {
+    w = j == 1 ? (T)1 : (T)0.75;
+    return j - 1;
+  }
+  const int off = j == 0 ? -3 : (j == 1 ? -1 : (j == 2 ? 0 : (j == 3 ? 1 : 3)));
+  w = j == 2 ? (T)1 : ((j == 1 || j == 3) ? (T)0.375 : (T)-0.125);
+  return off;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_lat_restrict(LatMap M, int nactive_c, const int* __restrict__ mapf,
+               const int* __restrict__ mapc, const T* __restrict__ df, T* __restrict__ rc,
+               int mask) {
+  pdl_enter();
+  const long nc = (long)M.lc[0] * M.lc[1] * M.lc[2];
+  const long gt = blockIdx.x * 256L + threadIdx.x;
+  const long idx = gt / kLatLanes;
+  const int lane = (int)(gt % kLatLanes);
+  const bool live = idx < nc;
+  int row = 0;
+  bool act = false;
+  int qd[3] = {0, 0, 0};
+  if (live) {
+    row = __ldg(mapc + idx);
+    act = !(mask && row >= nactive_c);
+    const int q[3] = {(int)(idx % M.lc[0]), (int)((idx / M.lc[0]) % M.lc[1]),
+                      (int)(idx / ((long)M.lc[0] * M.lc[1]))};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const int k = M.perm[d];
+      qd[d] = k == 0 ? q[0] : (k == 1 ? q[1] : q[2]);
+    }
+  }
+  T s = 0;
+  if (live && act) {
+    const int n0 = (qd[0] & 1) ? 3 : 5, n1 = (qd[1] & 1) ? 3 : 5, n2 = (qd[2] & 1) ? 3 : 5;
+    const int nt = n0 * n1 * n2;
+    for (int t = lane; t < nt; t += kLatLanes) {
+      const int a = t % n0, r = t / n0, b = r % n1, c = r / n1;
+      T wa, wb, wc;
+      const int f0 = M.sign[0] * (2 * qd[0] + lat_restrict_tap<T>(qd[0], a, wa) - M.t2f[0]);
+      const int f1 = M.sign[1] * (2 * qd[1] + lat_restrict_tap<T>(qd[1], b, wb) - M.t2f[1]);
+      const int f2 = M.sign[2] * (2 * qd[2] + lat_restrict_tap<T>(qd[2], c, wc) - M.t2f[2]);
+      if (f0 < 0 || f0 >= M.lf[0] || f1 < 0 || f1 >= M.lf[1] || f2 < 0 || f2 >= M.lf[2])
+        continue;
+      const long fi = ((long)f2 * M.lf[1] + f1) * M.lf[0] + f0;
+      s += ((wc * wb) * wa) * df[__ldg(mapf + fi)];
+    }
+  }
+#pragma unroll
+  for (int o = kLatLanes / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, kLatLanes);
+  if (live && lane == 0) rc[row] = act ? s : (T)0;
+}
+
+// every row of P against the lattice weights: the same coarse columns, the
+// values to 1e-12 (P drops no lattice tap: none is below its 1e-14 cut)
+__global__ void __launch_bounds__(256)
+k_lat_check(LatMap M, const int* __restrict__ mapf, const int* __restrict__ mapc,
+            const int* __restrict__ prp, const int* __restrict__ pcol,
+            const double* __restrict__ pval, int* bad) {
+  const long nf = (long)M.lf[0] * M.lf[1] * M.lf[2];
+  const long idx = blockIdx.x * 256L + threadIdx.x;
+  if (idx >= nf) return;
+  const int row = mapf[idx];
+  int nt[3], q[3][3];
+  double w[3][3];
+  lat_fine_taps(M, idx, nt, q, w);
+  const int e0 = prp[row], e1 = prp[row + 1];
+  if (e1 - e0 != nt[0] * nt[1] * nt[2]) {
+    atomicOr(bad, 1);
+    return;
+  }
+  for (int e = e0; e < e1; ++e) {
+    bool found = false;
+    for (int c = 0; c < nt[2] && !found; ++c)
+      for (int b = 0; b < nt[1] && !found; ++b)
+        for (int a = 0; a < nt[0] && !found; ++a) {
+          const int g = mapc[(long)q[2][c] * M.csf[2] + (long)q[1][b] * M.csf[1] +
+                             (long)q[0][a] * M.csf[0]];
+          if (g != pcol[e]) continue;
+          found = true;
+          if (fabs(pval[e] - w[2][c] * w[1][b] * w[0][a]) > 1e-12) atomicOr(bad, 2);
+        }
+    if (!found) atomicOr(bad, 4);
+  }
+}
+
+static LatMap lat_map(const DevLevel& F, const DevLevel& C) {
+  LatMap M;
+  for (int d = 0; d < 3; ++d) {
+    M.lf[d] = F.st_dims[d];
+    M.lc[d] = C.st_dims[d];
+    M.perm[d] = F.lt_perm[d];
+    M.sign[d] = F.lt_sign[d];
+    M.t2[d] = F.lt_t2[d];
+  }
+  const int cst[3] = {1, C.st_dims[0], C.st_dims[0] * C.st_dims[1]};
+  for (int d = 0; d < 3; ++d) {
+    M.t2f[d] = F.lt_t2[F.lt_perm[d]];
+    M.csf[d] = cst[F.lt_perm[d]];
+  }
+  return M;
+}
+
+// The fine points 0, 2 e_0, 2 e_1, 2 e_2 of F's lattice coincide with coarse
+// nodes (their P rows hold one entry, 1): their coarse lattice coordinates
+// give each fine axis's coarse axis, direction and offset; then every row of
+// P is checked on the device.
+int lattice_transfer_setup(cdg_context* ctx, DevLevel& F, const DevLevel& C) {
+  if (F.lt_state >= 0) return CDG_OK;
+  const char* e = std::getenv("CDG_LAT_TRANSFER");
+  if (!e || e[0] != '1') return CDG_OK;
+  if (F.mf_geo < 0 || C.mf_geo < 0) return CDG_OK;   // lattices not looked for yet
+  F.lt_state = 0;
+  if (!F.st_dims[0] || !C.st_dims[0] || !F.P_rp || !F.P_val) return CDG_OK;
+  const int* lf = F.st_dims;
+  const int* lc = C.st_dims;
+  const long ncp = (long)lc[0] * lc[1] * lc[2];
+  std::vector<int> cmap(ncp);
+  CDG_CUDA(cudaMemcpyAsync(cmap.data(), C.st_map, ncp * sizeof(int), cudaMemcpyDeviceToHost,
+                           ctx->stream));
+  const long probe[4] = {0, 2, 2L * lf[0], 2L * lf[0] * lf[1]};
+  int g[4], rp[8], col[4];
+  double val[4];
+  for (int k = 0; k < 4; ++k)
+    CDG_CUDA(cudaMemcpyAsync(&g[k], F.st_map + probe[k], sizeof(int), cudaMemcpyDeviceToHost,
+                             ctx->stream));
+  CDG_CUDA(cudaStreamSynchronize(ctx->stream));
+  for (int k = 0; k < 4; ++k) {
+    CDG_CUDA(cudaMemcpyAsync(&rp[2 * k], F.P_rp + g[k], 2 * sizeof(int), cudaMemcpyDeviceToHost,
+                             ctx->stream));
+  }
+  CDG_CUDA(cudaStreamSynchronize(ctx->stream));
+  for (int k = 0; k < 4; ++k) {
+    if (rp[2 * k + 1] - rp[2 * k] != 1) return CDG_OK;
+    CDG_CUDA(cudaMemcpyAsync(&col[k], F.P_col + rp[2 * k], sizeof(int), cudaMemcpyDeviceToHost,
+                             ctx->stream));
+    CDG_CUDA(cudaMemcpyAsync(&val[k], F.P_val + rp[2 * k], sizeof(double),
+                             cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  CDG_CUDA(cudaStreamSynchronize(ctx->stream));
+  int qc[4][3];
+  for (int k = 0; k < 4; ++k) {
+    if (std::fabs(val[k] - 1.0) > 1e-12) return CDG_OK;
+    long at = -1;
+    for (long i = 0; i < ncp && at < 0; ++i)
+      if (cmap[i] == col[k]) at = i;
+    if (at < 0) return CDG_OK;
+    qc[k][0] = (int)(at % lc[0]);
+    qc[k][1] = (int)((at / lc[0]) % lc[1]);
+    qc[k][2] = (int)(at / ((long)lc[0] * lc[1]));
+  }
+  int used = 0;
+  for (int d = 0; d < 3; ++d) {
+    int axis = -1, sg = 0;
+    for (int k = 0; k < 3; ++k) {
+      const int dq = qc[d + 1][k] - qc[0][k];
+      if (dq == 0) continue;
+      if ((dq != 1 && dq != -1) || axis >= 0) return CDG_OK;
+      axis = k;
+      sg = dq;
+    }
+    if (axis < 0 || (used >> axis) & 1) return CDG_OK;
+    used |= 1 << axis;
+    if (lf[d] != 2 * lc[axis] - 1) return CDG_OK;
+    F.lt_perm[d] = axis;
+    F.lt_sign[d] = sg;
+  }
+  for (int k = 0; k < 3; ++k) F.lt_t2[k] = 2 * qc[0][k];
+  int* bad = nullptr;
+  CDG_CUDA(cudaMalloc(&bad, sizeof(int)));
+  int hb = 1;
+  cudaError_t err = cudaMemsetAsync(bad, 0, sizeof(int), ctx->stream);
+  const long nf = (long)lf[0] * lf[1] * lf[2];
+  if (err == cudaSuccess) {
+    k_lat_check<<<(unsigned)((nf + 255) / 256), 256, 0, ctx->stream>>>(
+        lat_map(F, C), F.st_map, C.st_map, F.P_rp, F.P_col, F.P_val, bad);
+    ++ctx->launches;
+    err = cudaGetLastError();
+  }
+  if (err == cudaSuccess) err = cudaMemcpyAsync(&hb, bad, sizeof(int), cudaMemcpyDeviceToHost,
+                                                ctx->stream);
+  if (err == cudaSuccess) err = cudaStreamSynchronize(ctx->stream);
+  cudaFree(bad);
+  CDG_CUDA(err);
+  F.lt_state = hb == 0 ? 1 : 0;
+  return CDG_OK;
+}
+
 template <typename T>
 __global__ void k_coarse_init(int n, int na, const T* __restrict__ b, T* __restrict__ x) {
   pdl_enter();
@@ -1426,8 +1725,30 @@ static int defect(cdg_context* ctx, DevLevel& L) {
 // update_solution_in_finer_grid: fine.sol += damp * P coarse.sol on actives
 template <typename T>
 static int prolong_correct(cdg_context* ctx, DevLevel& F, DevLevel& C, T damp) {
+  if (F.lt_state == 1) {
+    const long nf = (long)F.st_dims[0] * F.st_dims[1] * F.st_dims[2];
+    CDG_LAUNCH_PDL(ctx, k_lat_prolong<T>, (int)((nf + 255) / 256), 256, 0, lat_map(F, C),
+                   F.nactive, F.st_map, C.st_map, (const T*)C.mg_sol, (T*)F.mg_sol, damp, 1);
+    return CDG_OK;
+  }
   CDG_LAUNCH_PDL(ctx, (k_prolong<T, 2>), grid_for<int>((long)F.ndof * 2, 256), 256, 0, F.ndof,
              F.nactive, F.P_rp, F.P_col, Prec<T>::P(F), (const T*)C.mg_sol, (T*)F.mg_sol, damp, 1);
+  return CDG_OK;
+}
+
+// r_c = R d_f with coarse non-actives zeroed (the multigrid's restriction)
+template <typename T>
+static int restrict_defect(cdg_context* ctx, DevLevel& F, DevLevel& C) {
+  if (F.lt_state == 1) {
+    const long nc = (long)C.st_dims[0] * C.st_dims[1] * C.st_dims[2];
+    CDG_LAUNCH_PDL(ctx, k_lat_restrict<T>, (int)((nc * kLatLanes + 255) / 256), 256, 0,
+                   lat_map(F, C),
+                   C.nactive, F.st_map, C.st_map, (const T*)F.mg_def, (T*)C.mg_rhs, 1);
+    return CDG_OK;
+  }
+  CDG_LAUNCH_PDL(ctx, (k_restrict<T, 8>), grid_for<int>((long)C.ndof * 8, 256), 256, 0,
+             C.ndof, C.nactive, F.R_rp, F.R_col, Prec<T>::R(F), (const T*)F.mg_def,
+             (T*)C.mg_rhs, 1);
   return CDG_OK;
 }
 
@@ -1556,9 +1877,7 @@ static int mg_cycle(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s
         if (read_start)
           CDG_CUDA(cudaMemsetAsync(C.mg_sol, 0, (size_t)C.ndof * sizeof(T), ctx->stream));
         C.mg_visited = false;   // zero start iterate again: shortcut valid
-        CDG_LAUNCH_PDL(ctx, (k_restrict<T, 8>), grid_for<int>((long)C.ndof * 8, 256), 256, 0,
-                   C.ndof, C.nactive, L.R_rp, L.R_col, Prec<T>::R(L), (const T*)L.mg_def,
-                   (T*)C.mg_rhs, 1);
+        CDG_TRY(restrict_defect<T>(ctx, L, C));
         level -= 1;
       } else if (dir == kUp) {
         CDG_TRY(prolong_correct<T>(ctx, lv(level + 1), L, cdamp));
@@ -1798,6 +2117,8 @@ int prepare_solver(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s)
     set_error("multigrid_n_levels=%d but the problem has %d levels", nl, (int)p->lev.size());
     return CDG_ERR_ARG;
   }
+  for (int k = 0; k + 1 < nl; ++k)
+    CDG_TRY(lattice_transfer_setup(ctx, p->lev[k], p->lev[k + 1]));
   const int elem = s.precision == 1 ? (int)sizeof(float) : (int)sizeof(double);
   // FP64 values of FP32-only levels where this solve needs them: every level
   // of an FP64 multigrid, the coarse inverse's level otherwise
@@ -1837,8 +2158,14 @@ int precondition(cdg_context* ctx, cdg_problem* p, const cdg_solver_params& s, c
   return CDG_OK;
 }
 
-int prolongate64(cdg_context* ctx, const DevLevel& F, const double* xc, double* xf,
-                 int add_actives_only, double damp) {
+int prolongate64(cdg_context* ctx, const DevLevel& F, const DevLevel& C, const double* xc,
+                 double* xf, int add_actives_only, double damp) {
+  if (F.lt_state == 1) {
+    const long nf = (long)F.st_dims[0] * F.st_dims[1] * F.st_dims[2];
+    CDG_LAUNCH_PDL(ctx, k_lat_prolong<double>, (int)((nf + 255) / 256), 256, 0, lat_map(F, C),
+                   F.nactive, F.st_map, C.st_map, xc, xf, damp, add_actives_only);
+    return CDG_OK;
+  }
   CDG_LAUNCH_PDL(ctx, (k_prolong<double, 2>), grid_for<int>((long)F.ndof * 2, 256), 256, 0, F.ndof,
              F.nactive, F.P_rp, F.P_col, F.P_val, xc, xf, damp, add_actives_only);
   return CDG_OK;
@@ -1846,6 +2173,13 @@ int prolongate64(cdg_context* ctx, const DevLevel& F, const double* xc, double* 
 
 int restrict64(cdg_context* ctx, const DevLevel& F, const DevLevel& C, const double* df,
                double* rc) {
+  if (F.lt_state == 1) {
+    const long nc = (long)C.st_dims[0] * C.st_dims[1] * C.st_dims[2];
+    CDG_LAUNCH_PDL(ctx, k_lat_restrict<double>, (int)((nc * kLatLanes + 255) / 256), 256, 0,
+                   lat_map(F, C),
+                   C.nactive, F.st_map, C.st_map, df, rc, 0);
+    return CDG_OK;
+  }
   CDG_LAUNCH_PDL(ctx, (k_restrict<double, 8>), grid_for<int>((long)C.ndof * 8, 256), 256, 0,
              C.ndof, C.nactive, F.R_rp, F.R_col, F.R_val, df, rc, 0);
   return CDG_OK;
