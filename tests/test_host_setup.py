@@ -34,6 +34,21 @@ def test_mesh_dofs_pattern_bit_exact(built, dim, order, nref, nmask):
         assert np.array_equal(rp1, rp2) and np.array_equal(c1, c2)
 
 
+@pytest.mark.parametrize("dim,order,nref", [(2, 1, 6), (3, 2, 5)])
+def test_config_size_numbering_bit_exact(built, dim, order, nref):
+    # the workloads' finest levels (64^2 Q1: 4,225 DOFs; 32^3 Q2: 274,625
+    # DOFs, 16,974,593 entries) against the oracle's marker algorithm
+    h = pg.Hierarchy(dim, order, nref, n_levels=1)
+    o = po.Problem(po.make_config(dim, order, nref, po.EX_SINE), 1)
+    assert h.info(0)["ndof"] == o.info(0)["ndof"]
+    assert h.info(0)["nactive"] == o.info(0)["nactive"]
+    assert np.array_equal(h.mesh(0), o.mesh(0))
+    assert np.array_equal(h.dofs(0), o.dofs(0) if hasattr(o, "dofs") else o.gdof(0))
+    rp1, c1 = h.pattern(0)
+    rp2, c2 = o.structure(0)
+    assert np.array_equal(rp1, rp2) and np.array_equal(c1, c2)
+
+
 def test_config_sizes(built):
     # 64x64 Q1: 4225 DOFs, 3969 active, nnz (3N+1)^2 (configs' CD2D case)
     h = pg.Hierarchy(2, 1, 6)
