@@ -1018,6 +1018,96 @@ static int nloc_of(int shape, int dim, int p) {
   return dim == 2 ? (p + 1) * (p + 1) : (p + 1) * (p + 1) * (p + 1);
 }
 
+/* compute_various_numbers (FESpace.C:1863-2099), no hanging nodes: the
+ * marks left by the cell loop become the global numbers (inner classes,
+ * then each boundary-condition type, then Dirichlet, each in the order of
+ * its first local DOF); gn is taken over by L */
+static int number_classes(int *gn, int sumlocdof, const int *bub, level_t *L) {
+  int total_bub = 0;
+  for (int i = 0; i < N_BC_TYPES; ++i) total_bub += bub[i];
+  int boundmark[N_BC_TYPES];
+  int l = FIRSTMARK;
+  for (int i = 0; i < N_BC_TYPES; ++i) {
+    l -= bub[i];
+    boundmark[i] = l;
+  }
+  int innermark = l;
+  int slavemark = l - sumlocdof;
+  int dirichlet_counter = 0;
+  int boundcounter[N_BC_TYPES];
+  l = 0;
+  for (int i = 0; i < N_BC_TYPES; ++i) {
+    l += bub[i];
+    boundcounter[i] = l;
+  }
+  int count = l;
+  int n_dirichlet = 0, n_inner = 0, n_bound[N_BC_TYPES] = {0};
+  for (int i = 0; i < sumlocdof; ++i) {
+    int v = gn[i];
+    if (v < -1) {
+      if (v <= slavemark) FAIL("hanging node in a conforming mesh");
+      if (v <= innermark) {
+        gn[i] = count++;
+        n_inner++;
+        continue;
+      }
+      int m = N_BC_TYPES - 1;
+      for (; m >= 0; m--) {
+        if (v <= boundmark[m]) {
+          gn[i] = boundcounter[m]++;
+          n_bound[m]++;
+          m = -2;
+          break;
+        }
+      }
+      if (m != -2 && v <= FIRSTMARK) {
+        gn[i] = dirichlet_counter++;
+        n_dirichlet++;
+      }
+    } else if (v >= 0) {
+      gn[i] = gn[v];
+    } else {
+      FAIL("unhandled local dof");
+    }
+  }
+  int nb = 0;
+  for (int i = 0; i < N_BC_TYPES; ++i) nb += n_bound[i];
+  int dirichlet_offset = n_inner + nb;
+  int inner_offset = -total_bub;
+  int boundoffset[N_BC_TYPES];
+  l = n_inner;
+  for (int i = 0, m = 0; i < N_BC_TYPES; ++i) {
+    m += bub[i];
+    boundoffset[i] = l - m;
+    l += n_bound[i];
+  }
+  int dirichletmark = bub[0];
+  l = bub[0];
+  for (int i = 0; i < N_BC_TYPES - 1; ++i) {
+    l += bub[i + 1];
+    boundmark[i] = l;
+  }
+  boundmark[N_BC_TYPES - 1] = l;
+  for (int i = 0; i < sumlocdof; ++i) {
+    int v = gn[i];
+    if (v < dirichletmark) {
+      gn[i] += dirichlet_offset;
+    } else if (v < boundmark[N_BC_TYPES - 1]) {
+      for (int m = 0; m < N_BC_TYPES; ++m)
+        if (v < boundmark[m]) {
+          gn[i] += boundoffset[m];
+          break;
+        }
+    } else {
+      gn[i] += inner_offset;
+    }
+  }
+  L->gdof = gn;
+  L->nactive = n_inner + nb;
+  L->ndof = n_inner + nb + n_dirichlet;
+  return 0;
+}
+
 static int build_space(const orc_config *cfg, level_t *L, int nref) {
   int dim = cfg->dim, p = cfg->order, nv = L->nv;
   int nj = dim == 2 ? 4 : 6;
@@ -1121,90 +1211,166 @@ static int build_space(const orc_config *cfg, level_t *L, int nref) {
   free(neigh);
   free(bcomp);
 
-  /* compute_various_numbers (FESpace.C:1863-2099), no hanging nodes */
-  int total_bub = 0;
-  for (int i = 0; i < N_BC_TYPES; ++i) total_bub += bub[i];
-  int boundmark[N_BC_TYPES];
-  int l = FIRSTMARK;
-  for (int i = 0; i < N_BC_TYPES; ++i) {
-    l -= bub[i];
-    boundmark[i] = l;
-  }
-  int innermark = l;
-  int sumlocdof = nc * nloc;
-  int slavemark = l - sumlocdof;
-  int dirichlet_counter = 0;
-  int boundcounter[N_BC_TYPES];
-  l = 0;
-  for (int i = 0; i < N_BC_TYPES; ++i) {
-    l += bub[i];
-    boundcounter[i] = l;
-  }
-  int count = l;
-  int n_dirichlet = 0, n_inner = 0, n_bound[N_BC_TYPES] = {0};
-  for (int i = 0; i < sumlocdof; ++i) {
-    int v = gn[i];
-    if (v < -1) {
-      if (v <= slavemark) FAIL("hanging node in a conforming mesh");
-      if (v <= innermark) {
-        gn[i] = count++;
-        n_inner++;
-        continue;
-      }
-      int m = N_BC_TYPES - 1;
-      for (; m >= 0; m--) {
-        if (v <= boundmark[m]) {
-          gn[i] = boundcounter[m]++;
-          n_bound[m]++;
-          m = -2;
+  return number_classes(gn, nc * nloc, bub, L);
+}
+
+/* Tetrahedra: the face-by-face identification of TFESpace3D::ConstructSpace
+ * (FESpace3D.C:186-420) on the caller's mesh.  Two cells share a face when
+ * the face's three vertex positions coincide (found through a hash of the
+ * sorted positions); a face without a neighbour is a boundary face of the
+ * unit cube, its component from its centroid; the DOFs of face j are the
+ * local DOFs whose barycentric coordinate j vanishes (the JointDOF lists of
+ * C_T_P1_3D / C_T_P2_3D, FE_C_T_P2_3D.h); a neighbour's DOF is identified by
+ * position.  P1 and P2 tetrahedra have no cell-inner DOFs.  The order in
+ * which a face's DOFs are identified does not change the result: the
+ * numbers go to the classes in the order of their first local DOF, and a
+ * boundary DOF keeps the lowest boundary-condition type it meets. */
+static const int TET_FACE_OPP[4][3] = {{1, 2, 3}, {0, 2, 3}, {0, 1, 3}, {0, 1, 2}};
+
+static void tet_face_key(const double *cv, int j, double *key) {
+  double v[3][3];
+  for (int m = 0; m < 3; ++m)
+    for (int a = 0; a < 3; ++a) v[m][a] = cv[TET_FACE_OPP[j][m] * 3 + a];
+  for (int i = 0; i < 2; ++i)
+    for (int k = 0; k < 2 - i; ++k) {
+      int gt = 0;
+      for (int a = 0; a < 3; ++a)
+        if (v[k][a] != v[k + 1][a]) {
+          gt = v[k][a] > v[k + 1][a];
           break;
         }
-      }
-      if (m != -2 && v <= FIRSTMARK) {
-        gn[i] = dirichlet_counter++;
-        n_dirichlet++;
-      }
-    } else if (v >= 0) {
-      gn[i] = gn[v];
-    } else {
-      FAIL("unhandled local dof");
-    }
-  }
-  int nb = 0;
-  for (int i = 0; i < N_BC_TYPES; ++i) nb += n_bound[i];
-  int dirichlet_offset = n_inner + nb;
-  int inner_offset = -total_bub;
-  int boundoffset[N_BC_TYPES];
-  l = n_inner;
-  for (int i = 0, m = 0; i < N_BC_TYPES; ++i) {
-    m += bub[i];
-    boundoffset[i] = l - m;
-    l += n_bound[i];
-  }
-  int dirichletmark = bub[0];
-  l = bub[0];
-  for (int i = 0; i < N_BC_TYPES - 1; ++i) {
-    l += bub[i + 1];
-    boundmark[i] = l;
-  }
-  boundmark[N_BC_TYPES - 1] = l;
-  for (int i = 0; i < sumlocdof; ++i) {
-    int v = gn[i];
-    if (v < dirichletmark) {
-      gn[i] += dirichlet_offset;
-    } else if (v < boundmark[N_BC_TYPES - 1]) {
-      for (int m = 0; m < N_BC_TYPES; ++m)
-        if (v < boundmark[m]) {
-          gn[i] += boundoffset[m];
-          break;
+      if (gt)
+        for (int a = 0; a < 3; ++a) {
+          double t = v[k][a];
+          v[k][a] = v[k + 1][a];
+          v[k + 1][a] = t;
         }
-    } else {
-      gn[i] += inner_offset;
+    }
+  memcpy(key, v, 9 * sizeof(double));
+}
+
+static unsigned long long hash_bytes(const void *p, size_t n) {
+  const unsigned char *b = (const unsigned char *)p;
+  unsigned long long h = 1469598103934665603ULL;
+  for (size_t i = 0; i < n; ++i) {
+    h ^= b[i];
+    h *= 1099511628211ULL;
+  }
+  return h;
+}
+
+static int build_space_tet(const orc_config *cfg, level_t *L) {
+  const int p = cfg->order, nc = L->ncells, nloc = L->nloc;
+  int fd[4][MAXLOC], nfd = 0;
+  for (int j = 0; j < 4; ++j) {
+    int cnt = 0;
+    for (int k = 0; k < nloc; ++k) {
+      double r[3];
+      local_dof_ref_s(2, 3, p, k, r);
+      const double lam[4] = {1.0 - r[0] - r[1] - r[2], r[0], r[1], r[2]};
+      if (fabs(lam[j]) < 1e-14) fd[j][cnt++] = k;
+    }
+    nfd = cnt;
+  }
+  const size_t nf = (size_t)nc * 4;
+  size_t cap = 1;
+  while (cap < 2 * nf) cap <<= 1;
+  int *tab = (int *)malloc(sizeof(int) * cap);
+  int *neigh = (int *)malloc(sizeof(int) * nf);
+  int *bcomp = (int *)malloc(sizeof(int) * nf);
+  for (size_t i = 0; i < cap; ++i) tab[i] = -1;
+  double key[9], key2[9];
+  for (int c = 0; c < nc; ++c)
+    for (int j = 0; j < 4; ++j) {
+      const int f = c * 4 + j;
+      neigh[f] = -1;
+      bcomp[f] = -1;
+      tet_face_key(L->verts + (size_t)c * 12, j, key);
+      size_t h = (size_t)(hash_bytes(key, sizeof key) & (cap - 1));
+      while (tab[h] >= 0) {
+        const int g = tab[h];
+        tet_face_key(L->verts + (size_t)(g / 4) * 12, g % 4, key2);
+        if (memcmp(key, key2, sizeof key) == 0) break;
+        h = (h + 1) & (cap - 1);
+      }
+      if (tab[h] < 0) {
+        tab[h] = f;
+      } else {
+        const int g = tab[h];
+        if (neigh[g] >= 0) FAIL("a face shared by three cells");
+        neigh[g] = c;
+        neigh[f] = g / 4;
+      }
+    }
+  free(tab);
+  int bub[N_BC_TYPES] = {0};
+  for (size_t f = 0; f < nf; ++f) {
+    if (neigh[f] >= 0) continue;
+    const double *cv = L->verts + (f / 4) * 12;
+    double ctr[3] = {0, 0, 0};
+    for (int m = 0; m < 3; ++m)
+      for (int a = 0; a < 3; ++a) ctr[a] += cv[TET_FACE_OPP[f % 4][m] * 3 + a] / 3.0;
+    bcomp[f] = boundary_comp(3, ctr);
+    if (bcomp[f] < 0) FAIL("a face without a neighbour inside the cube");
+    bub[bc_type(cfg, bcomp[f])] += nfd;
+  }
+  int counters[N_BC_TYPES + 1];
+  counters[0] = FIRSTMARK + 1;
+  for (int i = 0; i < N_BC_TYPES; ++i) counters[i + 1] = counters[i] - bub[i];
+  int *counter = &counters[N_BC_TYPES];
+  int *gn = (int *)malloc(sizeof(int) * nc * nloc);
+  for (int i = 0; i < nc * nloc; ++i) gn[i] = -1;
+  for (int c = 0; c < nc; ++c) {
+    const double *cv = L->verts + (size_t)c * 12;
+    const int I0 = c * nloc;
+    for (int j = 0; j < 4; ++j) {
+      const int f = c * 4 + j;
+      if (neigh[f] < 0) {
+        const int t = bc_type(cfg, bcomp[f]);
+        for (int m = 0; m < nfd; ++m) map_single_boundary_dof(gn, I0 + fd[j][m], &counters[t]);
+      } else if (neigh[f] > c) {
+        const int n = neigh[f];
+        const double *nvv = L->verts + (size_t)n * 12;
+        const int I1 = n * nloc;
+        for (int m = 0; m < nfd; ++m) {
+          double x0[3], x1[3];
+          dof_position_s(2, 3, p, cv, fd[j][m], x0);
+          int found = -1;
+          for (int k = 0; k < nloc && found < 0; ++k) {
+            dof_position_s(2, 3, p, nvv, k, x1);
+            if (fabs(x0[0] - x1[0]) + fabs(x0[1] - x1[1]) + fabs(x0[2] - x1[2]) < 1e-12)
+              found = k;
+          }
+          if (found < 0) FAIL("neighbour DOF not found");
+          if (map_single_dof(gn, I0 + fd[j][m], I1 + found, counter)) return -1;
+        }
+      }
     }
   }
-  L->gdof = gn;
-  L->nactive = n_inner + nb;
-  L->ndof = n_inner + nb + n_dirichlet;
+  free(neigh);
+  free(bcomp);
+  return number_classes(gn, nc * nloc, bub, L);
+}
+
+int orc_marker_numbering(const orc_config *cfg, int ncells, const double *verts, int *gdof,
+                         int *ndof, int *nactive) {
+  if (!cfg->tetra || cfg->dim != 3 || (cfg->order != 1 && cfg->order != 2) || ncells < 1 ||
+      !verts || !gdof || !ndof || !nactive) {
+    snprintf(g_err, sizeof g_err,
+             "tetrahedral P1/P2 meshes only (orc_create numbers its own hexahedra)");
+    return -1;
+  }
+  level_t L;
+  memset(&L, 0, sizeof L);
+  L.nv = 4;
+  L.nloc = nloc_of(2, 3, cfg->order);
+  L.ncells = ncells;
+  L.verts = (double *)verts;   /* read only */
+  if (build_space_tet(cfg, &L)) return -1;
+  memcpy(gdof, L.gdof, sizeof(int) * (size_t)ncells * L.nloc);
+  *ndof = L.ndof;
+  *nactive = L.nactive;
+  free(L.gdof);
   return 0;
 }
 

@@ -141,6 +141,13 @@ int orc_solve(orc_problem *p, const orc_solver_config *s, int *iterations,
               double *residual, double *initial_residual);
 /* errors[0..4] = L2, H1-semi, SD, DG(volume), L_inf */
 int orc_errors(const orc_problem *p, double *errors);
+/* the reference's marker-algorithm DOF numbering (TFESpace3D::ConstructSpace,
+ * FESpace3D.C:186-420; compute_various_numbers, FESpace.C:1863-2099) on the
+ * caller's tetrahedral mesh: verts[(cell * 4 + v) * 3 + a]; cfg->order 1 or 2,
+ * cfg->tetra set, cfg->neumann_mask the Neumann faces of the unit cube;
+ * gdof[cell * nloc + k] receives the global numbers */
+int orc_marker_numbering(const orc_config *cfg, int ncells, const double *verts, int *gdof,
+                         int *ndof, int *nactive);
 const char *orc_last_error(void);
 
 #ifdef __cplusplus

@@ -95,6 +95,7 @@ def lib():
             ("orc_get_tcd_matrix", [P, ctypes.c_int, ctypes.c_int, dp]),
             ("orc_quadrature_points", [P, ctypes.c_int, ip, dp]),
             ("orc_assemble_coefficients", [P, ctypes.c_int, dp]),
+            ("orc_marker_numbering", [ctypes.POINTER(Config), ctypes.c_int, dp, ip, ip, ip]),
         ]:
             f = getattr(L, name)
             f.restype = ctypes.c_int
@@ -105,6 +106,22 @@ def lib():
 
 def _dp(a):
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def marker_numbering(cfg, verts):
+    """The reference's marker-algorithm numbering (TFESpace3D::ConstructSpace,
+    FESpace3D.C:186-420) of a tetrahedral mesh given as verts[cell, 4, 3]:
+    (gdof[cell, nloc], ndof, nactive)."""
+    v = np.ascontiguousarray(verts, dtype=np.float64)
+    nc = v.shape[0]
+    nloc = 4 if cfg.order == 1 else 10
+    g = np.zeros((nc, nloc), dtype=np.int32)
+    nd = ctypes.c_int(0)
+    na = ctypes.c_int(0)
+    if lib().orc_marker_numbering(ctypes.byref(cfg), nc, _dp(v), _ip(g), ctypes.byref(nd),
+                                  ctypes.byref(na)):
+        raise RuntimeError(lib().orc_last_error().decode())
+    return g, nd.value, na.value
 
 
 def _ip(a):
